@@ -1,0 +1,117 @@
+"""ctypes binding of the C ABI declared in include/getm_gb300.h.
+
+The product path has exactly one implementation: the sm_103a CUDA library.
+If ``libgetm_gb300.so`` is missing this module raises on import - there is no
+CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import c_double, c_int, c_void_p
+from pathlib import Path
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("GETM_GB300_LIB", _HERE / "libgetm_gb300.so"))
+
+GETM_OK = 0
+ERRORS = {
+    1: "invalid argument",
+    2: "CUDA launch/runtime error",
+    3: "vertical advection exceeded itersmax sub-steps",
+    4: "too many layers for a column kernel",
+    5: "device work-buffer allocation failed",
+}
+
+if not LIB_PATH.exists():
+    raise ImportError(
+        f"{LIB_PATH} not found: build the CUDA library first "
+        "(python -c 'import __graft_entry__ as g; g.build()')"
+    )
+
+lib = ctypes.CDLL(str(LIB_PATH))
+
+# argument codes: i int, d double, p pointer (device array / handle / host array), s stream
+_SIGS = {
+    "getm_create_grid": "iiiiiiiip",
+    "getm_grid_finalize": "p",
+    "getm_grid_set_array": "pcp",
+    "getm_advection_create": "ipp",
+    "getm_advection_finalize": "p",
+    "getm_advection_uv_calculate": "iipppppdppps",
+    "getm_advection_w_calculate": "ppppdpps",
+    "getm_advection_apply_3d_batch": "ppppippppppdpppips",
+    "getm_advection_2d": "ppppiippppdpppps",
+    "getm_advection_get_status": "ps",
+    "getm_vertical_diffusion_create": "pp",
+    "getm_vertical_diffusion_finalize": "p",
+    "getm_vertical_diffusion_prepare": "piiidpddppps",
+    "getm_vertical_diffusion_apply": "piiipppppps",
+    "getm_vertical_diffusion_batch": "iiippddppipppps",
+    "getm_grid_interp_x": "iiippis",
+    "getm_grid_interp_y": "iiippis",
+    "getm_grid_interp_z": "iiiippis",
+    "getm_grid_interp_xy": "iiiiippiis",
+    "getm_momentum_diffusion": "ppppppippppppdpps",
+    "getm_thickness2center_depth": "iiiiiiippps",
+    "getm_thickness2vertical_coordinates": "iiippppps",
+    "getm_alpha": "ipddpps",
+    "getm_elevation2depth": "ippdpps",
+    "getm_multiply_add": "ippds",
+    "getm_advance_surface_elevation": "iiiippppppppds",
+    "getm_surface_pressure_gradient": "iiiiiippppppppdpps",
+    "getm_horizontal_diffusion": "iiiiiippppppppppdpps",
+    "getm_bottom_friction": "iippppppdpis",
+    "getm_collect_3d_momentum_sources": "iiiiipppppppppppdpps",
+    "getm_advance_2d_transport": "iiiippppppppppppppdps",
+    "getm_w_momentum_3d": "iiiiiiippppppppdps",
+    "getm_shear_frequency": "iiiiiiipppppps",
+    "getm_surface_shear_velocity": "iiiiiipppps",
+    "getm_bottom_shear_velocity": "iiiiiipppppppppps",
+    "getm_reconstruct_transport_change": "iiiiiiipppds",
+    "getm_blumberg_mellor": "iiiiiiipppppppppps",
+    "getm_shchepetkin_mcwilliams": "iiiiiiipppppppppppps",
+}
+_CT = {"i": c_int, "d": c_double, "p": c_void_p, "s": c_void_p, "c": ctypes.c_char_p}
+
+for _name, _sig in _SIGS.items():
+    _f = getattr(lib, _name)
+    _f.argtypes = [_CT[c] for c in _sig]
+    _f.restype = c_int
+
+EXPORTED = tuple(_SIGS)
+
+
+class GetmError(RuntimeError):
+    def __init__(self, name, code):
+        super().__init__(f"{name} failed with status {code} ({ERRORS.get(code, 'unknown')})")
+        self.code = code
+
+
+def call(name: str, *args) -> int:
+    """Call an entry point; raise GetmError on a non-zero status."""
+    rc = getattr(lib, name)(*args)
+    if rc != GETM_OK:
+        raise GetmError(name, rc)
+    return rc
+
+
+def ptr(t) -> int | None:
+    """Device pointer of a torch tensor (None passes NULL)."""
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def ptr_array(ptrs):
+    """Host array of device pointers (for the batched entry points)."""
+    arr = (c_void_p * len(ptrs))(*[p if p is not None else None for p in ptrs])
+    return arr
+
+
+def stream_handle(stream=None) -> int:
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream

@@ -1,0 +1,239 @@
+"""GPU counterpart of pygetm's Cython module ``_pygetm`` (python/_pygetm.pyx).
+
+Same function names, argument order and assertions as pyx:180-585; every call
+enqueues the matching C-ABI kernel of libgetm_gb300 on the current torch CUDA
+stream.  Arguments are ``getm_gb300.core.Array`` objects whose tensors live on
+the GPU.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .core import CENTERS, INTERFACES, Array, interp_x, interp_xy, interp_y, interp_z  # noqa: F401
+from ._lib import call
+
+
+def _s():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _p(a):
+    if a is None:
+        return None
+    return (a.all_values if isinstance(a, Array) else a).data_ptr()
+
+
+def momentum_diffusion(huu, huv, hvu, hvv, u, v, Am0, diffu, diffv):
+    """pyx:318-326"""
+    assert huu.grid is u.grid.ugrid
+    assert huv.grid is u.grid.vgrid
+    assert hvu.grid is v.grid.ugrid
+    assert hvv.grid is v.grid.vgrid
+    assert diffu.grid is u.grid
+    assert diffv.grid is v.grid
+    nk = u.all_values.shape[0] if u.z else 1
+    call("getm_momentum_diffusion", u.grid.handle, v.grid.handle, huu.grid.handle, huv.grid.handle, hvu.grid.handle,
+         hvv.grid.handle, nk, _p(huu), _p(huv), _p(hvu), _p(hvv), _p(u), _p(v), float(Am0), _p(diffu), _p(diffv), _s())
+
+
+def thickness2center_depth(mask, h, out=None):
+    """pyx:342-348"""
+    assert mask.grid is h.grid and h.z == CENTERS
+    if out is None:
+        out = h.grid.array(z=CENTERS)
+    g = mask.grid
+    call("getm_thickness2center_depth", g.nx_, g.ny_, g.nz_, 1 + g.halox, g.nx_ - g.halox, 1 + g.haloy, g.ny_ - g.haloy,
+         _p(mask), _p(h), _p(out), _s())
+    return out
+
+
+def thickness2vertical_coordinates(mask, H, h, zc, zf):
+    """pyx:350-355"""
+    assert mask.grid is h.grid and h.z == CENTERS
+    assert mask.grid is H.grid and not H.z
+    assert mask.grid is zc.grid and zc.z == CENTERS
+    assert mask.grid is zf.grid and zf.z == INTERFACES
+    g = mask.grid
+    call("getm_thickness2vertical_coordinates", g.nx_, g.ny_, g.nz_, _p(mask), _p(H), _p(h), _p(zc), _p(zf), _s())
+
+
+def alpha(D, Dmin, Dcrit, out):
+    """pyx:357-360"""
+    call("getm_alpha", D.all_values.numel(), _p(D), float(Dmin), float(Dcrit), _p(D.grid.mask), _p(out), _s())
+
+
+def elevation2depth(z, H, Dmin, D):
+    """pyx:362-367"""
+    assert z.grid is H.grid
+    assert z.grid is D.grid
+    call("getm_elevation2depth", z.all_values.numel(), _p(z), _p(H), float(Dmin), _p(z.grid.mask), _p(D), _s())
+
+
+def horizontal_diffusion(f, Ah_u, Ah_v, dt, out):
+    """pyx:369-390"""
+    g = f.grid
+    ug, vg = g.ugrid, g.vgrid
+    assert not f.z
+    assert Ah_u.grid is ug and not Ah_u.z
+    assert Ah_v.grid is vg and not Ah_v.z
+    assert out.grid is g and not out.z
+    call("getm_horizontal_diffusion", 1, g.nx, 1, g.ny, g.halox, g.haloy, _p(ug.mask), _p(vg.mask), _p(ug.idx), _p(ug.dy),
+         _p(vg.idy), _p(vg.dx), _p(Ah_u), _p(Ah_v), _p(g.mask), _p(g.iarea), float(dt), _p(f), _p(out), _s())
+
+
+def bottom_friction(u, v, D, avmmol, out, update_z0b):
+    """pyx:392-402"""
+    g = u.grid
+    assert not u.z
+    assert v.grid is g and not v.z
+    assert D.grid is g and not D.z
+    assert out.grid is g and not out.z
+    call("getm_bottom_friction", g.nx_, g.ny_, _p(g.mask), _p(u), _p(v), _p(D), _p(g.z0b), _p(g.z0b_min), float(avmmol),
+         _p(out), 1 if update_z0b else 0, _s())
+
+
+def collect_3d_momentum_sources(dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4):
+    """pyx:404-421"""
+    g = dp.grid
+    assert not dp.z, "dp"
+    assert cor.grid is g and cor.z == CENTERS, "cor"
+    assert adv.grid is g and adv.z == CENTERS, "adv"
+    assert diff.grid is g and diff.z == CENTERS, "diff"
+    assert idp.grid is g and idp.z == CENTERS, "idp"
+    assert taus.grid is g and not taus.z, "taus"
+    assert rr.grid is g and not rr.z, "rr"
+    assert ea2.z == CENTERS
+    assert ea4.z == CENTERS
+    call("getm_collect_3d_momentum_sources", g.nx_, g.ny_, g.nz, g.halox, g.haloy, _p(g.mask), _p(g.alpha), _p(g.ho),
+         _p(g.hn), _p(dp), _p(cor), _p(adv), _p(diff), _p(idp), _p(taus), _p(rr), float(dt), _p(ea2), _p(ea4), _s())
+
+
+def advance_2d_transport(U, dp, taus, cor, adv, diff, damp, SA, SB, SD, SF, r, dt):
+    """pyx:423-441"""
+    g = U.grid
+    for a, n in ((dp, "dp"), (taus, "taus"), (cor, "cor"), (adv, "adv"), (diff, "diff"), (damp, "damp"), (SA, "SA"),
+                 (SB, "SB"), (SD, "SD"), (SF, "SF"), (r, "rr")):
+        assert a.grid is g and not a.z, n
+    call("getm_advance_2d_transport", g.nx_, g.ny_, g.halox, g.haloy, _p(g.mask), _p(g.alpha), _p(g.D), _p(dp), _p(taus),
+         _p(cor), _p(adv), _p(diff), _p(damp), _p(SA), _p(SB), _p(SD), _p(SF), _p(r), float(dt), _p(U), _s())
+
+
+def w_momentum_3d(pk, qk, dt, w):
+    """pyx:443-455"""
+    g = w.grid
+    assert w.z == INTERFACES, "w"
+    assert pk.grid is g.ugrid and pk.z == CENTERS, "pk"
+    assert qk.grid is g.vgrid and qk.z == CENTERS, "qk"
+    call("getm_w_momentum_3d", g.nx_, g.ny_, g.nz, g.halox + 1, g.halox + g.nx + 1, g.haloy + 1, g.haloy + g.ny + 1,
+         _p(g.mask), _p(pk.grid.dy), _p(qk.grid.dx), _p(g.iarea), _p(g.ho), _p(g.hn), _p(pk), _p(qk), float(dt), _p(w), _s())
+
+
+def shear_frequency(uk, vk, SS):
+    """pyx:457-466"""
+    g = SS.grid
+    assert SS.z == INTERFACES, "w"
+    assert uk.grid is g.ugrid and uk.z == CENTERS, "uk"
+    assert vk.grid is g.vgrid and vk.z == CENTERS, "vk"
+    call("getm_shear_frequency", g.nx_, g.ny_, g.nz, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+         _p(g.mask), _p(uk.grid.hn), _p(vk.grid.hn), _p(uk), _p(vk), _p(SS), _s())
+
+
+def surface_shear_velocity(taux, tauy, ustar):
+    """pyx:481-488"""
+    g = ustar.grid
+    assert not ustar.z, "ustar"
+    assert taux.grid is g and not taux.z, "taux"
+    assert tauy.grid is g and not tauy.z, "tauy"
+    call("getm_surface_shear_velocity", g.nx_, g.ny_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+         _p(g.mask), _p(taux), _p(tauy), _p(ustar), _s())
+
+
+def bottom_shear_velocity(uk, vk, rru, rrv, ustar2_x, ustar2_y, ustar):
+    """pyx:490-504"""
+    g = ustar.grid
+    assert not ustar.z, "ustar"
+    assert uk.grid is g.ugrid, "uk"
+    assert vk.grid is g.vgrid, "vk"
+    assert rru.grid is g.ugrid and not rru.z, "rru"
+    assert rrv.grid is g.vgrid and not rrv.z, "rrv"
+    assert ustar2_x.grid is g.ugrid and not ustar2_x.z, "ustar2_x"
+    assert ustar2_y.grid is g.vgrid and not ustar2_y.z, "ustar2_y"
+    call("getm_bottom_shear_velocity", g.nx_, g.ny_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+         _p(g.mask), _p(g.ugrid.mask), _p(g.vgrid.mask), _p(uk), _p(vk), _p(rru), _p(rrv), _p(ustar2_x),
+         _p(ustar2_y), _p(ustar), _s())
+
+
+def reconstruct_transport_change(un, hn, Uo, timestep):
+    """pyx:506-510 (hn is a raw tensor, like the reference's ndarray)"""
+    g = Uo.grid
+    nz = 1 if Uo.ndim == 2 else g.nz_
+    call("getm_reconstruct_transport_change", g.nx_, g.ny_, nz, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+         _p(un), _p(hn), _p(Uo), float(timestep), _s())
+
+
+def advance_surface_elevation(timestep, z, U, V, fwf):
+    """pyx:512-523"""
+    g = z.grid
+    assert not z.z, "z"
+    assert U.grid is g.ugrid and not U.z, "U"
+    assert V.grid is g.vgrid and not V.z, "V"
+    assert fwf.grid is g and not fwf.z, "fwf"
+    call("getm_advance_surface_elevation", g.nx_, g.ny_, g.halox, g.haloy, _p(g.mask), _p(U.grid.dy), _p(V.grid.dx),
+         _p(g.iarea), _p(z), _p(U), _p(V), _p(fwf), float(timestep), _s())
+
+
+def surface_pressure_gradient(z, sp, dpdx, dpdy, Dmin):
+    """pyx:525-539"""
+    g = z.grid
+    assert not z.z, "z"
+    assert sp.grid is g and not sp.z, "sp"
+    assert dpdx.grid is g.ugrid and not dpdx.z, "dpdx"
+    assert dpdy.grid is g.vgrid and not dpdy.z, "dpdy"
+    call("getm_surface_pressure_gradient", g.nx_, g.ny_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+         _p(dpdx.grid.mask), _p(dpdy.grid.mask), _p(dpdx.grid.idx), _p(dpdy.grid.idy), _p(z), _p(sp), _p(g.H), _p(g.D),
+         float(Dmin), _p(dpdx), _p(dpdy), _s())
+
+
+def blumberg_mellor(buoy, idpdx, idpdy):
+    """pyx:541-553"""
+    g = buoy.grid
+    assert buoy.z == CENTERS, "buoy"
+    assert idpdx.grid is g.ugrid and idpdx.z == CENTERS, "idpdx"
+    assert idpdy.grid is g.vgrid and idpdy.z == CENTERS, "idpdy"
+    call("getm_blumberg_mellor", g.nx_, g.ny_, g.nz_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+         _p(idpdx.grid.mask), _p(idpdy.grid.mask), _p(idpdx.grid.idx), _p(idpdy.grid.idy), _p(idpdx.grid.hn),
+         _p(idpdy.grid.hn), _p(g.zf), _p(buoy), _p(idpdx), _p(idpdy), _s())
+
+
+_P_WORK = {}
+
+
+def shchepetkin_mcwilliams(buoy, idpdx, idpdy, P_work=None):
+    """pyx:555-568.  ``P_work`` (optional) is the 3D pressure work array; by
+    default one per grid is kept."""
+    g = buoy.grid
+    assert buoy.z == CENTERS, "buoy"
+    assert idpdx.grid is g.ugrid and idpdx.z == CENTERS, "idpdx"
+    assert idpdy.grid is g.vgrid and idpdy.z == CENTERS, "idpdy"
+    if P_work is None:
+        P_work = _P_WORK.get(id(g))
+        if P_work is None or P_work.shape != buoy.all_values.shape:
+            P_work = torch.zeros_like(buoy.all_values)
+            _P_WORK[id(g)] = P_work
+    call("getm_shchepetkin_mcwilliams", g.nx_, g.ny_, g.nz_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+         _p(g.mask), _p(idpdx.grid.mask), _p(idpdy.grid.mask), _p(idpdx.grid.idx), _p(idpdy.grid.idy), _p(g.hn),
+         _p(g.zin), _p(g.zc), _p(buoy), _p(idpdx), _p(idpdy), P_work.data_ptr(), _s())
+
+
+def multiply_add(tgt: torch.Tensor, add: torch.Tensor, scale_factor: float):
+    """pyx:570-572"""
+    if tgt.numel() != 0:
+        call("getm_multiply_add", tgt.numel(), tgt.data_ptr(), add.data_ptr(), float(scale_factor), _s())
+
+
+def new_handle():
+    return ctypes.c_void_p()

@@ -1,0 +1,712 @@
+// TVD directional-split advection (pygetm.operators.Advection) for sm_103a.
+//
+// Reference: src/operators/advection_schemes/advection.F90.template (u2d :23-121,
+// v2d :123-221, w3d :223-374), limiters.h, python/src/wrapper.F90:188-273 and
+// the split sequencing of python/pygetm/operators.py:52-193.
+//
+// GB300 design
+// * Horizontal passes are one kernel per direction and stage, batched over all
+//   tracers: the face geometry (mask, transport QU, Courant number, upwind
+//   side) and the layer-thickness update are computed once per cell and
+//   reused for every tracer.  Memory traffic per pass is the algorithmic
+//   minimum: read u, hu, h, var; write h, var.
+// * The reference updates var and h in place after computing all face fluxes
+//   of a layer.  A GPU block cannot see its neighbours' updates in order, so
+//   each pass reads from one buffer and writes a complete copy to another
+//   (ping-pong through handle-owned work buffers); the stage sequence is laid
+//   out so the final stage lands in the caller's arrays.
+// * x-direction: a warp covers 32 consecutive cells of a row; each lane
+//   computes the flux through its east face and receives the west face from
+//   its neighbour with a shuffle (lane 0 computes one extra face).
+// * y-direction: a 32 x BY block; each thread computes its north face and the
+//   south face comes from shared memory (row 0 computes one extra face).
+// * Vertical pass: one thread per water column, sweeping k with a register
+//   window (the per-column update is in place, as in the reference).  The
+//   adaptive sub-stepping (itersmax = 200, restart semantics of
+//   template :286-368) runs through handle-owned column work arrays.
+#include <stdlib.h>
+#include <string.h>
+
+#include "getm_common.cuh"
+
+#define GETM_MAX_BATCH 32
+#define GETM_V_BY 16
+
+// ---------------------------------------------------------------------------
+// grid handles
+// ---------------------------------------------------------------------------
+extern "C" int getm_create_grid(int imin, int imax, int jmin, int jmax, int kmin, int kmax,
+                                int halox, int haloy, getm_grid** grid)
+{
+    if (!grid || imax < imin || jmax < jmin || kmax < kmin - 1 || halox < 0 || haloy < 0)
+        return GETM_ERR_ARG;
+    getm_grid* g = (getm_grid*)calloc(1, sizeof(getm_grid));
+    if (!g) return GETM_ERR_ALLOC;
+    g->imin = imin; g->imax = imax; g->jmin = jmin; g->jmax = jmax;
+    g->kmin = kmin; g->kmax = kmax; g->halox = halox; g->haloy = haloy;
+    g->nx_ = imax - imin + 1 + 2 * halox;
+    g->ny_ = jmax - jmin + 1 + 2 * haloy;
+    *grid = g;
+    return GETM_OK;
+}
+
+extern "C" int getm_grid_finalize(getm_grid* grid)
+{
+    free(grid);
+    return GETM_OK;
+}
+
+extern "C" int getm_grid_set_array(getm_grid* g, const char* name, void* p)
+{
+    if (!g || !name) return GETM_ERR_ARG;
+    if (!strcmp(name, "mask")) g->mask = (const int*)p;
+    else if (!strcmp(name, "dx")) g->dx = (const double*)p;
+    else if (!strcmp(name, "dy")) g->dy = (const double*)p;
+    else if (!strcmp(name, "idx")) g->idx = (const double*)p;
+    else if (!strcmp(name, "idy")) g->idy = (const double*)p;
+    else if (!strcmp(name, "iarea")) g->iarea = (const double*)p;
+    else if (!strcmp(name, "area")) g->area = (const double*)p;
+    else return GETM_ERR_ARG;
+    return GETM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// advection handle: scheme plus device work buffers (grown on demand)
+// ---------------------------------------------------------------------------
+struct getm_advection {
+    int scheme;
+    getm_grid* tgrid;
+    size_t n3;                 // elements of one 3D field the buffers are sized for
+    double* hbuf[2];           // layer-thickness ping-pong buffers
+    double* colbuf[2];         // vertical sub-stepping work arrays (haux, faux)
+    double* tmp[GETM_MAX_BATCH * 8];  // per-tracer ping-pong buffers
+    int ntmp;
+    int* status;               // device status word (GETM_ERR_ITERS)
+};
+
+static void adv_free_buffers(getm_advection* a)
+{
+    for (int i = 0; i < 2; i++) { cudaFree(a->hbuf[i]); a->hbuf[i] = NULL; }
+    for (int i = 0; i < 2; i++) { cudaFree(a->colbuf[i]); a->colbuf[i] = NULL; }
+    for (int i = 0; i < a->ntmp; i++) { cudaFree(a->tmp[i]); a->tmp[i] = NULL; }
+    a->ntmp = 0;
+    a->n3 = 0;
+}
+
+// Make sure the work buffers can hold 3D fields of n3 elements and ntracer
+// per-tracer ping-pong copies.  Allocation happens on first use only (so a
+// warm-up call before stream capture makes later calls capturable).
+static int adv_reserve(getm_advection* a, size_t n3, int ntracer)
+{
+    if (ntracer > GETM_MAX_BATCH * 8) return GETM_ERR_ARG;
+    if (n3 > a->n3) {
+        adv_free_buffers(a);
+        for (int i = 0; i < 2; i++)
+            if (cudaMalloc(&a->hbuf[i], n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
+        for (int i = 0; i < 2; i++)
+            if (cudaMalloc(&a->colbuf[i], n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
+        a->n3 = n3;
+    }
+    while (a->ntmp < ntracer) {
+        if (cudaMalloc(&a->tmp[a->ntmp], a->n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
+        a->ntmp++;
+    }
+    return GETM_OK;
+}
+
+extern "C" int getm_advection_create(int scheme, getm_grid* tgrid, getm_advection** out)
+{
+    if (!out || scheme < GETM_SCHEME_HSIMT || scheme > GETM_SCHEME_UPSTREAM) return GETM_ERR_ARG;
+    getm_advection* a = (getm_advection*)calloc(1, sizeof(getm_advection));
+    if (!a) return GETM_ERR_ALLOC;
+    a->scheme = scheme;
+    a->tgrid = tgrid;
+    if (cudaMalloc(&a->status, sizeof(int)) != cudaSuccess) { free(a); return GETM_ERR_ALLOC; }
+    cudaMemset(a->status, 0, sizeof(int));
+    *out = a;
+    return GETM_OK;
+}
+
+extern "C" int getm_advection_finalize(getm_advection* a)
+{
+    if (!a) return GETM_OK;
+    adv_free_buffers(a);
+    cudaFree(a->status);
+    free(a);
+    return GETM_OK;
+}
+
+extern "C" int getm_advection_get_status(getm_advection* a, cudaStream_t stream)
+{
+    if (!a) return GETM_ERR_ARG;
+    int h = 0;
+    if (cudaMemcpyAsync(&h, a->status, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return GETM_ERR_CUDA;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return GETM_ERR_CUDA;
+    return h;
+}
+
+// ---------------------------------------------------------------------------
+// horizontal pass kernels
+// ---------------------------------------------------------------------------
+struct HPassArgs {
+    int nx_, ny_, nk;
+    long long plane;            // nx_ * ny_
+    int ilo, ihi, jlo, jhi;     // C interior bounds (inclusive) of the T grid
+    const int* umask;           // mask of the velocity grid of this direction
+    const double* idx;          // x: idx of U grid; y: idy of V grid (Courant number)
+    const double* dy;           // x: dy of U grid;  y: dx of V grid (face length)
+    const int* tmask;
+    const double* iA;
+    const double* Ah;           // 2D horizontal diffusivity on the velocity grid, or NULL
+    const double* u;            // velocity (nk layers)
+    const double* hu;           // layer thickness on the velocity grid (nk layers)
+    const double* h_in;
+    double* h_out;
+    double dt;
+    int scheme;
+    int ntracer;
+    const double* fin[GETM_MAX_BATCH];
+    double* fout[GETM_MAX_BATCH];
+};
+
+struct FaceGeom {
+    double QU, cfl;
+    bool active, up, uu_ok;
+};
+
+// Face quantities that do not depend on the advected field
+// (template :63-65, :70, :77).
+__device__ __forceinline__ FaceGeom face_geom(const HPassArgs& a, long long p2, long long p3,
+                                              long long s, bool in_range)
+{
+    FaceGeom g;
+    g.QU = 0.0; g.cfl = 0.0; g.active = false; g.up = false; g.uu_ok = false;
+    if (!in_range) return g;
+    int m = a.umask[p2];
+    if (!getm_flux_point(m)) return g;
+    double uu = a.u[p3];
+    g.active = true;
+    g.QU = uu * a.hu[p3] * a.dy[p2];
+    g.cfl = fabs(uu * a.dt * a.idx[p2]);
+    g.up = uu > 0;
+    g.uu_ok = getm_flux_point(g.up ? a.umask[p2 - s] : a.umask[p2 + s]);
+    return g;
+}
+
+// Tracer flux through one face (template :66-104).
+__device__ __forceinline__ double face_flux(const HPassArgs& a, const FaceGeom& g,
+                                            const double* __restrict__ f, long long p2,
+                                            long long p3, long long s)
+{
+    if (!g.active) return 0.0;
+    double fu, fuu, fd;
+    if (g.up) {
+        fu = f[p3];
+        fuu = g.uu_ok ? f[p3 - s] : fu;
+        fd = f[p3 + s];
+    } else {
+        fu = f[p3 + s];
+        fuu = g.uu_ok ? f[p3 + 2 * s] : fu;
+        fd = f[p3];
+    }
+    fu = getm_tvd_face<double>(a.scheme, fuu, fu, fd, g.cfl);
+    double flux = g.QU * fu;
+    if (a.Ah) flux = flux - a.Ah[p2] * a.hu[p3] * (f[p3 + s] - f[p3]) * a.idx[p2] * a.dy[p2];
+    return flux;
+}
+
+// x-direction pass.  blockDim = (32, BYX); grid = (ceil(nx_/32), ceil(ny_*nk/BYX)).
+__global__ void __launch_bounds__(256) hpass_x_kernel(HPassArgs a)
+{
+    const int lane = threadIdx.x;
+    const int i = blockIdx.x * 32 + lane;
+    const long long row = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+    if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
+    const int k = (int)(row / a.ny_);
+    const int j = (int)(row - (long long)k * a.ny_);
+    const bool inx = i < a.nx_;
+    const long long p2 = (long long)j * a.nx_ + i;
+    const long long p3 = (long long)k * a.plane + p2;
+    const bool jrow = j >= a.jlo && j <= a.jhi;
+
+    FaceGeom gr = face_geom(a, p2, p3, 1, inx && jrow && i >= a.ilo - 1 && i <= a.ihi);
+    FaceGeom gl = face_geom(a, p2 - 1, p3 - 1, 1, lane == 0 && jrow && i - 1 >= a.ilo - 1 && i - 1 <= a.ihi);
+    double QUl = __shfl_up_sync(0xffffffffu, gr.QU, 1);
+    if (lane == 0) QUl = gl.QU;
+    const bool upd = inx && jrow && i >= a.ilo && i <= a.ihi && a.tmask[p2] == 1;
+
+    double hold = 0.0, hnew = 0.0, iA = 0.0;
+    if (inx) {
+        hold = a.h_in[p3];
+        hnew = hold;
+        if (upd) {
+            iA = a.iA[p2];
+            hnew = hold - a.dt * (gr.QU - QUl) * iA;
+        }
+        a.h_out[p3] = hnew;
+    }
+    for (int t = 0; t < a.ntracer; t++) {
+        const double* __restrict__ f = a.fin[t];
+        double fr = inx ? face_flux(a, gr, f, p2, p3, 1) : 0.0;
+        double fl = __shfl_up_sync(0xffffffffu, fr, 1);
+        if (lane == 0) fl = face_flux(a, gl, f, p2 - 1, p3 - 1, 1);
+        if (inx) {
+            double fo = f[p3];
+            double fn = fo;
+            if (upd) {
+                double hfo = hold * fo;
+                double advn = (fr - fl) * iA;
+                fn = (hfo - a.dt * advn) / hnew;
+            }
+            a.fout[t][p3] = fn;
+        }
+    }
+}
+
+// y-direction pass.  blockDim = (32, GETM_V_BY); grid = (ceil(nx_/32), ceil(ny_/BY), nk).
+__global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs a)
+{
+    __shared__ double sQ[GETM_V_BY][32];
+    __shared__ double sF[GETM_V_BY][32];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = blockIdx.x * 32 + tx;
+    const int j = blockIdx.y * GETM_V_BY + ty;
+    const int k = blockIdx.z;
+    const bool in = i < a.nx_ && j < a.ny_;
+    const long long s = a.nx_;
+    const long long p2 = (long long)j * a.nx_ + i;
+    const long long p3 = (long long)k * a.plane + p2;
+    const bool icol = i >= a.ilo && i <= a.ihi;
+
+    FaceGeom gt = face_geom(a, p2, p3, s, in && icol && j >= a.jlo - 1 && j <= a.jhi);
+    FaceGeom gb = face_geom(a, p2 - s, p3 - s, s, in && ty == 0 && icol && j - 1 >= a.jlo - 1 && j - 1 <= a.jhi);
+    sQ[ty][tx] = gt.QU;
+    __syncthreads();
+    double QUb = ty > 0 ? sQ[ty - 1][tx] : gb.QU;
+    const bool upd = in && icol && j >= a.jlo && j <= a.jhi && a.tmask[p2] == 1;
+
+    double hold = 0.0, hnew = 0.0, iA = 0.0;
+    if (in) {
+        hold = a.h_in[p3];
+        hnew = hold;
+        if (upd) {
+            iA = a.iA[p2];
+            hnew = hold - a.dt * (gt.QU - QUb) * iA;
+        }
+        a.h_out[p3] = hnew;
+    }
+    for (int t = 0; t < a.ntracer; t++) {
+        const double* __restrict__ f = a.fin[t];
+        double ft = in ? face_flux(a, gt, f, p2, p3, s) : 0.0;
+        double fb = (ty == 0 && in) ? face_flux(a, gb, f, p2 - s, p3 - s, s) : 0.0;
+        __syncthreads();  // previous tracer's reads of sF are done
+        sF[ty][tx] = ft;
+        __syncthreads();
+        if (ty > 0) fb = sF[ty - 1][tx];
+        if (in) {
+            double fo = f[p3];
+            double fn = fo;
+            if (upd) {
+                double hfo = hold * fo;
+                double advn = (ft - fb) * iA;
+                fn = (hfo - a.dt * advn) / hnew;
+            }
+            a.fout[t][p3] = fn;
+        }
+    }
+}
+
+static int launch_hpass(int direction, HPassArgs& a, cudaStream_t stream)
+{
+    if (direction == 1) {
+        const int BY = 8;
+        dim3 block(32, BY);
+        dim3 grid(getm_div_up(a.nx_, 32), getm_div_up((long long)a.ny_ * a.nk, BY));
+        hpass_x_kernel<<<grid, block, 0, stream>>>(a);
+    } else {
+        dim3 block(32, GETM_V_BY);
+        dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, GETM_V_BY), a.nk);
+        hpass_y_kernel<<<grid, block, 0, stream>>>(a);
+    }
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// Fill the direction-dependent fields of HPassArgs from the grid handles
+// (wrapper.F90:240-253: direction 1 passes ugrid mask/idx/dy, 2 passes vgrid
+// mask/dx/idy).
+static int hpass_setup(HPassArgs& a, int direction, const getm_advection* adv,
+                       const getm_grid* tg, const getm_grid* vg, int nk, const double* u,
+                       const double* Ah, double dt, const double* hu)
+{
+    if (!tg || !vg || !u || !hu) return GETM_ERR_ARG;
+    if (tg->halox < 2 || tg->haloy < 2) return GETM_ERR_ARG;
+    if (!tg->mask || !tg->iarea || !vg->mask) return GETM_ERR_ARG;
+    memset(&a, 0, sizeof(a));
+    a.nx_ = tg->nx_; a.ny_ = tg->ny_; a.nk = nk;
+    a.plane = (long long)tg->nx_ * tg->ny_;
+    a.ilo = tg->halox; a.ihi = tg->halox + (tg->imax - tg->imin);
+    a.jlo = tg->haloy; a.jhi = tg->haloy + (tg->jmax - tg->jmin);
+    a.umask = vg->mask;
+    if (direction == 1) { a.idx = vg->idx; a.dy = vg->dy; }
+    else { a.idx = vg->idy; a.dy = vg->dx; }
+    if (!a.idx || !a.dy) return GETM_ERR_ARG;
+    a.tmask = tg->mask; a.iA = tg->iarea; a.Ah = Ah; a.u = u; a.hu = hu; a.dt = dt;
+    a.scheme = adv->scheme;
+    return GETM_OK;
+}
+
+// Run one horizontal stage for ntracer tracers, chunked by GETM_MAX_BATCH.
+static int run_hstage(HPassArgs& a, int direction, const double* h_in, double* h_out, int ntracer,
+                      const double* const* fin, double* const* fout, cudaStream_t stream)
+{
+    a.h_in = h_in; a.h_out = h_out;
+    int done = 0;
+    do {
+        int n = ntracer - done;
+        if (n > GETM_MAX_BATCH) n = GETM_MAX_BATCH;
+        a.ntracer = n;
+        for (int t = 0; t < n; t++) { a.fin[t] = fin[done + t]; a.fout[t] = fout[done + t]; }
+        int rc = launch_hpass(direction, a, stream);
+        if (rc) return rc;
+        done += n;
+    } while (done < ntracer);
+    return GETM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// vertical pass (template w3d :223-374)
+// ---------------------------------------------------------------------------
+struct WPassArgs {
+    int nx_, ny_, nz;
+    long long plane;
+    int ilo, ihi, jlo, jhi;
+    const int* tmask;
+    const double* w;            // nz+1 levels
+    const double* h_in;         // layer thickness at stage start (not modified)
+    double* h_out;              // layer thickness after the pass (last tracer's)
+    double* haux;               // column work arrays for sub-stepping (nz levels)
+    double* faux;
+    double dt;
+    int scheme;
+    int ntracer;
+    int* status;
+    const double* wvar[GETM_MAX_BATCH];
+    double* f[GETM_MAX_BATCH];  // updated in place
+};
+
+// One sub-step over a column: reads (hs, fs) levels 0..nz-1 (C), writes
+// (hd, fd).  hs == hd / fs == fd (in place) is allowed: every level is read
+// into the register window before it is overwritten.  When cfl_from_h is
+// false the per-interface Courant numbers are recomputed from w_var and hs
+// exactly as cfl0 (template :274) - the caller passes use0 = true for it == 1
+// where cfls = cfl0 and hs is the original thickness, so both coincide.
+__device__ void w_substep(const WPassArgs& a, long long c, const double* wv, const double* hs,
+                          const double* fs, double* hd, double* fdst, double dtk, double itersm1)
+{
+    const long long P = a.plane;
+    const int nz = a.nz;
+    // window of old values
+    double fkm1 = 0.0, fk = fs[c], fk1 = (nz > 1) ? fs[c + P] : 0.0;
+    double hk = hs[c], hk1 = (nz > 1) ? hs[c + P] : 0.0;
+    double fluxm = 0.0;  // flux(k-1), flux(0) = 0
+    double wkm1 = a.w[c];
+    for (int k = 0; k < nz; k++) {
+        // flux through the interface above C level k (Fortran interface k+1)
+        double flux = 0.0;
+        double fk2 = 0.0, hk2 = 0.0;
+        if (k + 2 < nz) { fk2 = fs[c + (k + 2) * P]; hk2 = hs[c + (k + 2) * P]; }
+        if (k < nz - 1) {
+            double wvk = wv[c + (k + 1) * P];
+            double cfl = fabs(wvk) * a.dt / fmin(hk, hk1) * itersm1;
+            double fu, fuu, fdn;
+            if (wvk > 0) {
+                fu = fk;
+                fuu = (k > 0) ? fkm1 : fu;
+                fdn = fk1;
+            } else {
+                fu = fk1;
+                fuu = (k < nz - 2) ? fk2 : fu;
+                fdn = fk;
+            }
+            fu = getm_tvd_face<double>(a.scheme, fuu, fu, fdn, cfl);
+            flux = wvk * fu;
+        }
+        double wk = a.w[c + (k + 1) * P];
+        double hfo = hk * fk;
+        double hn = hk - dtk * (wk - wkm1);
+        double advn = flux - fluxm;
+        hd[c + k * P] = hn;
+        fdst[c + k * P] = (hfo - dtk * advn) / hn;
+        // shift window
+        fluxm = flux; wkm1 = wk;
+        fkm1 = fk; fk = fk1; fk1 = fk2;
+        hk = hk1; hk1 = hk2;
+    }
+}
+
+// Largest Courant number over the interior interfaces of a column
+// (template :274, :294, :300).  Returns -1 when nz == 1 (no interfaces).
+__device__ double w_maxcfl(const WPassArgs& a, long long c, const double* wv, const double* hs)
+{
+    const long long P = a.plane;
+    double cmax = -1.0;
+    double hk = hs[c];
+    for (int k = 1; k < a.nz; k++) {
+        double hk1 = hs[c + k * P];
+        double cfl = fabs(wv[c + k * P]) * a.dt / fmin(hk, hk1);
+        if (k == 1 || cfl > cmax) cmax = cfl;
+        hk = hk1;
+    }
+    return cmax;
+}
+
+__device__ __forceinline__ int w_iters_from(double cfl)
+{
+    if (!(cfl > 1.0)) return 1;               // includes nz == 1 and NaN
+    double c = ceil(cfl);
+    return c > 1e9 ? 1000000000 : (int)c;
+}
+
+// Thread per column.  Note: the Courant number inside w_substep is
+// |w_var| dt / min(h) * itersm1 which equals cfls(k)*itersm1 of the reference
+// (cfls = |w_var| dt / min(haux) with haux = the sub-step's start thickness).
+__global__ void __launch_bounds__(128) wpass_kernel(WPassArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i < a.ilo || i > a.ihi || j < a.jlo || j > a.jhi) return;
+    const long long c = (long long)j * a.nx_ + i;
+    if (a.tmask[c] != 1) return;
+    const int itersmax = 200;
+    const long long P = a.plane;
+    int last_iters = 1;
+    for (int t = 0; t < a.ntracer; t++) {
+        const double* wv = a.wvar[t];
+        double* f = a.f[t];
+        int iters = 1;
+        double itersm1 = 1.0, dtk = a.dt;
+        int it = 1;
+        while (it <= iters) {
+            const double* hs = (it == 1) ? a.h_in : a.haux;
+            const double* fs = (it == 1) ? f : a.faux;
+            if (iters < itersmax) {
+                int iters_new = w_iters_from(w_maxcfl(a, c, wv, hs));
+                if (iters_new > iters) {
+                    if (iters_new > itersmax) {
+                        iters = itersmax;
+                        atomicOr(a.status, 1 << GETM_ERR_ITERS);
+                    } else {
+                        iters = iters_new;
+                    }
+                    itersm1 = 1.0 / iters;
+                    dtk = a.dt * itersm1;
+                    if (it > 1) { it = 1; continue; }
+                }
+            }
+            // The last sub-step writes the tracer in place and the thickness
+            // into haux (the stage's h_in must survive for the next tracer).
+            double* fd = (it == iters) ? f : a.faux;
+            w_substep(a, c, wv, hs, fs, a.haux, fd, dtk, itersm1);
+            it++;
+        }
+        last_iters = iters;
+    }
+    (void)last_iters;
+    // h after the pass = thickness of the last tracer's final sub-step
+    for (int k = 0; k < a.nz; k++) a.h_out[c + k * P] = a.haux[c + k * P];
+}
+
+// Copy h_in -> h_out for the columns the w pass does not touch, so h_out is a
+// complete field (ping-pong buffers must be fully written).
+__global__ void copy_untouched_kernel(WPassArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= a.nx_) return;
+    const long long c = (long long)j * a.nx_ + i;
+    bool touched = i >= a.ilo && i <= a.ihi && j >= a.jlo && j <= a.jhi && a.tmask[c] == 1 && a.ntracer > 0;
+    if (touched || a.h_out == a.h_in) return;
+    for (int k = 0; k < a.nz; k++) a.h_out[c + k * a.plane] = a.h_in[c + k * a.plane];
+}
+
+static int run_wstage(getm_advection* adv, const getm_grid* tg, const double* w,
+                      const double* const* wvar, double dt, const double* h_in, double* h_out,
+                      int ntracer, double* const* f, cudaStream_t stream)
+{
+    WPassArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nx_ = tg->nx_; a.ny_ = tg->ny_; a.nz = tg->kmax - tg->kmin + 1;
+    a.plane = (long long)tg->nx_ * tg->ny_;
+    a.ilo = tg->halox; a.ihi = tg->halox + (tg->imax - tg->imin);
+    a.jlo = tg->haloy; a.jhi = tg->haloy + (tg->jmax - tg->jmin);
+    a.tmask = tg->mask; a.w = w; a.dt = dt; a.scheme = adv->scheme; a.status = adv->status;
+    a.haux = adv->colbuf[0]; a.faux = adv->colbuf[1];
+    if (a.nz < 1) return GETM_ERR_ARG;
+    dim3 block(128);
+    dim3 grid(getm_div_up(a.nx_, 128), a.ny_);
+    // Chunks: every chunk starts from h_in; the final h is the last chunk's.
+    int done = 0;
+    do {
+        int n = ntracer - done;
+        if (n > GETM_MAX_BATCH) n = GETM_MAX_BATCH;
+        a.ntracer = n;
+        a.h_in = h_in; a.h_out = h_out;
+        for (int t = 0; t < n; t++) { a.wvar[t] = wvar[done + t]; a.f[t] = f[done + t]; }
+        wpass_kernel<<<grid, block, 0, stream>>>(a);
+        GETM_CHECK_LAUNCH();
+        done += n;
+    } while (done < ntracer);
+    copy_untouched_kernel<<<grid, block, 0, stream>>>(a);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" int getm_advection_uv_calculate(int direction, int nk, getm_advection* adv,
+                                           getm_grid* tgrid, getm_grid* ugrid, const double* u,
+                                           const double* Ah, double timestep, double* h,
+                                           const double* hu, double* var, cudaStream_t stream)
+{
+    if (!adv) return GETM_OK;  // wrapper.F90:227 returns silently without a scheme
+    if ((direction != 1 && direction != 2) || nk < 1 || !h || !var) return GETM_ERR_ARG;
+    HPassArgs a;
+    int rc = hpass_setup(a, direction, adv, tgrid, ugrid, nk, u, Ah, timestep, hu);
+    if (rc) return rc;
+    const size_t n3 = (size_t)a.plane * nk;
+    if ((rc = adv_reserve(adv, n3, 1))) return rc;
+    const double* fin[1] = {var};
+    double* fout[1] = {adv->tmp[0]};
+    if ((rc = run_hstage(a, direction, h, adv->hbuf[0], 1, fin, fout, stream))) return rc;
+    // in-place semantics of the reference: copy the results back
+    if (cudaMemcpyAsync(var, adv->tmp[0], n3 * sizeof(double), cudaMemcpyDeviceToDevice, stream) != cudaSuccess) return GETM_ERR_CUDA;
+    if (cudaMemcpyAsync(h, adv->hbuf[0], n3 * sizeof(double), cudaMemcpyDeviceToDevice, stream) != cudaSuccess) return GETM_ERR_CUDA;
+    return GETM_OK;
+}
+
+extern "C" int getm_advection_w_calculate(getm_advection* adv, getm_grid* tgrid, const double* w,
+                                          const double* w_var, double timestep, double* h,
+                                          double* var, cudaStream_t stream)
+{
+    if (!adv) return GETM_OK;  // wrapper.F90:265
+    if (!tgrid || !w || !w_var || !h || !var || !tgrid->mask) return GETM_ERR_ARG;
+    const int nz = tgrid->kmax - tgrid->kmin + 1;
+    const size_t n3 = (size_t)tgrid->nx_ * tgrid->ny_ * nz;
+    int rc = adv_reserve(adv, n3, 0);
+    if (rc) return rc;
+    const double* wv[1] = {w_var};
+    double* f[1] = {var};
+    if ((rc = run_wstage(adv, tgrid, w, wv, timestep, h, adv->hbuf[0], 1, f, stream))) return rc;
+    if (cudaMemcpyAsync(h, adv->hbuf[0], n3 * sizeof(double), cudaMemcpyDeviceToDevice, stream) != cudaSuccess) return GETM_ERR_CUDA;
+    return GETM_OK;
+}
+
+extern "C" int getm_advection_apply_3d_batch(getm_advection* adv, getm_grid* tgrid,
+                                             getm_grid* ugrid, getm_grid* vgrid, int ufirst,
+                                             const double* u, const double* v, const double* w,
+                                             const double* const* w_var, const double* Ah_u,
+                                             const double* Ah_v, double timestep, double* h,
+                                             const double* hu, const double* hv, int ntracer,
+                                             double* const* vars, cudaStream_t stream)
+{
+    if (!adv) return GETM_OK;
+    if (!tgrid || !w || !h || ntracer < 1 || !vars) return GETM_ERR_ARG;
+    const int nz = tgrid->kmax - tgrid->kmin + 1;
+    HPassArgs ax, ay;
+    int rc = hpass_setup(ax, 1, adv, tgrid, ugrid, nz, u, Ah_u, 0.5 * timestep, hu);
+    if (rc) return rc;
+    if ((rc = hpass_setup(ay, 2, adv, tgrid, vgrid, nz, v, Ah_v, 0.5 * timestep, hv))) return rc;
+    const size_t n3 = (size_t)ax.plane * nz;
+    if ((rc = adv_reserve(adv, n3, ntracer))) return rc;
+
+    const double* wv[GETM_MAX_BATCH * 8];
+    const double* fin[GETM_MAX_BATCH * 8];
+    double* fout[GETM_MAX_BATCH * 8];
+    for (int t = 0; t < ntracer; t++) wv[t] = (w_var && w_var[t]) ? w_var[t] : w;
+
+    HPassArgs* first = ufirst ? &ax : &ay;
+    const int dfirst = ufirst ? 1 : 2;
+    HPassArgs* second = ufirst ? &ay : &ax;
+    const int dsecond = ufirst ? 2 : 1;
+    double* A = adv->hbuf[0];
+    double* B = adv->hbuf[1];
+    double* const* tmp = adv->tmp;
+
+    // adv1(dt/2): vars -> tmp, h -> A   (operators.py:165-170)
+    for (int t = 0; t < ntracer; t++) { fin[t] = vars[t]; fout[t] = tmp[t]; }
+    if ((rc = run_hstage(*first, dfirst, h, A, ntracer, fin, fout, stream))) return rc;
+    // adv2(dt/2): tmp -> vars, A -> B   (:171-175)
+    for (int t = 0; t < ntracer; t++) { fin[t] = tmp[t]; fout[t] = vars[t]; }
+    if ((rc = run_hstage(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
+    // w(dt): vars in place, B -> A      (:176-182)
+    if ((rc = run_wstage(adv, tgrid, w, wv, timestep, B, A, ntracer, vars, stream))) return rc;
+    // adv2(dt/2): vars -> tmp, A -> B   (:183-188)
+    for (int t = 0; t < ntracer; t++) { fin[t] = vars[t]; fout[t] = tmp[t]; }
+    if ((rc = run_hstage(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
+    // adv1(dt/2): tmp -> vars, B -> h   (:189-193)
+    for (int t = 0; t < ntracer; t++) { fin[t] = tmp[t]; fout[t] = vars[t]; }
+    if ((rc = run_hstage(*first, dfirst, B, h, ntracer, fin, fout, stream))) return rc;
+    return GETM_OK;
+}
+
+extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
+                                 getm_grid* vgrid, int ufirst, int split, const double* u,
+                                 const double* v, const double* Ah_u, const double* Ah_v,
+                                 double timestep, double* D, const double* DU, const double* DV,
+                                 double* var, cudaStream_t stream)
+{
+    if (!adv) return GETM_OK;
+    if (!D || !var || split < 1 || split > 3) return GETM_ERR_ARG;
+    HPassArgs ax, ay;
+    int rc = hpass_setup(ax, 1, adv, tgrid, ugrid, 1, u, Ah_u, timestep, DU);
+    if (rc) return rc;
+    if ((rc = hpass_setup(ay, 2, adv, tgrid, vgrid, 1, v, Ah_v, timestep, DV))) return rc;
+    const size_t n2 = (size_t)ax.plane;
+    if ((rc = adv_reserve(adv, n2, 1))) return rc;
+    HPassArgs* p1 = ufirst ? &ax : &ay;
+    HPassArgs* p2 = ufirst ? &ay : &ax;
+    const int d1 = ufirst ? 1 : 2, d2 = ufirst ? 2 : 1;
+    double* T = adv->tmp[0];
+    double* A = adv->hbuf[0];
+    double* B = adv->hbuf[1];
+    const double* fin[1];
+    double* fout[1];
+    // Sequence of (pass, dt factor); ping-pong var<->T and D->A->B->...
+    int seq_n = 0;
+    int seq_dir[4];
+    double seq_dt[4];
+    HPassArgs* seq_a[4];
+    if (split == 1) {          // FULL: adv1(dt), adv2(dt)
+        seq_a[0] = p1; seq_dir[0] = d1; seq_dt[0] = timestep;
+        seq_a[1] = p2; seq_dir[1] = d2; seq_dt[1] = timestep;
+        seq_n = 2;
+    } else if (split == 2) {   // HALF: adv1(dt/2), adv2(dt), adv1(dt/2)
+        seq_a[0] = p1; seq_dir[0] = d1; seq_dt[0] = 0.5 * timestep;
+        seq_a[1] = p2; seq_dir[1] = d2; seq_dt[1] = timestep;
+        seq_a[2] = p1; seq_dir[2] = d1; seq_dt[2] = 0.5 * timestep;
+        seq_n = 3;
+    } else {                   // HALF_ALWAYS: adv1/2, adv2/2, adv2/2, adv1/2
+        seq_a[0] = p1; seq_dir[0] = d1; seq_dt[0] = 0.5 * timestep;
+        seq_a[1] = p2; seq_dir[1] = d2; seq_dt[1] = 0.5 * timestep;
+        seq_a[2] = p2; seq_dir[2] = d2; seq_dt[2] = 0.5 * timestep;
+        seq_a[3] = p1; seq_dir[3] = d1; seq_dt[3] = 0.5 * timestep;
+        seq_n = 4;
+    }
+    const double* hsrc = D;
+    double* fsrc = var;
+    for (int s = 0; s < seq_n; s++) {
+        double* hdst = (s == seq_n - 1) ? D : ((s % 2 == 0) ? A : B);
+        double* fdst = (fsrc == var) ? T : var;
+        seq_a[s]->dt = seq_dt[s];
+        fin[0] = fsrc; fout[0] = fdst;
+        if ((rc = run_hstage(*seq_a[s], seq_dir[s], hsrc, hdst, 1, fin, fout, stream))) return rc;
+        hsrc = hdst;
+        fsrc = fdst;
+    }
+    if (fsrc != var) {
+        if (cudaMemcpyAsync(var, fsrc, n2 * sizeof(double), cudaMemcpyDeviceToDevice, stream) != cudaSuccess) return GETM_ERR_CUDA;
+    }
+    return GETM_OK;
+}

@@ -1,0 +1,93 @@
+// Shared device/host helpers for the getm_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "getm_gb300.h"
+
+// Physical constants of python/src/wrapper.F90:11-13 (module pygetm).
+#define GETM_RHO0 1025.0
+#define GETM_KAPPA 0.4
+#define GETM_G 9.81
+
+// Grid handle: index extent plus device pointers to the static metrics that
+// the reference reads from its type_getm_grid (src/domain/domain.F90:85-140)
+// inside advection_uv_calculate / c_momentum_diffusion.
+struct getm_grid {
+    int imin, imax, jmin, jmax, kmin, kmax;  // Fortran 1-based interior bounds
+    int halox, haloy;
+    int nx_, ny_;                            // full extents incl. halos
+    const int* mask;
+    const double* dx;
+    const double* dy;
+    const double* idx;
+    const double* idy;
+    const double* iarea;
+    const double* area;
+};
+
+#define GETM_CHECK_LAUNCH()                                     \
+    do {                                                        \
+        cudaError_t e_ = cudaGetLastError();                    \
+        if (e_ != cudaSuccess) return GETM_ERR_CUDA;            \
+    } while (0)
+
+static inline unsigned int getm_div_up(long long a, long long b) { return (unsigned int)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// TVD limiter (src/operators/advection_schemes/limiters.h:1-44).  T is the
+// arithmetic type: double for the FP64 form, float for the mixed form.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T getm_limiter(int scheme, T ratio, T cfl)
+{
+    T limiter;
+    switch (scheme) {
+    case GETM_SCHEME_HSIMT: {
+        T kappa = T(1) - cfl;
+        T x = T(0.25) * (kappa - T(1.0) / T(3.0) / kappa);
+        limiter = (T(0.5) + x) + (T(0.5) - x) * ratio;
+        limiter = fmax(T(0), limiter);
+        limiter = fmin(fmin(T(2) * ratio, limiter), T(2));
+        break;
+    }
+    case GETM_SCHEME_MUSCL:
+        limiter = fmin(fmin(T(2) * ratio, T(0.5) * (T(1) + ratio)), T(2));
+        break;
+    case GETM_SCHEME_P2_PDM: {
+        T x = T(1.0) / T(6.0) * (T(1) - T(2) * cfl);
+        limiter = (T(0.5) + x) + (T(0.5) - x) * ratio;
+        limiter = fmin(fmin(T(2) * ratio / (cfl + T(1.e-10)), limiter), T(2) / (T(1) - cfl));
+        break;
+    }
+    case GETM_SCHEME_SPLMAX13:
+        limiter = fmin(fmin(T(2) * ratio, T(1.0) / T(3.0) * fmax(T(1) + T(2) * ratio, T(2) + ratio)), T(2));
+        break;
+    case GETM_SCHEME_SUPERBEE:
+        limiter = fmax(fmin(T(2) * ratio, T(1)), fmin(ratio, T(2)));
+        break;
+    default:
+        limiter = T(0);
+        break;
+    }
+    return limiter;
+}
+
+// One TVD face value: given upstream-upstream, upstream and downstream values
+// and the face Courant number, return the limited face value
+// (advection.F90.template:82-88, 344-350).
+template <typename T>
+__device__ __forceinline__ T getm_tvd_face(int scheme, T fuu, T fu, T fd, T cfl)
+{
+    T deltaf = fd - fu;
+    T deltafu = fu - fuu;
+    if (deltaf * deltafu > T(0)) {
+        T ratio = deltafu / deltaf;
+        T limiter = getm_limiter<T>(scheme, ratio, cfl);
+        fu = fu + T(0.5) * limiter * (T(1) - cfl) * deltaf;
+    }
+    return fu;
+}
+
+__device__ __forceinline__ bool getm_flux_point(int m) { return m == 1 || m == 2; }

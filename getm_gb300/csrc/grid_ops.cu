@@ -1,0 +1,280 @@
+// Grid utilities of python/src/wrapper.F90 and python/src/interpolation.F90
+// for sm_103a: staggered interpolation, depth/thickness bookkeeping, the
+// surface-elevation update and the surface pressure gradient.
+//
+// These are elementwise or single-pass column kernels; each thread owns one
+// output point (or one column for the vertical recursions), reads its inputs
+// once, and warps run along i so every access is coalesced.
+#include "getm_common.cuh"
+
+#define EW_THREADS 256
+
+// ---------------------------------------------------------------------------
+// interpolation.F90:9-72
+// ---------------------------------------------------------------------------
+__global__ void interp_x_kernel(int nx, int ny, int nz, const double* s, double* t, int ioff)
+{
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n = (long long)nx * ny * nz;
+    if (p >= n) return;
+    int i = (int)(p % nx);
+    if (i >= nx - 1) return;
+    t[p + ioff] = 0.5 * (s[p] + s[p + 1]);
+}
+
+__global__ void interp_y_kernel(int nx, int ny, int nz, const double* s, double* t, int joff)
+{
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n = (long long)nx * ny * nz;
+    if (p >= n) return;
+    int j = (int)((p / nx) % ny);
+    if (j >= ny - 1) return;
+    t[p + (long long)joff * nx] = 0.5 * (s[p] + s[p + nx]);
+}
+
+__global__ void interp_z_kernel(int nx, int ny, int nz1, const double* s, double* t, int koff)
+{
+    long long plane = (long long)nx * ny;
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= plane * (nz1 - 1)) return;
+    t[p + koff * plane] = 0.5 * (s[p] + s[p + plane]);
+}
+
+__global__ void interp_xy_kernel(int nx1, int ny1, int nx2, int ny2, int nz, const double* s,
+                                 double* t, int ioff, int joff)
+{
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n = (long long)(nx1 - 1) * (ny1 - 1) * nz;
+    if (p >= n) return;
+    int i = (int)(p % (nx1 - 1));
+    long long r = p / (nx1 - 1);
+    int j = (int)(r % (ny1 - 1));
+    int k = (int)(r / (ny1 - 1));
+    long long q = ((long long)k * ny1 + j) * nx1 + i;
+    t[((long long)k * ny2 + j + joff) * nx2 + i + ioff] = 0.25 * (s[q] + s[q + 1] + s[q + nx1] + s[q + nx1 + 1]);
+}
+
+extern "C" int getm_grid_interp_x(int nx, int ny, int nz, const double* source, double* target,
+                                  int ioffset, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || !source || !target) return GETM_ERR_ARG;
+    long long n = (long long)nx * ny * nz;
+    interp_x_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, source, target, ioffset);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_grid_interp_y(int nx, int ny, int nz, const double* source, double* target,
+                                  int joffset, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || !source || !target) return GETM_ERR_ARG;
+    long long n = (long long)nx * ny * nz;
+    interp_y_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, source, target, joffset);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_grid_interp_z(int nx, int ny, int nz1, int nz2, const double* source,
+                                  double* target, int koffset, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz1 < 1 || nz2 < 1 || !source || !target) return GETM_ERR_ARG;
+    if (nz1 < 2) return GETM_OK;
+    long long n = (long long)nx * ny * (nz1 - 1);
+    interp_z_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz1, source, target, koffset);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_grid_interp_xy(int nx1, int ny1, int nx2, int ny2, int nz, const double* source,
+                                   double* target, int ioffset, int joffset, cudaStream_t stream)
+{
+    if (nx1 < 1 || ny1 < 1 || nx2 < 1 || ny2 < 1 || nz < 1 || !source || !target) return GETM_ERR_ARG;
+    if (nx1 < 2 || ny1 < 2) return GETM_OK;
+    long long n = (long long)(nx1 - 1) * (ny1 - 1) * nz;
+    interp_xy_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx1, ny1, nx2, ny2, nz, source, target, ioffset, joffset);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// wrapper.F90 utilities
+// ---------------------------------------------------------------------------
+__global__ void elevation2depth_kernel(int n, const double* z, const double* H, double Dmin,
+                                       const int* mask, double* D)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n && mask[p] != 0) D[p] = fmax(H[p] + z[p], Dmin);  // wrapper.F90:444
+}
+
+__global__ void alpha_kernel(int n, const double* D, double Dmin, double Dcrit, const int* mask,
+                             double* alpha)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n && mask[p] != 0)  // wrapper.F90:434
+        alpha[p] = fmax(0.0, fmin(1.0, (D[p] - Dmin) / (Dcrit - Dmin)));
+}
+
+__global__ void multiply_add_kernel(int n, double* tgt, const double* add, double s)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) tgt[p] = tgt[p] + s * add[p];  // wrapper.F90:493
+}
+
+extern "C" int getm_elevation2depth(int n, const double* z, const double* H, double Dmin,
+                                    const int* mask, double* D, cudaStream_t stream)
+{
+    if (n < 0 || !z || !H || !mask || !D) return GETM_ERR_ARG;
+    if (n == 0) return GETM_OK;
+    elevation2depth_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(n, z, H, Dmin, mask, D);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_alpha(int n, const double* D, double Dmin, double Dcrit, const int* mask,
+                          double* alpha, cudaStream_t stream)
+{
+    if (n < 0 || !D || !mask || !alpha) return GETM_ERR_ARG;
+    if (n == 0) return GETM_OK;
+    alpha_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(n, D, Dmin, Dcrit, mask, alpha);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_multiply_add(int n, double* tgt, const double* add, double scale_factor,
+                                 cudaStream_t stream)
+{
+    if (n < 0 || (n > 0 && (!tgt || !add))) return GETM_ERR_ARG;
+    if (n == 0) return GETM_OK;
+    multiply_add_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(n, tgt, add, scale_factor);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// wrapper.F90:409-426: column recursion, thread per column
+__global__ void t2vc_kernel(int nx, int ny, int nz, const int* mask, const double* bd,
+                            const double* h, double* zc, double* zf)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    long long plane = (long long)nx * ny;
+    if (p >= plane || mask[p] == 0) return;
+    double zci = -bd[p] + 0.5 * h[p];
+    zc[p] = zci;
+    double hprev = h[p];
+    for (int k = 1; k < nz; k++) {
+        double hk = h[p + k * plane];
+        zci = zci + 0.5 * (hprev + hk);
+        zc[p + k * plane] = zci;
+        hprev = hk;
+    }
+    double zfi = -bd[p];
+    zf[p] = zfi;
+    for (int k = 1; k <= nz; k++) {
+        zfi = zfi + h[p + (k - 1) * plane];
+        zf[p + k * plane] = zfi;
+    }
+}
+
+extern "C" int getm_thickness2vertical_coordinates(int nx, int ny, int nz, const int* mask,
+                                                   const double* bottom_depth, const double* h,
+                                                   double* zc, double* zf, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || !mask || !bottom_depth || !h || !zc || !zf) return GETM_ERR_ARG;
+    int n = nx * ny;
+    t2vc_kernel<<<getm_div_up(n, 128), 128, 0, stream>>>(nx, ny, nz, mask, bottom_depth, h, zc, zf);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// wrapper.F90:395-407
+__global__ void t2cd_kernel(int nx, int ny, int nz, const int* mask, const double* h, double* out)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    long long plane = (long long)nx * ny;
+    if (p >= plane || mask[p] == 0) return;
+    double hk1 = h[p + (nz - 1) * plane];
+    double o = 0.5 * hk1;
+    out[p + (nz - 1) * plane] = o;
+    for (int k = nz - 2; k >= 0; k--) {
+        double hk = h[p + k * plane];
+        o = o + 0.5 * (hk + hk1);
+        out[p + k * plane] = o;
+        hk1 = hk;
+    }
+}
+
+extern "C" int getm_thickness2center_depth(int nx, int ny, int nz, int istart, int istop, int jstart,
+                                           int jstop, const int* mask, const double* h, double* out,
+                                           cudaStream_t stream)
+{
+    (void)istart; (void)istop; (void)jstart; (void)jstop;  // unused by the reference too
+    if (nx < 1 || ny < 1 || nz < 1 || !mask || !h || !out) return GETM_ERR_ARG;
+    int n = nx * ny;
+    t2cd_kernel<<<getm_div_up(n, 128), 128, 0, stream>>>(nx, ny, nz, mask, h, out);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// wrapper.F90:496-523
+__global__ void surface_elevation_kernel(int nx, int ny, int halox, int haloy, const int* mask,
+                                         const double* dyu, const double* dxv,
+                                         const double* iarea, double* z, const double* U,
+                                         const double* V, const double* fwf, double dt)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i < halox || i >= nx - halox || j < haloy || j >= ny - haloy) return;
+    long long p = (long long)j * nx + i;
+    if (mask[p] != 1) return;
+    z[p] = z[p] + dt * ((U[p - 1] * dyu[p - 1] - U[p] * dyu[p] + V[p - nx] * dxv[p - nx] - V[p] * dxv[p]) * iarea[p] + fwf[p]);
+}
+
+extern "C" int getm_advance_surface_elevation(int nx, int ny, int halox, int haloy, const int* mask,
+                                              const double* dyu, const double* dxv,
+                                              const double* iarea, double* z, const double* U,
+                                              const double* V, const double* fwf, double dt,
+                                              cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || halox < 1 || haloy < 1 || !mask || !dyu || !dxv || !iarea || !z || !U || !V || !fwf)
+        return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), ny);
+    surface_elevation_kernel<<<grid, 128, 0, stream>>>(nx, ny, halox, haloy, mask, dyu, dxv, iarea, z, U, V, fwf, dt);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// wrapper.F90:525-565; C bounds from Fortran 1-based imin..jmax
+__global__ void spg_kernel(int nx, int ny, int ilo, int ihi, int jlo, int jhi, const int* umask,
+                           const int* vmask, const double* idxu, const double* idyv,
+                           const double* z, const double* sp, const double* H, const double* D,
+                           double Dmin, double* dpdx, double* dpdy)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i < ilo || i > ihi || j < jlo || j > jhi) return;
+    long long p = (long long)j * nx + i;
+    const double gammai = 1.0 / (GETM_G * GETM_RHO0);
+    if (umask[p] == 1) {
+        double zp = fmax(z[p + 1], -H[p] + fmin(Dmin, D[p + 1]));
+        double zm = fmax(z[p], -H[p + 1] + fmin(Dmin, D[p]));
+        dpdx[p] = (zp - zm + (sp[p + 1] - sp[p]) * gammai) * idxu[p];
+    }
+    if (vmask[p] == 1) {
+        double zp = fmax(z[p + nx], -H[p] + fmin(Dmin, D[p + nx]));
+        double zm = fmax(z[p], -H[p + nx] + fmin(Dmin, D[p]));
+        dpdy[p] = (zp - zm + (sp[p + nx] - sp[p]) * gammai) * idyv[p];
+    }
+}
+
+extern "C" int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax, int jmin, int jmax,
+                                              const int* umask, const int* vmask, const double* idxu,
+                                              const double* idyv, const double* z, const double* sp,
+                                              const double* H, const double* D, double Dmin,
+                                              double* dpdx, double* dpdy, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || imin < 1 || jmin < 1 || imax >= nx || jmax >= ny) return GETM_ERR_ARG;
+    if (!umask || !vmask || !idxu || !idyv || !z || !sp || !H || !D || !dpdx || !dpdy) return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), ny);
+    spg_kernel<<<grid, 128, 0, stream>>>(nx, ny, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask, idxu, idyv, z, sp, H, D, Dmin, dpdx, dpdy);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}

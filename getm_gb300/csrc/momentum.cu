@@ -1,0 +1,386 @@
+// Momentum kernels of python/src/momentum.F90 and c_momentum_diffusion of
+// python/src/wrapper.F90:275-393, for sm_103a.
+//
+// Elementwise work maps one thread to one output point with warps along i;
+// the stencils that the reference evaluates as "flux array, then divergence"
+// recompute the two face fluxes of each point in registers instead of
+// writing a flux array (no intermediate traffic).  Column recursions
+// (w_momentum_3d) use one thread per column.
+#include "getm_common.cuh"
+
+#define EW_THREADS 256
+
+// momentum.F90:12-77
+__global__ void horizontal_diffusion_kernel(int nx_, int ny_, int ilo, int ihi, int jlo, int jhi,
+                                            const int* umask, const int* vmask, const double* idxu,
+                                            const double* dyu, const double* idyv, const double* dxv,
+                                            const double* Ah_u, const double* Ah_v, const int* tmask,
+                                            const double* iA, double dt, const double* f, double* df)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i < ilo || i > ihi || j < jlo || j > jhi) return;
+    long long p = (long long)j * nx_ + i;
+    if (tmask[p] != 1) return;
+    long long w = p - 1, s = p - nx_;
+    double ufe = (umask[p] == 1) ? Ah_u[p] * (f[p + 1] - f[p]) * idxu[p] * dyu[p] : 0.0;
+    double ufw = (umask[w] == 1) ? Ah_u[w] * (f[w + 1] - f[w]) * idxu[w] * dyu[w] : 0.0;
+    double vfn = (vmask[p] == 1) ? Ah_v[p] * (f[p + nx_] - f[p]) * idyv[p] * dxv[p] : 0.0;
+    double vfs = (vmask[s] == 1) ? Ah_v[s] * (f[s + nx_] - f[s]) * idyv[s] * dxv[s] : 0.0;
+    df[p] = dt * (ufe - ufw + vfn - vfs) * iA[p];
+}
+
+extern "C" int getm_horizontal_diffusion(int imin, int imax, int jmin, int jmax, int halox, int haloy,
+                                         const int* umask, const int* vmask, const double* idxu,
+                                         const double* dyu, const double* idyv, const double* dxv,
+                                         const double* Ah_u, const double* Ah_v, const int* tmask,
+                                         const double* iA, double dt, const double* f, double* out,
+                                         cudaStream_t stream)
+{
+    if (imax < imin || jmax < jmin || halox < 1 || haloy < 1) return GETM_ERR_ARG;
+    if (!umask || !vmask || !idxu || !dyu || !idyv || !dxv || !Ah_u || !Ah_v || !tmask || !iA || !f || !out)
+        return GETM_ERR_ARG;
+    int nx_ = imax - imin + 1 + 2 * halox, ny_ = jmax - jmin + 1 + 2 * haloy;
+    dim3 grid(getm_div_up(nx_, 128), ny_);
+    horizontal_diffusion_kernel<<<grid, 128, 0, stream>>>(nx_, ny_, halox, halox + imax - imin, haloy, haloy + jmax - jmin,
+                                                          umask, vmask, idxu, dyu, idyv, dxv, Ah_u, Ah_v, tmask, iA, dt, f, out);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// momentum.F90:79-101
+__global__ void bottom_friction_kernel(int n, const int* mask, const double* u, const double* v,
+                                       const double* D, double* z0b, const double* z0b_min,
+                                       double avmmol, double* ru, int iterate)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n || mask[p] != 1) return;
+    double uu = u[p], vv = v[p], DD = D[p];
+    double z0 = z0b[p];
+    double sqrtcd = GETM_KAPPA / log(1.0 + 0.5 * DD / z0);
+    if (iterate != 0) {
+        z0 = fmin(DD, z0b_min[p] + 0.1 * avmmol / fmax(avmmol, sqrtcd * sqrt(uu * uu + vv * vv)));
+        z0b[p] = z0;
+        sqrtcd = GETM_KAPPA / log(1.0 + 0.5 * DD / z0);
+    }
+    ru[p] = sqrtcd * sqrtcd * sqrt(uu * uu + vv * vv);
+}
+
+extern "C" int getm_bottom_friction(int nx, int ny, const int* mask, const double* u, const double* v,
+                                    const double* D, double* z0b, const double* z0b_in, double avmmol,
+                                    double* ru, int iterate, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || !mask || !u || !v || !D || !z0b || !ru || (iterate && !z0b_in)) return GETM_ERR_ARG;
+    int n = nx * ny;
+    bottom_friction_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(n, mask, u, v, D, z0b, z0b_in, avmmol, ru, iterate);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// momentum.F90:103-145: rows haloy..ny-haloy-1, every i, every k (mask unused)
+__global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const double* alpha,
+                                       const double* ho, const double* hn, const double* dp,
+                                       const double* cor, const double* adv, const double* diff,
+                                       const double* idp, const double* taus, const double* rr,
+                                       double dt, double* ea2, double* ea4)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + haloy;
+    if (i >= nx) return;
+    long long plane = (long long)nx * ny;
+    long long p = (long long)j * nx + i;
+    const double al = alpha[p], dpp = dp[p];
+    const double rho0i = 1.0 / GETM_RHO0;
+    for (int k = 0; k < nz; k++) {
+        long long q = p + k * plane;
+        double e = dt * (-0.5 * (ho[q] + hn[q]) * GETM_G * dpp + al * (cor[q] + adv[q] + diff[q] + idp[q]));
+        if (k == nz - 1) e = e + dt * al * taus[p] * rho0i;
+        ea4[q] = e;
+    }
+    ea2[p] = -dt * rr[p];
+}
+
+extern "C" int getm_collect_3d_momentum_sources(int nx, int ny, int nz, int halox, int haloy,
+                                                const int* mask, const double* alpha, const double* ho,
+                                                const double* hn, const double* dp, const double* cor,
+                                                const double* adv, const double* diff, const double* idp,
+                                                const double* taus, const double* rr, double dt,
+                                                double* ea2, double* ea4, cudaStream_t stream)
+{
+    (void)mask; (void)halox;
+    if (nx < 1 || ny <= 2 * haloy || nz < 1 || !alpha || !ho || !hn || !dp || !cor || !adv || !diff || !idp || !taus || !rr || !ea2 || !ea4)
+        return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), ny - 2 * haloy);
+    collect_sources_kernel<<<grid, 128, 0, stream>>>(nx, ny, nz, haloy, alpha, ho, hn, dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// momentum.F90:147-189
+__global__ void advance_2d_transport_kernel(int nx, int ny, int halox, int haloy, const int* mask,
+                                            const double* alpha, const double* D, const double* dp,
+                                            const double* taus, const double* cor, const double* adv,
+                                            const double* diff, const double* damp, const double* SA,
+                                            const double* SB, const double* SD, const double* SF,
+                                            const double* r, double dt, double* U)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i < halox || i >= nx - halox || j < haloy || j >= ny - haloy) return;
+    long long p = (long long)j * nx + i;
+    if (mask[p] != 1) return;
+    const double rho0i = 1.0 / GETM_RHO0;
+    double Up = U[p];
+    double Slr = (Up > 0.0) ? fmin(SF[p], 0.0) : fmax(SF[p], 0.0);
+    double Dp = D[p];
+    U[p] = (Up + dt * (-GETM_G * Dp * dp[p] + alpha[p] * (taus[p] * rho0i + cor[p] + adv[p] + diff[p] + damp[p] + SA[p] + SB[p] + SD[p] + Slr)))
+           / (1.0 + dt * r[p] / Dp);
+}
+
+extern "C" int getm_advance_2d_transport(int nx, int ny, int halox, int haloy, const int* mask,
+                                         const double* alpha, const double* D, const double* dp,
+                                         const double* taus, const double* cor, const double* adv,
+                                         const double* diff, const double* damp, const double* SA,
+                                         const double* SB, const double* SD, const double* SF,
+                                         const double* r, double dt, double* U, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || !mask || !alpha || !D || !dp || !taus || !cor || !adv || !diff || !damp || !SA || !SB || !SD || !SF || !r || !U)
+        return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), ny);
+    advance_2d_transport_kernel<<<grid, 128, 0, stream>>>(nx, ny, halox, haloy, mask, alpha, D, dp, taus, cor, adv, diff, damp, SA, SB, SD, SF, r, dt, U);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// momentum.F90:191-216: thread per column
+__global__ void w_momentum_3d_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
+                                     const int* mask, const double* dyu, const double* dxv,
+                                     const double* iarea, const double* ho, const double* hn,
+                                     const double* pk, const double* qk, double dt, double* w)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + jlo;
+    if (i < ilo || i > ihi || j > jhi) return;
+    long long p = (long long)j * nx + i;
+    if (mask[p] != 1) return;
+    long long plane = (long long)nx * ny;
+    const double idt = 1.0 / dt;
+    const double dyE = dyu[p], dyW = dyu[p - 1], dxN = dxv[p], dxS = dxv[p - nx], ia = iarea[p];
+    double wk = w[p];
+    for (int k = 1; k <= nz - 1; k++) {
+        long long q = p + (k - 1) * plane;
+        wk = wk - (hn[q] - ho[q]) * idt - (pk[q] * dyE - pk[q - 1] * dyW + qk[q] * dxN - qk[q - nx] * dxS) * ia;
+        w[p + k * plane] = wk;
+    }
+}
+
+extern "C" int getm_w_momentum_3d(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                  const int* mask, const double* dyu, const double* dxv,
+                                  const double* iarea, const double* ho, const double* hn,
+                                  const double* pk, const double* qk, double dt, double* w,
+                                  cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !dyu || !dxv || !iarea || !ho || !hn || !pk || !qk || !w) return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1);
+    w_momentum_3d_kernel<<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, dyu, dxv, iarea, ho, hn, pk, qk, dt, w);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// momentum.F90:218-241
+__global__ void shear_frequency_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
+                                       const int* mask, const double* hu, const double* hv,
+                                       const double* uk, const double* vk, double* SS)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + jlo;
+    int k = blockIdx.z + 1;  // Fortran interface k = 1..nz-1
+    if (i < ilo || i > ihi || j > jhi) return;
+    long long p = (long long)j * nx + i;
+    if (mask[p] <= 0) return;
+    long long plane = (long long)nx * ny;
+    long long a = p + (k - 1) * plane, b = p + k * plane;
+    double t1 = (uk[b] - uk[a]) / (0.5 * (hu[b] + hu[a]));
+    double t2 = (uk[b - 1] - uk[a - 1]) / (0.5 * (hu[b - 1] + hu[a - 1]));
+    double t3 = (vk[b] - vk[a]) / (0.5 * (hv[b] + hv[a]));
+    double t4 = (vk[b - nx] - vk[a - nx]) / (0.5 * (hv[b - nx] + hv[a - nx]));
+    SS[b] = 0.5 * (t1 * t1 + t2 * t2 + t3 * t3 + t4 * t4);
+}
+
+extern "C" int getm_shear_frequency(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                    const int* mask, const double* hu, const double* hv, const double* uk,
+                                    const double* vk, double* SS, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !hu || !hv || !uk || !vk || !SS) return GETM_ERR_ARG;
+    if (nz < 2) return GETM_OK;
+    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1, nz - 1);
+    shear_frequency_kernel<<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, hu, hv, uk, vk, SS);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// momentum.F90:270-284
+__global__ void surface_shear_velocity_kernel(int nx, int ilo, int ihi, int jlo, int jhi, const int* mask,
+                                              const double* taux, const double* tauy, double* ustar)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + jlo;
+    if (i < ilo || i > ihi || j > jhi) return;
+    long long p = (long long)j * nx + i;
+    if (mask[p] > 0) {
+        const double rho0i = 1.0 / GETM_RHO0;
+        ustar[p] = pow(taux[p] * taux[p] + tauy[p] * tauy[p], 0.25) * sqrt(rho0i);
+    }
+}
+
+extern "C" int getm_surface_shear_velocity(int nx, int ny, int imin, int imax, int jmin, int jmax,
+                                           const int* mask, const double* tausx, const double* tausy,
+                                           double* ustar2_s, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || imin < 1 || jmin < 1 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !tausx || !tausy || !ustar2_s) return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1);
+    surface_shear_velocity_kernel<<<grid, 128, 0, stream>>>(nx, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, tausx, tausy, ustar2_s);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// momentum.F90:286-321.  The two stress components are stored on their
+// rows and recomputed in registers where the shear velocity needs a
+// neighbour's value (same product, same result).
+__global__ void bottom_shear_velocity_kernel(int nx, int ny, int ilo, int ihi, int jlo, int jhi,
+                                             const int* mask, const double* uk_bot, const double* vk_bot,
+                                             const double* rru, const double* rrv, double* ustar2_x,
+                                             double* ustar2_y, double* ustar)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= nx || j >= ny) return;
+    long long p = (long long)j * nx + i;
+    if (j >= jlo && j <= jhi) ustar2_x[p] = -uk_bot[p] * rru[p];
+    if (j >= jlo - 1 && j <= jhi) ustar2_y[p] = -vk_bot[p] * rrv[p];
+    if (i >= ilo && i <= ihi && j >= jlo && j <= jhi && mask[p] == 1) {
+        double a = -uk_bot[p - 1] * rru[p - 1];
+        double b = -uk_bot[p] * rru[p];
+        double c = -vk_bot[p - nx] * rrv[p - nx];
+        double d = -vk_bot[p] * rrv[p];
+        ustar[p] = pow(0.5 * (a * a + b * b + c * c + d * d), 0.25);
+    }
+}
+
+extern "C" int getm_bottom_shear_velocity(int nx, int ny, int imin, int imax, int jmin, int jmax,
+                                          const int* mask, const int* umask, const int* vmask,
+                                          const double* uk_bot, const double* vk_bot, const double* rru,
+                                          const double* rrv, double* taubx, double* tauby,
+                                          double* ustar2_b, cudaStream_t stream)
+{
+    (void)umask; (void)vmask;
+    if (nx < 1 || ny < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !uk_bot || !vk_bot || !rru || !rrv || !taubx || !tauby || !ustar2_b) return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), ny);
+    bottom_shear_velocity_kernel<<<grid, 128, 0, stream>>>(nx, ny, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, uk_bot, vk_bot, rru, rrv, taubx, tauby, ustar2_b);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// momentum.F90:323-340: rows jmin..jmax, every i
+__global__ void reconstruct_kernel(int nx, int ny, int nz, int jlo, int jhi, double* un, const double* hn,
+                                   const double* Uo, double idt)
+{
+    long long plane = (long long)nx * ny;
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= plane * nz) return;
+    int j = (int)((p % plane) / nx);
+    if (j < jlo || j > jhi) return;
+    un[p] = (un[p] * hn[p] - Uo[p]) * idt;
+}
+
+extern "C" int getm_reconstruct_transport_change(int nx, int ny, int nz, int imin, int imax, int jmin,
+                                                 int jmax, double* un, const double* hn, const double* Uo,
+                                                 double timestep, cudaStream_t stream)
+{
+    (void)imin; (void)imax;
+    if (nx < 1 || ny < 1 || nz < 1 || jmin < 1 || jmax > ny || !un || !hn || !Uo) return GETM_ERR_ARG;
+    long long n = (long long)nx * ny * nz;
+    reconstruct_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, jmin - 1, jmax - 1, un, hn, Uo, 1.0 / timestep);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// wrapper.F90:275-393 (one layer per blockIdx.z).  All six grids share the
+// extent of the U grid (python/pygetm/domain.py:699-725).
+struct MomDiffArgs {
+    int nx, ny, ilo, ihi, jlo, jhi;
+    const int *umask, *vmask, *uumask, *uvmask, *vumask, *vvmask;
+    const double *uiarea, *viarea, *uudy, *uuidx, *uvdx, *uvidx, *uvidy, *vudy, *vuidx, *vuidy, *vvdx, *vvidy;
+    const double *huu, *huv, *hvu, *hvv, *u, *v;
+    double Am0;
+    double *diffu, *diffv;
+};
+
+__global__ void momentum_diffusion_kernel(MomDiffArgs a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    int k = blockIdx.z;
+    if (i < a.ilo || i > a.ihi || j < a.jlo || j > a.jhi) return;
+    const long long nx = a.nx;
+    long long p = (long long)j * nx + i;
+    long long off = (long long)k * nx * a.ny;
+    const double* u = a.u + off;
+    const double* v = a.v + off;
+    const double Am0 = a.Am0;
+#define FUU(q) ((a.uumask[q] != 0) ? 2.0 * Am0 * a.uudy[q] * a.huu[off + (q)] * (u[(q) + 1] - u[q]) * a.uuidx[q] : 0.0)
+#define FUV(q) ((a.uvmask[q] != 0) ? Am0 * a.uvdx[q] * a.huv[off + (q)] * ((u[(q) + nx] - u[q]) * a.uvidy[q] + (v[(q) + 1] - v[q]) * a.uvidx[q]) : 0.0)
+#define FVU(q) ((a.vumask[q] != 0) ? Am0 * a.vudy[q] * a.hvu[off + (q)] * ((u[(q) + nx] - u[q]) * a.vuidy[q] + (v[(q) + 1] - v[q]) * a.vuidx[q]) : 0.0)
+#define FVV(q) ((a.vvmask[q] != 0) ? 2.0 * Am0 * a.vvdx[q] * a.hvv[off + (q)] * (v[(q) + nx] - v[q]) * a.vvidy[q] : 0.0)
+    // diffu: :323-356
+    double du = 0.0;
+    int um = a.umask[p];
+    if (um == 1) du = (FUU(p) - FUU(p - 1)) * a.uiarea[p];
+    if (um == 1 || um == 2) du = du + (FUV(p) - FUV(p - nx)) * a.uiarea[p];
+    a.diffu[off + p] = du;
+    // diffv: :358-391
+    double dv = 0.0;
+    if (a.vmask[p] == 1) {
+        dv = (FVU(p) - FVU(p - 1)) * a.viarea[p];
+        dv = dv + (FVV(p) - FVV(p - nx)) * a.viarea[p];
+    }
+    a.diffv[off + p] = dv;
+#undef FUU
+#undef FUV
+#undef FVU
+#undef FVV
+}
+
+extern "C" int getm_momentum_diffusion(getm_grid* UG, getm_grid* VG, getm_grid* UUG, getm_grid* UVG,
+                                       getm_grid* VUG, getm_grid* VVG, int nk, const double* huu,
+                                       const double* huv, const double* hvu, const double* hvv,
+                                       const double* u, const double* v, double Am0, double* diffu,
+                                       double* diffv, cudaStream_t stream)
+{
+    if (!UG || !VG || !UUG || !UVG || !VUG || !VVG || nk < 1) return GETM_ERR_ARG;
+    if (!huu || !huv || !hvu || !hvv || !u || !v || !diffu || !diffv) return GETM_ERR_ARG;
+    MomDiffArgs a;
+    a.nx = UG->nx_; a.ny = UG->ny_;
+    a.ilo = UG->halox; a.ihi = UG->halox + UG->imax - UG->imin;
+    a.jlo = UG->haloy; a.jhi = UG->haloy + UG->jmax - UG->jmin;
+    a.umask = UG->mask; a.vmask = VG->mask; a.uumask = UUG->mask; a.uvmask = UVG->mask;
+    a.vumask = VUG->mask; a.vvmask = VVG->mask;
+    a.uiarea = UG->iarea; a.viarea = VG->iarea;
+    a.uudy = UUG->dy; a.uuidx = UUG->idx;
+    a.uvdx = UVG->dx; a.uvidx = UVG->idx; a.uvidy = UVG->idy;
+    a.vudy = VUG->dy; a.vuidx = VUG->idx; a.vuidy = VUG->idy;
+    a.vvdx = VVG->dx; a.vvidy = VVG->idy;
+    a.huu = huu; a.huv = huv; a.hvu = hvu; a.hvv = hvv; a.u = u; a.v = v; a.Am0 = Am0;
+    a.diffu = diffu; a.diffv = diffv;
+    if (!a.umask || !a.vmask || !a.uumask || !a.uvmask || !a.vumask || !a.vvmask || !a.uiarea || !a.viarea ||
+        !a.uudy || !a.uuidx || !a.uvdx || !a.uvidx || !a.uvidy || !a.vudy || !a.vuidx || !a.vuidy || !a.vvdx || !a.vvidy)
+        return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(a.nx, 128), a.ny, nk);
+    momentum_diffusion_kernel<<<grid, 128, 0, stream>>>(a);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}

@@ -1,0 +1,193 @@
+// Internal pressure gradients of python/src/internal_pressure.F90 for sm_103a:
+// Blumberg & Mellor (:9-60) and Shchepetkin & McWilliams (:63-217).
+//
+// Blumberg-Mellor: one thread per water column integrates downward from the
+// surface for the U and the V point of that column.
+// Shchepetkin-McWilliams, two kernels:
+//   1. thread per T column: vertical harmonic-mean slopes dR, dZ (kept in a
+//      register window, never stored) and the column pressure integral P,
+//      written to a caller-provided 3D work array;
+//   2. thread per (i, j, k) U/V point: horizontal harmonic-mean slopes from
+//      the three raw differences around the point, the density-Jacobian
+//      correction FC and the gradient.  The reference's per-level dZx/dRx
+//      work arrays are recomputed in registers (same operations, same values).
+#include "getm_common.cuh"
+
+// ---------------------------------------------------------------------------
+// Blumberg & Mellor
+// ---------------------------------------------------------------------------
+__global__ void blumberg_mellor_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
+                                       const int* umask, const int* vmask, const double* idxu,
+                                       const double* idyv, const double* hu, const double* hv,
+                                       const double* zf, const double* buoy, double* idpdx,
+                                       double* idpdy)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + jlo;
+    if (i < ilo || i > ihi || j > jhi) return;
+    const long long P = (long long)nx * ny;
+    const long long p = (long long)j * nx + i;
+    // levels: buoy/hu Fortran k -> plane k-1; zf Fortran k -> plane k
+    for (int dir = 0; dir < 2; dir++) {
+        const int* m = dir ? vmask : umask;
+        if (m[p] <= 0) continue;
+        const long long s = dir ? nx : 1;
+        const double id = dir ? idyv[p] : idxu[p];
+        const double* hh = dir ? hv : hu;
+        double* out = dir ? idpdy : idpdx;
+        long long q = p + (long long)(nz - 1) * P;
+        double grdl = (buoy[q + s] - buoy[q]) * id;
+        double buoyl = 0.5 * (buoy[q + s] + buoy[q]);
+        double hk1 = hh[q];
+        double prgr = grdl * 0.5 * hk1;
+        out[q] = hk1 * prgr;
+        for (int k = nz - 1; k >= 1; k--) {
+            q = p + (long long)(k - 1) * P;
+            double grdu = grdl;
+            grdl = (buoy[q + s] - buoy[q]) * id;
+            double buoyu = buoyl;
+            buoyl = 0.5 * (buoy[q + s] + buoy[q]);
+            long long qf = p + (long long)k * P;
+            double dxz = (zf[qf + s] - zf[qf]) * id;
+            double hk = hh[q];
+            prgr = prgr + 0.5 * (grdu + grdl) * 0.5 * (hk + hk1) - dxz * (buoyu - buoyl);
+            out[q] = hk * prgr;
+            hk1 = hk;
+        }
+    }
+}
+
+extern "C" int getm_blumberg_mellor(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                    const int* umask, const int* vmask, const double* idxu,
+                                    const double* idyv, const double* hu, const double* hv,
+                                    const double* zf, const double* buoy, double* idpdx, double* idpdy,
+                                    cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 1 || jmin < 1 || imax >= nx || jmax >= ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!umask || !vmask || !idxu || !idyv || !hu || !hv || !zf || !buoy || !idpdx || !idpdy) return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1);
+    blumberg_mellor_kernel<<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask, idxu, idyv, hu, hv, zf, buoy, idpdx, idpdy);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Shchepetkin & McWilliams
+// ---------------------------------------------------------------------------
+#define SMCW_EPS 1.e-10
+
+// Harmonic mean with the cut-off of internal_pressure.F90:93-98.
+__device__ __forceinline__ double smcw_harm_cut(double a, double b)
+{
+    double cff = 2.0 * a * b;
+    return (cff > SMCW_EPS) ? cff / (a + b) : 0.0;
+}
+
+// Phase 1 (internal_pressure.F90:80-118): column pressure integral P.
+// Columns with mask > 0 over C i in [ilo, ihi+1], j in [jlo, jhi+1].
+__global__ void smcw_column_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
+                                   const int* mask, const double* h, const double* zc,
+                                   const double* buoy, double* Pw)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + jlo;
+    if (i < ilo || i > ihi + 1 || j > jhi + 1) return;
+    const long long P = (long long)nx * ny;
+    const long long p = (long long)j * nx + i;
+    if (mask[p] <= 0) return;
+    const double x = 1.0 / 12.0;
+#define B(k) buoy[p + (long long)((k) - 1) * P]
+#define Z(k) zc[p + (long long)((k) - 1) * P]
+    // Fortran levels 1..nz.  Raw differences d(k) = v(k+1) - v(k), k = 1..nz-1,
+    // d(nz) = d(nz-1), d(0) = d(1); harmonic HR(k) from d(k), d(k-1).
+    double cff = 0.0;
+    if (nz > 1) cff = 0.5 * (B(nz) - B(nz - 1)) * 0.5 * h[p + (long long)(nz - 1) * P] / (Z(nz) - Z(nz - 1));
+    double Pk = (B(nz) + cff) * 0.5 * h[p + (long long)(nz - 1) * P];
+    Pw[p + (long long)(nz - 1) * P] = Pk;
+    if (nz == 1) return;
+    // window at level k+1 = nz: HR(nz) uses d(nz) = d(nz-1) and d(nz-1)
+    double bk1 = B(nz), zk1 = Z(nz);          // v(k+1)
+    double bk = B(nz - 1), zk = Z(nz - 1);    // v(k)
+    double dRk = bk1 - bk, dZk = zk1 - zk;    // d(k) with k = nz-1
+    double HR1 = smcw_harm_cut(dRk, dRk);     // HR(nz): d(nz) = d(nz-1)
+    double HZ1 = 2.0 * dZk * dZk / (dZk + dZk);
+    for (int k = nz - 1; k >= 1; k--) {
+        // d(k-1): for k == 1 it is d(0) = d(1)
+        double dRm, dZm, bkm1 = 0.0, zkm1 = 0.0;
+        if (k > 1) {
+            bkm1 = B(k - 1); zkm1 = Z(k - 1);
+            dRm = bk - bkm1; dZm = zk - zkm1;
+        } else {
+            dRm = dRk; dZm = dZk;
+        }
+        double HR0 = smcw_harm_cut(dRk, dRm);   // HR(k)
+        double HZ0 = 2.0 * dZk * dZm / (dZk + dZm);
+        Pk = Pk + 0.5 * ((bk1 + bk) * (zk1 - zk) - 0.2 * ((HR1 - HR0) * (zk1 - zk - x * (HZ1 + HZ0))
+                  - (HZ1 - HZ0) * (bk1 - bk - x * (HR1 + HR0))));
+        Pw[p + (long long)(k - 1) * P] = Pk;
+        // shift: level k becomes k+1
+        HR1 = HR0; HZ1 = HZ0;
+        bk1 = bk; zk1 = zk; bk = bkm1; zk = zkm1;
+        dRk = dRm; dZk = dZm;
+    }
+#undef B
+#undef Z
+}
+
+// Phase 2 (internal_pressure.F90:120-216) for one direction (s = 1: x, s = nx: y).
+__global__ void smcw_gradient_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
+                                     const int* umask, const int* vmask, const double* idxu,
+                                     const double* idyv, const double* h, const double* z,
+                                     const double* zc, const double* buoy, const double* Pw,
+                                     double* idpdx, double* idpdy)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + jlo;
+    int k = blockIdx.z;  // C level (Fortran k+1)
+    if (i < ilo || i > ihi || j > jhi) return;
+    const long long P = (long long)nx * ny;
+    const long long p = (long long)j * nx + i;
+    const long long q = p + (long long)k * P;
+    const long long qtop = p + (long long)(nz - 1) * P;
+    const double x = 1.0 / 12.0;
+    for (int dir = 0; dir < 2; dir++) {
+        const int* m = dir ? vmask : umask;
+        if (m[p] != 1) continue;
+        const long long s = dir ? nx : 1;
+        // raw differences at p, p+s, p+2s (Fortran i, i+1, i+2), each gated
+        // by the mask of the velocity point just before it
+        double rZ0 = 0.0, rR0 = 0.0, rZ1 = 0.0, rR1 = 0.0, rZ2 = 0.0, rR2 = 0.0;
+        if (m[p - s] > 0) { rZ0 = zc[q] - zc[q - s]; rR0 = buoy[q] - buoy[q - s]; }
+        if (m[p] > 0) { rZ1 = zc[q + s] - zc[q]; rR1 = buoy[q + s] - buoy[q]; }
+        if (m[p + s] > 0) { rZ2 = zc[q + 2 * s] - zc[q + s]; rR2 = buoy[q + 2 * s] - buoy[q + s]; }
+        double dZx0 = smcw_harm_cut(rZ0, rZ1), dZx1 = smcw_harm_cut(rZ1, rZ2);
+        double dRx0 = smcw_harm_cut(rR0, rR1), dRx1 = smcw_harm_cut(rR1, rR2);
+        double FC = 0.5 * ((buoy[q + s] + buoy[q]) * (zc[q + s] - zc[q])
+                    - 0.2 * ((dRx1 - dRx0) * (zc[q + s] - zc[q] - x * (dZx1 + dZx0))
+                    - (dZx1 - dZx0) * (buoy[q + s] - buoy[q] - x * (dRx1 + dRx0))));
+        double id = dir ? idyv[p] : idxu[p];
+        double* out = dir ? idpdy : idpdx;
+        out[q] = 0.5 * (h[q] + h[q + s]) * id
+                 * (Pw[q + s] - Pw[q] + FC - (z[p + s] - z[p]) * 0.5 * (buoy[qtop + s] + buoy[qtop]));
+    }
+}
+
+extern "C" int getm_shchepetkin_mcwilliams(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                           const int* mask, const int* umask, const int* vmask,
+                                           const double* idxu, const double* idyv, const double* h,
+                                           const double* z, const double* zc, const double* buoy,
+                                           double* idpdx, double* idpdy, double* P_work,
+                                           cudaStream_t stream)
+{
+    // the stencil reaches i+2 / j+2 of the last interior point
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax + 2 > nx || jmax + 2 > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !umask || !vmask || !idxu || !idyv || !h || !z || !zc || !buoy || !idpdx || !idpdy || !P_work)
+        return GETM_ERR_ARG;
+    dim3 g1(getm_div_up(nx, 128), jmax - jmin + 2);
+    smcw_column_kernel<<<g1, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, h, zc, buoy, P_work);
+    GETM_CHECK_LAUNCH();
+    dim3 g2(getm_div_up(nx, 128), jmax - jmin + 1, nz);
+    smcw_gradient_kernel<<<g2, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask, idxu, idyv, h, z, zc, buoy, P_work, idpdx, idpdy);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}

@@ -1,0 +1,273 @@
+// Implicit (Crank-Nicolson) vertical diffusion for sm_103a.
+//
+// Reference: src/operators/diffusion.F90 (prepare :135-204, apply :206-314)
+// reached through python/src/wrapper.F90:127-186 and
+// python/pygetm/operators.py:218-230 (VerticalDiffusion).
+//
+// GB300 design: one thread per water column.  The C layout [k][j][i] puts the
+// 32 columns of a warp next to each other at every level, so each per-level
+// load/store of the sweep is a fully coalesced 256-byte transaction.  The
+// tridiagonal matrix is never stored: its coefficients are formed on the fly
+// from nuh, ho, hn and var while sweeping down from the surface (the Thomas
+// forward elimination of diffusion.F90:285-292), keeping only the two
+// elimination coefficients per level in shared memory for the back
+// substitution (:304-307).  prepare+apply are fused (traffic per field: read
+// nuh, ho, hn, var [+ea2, ea4], write var).  A warp-per-column PCR solve would
+// cost O(nz log nz) FP64 divides per column instead of O(nz); GB300's FP64
+// rate makes the serial Thomas sweep the faster choice.
+#include <stdlib.h>
+#include <string.h>
+
+#include "getm_common.cuh"
+
+#define VD_MAX_BATCH 32
+
+struct getm_vertical_diffusion {
+    getm_grid* tgrid;
+    size_t n3;
+    double* auxo;   // prepare -> apply work arrays (diffusion.F90:88)
+    double* auxn;
+};
+
+struct VDArgs {
+    int nx_, ny_, nz;
+    long long plane;
+    const int* mask;
+    const double* nuh;     // nz+1 interface levels
+    const double* ho;
+    const double* hn;
+    const double* auxo;    // when prepared separately (else NULL)
+    const double* auxn;
+    double dt, cnpar;
+    int ntracer;
+    double molecular[VD_MAX_BATCH];
+    double* var[VD_MAX_BATCH];
+    const double* ea2[VD_MAX_BATCH];
+    const double* ea4[VD_MAX_BATCH];
+};
+
+// Coupling coefficients of the interface above C level k (between levels k and
+// k+1): diffusion.F90:166-168 with Fortran k = C k + 1.
+__device__ __forceinline__ void vd_aux(const VDArgs& a, long long c, int k, double mol,
+                                       double& auxo, double& auxn)
+{
+    const long long P = a.plane;
+    if (a.auxo) {
+        auxo = a.auxo[c + k * P];
+        auxn = a.auxn[c + k * P];
+        return;
+    }
+    double x = 2.0 * a.dt * (a.nuh[c + (k + 1) * P] + mol);
+    auxo = (1.0 - a.cnpar) * x / (a.ho[c + (k + 1) * P] + a.ho[c + k * P]);
+    auxn = a.cnpar * x / (a.hn[c + (k + 1) * P] + a.hn[c + k * P]);
+}
+
+// Thread per column; dynamic shared memory holds ru/qu: 2 * nz * blockDim doubles.
+__global__ void vd_column_kernel(VDArgs a)
+{
+    extern __shared__ double smem[];
+    const int tid = threadIdx.x;
+    const int nthreads = blockDim.x;
+    const int i = blockIdx.x * blockDim.x + tid;
+    const int j = blockIdx.y;
+    if (i >= a.nx_) return;
+    const long long c = (long long)j * a.nx_ + i;
+    const long long P = a.plane;
+    const int nz = a.nz;
+    if (nz == 1) {  // diffusion.F90:224-231: every point, mask not consulted
+        for (int t = 0; t < a.ntracer; t++) {
+            double a4 = a.ho[c] * a.var[t][c];
+            double a2 = a.hn[c];
+            if (a.ea4[t]) a4 = a4 + a.ea4[t][c];
+            if (a.ea2[t]) a2 = a2 - a.ea2[t][c];
+            a.var[t][c] = a4 / a2;
+        }
+        return;
+    }
+    if (a.mask[c] != 1) return;
+    double* ru = smem;                        // ru[k * nthreads + tid]
+    double* qu = smem + (size_t)nz * nthreads;
+    for (int t = 0; t < a.ntracer; t++) {
+        double* __restrict__ var = a.var[t];
+        const double* ea2 = a.ea2[t];
+        const double* ea4 = a.ea4[t];
+        const double mol = a.molecular[t];
+        // surface layer (C level nz-1), diffusion.F90:238-245
+        int k = nz - 1;
+        double aob, anb;                       // aux of the interface below level k
+        vd_aux(a, c, k - 1, mol, aob, anb);
+        double vk = var[c + k * P];
+        double vkm1 = var[c + (k - 1) * P];
+        double a1 = -anb;
+        double a2 = a.hn[c + k * P] + anb;
+        double a4 = vk * a.ho[c + k * P] + (vkm1 - vk) * aob;
+        if (ea2) a2 = a2 - ea2[c + k * P];
+        if (ea4) a4 = a4 + ea4[c + k * P];
+        double rk = a1 / a2;
+        double qk = a4 / a2;
+        ru[k * nthreads + tid] = rk;
+        qu[k * nthreads + tid] = qk;
+        // inner layers, diffusion.F90:247-258 and elimination :287-290
+        double aoa = aob, ana = anb;           // interface above level k-1
+        double vkp1 = vk;
+        vk = vkm1;
+        for (k = nz - 2; k >= 1; k--) {
+            vd_aux(a, c, k - 1, mol, aob, anb);
+            vkm1 = var[c + (k - 1) * P];
+            double a3 = -ana;
+            a1 = -anb;
+            a2 = a.hn[c + k * P] + ana + anb;
+            a4 = vk * a.ho[c + k * P] + (vkp1 - vk) * aoa + (vkm1 - vk) * aob;
+            if (ea2) a2 = a2 - ea2[c + k * P];
+            if (ea4) a4 = a4 + ea4[c + k * P];
+            double den = a2 - a3 * rk;
+            rk = a1 / den;
+            qk = (a4 - a3 * qk) / den;
+            ru[k * nthreads + tid] = rk;
+            qu[k * nthreads + tid] = qk;
+            aoa = aob; ana = anb;
+            vkp1 = vk; vk = vkm1;
+        }
+        // bottom layer, diffusion.F90:260-267 and :291-292
+        {
+            double a3 = -ana;
+            a2 = a.hn[c] + ana;
+            a4 = vk * a.ho[c] + (vkp1 - vk) * aoa;
+            if (ea2) a2 = a2 - ea2[c];
+            if (ea4) a4 = a4 + ea4[c];
+            double q0 = (a4 - a3 * qk) / (a2 - a3 * rk);
+            // back substitution :304-307
+            double vprev = q0;
+            var[c] = q0;
+            for (k = 1; k < nz; k++) {
+                vprev = qu[k * nthreads + tid] - ru[k * nthreads + tid] * vprev;
+                var[c + k * P] = vprev;
+            }
+        }
+    }
+}
+
+// prepare as a separate call (diffusion.F90:163-171): auxo/auxn at every
+// point of the halo-inclusive extent, Fortran levels kmin..kmax-1.
+__global__ void vd_prepare_kernel(int nx_, int ny_, int nz, long long plane, double molecular,
+                                  const double* nuh, double dt, double cnpar, const double* dzo,
+                                  const double* dzn, double* auxo, double* auxn)
+{
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n = plane * (nz - 1);
+    if (p >= n) return;
+    int k = (int)(p / plane);
+    long long c = p - (long long)k * plane;
+    double x = 2.0 * dt * (nuh[c + (k + 1) * plane] + molecular);
+    auxo[p] = (1.0 - cnpar) * x / (dzo[c + (k + 1) * plane] + dzo[c + k * plane]);
+    auxn[p] = cnpar * x / (dzn[c + (k + 1) * plane] + dzn[c + k * plane]);
+}
+
+static int vd_launch(VDArgs& a, cudaStream_t stream)
+{
+    int threads = 128;
+    while (threads > 32 && (size_t)2 * a.nz * threads * sizeof(double) > 160 * 1024) threads /= 2;
+    size_t smem = (size_t)2 * a.nz * threads * sizeof(double);
+    if (smem > 200 * 1024) return GETM_ERR_NZ;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(vd_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    dim3 grid(getm_div_up(a.nx_, threads), a.ny_);
+    vd_column_kernel<<<grid, threads, smem, stream>>>(a);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_vertical_diffusion_create(getm_grid* tgrid, getm_vertical_diffusion** out)
+{
+    if (!out) return GETM_ERR_ARG;
+    getm_vertical_diffusion* d = (getm_vertical_diffusion*)calloc(1, sizeof(*d));
+    if (!d) return GETM_ERR_ALLOC;
+    d->tgrid = tgrid;
+    *out = d;
+    return GETM_OK;
+}
+
+extern "C" int getm_vertical_diffusion_finalize(getm_vertical_diffusion* d)
+{
+    if (!d) return GETM_OK;
+    cudaFree(d->auxo);
+    cudaFree(d->auxn);
+    free(d);
+    return GETM_OK;
+}
+
+extern "C" int getm_vertical_diffusion_prepare(getm_vertical_diffusion* d, int nx, int ny, int nz,
+                                               double molecular, const double* nuh,
+                                               double timestep, double cnpar, const int* mask,
+                                               const double* ho, const double* hn,
+                                               cudaStream_t stream)
+{
+    (void)mask;
+    if (!d || nx < 1 || ny < 1 || nz < 1 || !nuh || !ho || !hn) return GETM_ERR_ARG;
+    if (nz > GETM_MAX_NZ) return GETM_ERR_NZ;
+    if (nz == 1) return GETM_OK;  // diffusion.F90:155
+    const long long plane = (long long)nx * ny;
+    const size_t n3 = (size_t)plane * nz;
+    if (n3 > d->n3) {
+        cudaFree(d->auxo); cudaFree(d->auxn);
+        d->auxo = d->auxn = NULL;
+        if (cudaMalloc(&d->auxo, n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
+        if (cudaMalloc(&d->auxn, n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
+        d->n3 = n3;
+    }
+    long long n = plane * (nz - 1);
+    vd_prepare_kernel<<<getm_div_up(n, 256), 256, 0, stream>>>(nx, ny, nz, plane, molecular, nuh, timestep, cnpar, ho, hn, d->auxo, d->auxn);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_vertical_diffusion_apply(getm_vertical_diffusion* d, int nx, int ny, int nz,
+                                             const int* mask, const double* ho, const double* hn,
+                                             double* var, const double* ea2, const double* ea4,
+                                             cudaStream_t stream)
+{
+    if (!d || nx < 1 || ny < 1 || nz < 1 || !mask || !ho || !hn || !var) return GETM_ERR_ARG;
+    if (nz > GETM_MAX_NZ) return GETM_ERR_NZ;
+    if (nz > 1 && (!d->auxo || d->n3 < (size_t)nx * ny * nz)) return GETM_ERR_ARG;  // not prepared
+    VDArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nx_ = nx; a.ny_ = ny; a.nz = nz; a.plane = (long long)nx * ny;
+    a.mask = mask; a.ho = ho; a.hn = hn; a.auxo = d->auxo; a.auxn = d->auxn;
+    a.ntracer = 1; a.var[0] = var; a.ea2[0] = ea2; a.ea4[0] = ea4;
+    return vd_launch(a, stream);
+}
+
+extern "C" int getm_vertical_diffusion_batch(int nx, int ny, int nz, const int* mask,
+                                             const double* nuh, double timestep, double cnpar,
+                                             const double* ho, const double* hn, int ntracer,
+                                             const double* molecular, double* const* vars,
+                                             const double* const* ea2, const double* const* ea4,
+                                             cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || !mask || !nuh || !ho || !hn || ntracer < 1 || !vars || !molecular)
+        return GETM_ERR_ARG;
+    if (nz > GETM_MAX_NZ) return GETM_ERR_NZ;
+    VDArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nx_ = nx; a.ny_ = ny; a.nz = nz; a.plane = (long long)nx * ny;
+    a.mask = mask; a.nuh = nuh; a.ho = ho; a.hn = hn; a.dt = timestep; a.cnpar = cnpar;
+    int done = 0;
+    do {
+        int n = ntracer - done;
+        if (n > VD_MAX_BATCH) n = VD_MAX_BATCH;
+        a.ntracer = n;
+        for (int t = 0; t < n; t++) {
+            a.molecular[t] = molecular[done + t];
+            a.var[t] = vars[done + t];
+            a.ea2[t] = ea2 ? ea2[done + t] : NULL;
+            a.ea4[t] = ea4 ? ea4[done + t] : NULL;
+        }
+        int rc = vd_launch(a, stream);
+        if (rc) return rc;
+        done += n;
+    } while (done < ntracer);
+    return GETM_OK;
+}

@@ -1,0 +1,189 @@
+"""Seeded synthetic workloads (host-side set-up, numpy).
+
+There is no public dataset for this path: the workloads are generated from a
+seed with the shapes, sizes and value distributions of the benchmark
+configurations:
+
+* ``tracer_transport`` - plain FP64 tracer transport on a 120 x 100 x 30 sigma
+  grid, dx = dy = 1 km, Gaussian-smoothed random bathymetry 10-60 m with cells
+  shallower than 12 m masked as land, solid-body rotation (max 0.5 m/s),
+  w from continuity, a 3D Gaussian tracer blob, parabolic diffusivity
+  1e-4..1e-2 m2/s; superbee, dt = 30 s.
+* ``seamount`` - the baroclinic split-explicit box: 400 x 300 x 40 sigma,
+  dx = 2 km, 4500 m deep with a 4000 m high, 25 km radius Gaussian seamount,
+  T 20 -> 4 degC linear in depth, S = 35, f = 1e-4, 3D dt = 120 s with 30
+  substeps.
+
+Each returns a ``Workload`` with the host grid tree and initial fields as
+numpy arrays (pygetm layout, halos included); the GPU path and the oracle are
+both started from these same arrays.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+from typing import Dict, Optional
+
+import numpy as np
+from scipy.ndimage import gaussian_filter
+
+from .domain import FILL_VALUE, HostGrid, calculate_sigma, create_cartesian
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    T: HostGrid
+    dga: np.ndarray
+    fields: Dict[str, np.ndarray]
+    params: Dict[str, float]
+
+    @property
+    def cells(self) -> int:
+        """Interior T cells, land included (the cell-update unit)."""
+        return self.T.nx * self.T.ny * self.T.nz
+
+    @property
+    def wet_cells(self) -> int:
+        return int((self.T.mask[self.T.interior[1:]] != 0).sum()) * self.T.nz
+
+
+def _norm01(a):
+    return (a - a.min()) / (a.max() - a.min())
+
+
+def sigma_thicknesses(g: HostGrid, dga: np.ndarray, D: np.ndarray) -> np.ndarray:
+    """Sigma.__call__ (python/pygetm/vertical_coordinates.py:106-113):
+    hn = dga * D where mask != 0, FILL_VALUE elsewhere."""
+    hn = np.full((dga.size,) + D.shape, FILL_VALUE)
+    water = g.mask != 0
+    hn[:, water] = dga[:, None] * D[water][None, :]
+    return hn
+
+
+def vertical_coordinates(g: HostGrid, hn: np.ndarray):
+    """thickness2vertical_coordinates (python/src/wrapper.F90:409-426) in numpy,
+    for set-up only (zc, zf start at -H as in python/pygetm/core.py:356-362)."""
+    nz = hn.shape[0]
+    zc = np.broadcast_to(-g.H_unmasked, hn.shape).copy()
+    zf = np.broadcast_to(-g.H_unmasked, (nz + 1,) + hn.shape[1:]).copy()
+    water = g.mask != 0
+    H = g.H
+    zf[0, water] = -H[water]
+    for k in range(nz):
+        zf[k + 1, water] = zf[k, water] + hn[k, water]
+    zc[0, water] = -H[water] + 0.5 * hn[0, water]
+    for k in range(1, nz):
+        zc[k, water] = zc[k - 1, water] + 0.5 * (hn[k - 1, water] + hn[k, water])
+    return zc, zf
+
+
+def continuity_w(T: HostGrid, pk: np.ndarray, qk: np.ndarray) -> np.ndarray:
+    """w from discrete continuity with ho == hn: the recursion of
+    c_w_momentum_3d (python/src/momentum.F90:191-216) over the range pygetm
+    passes (python/_pygetm.pyx:454), in numpy."""
+    nz = pk.shape[0]
+    w = np.zeros((nz + 1, T.ny_, T.nx_))
+    dyu, dxv = T.ugrid.dy, T.vgrid.dx
+    j0, j1 = T.haloy, T.haloy + T.ny + 1
+    i0, i1 = T.halox, T.halox + T.nx + 1
+    sl = (slice(j0, j1), slice(i0, i1))
+    slw = (slice(j0, j1), slice(i0 - 1, i1 - 1))
+    sls = (slice(j0 - 1, j1 - 1), slice(i0, i1))
+    wet = T.mask[sl] == 1
+    for k in range(1, nz):
+        div = (pk[k - 1][sl] * dyu[sl] - pk[k - 1][slw] * dyu[slw] + qk[k - 1][sl] * dxv[sl] - qk[k - 1][sls] * dxv[sls]) * T.iarea[sl]
+        wk = w[k - 1][sl] - div
+        w[k][sl] = np.where(wet, wk, w[k][sl])
+    return w
+
+
+def _bathymetry(rng, nx, ny, Hmin, Hmax, Hland, land_fraction, sigma=8.0):
+    """Gaussian-smoothed noise scaled to [Hmin, Hmax]; a power law on the
+    normalised field puts the requested fraction of cells below Hland."""
+    q = _norm01(gaussian_filter(rng.standard_normal((ny, nx)), sigma=sigma))
+    qland = (Hland - Hmin) / (Hmax - Hmin)
+    qf = np.quantile(q, land_fraction)
+    p = np.log(qland) / np.log(qf)
+    return Hmin + (Hmax - Hmin) * q**p
+
+
+def rotating_transport(T: HostGrid, omega: float, D0: float, Htaper: float, Hland: float):
+    """Depth-integrated transport in solid-body rotation about the domain
+    centre, from a streamfunction psi on X points:
+    psi = -omega/2 r^2 D0 phi(H_X) * xmask, phi = min(1, ((H_X-Hland)/Htaper)^2)
+    for H_X > Hland else 0.  U = -(psi_N - psi_S)/dy, V = (psi_E - psi_W)/dx is
+    discretely non-divergent, with zero transport through every masked face."""
+    X = T.xgrid
+    xc = 0.5 * (T.x[T.interior[1:]].min() + T.x[T.interior[1:]].max())
+    yc = 0.5 * (T.y[T.interior[1:]].min() + T.y[T.interior[1:]].max())
+    with np.errstate(invalid="ignore"):
+        HX = X.H_unmasked
+        phi = np.clip((HX - Hland) / Htaper, 0.0, None) ** 2
+        phi = np.minimum(phi, 1.0)
+        r2 = (X.x - xc) ** 2 + (X.y - yc) ** 2
+        psi = np.where(X.mask != 0, -0.5 * omega * r2 * D0 * phi, 0.0)
+    psi = np.nan_to_num(psi)
+    U = np.zeros((T.ny_, T.nx_))
+    V = np.zeros((T.ny_, T.nx_))
+    # U(i, j) lies between corners X(i+1, j) [south] and X(i+1, j+1) [north];
+    # V(i, j) between X(i, j+1) [west] and X(i+1, j+1) [east] (X = T shifted
+    # by one corner: X local i is the south-west corner of T local i).
+    U[:, :] = -(psi[1:, 1:] - psi[:-1, 1:]) / T.ugrid.dy
+    V[:, :] = (psi[1:, 1:] - psi[1:, :-1]) / T.vgrid.dx
+    U[T.ugrid.mask == 0] = 0.0
+    V[T.vgrid.mask == 0] = 0.0
+    return U, V
+
+
+def tracer_transport(nx: int = 120, ny: int = 100, nz: int = 30, seed: int = 1, dt: float = 30.0) -> Workload:
+    """Plain FP64 tracer-transport workload (120 x 100 x 30 by default)."""
+    rng = np.random.default_rng(seed)
+    dx = 1000.0
+    x = dx * (np.arange(nx) + 0.5)
+    y = dx * (np.arange(ny) + 0.5)
+    H = _bathymetry(rng, nx, ny, 10.0, 60.0, 12.0, 0.15)
+    mask = (H >= 12.0).astype(int)
+    dom = create_cartesian(x, y, mask=mask, H=H, f=0.0)
+    T = dom.create_grids(nz, halox=2, haloy=2, velocity_grids=2)
+    dga = calculate_sigma(nz)
+    U, V = T.ugrid, T.vgrid
+    fields: Dict[str, np.ndarray] = {}
+    for g, n in ((T, "T"), (U, "U"), (V, "V"), (T.xgrid, "X")):
+        D = np.where(g.mask != 0, g.H, FILL_VALUE)
+        fields[f"D_{n}"] = D
+        fields[f"hn_{n}"] = sigma_thicknesses(g, dga, D)
+    uwet = U.mask != 0
+    vwet = V.mask != 0
+    Ut, Vt = rotating_transport(T, 1.0, 30.0, 10.0, 12.0)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        u2 = np.where(uwet, Ut / fields["D_U"], 0.0)
+        v2 = np.where(vwet, Vt / fields["D_V"], 0.0)
+    scale = 0.5 / max(np.abs(u2).max(), np.abs(v2).max())
+    u2 *= scale
+    v2 *= scale
+    uk = np.broadcast_to(u2, (nz,) + u2.shape).copy()
+    vk = np.broadcast_to(v2, (nz,) + v2.shape).copy()
+    pk = uk * np.where(uwet, fields["hn_U"], 0.0)
+    qk = vk * np.where(vwet, fields["hn_V"], 0.0)
+    w = continuity_w(T, pk, qk)
+    zc, zf = vertical_coordinates(T, fields["hn_T"])
+    D = fields["D_T"]
+    xc = 0.5 * (x[0] + x[-1])
+    yc = 0.5 * (y[0] + y[-1])
+    x0, y0 = xc + 25000.0, yc
+    L = 10000.0
+    with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+        c = np.exp(-((T.x - x0) ** 2 + (T.y - y0) ** 2)[None] / L**2 - ((zc + 0.5 * D[None]) / (0.25 * D[None])) ** 2)
+    c = np.where(T.mask[None] != 0, c, FILL_VALUE)
+    # parabolic diffusivity at interfaces, s = height fraction above the bottom
+    s = np.linspace(0.0, 1.0, nz + 1)[:, None, None]
+    nuh = np.broadcast_to(1e-4 + (1e-2 - 1e-4) * 4 * s * (1 - s), (nz + 1, T.ny_, T.nx_)).copy()
+    nuh[:, T.mask == 0] = FILL_VALUE
+    fields.update(uk=uk, vk=vk, w=w, tracer=c, nuh=nuh, zc_T=zc, zf_T=zf)
+    return Workload("tracer_transport", T, dga, fields, dict(dt=dt, umax=0.5, scheme=5, cnpar=1.0))
+
+
+def land_fraction(wl: Workload) -> float:
+    m = wl.T.mask[wl.T.interior[1:]]
+    return float((m == 0).mean())

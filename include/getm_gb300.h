@@ -1,0 +1,244 @@
+/*
+ * getm_gb300: C ABI of the GB300 (sm_103a) implementation of pygetm's
+ * split-explicit time-step operators.
+ *
+ * Every entry point mirrors one bind(c) routine of the reference Fortran
+ * library (declared to Cython at python/_pygetm.pyx:24-66) with the same
+ * argument list and meaning, and adds:
+ *   - all array arguments are DEVICE pointers (C layout [k][j][i], i fastest,
+ *     halos included, exactly as pygetm passes them);
+ *   - a trailing cudaStream_t on which the work is enqueued (stream-ordered,
+ *     no host synchronisation);
+ *   - an int status return (GETM_OK = 0) instead of a void return; the
+ *     reference aborts or silently returns where these return an error code.
+ * Functions named *_f32 are the mixed-precision form: bulk fields in float,
+ * layer thicknesses and elevations in double.
+ * Index bounds (imin..jmax) are the reference's Fortran 1-based ones.
+ */
+#ifndef GETM_GB300_H
+#define GETM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef __CUDA_RUNTIME_H__
+typedef struct CUstream_st* cudaStream_t;
+#endif
+
+/* status codes */
+#define GETM_OK 0
+#define GETM_ERR_ARG 1          /* null pointer, bad extent or unknown name */
+#define GETM_ERR_CUDA 2         /* a CUDA launch/runtime call failed */
+#define GETM_ERR_ITERS 3        /* vertical advection hit itersmax (200) sub-steps */
+#define GETM_ERR_NZ 4           /* more layers than a column kernel supports */
+#define GETM_ERR_ALLOC 5        /* device work-buffer allocation failed */
+
+/* advection schemes: src/operators/advection.F90:22-30 */
+#define GETM_SCHEME_HSIMT 1
+#define GETM_SCHEME_MUSCL 2
+#define GETM_SCHEME_P2_PDM 3
+#define GETM_SCHEME_SPLMAX13 4
+#define GETM_SCHEME_SUPERBEE 5
+#define GETM_SCHEME_UPSTREAM 6
+
+/* largest number of layers the column kernels (vertical advection and
+ * diffusion) accept */
+#define GETM_MAX_NZ 256
+
+typedef struct getm_grid getm_grid;
+typedef struct getm_advection getm_advection;
+typedef struct getm_vertical_diffusion getm_vertical_diffusion;
+
+/* ---- grids --------------------------------------------------------------
+ * create_grid: python/src/wrapper.F90:48-59 (pyx:26)
+ * grid_finalize: wrapper.F90:61-68 (pyx:27)
+ * getm_grid_set_array replaces get_array (wrapper.F90:70-125, pyx:34): the
+ * reference grid owns its metric arrays and hands out pointers to them; here
+ * the caller owns the device storage and registers it by the same names
+ * ("mask", "dx", "dy", "idx", "idy", "iarea", "area").                        */
+int getm_create_grid(int imin, int imax, int jmin, int jmax, int kmin, int kmax, int halox,
+                     int haloy, getm_grid** grid);
+int getm_grid_finalize(getm_grid* grid);
+int getm_grid_set_array(getm_grid* grid, const char* name, void* device_ptr);
+
+/* ---- advection ----------------------------------------------------------
+ * advection_create/finalize: wrapper.F90:188-211 (pyx:35-36)
+ * advection_uv_calculate: wrapper.F90:213-254 (pyx:37); direction 1 = x
+ *   (ugrid mask/idx/dy), 2 = y (vgrid mask/dx/idy); Ah == NULL: no diffusion.
+ * advection_w_calculate: wrapper.F90:256-273 (pyx:38).                      */
+int getm_advection_create(int scheme, getm_grid* tgrid, getm_advection** adv);
+int getm_advection_finalize(getm_advection* adv);
+int getm_advection_uv_calculate(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
+                                getm_grid* ugrid, const double* u, const double* Ah,
+                                double timestep, double* h, const double* hu, double* var,
+                                cudaStream_t stream);
+int getm_advection_w_calculate(getm_advection* adv, getm_grid* tgrid, const double* w,
+                               const double* w_var, double timestep, double* h, double* var,
+                               cudaStream_t stream);
+/* Fused 3D Strang split of python/pygetm/operators.py:135-193
+ * (Advection.apply_3d_batch; apply_3d is ntracer == 1): adv1(dt/2),
+ * adv2(dt/2), w(dt), adv2(dt/2), adv1(dt/2) with adv1 = v unless ufirst, for
+ * ntracer tracers sharing one evolving layer thickness h (in/out).  w_var[t]
+ * may equal w.  ugrid/vgrid metrics come from the grid handles.              */
+int getm_advection_apply_3d_batch(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
+                                  getm_grid* vgrid, int ufirst, const double* u,
+                                  const double* v, const double* w, const double* const* w_var,
+                                  const double* Ah_u, const double* Ah_v, double timestep,
+                                  double* h, const double* hu, const double* hv, int ntracer,
+                                  double* const* vars, cudaStream_t stream);
+/* Fused 2D split of Advection.__call__ (operators.py:52-93): split 1 = FULL,
+ * 2 = HALF, 3 = HALF_ALWAYS; D (in/out) is the column-height work array.    */
+int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
+                      int ufirst, int split, const double* u, const double* v,
+                      const double* Ah_u, const double* Ah_v, double timestep, double* D,
+                      const double* DU, const double* DV, double* var, cudaStream_t stream);
+/* Status word of the last vertical advection on this handle's stream:
+ * GETM_ERR_ITERS if a column needed more than itersmax sub-steps.  Blocks
+ * until the handle's pending work on `stream` is done.                      */
+int getm_advection_get_status(getm_advection* adv, cudaStream_t stream);
+
+/* ---- vertical diffusion -------------------------------------------------
+ * vertical_diffusion_create/finalize: wrapper.F90:127-147 (pyx:39-40)
+ * c_vertical_diffusion_prepare: wrapper.F90:149-161 -> diffusion.F90:135-204
+ * c_vertical_diffusion_apply: wrapper.F90:163-186 -> diffusion.F90:206-314
+ * nuh has nz+1 interface levels; ea2/ea4 may be NULL.                       */
+int getm_vertical_diffusion_create(getm_grid* tgrid, getm_vertical_diffusion** diff);
+int getm_vertical_diffusion_finalize(getm_vertical_diffusion* diff);
+int getm_vertical_diffusion_prepare(getm_vertical_diffusion* diff, int nx, int ny, int nz,
+                                    double molecular, const double* nuh, double timestep,
+                                    double cnpar, const int* mask, const double* ho,
+                                    const double* hn, cudaStream_t stream);
+int getm_vertical_diffusion_apply(getm_vertical_diffusion* diff, int nx, int ny, int nz,
+                                  const int* mask, const double* ho, const double* hn,
+                                  double* var, const double* ea2, const double* ea4,
+                                  cudaStream_t stream);
+/* prepare + apply fused per column (VerticalDiffusion.__call__,
+ * operators.py:218-230) for ntracer fields, each with its own molecular
+ * diffusivity and optional ea2/ea4 (arrays of device pointers, entries may be
+ * NULL; the arrays themselves may be NULL).                                 */
+int getm_vertical_diffusion_batch(int nx, int ny, int nz, const int* mask, const double* nuh,
+                                  double timestep, double cnpar, const double* ho,
+                                  const double* hn, int ntracer, const double* molecular,
+                                  double* const* vars, const double* const* ea2,
+                                  const double* const* ea4, cudaStream_t stream);
+
+/* ---- python/src/interpolation.F90:9-72 (pyx:28-31) ---------------------- */
+int getm_grid_interp_x(int nx, int ny, int nz, const double* source, double* target, int ioffset,
+                       cudaStream_t stream);
+int getm_grid_interp_y(int nx, int ny, int nz, const double* source, double* target, int joffset,
+                       cudaStream_t stream);
+int getm_grid_interp_z(int nx, int ny, int nz1, int nz2, const double* source, double* target,
+                       int koffset, cudaStream_t stream);
+int getm_grid_interp_xy(int nx1, int ny1, int nx2, int ny2, int nz, const double* source,
+                        double* target, int ioffset, int joffset, cudaStream_t stream);
+
+/* ---- python/src/wrapper.F90 --------------------------------------------- */
+/* c_momentum_diffusion: wrapper.F90:275-393 (pyx:43) */
+int getm_momentum_diffusion(getm_grid* ugrid, getm_grid* vgrid, getm_grid* uugrid,
+                            getm_grid* uvgrid, getm_grid* vugrid, getm_grid* vvgrid, int nk,
+                            const double* huu, const double* huv, const double* hvu,
+                            const double* hvv, const double* u, const double* v, double Am0,
+                            double* diffu, double* diffv, cudaStream_t stream);
+/* c_thickness2center_depth: wrapper.F90:395-407 (pyx:46) */
+int getm_thickness2center_depth(int nx, int ny, int nz, int istart, int istop, int jstart,
+                                int jstop, const int* mask, const double* h, double* out,
+                                cudaStream_t stream);
+/* c_thickness2vertical_coordinates: wrapper.F90:409-426 (pyx:47) */
+int getm_thickness2vertical_coordinates(int nx, int ny, int nz, const int* mask,
+                                        const double* bottom_depth, const double* h, double* zc,
+                                        double* zf, cudaStream_t stream);
+/* c_alpha: wrapper.F90:428-435 (pyx:48) */
+int getm_alpha(int n, const double* D, double Dmin, double Dcrit, const int* mask, double* alpha,
+               cudaStream_t stream);
+/* c_elevation2depth: wrapper.F90:437-445 (pyx:49) */
+int getm_elevation2depth(int n, const double* z, const double* H, double Dmin, const int* mask,
+                         double* D, cudaStream_t stream);
+/* c_multiply_add: wrapper.F90:488-494 (pyx:60) */
+int getm_multiply_add(int n, double* tgt, const double* add, double scale_factor,
+                      cudaStream_t stream);
+/* c_advance_surface_elevation: wrapper.F90:496-523 (pyx:61) */
+int getm_advance_surface_elevation(int nx, int ny, int halox, int haloy, const int* mask,
+                                   const double* dyu, const double* dxv, const double* iarea,
+                                   double* z, const double* U, const double* V,
+                                   const double* fwf, double dt, cudaStream_t stream);
+/* c_surface_pressure_gradient: wrapper.F90:525-565 (pyx:62) */
+int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax, int jmin, int jmax,
+                                   const int* umask, const int* vmask, const double* idxu,
+                                   const double* idyv, const double* z, const double* sp,
+                                   const double* H, const double* D, double Dmin, double* dpdx,
+                                   double* dpdy, cudaStream_t stream);
+
+/* ---- python/src/momentum.F90 --------------------------------------------- */
+/* c_horizontal_diffusion: momentum.F90:12-77 (pyx:50) */
+int getm_horizontal_diffusion(int imin, int imax, int jmin, int jmax, int halox, int haloy,
+                              const int* umask, const int* vmask, const double* idxu,
+                              const double* dyu, const double* idyv, const double* dxv,
+                              const double* Ah_u, const double* Ah_v, const int* tmask,
+                              const double* iA, double dt, const double* f, double* out,
+                              cudaStream_t stream);
+/* c_bottom_friction: momentum.F90:79-101 (pyx:51) */
+int getm_bottom_friction(int nx, int ny, const int* mask, const double* u, const double* v,
+                         const double* D, double* z0b, const double* z0b_in, double avmmol,
+                         double* ru, int iterate, cudaStream_t stream);
+/* c_collect_3d_momentum_sources: momentum.F90:103-145 (pyx:52) */
+int getm_collect_3d_momentum_sources(int nx, int ny, int nz, int halox, int haloy,
+                                     const int* mask, const double* alpha, const double* ho,
+                                     const double* hn, const double* dp, const double* cor,
+                                     const double* adv, const double* diff, const double* idp,
+                                     const double* taus, const double* rr, double dt,
+                                     double* ea2, double* ea4, cudaStream_t stream);
+/* c_advance_2d_transport: momentum.F90:147-189 (pyx:53) */
+int getm_advance_2d_transport(int nx, int ny, int halox, int haloy, const int* mask,
+                              const double* alpha, const double* D, const double* dp,
+                              const double* taus, const double* cor, const double* adv,
+                              const double* diff, const double* damp, const double* SA,
+                              const double* SB, const double* SD, const double* SF,
+                              const double* r, double dt, double* U, cudaStream_t stream);
+/* c_w_momentum_3d: momentum.F90:191-216 (pyx:54) */
+int getm_w_momentum_3d(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                       const int* mask, const double* dyu, const double* dxv,
+                       const double* iarea, const double* ho, const double* hn,
+                       const double* pk, const double* qk, double dt, double* w,
+                       cudaStream_t stream);
+/* c_shear_frequency: momentum.F90:218-241 (pyx:55) */
+int getm_shear_frequency(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                         const int* mask, const double* hu, const double* hv, const double* uk,
+                         const double* vk, double* SS, cudaStream_t stream);
+/* c_surface_shear_velocity: momentum.F90:270-284 (pyx:57) */
+int getm_surface_shear_velocity(int nx, int ny, int imin, int imax, int jmin, int jmax,
+                                const int* mask, const double* tausx, const double* tausy,
+                                double* ustar2_s, cudaStream_t stream);
+/* c_bottom_shear_velocity: momentum.F90:286-321 (pyx:58) */
+int getm_bottom_shear_velocity(int nx, int ny, int imin, int imax, int jmin, int jmax,
+                               const int* mask, const int* umask, const int* vmask,
+                               const double* uk_bot, const double* vk_bot, const double* rru,
+                               const double* rrv, double* taubx, double* tauby,
+                               double* ustar2_b, cudaStream_t stream);
+/* c_reconstruct_transport_change: momentum.F90:323-340 (pyx:59) */
+int getm_reconstruct_transport_change(int nx, int ny, int nz, int imin, int imax, int jmin,
+                                      int jmax, double* un, const double* hn, const double* Uo,
+                                      double timestep, cudaStream_t stream);
+
+/* ---- python/src/internal_pressure.F90 ----------------------------------- */
+/* c_blumberg_mellor: internal_pressure.F90:9-60 (pyx:63) */
+int getm_blumberg_mellor(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                         const int* umask, const int* vmask, const double* idxu,
+                         const double* idyv, const double* hu, const double* hv,
+                         const double* zf, const double* buoy, double* idpdx, double* idpdy,
+                         cudaStream_t stream);
+/* c_shchepetkin_mcwilliams: internal_pressure.F90:63-217 (pyx:64).
+ * P_work: caller-provided device scratch of nx*ny*nz doubles (the
+ * reference allocates dR, dZ, P per call).                                  */
+int getm_shchepetkin_mcwilliams(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                const int* mask, const int* umask, const int* vmask,
+                                const double* idxu, const double* idyv, const double* h,
+                                const double* z, const double* zc, const double* buoy,
+                                double* idpdx, double* idpdy, double* P_work,
+                                cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GETM_GB300_H */

@@ -1,0 +1,318 @@
+"""Benchmark: 3D cell-updates/s of the split-explicit baroclinic step.
+
+Workload: the seamount box of 400 x 300 x 40 sigma layers (dx = 2 km, 4500 m
+deep, 4000 m Gaussian seamount, linear stratification, nonlinear EOS,
+Shchepetkin-McWilliams internal pressure, dt2d = 4 s, 30 substeps per 3D step,
+f = 1e-4, log-law bottom drag).  One step = one 3D (macro) time step with its
+30 2D substeps and both active tracers.  Unit of work: one cell-update = one
+interior T cell (land included) advanced by one 3D step.
+
+Our arm (default): FP64 GPU path, state resident in HBM, the two-macro-step
+sequence replayed from a CUDA graph, timed with CUDA events.  ``e2e`` repeats
+the timing through the public API with the per-step surface forcing copied
+host->device from pinned memory and the surface elevation copied back.
+``--impl reference``: the reference's CPU algorithm (the C/numpy oracle
+restatement, OpenMP over all host cores) on a bounded sample of the same
+workload.  Multi-GPU: independent replicas (one domain per GPU, no
+collective); the value is the sum over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nx", type=int, default=400)
+    ap.add_argument("--ny", type=int, default=300)
+    ap.add_argument("--nz", type=int, default=40)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_reference(args, nmacro: int, threads: int):
+    """Time the oracle restatement of the reference's CPU path."""
+    import numpy as np
+
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    os.environ.setdefault("GETM_ORACLE_VARIANT", "omp" if threads > 1 else "serial")
+    from getm_gb300 import workloads
+    from oracle import models
+
+    wl = workloads.seamount(nx=args.nx, ny=args.ny, nz=args.nz)
+    p = wl.params
+    s = models.Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"])
+    s.temp[...] = np.where(s.T.mask[None] != 0, workloads.seamount_temperature(s.T.zc), s.temp)
+    s.start(p["timestep"], p["split_factor"])
+    t0 = time.perf_counter()
+    for _ in range(nmacro * p["split_factor"]):
+        s.advance()
+    dt = time.perf_counter() - t0
+    return wl.cells * nmacro / dt, dt
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 3))
+    for _ in range(min(args.warmup, 1)):
+        pass
+    value, dt = cpu_reference(args, steps, threads)
+    cfg = {"workload": f"seamount {args.nx}x{args.ny}x{args.nz}, 30 substeps per 3D step, FP64",
+           "sample": f"{steps} 3D steps"}
+    line = {"metric": "3D cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": 0, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                             "sample": f"{steps} 3D steps of the full workload"},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from getm_gb300 import _lib, workloads
+    from getm_gb300.simulation import Simulation
+
+    wl = workloads.seamount(nx=args.nx, ny=args.ny, nz=args.nz)
+    p = wl.params
+    split = p["split_factor"]
+    sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], device=f"cuda:{local}")
+    zc = sim.T.zc.all_values
+    sim.temp.all_values.copy_(torch.where(sim.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
+                                          sim.temp.all_values))
+    sim.start(p["timestep"], split)
+    period = 2  # the 3D momentum update alternates u/v order every 3D step
+    for _ in range(max(args.warmup, 3) * split):
+        sim.advance()
+    torch.cuda.synchronize()
+    nsteps = args.steps + (args.steps % period)
+    graph = None
+    if not args.no_graph:
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        n0 = _lib.launch_count()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            with torch.cuda.graph(graph, stream=stream):
+                for _ in range(period * split):
+                    sim.advance()
+        torch.cuda.current_stream().wait_stream(stream)
+        launches_per_period = _lib.launch_count() - n0
+        for _ in range(2):
+            graph.replay()
+        torch.cuda.synchronize()
+    else:
+        n0 = _lib.launch_count()
+        for _ in range(period * split):
+            sim.advance()
+        launches_per_period = _lib.launch_count() - n0
+
+    def run_period():
+        if graph is not None:
+            graph.replay()
+        else:
+            for _ in range(period * split):
+                sim.advance()
+
+    # device-timed region
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        start.record()
+        for _ in range(nsteps // period):
+            run_period()
+        end.record()
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    cells = wl.cells
+    value = cells * nsteps * ws / (ms / 1000.0)
+
+    # end to end through the public API: per 3D step, upload the surface
+    # forcing (taux, tauy, sp) from pinned host memory and read back z
+    forcing = [sim.airsea.taux, sim.airsea.tauy, sim.airsea.sp]
+    host_in = [f.all_values.detach().cpu().pin_memory() for f in forcing]
+    host_out = torch.empty_like(sim.T.z.all_values, device="cpu").pin_memory()
+    h2d = sum(h.numel() * h.element_size() for h in host_in)
+    d2h = host_out.numel() * host_out.element_size()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(nsteps // period):
+        for _ in range(period):
+            for f, h in zip(forcing, host_in):
+                f.all_values.copy_(h, non_blocking=True)
+        run_period()
+        host_out.copy_(sim.T.z.all_values, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": cells * nsteps * ws / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h // period}
+
+    # roofline of the dominant kernel: the fused tracer vertical diffusion
+    # (vd_column_kernel), timed alone on the live state
+    peak, peak_kind = _peaks()
+    tr = sim.tracers
+    reps = 20
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tr._diffuse(sim.macrotimestep, sim.nuh)
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(reps):
+        tr._diffuse(sim.macrotimestep, sim.nuh)
+    ev1.record()
+    torch.cuda.synchronize()
+    t_kernel = ev0.elapsed_time(ev1) / reps / 1000.0
+    ncol = (wl.T.nx * wl.T.ny)
+    nz = wl.T.nz
+    ntr = len(tr)
+    # algorithmic bytes: nuh (nz+1 levels), ho, hn read once; each tracer read+written
+    alg_bytes = 8 * (ncol * (nz + 1) + 2 * ncol * nz + ntr * 2 * ncol * nz)
+    achieved = alg_bytes / t_kernel / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "vd_column_kernel (2 tracers)", "peak_kind": peak_kind}
+
+    line = {"metric": "3D cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws,
+            "steps": nsteps, "warmup": max(args.warmup, 3), "ms_per_step": ms / nsteps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"seamount {wl.T.nx}x{wl.T.ny}x{wl.T.nz} baroclinic split-explicit, "
+                                   f"{split} substeps per 3D step, FP64",
+                       "cells": cells, "wet_cells": wl.wet_cells, "cuda_graph": graph is not None,
+                       "l2": "working set (> 1 GB of 3D fields) exceeds L2; no flush needed",
+                       "parallelism": f"replicas x{ws}"},
+            "e2e": e2e, "roofline": roofline, "gpu_launches": launches_per_period * (nsteps // period),
+            "clocks": clocks.summary()}
+    if rank == 0 and not args.no_cpu_baseline and ws == 1:
+        threads = os.cpu_count() or 1
+        v, dt = cpu_reference(args, 2, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                                "sample": f"2 3D steps of the full workload ({dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

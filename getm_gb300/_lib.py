@@ -72,6 +72,8 @@ _SIGS = {
     "getm_reconstruct_transport_change": "iiiiiiipppds",
     "getm_blumberg_mellor": "iiiiiiipppppppppps",
     "getm_shchepetkin_mcwilliams": "iiiiiiipppppppppppps",
+    "getm_density_buoyancy": "ippppps",
+    "getm_launch_count": "p",
 }
 _CT = {"i": c_int, "d": c_double, "p": c_void_p, "s": c_void_p, "c": ctypes.c_char_p}
 
@@ -108,6 +110,13 @@ def ptr_array(ptrs):
     """Host array of device pointers (for the batched entry points)."""
     arr = (c_void_p * len(ptrs))(*[p if p is not None else None for p in ptrs])
     return arr
+
+
+def launch_count() -> int:
+    """Kernel launches issued by libgetm_gb300 so far in this process."""
+    n = ctypes.c_ulonglong(0)
+    call("getm_launch_count", ctypes.byref(n))
+    return int(n.value)
 
 
 def stream_handle(stream=None) -> int:

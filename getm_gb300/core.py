@@ -194,8 +194,10 @@ class Grid:
         nlev = {False: None, None: None, CENTERS: self.nz, INTERFACES: self.nz + 1}[z]
         shape = (self.ny_, self.nx_) if nlev is None else (nlev, self.ny_, self.nx_)
         a = Array(self, torch.empty(shape, dtype=dtype, device=self.device), z=z, fill_value=fill_value, name=name)
+        # Array.create (python/pygetm/core.py:853-900): an explicit fill is
+        # written everywhere (land included); otherwise the fill value is.
         if fill is not None:
-            a.fill(fill)
+            a.all_values.fill_(fill)
         else:
             a.all_values.fill_(fill_value if fill_value is not None else 0)
         return a

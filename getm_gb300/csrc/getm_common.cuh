@@ -27,8 +27,13 @@ struct getm_grid {
     const double* area;
 };
 
+// Host-side count of kernel launches issued by this library (one increment
+// per launch site executed); read with getm_launch_count().
+extern "C" unsigned long long getm_launch_counter_add(void);
+
 #define GETM_CHECK_LAUNCH()                                     \
     do {                                                        \
+        getm_launch_counter_add();                              \
         cudaError_t e_ = cudaGetLastError();                    \
         if (e_ != cudaSuccess) return GETM_ERR_CUDA;            \
     } while (0)

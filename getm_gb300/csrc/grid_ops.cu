@@ -9,6 +9,19 @@
 
 #define EW_THREADS 256
 
+#include <atomic>
+
+static std::atomic<unsigned long long> g_launches{0};
+
+extern "C" unsigned long long getm_launch_counter_add(void) { return ++g_launches; }
+
+extern "C" int getm_launch_count(unsigned long long* count)
+{
+    if (!count) return GETM_ERR_ARG;
+    *count = g_launches.load();
+    return GETM_OK;
+}
+
 // ---------------------------------------------------------------------------
 // interpolation.F90:9-72
 // ---------------------------------------------------------------------------

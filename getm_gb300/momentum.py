@@ -1,0 +1,301 @@
+"""2D and 3D momentum on the GPU: counterpart of pygetm.momentum.Momentum
+(python/pygetm/momentum.py:24-1214) for closed domains.
+
+Field names, the order of operations and the Coriolis/advection/friction
+coupling follow the reference; every kernel is a libgetm_gb300 launch (via
+``_pygetm``/``operators``) or a torch elementwise op on device tensors.
+"""
+
+from __future__ import annotations
+
+import enum
+from typing import Optional
+
+import torch
+
+from . import _pygetm
+from .core import CENTERS, INTERFACES, Array, Grid
+from .domain import FILL_VALUE
+from .operators import Advection, AdvectionScheme, AdvectionSplit, VerticalDiffusion
+
+
+class CoriolisScheme(enum.IntEnum):
+    """python/pygetm/momentum.py:14-17"""
+
+    OFF = 0
+    DEFAULT = 1
+    ESPELID = 2
+
+
+MASK_ZERO_2D = ("U", "V", "u1", "v1")  # momentum.py:20
+MASK_ZERO_3D = ("pk", "qk", "uk", "vk", "Ui", "Vi", "rru", "rrv")  # momentum.py:21
+
+
+class Momentum:
+    def __init__(self, Am: float = 0.0, An: float = 0.0, cnpar: float = 1.0,
+                 advection_scheme: Optional[AdvectionScheme] = None,
+                 advection_split_2d: AdvectionSplit = AdvectionSplit.FULL,
+                 coriolis_scheme: CoriolisScheme = CoriolisScheme.DEFAULT, avmmol: float = 1.8e-6):
+        """momentum.py:113-144"""
+        self._Am_const = Am
+        self._An_const = An
+        self.cnpar = cnpar
+        self.advection_scheme = advection_scheme
+        self.advection_split_2d = advection_split_2d
+        self.coriolis_scheme = coriolis_scheme
+        self.avmmol = avmmol
+
+    # ------------------------------------------------------------------ setup
+    def _create_arrays(self, tgrid: Grid, three_d: bool):
+        """momentum.py:146-487 (fill values as in the reference)."""
+        ug, vg = tgrid.ugrid, tgrid.vgrid
+        for n in ("U", "u1", "SxA", "SxB", "SxD", "SxF", "corU", "advU", "diffU", "dampU", "ru"):
+            setattr(self, n, ug.array(name=n))
+        for n in ("V", "v1", "SyA", "SyB", "SyD", "SyF", "corV", "advV", "diffV", "dampV", "rv"):
+            setattr(self, n, vg.array(name=n))
+        nan = float("nan")
+        self.uua = ug.ugrid.array(fill=nan)
+        self.uva = ug.vgrid.array(fill=nan)
+        self.vua = vg.ugrid.array(fill=nan)
+        self.vva = vg.vgrid.array(fill=nan)
+        if not three_d:
+            return
+        for n in ("pk", "uk", "corpk", "advpk", "diffpk"):
+            setattr(self, n, ug.array(name=n, z=CENTERS))
+        for n in ("qk", "vk", "corqk", "advqk", "diffqk"):
+            setattr(self, n, vg.array(name=n, z=CENTERS))
+        self.ww = tgrid.array(name="ww", z=INTERFACES)
+        self.SS = tgrid.array(name="SS", z=INTERFACES)
+        for n in ("rru", "Ui", "udev", "ustar2_bx"):
+            setattr(self, n, ug.array(name=n))
+        for n in ("rrv", "Vi", "vdev", "ustar2_by"):
+            setattr(self, n, vg.array(name=n))
+        self._U_cum = torch.zeros_like(self.Ui.all_values)
+        self._V_cum = torch.zeros_like(self.Vi.all_values)
+        self.uua3d = ug.ugrid.array(fill=nan, z=CENTERS)
+        self.uva3d = ug.vgrid.array(fill=nan, z=CENTERS)
+        self.vua3d = vg.ugrid.array(fill=nan, z=CENTERS)
+        self.vva3d = vg.vgrid.array(fill=nan, z=CENTERS)
+        self.ustar_b = tgrid.array(name="ustar_b")
+        # interpolation targets reused every step (pygetm allocates these per call)
+        self._visc_u = ug.array(z=INTERFACES, fill_value=None)
+        self._visc_v = vg.array(z=INTERFACES, fill_value=None)
+        self._ww_u = ug.array(z=INTERFACES, fill_value=None)
+        self._ww_v = vg.array(z=INTERFACES, fill_value=None)
+
+    def initialize(self, tgrid: Grid, runtype: int, default_advection_scheme: AdvectionScheme):
+        """momentum.py:489-616"""
+        three_d = runtype > 1
+        self._create_arrays(tgrid, three_d)
+        ug, vg = tgrid.ugrid, tgrid.vgrid
+        self.runtype = runtype
+        z0b_u = (ug.z0b_min.all_values[ug.water] == 0.0).any()
+        z0b_v = (vg.z0b_min.all_values[vg.water] == 0.0).any()
+        self.apply_bottom_friction = not bool(z0b_u or z0b_v)
+        self.diffuse_momentum = self._Am_const > 0.0
+        zero_everywhere = MASK_ZERO_2D + (MASK_ZERO_3D if three_d else ())
+        zero_unmasked = ("SxA", "SyA", "SxB", "SyB", "SxD", "SyD", "SxF", "SyF", "dampU", "dampV", "advU", "advV",
+                         "diffU", "diffV", "ru", "rv", "corU", "corV")
+        if three_d:
+            zero_unmasked += ("SS", "advpk", "advqk", "diffpk", "diffqk", "corpk", "corqk", "ww")
+        for n in zero_everywhere:
+            getattr(self, n).all_values.zero_()
+        for n in zero_unmasked:
+            getattr(self, n).fill(0.0)
+        self.corU.all_values[:, -1] = 0.0
+        self.corU.all_values[0, :] = 0.0
+        self.corV.all_values[:, 0] = 0.0
+        self.corV.all_values[-1, :] = 0.0
+        if three_d:
+            self.corpk.all_values[:, :, -1] = 0.0
+            self.corpk.all_values[:, 0, :] = 0.0
+            self.corqk.all_values[:, :, 0] = 0.0
+            self.corqk.all_values[:, -1, :] = 0.0
+        if self.advection_scheme is None:
+            self.advection_scheme = default_advection_scheme
+        self.uadv = Advection(ug, scheme=self.advection_scheme, split_2d=self.advection_split_2d)
+        self.vadv = Advection(vg, scheme=self.advection_scheme, split_2d=self.advection_split_2d)
+        if three_d:
+            self.hU_bot = ug.hn.isel(z=0)
+            self.hV_bot = vg.hn.isel(z=0)
+            self.u_bot = self.uk.isel(z=0)
+            self.v_bot = self.vk.isel(z=0)
+            self._vertical_diffusion = VerticalDiffusion(tgrid, cnpar=self.cnpar)
+            self.ea2 = tgrid.array(fill=0.0, z=CENTERS)
+            self.ea4 = tgrid.array(fill=0.0, z=CENTERS)
+        self.An = tgrid.array(name="An")
+        self.An.fill(self._An_const)
+        self._ufirst = False
+        self._u3dfirst = False
+        self.An_uu = self.An_uv = self.An_vu = self.An_vv = None
+
+    def start(self):
+        """momentum.py:618-642"""
+        zero = MASK_ZERO_2D + (MASK_ZERO_3D if self.runtype > 1 else ())
+        for n in zero:
+            a = getattr(self, n)
+            a.all_values[..., a.grid.land] = 0.0
+        self.An.all_values[self.An.grid.land] = FILL_VALUE
+        if bool((self.An.all_values[self.An.grid.water] == 0.0).all()):
+            self.An_uu = self.An_uv = self.An_vu = self.An_vv = None
+        else:
+            nan = float("nan")
+            self.An_uu = self.An.interp(self.U.grid.ugrid.array(fill=nan))
+            self.An_uv = self.An.interp(self.U.grid.vgrid.array(fill=nan))
+            self.An_vu = self.An.interp(self.V.grid.ugrid.array(fill=nan))
+            self.An_vv = self.An.interp(self.V.grid.vgrid.array(fill=nan))
+
+    # ------------------------------------------------------------------ 2D
+    def advance_depth_integrated(self, timestep: float, tausx: Array, tausy: Array, dpdx: Array, dpdy: Array):
+        """momentum.py:644-718"""
+
+        def u():
+            _pygetm.advance_2d_transport(self.U, dpdx, tausx, self.corU, self.advU, self.diffU, self.dampU,
+                                         self.SxA, self.SxB, self.SxD, self.SxF, self.ru, timestep)
+            self.coriolis(self.U, self.corV, True)
+
+        def v():
+            _pygetm.advance_2d_transport(self.V, dpdy, tausy, self.corV, self.advV, self.diffV, self.dampV,
+                                         self.SyA, self.SyB, self.SyD, self.SyF, self.rv, timestep)
+            self.coriolis(self.V, self.corU, False)
+
+        if self._ufirst:
+            u()
+            v()
+        else:
+            v()
+            u()
+        self._ufirst = not self._ufirst
+        if self.runtype > 1:
+            self._U_cum += self.U.all_values
+            self._V_cum += self.V.all_values
+
+    def update_depth_integrated_diagnostics(self, timestep: float, skip_coriolis: bool = False,
+                                            update_z0b: bool = False):
+        """momentum.py:720-758"""
+        if not skip_coriolis:
+            self.coriolis(self.U, self.corV, True)
+            self.coriolis(self.V, self.corU, False)
+        self._transport_2d_momentum(self.U, self.V, timestep, self.advU, self.advV, self.diffU, self.diffV, update_z0b)
+        if self.An_uu is not None:
+            _pygetm.horizontal_diffusion(self.U, self.An_uu, self.An_uv, timestep, self.dampU)
+            _pygetm.horizontal_diffusion(self.V, self.An_vu, self.An_vv, timestep, self.dampV)
+
+    def _transport_2d_momentum(self, U: Array, V: Array, timestep: float, advU: Array, advV: Array,
+                               diffU: Array, diffV: Array, update_z0b: bool):
+        """momentum.py:1017-1097"""
+        torch.div(U.all_values, U.grid.D.all_values, out=self.u1.all_values)
+        torch.div(V.all_values, V.grid.D.all_values, out=self.v1.all_values)
+        if self.diffuse_momentum:
+            _pygetm.momentum_diffusion(self.uua.grid.D, self.uva.grid.D, self.vua.grid.D, self.vva.grid.D,
+                                       self.u1, self.v1, self._Am_const, diffU, diffV)
+        if self.apply_bottom_friction:
+            self.bottom_friction(self.u1, self.v1, self.u1.grid.D, self.v1.grid.D, self.ru, self.rv, update_z0b)
+        U.interp(self.uua)
+        V.interp(self.uva)
+        self.uua.all_values.div_(self.uua.grid.D.all_values)
+        self.uva.all_values.div_(self.uva.grid.D.all_values)
+        advU.all_values.copy_(self.u1.all_values)
+        self.uadv(self.uua, self.uva, timestep, advU, skip_initial_halo_exchange=True)
+        _pygetm.reconstruct_transport_change(advU, self.uadv.D, U, timestep)
+        U.interp(self.vua)
+        V.interp(self.vva)
+        self.vua.all_values.div_(self.vua.grid.D.all_values)
+        self.vva.all_values.div_(self.vva.grid.D.all_values)
+        advV.all_values.copy_(self.v1.all_values)
+        self.vadv(self.vua, self.vva, timestep, advV, skip_initial_halo_exchange=True)
+        _pygetm.reconstruct_transport_change(advV, self.vadv.D, V, timestep)
+
+    def bottom_friction(self, u: Array, v: Array, DU: Array, DV: Array, ru: Array, rv: Array,
+                        update_z0b: bool = False):
+        """momentum.py:1099-1125"""
+        u_V = u.interp(v.grid._work)
+        v_U = v.interp(u.grid._work)
+        _pygetm.bottom_friction(u, v_U, DU, self.avmmol, ru, update_z0b)
+        _pygetm.bottom_friction(u_V, v, DV, self.avmmol, rv, update_z0b)
+
+    def coriolis(self, U: Array, out: Array, x_direction: bool):
+        """momentum.py:1127-1148 (DEFAULT scheme)"""
+        assert U.grid is not out.grid
+        if self.coriolis_scheme == CoriolisScheme.ESPELID:
+            raise NotImplementedError("Espelid Coriolis interpolation is not implemented")
+        U.interp(out)
+        out.all_values.mul_(out.grid.cor.all_values)
+        if x_direction:
+            out.all_values.neg_()
+
+    # ------------------------------------------------------------------ 3D
+    def advance(self, timestep: float, split_factor: int, tausx: Array, tausy: Array, dpdx: Array, dpdy: Array,
+                idpdx: Array, idpdy: Array, viscosity: Array):
+        """momentum.py:760-858"""
+        torch.mul(self._U_cum, 1.0 / split_factor, out=self.Ui.all_values)
+        torch.mul(self._V_cum, 1.0 / split_factor, out=self.Vi.all_values)
+        self._U_cum.zero_()
+        self._V_cum.zero_()
+
+        def u():
+            self.advance_3d_transport(self.pk, self.Ui, self.uk, dpdx, self.corpk, self.advpk, self.diffpk, idpdx,
+                                      tausx, self.rru, viscosity, self.udev, timestep, self._visc_u)
+            self.coriolis(self.pk, self.corqk, True)
+
+        def v():
+            self.advance_3d_transport(self.qk, self.Vi, self.vk, dpdy, self.corqk, self.advqk, self.diffqk, idpdy,
+                                      tausy, self.rrv, viscosity, self.vdev, timestep, self._visc_v)
+            self.coriolis(self.qk, self.corpk, False)
+
+        if self._u3dfirst:
+            u()
+            v()
+        else:
+            v()
+            u()
+        self._u3dfirst = not self._u3dfirst
+        self.update_diagnostics(timestep, viscosity, skip_coriolis=True)
+
+    def update_diagnostics(self, timestep: float, viscosity: Array, skip_coriolis: bool = False):
+        """momentum.py:860-1015"""
+        if not skip_coriolis:
+            self.coriolis(self.pk, self.corqk, True)
+            self.coriolis(self.qk, self.corpk, False)
+        _pygetm.w_momentum_3d(self.pk, self.qk, timestep, self.ww)
+        torch.div(self.pk.all_values, self.pk.grid.hn.all_values, out=self.uk.all_values)
+        torch.div(self.qk.all_values, self.qk.grid.hn.all_values, out=self.vk.all_values)
+        _pygetm.shear_frequency(self.uk, self.vk, self.SS)
+        if self.apply_bottom_friction:
+            self.bottom_friction(self.u_bot, self.v_bot, self.hU_bot, self.hV_bot, self.rru, self.rrv)
+        _pygetm.bottom_shear_velocity(self.u_bot, self.v_bot, self.rru, self.rrv, self.ustar2_bx, self.ustar2_by,
+                                      self.ustar_b)
+        self.advpk.all_values.copy_(self.uk.all_values)
+        self.uadv.apply_3d(self.uk.interp(self.uua3d), self.vk.interp(self.uva3d), self.ww.interp(self._ww_u),
+                           timestep, self.advpk, new_h=True, skip_initial_halo_exchange=True)
+        _pygetm.reconstruct_transport_change(self.advpk, self.uadv.h, self.pk, timestep)
+        self.advqk.all_values.copy_(self.vk.all_values)
+        self.vadv.apply_3d(self.uk.interp(self.vua3d), self.vk.interp(self.vva3d), self.ww.interp(self._ww_v),
+                           timestep, self.advqk, new_h=True, skip_initial_halo_exchange=True)
+        _pygetm.reconstruct_transport_change(self.advqk, self.vadv.h, self.qk, timestep)
+        if self.diffuse_momentum:
+            _pygetm.momentum_diffusion(self.uua.grid.hn, self.uva.grid.hn, self.vua.grid.hn, self.vva.grid.hn,
+                                       self.uk, self.vk, self._Am_const, self.diffpk, self.diffqk)
+        self._transport_2d_momentum(self.Ui, self.Vi, timestep, self.SxA, self.SyA, self.SxD, self.SyD, False)
+        torch.sub(self.advpk.all_values.sum(dim=0), self.SxA.all_values, out=self.SxA.all_values)
+        torch.sub(self.advqk.all_values.sum(dim=0), self.SyA.all_values, out=self.SyA.all_values)
+        torch.sub(self.diffpk.all_values.sum(dim=0), self.SxD.all_values, out=self.SxD.all_values)
+        torch.sub(self.diffqk.all_values.sum(dim=0), self.SyD.all_values, out=self.SyD.all_values)
+        if self.apply_bottom_friction:
+            torch.add(self.ustar2_bx.all_values, self.ru.all_values * self.u1.all_values, out=self.SxF.all_values)
+            torch.add(self.ustar2_by.all_values, self.rv.all_values * self.v1.all_values, out=self.SyF.all_values)
+
+    def advance_3d_transport(self, tp3d: Array, tp2d: Array, vel3d: Array, dp: Array, cor: Array, adv: Array,
+                             diff: Array, idp: Array, taus: Array, rr: Array, viscosity: Array, dev: Array,
+                             timestep: float, visc_target: Optional[Array] = None):
+        """momentum.py:1164-1214"""
+        grid = tp3d.grid
+        _pygetm.collect_3d_momentum_sources(dp, cor, adv, diff, idp, taus, rr, timestep, self.ea2, self.ea4)
+        visc = viscosity.interp(visc_target if visc_target is not None else grid)
+        self._vertical_diffusion(visc, timestep, vel3d, molecular=self.avmmol, ea2=self.ea2, ea4=self.ea4,
+                                 use_ho=True)
+        torch.mul(vel3d.all_values, grid.hn.all_values, out=tp3d.all_values)
+        torch.sum(tp3d.all_values, dim=0, out=dev.all_values)
+        dev.all_values.sub_(tp2d.all_values)
+        dev.all_values.div_(grid.D.all_values)
+        tp3d.all_values.sub_(dev.all_values * grid.hn.all_values)

@@ -51,3 +51,287 @@ class TracerTransport:
     def run(self, nstep: int):
         for _ in range(nstep):
             self.step()
+
+
+# ---------------------------------------------------------------------------
+# split-explicit baroclinic simulation
+# ---------------------------------------------------------------------------
+import enum  # noqa: E402
+
+from . import _pygetm  # noqa: E402
+from .domain import FILL_VALUE, GRAVITY, RHO0  # noqa: E402
+from .momentum import Momentum  # noqa: E402
+
+
+class RunType(enum.IntEnum):
+    """python/pygetm/constants.py:19-23"""
+
+    BAROTROPIC_2D = 1
+    BAROTROPIC_3D = 2
+    FROZEN_DENSITY = 3
+    BAROCLINIC = 4
+
+
+class Fluxes:
+    """Prescribed constant surface fluxes (python/pygetm/airsea.py:109-147)."""
+
+    def __init__(self, taux=0.0, tauy=0.0, sp=101325.0, shf=0.0, swr=0.0, pe=0.0):
+        self._ini = dict(taux=taux, tauy=tauy, sp=sp, shf=shf, swr=swr, pe=pe)
+
+    def initialize(self, grid):
+        for n, v in self._ini.items():
+            a = grid.array(name=n)
+            a.fill(v)
+            setattr(self, n, a)
+
+
+class Simulation:
+    """GPU counterpart of pygetm.Simulation (python/pygetm/simulation.py:477-1630)
+    for closed domains with prescribed surface fluxes and prescribed vertical
+    mixing (``num``/``nuh``), Sigma coordinates, Shchepetkin-McWilliams (or
+    Blumberg-Mellor) internal pressure and the device equation of state.
+
+    ``T_host``: HostGrid tree from ``Domain.create_grids(nz, velocity_grids=2)``;
+    ``dga``: sigma layer fractions (bottom to surface).
+    """
+
+    def __init__(self, T_host, dga, *, runtype: RunType = RunType.BAROCLINIC,
+                 advection_scheme: AdvectionScheme = AdvectionScheme.DEFAULT, momentum: Optional[Momentum] = None,
+                 airsea: Optional[Fluxes] = None, internal_pressure: str = "shchepetkin_mcwilliams",
+                 Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
+                 nuh: float = 0.0, device="cuda"):
+        if Dmin <= 0.0:
+            raise Exception("Dmin<=0")
+        if Dcrit < 2.5 * Dmin:
+            raise Exception("Dcrit < 2.5*Dmin")
+        self.runtype = RunType(runtype)
+        self.dga = torch.as_tensor(dga, dtype=torch.float64, device=device)[:, None, None]
+        self.T = T = make_grids(T_host, device)
+        self.U, self.V, self.X = T.ugrid, T.vgrid, T.xgrid
+        self.Dmin, self.Dcrit = Dmin, Dcrit
+        self.delay_slow_ip = delay_slow_ip
+        three_d = self.runtype > RunType.BAROTROPIC_2D
+        T.z = T.array(name="zt")
+        T.zo = T.array(name="zot")
+        T.z.fill(0.0)
+        T.zo.fill(0.0)
+        if three_d:
+            T.zin = T.array(name="zint")
+            T.zio = T.array(name="ziot")
+            for g in (T, self.U, self.V):
+                g.ho = g.array(name="ho" + g.postfix, z=CENTERS)
+        T.Dclip = T.array(name="Dclip")
+        if three_d:
+            self.h_T_half = T.array(fill=float("nan"), z=CENTERS)
+            self.depth = T.array(z=CENTERS, name="pres")
+        self.momentum = momentum or Momentum()
+        self.momentum.initialize(T, int(self.runtype), advection_scheme)
+        self.airsea = airsea or Fluxes()
+        self.airsea.initialize(T)
+        self.dpdx = self.U.array(name="dpdx")
+        self.dpdy = self.V.array(name="dpdy")
+        self.tausx = self.U.array(name="tausxu")
+        self.tausy = self.V.array(name="tausyv")
+        self.fwf = T.array(name="fwf")
+        self.fwf.fill(0.0)
+        self.tracers = TracerCollection(T, advection_scheme)
+        if three_d:
+            self.num = T.array(z=INTERFACES, name="num")
+            self.nuh = T.array(z=INTERFACES, name="nuh")
+            self.num.fill(num)
+            self.nuh.fill(nuh)
+            self.ustar_s = T.array(fill=0.0, name="ustar_s")
+            self.tausxo = self.U.array(fill_value=None)
+            self.tausyo = self.V.array(fill_value=None)
+            self.dpdxo = self.U.array(fill_value=None)
+            self.dpdyo = self.V.array(fill_value=None)
+        self.idpdx = self.idpdy = None
+        if self.runtype == RunType.BAROCLINIC:
+            self.temp = self.tracers.add("temp", molecular_diffusivity=1.4e-7)
+            self.salt = self.tracers.add("salt", molecular_diffusivity=1.1e-9)
+            self.temp.fill(5.0)
+            self.salt.fill(35.0)
+            self.rho = T.array(z=CENTERS, name="rho")
+            self.buoy = T.array(z=CENTERS, name="buoy")
+            self.internal_pressure_method = internal_pressure
+        if three_d:
+            # internal_pressure.Base.initialize (python/pygetm/internal_pressure.py:14-30)
+            self.idpdx = self.U.array(z=CENTERS, name="idpdx")
+            self.idpdy = self.V.array(z=CENTERS, name="idpdy")
+            self.idpdx.fill(0.0)
+            self.idpdy.fill(0.0)
+            self._P_work = torch.zeros((T.nz, T.ny_, T.nx_), dtype=torch.float64, device=T.device)
+        self.update_depth(_3d=three_d)
+        self.update_depth(_3d=three_d)
+
+    # ---------------------------------------------------------------- driver
+    def start(self, timestep: float, split_factor: int = 1):
+        """python/pygetm/simulation.py:207-275"""
+        self.timestep = float(timestep)
+        self.split_factor = int(split_factor)
+        self.macrotimestep = self.timestep * self.split_factor
+        self.istep = 0
+        self._start()
+        self._update_forcing_and_diagnostics(macro_active=True)
+
+    def advance(self):
+        """python/pygetm/simulation.py:291-325"""
+        self.istep += 1
+        macro_active = self.istep % self.split_factor == 0
+        self._advance_state(macro_active)
+        self._update_forcing_and_diagnostics(macro_active)
+
+    def _start(self):
+        """python/pygetm/simulation.py:948-1031"""
+        T = self.T
+        self.momentum.start()
+        for grid in (self.U, self.V):
+            edges = grid.water_contact & grid.land
+            grid.D.all_values[edges] = FILL_VALUE
+            if grid.hn is not None:
+                grid.hn.all_values[..., edges] = FILL_VALUE
+
+        minz = -T.H.all_values + self.Dmin
+
+        def clip_z(z):
+            shallow = (z.all_values < minz) & T.water
+            z.all_values[shallow] = minz[shallow]
+
+        clip_z(T.z)
+        clip_z(T.zo)
+        three_d = self.runtype > RunType.BAROTROPIC_2D
+        if three_d:
+            clip_z(T.zin)
+            clip_z(T.zio)
+        z_backup = T.z.all_values.clone()
+        T.z.all_values.copy_(T.zo.all_values)
+        self.update_depth(_3d=False)
+        if three_d:
+            zin_backup = T.zin.all_values.clone()
+            T.z.all_values.copy_(T.zio.all_values)
+            T.zio.fill(float("nan"))
+            T.ho.fill(float("nan"))
+            self.update_depth(_3d=True)
+            T.z.all_values.copy_(zin_backup)
+            self.update_depth(_3d=True, timestep=self.macrotimestep)
+            self.momentum.update_diagnostics(self.macrotimestep, self.num)
+        T.z.all_values.copy_(z_backup)
+
+    def _advance_state(self, macro_active: bool):
+        """python/pygetm/simulation.py:1033-1136"""
+        self.momentum.advance_depth_integrated(self.timestep, self.tausx, self.tausy, self.dpdx, self.dpdy)
+        self.advance_surface_elevation(self.timestep, self.momentum.U, self.momentum.V, self.fwf)
+        if self.runtype > RunType.BAROTROPIC_2D and macro_active:
+            # add_freshwater_inputs (simulation.py:1335-1406) is an exact no-op
+            # without rivers and with zero precipitation-evaporation.
+            self.update_depth(_3d=True, timestep=self.macrotimestep)
+            self.momentum.advance(self.macrotimestep, self.split_factor, self.tausxo, self.tausyo, self.dpdxo,
+                                  self.dpdyo, self.idpdx, self.idpdy, self.num)
+            self.tracers.advance(self.macrotimestep, self.momentum.uk, self.momentum.vk, self.momentum.ww, self.nuh)
+            if self.runtype == RunType.BAROCLINIC and self.delay_slow_ip:
+                torch.sum(self.idpdx.all_values, dim=0, out=self.momentum.SxB.all_values)
+                torch.sum(self.idpdy.all_values, dim=0, out=self.momentum.SyB.all_values)
+
+    def _update_forcing_and_diagnostics(self, macro_active: bool):
+        """python/pygetm/simulation.py:1138-1304"""
+        starting = self.istep == 0
+        update_z0b = self.runtype == RunType.BAROTROPIC_2D and not starting
+        update_3d = self.runtype > RunType.BAROTROPIC_2D and macro_active
+        update_baroclinic = self.runtype == RunType.BAROCLINIC and macro_active
+        if update_baroclinic:
+            self.update_density()
+            self.update_internal_pressure()
+            if not self.delay_slow_ip:
+                torch.sum(self.idpdx.all_values, dim=0, out=self.momentum.SxB.all_values)
+                torch.sum(self.idpdy.all_values, dim=0, out=self.momentum.SyB.all_values)
+        self.update_depth()
+        self.momentum.update_depth_integrated_diagnostics(self.timestep, skip_coriolis=not starting,
+                                                         update_z0b=update_z0b)
+        self.fwf.all_values.copy_(self.airsea.pe.all_values)
+        self.update_surface_pressure_gradient(self.T.z, self.airsea.sp)
+        self.airsea.taux.interp(self.tausx)
+        self.airsea.tauy.interp(self.tausy)
+        if update_3d:
+            self.tausxo.all_values.copy_(self.tausx.all_values)
+            self.tausyo.all_values.copy_(self.tausy.all_values)
+            self.dpdxo.all_values.copy_(self.dpdx.all_values)
+            self.dpdyo.all_values.copy_(self.dpdy.all_values)
+            _pygetm.surface_shear_velocity(self.airsea.taux, self.airsea.tauy, self.ustar_s)
+
+    # ------------------------------------------------------------ components
+    def update_density(self):
+        """density.get_density + buoyancy (simulation.py:1178-1184) with the
+        device equation of state."""
+        n = self.rho.all_values.numel()
+        from ._lib import call
+
+        call("getm_density_buoyancy", n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
+             self.depth.all_values.data_ptr(), self.rho.all_values.data_ptr(), self.buoy.all_values.data_ptr(),
+             torch.cuda.current_stream().cuda_stream)
+
+    def update_internal_pressure(self):
+        if self.internal_pressure_method == "blumberg_mellor":
+            _pygetm.blumberg_mellor(self.buoy, self.idpdx, self.idpdy)
+        else:
+            _pygetm.shchepetkin_mcwilliams(self.buoy, self.idpdx, self.idpdy, self._P_work)
+
+    def advance_surface_elevation(self, timestep: float, U: Array, V: Array, fwf: Array):
+        """simulation.py:1468-1486"""
+        self.T.zo.all_values.copy_(self.T.z.all_values)
+        _pygetm.advance_surface_elevation(timestep, self.T.z, U, V, fwf)
+
+    def update_surface_pressure_gradient(self, z: Array, sp: Array):
+        """simulation.py:1488-1489"""
+        _pygetm.surface_pressure_gradient(z, sp, self.dpdx, self.dpdy, self.Dmin)
+
+    def _sigma(self, grid):
+        """Sigma.__call__ on one grid (vertical_coordinates.py:106-113)."""
+        hn = grid.hn.all_values
+        D = grid.Dclip.all_values
+        wet = (grid.mask.all_values != 0)
+        torch.where(wet, self.dga * D, hn, out=hn)
+
+    def update_depth(self, _3d: bool = False, timestep: float = 0.0):
+        """simulation.py:1498-1630"""
+        T, U, V, X = self.T, self.U, self.V, self.X
+        if _3d:
+            T.zio.all_values.copy_(T.zin.all_values)
+            T.zin.all_values.copy_(T.z.all_values)
+            z_T, zo_T = T.zin, T.zio
+        else:
+            z_T, zo_T = T.z, T.zo
+        z_U, z_V, z_X, z_T_half = U._work, V._work, X._work, T._work
+        _pygetm.elevation2depth(z_T, T.H, -1000.0, T.D)
+        torch.clamp(T.D.all_values, min=self.Dmin, out=T.Dclip.all_values)
+        torch.add(zo_T.all_values, z_T.all_values, out=z_T_half.all_values)
+        z_T_half.all_values.mul_(0.5)
+        z_T_half.interp(z_U)
+        _pygetm.elevation2depth(z_U, U.H, self.Dmin, U.D)
+        z_T_half.interp(z_V)
+        _pygetm.elevation2depth(z_V, V.H, self.Dmin, V.D)
+        z_T_half.interp(z_X)
+        _pygetm.elevation2depth(z_X, X.H, self.Dmin, X.D)
+        _pygetm.alpha(U.D, 2 * self.Dmin, self.Dcrit, U.alpha)
+        _pygetm.alpha(V.D, 2 * self.Dmin, self.Dcrit, V.alpha)
+        D_T_half = T._work
+        _pygetm.elevation2depth(z_T_half, T.H, self.Dmin, D_T_half)
+        U.ugrid.D.all_values[:, :-1] = D_T_half.all_values[:, 1:]
+        V.vgrid.D.all_values[:-1, :] = D_T_half.all_values[1:, :]
+        U.vgrid.D.all_values[:, :] = X.D.all_values[1:, 1:]
+        V.ugrid.D.all_values[:, :] = U.vgrid.D.all_values
+        if _3d:
+            T.ho.all_values.copy_(T.hn.all_values)
+            U.ho.all_values.copy_(U.hn.all_values)
+            V.ho.all_values.copy_(V.hn.all_values)
+            for g in (T, U, V, X):
+                self._sigma(g)
+            for g in (T, U, V):
+                _pygetm.thickness2vertical_coordinates(g.mask, g.H, g.hn, g.zc, g.zf)
+            torch.add(T.ho.all_values, T.hn.all_values, out=self.h_T_half.all_values)
+            self.h_T_half.all_values.mul_(0.5)
+            U.ugrid.hn.all_values[:, :, :-1] = self.h_T_half.all_values[:, :, 1:]
+            V.vgrid.hn.all_values[:, :-1, :] = self.h_T_half.all_values[:, 1:, :]
+            U.vgrid.hn.all_values[:, :, :] = X.hn.all_values[:, 1:, 1:]
+            V.ugrid.hn.all_values[:, :, :] = U.vgrid.hn.all_values
+            if self.runtype == RunType.BAROCLINIC:
+                _pygetm.thickness2center_depth(T.mask, T.hn, self.depth)

@@ -184,6 +184,33 @@ def tracer_transport(nx: int = 120, ny: int = 100, nz: int = 30, seed: int = 1, 
     return Workload("tracer_transport", T, dga, fields, dict(dt=dt, umax=0.5, scheme=5, cnpar=1.0))
 
 
+def seamount(nx: int = 400, ny: int = 300, nz: int = 40, seed: int = 2, dx: float = 2000.0,
+             timestep: float = 4.0, split_factor: int = 30) -> Workload:
+    """Baroclinic seamount box (400 x 300 x 40 by default): 4500 m deep with a
+    4000 m high Gaussian seamount of radius 25 km at the centre, f = 1e-4,
+    closed boundaries, no wind, prescribed num = nuh = 1e-4 m2/s, bottom
+    roughness z0 = 0.755 m (drag coefficient 2.5e-3 at D = 4500 m with the
+    log-law of python/src/momentum.F90:93), T = 4 + 16 (z + 4500)/4500 degC,
+    S = 35.  The random seed is unused: the configuration is deterministic."""
+    del seed
+    x = dx * (np.arange(nx) - 0.5 * (nx - 1))
+    y = dx * (np.arange(ny) - 0.5 * (ny - 1))
+    r2 = x[None, :] ** 2 + y[:, None] ** 2
+    H = 4500.0 - 4000.0 * np.exp(-r2 / 25000.0**2)
+    kappa, cd = 0.4, 2.5e-3
+    z0 = 0.5 * 4500.0 / (np.exp(kappa / np.sqrt(cd)) - 1.0)
+    dom = create_cartesian(x, y, H=H, f=1e-4, z0=z0)
+    T = dom.create_grids(nz, halox=2, haloy=2, velocity_grids=2)
+    dga = calculate_sigma(nz)
+    params = dict(timestep=timestep, split_factor=split_factor, num=1e-4, nuh=1e-4, z0=z0, scheme=5)
+    return Workload("seamount", T, dga, {}, params)
+
+
+def seamount_temperature(zc: np.ndarray) -> np.ndarray:
+    """Linear stratification 20 degC at the surface to 4 degC at 4500 m."""
+    return 4.0 + 16.0 * (zc + 4500.0) / 4500.0
+
+
 def land_fraction(wl: Workload) -> float:
     m = wl.T.mask[wl.T.interior[1:]]
     return float((m == 0).mean())

@@ -237,6 +237,21 @@ int getm_shchepetkin_mcwilliams(int nx, int ny, int nz, int imin, int imax, int 
                                 double* idpdx, double* idpdy, double* P_work,
                                 cudaStream_t stream);
 
+/* ---- instrumentation ----------------------------------------------------
+ * No counterpart in the reference.  Number of kernel launches this library
+ * has issued in the process so far (launches captured into a CUDA graph are
+ * counted once, at capture).                                                */
+int getm_launch_count(unsigned long long* count);
+
+/* ---- equation of state --------------------------------------------------
+ * No counterpart in the reference's Fortran: pygetm takes density from the
+ * external TEOS-10 package pygsw (python/pygetm/density.py:62-95).  This
+ * device EOS is the simplified nonlinear equation of state of Roquet et al.
+ * (2015); p is depth below the surface (m).  Writes rho and/or buoyancy
+ * -g/rho0 (rho - rho0) (python/pygetm/simulation.py:1184); either may be NULL. */
+int getm_density_buoyancy(int n, const double* salt, const double* temp, const double* p, double* rho,
+                          double* buoy, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

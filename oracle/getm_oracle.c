@@ -158,19 +158,24 @@ void oracle_advection_uv_calculate(int direction, int nk, int scheme, int imin, 
                                    const int *tmask, const double *iA)
 {
     const size_t n2 = (size_t)(imax - imin + 1 + 2 * halox) * (size_t)(jmax - jmin + 1 + 2 * haloy);
-    double *flux = (double *)calloc(n2, sizeof(double));
-    double *QU = (double *)calloc(n2, sizeof(double));
-    for (int k = 0; k < nk; k++) {
-        /* u2d receives (umask, idxu, dyu); v2d receives (vmask, dxv, idyv) and
-         * uses dxv in the transport and idyv in the cfl (template :164-165). */
-        const double *idx_ = (direction == 1) ? m1 : m2;
-        const double *dy_ = (direction == 1) ? m2 : m1;
-        advect_layer(direction, scheme, imin, imax, jmin, jmax, halox, haloy, umask, idx_, dy_,
-                     hu + k * n2, u + k * n2, tmask, iA, Ah != NULL, Ah ? Ah : u, timestep,
-                     h + k * n2, var + k * n2, flux, QU);
+    /* layers are independent (wrapper.F90:242-252): threads take whole layers */
+#pragma omp parallel
+    {
+        double *flux = (double *)calloc(n2, sizeof(double));
+        double *QU = (double *)calloc(n2, sizeof(double));
+#pragma omp for schedule(static)
+        for (int k = 0; k < nk; k++) {
+            /* u2d receives (umask, idxu, dyu); v2d receives (vmask, dxv, idyv) and
+             * uses dxv in the transport and idyv in the cfl (template :164-165). */
+            const double *idx_ = (direction == 1) ? m1 : m2;
+            const double *dy_ = (direction == 1) ? m2 : m1;
+            advect_layer(direction, scheme, imin, imax, jmin, jmax, halox, haloy, umask, idx_, dy_,
+                         hu + k * n2, u + k * n2, tmask, iA, Ah != NULL, Ah ? Ah : u, timestep,
+                         h + k * n2, var + k * n2, flux, QU);
+        }
+        free(flux);
+        free(QU);
     }
-    free(flux);
-    free(QU);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -186,17 +191,20 @@ int oracle_advection_w_calculate(int scheme, int imin, int imax, int jmin, int j
     const int itersmax = 200;
     const int nx_ = imax - imin + 1 + 2 * halox;
     const int ny_ = jmax - jmin + 1 + 2 * haloy;
+    int maxiters = 0;
+    /* Fortran level k of h/f (1..kmax) -> C plane k-1; w level k (0..kmax) -> plane k */
+#define HF(i, j, k) IDX3((i) - (imin - halox), (j) - (jmin - haloy), (k) - 1)
+#define WW(i, j, k) IDX3((i) - (imin - halox), (j) - (jmin - haloy), (k))
+#pragma omp parallel reduction(max : maxiters)
+    {
     double *flux = (double *)calloc((size_t)kmax + 1, sizeof(double));
     double *cfl0 = (double *)calloc((size_t)kmax + 1, sizeof(double));
     double *cfls = (double *)calloc((size_t)kmax + 1, sizeof(double));
     double *haux = (double *)calloc((size_t)kmax + 1, sizeof(double));
     double *faux = (double *)calloc((size_t)kmax + 1, sizeof(double));
-    int maxiters = 0;
-    /* Fortran level k of h/f (1..kmax) -> C plane k-1; w level k (0..kmax) -> plane k */
-#define HF(i, j, k) IDX3((i) - (imin - halox), (j) - (jmin - haloy), (k) - 1)
-#define WW(i, j, k) IDX3((i) - (imin - halox), (j) - (jmin - haloy), (k))
     flux[0] = 0.0;
     flux[kmax] = 0.0;
+#pragma omp for schedule(dynamic, 4)
     for (int j = jmin; j <= jmax; j++) {
         for (int i = imin; i <= imax; i++) {
             if (tmask[IDX2(i - (imin - halox), j - (jmin - haloy))] != 1) continue;
@@ -278,13 +286,14 @@ int oracle_advection_w_calculate(int scheme, int imin, int imax, int jmin, int j
             if (iters > maxiters) maxiters = iters;
         }
     }
-#undef HF
-#undef WW
     free(flux);
     free(cfl0);
     free(cfls);
     free(haux);
     free(faux);
+    }
+#undef HF
+#undef WW
     return maxiters;
 }
 
@@ -302,6 +311,7 @@ void oracle_vertical_diffusion_prepare(int nx_, int ny_, int nz, double molecula
     (void)mask;
     if (nz == 1) return; /* diffusion.F90:155 */
     /* diffusion.F90:163-171: all i, j including halos; Fortran k = kmin..kmax-1 */
+#pragma omp parallel for schedule(static)
     for (int k = 1; k <= nz - 1; k++) {
         for (int j = 0; j < ny_; j++) {
             for (int i = 0; i < nx_; i++) {
@@ -329,13 +339,16 @@ void oracle_vertical_diffusion_apply(int nx_, int ny_, int nz, const int *mask,
         }
         return;
     }
+    const int kmin = 0, kmax = nz - 1; /* C levels; Fortran kmin=1..kmax=nz */
+#pragma omp parallel
+    {
     double *a1 = (double *)malloc(sizeof(double) * nz);
     double *a2 = (double *)malloc(sizeof(double) * nz);
     double *a3 = (double *)malloc(sizeof(double) * nz);
     double *a4 = (double *)malloc(sizeof(double) * nz);
     double *ru = (double *)malloc(sizeof(double) * nz);
     double *qu = (double *)malloc(sizeof(double) * nz);
-    const int kmin = 0, kmax = nz - 1; /* C levels; Fortran kmin=1..kmax=nz */
+#pragma omp for schedule(static)
     for (int j = 0; j < ny_; j++) {
         for (int i = 0; i < nx_; i++) {
             if (mask[IDX2(i, j)] != 1) continue;
@@ -379,6 +392,7 @@ void oracle_vertical_diffusion_apply(int nx_, int ny_, int nz, const int *mask,
         }
     }
     free(a1); free(a2); free(a3); free(a4); free(ru); free(qu);
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -386,6 +400,7 @@ void oracle_vertical_diffusion_apply(int nx_, int ny_, int nz, const int *mask,
 /* ------------------------------------------------------------------------ */
 void oracle_grid_interp_x(int nx_, int ny_, int nz, const double *source, double *target, int ioffset)
 {
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < nz; k++)
         for (int j = 0; j < ny_; j++)
             for (int i = 0; i < nx_ - 1; i++)
@@ -394,6 +409,7 @@ void oracle_grid_interp_x(int nx_, int ny_, int nz, const double *source, double
 
 void oracle_grid_interp_y(int nx_, int ny_, int nz, const double *source, double *target, int joffset)
 {
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < nz; k++)
         for (int j = 0; j < ny_ - 1; j++)
             for (int i = 0; i < nx_; i++)
@@ -403,6 +419,7 @@ void oracle_grid_interp_y(int nx_, int ny_, int nz, const double *source, double
 void oracle_grid_interp_z(int nx_, int ny_, int nz1, int nz2, const double *source, double *target, int koffset)
 {
     (void)nz2;
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < nz1 - 1; k++)
         for (int j = 0; j < ny_; j++)
             for (int i = 0; i < nx_; i++)
@@ -412,6 +429,7 @@ void oracle_grid_interp_z(int nx_, int ny_, int nz1, int nz2, const double *sour
 void oracle_grid_interp_xy(int nx1, int ny1, int nx2, int ny2, int nz, const double *source,
                            double *target, int ioffset, int joffset)
 {
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < nz; k++)
         for (int j = 0; j < ny1 - 1; j++)
             for (int i = 0; i < nx1 - 1; i++) {
@@ -443,6 +461,7 @@ void oracle_thickness2vertical_coordinates(int nx_, int ny_, int nz, const int *
                                            const double *bottom_depth, const double *h,
                                            double *zc, double *zf)
 {
+#pragma omp parallel for schedule(static)
     for (int j = 0; j < ny_; j++)
         for (int i = 0; i < nx_; i++) {
             size_t p = IDX2(i, j);
@@ -459,6 +478,7 @@ void oracle_thickness2vertical_coordinates(int nx_, int ny_, int nz, const int *
 /* wrapper.F90:395-407 (istart..jstop unused by the reference routine too) */
 void oracle_thickness2center_depth(int nx_, int ny_, int nz, const int *mask, const double *h, double *out)
 {
+#pragma omp parallel for schedule(static)
     for (int j = 0; j < ny_; j++)
         for (int i = 0; i < nx_; i++) {
             if (mask[IDX2(i, j)] == 0) continue;
@@ -654,6 +674,7 @@ void oracle_collect_3d_momentum_sources(int nx_, int ny_, int nz, int halox, int
     (void)mask;
     (void)halox;
     const double rho0i = 1.0 / RHO0;
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < nz; k++)
         for (int j = haloy; j < ny_ - haloy; j++)
             for (int i = 0; i < nx_; i++) {
@@ -694,8 +715,9 @@ void oracle_w_momentum_3d(int nx_, int ny_, int nz, int imin, int imax, int jmin
 {
     const double idt = 1.0 / dt;
     /* w has nz+1 levels (0..nz); h/pk/qk level k (1..nz) is C plane k-1 */
-    for (int k = 1; k <= nz - 1; k++)
-        for (int j = jmin - 1; j <= jmax - 1; j++)
+#pragma omp parallel for schedule(static)
+    for (int j = jmin - 1; j <= jmax - 1; j++)
+        for (int k = 1; k <= nz - 1; k++)
             for (int i = imin - 1; i <= imax - 1; i++) {
                 size_t p = IDX2(i, j);
                 if (mask[p] != 1) continue;
@@ -710,6 +732,7 @@ void oracle_shear_frequency(int nx_, int ny_, int nz, int imin, int imax, int jm
                             const int *mask, const double *hu, const double *hv,
                             const double *uk, const double *vk, double *SS)
 {
+#pragma omp parallel for schedule(static)
     for (int k = 1; k <= nz - 1; k++)
         for (int j = jmin - 1; j <= jmax - 1; j++)
             for (int i = imin - 1; i <= imax - 1; i++) {
@@ -773,6 +796,7 @@ void oracle_reconstruct_transport_change(int nx_, int ny_, int nz, int imin, int
 {
     (void)imin; (void)imax;
     const double idt = 1.0 / timestep;
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < nz; k++)
         for (int j = jmin - 1; j <= jmax - 1; j++)
             for (int i = 0; i < nx_; i++) {
@@ -792,6 +816,7 @@ void oracle_blumberg_mellor(int nx_, int ny_, int nz, int imin, int imax, int jm
 {
     /* buoy/hu/idpdx level k (1..nz) -> plane k-1; zf level k (0..nz) -> plane k */
 #define B(i, j, k) buoy[IDX3(i, j, (k) - 1)]
+#pragma omp parallel for schedule(static)
     for (int j = jmin - 1; j <= jmax - 1; j++)
         for (int i = imin - 1; i <= imax - 1; i++) {
             size_t p = IDX2(i, j);
@@ -810,6 +835,7 @@ void oracle_blumberg_mellor(int nx_, int ny_, int nz, int imin, int imax, int jm
                 idpdx[IDX3(i, j, k - 1)] = hu[IDX3(i, j, k - 1)] * prgr;
             }
         }
+#pragma omp parallel for schedule(static)
     for (int j = jmin - 1; j <= jmax - 1; j++)
         for (int i = imin - 1; i <= imax - 1; i++) {
             size_t p = IDX2(i, j);
@@ -854,6 +880,7 @@ void oracle_shchepetkin_mcwilliams(int nx_, int ny_, int nz, int imin, int imax,
 #define DZ(i, j, k) dZ[IDX3(i, j, k)]
 #define PP(i, j, k) P[IDX3(i, j, (k) - 1)]
     /* :80-118  (C i in imin-1..imax, j in jmin-1..jmax: Fortran imin..imax+1) */
+#pragma omp parallel for schedule(static)
     for (int j = jmin - 1; j <= jmax; j++)
         for (int i = imin - 1; i <= imax; i++) {
             if (mask[IDX2(i, j)] <= 0) continue;
@@ -886,6 +913,7 @@ void oracle_shchepetkin_mcwilliams(int nx_, int ny_, int nz, int imin, int imax,
         }
     /* x-direction :120-167 */
     for (int k = nz; k >= 1; k--) {
+#pragma omp parallel for schedule(static)
         for (int j = jmin - 1; j <= jmax - 1; j++)
             for (int i = imin - 1; i <= imax + 1; i++) {
                 size_t p = IDX2(i, j);
@@ -897,6 +925,7 @@ void oracle_shchepetkin_mcwilliams(int nx_, int ny_, int nz, int imin, int imax,
                     dRx[p] = 0.0;
                 }
             }
+#pragma omp parallel for schedule(static)
         for (int j = jmin - 1; j <= jmax - 1; j++)
             for (int i = imin - 1; i <= imax; i++) {
                 size_t p = IDX2(i, j);
@@ -905,6 +934,7 @@ void oracle_shchepetkin_mcwilliams(int nx_, int ny_, int nz, int imin, int imax,
                 cff = 2.0 * dRx[p] * dRx[p + 1];
                 dRx[p] = (cff > eps) ? cff / (dRx[p] + dRx[p + 1]) : 0.0;
             }
+#pragma omp parallel for schedule(static)
         for (int j = jmin - 1; j <= jmax - 1; j++)
             for (int i = imin - 1; i <= imax - 1; i++) {
                 size_t p = IDX2(i, j);
@@ -918,6 +948,7 @@ void oracle_shchepetkin_mcwilliams(int nx_, int ny_, int nz, int imin, int imax,
     }
     /* y-direction :169-216 */
     for (int k = nz; k >= 1; k--) {
+#pragma omp parallel for schedule(static)
         for (int j = jmin - 1; j <= jmax + 1; j++)
             for (int i = imin - 1; i <= imax - 1; i++) {
                 size_t p = IDX2(i, j);
@@ -929,6 +960,7 @@ void oracle_shchepetkin_mcwilliams(int nx_, int ny_, int nz, int imin, int imax,
                     dRx[p] = 0.0;
                 }
             }
+#pragma omp parallel for schedule(static)
         for (int j = jmin - 1; j <= jmax; j++)
             for (int i = imin - 1; i <= imax - 1; i++) {
                 size_t p = IDX2(i, j);
@@ -937,6 +969,7 @@ void oracle_shchepetkin_mcwilliams(int nx_, int ny_, int nz, int imin, int imax,
                 cff = 2.0 * dRx[p] * dRx[p + nx_];
                 dRx[p] = (cff > eps) ? cff / (dRx[p] + dRx[p + nx_]) : 0.0;
             }
+#pragma omp parallel for schedule(static)
         for (int j = jmin - 1; j <= jmax - 1; j++)
             for (int i = imin - 1; i <= imax - 1; i++) {
                 size_t p = IDX2(i, j);

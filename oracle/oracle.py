@@ -33,7 +33,10 @@ FILL_VALUE = -2e20
 RHO0 = 1025.0
 GRAVITY = 9.81
 
-_lib = ctypes.CDLL(str(_build.build("serial")))
+import os as _os
+
+# GETM_ORACLE_VARIANT=omp selects the OpenMP build (same results, all cores)
+_lib = ctypes.CDLL(str(_build.build(_os.environ.get("GETM_ORACLE_VARIANT", "serial"))))
 
 
 def load_variant(variant: str):

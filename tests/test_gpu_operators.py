@@ -1,8 +1,10 @@
 """Parity of the CUDA operators (called through the C ABI via the pygetm-style
 API) with the CPU oracle on identical seeded inputs.
 
-Tolerance: FP64, 1e-12 relative to the field's magnitude per call (the GPU
-contracts multiply-adds into FMAs; the oracle does not)."""
+Tolerance: FP64, 1e-12 relative to the field's magnitude per kernel call and
+1e-11 for a full 5-pass Strang split (the GPU contracts multiply-adds into
+FMAs, the oracle does not; most points agree bit for bit, and HSIMT's
+1/(1-cfl) term amplifies the last-bit differences of the rest)."""
 
 import numpy as np
 import pytest
@@ -84,7 +86,7 @@ def test_apply_3d_batch(scheme, ufirst):
                       Ah_u=None if Ah_u is None else wrap(Td.ugrid, Ah_u, False),
                       Ah_v=None if Ah_v is None else wrap(Td.vgrid, Ah_v, False))
     for a, b in zip(trd, tro):
-        close(host(a.all_values), b)
+        close(host(a.all_values), b, rtol=1e-11)
     close(host(ad.h), ao.h)
 
 
@@ -97,18 +99,21 @@ def test_vertical_substeps_and_restart():
 
     Th, To, Td, rng = setup(seed=11)
     nz = Th.nz
-    w = rng.uniform(-0.05, 0.05, (nz + 1, Th.ny_, Th.nx_))
-    w[0] = 0.0
-    w[-1] = 0.0
+    # Courant numbers up to ~4 from w_var; w moves thicknesses by up to ~20 %
+    # so some columns need more sub-steps after the first and restart
+    w = rng.uniform(-5e-4, 5e-4, (nz + 1, Th.ny_, Th.nx_))
+    w_var = rng.uniform(-0.02, 0.02, (nz + 1, Th.ny_, Th.nx_))
+    for a in (w, w_var):
+        a[0] = 0.0
+        a[-1] = 0.0
     t = rng.uniform(0.0, 1.0, (nz, Th.ny_, Th.nx_))
     for scheme in (1, 5):
         ao = O.VerticalAdvection(To, scheme)
         to = t.copy()
-        ao(w, w, 600.0, to)
+        ao(w, w_var, 600.0, to)
         ad = operators.VerticalAdvection(Td, operators.AdvectionScheme(scheme))
         td = wrap(Td, t, CENTERS)
-        wd = wrap(Td, w, INTERFACES)
-        ad(wd, wd, 600.0, td)
+        ad(wrap(Td, w, INTERFACES), wrap(Td, w_var, INTERFACES), 600.0, td)
         close(host(td.all_values), to)
         close(host(ad.h), ao.h)
     assert O._lib  # oracle loaded

@@ -57,6 +57,8 @@ class TracerCollection:
     def advance(self, timestep: float, u: Array, v: Array, w: Array, diffusivity: Array):
         """tracer.py:193-246: advection of all tracers (one fused call), then
         vertical diffusion with sources."""
+        if not self._tracers:  # the reference's per-tracer loops do nothing
+            return
         self._advection.apply_3d_batch(u, v, w, timestep, self._tracers, Ah_u=self.Ah_u, Ah_v=self.Ah_v)
         self._diffuse(timestep, diffusivity)
 

@@ -22,6 +22,7 @@ ERRORS = {
     3: "vertical advection exceeded itersmax sub-steps",
     4: "too many layers for a column kernel",
     5: "device work-buffer allocation failed",
+    6: "domain larger than the fixed scratch of an allocation-free call",
 }
 
 if not LIB_PATH.exists():
@@ -44,6 +45,7 @@ _SIGS = {
     "getm_advection_apply_3d_batch": "ppppippppppdpppips",
     "getm_advection_2d": "ppppiippppdpppps",
     "getm_advection_get_status": "ps",
+    "getm_advection_2d_noalloc": "ipppiippppdpppps",
     "getm_vertical_diffusion_create": "pp",
     "getm_vertical_diffusion_finalize": "p",
     "getm_vertical_diffusion_prepare": "piiidpddppps",

@@ -710,3 +710,120 @@ extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_gri
     }
     return GETM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the 2D advection split
+// ---------------------------------------------------------------------------
+// getm_advection_2d keeps its ping-pong buffers in a handle that allocates
+// them with cudaMalloc on first use.  Some callers cannot allow that: a host
+// model that hands all device memory to its own pool allocator at start-up
+// (a library cudaMalloc then fails or breaks the pool's accounting), and
+// drivers that must not let a library call synchronize the device (cudaMalloc
+// and cudaFree may do so implicitly).  getm_advection_2d_noalloc takes the
+// scheme instead of a handle and keeps its three work buffers (tracer
+// ping-pong copy and two column-height buffers) in one file-scope device
+// array of fixed size, so it allocates nothing.
+//
+// Limits and sharing rules:
+// * the domain may have at most GETM_NOALLOC_MAX_POINTS points including
+//   halos (nx_ * ny_); larger domains get GETM_ERR_TOO_LARGE and nothing runs;
+// * every GPU that loads the library holds the 3 * 2^20 doubles (24 MiB)
+//   until the process exits;
+// * all calls share the one array, which keeps the previous call's contents.
+//   Nothing in it has to start at zero: every pass writes all points of the
+//   buffer it produces before the next pass reads them.  Calls that overlap on
+//   the GPU (different streams, or different host threads without ordering)
+//   race on the array and corrupt each other's results;
+// * the first call on a device looks up the array's device address with
+//   cudaGetSymbolAddress (once per device, with that device current).  Make
+//   that first call before any stream capture.
+#include <mutex>
+
+#define GETM_NOALLOC_MAX_POINTS (1 << 20)
+#define GETM_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) double g_noalloc_scratch[3 * GETM_NOALLOC_MAX_POINTS];
+static double* g_noalloc_ptr[GETM_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array for the current device.
+static int noalloc_scratch(double** out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GETM_ERR_CUDA;
+    if (dev < 0 || dev >= GETM_NOALLOC_MAX_DEVICES) return GETM_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = NULL;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == NULL) return GETM_ERR_CUDA;
+        g_noalloc_ptr[dev] = (double*)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return GETM_OK;
+}
+
+extern "C" int getm_advection_2d_noalloc(int scheme, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
+                                         int ufirst, int split, const double* u, const double* v,
+                                         const double* Ah_u, const double* Ah_v, double timestep, double* D,
+                                         const double* DU, const double* DV, double* var, cudaStream_t stream)
+{
+    if (scheme < GETM_SCHEME_HSIMT || scheme > GETM_SCHEME_UPSTREAM) return GETM_ERR_ARG;
+    if (!tgrid || !D || !var || split < 1 || split > 3) return GETM_ERR_ARG;
+    const long long npoints = (long long)tgrid->nx_ * tgrid->ny_;
+    if (npoints > GETM_NOALLOC_MAX_POINTS) return GETM_ERR_TOO_LARGE;
+    getm_advection adv;  // scheme only: lives on the host stack, owns nothing
+    memset(&adv, 0, sizeof(adv));
+    adv.scheme = scheme;
+    HPassArgs ax, ay;
+    int rc = hpass_setup(ax, 1, &adv, tgrid, ugrid, 1, u, Ah_u, timestep, DU);
+    if (rc) return rc;
+    if ((rc = hpass_setup(ay, 2, &adv, tgrid, vgrid, 1, v, Ah_v, timestep, DV))) return rc;
+    double* scratch = NULL;
+    if ((rc = noalloc_scratch(&scratch))) return rc;
+    double* T = scratch;
+    double* A = scratch + GETM_NOALLOC_MAX_POINTS;
+    double* B = scratch + 2 * GETM_NOALLOC_MAX_POINTS;
+    HPassArgs* p1 = ufirst ? &ax : &ay;
+    HPassArgs* p2 = ufirst ? &ay : &ax;
+    const int d1 = ufirst ? 1 : 2, d2 = ufirst ? 2 : 1;
+    int seq_n = 0;
+    int seq_dir[4];
+    double seq_dt[4];
+    HPassArgs* seq_a[4];
+    if (split == 1) {  // FULL (operators.py:76-79)
+        seq_a[0] = p1; seq_dir[0] = d1; seq_dt[0] = timestep;
+        seq_a[1] = p2; seq_dir[1] = d2; seq_dt[1] = timestep;
+        seq_n = 2;
+    } else if (split == 2) {  // HALF (operators.py:80-85)
+        seq_a[0] = p1; seq_dir[0] = d1; seq_dt[0] = 0.5 * timestep;
+        seq_a[1] = p2; seq_dir[1] = d2; seq_dt[1] = timestep;
+        seq_a[2] = p1; seq_dir[2] = d1; seq_dt[2] = 0.5 * timestep;
+        seq_n = 3;
+    } else {  // HALF_ALWAYS (operators.py:86-93)
+        seq_a[0] = p1; seq_dir[0] = d1; seq_dt[0] = 0.5 * timestep;
+        seq_a[1] = p2; seq_dir[1] = d2; seq_dt[1] = 0.5 * timestep;
+        seq_a[2] = p2; seq_dir[2] = d2; seq_dt[2] = 0.5 * timestep;
+        seq_a[3] = p1; seq_dir[3] = d1; seq_dt[3] = 0.5 * timestep;
+        seq_n = 4;
+    }
+    const double* fin[1];
+    double* fout[1];
+    const double* hsrc = D;
+    double* fsrc = var;
+    for (int s = 0; s < seq_n; s++) {
+        double* hdst = (s == seq_n - 1) ? D : ((s % 2 == 0) ? A : B);
+        double* fdst = (fsrc == var) ? T : var;
+        seq_a[s]->dt = seq_dt[s];
+        fin[0] = fsrc;
+        fout[0] = fdst;
+        if ((rc = run_hstage(*seq_a[s], seq_dir[s], hsrc, hdst, 1, fin, fout, stream))) return rc;
+        hsrc = hdst;
+        fsrc = fdst;
+    }
+    if (fsrc != var) {
+        if (cudaMemcpyAsync(var, fsrc, (size_t)npoints * sizeof(double), cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+            return GETM_ERR_CUDA;
+    }
+    return GETM_OK;
+}

@@ -33,6 +33,7 @@ typedef struct CUstream_st* cudaStream_t;
 #define GETM_ERR_ITERS 3        /* vertical advection hit itersmax (200) sub-steps */
 #define GETM_ERR_NZ 4           /* more layers than a column kernel supports */
 #define GETM_ERR_ALLOC 5        /* device work-buffer allocation failed */
+#define GETM_ERR_TOO_LARGE 6    /* domain exceeds the fixed scratch of an allocation-free call */
 
 /* advection schemes: src/operators/advection.F90:22-30 */
 #define GETM_SCHEME_HSIMT 1
@@ -93,6 +94,20 @@ int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, g
                       int ufirst, int split, const double* u, const double* v,
                       const double* Ah_u, const double* Ah_v, double timestep, double* D,
                       const double* DU, const double* DV, double* var, cudaStream_t stream);
+/* Allocation-free 2D split.  No counterpart in the reference: it is
+ * getm_advection_2d for callers that cannot let the library call cudaMalloc
+ * (a host model whose pool allocator owns all device memory, or a driver that
+ * must not let a library call synchronize the device).  Takes the scheme
+ * instead of an advection handle and keeps its work buffers in a fixed
+ * file-scope device array: at most 1048576 points (nx_*ny_, halos included),
+ * else GETM_ERR_TOO_LARGE; 24 MiB held per GPU until exit.  All calls share
+ * that array: calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) and should come before
+ * any stream capture.                                                        */
+int getm_advection_2d_noalloc(int scheme, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
+                              int ufirst, int split, const double* u, const double* v,
+                              const double* Ah_u, const double* Ah_v, double timestep, double* D,
+                              const double* DU, const double* DV, double* var, cudaStream_t stream);
 /* Status word of the last vertical advection on this handle's stream:
  * GETM_ERR_ITERS if a column needed more than itersmax sub-steps.  Blocks
  * until the handle's pending work on `stream` is done.                      */

@@ -7,8 +7,10 @@ f = 1e-4, log-law bottom drag).  One step = one 3D (macro) time step with its
 30 2D substeps and both active tracers.  Unit of work: one cell-update = one
 interior T cell (land included) advanced by one 3D step.
 
-Our arm (default): FP64 GPU path, state resident in HBM, the two-macro-step
-sequence replayed from a CUDA graph, timed with CUDA events.  ``e2e`` repeats
+Our arm (default): the mixed-precision GPU path (``--precision fp64`` for the
+plain form; the other form is measured beside it, with the mixed form's error
+against FP64), state resident in HBM, the two-3D-step sequence replayed from
+a CUDA graph, timed with CUDA events.  ``e2e`` repeats
 the timing through the public API with the per-step surface forcing copied
 host->device from pinned memory and the surface elevation copied back.
 ``--impl reference``: the reference's CPU algorithm (the C/numpy oracle
@@ -40,6 +42,8 @@ def _args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--no-compare", action="store_true", help="skip the other precision form")
     ap.add_argument("--nx", type=int, default=400)
     ap.add_argument("--ny", type=int, default=300)
     ap.add_argument("--nz", type=int, default=40)
@@ -158,6 +162,128 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _make_sim(wl, precision, device):
+    import torch
+
+    from getm_gb300.simulation import Simulation
+
+    p = wl.params
+    sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device)
+    zc = sim.T.zc.all_values
+    temp0 = torch.where(sim.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
+                        sim.temp.all_values.double())
+    sim.temp.all_values.copy_(temp0)
+    sim.start(p["timestep"], p["split_factor"])
+    return sim
+
+
+class Runner:
+    """Warm-up, CUDA-graph capture and replay of one simulation (two 3D steps
+    per graph: the 3D momentum update alternates its u/v order each step)."""
+
+    period = 2
+
+    def __init__(self, sim, warmup, use_graph):
+        import torch
+
+        from getm_gb300 import _lib
+
+        self.sim = sim
+        split = sim.split_factor
+        for _ in range(max(warmup, 3) * split):
+            sim.advance()
+        torch.cuda.synchronize()
+        n0 = _lib.launch_count()
+        self.graph = None
+        if use_graph:
+            stream = torch.cuda.Stream()
+            stream.wait_stream(torch.cuda.current_stream())
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(stream):
+                with torch.cuda.graph(self.graph, stream=stream):
+                    for _ in range(self.period * split):
+                        sim.advance()
+            torch.cuda.current_stream().wait_stream(stream)
+            self.launches_per_period = _lib.launch_count() - n0
+            for _ in range(2):
+                self.graph.replay()
+        else:
+            for _ in range(self.period * split):
+                sim.advance()
+            self.launches_per_period = _lib.launch_count() - n0
+        torch.cuda.synchronize()
+
+    def run_period(self):
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            for _ in range(self.period * self.sim.split_factor):
+                self.sim.advance()
+
+    def timed(self, nperiods, clocks_index=None):
+        import torch
+
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(clocks_index) if clocks_index is not None else None
+        if sampler:
+            sampler.__enter__()
+        start.record()
+        for _ in range(nperiods):
+            self.run_period()
+        end.record()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__(None, None, None)
+        return start.elapsed_time(end), (sampler.summary() if sampler else None)
+
+
+def _roofline(sim, peak, peak_kind):
+    """Time the dominant kernel alone on the live state: one x-direction
+    advection pass of both tracers (hpass_x_kernel, one launch)."""
+    import torch
+
+    from getm_gb300 import _lib
+
+    T = sim.T
+    tr = sim.tracers
+    adv = tr._advection
+    u = sim.momentum.uk.all_values
+    hu = T.ugrid.hn.all_values
+    h_in = T.hn.all_values
+    h_out = torch.empty_like(h_in)
+    fin = [x.all_values for x in tr._tracers]
+    fout = [torch.empty_like(x) for x in fin]
+    sfx = "_f32" if u.dtype == torch.float32 else ""
+    pin = _lib.ptr_array([x.data_ptr() for x in fin])
+    pout = _lib.ptr_array([x.data_ptr() for x in fout])
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def launch():
+        _lib.call("getm_advection_uv_pass" + sfx, 1, T.nz, adv.p, T.handle, T.ugrid.handle, u.data_ptr(), None,
+                  0.5 * sim.macrotimestep, h_in.data_ptr(), h_out.data_ptr(), hu.data_ptr(), len(fin), pin, pout,
+                  stream)
+
+    launch()
+    torch.cuda.synchronize()
+    reps = 50
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(reps):
+        launch()
+    ev1.record()
+    torch.cuda.synchronize()
+    t_kernel = ev0.elapsed_time(ev1) / reps / 1000.0
+    n3 = h_in.numel()
+    sz = u.element_size()
+    # u, hu, h in + h out + per tracer in + out (each 3D field read or written once)
+    alg = n3 * (sz + 8 + 8 + 8 + len(fin) * 2 * sz)
+    achieved = alg / t_kernel / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": f"hpass_x_kernel<{'float' if sz == 4 else 'double'}> (2 tracers)",
+            "bytes_per_launch": alg, "us_per_launch": t_kernel * 1e6, "peak_kind": peak_kind}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -171,128 +297,95 @@ def run_ours(args):
     import __graft_entry__
 
     __graft_entry__.build()
-    from getm_gb300 import _lib, workloads
-    from getm_gb300.simulation import Simulation
+    from getm_gb300 import workloads
 
+    device = f"cuda:{local}"
     wl = workloads.seamount(nx=args.nx, ny=args.ny, nz=args.nz)
-    p = wl.params
-    split = p["split_factor"]
-    sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], device=f"cuda:{local}")
-    zc = sim.T.zc.all_values
-    sim.temp.all_values.copy_(torch.where(sim.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
-                                          sim.temp.all_values))
-    sim.start(p["timestep"], split)
-    period = 2  # the 3D momentum update alternates u/v order every 3D step
-    for _ in range(max(args.warmup, 3) * split):
-        sim.advance()
-    torch.cuda.synchronize()
+    split = wl.params["split_factor"]
+    period = Runner.period
     nsteps = args.steps + (args.steps % period)
-    graph = None
-    if not args.no_graph:
-        stream = torch.cuda.Stream()
-        stream.wait_stream(torch.cuda.current_stream())
-        n0 = _lib.launch_count()
-        graph = torch.cuda.CUDAGraph()
-        with torch.cuda.stream(stream):
-            with torch.cuda.graph(graph, stream=stream):
-                for _ in range(period * split):
-                    sim.advance()
-        torch.cuda.current_stream().wait_stream(stream)
-        launches_per_period = _lib.launch_count() - n0
-        for _ in range(2):
-            graph.replay()
-        torch.cuda.synchronize()
-    else:
-        n0 = _lib.launch_count()
-        for _ in range(period * split):
-            sim.advance()
-        launches_per_period = _lib.launch_count() - n0
+    nper = nsteps // period
+    primary = args.precision
+    forms = [primary] + ([] if args.no_compare else [f for f in ("fp64", "mixed") if f != primary])
+    runners = {f: Runner(_make_sim(wl, f, device), args.warmup, not args.no_graph) for f in forms}
 
-    def run_period():
-        if graph is not None:
-            graph.replay()
-        else:
-            for _ in range(period * split):
-                sim.advance()
+    # device-timed region for each form
+    ms = {}
+    clocks = None
+    for f in forms:
+        if ws > 1:
+            import torch.distributed as dist
 
-    # device-timed region
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.barrier()
-    torch.cuda.synchronize()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        start.record()
-        for _ in range(nsteps // period):
-            run_period()
-        end.record()
-        torch.cuda.synchronize()
-    ms = start.elapsed_time(end)
-    if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+            dist.barrier()
+        m, c = runners[f].timed(nper, clocks_index=local if f == primary else None)
+        if f == primary:
+            clocks = c
+        if ws > 1:
+            t = torch.tensor([m], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            m = float(t.item())
+        ms[f] = m
     cells = wl.cells
-    value = cells * nsteps * ws / (ms / 1000.0)
+    values = {f: cells * nsteps * ws / (ms[f] / 1000.0) for f in forms}
 
     # end to end through the public API: per 3D step, upload the surface
     # forcing (taux, tauy, sp) from pinned host memory and read back z
-    forcing = [sim.airsea.taux, sim.airsea.tauy, sim.airsea.sp]
-    host_in = [f.all_values.detach().cpu().pin_memory() for f in forcing]
-    host_out = torch.empty_like(sim.T.z.all_values, device="cpu").pin_memory()
-    h2d = sum(h.numel() * h.element_size() for h in host_in)
-    d2h = host_out.numel() * host_out.element_size()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in range(nsteps // period):
-        for _ in range(period):
-            for f, h in zip(forcing, host_in):
-                f.all_values.copy_(h, non_blocking=True)
-        run_period()
-        host_out.copy_(sim.T.z.all_values, non_blocking=True)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    e2e = {"value": cells * nsteps * ws / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h // period}
+    e2e = {}
+    for f in forms:
+        sim = runners[f].sim
+        forcing = [sim.airsea.taux, sim.airsea.tauy, sim.airsea.sp]
+        host_in = [x.all_values.detach().cpu().pin_memory() for x in forcing]
+        host_out = torch.empty(sim.T.z.all_values.shape, dtype=torch.float64).pin_memory()
+        h2d = sum(h.numel() * h.element_size() for h in host_in)
+        d2h = host_out.numel() * host_out.element_size()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(nper):
+            for _ in range(period):
+                for x, h in zip(forcing, host_in):
+                    x.all_values.copy_(h, non_blocking=True)
+            runners[f].run_period()
+            host_out.copy_(sim.T.z.all_values, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        e2e[f] = {"value": cells * nsteps * ws / dt, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
+                  "d2h_bytes_per_step": d2h // period}
 
-    # roofline of the dominant kernel: the fused tracer vertical diffusion
-    # (vd_column_kernel), timed alone on the live state
+    # error of the mixed form against FP64 (both advanced the same steps)
+    err = None
+    if "mixed" in runners and "fp64" in runners:
+        a, b = runners["mixed"].sim, runners["fp64"].sim
+        wet = torch.from_numpy(wl.T.mask == 1).to(device)
+
+        def rel(x, y):
+            x = x.double()[..., wet]
+            y = y.double()[..., wet]
+            return float((x - y).abs().max() / y.abs().max())
+
+        err = {"temp": rel(a.temp.all_values, b.temp.all_values), "salt": rel(a.salt.all_values, b.salt.all_values),
+               "z": rel(a.T.z.all_values, b.T.z.all_values), "U": rel(a.momentum.U.all_values, b.momentum.U.all_values),
+               "steps": runners[primary].sim.istep // split}
+
     peak, peak_kind = _peaks()
-    tr = sim.tracers
-    reps = 20
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    tr._diffuse(sim.macrotimestep, sim.nuh)
-    torch.cuda.synchronize()
-    ev0.record()
-    for _ in range(reps):
-        tr._diffuse(sim.macrotimestep, sim.nuh)
-    ev1.record()
-    torch.cuda.synchronize()
-    t_kernel = ev0.elapsed_time(ev1) / reps / 1000.0
-    ncol = (wl.T.nx * wl.T.ny)
-    nz = wl.T.nz
-    ntr = len(tr)
-    # algorithmic bytes: nuh (nz+1 levels), ho, hn read once; each tracer read+written
-    alg_bytes = 8 * (ncol * (nz + 1) + 2 * ncol * nz + ntr * 2 * ncol * nz)
-    achieved = alg_bytes / t_kernel / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "vd_column_kernel (2 tracers)", "peak_kind": peak_kind}
-
-    line = {"metric": "3D cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws,
-            "steps": nsteps, "warmup": max(args.warmup, 3), "ms_per_step": ms / nsteps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
+    roofline = _roofline(runners[primary].sim, peak, peak_kind)
+    r = runners[primary]
+    line = {"metric": "3D cell-updates/s", "value": values[primary], "unit": "cell-updates/s", "n_gpus": ws,
+            "steps": nsteps, "warmup": max(args.warmup, 3), "ms_per_step": ms[primary] / nsteps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if primary == "mixed" else "f64", "data": "synthetic",
             "config": {"workload": f"seamount {wl.T.nx}x{wl.T.ny}x{wl.T.nz} baroclinic split-explicit, "
-                                   f"{split} substeps per 3D step, FP64",
-                       "cells": cells, "wet_cells": wl.wet_cells, "cuda_graph": graph is not None,
+                                   f"{split} substeps per 3D step, {primary} form",
+                       "precision": primary, "cells": cells, "wet_cells": wl.wet_cells,
+                       "cuda_graph": r.graph is not None,
                        "l2": "working set (> 1 GB of 3D fields) exceeds L2; no flush needed",
                        "parallelism": f"replicas x{ws}"},
-            "e2e": e2e, "roofline": roofline, "gpu_launches": launches_per_period * (nsteps // period),
-            "clocks": clocks.summary()}
+            "e2e": e2e[primary], "roofline": roofline,
+            "gpu_launches": r.launches_per_period * nper, "clocks": clocks}
+    for f in forms:
+        if f != primary:
+            line[f] = {"value": values[f], "ms_per_step": ms[f] / nsteps, "e2e": e2e[f]["value"]}
+    if err is not None:
+        line["error_vs_fp64"] = err
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
         v, dt = cpu_reference(args, 2, threads)

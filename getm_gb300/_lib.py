@@ -46,6 +46,8 @@ _SIGS = {
     "getm_advection_2d": "ppppiippppdpppps",
     "getm_advection_get_status": "ps",
     "getm_advection_2d_noalloc": "ipppiippppdpppps",
+    "getm_advection_uv_pass": "iipppppdpppipps",
+    "getm_advection_uv_pass_f32": "iipppppdpppipps",
     "getm_vertical_diffusion_create": "pp",
     "getm_vertical_diffusion_finalize": "p",
     "getm_vertical_diffusion_prepare": "piiidpddppps",
@@ -76,6 +78,19 @@ _SIGS = {
     "getm_shchepetkin_mcwilliams": "iiiiiiipppppppppppps",
     "getm_density_buoyancy": "ippppps",
     "getm_launch_count": "p",
+    "getm_advection_apply_3d_batch_f32": "ppppippppppdpppips",
+    "getm_vertical_diffusion_batch_f32": "iiippddppipppps",
+    "getm_grid_interp_x_f32": "iiippis",
+    "getm_grid_interp_y_f32": "iiippis",
+    "getm_grid_interp_z_f32": "iiiippis",
+    "getm_grid_interp_xy_f32": "iiiiippiis",
+    "getm_collect_3d_momentum_sources_f32": "iiiiipppppppppppdpps",
+    "getm_w_momentum_3d_f32": "iiiiiiippppppppdps",
+    "getm_shear_frequency_f32": "iiiiiiipppppps",
+    "getm_reconstruct_transport_change_f32": "iiiiiiipppds",
+    "getm_blumberg_mellor_f32": "iiiiiiipppppppppps",
+    "getm_shchepetkin_mcwilliams_f32": "iiiiiiipppppppppppps",
+    "getm_density_buoyancy_f32": "ippppps",
 }
 _CT = {"i": c_int, "d": c_double, "p": c_void_p, "s": c_void_p, "c": ctypes.c_char_p}
 

@@ -13,7 +13,7 @@ import ctypes
 import torch
 
 from . import _lib
-from .core import CENTERS, INTERFACES, Array, interp_x, interp_xy, interp_y, interp_z  # noqa: F401
+from .core import CENTERS, INTERFACES, Array, _sfx, interp_x, interp_xy, interp_y, interp_z  # noqa: F401
 from ._lib import call
 
 
@@ -108,7 +108,8 @@ def collect_3d_momentum_sources(dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4)
     assert rr.grid is g and not rr.z, "rr"
     assert ea2.z == CENTERS
     assert ea4.z == CENTERS
-    call("getm_collect_3d_momentum_sources", g.nx_, g.ny_, g.nz, g.halox, g.haloy, _p(g.mask), _p(g.alpha), _p(g.ho),
+    sfx = _sfx(cor.all_values, adv.all_values, diff.all_values, idp.all_values, ea2.all_values, ea4.all_values)
+    call("getm_collect_3d_momentum_sources" + sfx, g.nx_, g.ny_, g.nz, g.halox, g.haloy, _p(g.mask), _p(g.alpha), _p(g.ho),
          _p(g.hn), _p(dp), _p(cor), _p(adv), _p(diff), _p(idp), _p(taus), _p(rr), float(dt), _p(ea2), _p(ea4), _s())
 
 
@@ -128,7 +129,7 @@ def w_momentum_3d(pk, qk, dt, w):
     assert w.z == INTERFACES, "w"
     assert pk.grid is g.ugrid and pk.z == CENTERS, "pk"
     assert qk.grid is g.vgrid and qk.z == CENTERS, "qk"
-    call("getm_w_momentum_3d", g.nx_, g.ny_, g.nz, g.halox + 1, g.halox + g.nx + 1, g.haloy + 1, g.haloy + g.ny + 1,
+    call("getm_w_momentum_3d" + _sfx(pk.all_values, qk.all_values, w.all_values), g.nx_, g.ny_, g.nz, g.halox + 1, g.halox + g.nx + 1, g.haloy + 1, g.haloy + g.ny + 1,
          _p(g.mask), _p(pk.grid.dy), _p(qk.grid.dx), _p(g.iarea), _p(g.ho), _p(g.hn), _p(pk), _p(qk), float(dt), _p(w), _s())
 
 
@@ -138,7 +139,7 @@ def shear_frequency(uk, vk, SS):
     assert SS.z == INTERFACES, "w"
     assert uk.grid is g.ugrid and uk.z == CENTERS, "uk"
     assert vk.grid is g.vgrid and vk.z == CENTERS, "vk"
-    call("getm_shear_frequency", g.nx_, g.ny_, g.nz, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+    call("getm_shear_frequency" + _sfx(uk.all_values, vk.all_values, SS.all_values), g.nx_, g.ny_, g.nz, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
          _p(g.mask), _p(uk.grid.hn), _p(vk.grid.hn), _p(uk), _p(vk), _p(SS), _s())
 
 
@@ -171,7 +172,7 @@ def reconstruct_transport_change(un, hn, Uo, timestep):
     """pyx:506-510 (hn is a raw tensor, like the reference's ndarray)"""
     g = Uo.grid
     nz = 1 if Uo.ndim == 2 else g.nz_
-    call("getm_reconstruct_transport_change", g.nx_, g.ny_, nz, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+    call("getm_reconstruct_transport_change" + _sfx(un.all_values, Uo.all_values), g.nx_, g.ny_, nz, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
          _p(un), _p(hn), _p(Uo), float(timestep), _s())
 
 
@@ -204,7 +205,7 @@ def blumberg_mellor(buoy, idpdx, idpdy):
     assert buoy.z == CENTERS, "buoy"
     assert idpdx.grid is g.ugrid and idpdx.z == CENTERS, "idpdx"
     assert idpdy.grid is g.vgrid and idpdy.z == CENTERS, "idpdy"
-    call("getm_blumberg_mellor", g.nx_, g.ny_, g.nz_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+    call("getm_blumberg_mellor" + _sfx(buoy.all_values, idpdx.all_values, idpdy.all_values), g.nx_, g.ny_, g.nz_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
          _p(idpdx.grid.mask), _p(idpdy.grid.mask), _p(idpdx.grid.idx), _p(idpdy.grid.idy), _p(idpdx.grid.hn),
          _p(idpdy.grid.hn), _p(g.zf), _p(buoy), _p(idpdx), _p(idpdy), _s())
 
@@ -222,9 +223,9 @@ def shchepetkin_mcwilliams(buoy, idpdx, idpdy, P_work=None):
     if P_work is None:
         P_work = _P_WORK.get(id(g))
         if P_work is None or P_work.shape != buoy.all_values.shape:
-            P_work = torch.zeros_like(buoy.all_values)
+            P_work = torch.zeros(buoy.all_values.shape, dtype=torch.float64, device=buoy.all_values.device)
             _P_WORK[id(g)] = P_work
-    call("getm_shchepetkin_mcwilliams", g.nx_, g.ny_, g.nz_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+    call("getm_shchepetkin_mcwilliams" + _sfx(buoy.all_values, idpdx.all_values, idpdy.all_values), g.nx_, g.ny_, g.nz_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
          _p(g.mask), _p(idpdx.grid.mask), _p(idpdy.grid.mask), _p(idpdx.grid.idx), _p(idpdy.grid.idy), _p(g.hn),
          _p(g.zin), _p(g.zc), _p(buoy), _p(idpdx), _p(idpdy), P_work.data_ptr(), _s())
 

@@ -110,24 +110,40 @@ def _stream():
     return torch.cuda.current_stream().cuda_stream
 
 
+def _sfx(*tensors):
+    """Entry-point suffix for the tensors' type: '' (FP64) or '_f32'."""
+    dt = tensors[0].dtype
+    for x in tensors[1:]:
+        if x.dtype != dt:
+            raise TypeError(f"mixed dtypes {[y.dtype for y in tensors]} in one call")
+    if dt == torch.float64:
+        return ""
+    if dt == torch.float32:
+        return "_f32"
+    raise TypeError(f"unsupported dtype {dt}")
+
+
 def interp_x(s, t, offset):
     s3 = s if s.ndim == 3 else s.unsqueeze(0)
-    _lib.call("getm_grid_interp_x", s3.shape[2], s3.shape[1], s3.shape[0], s.data_ptr(), t.data_ptr(), offset, _stream())
+    _lib.call("getm_grid_interp_x" + _sfx(s, t), s3.shape[2], s3.shape[1], s3.shape[0], s.data_ptr(), t.data_ptr(),
+              offset, _stream())
 
 
 def interp_y(s, t, offset):
     s3 = s if s.ndim == 3 else s.unsqueeze(0)
-    _lib.call("getm_grid_interp_y", s3.shape[2], s3.shape[1], s3.shape[0], s.data_ptr(), t.data_ptr(), offset, _stream())
+    _lib.call("getm_grid_interp_y" + _sfx(s, t), s3.shape[2], s3.shape[1], s3.shape[0], s.data_ptr(), t.data_ptr(),
+              offset, _stream())
 
 
 def interp_z(s, t, offset):
-    _lib.call("getm_grid_interp_z", s.shape[2], s.shape[1], s.shape[0], t.shape[0], s.data_ptr(), t.data_ptr(), offset, _stream())
+    _lib.call("getm_grid_interp_z" + _sfx(s, t), s.shape[2], s.shape[1], s.shape[0], t.shape[0], s.data_ptr(),
+              t.data_ptr(), offset, _stream())
 
 
 def interp_xy(s, t, ioffset, joffset):
     s3 = s if s.ndim == 3 else s.unsqueeze(0)
     t3 = t if t.ndim == 3 else t.unsqueeze(0)
-    _lib.call("getm_grid_interp_xy", s3.shape[2], s3.shape[1], t3.shape[2], t3.shape[1], s3.shape[0],
+    _lib.call("getm_grid_interp_xy" + _sfx(s, t), s3.shape[2], s3.shape[1], t3.shape[2], t3.shape[1], s3.shape[0],
               s.data_ptr(), t.data_ptr(), ioffset, joffset, _stream())
 
 

@@ -148,6 +148,11 @@ extern "C" int getm_advection_get_status(getm_advection* a, cudaStream_t stream)
 // ---------------------------------------------------------------------------
 // horizontal pass kernels
 // ---------------------------------------------------------------------------
+// T is the type of the advected fields and of the velocities: double for the
+// FP64 form, float for the mixed form.  Layer thicknesses, the transports QU
+// that update them and all grid metrics are double in both forms.  For
+// T = double every expression below is the FP64 reference arithmetic.
+template <typename T>
 struct HPassArgs {
     int nx_, ny_, nk;
     long long plane;            // nx_ * ny_
@@ -158,48 +163,51 @@ struct HPassArgs {
     const int* tmask;
     const double* iA;
     const double* Ah;           // 2D horizontal diffusivity on the velocity grid, or NULL
-    const double* u;            // velocity (nk layers)
+    const T* u;                 // velocity (nk layers)
     const double* hu;           // layer thickness on the velocity grid (nk layers)
     const double* h_in;
     double* h_out;
     double dt;
     int scheme;
     int ntracer;
-    const double* fin[GETM_MAX_BATCH];
-    double* fout[GETM_MAX_BATCH];
+    const T* fin[GETM_MAX_BATCH];
+    T* fout[GETM_MAX_BATCH];
 };
 
+template <typename T>
 struct FaceGeom {
-    double QU, cfl;
+    double QU;
+    T cfl;
     bool active, up, uu_ok;
 };
 
 // Face quantities that do not depend on the advected field
 // (template :63-65, :70, :77).
-__device__ __forceinline__ FaceGeom face_geom(const HPassArgs& a, long long p2, long long p3,
-                                              long long s, bool in_range)
+template <typename T>
+__device__ __forceinline__ FaceGeom<T> face_geom(const HPassArgs<T>& a, long long p2, long long p3,
+                                                 long long s, bool in_range)
 {
-    FaceGeom g;
-    g.QU = 0.0; g.cfl = 0.0; g.active = false; g.up = false; g.uu_ok = false;
+    FaceGeom<T> g;
+    g.QU = 0.0; g.cfl = T(0); g.active = false; g.up = false; g.uu_ok = false;
     if (!in_range) return g;
     int m = a.umask[p2];
     if (!getm_flux_point(m)) return g;
-    double uu = a.u[p3];
+    T uu = a.u[p3];
     g.active = true;
-    g.QU = uu * a.hu[p3] * a.dy[p2];
-    g.cfl = fabs(uu * a.dt * a.idx[p2]);
-    g.up = uu > 0;
+    g.QU = (double)uu * a.hu[p3] * a.dy[p2];
+    g.cfl = fabs(uu * (T)a.dt * (T)a.idx[p2]);
+    g.up = uu > T(0);
     g.uu_ok = getm_flux_point(g.up ? a.umask[p2 - s] : a.umask[p2 + s]);
     return g;
 }
 
 // Tracer flux through one face (template :66-104).
-__device__ __forceinline__ double face_flux(const HPassArgs& a, const FaceGeom& g,
-                                            const double* __restrict__ f, long long p2,
-                                            long long p3, long long s)
+template <typename T>
+__device__ __forceinline__ T face_flux(const HPassArgs<T>& a, const FaceGeom<T>& g, const T* __restrict__ f,
+                                       long long p2, long long p3, long long s)
 {
-    if (!g.active) return 0.0;
-    double fu, fuu, fd;
+    if (!g.active) return T(0);
+    T fu, fuu, fd;
     if (g.up) {
         fu = f[p3];
         fuu = g.uu_ok ? f[p3 - s] : fu;
@@ -209,14 +217,15 @@ __device__ __forceinline__ double face_flux(const HPassArgs& a, const FaceGeom& 
         fuu = g.uu_ok ? f[p3 + 2 * s] : fu;
         fd = f[p3];
     }
-    fu = getm_tvd_face<double>(a.scheme, fuu, fu, fd, g.cfl);
-    double flux = g.QU * fu;
-    if (a.Ah) flux = flux - a.Ah[p2] * a.hu[p3] * (f[p3 + s] - f[p3]) * a.idx[p2] * a.dy[p2];
+    fu = getm_tvd_face<T>(a.scheme, fuu, fu, fd, g.cfl);
+    T flux = (T)g.QU * fu;
+    if (a.Ah) flux = flux - (T)a.Ah[p2] * (T)a.hu[p3] * (f[p3 + s] - f[p3]) * (T)a.idx[p2] * (T)a.dy[p2];
     return flux;
 }
 
 // x-direction pass.  blockDim = (32, BYX); grid = (ceil(nx_/32), ceil(ny_*nk/BYX)).
-__global__ void __launch_bounds__(256) hpass_x_kernel(HPassArgs a)
+template <typename T>
+__global__ void __launch_bounds__(256) hpass_x_kernel(HPassArgs<T> a)
 {
     const int lane = threadIdx.x;
     const int i = blockIdx.x * 32 + lane;
@@ -229,8 +238,8 @@ __global__ void __launch_bounds__(256) hpass_x_kernel(HPassArgs a)
     const long long p3 = (long long)k * a.plane + p2;
     const bool jrow = j >= a.jlo && j <= a.jhi;
 
-    FaceGeom gr = face_geom(a, p2, p3, 1, inx && jrow && i >= a.ilo - 1 && i <= a.ihi);
-    FaceGeom gl = face_geom(a, p2 - 1, p3 - 1, 1, lane == 0 && jrow && i - 1 >= a.ilo - 1 && i - 1 <= a.ihi);
+    FaceGeom<T> gr = face_geom(a, p2, p3, 1, inx && jrow && i >= a.ilo - 1 && i <= a.ihi);
+    FaceGeom<T> gl = face_geom(a, p2 - 1, p3 - 1, 1, lane == 0 && jrow && i - 1 >= a.ilo - 1 && i - 1 <= a.ihi);
     double QUl = __shfl_up_sync(0xffffffffu, gr.QU, 1);
     if (lane == 0) QUl = gl.QU;
     const bool upd = inx && jrow && i >= a.ilo && i <= a.ihi && a.tmask[p2] == 1;
@@ -246,17 +255,17 @@ __global__ void __launch_bounds__(256) hpass_x_kernel(HPassArgs a)
         a.h_out[p3] = hnew;
     }
     for (int t = 0; t < a.ntracer; t++) {
-        const double* __restrict__ f = a.fin[t];
-        double fr = inx ? face_flux(a, gr, f, p2, p3, 1) : 0.0;
-        double fl = __shfl_up_sync(0xffffffffu, fr, 1);
+        const T* __restrict__ f = a.fin[t];
+        T fr = inx ? face_flux(a, gr, f, p2, p3, 1) : T(0);
+        T fl = __shfl_up_sync(0xffffffffu, fr, 1);
         if (lane == 0) fl = face_flux(a, gl, f, p2 - 1, p3 - 1, 1);
         if (inx) {
-            double fo = f[p3];
-            double fn = fo;
+            T fo = f[p3];
+            T fn = fo;
             if (upd) {
-                double hfo = hold * fo;
-                double advn = (fr - fl) * iA;
-                fn = (hfo - a.dt * advn) / hnew;
+                T hfo = (T)hold * fo;
+                T advn = (fr - fl) * (T)iA;
+                fn = (hfo - (T)a.dt * advn) / (T)hnew;
             }
             a.fout[t][p3] = fn;
         }
@@ -264,10 +273,11 @@ __global__ void __launch_bounds__(256) hpass_x_kernel(HPassArgs a)
 }
 
 // y-direction pass.  blockDim = (32, GETM_V_BY); grid = (ceil(nx_/32), ceil(ny_/BY), nk).
-__global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs a)
+template <typename T>
+__global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs<T> a)
 {
     __shared__ double sQ[GETM_V_BY][32];
-    __shared__ double sF[GETM_V_BY][32];
+    __shared__ T sF[GETM_V_BY][32];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i = blockIdx.x * 32 + tx;
     const int j = blockIdx.y * GETM_V_BY + ty;
@@ -278,8 +288,8 @@ __global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs a)
     const long long p3 = (long long)k * a.plane + p2;
     const bool icol = i >= a.ilo && i <= a.ihi;
 
-    FaceGeom gt = face_geom(a, p2, p3, s, in && icol && j >= a.jlo - 1 && j <= a.jhi);
-    FaceGeom gb = face_geom(a, p2 - s, p3 - s, s, in && ty == 0 && icol && j - 1 >= a.jlo - 1 && j - 1 <= a.jhi);
+    FaceGeom<T> gt = face_geom(a, p2, p3, s, in && icol && j >= a.jlo - 1 && j <= a.jhi);
+    FaceGeom<T> gb = face_geom(a, p2 - s, p3 - s, s, in && ty == 0 && icol && j - 1 >= a.jlo - 1 && j - 1 <= a.jhi);
     sQ[ty][tx] = gt.QU;
     __syncthreads();
     double QUb = ty > 0 ? sQ[ty - 1][tx] : gb.QU;
@@ -296,37 +306,38 @@ __global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs a)
         a.h_out[p3] = hnew;
     }
     for (int t = 0; t < a.ntracer; t++) {
-        const double* __restrict__ f = a.fin[t];
-        double ft = in ? face_flux(a, gt, f, p2, p3, s) : 0.0;
-        double fb = (ty == 0 && in) ? face_flux(a, gb, f, p2 - s, p3 - s, s) : 0.0;
+        const T* __restrict__ f = a.fin[t];
+        T ft = in ? face_flux(a, gt, f, p2, p3, s) : T(0);
+        T fb = (ty == 0 && in) ? face_flux(a, gb, f, p2 - s, p3 - s, s) : T(0);
         __syncthreads();  // previous tracer's reads of sF are done
         sF[ty][tx] = ft;
         __syncthreads();
         if (ty > 0) fb = sF[ty - 1][tx];
         if (in) {
-            double fo = f[p3];
-            double fn = fo;
+            T fo = f[p3];
+            T fn = fo;
             if (upd) {
-                double hfo = hold * fo;
-                double advn = (ft - fb) * iA;
-                fn = (hfo - a.dt * advn) / hnew;
+                T hfo = (T)hold * fo;
+                T advn = (ft - fb) * (T)iA;
+                fn = (hfo - (T)a.dt * advn) / (T)hnew;
             }
             a.fout[t][p3] = fn;
         }
     }
 }
 
-static int launch_hpass(int direction, HPassArgs& a, cudaStream_t stream)
+template <typename T>
+static int launch_hpass(int direction, HPassArgs<T>& a, cudaStream_t stream)
 {
     if (direction == 1) {
         const int BY = 8;
         dim3 block(32, BY);
         dim3 grid(getm_div_up(a.nx_, 32), getm_div_up((long long)a.ny_ * a.nk, BY));
-        hpass_x_kernel<<<grid, block, 0, stream>>>(a);
+        hpass_x_kernel<T><<<grid, block, 0, stream>>>(a);
     } else {
         dim3 block(32, GETM_V_BY);
         dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, GETM_V_BY), a.nk);
-        hpass_y_kernel<<<grid, block, 0, stream>>>(a);
+        hpass_y_kernel<T><<<grid, block, 0, stream>>>(a);
     }
     GETM_CHECK_LAUNCH();
     return GETM_OK;
@@ -335,9 +346,9 @@ static int launch_hpass(int direction, HPassArgs& a, cudaStream_t stream)
 // Fill the direction-dependent fields of HPassArgs from the grid handles
 // (wrapper.F90:240-253: direction 1 passes ugrid mask/idx/dy, 2 passes vgrid
 // mask/dx/idy).
-static int hpass_setup(HPassArgs& a, int direction, const getm_advection* adv,
-                       const getm_grid* tg, const getm_grid* vg, int nk, const double* u,
-                       const double* Ah, double dt, const double* hu)
+template <typename T>
+static int hpass_setup(HPassArgs<T>& a, int direction, const getm_advection* adv, const getm_grid* tg,
+                       const getm_grid* vg, int nk, const T* u, const double* Ah, double dt, const double* hu)
 {
     if (!tg || !vg || !u || !hu) return GETM_ERR_ARG;
     if (tg->halox < 2 || tg->haloy < 2) return GETM_ERR_ARG;
@@ -357,8 +368,9 @@ static int hpass_setup(HPassArgs& a, int direction, const getm_advection* adv,
 }
 
 // Run one horizontal stage for ntracer tracers, chunked by GETM_MAX_BATCH.
-static int run_hstage(HPassArgs& a, int direction, const double* h_in, double* h_out, int ntracer,
-                      const double* const* fin, double* const* fout, cudaStream_t stream)
+template <typename T>
+static int run_hstage(HPassArgs<T>& a, int direction, const double* h_in, double* h_out, int ntracer,
+                      const T* const* fin, T* const* fout, cudaStream_t stream)
 {
     a.h_in = h_in; a.h_out = h_out;
     int done = 0;
@@ -367,7 +379,7 @@ static int run_hstage(HPassArgs& a, int direction, const double* h_in, double* h
         if (n > GETM_MAX_BATCH) n = GETM_MAX_BATCH;
         a.ntracer = n;
         for (int t = 0; t < n; t++) { a.fin[t] = fin[done + t]; a.fout[t] = fout[done + t]; }
-        int rc = launch_hpass(direction, a, stream);
+        int rc = launch_hpass<T>(direction, a, stream);
         if (rc) return rc;
         done += n;
     } while (done < ntracer);
@@ -377,50 +389,51 @@ static int run_hstage(HPassArgs& a, int direction, const double* h_in, double* h
 // ---------------------------------------------------------------------------
 // vertical pass (template w3d :223-374)
 // ---------------------------------------------------------------------------
+template <typename T>
 struct WPassArgs {
     int nx_, ny_, nz;
     long long plane;
     int ilo, ihi, jlo, jhi;
     const int* tmask;
-    const double* w;            // nz+1 levels
+    const T* w;                 // nz+1 levels
     const double* h_in;         // layer thickness at stage start (not modified)
     double* h_out;              // layer thickness after the pass (last tracer's)
     double* haux;               // column work arrays for sub-stepping (nz levels)
-    double* faux;
+    T* faux;
     double dt;
     int scheme;
     int ntracer;
     int* status;
-    const double* wvar[GETM_MAX_BATCH];
-    double* f[GETM_MAX_BATCH];  // updated in place
+    const T* wvar[GETM_MAX_BATCH];
+    T* f[GETM_MAX_BATCH];       // updated in place
 };
 
 // One sub-step over a column: reads (hs, fs) levels 0..nz-1 (C), writes
-// (hd, fd).  hs == hd / fs == fd (in place) is allowed: every level is read
-// into the register window before it is overwritten.  When cfl_from_h is
-// false the per-interface Courant numbers are recomputed from w_var and hs
-// exactly as cfl0 (template :274) - the caller passes use0 = true for it == 1
-// where cfls = cfl0 and hs is the original thickness, so both coincide.
-__device__ void w_substep(const WPassArgs& a, long long c, const double* wv, const double* hs,
-                          const double* fs, double* hd, double* fdst, double dtk, double itersm1)
+// (hd, fdst).  hs == hd / fs == fdst (in place) is allowed: every level is
+// read into the register window before it is overwritten.  The Courant number
+// |w_var| dt / min(h) * itersm1 equals cfls(k)*itersm1 of the reference
+// (cfls = |w_var| dt / min(haux), haux = the sub-step's start thickness).
+template <typename T>
+__device__ void w_substep(const WPassArgs<T>& a, long long c, const T* wv, const double* hs, const T* fs,
+                          double* hd, T* fdst, double dtk, double itersm1)
 {
     const long long P = a.plane;
     const int nz = a.nz;
-    // window of old values
-    double fkm1 = 0.0, fk = fs[c], fk1 = (nz > 1) ? fs[c + P] : 0.0;
+    T fkm1 = T(0), fk = fs[c], fk1 = (nz > 1) ? fs[c + P] : T(0);
     double hk = hs[c], hk1 = (nz > 1) ? hs[c + P] : 0.0;
-    double fluxm = 0.0;  // flux(k-1), flux(0) = 0
-    double wkm1 = a.w[c];
+    T fluxm = T(0);  // flux(k-1), flux(0) = 0
+    T wkm1 = a.w[c];
     for (int k = 0; k < nz; k++) {
         // flux through the interface above C level k (Fortran interface k+1)
-        double flux = 0.0;
-        double fk2 = 0.0, hk2 = 0.0;
+        T flux = T(0);
+        T fk2 = T(0);
+        double hk2 = 0.0;
         if (k + 2 < nz) { fk2 = fs[c + (k + 2) * P]; hk2 = hs[c + (k + 2) * P]; }
         if (k < nz - 1) {
-            double wvk = wv[c + (k + 1) * P];
-            double cfl = fabs(wvk) * a.dt / fmin(hk, hk1) * itersm1;
-            double fu, fuu, fdn;
-            if (wvk > 0) {
+            T wvk = wv[c + (k + 1) * P];
+            T cfl = fabs(wvk) * (T)a.dt / (T)fmin(hk, hk1) * (T)itersm1;
+            T fu, fuu, fdn;
+            if (wvk > T(0)) {
                 fu = fk;
                 fuu = (k > 0) ? fkm1 : fu;
                 fdn = fk1;
@@ -429,15 +442,15 @@ __device__ void w_substep(const WPassArgs& a, long long c, const double* wv, con
                 fuu = (k < nz - 2) ? fk2 : fu;
                 fdn = fk;
             }
-            fu = getm_tvd_face<double>(a.scheme, fuu, fu, fdn, cfl);
+            fu = getm_tvd_face<T>(a.scheme, fuu, fu, fdn, cfl);
             flux = wvk * fu;
         }
-        double wk = a.w[c + (k + 1) * P];
-        double hfo = hk * fk;
-        double hn = hk - dtk * (wk - wkm1);
-        double advn = flux - fluxm;
+        T wk = a.w[c + (k + 1) * P];
+        T hfo = (T)hk * fk;
+        double hn = hk - dtk * ((double)wk - (double)wkm1);
+        T advn = flux - fluxm;
         hd[c + k * P] = hn;
-        fdst[c + k * P] = (hfo - dtk * advn) / hn;
+        fdst[c + k * P] = (hfo - (T)dtk * advn) / (T)hn;
         // shift window
         fluxm = flux; wkm1 = wk;
         fkm1 = fk; fk = fk1; fk1 = fk2;
@@ -447,18 +460,19 @@ __device__ void w_substep(const WPassArgs& a, long long c, const double* wv, con
 
 // Largest Courant number over the interior interfaces of a column
 // (template :274, :294, :300).  Returns -1 when nz == 1 (no interfaces).
-__device__ double w_maxcfl(const WPassArgs& a, long long c, const double* wv, const double* hs)
+template <typename T>
+__device__ double w_maxcfl(const WPassArgs<T>& a, long long c, const T* wv, const double* hs)
 {
     const long long P = a.plane;
-    double cmax = -1.0;
+    T cmax = T(-1);
     double hk = hs[c];
     for (int k = 1; k < a.nz; k++) {
         double hk1 = hs[c + k * P];
-        double cfl = fabs(wv[c + k * P]) * a.dt / fmin(hk, hk1);
+        T cfl = fabs(wv[c + k * P]) * (T)a.dt / (T)fmin(hk, hk1);
         if (k == 1 || cfl > cmax) cmax = cfl;
         hk = hk1;
     }
-    return cmax;
+    return (double)cmax;
 }
 
 __device__ __forceinline__ int w_iters_from(double cfl)
@@ -468,10 +482,9 @@ __device__ __forceinline__ int w_iters_from(double cfl)
     return c > 1e9 ? 1000000000 : (int)c;
 }
 
-// Thread per column.  Note: the Courant number inside w_substep is
-// |w_var| dt / min(h) * itersm1 which equals cfls(k)*itersm1 of the reference
-// (cfls = |w_var| dt / min(haux) with haux = the sub-step's start thickness).
-__global__ void __launch_bounds__(128) wpass_kernel(WPassArgs a)
+// Thread per column.
+template <typename T>
+__global__ void __launch_bounds__(128) wpass_kernel(WPassArgs<T> a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
@@ -480,16 +493,15 @@ __global__ void __launch_bounds__(128) wpass_kernel(WPassArgs a)
     if (a.tmask[c] != 1) return;
     const int itersmax = 200;
     const long long P = a.plane;
-    int last_iters = 1;
     for (int t = 0; t < a.ntracer; t++) {
-        const double* wv = a.wvar[t];
-        double* f = a.f[t];
+        const T* wv = a.wvar[t];
+        T* f = a.f[t];
         int iters = 1;
         double itersm1 = 1.0, dtk = a.dt;
         int it = 1;
         while (it <= iters) {
             const double* hs = (it == 1) ? a.h_in : a.haux;
-            const double* fs = (it == 1) ? f : a.faux;
+            const T* fs = (it == 1) ? f : a.faux;
             if (iters < itersmax) {
                 int iters_new = w_iters_from(w_maxcfl(a, c, wv, hs));
                 if (iters_new > iters) {
@@ -506,20 +518,19 @@ __global__ void __launch_bounds__(128) wpass_kernel(WPassArgs a)
             }
             // The last sub-step writes the tracer in place and the thickness
             // into haux (the stage's h_in must survive for the next tracer).
-            double* fd = (it == iters) ? f : a.faux;
+            T* fd = (it == iters) ? f : a.faux;
             w_substep(a, c, wv, hs, fs, a.haux, fd, dtk, itersm1);
             it++;
         }
-        last_iters = iters;
     }
-    (void)last_iters;
     // h after the pass = thickness of the last tracer's final sub-step
     for (int k = 0; k < a.nz; k++) a.h_out[c + k * P] = a.haux[c + k * P];
 }
 
 // Copy h_in -> h_out for the columns the w pass does not touch, so h_out is a
 // complete field (ping-pong buffers must be fully written).
-__global__ void copy_untouched_kernel(WPassArgs a)
+template <typename T>
+__global__ void copy_untouched_kernel(WPassArgs<T> a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
@@ -530,18 +541,18 @@ __global__ void copy_untouched_kernel(WPassArgs a)
     for (int k = 0; k < a.nz; k++) a.h_out[c + k * a.plane] = a.h_in[c + k * a.plane];
 }
 
-static int run_wstage(getm_advection* adv, const getm_grid* tg, const double* w,
-                      const double* const* wvar, double dt, const double* h_in, double* h_out,
-                      int ntracer, double* const* f, cudaStream_t stream)
+template <typename T>
+static int run_wstage(getm_advection* adv, const getm_grid* tg, const T* w, const T* const* wvar, double dt,
+                      const double* h_in, double* h_out, int ntracer, T* const* f, cudaStream_t stream)
 {
-    WPassArgs a;
+    WPassArgs<T> a;
     memset(&a, 0, sizeof(a));
     a.nx_ = tg->nx_; a.ny_ = tg->ny_; a.nz = tg->kmax - tg->kmin + 1;
     a.plane = (long long)tg->nx_ * tg->ny_;
     a.ilo = tg->halox; a.ihi = tg->halox + (tg->imax - tg->imin);
     a.jlo = tg->haloy; a.jhi = tg->haloy + (tg->jmax - tg->jmin);
     a.tmask = tg->mask; a.w = w; a.dt = dt; a.scheme = adv->scheme; a.status = adv->status;
-    a.haux = adv->colbuf[0]; a.faux = adv->colbuf[1];
+    a.haux = adv->colbuf[0]; a.faux = (T*)adv->colbuf[1];
     if (a.nz < 1) return GETM_ERR_ARG;
     dim3 block(128);
     dim3 grid(getm_div_up(a.nx_, 128), a.ny_);
@@ -553,12 +564,63 @@ static int run_wstage(getm_advection* adv, const getm_grid* tg, const double* w,
         a.ntracer = n;
         a.h_in = h_in; a.h_out = h_out;
         for (int t = 0; t < n; t++) { a.wvar[t] = wvar[done + t]; a.f[t] = f[done + t]; }
-        wpass_kernel<<<grid, block, 0, stream>>>(a);
+        wpass_kernel<T><<<grid, block, 0, stream>>>(a);
         GETM_CHECK_LAUNCH();
         done += n;
     } while (done < ntracer);
-    copy_untouched_kernel<<<grid, block, 0, stream>>>(a);
+    copy_untouched_kernel<T><<<grid, block, 0, stream>>>(a);
     GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// Fused Strang split for either form (see getm_advection_apply_3d_batch).
+template <typename T>
+static int apply_3d_batch_impl(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
+                               int ufirst, const T* u, const T* v, const T* w, const T* const* w_var,
+                               const double* Ah_u, const double* Ah_v, double timestep, double* h,
+                               const double* hu, const double* hv, int ntracer, T* const* vars,
+                               cudaStream_t stream)
+{
+    if (!adv) return GETM_OK;
+    if (!tgrid || !w || !h || ntracer < 1 || !vars) return GETM_ERR_ARG;
+    const int nz = tgrid->kmax - tgrid->kmin + 1;
+    HPassArgs<T> ax, ay;
+    int rc = hpass_setup<T>(ax, 1, adv, tgrid, ugrid, nz, u, Ah_u, 0.5 * timestep, hu);
+    if (rc) return rc;
+    if ((rc = hpass_setup<T>(ay, 2, adv, tgrid, vgrid, nz, v, Ah_v, 0.5 * timestep, hv))) return rc;
+    const size_t n3 = (size_t)ax.plane * nz;
+    if ((rc = adv_reserve(adv, n3, ntracer))) return rc;
+
+    const T* wv[GETM_MAX_BATCH * 8];
+    const T* fin[GETM_MAX_BATCH * 8];
+    T* fout[GETM_MAX_BATCH * 8];
+    T* tmp[GETM_MAX_BATCH * 8];
+    for (int t = 0; t < ntracer; t++) {
+        wv[t] = (w_var && w_var[t]) ? w_var[t] : w;
+        tmp[t] = (T*)adv->tmp[t];
+    }
+
+    HPassArgs<T>* first = ufirst ? &ax : &ay;
+    const int dfirst = ufirst ? 1 : 2;
+    HPassArgs<T>* second = ufirst ? &ay : &ax;
+    const int dsecond = ufirst ? 2 : 1;
+    double* A = adv->hbuf[0];
+    double* B = adv->hbuf[1];
+
+    // adv1(dt/2): vars -> tmp, h -> A   (operators.py:165-170)
+    for (int t = 0; t < ntracer; t++) { fin[t] = vars[t]; fout[t] = tmp[t]; }
+    if ((rc = run_hstage<T>(*first, dfirst, h, A, ntracer, fin, fout, stream))) return rc;
+    // adv2(dt/2): tmp -> vars, A -> B   (:171-175)
+    for (int t = 0; t < ntracer; t++) { fin[t] = tmp[t]; fout[t] = vars[t]; }
+    if ((rc = run_hstage<T>(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
+    // w(dt): vars in place, B -> A      (:176-182)
+    if ((rc = run_wstage<T>(adv, tgrid, w, wv, timestep, B, A, ntracer, vars, stream))) return rc;
+    // adv2(dt/2): vars -> tmp, A -> B   (:183-188)
+    for (int t = 0; t < ntracer; t++) { fin[t] = vars[t]; fout[t] = tmp[t]; }
+    if ((rc = run_hstage<T>(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
+    // adv1(dt/2): tmp -> vars, B -> h   (:189-193)
+    for (int t = 0; t < ntracer; t++) { fin[t] = tmp[t]; fout[t] = vars[t]; }
+    if ((rc = run_hstage<T>(*first, dfirst, B, h, ntracer, fin, fout, stream))) return rc;
     return GETM_OK;
 }
 
@@ -572,7 +634,7 @@ extern "C" int getm_advection_uv_calculate(int direction, int nk, getm_advection
 {
     if (!adv) return GETM_OK;  // wrapper.F90:227 returns silently without a scheme
     if ((direction != 1 && direction != 2) || nk < 1 || !h || !var) return GETM_ERR_ARG;
-    HPassArgs a;
+    HPassArgs<double> a;
     int rc = hpass_setup(a, direction, adv, tgrid, ugrid, nk, u, Ah, timestep, hu);
     if (rc) return rc;
     const size_t n3 = (size_t)a.plane * nk;
@@ -598,7 +660,7 @@ extern "C" int getm_advection_w_calculate(getm_advection* adv, getm_grid* tgrid,
     if (rc) return rc;
     const double* wv[1] = {w_var};
     double* f[1] = {var};
-    if ((rc = run_wstage(adv, tgrid, w, wv, timestep, h, adv->hbuf[0], 1, f, stream))) return rc;
+    if ((rc = run_wstage<double>(adv, tgrid, w, wv, timestep, h, adv->hbuf[0], 1, f, stream))) return rc;
     if (cudaMemcpyAsync(h, adv->hbuf[0], n3 * sizeof(double), cudaMemcpyDeviceToDevice, stream) != cudaSuccess) return GETM_ERR_CUDA;
     return GETM_OK;
 }
@@ -611,44 +673,54 @@ extern "C" int getm_advection_apply_3d_batch(getm_advection* adv, getm_grid* tgr
                                              const double* hu, const double* hv, int ntracer,
                                              double* const* vars, cudaStream_t stream)
 {
-    if (!adv) return GETM_OK;
-    if (!tgrid || !w || !h || ntracer < 1 || !vars) return GETM_ERR_ARG;
-    const int nz = tgrid->kmax - tgrid->kmin + 1;
-    HPassArgs ax, ay;
-    int rc = hpass_setup(ax, 1, adv, tgrid, ugrid, nz, u, Ah_u, 0.5 * timestep, hu);
+    return apply_3d_batch_impl<double>(adv, tgrid, ugrid, vgrid, ufirst, u, v, w, w_var, Ah_u, Ah_v, timestep, h,
+                                       hu, hv, ntracer, vars, stream);
+}
+
+extern "C" int getm_advection_apply_3d_batch_f32(getm_advection* adv, getm_grid* tgrid,
+                                                 getm_grid* ugrid, getm_grid* vgrid, int ufirst,
+                                                 const float* u, const float* v, const float* w,
+                                                 const float* const* w_var, const double* Ah_u,
+                                                 const double* Ah_v, double timestep, double* h,
+                                                 const double* hu, const double* hv, int ntracer,
+                                                 float* const* vars, cudaStream_t stream)
+{
+    return apply_3d_batch_impl<float>(adv, tgrid, ugrid, vgrid, ufirst, u, v, w, w_var, Ah_u, Ah_v, timestep, h,
+                                      hu, hv, ntracer, vars, stream);
+}
+
+template <typename T>
+static int uv_pass_impl(int direction, int nk, getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
+                        const T* u, const double* Ah, double timestep, const double* h_in, double* h_out,
+                        const double* hu, int ntracer, const T* const* fin, T* const* fout, cudaStream_t stream)
+{
+    if (!adv || (direction != 1 && direction != 2) || nk < 1 || !h_in || !h_out || ntracer < 0) return GETM_ERR_ARG;
+    if (ntracer > 0 && (!fin || !fout)) return GETM_ERR_ARG;
+    if (h_in == h_out) return GETM_ERR_ARG;
+    for (int t = 0; t < ntracer; t++)
+        if (!fin[t] || !fout[t] || (const void*)fin[t] == (const void*)fout[t]) return GETM_ERR_ARG;
+    HPassArgs<T> a;
+    int rc = hpass_setup<T>(a, direction, adv, tgrid, ugrid, nk, u, Ah, timestep, hu);
     if (rc) return rc;
-    if ((rc = hpass_setup(ay, 2, adv, tgrid, vgrid, nz, v, Ah_v, 0.5 * timestep, hv))) return rc;
-    const size_t n3 = (size_t)ax.plane * nz;
-    if ((rc = adv_reserve(adv, n3, ntracer))) return rc;
+    return run_hstage<T>(a, direction, h_in, h_out, ntracer, fin, fout, stream);
+}
 
-    const double* wv[GETM_MAX_BATCH * 8];
-    const double* fin[GETM_MAX_BATCH * 8];
-    double* fout[GETM_MAX_BATCH * 8];
-    for (int t = 0; t < ntracer; t++) wv[t] = (w_var && w_var[t]) ? w_var[t] : w;
+extern "C" int getm_advection_uv_pass(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
+                                      getm_grid* ugrid, const double* u, const double* Ah, double timestep,
+                                      const double* h_in, double* h_out, const double* hu, int ntracer,
+                                      const double* const* var_in, double* const* var_out, cudaStream_t stream)
+{
+    return uv_pass_impl<double>(direction, nk, adv, tgrid, ugrid, u, Ah, timestep, h_in, h_out, hu, ntracer, var_in,
+                                var_out, stream);
+}
 
-    HPassArgs* first = ufirst ? &ax : &ay;
-    const int dfirst = ufirst ? 1 : 2;
-    HPassArgs* second = ufirst ? &ay : &ax;
-    const int dsecond = ufirst ? 2 : 1;
-    double* A = adv->hbuf[0];
-    double* B = adv->hbuf[1];
-    double* const* tmp = adv->tmp;
-
-    // adv1(dt/2): vars -> tmp, h -> A   (operators.py:165-170)
-    for (int t = 0; t < ntracer; t++) { fin[t] = vars[t]; fout[t] = tmp[t]; }
-    if ((rc = run_hstage(*first, dfirst, h, A, ntracer, fin, fout, stream))) return rc;
-    // adv2(dt/2): tmp -> vars, A -> B   (:171-175)
-    for (int t = 0; t < ntracer; t++) { fin[t] = tmp[t]; fout[t] = vars[t]; }
-    if ((rc = run_hstage(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
-    // w(dt): vars in place, B -> A      (:176-182)
-    if ((rc = run_wstage(adv, tgrid, w, wv, timestep, B, A, ntracer, vars, stream))) return rc;
-    // adv2(dt/2): vars -> tmp, A -> B   (:183-188)
-    for (int t = 0; t < ntracer; t++) { fin[t] = vars[t]; fout[t] = tmp[t]; }
-    if ((rc = run_hstage(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
-    // adv1(dt/2): tmp -> vars, B -> h   (:189-193)
-    for (int t = 0; t < ntracer; t++) { fin[t] = tmp[t]; fout[t] = vars[t]; }
-    if ((rc = run_hstage(*first, dfirst, B, h, ntracer, fin, fout, stream))) return rc;
-    return GETM_OK;
+extern "C" int getm_advection_uv_pass_f32(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
+                                          getm_grid* ugrid, const float* u, const double* Ah, double timestep,
+                                          const double* h_in, double* h_out, const double* hu, int ntracer,
+                                          const float* const* var_in, float* const* var_out, cudaStream_t stream)
+{
+    return uv_pass_impl<float>(direction, nk, adv, tgrid, ugrid, u, Ah, timestep, h_in, h_out, hu, ntracer, var_in,
+                               var_out, stream);
 }
 
 extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
@@ -659,14 +731,14 @@ extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_gri
 {
     if (!adv) return GETM_OK;
     if (!D || !var || split < 1 || split > 3) return GETM_ERR_ARG;
-    HPassArgs ax, ay;
+    HPassArgs<double> ax, ay;
     int rc = hpass_setup(ax, 1, adv, tgrid, ugrid, 1, u, Ah_u, timestep, DU);
     if (rc) return rc;
     if ((rc = hpass_setup(ay, 2, adv, tgrid, vgrid, 1, v, Ah_v, timestep, DV))) return rc;
     const size_t n2 = (size_t)ax.plane;
     if ((rc = adv_reserve(adv, n2, 1))) return rc;
-    HPassArgs* p1 = ufirst ? &ax : &ay;
-    HPassArgs* p2 = ufirst ? &ay : &ax;
+    HPassArgs<double>* p1 = ufirst ? &ax : &ay;
+    HPassArgs<double>* p2 = ufirst ? &ay : &ax;
     const int d1 = ufirst ? 1 : 2, d2 = ufirst ? 2 : 1;
     double* T = adv->tmp[0];
     double* A = adv->hbuf[0];
@@ -677,7 +749,7 @@ extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_gri
     int seq_n = 0;
     int seq_dir[4];
     double seq_dt[4];
-    HPassArgs* seq_a[4];
+    HPassArgs<double>* seq_a[4];
     if (split == 1) {          // FULL: adv1(dt), adv2(dt)
         seq_a[0] = p1; seq_dir[0] = d1; seq_dt[0] = timestep;
         seq_a[1] = p2; seq_dir[1] = d2; seq_dt[1] = timestep;
@@ -775,7 +847,7 @@ extern "C" int getm_advection_2d_noalloc(int scheme, getm_grid* tgrid, getm_grid
     getm_advection adv;  // scheme only: lives on the host stack, owns nothing
     memset(&adv, 0, sizeof(adv));
     adv.scheme = scheme;
-    HPassArgs ax, ay;
+    HPassArgs<double> ax, ay;
     int rc = hpass_setup(ax, 1, &adv, tgrid, ugrid, 1, u, Ah_u, timestep, DU);
     if (rc) return rc;
     if ((rc = hpass_setup(ay, 2, &adv, tgrid, vgrid, 1, v, Ah_v, timestep, DV))) return rc;
@@ -784,13 +856,13 @@ extern "C" int getm_advection_2d_noalloc(int scheme, getm_grid* tgrid, getm_grid
     double* T = scratch;
     double* A = scratch + GETM_NOALLOC_MAX_POINTS;
     double* B = scratch + 2 * GETM_NOALLOC_MAX_POINTS;
-    HPassArgs* p1 = ufirst ? &ax : &ay;
-    HPassArgs* p2 = ufirst ? &ay : &ax;
+    HPassArgs<double>* p1 = ufirst ? &ax : &ay;
+    HPassArgs<double>* p2 = ufirst ? &ay : &ax;
     const int d1 = ufirst ? 1 : 2, d2 = ufirst ? 2 : 1;
     int seq_n = 0;
     int seq_dir[4];
     double seq_dt[4];
-    HPassArgs* seq_a[4];
+    HPassArgs<double>* seq_a[4];
     if (split == 1) {  // FULL (operators.py:76-79)
         seq_a[0] = p1; seq_dir[0] = d1; seq_dt[0] = timestep;
         seq_a[1] = p2; seq_dir[1] = d2; seq_dt[1] = timestep;

@@ -23,38 +23,41 @@ extern "C" int getm_launch_count(unsigned long long* count)
 }
 
 // ---------------------------------------------------------------------------
-// interpolation.F90:9-72
+// interpolation.F90:9-72 (T: double for the FP64 form, float for the mixed form)
 // ---------------------------------------------------------------------------
-__global__ void interp_x_kernel(int nx, int ny, int nz, const double* s, double* t, int ioff)
+template <typename T>
+__global__ void interp_x_kernel(int nx, int ny, int nz, const T* s, T* t, int ioff)
 {
     long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long n = (long long)nx * ny * nz;
     if (p >= n) return;
     int i = (int)(p % nx);
     if (i >= nx - 1) return;
-    t[p + ioff] = 0.5 * (s[p] + s[p + 1]);
+    t[p + ioff] = T(0.5) * (s[p] + s[p + 1]);
 }
 
-__global__ void interp_y_kernel(int nx, int ny, int nz, const double* s, double* t, int joff)
+template <typename T>
+__global__ void interp_y_kernel(int nx, int ny, int nz, const T* s, T* t, int joff)
 {
     long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long n = (long long)nx * ny * nz;
     if (p >= n) return;
     int j = (int)((p / nx) % ny);
     if (j >= ny - 1) return;
-    t[p + (long long)joff * nx] = 0.5 * (s[p] + s[p + nx]);
+    t[p + (long long)joff * nx] = T(0.5) * (s[p] + s[p + nx]);
 }
 
-__global__ void interp_z_kernel(int nx, int ny, int nz1, const double* s, double* t, int koff)
+template <typename T>
+__global__ void interp_z_kernel(int nx, int ny, int nz1, const T* s, T* t, int koff)
 {
     long long plane = (long long)nx * ny;
     long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= plane * (nz1 - 1)) return;
-    t[p + koff * plane] = 0.5 * (s[p] + s[p + plane]);
+    t[p + koff * plane] = T(0.5) * (s[p] + s[p + plane]);
 }
 
-__global__ void interp_xy_kernel(int nx1, int ny1, int nx2, int ny2, int nz, const double* s,
-                                 double* t, int ioff, int joff)
+template <typename T>
+__global__ void interp_xy_kernel(int nx1, int ny1, int nx2, int ny2, int nz, const T* s, T* t, int ioff, int joff)
 {
     long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long n = (long long)(nx1 - 1) * (ny1 - 1) * nz;
@@ -64,49 +67,99 @@ __global__ void interp_xy_kernel(int nx1, int ny1, int nx2, int ny2, int nz, con
     int j = (int)(r % (ny1 - 1));
     int k = (int)(r / (ny1 - 1));
     long long q = ((long long)k * ny1 + j) * nx1 + i;
-    t[((long long)k * ny2 + j + joff) * nx2 + i + ioff] = 0.25 * (s[q] + s[q + 1] + s[q + nx1] + s[q + nx1 + 1]);
+    t[((long long)k * ny2 + j + joff) * nx2 + i + ioff] = T(0.25) * (s[q] + s[q + 1] + s[q + nx1] + s[q + nx1 + 1]);
 }
 
-extern "C" int getm_grid_interp_x(int nx, int ny, int nz, const double* source, double* target,
-                                  int ioffset, cudaStream_t stream)
+template <typename T>
+static int interp_x_impl(int nx, int ny, int nz, const T* source, T* target, int ioffset, cudaStream_t stream)
 {
     if (nx < 1 || ny < 1 || nz < 1 || !source || !target) return GETM_ERR_ARG;
     long long n = (long long)nx * ny * nz;
-    interp_x_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, source, target, ioffset);
+    interp_x_kernel<T><<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, source, target, ioffset);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
 
-extern "C" int getm_grid_interp_y(int nx, int ny, int nz, const double* source, double* target,
-                                  int joffset, cudaStream_t stream)
+template <typename T>
+static int interp_y_impl(int nx, int ny, int nz, const T* source, T* target, int joffset, cudaStream_t stream)
 {
     if (nx < 1 || ny < 1 || nz < 1 || !source || !target) return GETM_ERR_ARG;
     long long n = (long long)nx * ny * nz;
-    interp_y_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, source, target, joffset);
+    interp_y_kernel<T><<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, source, target, joffset);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
 
-extern "C" int getm_grid_interp_z(int nx, int ny, int nz1, int nz2, const double* source,
-                                  double* target, int koffset, cudaStream_t stream)
+template <typename T>
+static int interp_z_impl(int nx, int ny, int nz1, int nz2, const T* source, T* target, int koffset,
+                         cudaStream_t stream)
 {
     if (nx < 1 || ny < 1 || nz1 < 1 || nz2 < 1 || !source || !target) return GETM_ERR_ARG;
     if (nz1 < 2) return GETM_OK;
     long long n = (long long)nx * ny * (nz1 - 1);
-    interp_z_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz1, source, target, koffset);
+    interp_z_kernel<T><<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz1, source, target, koffset);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
 
-extern "C" int getm_grid_interp_xy(int nx1, int ny1, int nx2, int ny2, int nz, const double* source,
-                                   double* target, int ioffset, int joffset, cudaStream_t stream)
+template <typename T>
+static int interp_xy_impl(int nx1, int ny1, int nx2, int ny2, int nz, const T* source, T* target, int ioffset,
+                          int joffset, cudaStream_t stream)
 {
     if (nx1 < 1 || ny1 < 1 || nx2 < 1 || ny2 < 1 || nz < 1 || !source || !target) return GETM_ERR_ARG;
     if (nx1 < 2 || ny1 < 2) return GETM_OK;
     long long n = (long long)(nx1 - 1) * (ny1 - 1) * nz;
-    interp_xy_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx1, ny1, nx2, ny2, nz, source, target, ioffset, joffset);
+    interp_xy_kernel<T><<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx1, ny1, nx2, ny2, nz, source, target, ioffset, joffset);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
+}
+
+extern "C" int getm_grid_interp_x(int nx, int ny, int nz, const double* source, double* target, int ioffset,
+                                  cudaStream_t stream)
+{
+    return interp_x_impl<double>(nx, ny, nz, source, target, ioffset, stream);
+}
+
+extern "C" int getm_grid_interp_y(int nx, int ny, int nz, const double* source, double* target, int joffset,
+                                  cudaStream_t stream)
+{
+    return interp_y_impl<double>(nx, ny, nz, source, target, joffset, stream);
+}
+
+extern "C" int getm_grid_interp_z(int nx, int ny, int nz1, int nz2, const double* source, double* target,
+                                  int koffset, cudaStream_t stream)
+{
+    return interp_z_impl<double>(nx, ny, nz1, nz2, source, target, koffset, stream);
+}
+
+extern "C" int getm_grid_interp_xy(int nx1, int ny1, int nx2, int ny2, int nz, const double* source, double* target,
+                                   int ioffset, int joffset, cudaStream_t stream)
+{
+    return interp_xy_impl<double>(nx1, ny1, nx2, ny2, nz, source, target, ioffset, joffset, stream);
+}
+
+extern "C" int getm_grid_interp_x_f32(int nx, int ny, int nz, const float* source, float* target, int ioffset,
+                                      cudaStream_t stream)
+{
+    return interp_x_impl<float>(nx, ny, nz, source, target, ioffset, stream);
+}
+
+extern "C" int getm_grid_interp_y_f32(int nx, int ny, int nz, const float* source, float* target, int joffset,
+                                      cudaStream_t stream)
+{
+    return interp_y_impl<float>(nx, ny, nz, source, target, joffset, stream);
+}
+
+extern "C" int getm_grid_interp_z_f32(int nx, int ny, int nz1, int nz2, const float* source, float* target,
+                                      int koffset, cudaStream_t stream)
+{
+    return interp_z_impl<float>(nx, ny, nz1, nz2, source, target, koffset, stream);
+}
+
+extern "C" int getm_grid_interp_xy_f32(int nx1, int ny1, int nx2, int ny2, int nz, const float* source,
+                                       float* target, int ioffset, int joffset, cudaStream_t stream)
+{
+    return interp_xy_impl<float>(nx1, ny1, nx2, ny2, nz, source, target, ioffset, joffset, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -77,12 +77,14 @@ extern "C" int getm_bottom_friction(int nx, int ny, const int* mask, const doubl
     return GETM_OK;
 }
 
-// momentum.F90:103-145: rows haloy..ny-haloy-1, every i, every k (mask unused)
+// momentum.F90:103-145: rows haloy..ny-haloy-1, every i, every k (mask unused).
+// T: type of the 3D source fields and of ea2/ea4; the sum is formed in FP64.
+template <typename T>
 __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const double* alpha,
                                        const double* ho, const double* hn, const double* dp,
-                                       const double* cor, const double* adv, const double* diff,
-                                       const double* idp, const double* taus, const double* rr,
-                                       double dt, double* ea2, double* ea4)
+                                       const T* cor, const T* adv, const T* diff,
+                                       const T* idp, const double* taus, const double* rr,
+                                       double dt, T* ea2, T* ea4)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + haloy;
@@ -93,11 +95,25 @@ __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const 
     const double rho0i = 1.0 / GETM_RHO0;
     for (int k = 0; k < nz; k++) {
         long long q = p + k * plane;
-        double e = dt * (-0.5 * (ho[q] + hn[q]) * GETM_G * dpp + al * (cor[q] + adv[q] + diff[q] + idp[q]));
+        double e = dt * (-0.5 * (ho[q] + hn[q]) * GETM_G * dpp
+                         + al * ((double)cor[q] + (double)adv[q] + (double)diff[q] + (double)idp[q]));
         if (k == nz - 1) e = e + dt * al * taus[p] * rho0i;
-        ea4[q] = e;
+        ea4[q] = (T)e;
     }
-    ea2[p] = -dt * rr[p];
+    ea2[p] = (T)(-dt * rr[p]);
+}
+
+template <typename T>
+static int collect_impl(int nx, int ny, int nz, int haloy, const double* alpha, const double* ho, const double* hn,
+                        const double* dp, const T* cor, const T* adv, const T* diff, const T* idp,
+                        const double* taus, const double* rr, double dt, T* ea2, T* ea4, cudaStream_t stream)
+{
+    if (nx < 1 || ny <= 2 * haloy || nz < 1 || !alpha || !ho || !hn || !dp || !cor || !adv || !diff || !idp || !taus || !rr || !ea2 || !ea4)
+        return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), ny - 2 * haloy);
+    collect_sources_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, haloy, alpha, ho, hn, dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 extern "C" int getm_collect_3d_momentum_sources(int nx, int ny, int nz, int halox, int haloy,
@@ -108,12 +124,18 @@ extern "C" int getm_collect_3d_momentum_sources(int nx, int ny, int nz, int halo
                                                 double* ea2, double* ea4, cudaStream_t stream)
 {
     (void)mask; (void)halox;
-    if (nx < 1 || ny <= 2 * haloy || nz < 1 || !alpha || !ho || !hn || !dp || !cor || !adv || !diff || !idp || !taus || !rr || !ea2 || !ea4)
-        return GETM_ERR_ARG;
-    dim3 grid(getm_div_up(nx, 128), ny - 2 * haloy);
-    collect_sources_kernel<<<grid, 128, 0, stream>>>(nx, ny, nz, haloy, alpha, ho, hn, dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4);
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
+    return collect_impl<double>(nx, ny, nz, haloy, alpha, ho, hn, dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4, stream);
+}
+
+extern "C" int getm_collect_3d_momentum_sources_f32(int nx, int ny, int nz, int halox, int haloy,
+                                                    const int* mask, const double* alpha, const double* ho,
+                                                    const double* hn, const double* dp, const float* cor,
+                                                    const float* adv, const float* diff, const float* idp,
+                                                    const double* taus, const double* rr, double dt,
+                                                    float* ea2, float* ea4, cudaStream_t stream)
+{
+    (void)mask; (void)halox;
+    return collect_impl<float>(nx, ny, nz, haloy, alpha, ho, hn, dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4, stream);
 }
 
 // momentum.F90:147-189
@@ -152,11 +174,13 @@ extern "C" int getm_advance_2d_transport(int nx, int ny, int halox, int haloy, c
     return GETM_OK;
 }
 
-// momentum.F90:191-216: thread per column
+// momentum.F90:191-216: thread per column; the recursion runs in FP64 for
+// both forms (T: type of pk, qk and w).
+template <typename T>
 __global__ void w_momentum_3d_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
                                      const int* mask, const double* dyu, const double* dxv,
                                      const double* iarea, const double* ho, const double* hn,
-                                     const double* pk, const double* qk, double dt, double* w)
+                                     const T* pk, const T* qk, double dt, T* w)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;
@@ -166,12 +190,26 @@ __global__ void w_momentum_3d_kernel(int nx, int ny, int nz, int ilo, int ihi, i
     long long plane = (long long)nx * ny;
     const double idt = 1.0 / dt;
     const double dyE = dyu[p], dyW = dyu[p - 1], dxN = dxv[p], dxS = dxv[p - nx], ia = iarea[p];
-    double wk = w[p];
+    double wk = (double)w[p];
     for (int k = 1; k <= nz - 1; k++) {
         long long q = p + (k - 1) * plane;
-        wk = wk - (hn[q] - ho[q]) * idt - (pk[q] * dyE - pk[q - 1] * dyW + qk[q] * dxN - qk[q - nx] * dxS) * ia;
-        w[p + k * plane] = wk;
+        wk = wk - (hn[q] - ho[q]) * idt
+             - ((double)pk[q] * dyE - (double)pk[q - 1] * dyW + (double)qk[q] * dxN - (double)qk[q - nx] * dxS) * ia;
+        w[p + k * plane] = (T)wk;
     }
+}
+
+template <typename T>
+static int w_momentum_impl(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* mask,
+                           const double* dyu, const double* dxv, const double* iarea, const double* ho,
+                           const double* hn, const T* pk, const T* qk, double dt, T* w, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !dyu || !dxv || !iarea || !ho || !hn || !pk || !qk || !w) return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1);
+    w_momentum_3d_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, dyu, dxv, iarea, ho, hn, pk, qk, dt, w);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 extern "C" int getm_w_momentum_3d(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
@@ -180,18 +218,23 @@ extern "C" int getm_w_momentum_3d(int nx, int ny, int nz, int imin, int imax, in
                                   const double* pk, const double* qk, double dt, double* w,
                                   cudaStream_t stream)
 {
-    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
-    if (!mask || !dyu || !dxv || !iarea || !ho || !hn || !pk || !qk || !w) return GETM_ERR_ARG;
-    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1);
-    w_momentum_3d_kernel<<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, dyu, dxv, iarea, ho, hn, pk, qk, dt, w);
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
+    return w_momentum_impl<double>(nx, ny, nz, imin, imax, jmin, jmax, mask, dyu, dxv, iarea, ho, hn, pk, qk, dt, w, stream);
 }
 
-// momentum.F90:218-241
+extern "C" int getm_w_momentum_3d_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                      const int* mask, const double* dyu, const double* dxv,
+                                      const double* iarea, const double* ho, const double* hn,
+                                      const float* pk, const float* qk, double dt, float* w,
+                                      cudaStream_t stream)
+{
+    return w_momentum_impl<float>(nx, ny, nz, imin, imax, jmin, jmax, mask, dyu, dxv, iarea, ho, hn, pk, qk, dt, w, stream);
+}
+
+// momentum.F90:218-241 (T: type of uk, vk, SS and of the arithmetic)
+template <typename T>
 __global__ void shear_frequency_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
                                        const int* mask, const double* hu, const double* hv,
-                                       const double* uk, const double* vk, double* SS)
+                                       const T* uk, const T* vk, T* SS)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;
@@ -201,24 +244,38 @@ __global__ void shear_frequency_kernel(int nx, int ny, int nz, int ilo, int ihi,
     if (mask[p] <= 0) return;
     long long plane = (long long)nx * ny;
     long long a = p + (k - 1) * plane, b = p + k * plane;
-    double t1 = (uk[b] - uk[a]) / (0.5 * (hu[b] + hu[a]));
-    double t2 = (uk[b - 1] - uk[a - 1]) / (0.5 * (hu[b - 1] + hu[a - 1]));
-    double t3 = (vk[b] - vk[a]) / (0.5 * (hv[b] + hv[a]));
-    double t4 = (vk[b - nx] - vk[a - nx]) / (0.5 * (hv[b - nx] + hv[a - nx]));
-    SS[b] = 0.5 * (t1 * t1 + t2 * t2 + t3 * t3 + t4 * t4);
+    T t1 = (uk[b] - uk[a]) / (T(0.5) * ((T)hu[b] + (T)hu[a]));
+    T t2 = (uk[b - 1] - uk[a - 1]) / (T(0.5) * ((T)hu[b - 1] + (T)hu[a - 1]));
+    T t3 = (vk[b] - vk[a]) / (T(0.5) * ((T)hv[b] + (T)hv[a]));
+    T t4 = (vk[b - nx] - vk[a - nx]) / (T(0.5) * ((T)hv[b - nx] + (T)hv[a - nx]));
+    SS[b] = T(0.5) * (t1 * t1 + t2 * t2 + t3 * t3 + t4 * t4);
+}
+
+template <typename T>
+static int shear_impl(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* mask,
+                      const double* hu, const double* hv, const T* uk, const T* vk, T* SS, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !hu || !hv || !uk || !vk || !SS) return GETM_ERR_ARG;
+    if (nz < 2) return GETM_OK;
+    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1, nz - 1);
+    shear_frequency_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, hu, hv, uk, vk, SS);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 extern "C" int getm_shear_frequency(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
                                     const int* mask, const double* hu, const double* hv, const double* uk,
                                     const double* vk, double* SS, cudaStream_t stream)
 {
-    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
-    if (!mask || !hu || !hv || !uk || !vk || !SS) return GETM_ERR_ARG;
-    if (nz < 2) return GETM_OK;
-    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1, nz - 1);
-    shear_frequency_kernel<<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, hu, hv, uk, vk, SS);
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
+    return shear_impl<double>(nx, ny, nz, imin, imax, jmin, jmax, mask, hu, hv, uk, vk, SS, stream);
+}
+
+extern "C" int getm_shear_frequency_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                        const int* mask, const double* hu, const double* hv, const float* uk,
+                                        const float* vk, float* SS, cudaStream_t stream)
+{
+    return shear_impl<float>(nx, ny, nz, imin, imax, jmin, jmax, mask, hu, hv, uk, vk, SS, stream);
 }
 
 // momentum.F90:270-284
@@ -285,16 +342,28 @@ extern "C" int getm_bottom_shear_velocity(int nx, int ny, int imin, int imax, in
     return GETM_OK;
 }
 
-// momentum.F90:323-340: rows jmin..jmax, every i
-__global__ void reconstruct_kernel(int nx, int ny, int nz, int jlo, int jhi, double* un, const double* hn,
-                                   const double* Uo, double idt)
+// momentum.F90:323-340: rows jmin..jmax, every i (T: type of un and Uo)
+template <typename T>
+__global__ void reconstruct_kernel(int nx, int ny, int nz, int jlo, int jhi, T* un, const double* hn,
+                                   const T* Uo, double idt)
 {
     long long plane = (long long)nx * ny;
     long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= plane * nz) return;
     int j = (int)((p % plane) / nx);
     if (j < jlo || j > jhi) return;
-    un[p] = (un[p] * hn[p] - Uo[p]) * idt;
+    un[p] = (un[p] * (T)hn[p] - Uo[p]) * (T)idt;
+}
+
+template <typename T>
+static int reconstruct_impl(int nx, int ny, int nz, int jmin, int jmax, T* un, const double* hn, const T* Uo,
+                            double timestep, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || jmin < 1 || jmax > ny || !un || !hn || !Uo) return GETM_ERR_ARG;
+    long long n = (long long)nx * ny * nz;
+    reconstruct_kernel<T><<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, jmin - 1, jmax - 1, un, hn, Uo, 1.0 / timestep);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 extern "C" int getm_reconstruct_transport_change(int nx, int ny, int nz, int imin, int imax, int jmin,
@@ -302,11 +371,15 @@ extern "C" int getm_reconstruct_transport_change(int nx, int ny, int nz, int imi
                                                  double timestep, cudaStream_t stream)
 {
     (void)imin; (void)imax;
-    if (nx < 1 || ny < 1 || nz < 1 || jmin < 1 || jmax > ny || !un || !hn || !Uo) return GETM_ERR_ARG;
-    long long n = (long long)nx * ny * nz;
-    reconstruct_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(nx, ny, nz, jmin - 1, jmax - 1, un, hn, Uo, 1.0 / timestep);
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
+    return reconstruct_impl<double>(nx, ny, nz, jmin, jmax, un, hn, Uo, timestep, stream);
+}
+
+extern "C" int getm_reconstruct_transport_change_f32(int nx, int ny, int nz, int imin, int imax, int jmin,
+                                                     int jmax, float* un, const double* hn, const float* Uo,
+                                                     double timestep, cudaStream_t stream)
+{
+    (void)imin; (void)imax;
+    return reconstruct_impl<float>(nx, ny, nz, jmin, jmax, un, hn, Uo, timestep, stream);
 }
 
 // wrapper.F90:275-393 (one layer per blockIdx.z).  All six grids share the

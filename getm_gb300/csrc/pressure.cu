@@ -16,11 +16,12 @@
 // ---------------------------------------------------------------------------
 // Blumberg & Mellor
 // ---------------------------------------------------------------------------
+// T: type of buoyancy and of the gradients; the integration runs in FP64.
+template <typename T>
 __global__ void blumberg_mellor_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
                                        const int* umask, const int* vmask, const double* idxu,
                                        const double* idyv, const double* hu, const double* hv,
-                                       const double* zf, const double* buoy, double* idpdx,
-                                       double* idpdy)
+                                       const double* zf, const T* buoy, T* idpdx, T* idpdy)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;
@@ -34,27 +35,40 @@ __global__ void blumberg_mellor_kernel(int nx, int ny, int nz, int ilo, int ihi,
         const long long s = dir ? nx : 1;
         const double id = dir ? idyv[p] : idxu[p];
         const double* hh = dir ? hv : hu;
-        double* out = dir ? idpdy : idpdx;
+        T* out = dir ? idpdy : idpdx;
         long long q = p + (long long)(nz - 1) * P;
-        double grdl = (buoy[q + s] - buoy[q]) * id;
-        double buoyl = 0.5 * (buoy[q + s] + buoy[q]);
+        double grdl = ((double)buoy[q + s] - (double)buoy[q]) * id;
+        double buoyl = 0.5 * ((double)buoy[q + s] + (double)buoy[q]);
         double hk1 = hh[q];
         double prgr = grdl * 0.5 * hk1;
-        out[q] = hk1 * prgr;
+        out[q] = (T)(hk1 * prgr);
         for (int k = nz - 1; k >= 1; k--) {
             q = p + (long long)(k - 1) * P;
             double grdu = grdl;
-            grdl = (buoy[q + s] - buoy[q]) * id;
+            grdl = ((double)buoy[q + s] - (double)buoy[q]) * id;
             double buoyu = buoyl;
-            buoyl = 0.5 * (buoy[q + s] + buoy[q]);
+            buoyl = 0.5 * ((double)buoy[q + s] + (double)buoy[q]);
             long long qf = p + (long long)k * P;
             double dxz = (zf[qf + s] - zf[qf]) * id;
             double hk = hh[q];
             prgr = prgr + 0.5 * (grdu + grdl) * 0.5 * (hk + hk1) - dxz * (buoyu - buoyl);
-            out[q] = hk * prgr;
+            out[q] = (T)(hk * prgr);
             hk1 = hk;
         }
     }
+}
+
+template <typename T>
+static int bm_impl(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* umask,
+                   const int* vmask, const double* idxu, const double* idyv, const double* hu, const double* hv,
+                   const double* zf, const T* buoy, T* idpdx, T* idpdy, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 1 || jmin < 1 || imax >= nx || jmax >= ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!umask || !vmask || !idxu || !idyv || !hu || !hv || !zf || !buoy || !idpdx || !idpdy) return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1);
+    blumberg_mellor_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask, idxu, idyv, hu, hv, zf, buoy, idpdx, idpdy);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 extern "C" int getm_blumberg_mellor(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
@@ -63,12 +77,16 @@ extern "C" int getm_blumberg_mellor(int nx, int ny, int nz, int imin, int imax, 
                                     const double* zf, const double* buoy, double* idpdx, double* idpdy,
                                     cudaStream_t stream)
 {
-    if (nx < 1 || ny < 1 || nz < 1 || imin < 1 || jmin < 1 || imax >= nx || jmax >= ny || jmax < jmin) return GETM_ERR_ARG;
-    if (!umask || !vmask || !idxu || !idyv || !hu || !hv || !zf || !buoy || !idpdx || !idpdy) return GETM_ERR_ARG;
-    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1);
-    blumberg_mellor_kernel<<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask, idxu, idyv, hu, hv, zf, buoy, idpdx, idpdy);
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
+    return bm_impl<double>(nx, ny, nz, imin, imax, jmin, jmax, umask, vmask, idxu, idyv, hu, hv, zf, buoy, idpdx, idpdy, stream);
+}
+
+extern "C" int getm_blumberg_mellor_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                        const int* umask, const int* vmask, const double* idxu,
+                                        const double* idyv, const double* hu, const double* hv,
+                                        const double* zf, const float* buoy, float* idpdx, float* idpdy,
+                                        cudaStream_t stream)
+{
+    return bm_impl<float>(nx, ny, nz, imin, imax, jmin, jmax, umask, vmask, idxu, idyv, hu, hv, zf, buoy, idpdx, idpdy, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -77,17 +95,19 @@ extern "C" int getm_blumberg_mellor(int nx, int ny, int nz, int imin, int imax, 
 #define SMCW_EPS 1.e-10
 
 // Harmonic mean with the cut-off of internal_pressure.F90:93-98.
-__device__ __forceinline__ double smcw_harm_cut(double a, double b)
+template <typename T>
+__device__ __forceinline__ T smcw_harm_cut(T a, T b)
 {
-    double cff = 2.0 * a * b;
-    return (cff > SMCW_EPS) ? cff / (a + b) : 0.0;
+    T cff = T(2) * a * b;
+    return (cff > T(SMCW_EPS)) ? cff / (a + b) : T(0);
 }
 
 // Phase 1 (internal_pressure.F90:80-118): column pressure integral P.
 // Columns with mask > 0 over C i in [ilo, ihi+1], j in [jlo, jhi+1].
+template <typename T>
 __global__ void smcw_column_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
                                    const int* mask, const double* h, const double* zc,
-                                   const double* buoy, double* Pw)
+                                   const T* buoy, double* Pw)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;
@@ -96,7 +116,7 @@ __global__ void smcw_column_kernel(int nx, int ny, int nz, int ilo, int ihi, int
     const long long p = (long long)j * nx + i;
     if (mask[p] <= 0) return;
     const double x = 1.0 / 12.0;
-#define B(k) buoy[p + (long long)((k) - 1) * P]
+#define B(k) ((double)buoy[p + (long long)((k) - 1) * P])
 #define Z(k) zc[p + (long long)((k) - 1) * P]
     // Fortran levels 1..nz.  Raw differences d(k) = v(k+1) - v(k), k = 1..nz-1,
     // d(nz) = d(nz-1), d(0) = d(1); harmonic HR(k) from d(k), d(k-1).
@@ -109,7 +129,7 @@ __global__ void smcw_column_kernel(int nx, int ny, int nz, int ilo, int ihi, int
     double bk1 = B(nz), zk1 = Z(nz);          // v(k+1)
     double bk = B(nz - 1), zk = Z(nz - 1);    // v(k)
     double dRk = bk1 - bk, dZk = zk1 - zk;    // d(k) with k = nz-1
-    double HR1 = smcw_harm_cut(dRk, dRk);     // HR(nz): d(nz) = d(nz-1)
+    double HR1 = smcw_harm_cut<double>(dRk, dRk);     // HR(nz): d(nz) = d(nz-1)
     double HZ1 = 2.0 * dZk * dZk / (dZk + dZk);
     for (int k = nz - 1; k >= 1; k--) {
         // d(k-1): for k == 1 it is d(0) = d(1)
@@ -120,7 +140,7 @@ __global__ void smcw_column_kernel(int nx, int ny, int nz, int ilo, int ihi, int
         } else {
             dRm = dRk; dZm = dZk;
         }
-        double HR0 = smcw_harm_cut(dRk, dRm);   // HR(k)
+        double HR0 = smcw_harm_cut<double>(dRk, dRm);   // HR(k)
         double HZ0 = 2.0 * dZk * dZm / (dZk + dZm);
         Pk = Pk + 0.5 * ((bk1 + bk) * (zk1 - zk) - 0.2 * ((HR1 - HR0) * (zk1 - zk - x * (HZ1 + HZ0))
                   - (HZ1 - HZ0) * (bk1 - bk - x * (HR1 + HR0))));
@@ -134,12 +154,15 @@ __global__ void smcw_column_kernel(int nx, int ny, int nz, int ilo, int ihi, int
 #undef Z
 }
 
-// Phase 2 (internal_pressure.F90:120-216) for one direction (s = 1: x, s = nx: y).
+// Phase 2 (internal_pressure.F90:120-216), both directions (s = 1: x,
+// s = nx: y).  T: type of buoyancy, of the gradients and of the slope
+// arithmetic; height and pressure differences are formed in FP64 first.
+template <typename T>
 __global__ void smcw_gradient_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
                                      const int* umask, const int* vmask, const double* idxu,
                                      const double* idyv, const double* h, const double* z,
-                                     const double* zc, const double* buoy, const double* Pw,
-                                     double* idpdx, double* idpdy)
+                                     const double* zc, const T* buoy, const double* Pw,
+                                     T* idpdx, T* idpdy)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;
@@ -149,27 +172,47 @@ __global__ void smcw_gradient_kernel(int nx, int ny, int nz, int ilo, int ihi, i
     const long long p = (long long)j * nx + i;
     const long long q = p + (long long)k * P;
     const long long qtop = p + (long long)(nz - 1) * P;
-    const double x = 1.0 / 12.0;
+    const T x = T(1.0) / T(12.0);
     for (int dir = 0; dir < 2; dir++) {
         const int* m = dir ? vmask : umask;
         if (m[p] != 1) continue;
         const long long s = dir ? nx : 1;
         // raw differences at p, p+s, p+2s (Fortran i, i+1, i+2), each gated
         // by the mask of the velocity point just before it
-        double rZ0 = 0.0, rR0 = 0.0, rZ1 = 0.0, rR1 = 0.0, rZ2 = 0.0, rR2 = 0.0;
-        if (m[p - s] > 0) { rZ0 = zc[q] - zc[q - s]; rR0 = buoy[q] - buoy[q - s]; }
-        if (m[p] > 0) { rZ1 = zc[q + s] - zc[q]; rR1 = buoy[q + s] - buoy[q]; }
-        if (m[p + s] > 0) { rZ2 = zc[q + 2 * s] - zc[q + s]; rR2 = buoy[q + 2 * s] - buoy[q + s]; }
-        double dZx0 = smcw_harm_cut(rZ0, rZ1), dZx1 = smcw_harm_cut(rZ1, rZ2);
-        double dRx0 = smcw_harm_cut(rR0, rR1), dRx1 = smcw_harm_cut(rR1, rR2);
-        double FC = 0.5 * ((buoy[q + s] + buoy[q]) * (zc[q + s] - zc[q])
-                    - 0.2 * ((dRx1 - dRx0) * (zc[q + s] - zc[q] - x * (dZx1 + dZx0))
-                    - (dZx1 - dZx0) * (buoy[q + s] - buoy[q] - x * (dRx1 + dRx0))));
+        T rZ0 = T(0), rR0 = T(0), rZ1 = T(0), rR1 = T(0), rZ2 = T(0), rR2 = T(0);
+        if (m[p - s] > 0) { rZ0 = (T)(zc[q] - zc[q - s]); rR0 = buoy[q] - buoy[q - s]; }
+        if (m[p] > 0) { rZ1 = (T)(zc[q + s] - zc[q]); rR1 = buoy[q + s] - buoy[q]; }
+        if (m[p + s] > 0) { rZ2 = (T)(zc[q + 2 * s] - zc[q + s]); rR2 = buoy[q + 2 * s] - buoy[q + s]; }
+        T dZx0 = smcw_harm_cut<T>(rZ0, rZ1), dZx1 = smcw_harm_cut<T>(rZ1, rZ2);
+        T dRx0 = smcw_harm_cut<T>(rR0, rR1), dRx1 = smcw_harm_cut<T>(rR1, rR2);
+        T dzc = (T)(zc[q + s] - zc[q]);
+        T FC = T(0.5) * ((buoy[q + s] + buoy[q]) * dzc
+               - T(0.2) * ((dRx1 - dRx0) * (dzc - x * (dZx1 + dZx0))
+               - (dZx1 - dZx0) * (buoy[q + s] - buoy[q] - x * (dRx1 + dRx0))));
         double id = dir ? idyv[p] : idxu[p];
-        double* out = dir ? idpdy : idpdx;
-        out[q] = 0.5 * (h[q] + h[q + s]) * id
-                 * (Pw[q + s] - Pw[q] + FC - (z[p + s] - z[p]) * 0.5 * (buoy[qtop + s] + buoy[qtop]));
+        T* out = dir ? idpdy : idpdx;
+        out[q] = (T)(0.5 * (h[q] + h[q + s]) * id)
+                 * ((T)(Pw[q + s] - Pw[q]) + FC - (T)(z[p + s] - z[p]) * T(0.5) * (buoy[qtop + s] + buoy[qtop]));
     }
+}
+
+template <typename T>
+static int smcw_impl(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* mask,
+                     const int* umask, const int* vmask, const double* idxu, const double* idyv, const double* h,
+                     const double* z, const double* zc, const T* buoy, T* idpdx, T* idpdy, double* P_work,
+                     cudaStream_t stream)
+{
+    // the stencil reaches i+2 / j+2 of the last interior point
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax + 2 > nx || jmax + 2 > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !umask || !vmask || !idxu || !idyv || !h || !z || !zc || !buoy || !idpdx || !idpdy || !P_work)
+        return GETM_ERR_ARG;
+    dim3 g1(getm_div_up(nx, 128), jmax - jmin + 2);
+    smcw_column_kernel<T><<<g1, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, h, zc, buoy, P_work);
+    GETM_CHECK_LAUNCH();
+    dim3 g2(getm_div_up(nx, 128), jmax - jmin + 1, nz);
+    smcw_gradient_kernel<T><<<g2, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask, idxu, idyv, h, z, zc, buoy, P_work, idpdx, idpdy);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 extern "C" int getm_shchepetkin_mcwilliams(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
@@ -179,15 +222,17 @@ extern "C" int getm_shchepetkin_mcwilliams(int nx, int ny, int nz, int imin, int
                                            double* idpdx, double* idpdy, double* P_work,
                                            cudaStream_t stream)
 {
-    // the stencil reaches i+2 / j+2 of the last interior point
-    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax + 2 > nx || jmax + 2 > ny || jmax < jmin) return GETM_ERR_ARG;
-    if (!mask || !umask || !vmask || !idxu || !idyv || !h || !z || !zc || !buoy || !idpdx || !idpdy || !P_work)
-        return GETM_ERR_ARG;
-    dim3 g1(getm_div_up(nx, 128), jmax - jmin + 2);
-    smcw_column_kernel<<<g1, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, h, zc, buoy, P_work);
-    GETM_CHECK_LAUNCH();
-    dim3 g2(getm_div_up(nx, 128), jmax - jmin + 1, nz);
-    smcw_gradient_kernel<<<g2, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask, idxu, idyv, h, z, zc, buoy, P_work, idpdx, idpdy);
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
+    return smcw_impl<double>(nx, ny, nz, imin, imax, jmin, jmax, mask, umask, vmask, idxu, idyv, h, z, zc, buoy,
+                             idpdx, idpdy, P_work, stream);
+}
+
+extern "C" int getm_shchepetkin_mcwilliams_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                               const int* mask, const int* umask, const int* vmask,
+                                               const double* idxu, const double* idyv, const double* h,
+                                               const double* z, const double* zc, const float* buoy,
+                                               float* idpdx, float* idpdy, double* P_work,
+                                               cudaStream_t stream)
+{
+    return smcw_impl<float>(nx, ny, nz, imin, imax, jmin, jmax, mask, umask, vmask, idxu, idyv, h, z, zc, buoy,
+                            idpdx, idpdy, P_work, stream);
 }

@@ -29,43 +29,47 @@ struct getm_vertical_diffusion {
     double* auxn;
 };
 
+// T: type of the diffused fields, of nuh and of the solve (double: FP64 form;
+// float: mixed form).  Layer thicknesses are double in both forms.
+template <typename T>
 struct VDArgs {
     int nx_, ny_, nz;
     long long plane;
     const int* mask;
-    const double* nuh;     // nz+1 interface levels
+    const T* nuh;          // nz+1 interface levels
     const double* ho;
     const double* hn;
-    const double* auxo;    // when prepared separately (else NULL)
+    const double* auxo;    // FP64 form, when prepared separately (else NULL)
     const double* auxn;
     double dt, cnpar;
     int ntracer;
     double molecular[VD_MAX_BATCH];
-    double* var[VD_MAX_BATCH];
-    const double* ea2[VD_MAX_BATCH];
-    const double* ea4[VD_MAX_BATCH];
+    T* var[VD_MAX_BATCH];
+    const T* ea2[VD_MAX_BATCH];
+    const T* ea4[VD_MAX_BATCH];
 };
 
 // Coupling coefficients of the interface above C level k (between levels k and
 // k+1): diffusion.F90:166-168 with Fortran k = C k + 1.
-__device__ __forceinline__ void vd_aux(const VDArgs& a, long long c, int k, double mol,
-                                       double& auxo, double& auxn)
+template <typename T>
+__device__ __forceinline__ void vd_aux(const VDArgs<T>& a, long long c, int k, double mol, T& auxo, T& auxn)
 {
     const long long P = a.plane;
     if (a.auxo) {
-        auxo = a.auxo[c + k * P];
-        auxn = a.auxn[c + k * P];
+        auxo = (T)a.auxo[c + k * P];
+        auxn = (T)a.auxn[c + k * P];
         return;
     }
-    double x = 2.0 * a.dt * (a.nuh[c + (k + 1) * P] + mol);
-    auxo = (1.0 - a.cnpar) * x / (a.ho[c + (k + 1) * P] + a.ho[c + k * P]);
-    auxn = a.cnpar * x / (a.hn[c + (k + 1) * P] + a.hn[c + k * P]);
+    T x = (T)(2.0 * a.dt) * (a.nuh[c + (k + 1) * P] + (T)mol);
+    auxo = (T)(1.0 - a.cnpar) * x / ((T)a.ho[c + (k + 1) * P] + (T)a.ho[c + k * P]);
+    auxn = (T)a.cnpar * x / ((T)a.hn[c + (k + 1) * P] + (T)a.hn[c + k * P]);
 }
 
-// Thread per column; dynamic shared memory holds ru/qu: 2 * nz * blockDim doubles.
-__global__ void vd_column_kernel(VDArgs a)
+// Thread per column; dynamic shared memory holds ru/qu: 2 * nz * blockDim values.
+template <typename T>
+__global__ void vd_column_kernel(VDArgs<T> a)
 {
-    extern __shared__ double smem[];
+    extern __shared__ __align__(16) unsigned char vd_smem[];
     const int tid = threadIdx.x;
     const int nthreads = blockDim.x;
     const int i = blockIdx.x * blockDim.x + tid;
@@ -76,8 +80,8 @@ __global__ void vd_column_kernel(VDArgs a)
     const int nz = a.nz;
     if (nz == 1) {  // diffusion.F90:224-231: every point, mask not consulted
         for (int t = 0; t < a.ntracer; t++) {
-            double a4 = a.ho[c] * a.var[t][c];
-            double a2 = a.hn[c];
+            T a4 = (T)a.ho[c] * a.var[t][c];
+            T a2 = (T)a.hn[c];
             if (a.ea4[t]) a4 = a4 + a.ea4[t][c];
             if (a.ea2[t]) a2 = a2 - a.ea2[t][c];
             a.var[t][c] = a4 / a2;
@@ -85,42 +89,42 @@ __global__ void vd_column_kernel(VDArgs a)
         return;
     }
     if (a.mask[c] != 1) return;
-    double* ru = smem;                        // ru[k * nthreads + tid]
-    double* qu = smem + (size_t)nz * nthreads;
+    T* ru = (T*)vd_smem;                        // ru[k * nthreads + tid]
+    T* qu = ru + (size_t)nz * nthreads;
     for (int t = 0; t < a.ntracer; t++) {
-        double* __restrict__ var = a.var[t];
-        const double* ea2 = a.ea2[t];
-        const double* ea4 = a.ea4[t];
+        T* __restrict__ var = a.var[t];
+        const T* ea2 = a.ea2[t];
+        const T* ea4 = a.ea4[t];
         const double mol = a.molecular[t];
         // surface layer (C level nz-1), diffusion.F90:238-245
         int k = nz - 1;
-        double aob, anb;                       // aux of the interface below level k
+        T aob, anb;                             // aux of the interface below level k
         vd_aux(a, c, k - 1, mol, aob, anb);
-        double vk = var[c + k * P];
-        double vkm1 = var[c + (k - 1) * P];
-        double a1 = -anb;
-        double a2 = a.hn[c + k * P] + anb;
-        double a4 = vk * a.ho[c + k * P] + (vkm1 - vk) * aob;
+        T vk = var[c + k * P];
+        T vkm1 = var[c + (k - 1) * P];
+        T a1 = -anb;
+        T a2 = (T)a.hn[c + k * P] + anb;
+        T a4 = vk * (T)a.ho[c + k * P] + (vkm1 - vk) * aob;
         if (ea2) a2 = a2 - ea2[c + k * P];
         if (ea4) a4 = a4 + ea4[c + k * P];
-        double rk = a1 / a2;
-        double qk = a4 / a2;
+        T rk = a1 / a2;
+        T qk = a4 / a2;
         ru[k * nthreads + tid] = rk;
         qu[k * nthreads + tid] = qk;
         // inner layers, diffusion.F90:247-258 and elimination :287-290
-        double aoa = aob, ana = anb;           // interface above level k-1
-        double vkp1 = vk;
+        T aoa = aob, ana = anb;                 // interface above level k-1
+        T vkp1 = vk;
         vk = vkm1;
         for (k = nz - 2; k >= 1; k--) {
             vd_aux(a, c, k - 1, mol, aob, anb);
             vkm1 = var[c + (k - 1) * P];
-            double a3 = -ana;
+            T a3 = -ana;
             a1 = -anb;
-            a2 = a.hn[c + k * P] + ana + anb;
-            a4 = vk * a.ho[c + k * P] + (vkp1 - vk) * aoa + (vkm1 - vk) * aob;
+            a2 = (T)a.hn[c + k * P] + ana + anb;
+            a4 = vk * (T)a.ho[c + k * P] + (vkp1 - vk) * aoa + (vkm1 - vk) * aob;
             if (ea2) a2 = a2 - ea2[c + k * P];
             if (ea4) a4 = a4 + ea4[c + k * P];
-            double den = a2 - a3 * rk;
+            T den = a2 - a3 * rk;
             rk = a1 / den;
             qk = (a4 - a3 * qk) / den;
             ru[k * nthreads + tid] = rk;
@@ -130,14 +134,14 @@ __global__ void vd_column_kernel(VDArgs a)
         }
         // bottom layer, diffusion.F90:260-267 and :291-292
         {
-            double a3 = -ana;
-            a2 = a.hn[c] + ana;
-            a4 = vk * a.ho[c] + (vkp1 - vk) * aoa;
+            T a3 = -ana;
+            a2 = (T)a.hn[c] + ana;
+            a4 = vk * (T)a.ho[c] + (vkp1 - vk) * aoa;
             if (ea2) a2 = a2 - ea2[c];
             if (ea4) a4 = a4 + ea4[c];
-            double q0 = (a4 - a3 * qk) / (a2 - a3 * rk);
+            T q0 = (a4 - a3 * qk) / (a2 - a3 * rk);
             // back substitution :304-307
-            double vprev = q0;
+            T vprev = q0;
             var[c] = q0;
             for (k = 1; k < nz; k++) {
                 vprev = qu[k * nthreads + tid] - ru[k * nthreads + tid] * vprev;
@@ -163,19 +167,20 @@ __global__ void vd_prepare_kernel(int nx_, int ny_, int nz, long long plane, dou
     auxn[p] = cnpar * x / (dzn[c + (k + 1) * plane] + dzn[c + k * plane]);
 }
 
-static int vd_launch(VDArgs& a, cudaStream_t stream)
+template <typename T>
+static int vd_launch(VDArgs<T>& a, cudaStream_t stream)
 {
     int threads = 128;
-    while (threads > 32 && (size_t)2 * a.nz * threads * sizeof(double) > 160 * 1024) threads /= 2;
-    size_t smem = (size_t)2 * a.nz * threads * sizeof(double);
+    while (threads > 32 && (size_t)2 * a.nz * threads * sizeof(T) > 160 * 1024) threads /= 2;
+    size_t smem = (size_t)2 * a.nz * threads * sizeof(T);
     if (smem > 200 * 1024) return GETM_ERR_NZ;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(vd_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(vd_column_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     dim3 grid(getm_div_up(a.nx_, threads), a.ny_);
-    vd_column_kernel<<<grid, threads, smem, stream>>>(a);
+    vd_column_kernel<T><<<grid, threads, smem, stream>>>(a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
@@ -232,7 +237,7 @@ extern "C" int getm_vertical_diffusion_apply(getm_vertical_diffusion* d, int nx,
     if (!d || nx < 1 || ny < 1 || nz < 1 || !mask || !ho || !hn || !var) return GETM_ERR_ARG;
     if (nz > GETM_MAX_NZ) return GETM_ERR_NZ;
     if (nz > 1 && (!d->auxo || d->n3 < (size_t)nx * ny * nz)) return GETM_ERR_ARG;  // not prepared
-    VDArgs a;
+    VDArgs<double> a;
     memset(&a, 0, sizeof(a));
     a.nx_ = nx; a.ny_ = ny; a.nz = nz; a.plane = (long long)nx * ny;
     a.mask = mask; a.ho = ho; a.hn = hn; a.auxo = d->auxo; a.auxn = d->auxn;
@@ -240,17 +245,15 @@ extern "C" int getm_vertical_diffusion_apply(getm_vertical_diffusion* d, int nx,
     return vd_launch(a, stream);
 }
 
-extern "C" int getm_vertical_diffusion_batch(int nx, int ny, int nz, const int* mask,
-                                             const double* nuh, double timestep, double cnpar,
-                                             const double* ho, const double* hn, int ntracer,
-                                             const double* molecular, double* const* vars,
-                                             const double* const* ea2, const double* const* ea4,
-                                             cudaStream_t stream)
+template <typename T>
+static int vd_batch_impl(int nx, int ny, int nz, const int* mask, const T* nuh, double timestep, double cnpar,
+                         const double* ho, const double* hn, int ntracer, const double* molecular,
+                         T* const* vars, const T* const* ea2, const T* const* ea4, cudaStream_t stream)
 {
     if (nx < 1 || ny < 1 || nz < 1 || !mask || !nuh || !ho || !hn || ntracer < 1 || !vars || !molecular)
         return GETM_ERR_ARG;
     if (nz > GETM_MAX_NZ) return GETM_ERR_NZ;
-    VDArgs a;
+    VDArgs<T> a;
     memset(&a, 0, sizeof(a));
     a.nx_ = nx; a.ny_ = ny; a.nz = nz; a.plane = (long long)nx * ny;
     a.mask = mask; a.nuh = nuh; a.ho = ho; a.hn = hn; a.dt = timestep; a.cnpar = cnpar;
@@ -265,9 +268,30 @@ extern "C" int getm_vertical_diffusion_batch(int nx, int ny, int nz, const int* 
             a.ea2[t] = ea2 ? ea2[done + t] : NULL;
             a.ea4[t] = ea4 ? ea4[done + t] : NULL;
         }
-        int rc = vd_launch(a, stream);
+        int rc = vd_launch<T>(a, stream);
         if (rc) return rc;
         done += n;
     } while (done < ntracer);
     return GETM_OK;
+}
+
+extern "C" int getm_vertical_diffusion_batch(int nx, int ny, int nz, const int* mask,
+                                             const double* nuh, double timestep, double cnpar,
+                                             const double* ho, const double* hn, int ntracer,
+                                             const double* molecular, double* const* vars,
+                                             const double* const* ea2, const double* const* ea4,
+                                             cudaStream_t stream)
+{
+    return vd_batch_impl<double>(nx, ny, nz, mask, nuh, timestep, cnpar, ho, hn, ntracer, molecular, vars, ea2, ea4,
+                                 stream);
+}
+
+extern "C" int getm_vertical_diffusion_batch_f32(int nx, int ny, int nz, const int* mask, const float* nuh,
+                                                 double timestep, double cnpar, const double* ho,
+                                                 const double* hn, int ntracer, const double* molecular,
+                                                 float* const* vars, const float* const* ea2,
+                                                 const float* const* ea4, cudaStream_t stream)
+{
+    return vd_batch_impl<float>(nx, ny, nz, mask, nuh, timestep, cnpar, ho, hn, ntracer, molecular, vars, ea2, ea4,
+                                stream);
 }

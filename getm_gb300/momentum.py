@@ -35,8 +35,11 @@ class Momentum:
     def __init__(self, Am: float = 0.0, An: float = 0.0, cnpar: float = 1.0,
                  advection_scheme: Optional[AdvectionScheme] = None,
                  advection_split_2d: AdvectionSplit = AdvectionSplit.FULL,
-                 coriolis_scheme: CoriolisScheme = CoriolisScheme.DEFAULT, avmmol: float = 1.8e-6):
-        """momentum.py:113-144"""
+                 coriolis_scheme: CoriolisScheme = CoriolisScheme.DEFAULT, avmmol: float = 1.8e-6,
+                 dtype: torch.dtype = torch.float64):
+        """momentum.py:113-144.  ``dtype`` is the type of the 3D (depth-explicit)
+        fields: float64 for the FP64 form, float32 for the mixed form; 2D
+        transports and everything tied to layer thickness stay float64."""
         self._Am_const = Am
         self._An_const = An
         self.cnpar = cnpar
@@ -44,6 +47,7 @@ class Momentum:
         self.advection_split_2d = advection_split_2d
         self.coriolis_scheme = coriolis_scheme
         self.avmmol = avmmol
+        self.dtype3d = dtype
 
     # ------------------------------------------------------------------ setup
     def _create_arrays(self, tgrid: Grid, three_d: bool):
@@ -60,28 +64,32 @@ class Momentum:
         self.vva = vg.vgrid.array(fill=nan)
         if not three_d:
             return
+        d3 = self.dtype3d
         for n in ("pk", "uk", "corpk", "advpk", "diffpk"):
-            setattr(self, n, ug.array(name=n, z=CENTERS))
+            setattr(self, n, ug.array(name=n, z=CENTERS, dtype=d3))
         for n in ("qk", "vk", "corqk", "advqk", "diffqk"):
-            setattr(self, n, vg.array(name=n, z=CENTERS))
-        self.ww = tgrid.array(name="ww", z=INTERFACES)
-        self.SS = tgrid.array(name="SS", z=INTERFACES)
+            setattr(self, n, vg.array(name=n, z=CENTERS, dtype=d3))
+        self.ww = tgrid.array(name="ww", z=INTERFACES, dtype=d3)
+        self.SS = tgrid.array(name="SS", z=INTERFACES, dtype=d3)
         for n in ("rru", "Ui", "udev", "ustar2_bx"):
             setattr(self, n, ug.array(name=n))
         for n in ("rrv", "Vi", "vdev", "ustar2_by"):
             setattr(self, n, vg.array(name=n))
         self._U_cum = torch.zeros_like(self.Ui.all_values)
         self._V_cum = torch.zeros_like(self.Vi.all_values)
-        self.uua3d = ug.ugrid.array(fill=nan, z=CENTERS)
-        self.uva3d = ug.vgrid.array(fill=nan, z=CENTERS)
-        self.vua3d = vg.ugrid.array(fill=nan, z=CENTERS)
-        self.vva3d = vg.vgrid.array(fill=nan, z=CENTERS)
+        self.uua3d = ug.ugrid.array(fill=nan, z=CENTERS, dtype=d3)
+        self.uva3d = ug.vgrid.array(fill=nan, z=CENTERS, dtype=d3)
+        self.vua3d = vg.ugrid.array(fill=nan, z=CENTERS, dtype=d3)
+        self.vva3d = vg.vgrid.array(fill=nan, z=CENTERS, dtype=d3)
         self.ustar_b = tgrid.array(name="ustar_b")
         # interpolation targets reused every step (pygetm allocates these per call)
-        self._visc_u = ug.array(z=INTERFACES, fill_value=None)
-        self._visc_v = vg.array(z=INTERFACES, fill_value=None)
-        self._ww_u = ug.array(z=INTERFACES, fill_value=None)
-        self._ww_v = vg.array(z=INTERFACES, fill_value=None)
+        self._visc_u = ug.array(z=INTERFACES, fill_value=None, dtype=d3)
+        self._visc_v = vg.array(z=INTERFACES, fill_value=None, dtype=d3)
+        self._ww_u = ug.array(z=INTERFACES, fill_value=None, dtype=d3)
+        self._ww_v = vg.array(z=INTERFACES, fill_value=None, dtype=d3)
+        # bottom-layer velocities for the FP64 2D friction kernels
+        self._u_bot64 = ug.array(fill=0.0)
+        self._v_bot64 = vg.array(fill=0.0)
 
     def initialize(self, tgrid: Grid, runtype: int, default_advection_scheme: AdvectionScheme):
         """momentum.py:489-616"""
@@ -118,11 +126,14 @@ class Momentum:
         if three_d:
             self.hU_bot = ug.hn.isel(z=0)
             self.hV_bot = vg.hn.isel(z=0)
-            self.u_bot = self.uk.isel(z=0)
-            self.v_bot = self.vk.isel(z=0)
+            if self.dtype3d == torch.float64:
+                self.u_bot = self.uk.isel(z=0)
+                self.v_bot = self.vk.isel(z=0)
+            else:
+                self.u_bot, self.v_bot = self._u_bot64, self._v_bot64
             self._vertical_diffusion = VerticalDiffusion(tgrid, cnpar=self.cnpar)
-            self.ea2 = tgrid.array(fill=0.0, z=CENTERS)
-            self.ea4 = tgrid.array(fill=0.0, z=CENTERS)
+            self.ea2 = tgrid.array(fill=0.0, z=CENTERS, dtype=self.dtype3d)
+            self.ea4 = tgrid.array(fill=0.0, z=CENTERS, dtype=self.dtype3d)
         self.An = tgrid.array(name="An")
         self.An.fill(self._An_const)
         self._ufirst = False
@@ -261,6 +272,9 @@ class Momentum:
         torch.div(self.pk.all_values, self.pk.grid.hn.all_values, out=self.uk.all_values)
         torch.div(self.qk.all_values, self.qk.grid.hn.all_values, out=self.vk.all_values)
         _pygetm.shear_frequency(self.uk, self.vk, self.SS)
+        if self.u_bot is self._u_bot64:
+            self._u_bot64.all_values.copy_(self.uk.all_values[0])
+            self._v_bot64.all_values.copy_(self.vk.all_values[0])
         if self.apply_bottom_friction:
             self.bottom_friction(self.u_bot, self.v_bot, self.hU_bot, self.hV_bot, self.rru, self.rrv)
         _pygetm.bottom_shear_velocity(self.u_bot, self.v_bot, self.rru, self.rrv, self.ustar2_bx, self.ustar2_by,
@@ -277,10 +291,11 @@ class Momentum:
             _pygetm.momentum_diffusion(self.uua.grid.hn, self.uva.grid.hn, self.vua.grid.hn, self.vva.grid.hn,
                                        self.uk, self.vk, self._Am_const, self.diffpk, self.diffqk)
         self._transport_2d_momentum(self.Ui, self.Vi, timestep, self.SxA, self.SyA, self.SxD, self.SyD, False)
-        torch.sub(self.advpk.all_values.sum(dim=0), self.SxA.all_values, out=self.SxA.all_values)
-        torch.sub(self.advqk.all_values.sum(dim=0), self.SyA.all_values, out=self.SyA.all_values)
-        torch.sub(self.diffpk.all_values.sum(dim=0), self.SxD.all_values, out=self.SxD.all_values)
-        torch.sub(self.diffqk.all_values.sum(dim=0), self.SyD.all_values, out=self.SyD.all_values)
+        f64 = torch.float64
+        torch.sub(self.advpk.all_values.sum(dim=0, dtype=f64), self.SxA.all_values, out=self.SxA.all_values)
+        torch.sub(self.advqk.all_values.sum(dim=0, dtype=f64), self.SyA.all_values, out=self.SyA.all_values)
+        torch.sub(self.diffpk.all_values.sum(dim=0, dtype=f64), self.SxD.all_values, out=self.SxD.all_values)
+        torch.sub(self.diffqk.all_values.sum(dim=0, dtype=f64), self.SyD.all_values, out=self.SyD.all_values)
         if self.apply_bottom_friction:
             torch.add(self.ustar2_bx.all_values, self.ru.all_values * self.u1.all_values, out=self.SxF.all_values)
             torch.add(self.ustar2_by.all_values, self.rv.all_values * self.v1.all_values, out=self.SyF.all_values)
@@ -295,7 +310,10 @@ class Momentum:
         self._vertical_diffusion(visc, timestep, vel3d, molecular=self.avmmol, ea2=self.ea2, ea4=self.ea4,
                                  use_ho=True)
         torch.mul(vel3d.all_values, grid.hn.all_values, out=tp3d.all_values)
-        torch.sum(tp3d.all_values, dim=0, out=dev.all_values)
+        if tp3d.dtype == torch.float64:
+            torch.sum(tp3d.all_values, dim=0, out=dev.all_values)
+        else:
+            dev.all_values.copy_(tp3d.all_values.sum(dim=0, dtype=torch.float64))
         dev.all_values.sub_(tp2d.all_values)
         dev.all_values.div_(grid.D.all_values)
         tp3d.all_values.sub_(dev.all_values * grid.hn.all_values)

@@ -18,7 +18,7 @@ import torch
 
 from . import _lib
 from ._lib import call
-from .core import CENTERS, INTERFACES, Array, Grid
+from .core import CENTERS, INTERFACES, Array, Grid, _sfx
 
 
 class AdvectionScheme(enum.IntEnum):
@@ -169,7 +169,8 @@ class Advection:
         self.h.copy_((self.grid.hn if new_h else self.grid.ho).all_values)
         wv = _lib.ptr_array([_p(x) for x in w_vars])
         vv = _lib.ptr_array([_p(x) for x in vars])
-        call("getm_advection_apply_3d_batch", self.p, self.grid.handle, self.ugrid.handle, self.vgrid.handle,
+        sfx = _sfx(*([u.all_values, v.all_values, w.all_values] + [x.all_values for x in list(w_vars) + list(vars)]))
+        call("getm_advection_apply_3d_batch" + sfx, self.p, self.grid.handle, self.ugrid.handle, self.vgrid.handle,
              int(self._ufirst), _p(u), _p(v), _p(w), wv, _p(Ah_u), _p(Ah_v), float(timestep), self.h.data_ptr(),
              _p(self.ugrid.hn), _p(self.vgrid.hn), len(vars), vv, _s())
 
@@ -252,5 +253,6 @@ class VerticalDiffusion:
         vv = _lib.ptr_array([_p(v) for v in vars])
         e2 = _lib.ptr_array([_p(e) for e in ea2s]) if ea2s is not None and any(e is not None for e in ea2s) else None
         e4 = _lib.ptr_array([_p(e) for e in ea4s]) if ea4s is not None and any(e is not None for e in ea4s) else None
-        call("getm_vertical_diffusion_batch", g.nx_, g.ny_, g.nz_, _p(g.mask), _p(nuh), float(timestep),
+        sfx = _sfx(nuh.all_values, *[v.all_values for v in vars])
+        call("getm_vertical_diffusion_batch" + sfx, g.nx_, g.ny_, g.nz_, _p(g.mask), _p(nuh), float(timestep),
              float(self.cnpar), _p(ho), _p(g.hn), n, mol, vv, e2, e4, _s())

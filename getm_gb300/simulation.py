@@ -99,7 +99,16 @@ class Simulation:
                  advection_scheme: AdvectionScheme = AdvectionScheme.DEFAULT, momentum: Optional[Momentum] = None,
                  airsea: Optional[Fluxes] = None, internal_pressure: str = "shchepetkin_mcwilliams",
                  Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
-                 nuh: float = 0.0, device="cuda"):
+                 nuh: float = 0.0, precision: str = "fp64", device="cuda"):
+        """``precision``: "fp64" (the plain form) or "mixed" (float32 tracers,
+        3D velocities and their tendencies, diffusivities, buoyancy and
+        internal pressure; float64 elevations, depths, layer thicknesses, 2D
+        transports and their accumulation)."""
+        if precision not in ("fp64", "mixed"):
+            raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
+        self.precision = precision
+        d3 = torch.float32 if precision == "mixed" else torch.float64
+        self.dtype3d = d3
         if Dmin <= 0.0:
             raise Exception("Dmin<=0")
         if Dcrit < 2.5 * Dmin:
@@ -124,7 +133,7 @@ class Simulation:
         if three_d:
             self.h_T_half = T.array(fill=float("nan"), z=CENTERS)
             self.depth = T.array(z=CENTERS, name="pres")
-        self.momentum = momentum or Momentum()
+        self.momentum = momentum or Momentum(dtype=d3)
         self.momentum.initialize(T, int(self.runtype), advection_scheme)
         self.airsea = airsea or Fluxes()
         self.airsea.initialize(T)
@@ -134,10 +143,10 @@ class Simulation:
         self.tausy = self.V.array(name="tausyv")
         self.fwf = T.array(name="fwf")
         self.fwf.fill(0.0)
-        self.tracers = TracerCollection(T, advection_scheme)
+        self.tracers = TracerCollection(T, advection_scheme, dtype=d3)
         if three_d:
-            self.num = T.array(z=INTERFACES, name="num")
-            self.nuh = T.array(z=INTERFACES, name="nuh")
+            self.num = T.array(z=INTERFACES, name="num", dtype=d3)
+            self.nuh = T.array(z=INTERFACES, name="nuh", dtype=d3)
             self.num.fill(num)
             self.nuh.fill(nuh)
             self.ustar_s = T.array(fill=0.0, name="ustar_s")
@@ -151,13 +160,13 @@ class Simulation:
             self.salt = self.tracers.add("salt", molecular_diffusivity=1.1e-9)
             self.temp.fill(5.0)
             self.salt.fill(35.0)
-            self.rho = T.array(z=CENTERS, name="rho")
-            self.buoy = T.array(z=CENTERS, name="buoy")
+            self.rho = T.array(z=CENTERS, name="rho", dtype=d3)
+            self.buoy = T.array(z=CENTERS, name="buoy", dtype=d3)
             self.internal_pressure_method = internal_pressure
         if three_d:
             # internal_pressure.Base.initialize (python/pygetm/internal_pressure.py:14-30)
-            self.idpdx = self.U.array(z=CENTERS, name="idpdx")
-            self.idpdy = self.V.array(z=CENTERS, name="idpdy")
+            self.idpdx = self.U.array(z=CENTERS, name="idpdx", dtype=d3)
+            self.idpdy = self.V.array(z=CENTERS, name="idpdy", dtype=d3)
             self.idpdx.fill(0.0)
             self.idpdy.fill(0.0)
             self._P_work = torch.zeros((T.nz, T.ny_, T.nx_), dtype=torch.float64, device=T.device)
@@ -229,8 +238,8 @@ class Simulation:
                                   self.dpdyo, self.idpdx, self.idpdy, self.num)
             self.tracers.advance(self.macrotimestep, self.momentum.uk, self.momentum.vk, self.momentum.ww, self.nuh)
             if self.runtype == RunType.BAROCLINIC and self.delay_slow_ip:
-                torch.sum(self.idpdx.all_values, dim=0, out=self.momentum.SxB.all_values)
-                torch.sum(self.idpdy.all_values, dim=0, out=self.momentum.SyB.all_values)
+                self.momentum.SxB.all_values.copy_(self.idpdx.all_values.sum(dim=0, dtype=torch.float64))
+                self.momentum.SyB.all_values.copy_(self.idpdy.all_values.sum(dim=0, dtype=torch.float64))
 
     def _update_forcing_and_diagnostics(self, macro_active: bool):
         """python/pygetm/simulation.py:1138-1304"""
@@ -242,8 +251,8 @@ class Simulation:
             self.update_density()
             self.update_internal_pressure()
             if not self.delay_slow_ip:
-                torch.sum(self.idpdx.all_values, dim=0, out=self.momentum.SxB.all_values)
-                torch.sum(self.idpdy.all_values, dim=0, out=self.momentum.SyB.all_values)
+                self.momentum.SxB.all_values.copy_(self.idpdx.all_values.sum(dim=0, dtype=torch.float64))
+                self.momentum.SyB.all_values.copy_(self.idpdy.all_values.sum(dim=0, dtype=torch.float64))
         self.update_depth()
         self.momentum.update_depth_integrated_diagnostics(self.timestep, skip_coriolis=not starting,
                                                          update_z0b=update_z0b)
@@ -264,8 +273,9 @@ class Simulation:
         device equation of state."""
         n = self.rho.all_values.numel()
         from ._lib import call
+        from .core import _sfx
 
-        call("getm_density_buoyancy", n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
+        call("getm_density_buoyancy" + _sfx(self.salt.all_values, self.rho.all_values), n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
              self.depth.all_values.data_ptr(), self.rho.all_values.data_ptr(), self.buoy.all_values.data_ptr(),
              torch.cuda.current_stream().cuda_stream)
 

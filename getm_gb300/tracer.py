@@ -19,10 +19,11 @@ class Tracer(Array):
     __slots__ = ("molecular_diffusivity", "source", "surface_flux", "source_scale", "vertical_velocity")
 
     def __init__(self, grid: Grid, name: str, molecular_diffusivity: float = 0.0, source: Optional[Array] = None,
-                 surface_flux: Optional[Array] = None, source_scale: float = 1.0, fill_value=None):
+                 surface_flux: Optional[Array] = None, source_scale: float = 1.0, fill_value=None,
+                 dtype: torch.dtype = torch.float64):
         from .domain import FILL_VALUE
 
-        data = torch.full((grid.nz, grid.ny_, grid.nx_), FILL_VALUE, dtype=torch.float64, device=grid.device)
+        data = torch.full((grid.nz, grid.ny_, grid.nx_), FILL_VALUE, dtype=dtype, device=grid.device)
         super().__init__(grid, data, z=CENTERS, fill_value=FILL_VALUE if fill_value is None else fill_value, name=name)
         self.molecular_diffusivity = molecular_diffusivity
         self.source = source
@@ -34,8 +35,11 @@ class Tracer(Array):
 class TracerCollection:
     """python/pygetm/tracer.py:128-276 (advance and _diffuse)."""
 
-    def __init__(self, grid: Grid, advection_scheme: AdvectionScheme = AdvectionScheme.DEFAULT, cnpar: float = 1.0):
+    def __init__(self, grid: Grid, advection_scheme: AdvectionScheme = AdvectionScheme.DEFAULT, cnpar: float = 1.0,
+                 dtype: torch.dtype = torch.float64):
+        """``dtype``: float64 (FP64 form) or float32 (mixed form) tracers."""
         self.grid = grid
+        self.dtype = dtype
         self._tracers: List[Tracer] = []
         self._source = grid.array(z=CENTERS)
         self._advection = Advection(grid, scheme=advection_scheme)
@@ -50,6 +54,7 @@ class TracerCollection:
         return len(self._tracers)
 
     def add(self, name: str, **kwargs) -> Tracer:
+        kwargs.setdefault("dtype", self.dtype)
         t = Tracer(self.grid, name, **kwargs)
         self._tracers.append(t)
         return t

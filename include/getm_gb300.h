@@ -88,6 +88,14 @@ int getm_advection_apply_3d_batch(getm_advection* adv, getm_grid* tgrid, getm_gr
                                   const double* Ah_u, const double* Ah_v, double timestep,
                                   double* h, const double* hu, const double* hv, int ntracer,
                                   double* const* vars, cudaStream_t stream);
+/* One directional pass of advection_uv_calculate (wrapper.F90:213-254),
+ * out of place and batched: reads h_in and var_in[t], writes the complete
+ * fields h_out and var_out[t] (every point; untouched points are copied).
+ * One kernel launch for up to 32 tracers.  Buffers must not alias.          */
+int getm_advection_uv_pass(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
+                           getm_grid* ugrid, const double* u, const double* Ah, double timestep,
+                           const double* h_in, double* h_out, const double* hu, int ntracer,
+                           const double* const* var_in, double* const* var_out, cudaStream_t stream);
 /* Fused 2D split of Advection.__call__ (operators.py:52-93): split 1 = FULL,
  * 2 = HALF, 3 = HALF_ALWAYS; D (in/out) is the column-height work array.    */
 int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
@@ -266,6 +274,68 @@ int getm_launch_count(unsigned long long* count);
  * -g/rho0 (rho - rho0) (python/pygetm/simulation.py:1184); either may be NULL. */
 int getm_density_buoyancy(int n, const double* salt, const double* temp, const double* p, double* rho,
                           double* buoy, cudaStream_t stream);
+
+/* ---- mixed-precision form ------------------------------------------------
+ * Same routines with float bulk fields (tracers, 3D velocities/transports,
+ * their tendencies, nuh/num, buoyancy and the internal pressure gradient)
+ * and float arithmetic for fluxes, limiters, the tridiagonal solve and the
+ * pressure-gradient slopes.  Layer thicknesses, elevations, water depths,
+ * metrics and 2D transports stay double; sums that decide conservation
+ * (thickness updates, the w recursion, momentum sources, the EOS and the
+ * column pressure integral) are evaluated in FP64.                        */
+int getm_advection_apply_3d_batch_f32(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
+                                      getm_grid* vgrid, int ufirst, const float* u, const float* v,
+                                      const float* w, const float* const* w_var, const double* Ah_u,
+                                      const double* Ah_v, double timestep, double* h,
+                                      const double* hu, const double* hv, int ntracer,
+                                      float* const* vars, cudaStream_t stream);
+int getm_advection_uv_pass_f32(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
+                               getm_grid* ugrid, const float* u, const double* Ah, double timestep,
+                               const double* h_in, double* h_out, const double* hu, int ntracer,
+                               const float* const* var_in, float* const* var_out, cudaStream_t stream);
+int getm_vertical_diffusion_batch_f32(int nx, int ny, int nz, const int* mask, const float* nuh,
+                                      double timestep, double cnpar, const double* ho,
+                                      const double* hn, int ntracer, const double* molecular,
+                                      float* const* vars, const float* const* ea2,
+                                      const float* const* ea4, cudaStream_t stream);
+int getm_grid_interp_x_f32(int nx, int ny, int nz, const float* source, float* target, int ioffset,
+                           cudaStream_t stream);
+int getm_grid_interp_y_f32(int nx, int ny, int nz, const float* source, float* target, int joffset,
+                           cudaStream_t stream);
+int getm_grid_interp_z_f32(int nx, int ny, int nz1, int nz2, const float* source, float* target,
+                           int koffset, cudaStream_t stream);
+int getm_grid_interp_xy_f32(int nx1, int ny1, int nx2, int ny2, int nz, const float* source,
+                            float* target, int ioffset, int joffset, cudaStream_t stream);
+int getm_collect_3d_momentum_sources_f32(int nx, int ny, int nz, int halox, int haloy,
+                                         const int* mask, const double* alpha, const double* ho,
+                                         const double* hn, const double* dp, const float* cor,
+                                         const float* adv, const float* diff, const float* idp,
+                                         const double* taus, const double* rr, double dt,
+                                         float* ea2, float* ea4, cudaStream_t stream);
+int getm_w_momentum_3d_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                           const int* mask, const double* dyu, const double* dxv,
+                           const double* iarea, const double* ho, const double* hn,
+                           const float* pk, const float* qk, double dt, float* w,
+                           cudaStream_t stream);
+int getm_shear_frequency_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                             const int* mask, const double* hu, const double* hv, const float* uk,
+                             const float* vk, float* SS, cudaStream_t stream);
+int getm_reconstruct_transport_change_f32(int nx, int ny, int nz, int imin, int imax, int jmin,
+                                          int jmax, float* un, const double* hn, const float* Uo,
+                                          double timestep, cudaStream_t stream);
+int getm_blumberg_mellor_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                             const int* umask, const int* vmask, const double* idxu,
+                             const double* idyv, const double* hu, const double* hv,
+                             const double* zf, const float* buoy, float* idpdx, float* idpdy,
+                             cudaStream_t stream);
+int getm_shchepetkin_mcwilliams_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                    const int* mask, const int* umask, const int* vmask,
+                                    const double* idxu, const double* idyv, const double* h,
+                                    const double* z, const double* zc, const float* buoy,
+                                    float* idpdx, float* idpdy, double* P_work,
+                                    cudaStream_t stream);
+int getm_density_buoyancy_f32(int n, const float* salt, const float* temp, const double* p,
+                              float* rho, float* buoy, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -108,7 +108,9 @@ def collect_3d_momentum_sources(dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4)
     assert rr.grid is g and not rr.z, "rr"
     assert ea2.z == CENTERS
     assert ea4.z == CENTERS
-    sfx = _sfx(cor.all_values, adv.all_values, diff.all_values, idp.all_values, ea2.all_values, ea4.all_values)
+    sfx = _sfx(cor.all_values, adv.all_values, diff.all_values, ea2.all_values, ea4.all_values)
+    if idp.all_values.dtype != torch.float64:
+        raise TypeError("the internal pressure gradient idp must be float64 in both forms")
     call("getm_collect_3d_momentum_sources" + sfx, g.nx_, g.ny_, g.nz, g.halox, g.haloy, _p(g.mask), _p(g.alpha), _p(g.ho),
          _p(g.hn), _p(dp), _p(cor), _p(adv), _p(diff), _p(idp), _p(taus), _p(rr), float(dt), _p(ea2), _p(ea4), _s())
 

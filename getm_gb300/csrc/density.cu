@@ -27,16 +27,18 @@ __device__ __forceinline__ double seos_rho(double S, double T, double z)
            + SEOS_B0 * (1.0 - 0.5 * SEOS_LAMBDA2 * Sa - SEOS_MU2 * z) * Sa - SEOS_NU * Ta * Sa;
 }
 
-// R: type of salinity, temperature, rho and buoyancy; the EOS itself is
-// evaluated in FP64 for both forms (rho - rho0 cancels 3 significant digits).
+// R: type of salinity and temperature.  Density and buoyancy are evaluated
+// and stored in FP64 in both forms: rho - rho0 cancels three significant
+// digits, and the internal pressure gradient is a small difference of large
+// column integrals of buoyancy.
 template <typename R>
-__global__ void density_kernel(long long n, const R* S, const R* T, const double* p, R* rho, R* buoy)
+__global__ void density_kernel(long long n, const R* S, const R* T, const double* p, double* rho, double* buoy)
 {
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     double r = seos_rho((double)S[q], (double)T[q], p[q]);
-    if (rho) rho[q] = (R)r;
-    if (buoy) buoy[q] = (R)((-GETM_G / GETM_RHO0) * (r - GETM_RHO0));
+    if (rho) rho[q] = r;
+    if (buoy) buoy[q] = (-GETM_G / GETM_RHO0) * (r - GETM_RHO0);
 }
 
 extern "C" int getm_density_buoyancy(int n, const double* salt, const double* temp, const double* p,
@@ -50,7 +52,7 @@ extern "C" int getm_density_buoyancy(int n, const double* salt, const double* te
 }
 
 extern "C" int getm_density_buoyancy_f32(int n, const float* salt, const float* temp, const double* p,
-                                         float* rho, float* buoy, cudaStream_t stream)
+                                         double* rho, double* buoy, cudaStream_t stream)
 {
     if (n < 0 || (n > 0 && (!salt || !temp || !p || (!rho && !buoy)))) return GETM_ERR_ARG;
     if (n == 0) return GETM_OK;

@@ -78,12 +78,13 @@ extern "C" int getm_bottom_friction(int nx, int ny, const int* mask, const doubl
 }
 
 // momentum.F90:103-145: rows haloy..ny-haloy-1, every i, every k (mask unused).
-// T: type of the 3D source fields and of ea2/ea4; the sum is formed in FP64.
+// T: type of the 3D tendency fields and of ea2/ea4; the internal pressure
+// gradient idp is double in both forms; the sum is formed in FP64.
 template <typename T>
 __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const double* alpha,
                                        const double* ho, const double* hn, const double* dp,
                                        const T* cor, const T* adv, const T* diff,
-                                       const T* idp, const double* taus, const double* rr,
+                                       const double* idp, const double* taus, const double* rr,
                                        double dt, T* ea2, T* ea4)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -96,7 +97,7 @@ __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const 
     for (int k = 0; k < nz; k++) {
         long long q = p + k * plane;
         double e = dt * (-0.5 * (ho[q] + hn[q]) * GETM_G * dpp
-                         + al * ((double)cor[q] + (double)adv[q] + (double)diff[q] + (double)idp[q]));
+                         + al * ((double)cor[q] + (double)adv[q] + (double)diff[q] + idp[q]));
         if (k == nz - 1) e = e + dt * al * taus[p] * rho0i;
         ea4[q] = (T)e;
     }
@@ -105,7 +106,7 @@ __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const 
 
 template <typename T>
 static int collect_impl(int nx, int ny, int nz, int haloy, const double* alpha, const double* ho, const double* hn,
-                        const double* dp, const T* cor, const T* adv, const T* diff, const T* idp,
+                        const double* dp, const T* cor, const T* adv, const T* diff, const double* idp,
                         const double* taus, const double* rr, double dt, T* ea2, T* ea4, cudaStream_t stream)
 {
     if (nx < 1 || ny <= 2 * haloy || nz < 1 || !alpha || !ho || !hn || !dp || !cor || !adv || !diff || !idp || !taus || !rr || !ea2 || !ea4)
@@ -130,7 +131,7 @@ extern "C" int getm_collect_3d_momentum_sources(int nx, int ny, int nz, int halo
 extern "C" int getm_collect_3d_momentum_sources_f32(int nx, int ny, int nz, int halox, int haloy,
                                                     const int* mask, const double* alpha, const double* ho,
                                                     const double* hn, const double* dp, const float* cor,
-                                                    const float* adv, const float* diff, const float* idp,
+                                                    const float* adv, const float* diff, const double* idp,
                                                     const double* taus, const double* rr, double dt,
                                                     float* ea2, float* ea4, cudaStream_t stream)
 {

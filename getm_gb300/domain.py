@@ -33,6 +33,15 @@ GRAVITY = 9.81  # python/pygetm/constants.py:4
 RHO0 = 1025.0  # python/pygetm/constants.py:3
 
 
+OMEGA = 2.0 * np.pi / 86164.0  # rotation rate of the earth (python/pygetm/domain.py:55-57)
+DEG2RAD = np.pi / 180
+
+
+def coriolis(lat):
+    """Coriolis parameter for latitude (python/pygetm/domain.py:60-69)."""
+    return (2.0 * OMEGA) * np.sin(DEG2RAD * np.asarray(lat, dtype=float))
+
+
 class EdgeTreatment(enum.Enum):
     """How supergrid edges are filled (python/pygetm/domain.py:19-24)."""
 
@@ -229,7 +238,12 @@ class Domain:
     parameter f, each given at centres (ny, nx) or as a scalar.
     """
 
-    def __init__(self, nx, ny, *, x, y, mask=1, H=None, z0=0.0, f=0.0, periodic_x=False, periodic_y=False):
+    def __init__(self, nx, ny, *, x, y, mask=1, H=None, z0=0.0, f=None, lat=None, periodic_x=False,
+                 periodic_y=False):
+        if f is None and lat is None:
+            raise Exception("Either lat of f must be provided to determine the Coriolis parameter.")
+        if f is None:
+            f = coriolis(lat)
         if periodic_x or periodic_y:
             raise NotImplementedError("periodic domains are not supported")
         self.nx, self.ny = nx, ny

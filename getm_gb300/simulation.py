@@ -160,13 +160,14 @@ class Simulation:
             self.salt = self.tracers.add("salt", molecular_diffusivity=1.1e-9)
             self.temp.fill(5.0)
             self.salt.fill(35.0)
-            self.rho = T.array(z=CENTERS, name="rho", dtype=d3)
-            self.buoy = T.array(z=CENTERS, name="buoy", dtype=d3)
+            # density, buoyancy and internal pressure stay float64 in both forms
+            self.rho = T.array(z=CENTERS, name="rho")
+            self.buoy = T.array(z=CENTERS, name="buoy")
             self.internal_pressure_method = internal_pressure
         if three_d:
             # internal_pressure.Base.initialize (python/pygetm/internal_pressure.py:14-30)
-            self.idpdx = self.U.array(z=CENTERS, name="idpdx", dtype=d3)
-            self.idpdy = self.V.array(z=CENTERS, name="idpdy", dtype=d3)
+            self.idpdx = self.U.array(z=CENTERS, name="idpdx")
+            self.idpdy = self.V.array(z=CENTERS, name="idpdy")
             self.idpdx.fill(0.0)
             self.idpdy.fill(0.0)
             self._P_work = torch.zeros((T.nz, T.ny_, T.nx_), dtype=torch.float64, device=T.device)
@@ -275,7 +276,7 @@ class Simulation:
         from ._lib import call
         from .core import _sfx
 
-        call("getm_density_buoyancy" + _sfx(self.salt.all_values, self.rho.all_values), n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
+        call("getm_density_buoyancy" + _sfx(self.salt.all_values, self.temp.all_values), n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
              self.depth.all_values.data_ptr(), self.rho.all_values.data_ptr(), self.buoy.all_values.data_ptr(),
              torch.cuda.current_stream().cuda_stream)
 

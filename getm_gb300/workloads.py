@@ -211,6 +211,44 @@ def seamount_temperature(zc: np.ndarray) -> np.ndarray:
     return 4.0 + 16.0 * (zc + 4500.0) / 4500.0
 
 
+def ensemble_member(rng: np.random.Generator, nmin: int = 64, nmax: int = 256, nzmin: int = 20,
+                    nzmax: int = 40, dx: float = 1000.0) -> Workload:
+    """One domain of the batched ensemble: sides log-uniform in [nmin, nmax],
+    nz log-uniform in [nzmin, nzmax], smoothed bathymetry 10-100 m, a 10-30 %
+    land mask (quantile threshold of a second smoothed field), a temperature
+    drop of 5-15 degC from surface to 100 m, wind stress uniform in
+    [0, 0.2] Pa along x, 20-40 substeps per 3D step."""
+    nx = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+    ny = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+    nz = int(round(np.exp(rng.uniform(np.log(nzmin), np.log(nzmax)))))
+    H = 10.0 + 90.0 * _norm01(gaussian_filter(rng.standard_normal((ny, nx)), sigma=6))
+    landf = rng.uniform(0.1, 0.3)
+    q = gaussian_filter(rng.standard_normal((ny, nx)), sigma=8)
+    mask = (q >= np.quantile(q, landf)).astype(int)
+    x = dx * (np.arange(nx) + 0.5)
+    y = dx * (np.arange(ny) + 0.5)
+    kappa, cd = 0.4, 2.5e-3
+    z0 = 0.5 * 50.0 / (np.exp(kappa / np.sqrt(cd)) - 1.0)
+    dom = create_cartesian(x, y, mask=mask, H=H, f=1e-4, z0=z0)
+    T = dom.create_grids(nz, halox=2, haloy=2, velocity_grids=2)
+    dga = calculate_sigma(nz)
+    split = int(rng.integers(20, 41))
+    params = dict(timestep=10.0, split_factor=split, num=1e-4, nuh=1e-4, z0=z0, scheme=5,
+                  taux=float(rng.uniform(0.0, 0.2)), dT=float(rng.uniform(5.0, 15.0)), land=landf)
+    return Workload(f"member{nx}x{ny}x{nz}", T, dga, {}, params)
+
+
+def ensemble(n: int = 256, seed: int = 4, **kwargs):
+    """The batched ensemble: n independent members (seeded)."""
+    rng = np.random.default_rng(seed)
+    return [ensemble_member(rng, **kwargs) for _ in range(n)]
+
+
+def member_temperature(zc: np.ndarray, dT: float) -> np.ndarray:
+    """Linear stratification: 20 degC at the surface, dT colder at 100 m."""
+    return 20.0 + dT * zc / 100.0
+
+
 def land_fraction(wl: Workload) -> float:
     m = wl.T.mask[wl.T.interior[1:]]
     return float((m == 0).mean())

@@ -277,12 +277,13 @@ int getm_density_buoyancy(int n, const double* salt, const double* temp, const d
 
 /* ---- mixed-precision form ------------------------------------------------
  * Same routines with float bulk fields (tracers, 3D velocities/transports,
- * their tendencies, nuh/num, buoyancy and the internal pressure gradient)
- * and float arithmetic for fluxes, limiters, the tridiagonal solve and the
- * pressure-gradient slopes.  Layer thicknesses, elevations, water depths,
- * metrics and 2D transports stay double; sums that decide conservation
- * (thickness updates, the w recursion, momentum sources, the EOS and the
- * column pressure integral) are evaluated in FP64.                        */
+ * their tendencies, nuh/num) and float arithmetic for fluxes, limiters and
+ * the tridiagonal solves.  Layer thicknesses, elevations, water depths,
+ * metrics, 2D transports, density, buoyancy and the internal pressure
+ * gradient stay double (the gradient is a small difference of large column
+ * integrals of buoyancy); the thickness updates, the w recursion and the
+ * momentum sources are evaluated in FP64.  The *_f32 internal-pressure
+ * entry points (float buoyancy and gradients) remain available.           */
 int getm_advection_apply_3d_batch_f32(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
                                       getm_grid* vgrid, int ufirst, const float* u, const float* v,
                                       const float* w, const float* const* w_var, const double* Ah_u,
@@ -309,7 +310,7 @@ int getm_grid_interp_xy_f32(int nx1, int ny1, int nx2, int ny2, int nz, const fl
 int getm_collect_3d_momentum_sources_f32(int nx, int ny, int nz, int halox, int haloy,
                                          const int* mask, const double* alpha, const double* ho,
                                          const double* hn, const double* dp, const float* cor,
-                                         const float* adv, const float* diff, const float* idp,
+                                         const float* adv, const float* diff, const double* idp,
                                          const double* taus, const double* rr, double dt,
                                          float* ea2, float* ea4, cudaStream_t stream);
 int getm_w_momentum_3d_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
@@ -335,7 +336,7 @@ int getm_shchepetkin_mcwilliams_f32(int nx, int ny, int nz, int imin, int imax, 
                                     float* idpdx, float* idpdy, double* P_work,
                                     cudaStream_t stream);
 int getm_density_buoyancy_f32(int n, const float* salt, const float* temp, const double* p,
-                              float* rho, float* buoy, cudaStream_t stream);
+                              double* rho, double* buoy, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

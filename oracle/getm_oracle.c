@@ -1,7 +1,7 @@
 /*
  * CPU oracle: a plain-C restatement of pygetm's Fortran operators on the
- * split-explicit time-step path.  TEST INFRASTRUCTURE ONLY - it is the checker
- * for the CUDA library, never part of the product path.
+ * split-explicit time-step path.  TEST INFRASTRUCTURE ONLY - the CUDA library
+ * is compared against it; it is never part of the product path.
  *
  * Every routine cites the reference routine it restates (paths within the
  * BoldingBruggeman/getm project).  Arithmetic is FP64 and follows the Fortran

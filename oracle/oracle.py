@@ -3,7 +3,7 @@
 Python/numpy restatement of pygetm's operator orchestration around the C
 restatement of its Fortran kernels (``getm_oracle.c``).  Only the tests,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use it, as the
-checker; the product path never imports it.
+reference for comparison; the product path never imports it.
 
 Parity pins: the reference ships no golden vectors and cannot be built here
 (no Fortran compiler, empty submodules), so the oracle is pinned by the

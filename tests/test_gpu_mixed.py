@@ -51,8 +51,10 @@ def test_apply_3d_batch_f32(scheme):
     trd = [wrap32(Td, t, CENTERS) for t in tr]
     ad.apply_3d_batch(wrap32(Td.ugrid, u, CENTERS), wrap32(Td.vgrid, v, CENTERS), wrap32(Td, w, INTERFACES), 600.0, trd)
     wet = Th.mask == 1
+    # HSIMT's 1/(1-cfl) term amplifies float32 rounding
+    tol = 1e-5 if scheme == 1 else 2e-6
     for a, b in zip(trd, tro):
-        assert rel(host(a.all_values), b, wet) < 2e-6
+        assert rel(host(a.all_values), b, wet) < tol
     # layer thicknesses are updated in float64 in both forms
     assert rel(host(ad.h), ao.h, wet) < 1e-12
 

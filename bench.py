@@ -47,6 +47,8 @@ def _args():
     ap.add_argument("--nx", type=int, default=400)
     ap.add_argument("--ny", type=int, default=300)
     ap.add_argument("--nz", type=int, default=40)
+    ap.add_argument("--error-steps", type=int, default=1000,
+                    help="3D steps after which the mixed form is compared with FP64 (0: skip)")
     return ap.parse_args()
 
 
@@ -162,7 +164,10 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _make_sim(wl, precision, device):
+def _make_sim(wl, precision, device, round_to_float32=True):
+    """Seamount simulation from rest; the initial temperature (20 -> 4 degC,
+    linear in depth) is rounded to float32 unless told otherwise, so both
+    forms start from identical fields."""
     import torch
 
     from getm_gb300.simulation import Simulation
@@ -172,6 +177,8 @@ def _make_sim(wl, precision, device):
     zc = sim.T.zc.all_values
     temp0 = torch.where(sim.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
                         sim.temp.all_values.double())
+    if round_to_float32:
+        temp0 = temp0.float().double()
     sim.temp.all_values.copy_(temp0)
     sim.start(p["timestep"], p["split_factor"])
     return sim
@@ -189,9 +196,13 @@ class Runner:
         from getm_gb300 import _lib
 
         self.sim = sim
+        self.totals0 = sim.totals_device().clone()
         split = sim.split_factor
-        for _ in range(max(warmup, 3) * split):
+        nwarm = max(warmup, 3)
+        nwarm += nwarm % self.period  # captured periods start on an even 3D step
+        for _ in range(nwarm * split):
             sim.advance()
+        self.steps_done = nwarm  # 3D steps run on the device so far
         torch.cuda.synchronize()
         n0 = _lib.launch_count()
         self.graph = None
@@ -207,10 +218,12 @@ class Runner:
             self.launches_per_period = _lib.launch_count() - n0
             for _ in range(2):
                 self.graph.replay()
+            self.steps_done += 2 * self.period  # the capture itself runs nothing
         else:
             for _ in range(self.period * split):
                 sim.advance()
             self.launches_per_period = _lib.launch_count() - n0
+            self.steps_done += self.period
         torch.cuda.synchronize()
 
     def run_period(self):
@@ -219,6 +232,11 @@ class Runner:
         else:
             for _ in range(self.period * self.sim.split_factor):
                 self.sim.advance()
+        self.steps_done += self.period
+
+    def run_to(self, nsteps):
+        while self.steps_done < nsteps:
+            self.run_period()
 
     def timed(self, nperiods, clocks_index=None):
         import torch
@@ -280,8 +298,50 @@ def _roofline(sim, peak, peak_kind):
     alg = n3 * (sz + 8 + 8 + 8 + len(fin) * 2 * sz)
     achieved = alg / t_kernel / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": f"hpass_x_kernel<{'float' if sz == 4 else 'double'}> (2 tracers)",
+            "traffic": None, "kernel": f"{'hpass_x_f32_kernel' if sz == 4 else 'hpass_x_kernel<double>'} (2 tracers)",
             "bytes_per_launch": alg, "us_per_launch": t_kernel * 1e6, "peak_kind": peak_kind}
+
+
+def _errors(wl, runners, args, device):
+    """Advance both forms (and an FP64 run from the unrounded initial
+    temperature, which shows how strongly the flow reacts to float32 rounding
+    of its initial state alone) to the same 3D step and compare fields and
+    compensated domain totals."""
+    import torch
+
+    target = max(args.error_steps, max(r.steps_done for r in runners.values()))
+    cond = Runner(_make_sim(wl, "fp64", device, round_to_float32=False), args.warmup, not args.no_graph)
+    for r in list(runners.values()) + [cond]:
+        r.run_to(target)
+    torch.cuda.synchronize()
+    steps = {r.steps_done for r in list(runners.values()) + [cond]}
+    assert len(steps) == 1, steps
+    wet = torch.from_numpy(wl.T.mask == 1).to(device)
+    uwet = torch.from_numpy(wl.T.ugrid.mask == 1).to(device)
+
+    def rel(x, y, m=wet):
+        x = x.double()[..., m]
+        y = y.double()[..., m]
+        return float((x - y).abs().max() / y.abs().max())
+
+    def compare(a, b):
+        za, zb = a.T.z.all_values[wet], b.T.z.all_values[wet]
+        return {"temp": rel(a.temp.all_values, b.temp.all_values), "salt": rel(a.salt.all_values, b.salt.all_values),
+                "z": float((za - zb).abs().max() / zb.abs().max()), "z_abs_m": float((za - zb).abs().max()),
+                "z_max_m": float(zb.abs().max()), "U": rel(a.momentum.U.all_values, b.momentum.U.all_values, uwet),
+                "uk": rel(a.momentum.uk.all_values, b.momentum.uk.all_values, uwet)}
+
+    a, b = runners["mixed"], runners["fp64"]
+    out = {"steps": steps.pop()}
+    out.update(compare(a.sim, b.sim))
+    ta, tb = a.sim.totals_device(), b.sim.totals_device()
+    names = ["volume", "temp", "salt"]
+    out["totals_vs_fp64"] = {n: float((x - y) / y) for n, x, y in zip(names, ta.tolist(), tb.tolist())}
+    out["totals_drift"] = {f: {n: float((x - y) / y) for n, x, y in
+                               zip(names, r.sim.totals_device().tolist(), r.totals0.tolist())}
+                           for f, r in (("mixed", a), ("fp64", b))}
+    out["fp64_from_unrounded_initial_state"] = compare(cond.sim, b.sim)
+    return out
 
 
 def run_ours(args):
@@ -351,20 +411,10 @@ def run_ours(args):
         e2e[f] = {"value": cells * nsteps * ws / dt, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                   "d2h_bytes_per_step": d2h // period}
 
-    # error of the mixed form against FP64 (both advanced the same steps)
+    # error of the mixed form against FP64 after the same number of 3D steps
     err = None
-    if "mixed" in runners and "fp64" in runners:
-        a, b = runners["mixed"].sim, runners["fp64"].sim
-        wet = torch.from_numpy(wl.T.mask == 1).to(device)
-
-        def rel(x, y):
-            x = x.double()[..., wet]
-            y = y.double()[..., wet]
-            return float((x - y).abs().max() / y.abs().max())
-
-        err = {"temp": rel(a.temp.all_values, b.temp.all_values), "salt": rel(a.salt.all_values, b.salt.all_values),
-               "z": rel(a.T.z.all_values, b.T.z.all_values), "U": rel(a.momentum.U.all_values, b.momentum.U.all_values),
-               "steps": runners[primary].sim.istep // split}
+    if "mixed" in runners and "fp64" in runners and args.error_steps > 0 and rank == 0:
+        err = _errors(wl, runners, args, device)
 
     peak, peak_kind = _peaks()
     roofline = _roofline(runners[primary].sim, peak, peak_kind)

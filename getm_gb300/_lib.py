@@ -16,6 +16,8 @@ _HERE = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ.get("GETM_GB300_LIB", _HERE / "libgetm_gb300.so"))
 
 GETM_OK = 0
+GETM_MAX_TOTALS = 16      # include/getm_gb300.h
+GETM_TOTALS_BLOCKS = 608  # include/getm_gb300.h
 ERRORS = {
     1: "invalid argument",
     2: "CUDA launch/runtime error",
@@ -91,6 +93,8 @@ _SIGS = {
     "getm_blumberg_mellor_f32": "iiiiiiipppppppppps",
     "getm_shchepetkin_mcwilliams_f32": "iiiiiiipppppppppppps",
     "getm_density_buoyancy_f32": "ippppps",
+    "getm_domain_totals": "iiiiiiippppippps",
+    "getm_domain_totals_f32": "iiiiiiippppippps",
 }
 _CT = {"i": c_int, "d": c_double, "p": c_void_p, "s": c_void_p, "c": ctypes.c_char_p}
 

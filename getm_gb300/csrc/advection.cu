@@ -52,7 +52,42 @@ extern "C" int getm_create_grid(int imin, int imax, int jmin, int jmax, int kmin
 
 extern "C" int getm_grid_finalize(getm_grid* grid)
 {
+    if (grid) {
+        cudaFree(grid->dx_f); cudaFree(grid->dy_f); cudaFree(grid->idx_f);
+        cudaFree(grid->idy_f); cudaFree(grid->iarea_f);
+    }
     free(grid);
+    return GETM_OK;
+}
+
+__global__ void to_float_kernel(long long n, const double* src, float* dst)
+{
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) dst[p] = (float)src[p];
+}
+
+int getm_grid_f32_metrics(getm_grid* g, cudaStream_t stream)
+{
+    if (!g) return GETM_ERR_ARG;
+    if (g->iarea_f) return GETM_OK;  // built last: its presence means all are there
+    const long long n = (long long)g->nx_ * g->ny_;
+    // one-time setup: order it after every earlier write of the metrics on
+    // any stream, and complete it before returning
+    if (cudaDeviceSynchronize() != cudaSuccess) return GETM_ERR_CUDA;
+    const double* src[5] = {g->dx, g->dy, g->idx, g->idy, g->iarea};
+    float** dst[5] = {&g->dx_f, &g->dy_f, &g->idx_f, &g->idy_f, &g->iarea_f};
+    for (int q = 0; q < 5; q++) {
+        if (!src[q]) continue;  // metric not registered on this grid
+        float* d = NULL;
+        if (cudaMalloc(&d, n * sizeof(float)) != cudaSuccess) return GETM_ERR_ALLOC;
+        to_float_kernel<<<getm_div_up(n, 256), 256, 0, stream>>>(n, src[q], d);
+        GETM_CHECK_LAUNCH();
+        *dst[q] = d;
+    }
+    if (!g->iarea_f) {  // grids without cell areas (velocity grids): mark as built
+        if (cudaMalloc(&g->iarea_f, sizeof(float)) != cudaSuccess) return GETM_ERR_ALLOC;
+    }
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return GETM_ERR_CUDA;
     return GETM_OK;
 }
 
@@ -170,6 +205,11 @@ struct HPassArgs {
     double dt;
     int scheme;
     int ntracer;
+    // mixed form: float copies of dt and of the metrics above
+    float dtf;
+    const float* idx_f;
+    const float* dy_f;
+    const float* iA_f;
     const T* fin[GETM_MAX_BATCH];
     T* fout[GETM_MAX_BATCH];
 };
@@ -326,6 +366,163 @@ __global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs<T> a)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed form (float fields): increment form of the same passes.
+//
+// With hold - hnew = dt iA (QU_e - QU_w), the reference update
+// (hold f - dt iA (QU_e f_e - QU_w f_w)) / hnew equals
+//     f - dt iA (QU_e (f_e - f) - QU_w (f_w - f)) / hnew
+// exactly, where f_e, f_w are the limited face values.  Each face therefore
+// provides QU (face - left cell) and QU (face - right cell), formed from
+// differences of neighbouring values, so float32 rounding scales with the
+// change of the field, a field at rest is reproduced exactly, and the only
+// FP64 operations per cell are the thickness update hnew = hold - dh.
+// ---------------------------------------------------------------------------
+struct FaceGeomF {
+    float QU, cfl;
+    bool active, up, uu_ok;
+};
+
+__device__ __forceinline__ FaceGeomF face_geom_f32(const HPassArgs<float>& a, long long p2, long long p3,
+                                                    long long s, bool in_range)
+{
+    FaceGeomF g;
+    g.QU = 0.f; g.cfl = 0.f; g.active = false; g.up = false; g.uu_ok = false;
+    if (!in_range) return g;
+    int m = a.umask[p2];
+    if (!getm_flux_point(m)) return g;
+    float uu = a.u[p3];
+    g.active = true;
+    g.QU = uu * (float)a.hu[p3] * a.dy_f[p2];
+    g.cfl = fabsf(uu * a.dtf * a.idx_f[p2]);
+    g.up = uu > 0.f;
+    g.uu_ok = getm_flux_point(g.up ? a.umask[p2 - s] : a.umask[p2 + s]);
+    return g;
+}
+
+// Face between cells p and p+s: el = QU (face - f[p]), er = QU (face - f[p+s]),
+// the diffusive flux (when Ah is given) added to both.
+__device__ __forceinline__ void face_dev_f32(const HPassArgs<float>& a, const FaceGeomF& g,
+                                             const float* __restrict__ f, long long p2, long long p3,
+                                             long long s, float& el, float& er)
+{
+    el = 0.f; er = 0.f;
+    if (!g.active) return;
+    const float f0 = f[p3], f1 = f[p3 + s];
+    const float d = f1 - f0;
+    float dev;
+    if (g.up) dev = getm_tvd_dev<float>(a.scheme, g.uu_ok ? f[p3 - s] : f0, f0, f1, g.cfl);
+    else dev = getm_tvd_dev<float>(a.scheme, g.uu_ok ? f[p3 + 2 * s] : f1, f1, f0, g.cfl);
+    el = g.QU * (g.up ? dev : d + dev);
+    er = g.QU * (g.up ? dev - d : dev);
+    if (a.Ah) {
+        float fdiff = -(float)a.Ah[p2] * (float)a.hu[p3] * d * a.idx_f[p2] * a.dy_f[p2];
+        el += fdiff;
+        er += fdiff;
+    }
+}
+
+// x-direction pass, float fields.  Launch geometry as hpass_x_kernel.
+__global__ void __launch_bounds__(256) hpass_x_f32_kernel(HPassArgs<float> a)
+{
+    const int lane = threadIdx.x;
+    const int i = blockIdx.x * 32 + lane;
+    const long long row = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+    if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
+    const int k = (int)(row / a.ny_);
+    const int j = (int)(row - (long long)k * a.ny_);
+    const bool inx = i < a.nx_;
+    const long long p2 = (long long)j * a.nx_ + i;
+    const long long p3 = (long long)k * a.plane + p2;
+    const bool jrow = j >= a.jlo && j <= a.jhi;
+
+    FaceGeomF gr = face_geom_f32(a, p2, p3, 1, inx && jrow && i >= a.ilo - 1 && i <= a.ihi);
+    FaceGeomF gl = face_geom_f32(a, p2 - 1, p3 - 1, 1, lane == 0 && jrow && i - 1 >= a.ilo - 1 && i - 1 <= a.ihi);
+    float QUl = __shfl_up_sync(0xffffffffu, gr.QU, 1);
+    if (lane == 0) QUl = gl.QU;
+    const bool upd = inx && jrow && i >= a.ilo && i <= a.ihi && a.tmask[p2] == 1;
+
+    float coef = 0.f;  // dt iA / hnew
+    if (inx) {
+        const double hold = a.h_in[p3];
+        double hnew = hold;
+        if (upd) {
+            const float ia = a.iA_f[p2];
+            const float dh = a.dtf * (gr.QU - QUl) * ia;
+            hnew = hold - (double)dh;
+            coef = a.dtf * ia / (float)hnew;
+        }
+        a.h_out[p3] = hnew;
+    }
+    for (int t = 0; t < a.ntracer; t++) {
+        const float* __restrict__ f = a.fin[t];
+        float el = 0.f, er = 0.f;
+        if (inx) face_dev_f32(a, gr, f, p2, p3, 1, el, er);
+        float erw = __shfl_up_sync(0xffffffffu, er, 1);
+        if (lane == 0) {
+            float elw;
+            face_dev_f32(a, gl, f, p2 - 1, p3 - 1, 1, elw, erw);
+        }
+        if (inx) {
+            const float fo = f[p3];
+            a.fout[t][p3] = upd ? fo - coef * (el - erw) : fo;
+        }
+    }
+}
+
+// y-direction pass, float fields.  Launch geometry as hpass_y_kernel.
+__global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_f32_kernel(HPassArgs<float> a)
+{
+    __shared__ float sQ[GETM_V_BY][32];
+    __shared__ float sE[GETM_V_BY][32];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = blockIdx.x * 32 + tx;
+    const int j = blockIdx.y * GETM_V_BY + ty;
+    const int k = blockIdx.z;
+    const bool in = i < a.nx_ && j < a.ny_;
+    const long long s = a.nx_;
+    const long long p2 = (long long)j * a.nx_ + i;
+    const long long p3 = (long long)k * a.plane + p2;
+    const bool icol = i >= a.ilo && i <= a.ihi;
+
+    FaceGeomF gt = face_geom_f32(a, p2, p3, s, in && icol && j >= a.jlo - 1 && j <= a.jhi);
+    FaceGeomF gb = face_geom_f32(a, p2 - s, p3 - s, s, in && ty == 0 && icol && j - 1 >= a.jlo - 1 && j - 1 <= a.jhi);
+    sQ[ty][tx] = gt.QU;
+    __syncthreads();
+    const float QUb = ty > 0 ? sQ[ty - 1][tx] : gb.QU;
+    const bool upd = in && icol && j >= a.jlo && j <= a.jhi && a.tmask[p2] == 1;
+
+    float coef = 0.f;
+    if (in) {
+        const double hold = a.h_in[p3];
+        double hnew = hold;
+        if (upd) {
+            const float ia = a.iA_f[p2];
+            const float dh = a.dtf * (gt.QU - QUb) * ia;
+            hnew = hold - (double)dh;
+            coef = a.dtf * ia / (float)hnew;
+        }
+        a.h_out[p3] = hnew;
+    }
+    for (int t = 0; t < a.ntracer; t++) {
+        const float* __restrict__ f = a.fin[t];
+        float el = 0.f, er = 0.f, ers = 0.f;
+        if (in) face_dev_f32(a, gt, f, p2, p3, s, el, er);
+        if (ty == 0 && in) {
+            float els;
+            face_dev_f32(a, gb, f, p2 - s, p3 - s, s, els, ers);
+        }
+        __syncthreads();  // previous tracer's reads of sE are done
+        sE[ty][tx] = er;
+        __syncthreads();
+        if (ty > 0) ers = sE[ty - 1][tx];
+        if (in) {
+            const float fo = f[p3];
+            a.fout[t][p3] = upd ? fo - coef * (el - ers) : fo;
+        }
+    }
+}
+
 template <typename T>
 static int launch_hpass(int direction, HPassArgs<T>& a, cudaStream_t stream)
 {
@@ -333,11 +530,13 @@ static int launch_hpass(int direction, HPassArgs<T>& a, cudaStream_t stream)
         const int BY = 8;
         dim3 block(32, BY);
         dim3 grid(getm_div_up(a.nx_, 32), getm_div_up((long long)a.ny_ * a.nk, BY));
-        hpass_x_kernel<T><<<grid, block, 0, stream>>>(a);
+        if constexpr (getm_increment_form<T>) hpass_x_f32_kernel<<<grid, block, 0, stream>>>(a);
+        else hpass_x_kernel<T><<<grid, block, 0, stream>>>(a);
     } else {
         dim3 block(32, GETM_V_BY);
         dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, GETM_V_BY), a.nk);
-        hpass_y_kernel<T><<<grid, block, 0, stream>>>(a);
+        if constexpr (getm_increment_form<T>) hpass_y_f32_kernel<<<grid, block, 0, stream>>>(a);
+        else hpass_y_kernel<T><<<grid, block, 0, stream>>>(a);
     }
     GETM_CHECK_LAUNCH();
     return GETM_OK;
@@ -364,6 +563,16 @@ static int hpass_setup(HPassArgs<T>& a, int direction, const getm_advection* adv
     if (!a.idx || !a.dy) return GETM_ERR_ARG;
     a.tmask = tg->mask; a.iA = tg->iarea; a.Ah = Ah; a.u = u; a.hu = hu; a.dt = dt;
     a.scheme = adv->scheme;
+    a.dtf = (float)dt;
+    if constexpr (getm_increment_form<T>) {
+        int rc = getm_grid_f32_metrics(const_cast<getm_grid*>(tg), 0);
+        if (!rc) rc = getm_grid_f32_metrics(const_cast<getm_grid*>(vg), 0);
+        if (rc) return rc;
+        a.iA_f = tg->iarea_f;
+        if (direction == 1) { a.idx_f = vg->idx_f; a.dy_f = vg->dy_f; }
+        else { a.idx_f = vg->idy_f; a.dy_f = vg->dx_f; }
+        if (!a.iA_f || !a.idx_f || !a.dy_f) return GETM_ERR_ARG;
+    }
     return GETM_OK;
 }
 
@@ -446,15 +655,61 @@ __device__ void w_substep(const WPassArgs<T>& a, long long c, const T* wv, const
             flux = wvk * fu;
         }
         T wk = a.w[c + (k + 1) * P];
-        T hfo = (T)hk * fk;
-        double hn = hk - dtk * ((double)wk - (double)wkm1);
+        double dh = dtk * ((double)wk - (double)wkm1);
+        double hn = hk - dh;
         T advn = flux - fluxm;
         hd[c + k * P] = hn;
+        T hfo = (T)hk * fk;
         fdst[c + k * P] = (hfo - (T)dtk * advn) / (T)hn;
         // shift window
         fluxm = flux; wkm1 = wk;
         fkm1 = fk; fk = fk1; fk1 = fk2;
         hk = hk1; hk1 = hk2;
+    }
+}
+
+// Mixed form of w_substep: the increment form of the horizontal passes in
+// the vertical (see hpass_x_f32_kernel).  With flux_k = W_k f + e_k at the
+// interface above level k (W_k = w_var there, 0 at the surface) and
+// dh = dtk (w_k - w_{k-1}), the reference update equals
+//     f + dtk ((w_k - W_k - w_{k-1} + W_{k-1}) f - e_k + e'_{k-1}) / hn
+// with e_k = W_k (face_k - f_k) and e'_{k-1} = W_{k-1} (face_{k-1} - f_k).
+__device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const float* wv, const double* hs,
+                              const float* fs, double* hd, float* fdst, double dtk, double itersm1)
+{
+    const long long P = a.plane;
+    const int nz = a.nz;
+    const float dtkf = (float)dtk, itf = (float)itersm1, dtf = (float)a.dt;
+    float fkm1 = 0.f, fk = fs[c], fk1 = (nz > 1) ? fs[c + P] : 0.f;
+    double hk = hs[c], hk1 = (nz > 1) ? hs[c + P] : 0.0;
+    float hkf = (float)hk, hk1f = (float)hk1;
+    float erm = 0.f;   // e'_{k-1}: interface below, deviation from level k
+    float Wm = 0.f;    // W_{k-1} (0 below the bottom level)
+    float wkm1 = a.w[c];
+    for (int k = 0; k < nz; k++) {
+        float fk2 = 0.f;
+        double hk2 = 0.0;
+        if (k + 2 < nz) { fk2 = fs[c + (k + 2) * P]; hk2 = hs[c + (k + 2) * P]; }
+        float el = 0.f, er = 0.f, W = 0.f;
+        if (k < nz - 1) {
+            W = wv[c + (k + 1) * P];
+            const float cfl = fabsf(W) * dtf / fminf(hkf, hk1f) * itf;
+            const float d = fk1 - fk;
+            float dev;
+            if (W > 0.f) dev = getm_tvd_dev<float>(a.scheme, (k > 0) ? fkm1 : fk, fk, fk1, cfl);
+            else dev = getm_tvd_dev<float>(a.scheme, (k < nz - 2) ? fk2 : fk1, fk1, fk, cfl);
+            el = W * (W > 0.f ? dev : d + dev);
+            er = W * (W > 0.f ? dev - d : dev);
+        }
+        const float wk = a.w[c + (k + 1) * P];
+        const float dh = dtkf * (wk - wkm1);
+        const double hn = hk - (double)dh;
+        hd[c + k * P] = hn;
+        fdst[c + k * P] = fk + dtkf * (((wk - W) - (wkm1 - Wm)) * fk - el + erm) / (float)hn;
+        erm = er; Wm = W; wkm1 = wk;
+        fkm1 = fk; fk = fk1; fk1 = fk2;
+        hk = hk1; hk1 = hk2;
+        hkf = hk1f; hk1f = (float)hk2;
     }
 }
 
@@ -465,6 +720,17 @@ __device__ double w_maxcfl(const WPassArgs<T>& a, long long c, const T* wv, cons
 {
     const long long P = a.plane;
     T cmax = T(-1);
+    if constexpr (getm_increment_form<T>) {
+        const float dtf = (float)a.dt;
+        float hk = (float)hs[c];
+        for (int k = 1; k < a.nz; k++) {
+            const float hk1 = (float)hs[c + k * P];
+            const float cfl = fabsf(wv[c + k * P]) * dtf / fminf(hk, hk1);
+            if (k == 1 || cfl > cmax) cmax = cfl;
+            hk = hk1;
+        }
+        return (double)cmax;
+    }
     double hk = hs[c];
     for (int k = 1; k < a.nz; k++) {
         double hk1 = hs[c + k * P];
@@ -519,7 +785,8 @@ __global__ void __launch_bounds__(128) wpass_kernel(WPassArgs<T> a)
             // The last sub-step writes the tracer in place and the thickness
             // into haux (the stage's h_in must survive for the next tracer).
             T* fd = (it == iters) ? f : a.faux;
-            w_substep(a, c, wv, hs, fs, a.haux, fd, dtk, itersm1);
+            if constexpr (getm_increment_form<T>) w_substep_f32(a, c, wv, hs, fs, a.haux, fd, dtk, itersm1);
+            else w_substep(a, c, wv, hs, fs, a.haux, fd, dtk, itersm1);
             it++;
         }
     }

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "getm_gb300.h"
 
 // Physical constants of python/src/wrapper.F90:11-13 (module pygetm).
@@ -25,7 +27,21 @@ struct getm_grid {
     const double* idy;
     const double* iarea;
     const double* area;
+    // float copies of the metrics for the mixed form, built on first use by
+    // getm_grid_f32_metrics (device memory owned by the handle)
+    float* dx_f;
+    float* dy_f;
+    float* idx_f;
+    float* idy_f;
+    float* iarea_f;
 };
+
+// Build the float metric copies of a grid if they do not exist yet (one
+// cudaMalloc per array and a conversion kernel on `stream`, synchronised with
+// the whole device before and after); returns a GETM_* status.  The first
+// mixed-form call on a grid makes them, so that call must precede any stream
+// capture.
+int getm_grid_f32_metrics(getm_grid* g, cudaStream_t stream);
 
 // Host-side count of kernel launches issued by this library (one increment
 // per launch site executed); read with getm_launch_count().
@@ -39,6 +55,14 @@ extern "C" unsigned long long getm_launch_counter_add(void);
     } while (0)
 
 static inline unsigned int getm_div_up(long long a, long long b) { return (unsigned int)((a + b - 1) / b); }
+
+// True for the mixed form's float bulk type.  Its update kernels use the
+// increment form x_new = x_old + dx, with dx formed from small differences,
+// so a field that does not change is reproduced exactly and float32 rounding
+// scales with the change rather than with the field; the FP64 form keeps the
+// reference's evaluation order operation by operation.
+template <typename T>
+constexpr bool getm_increment_form = std::is_same<T, float>::value;
 
 // ---------------------------------------------------------------------------
 // TVD limiter (src/operators/advection_schemes/limiters.h:1-44).  T is the
@@ -93,6 +117,22 @@ __device__ __forceinline__ T getm_tvd_face(int scheme, T fuu, T fu, T fd, T cfl)
         fu = fu + T(0.5) * limiter * (T(1) - cfl) * deltaf;
     }
     return fu;
+}
+
+// The limited part of the TVD face value, face - fu (0 where the limiter is
+// inactive): the same arithmetic as getm_tvd_face without the final sum, so
+// the increment form can work with deviations from cell values.
+template <typename T>
+__device__ __forceinline__ T getm_tvd_dev(int scheme, T fuu, T fu, T fd, T cfl)
+{
+    T deltaf = fd - fu;
+    T deltafu = fu - fuu;
+    if (deltaf * deltafu > T(0)) {
+        T ratio = deltafu / deltaf;
+        T limiter = getm_limiter<T>(scheme, ratio, cfl);
+        return T(0.5) * limiter * (T(1) - cfl) * deltaf;
+    }
+    return T(0);
 }
 
 __device__ __forceinline__ bool getm_flux_point(int m) { return m == 1 || m == 2; }

@@ -65,11 +65,23 @@ __device__ __forceinline__ void vd_aux(const VDArgs<T>& a, long long c, int k, d
     auxn = (T)a.cnpar * x / ((T)a.hn[c + (k + 1) * P] + (T)a.hn[c + k * P]);
 }
 
-// Thread per column; dynamic shared memory holds ru/qu: 2 * nz * blockDim values.
+// Thread per column; dynamic shared memory holds ru/qu (and, in the
+// increment form, the old values): vd_smem_arrays<T> * nz * blockDim values.
+//
+// Increment form (float): with x the old values and A x_new = a4 the
+// reference system, the kernel solves A dx = a4 - A x, whose right-hand side
+// reduces to differences that float32 holds exactly or nearly so:
+//   r_k = x_k (ho_k - hn_k) + (x_{k+1} - x_k)(auxo + auxn)_{k+1/2}
+//         + (x_{k-1} - x_k)(auxo + auxn)_{k-1/2} + ea4_k + ea2_k x_k
+// and writes x + dx.
+template <typename T>
+constexpr int vd_smem_arrays = getm_increment_form<T> ? 3 : 2;
+
 template <typename T>
 __global__ void vd_column_kernel(VDArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char vd_smem[];
+    constexpr bool inc = getm_increment_form<T>;
     const int tid = threadIdx.x;
     const int nthreads = blockDim.x;
     const int i = blockIdx.x * blockDim.x + tid;
@@ -80,17 +92,26 @@ __global__ void vd_column_kernel(VDArgs<T> a)
     const int nz = a.nz;
     if (nz == 1) {  // diffusion.F90:224-231: every point, mask not consulted
         for (int t = 0; t < a.ntracer; t++) {
-            T a4 = (T)a.ho[c] * a.var[t][c];
+            T x = a.var[t][c];
             T a2 = (T)a.hn[c];
-            if (a.ea4[t]) a4 = a4 + a.ea4[t][c];
             if (a.ea2[t]) a2 = a2 - a.ea2[t][c];
-            a.var[t][c] = a4 / a2;
+            if constexpr (inc) {
+                T r = x * (T)(a.ho[c] - a.hn[c]);
+                if (a.ea4[t]) r = r + a.ea4[t][c];
+                if (a.ea2[t]) r = r + a.ea2[t][c] * x;
+                a.var[t][c] = x + r / a2;
+            } else {
+                T a4 = (T)a.ho[c] * x;
+                if (a.ea4[t]) a4 = a4 + a.ea4[t][c];
+                a.var[t][c] = a4 / a2;
+            }
         }
         return;
     }
     if (a.mask[c] != 1) return;
     T* ru = (T*)vd_smem;                        // ru[k * nthreads + tid]
     T* qu = ru + (size_t)nz * nthreads;
+    T* xo = qu + (size_t)nz * nthreads;         // increment form: old values
     for (int t = 0; t < a.ntracer; t++) {
         T* __restrict__ var = a.var[t];
         const T* ea2 = a.ea2[t];
@@ -104,7 +125,14 @@ __global__ void vd_column_kernel(VDArgs<T> a)
         T vkm1 = var[c + (k - 1) * P];
         T a1 = -anb;
         T a2 = (T)a.hn[c + k * P] + anb;
-        T a4 = vk * (T)a.ho[c + k * P] + (vkm1 - vk) * aob;
+        T a4;
+        if constexpr (inc) {
+            xo[k * nthreads + tid] = vk;
+            a4 = vk * (T)(a.ho[c + k * P] - a.hn[c + k * P]) + (vkm1 - vk) * (aob + anb);
+            if (ea2) a4 = a4 + ea2[c + k * P] * vk;
+        } else {
+            a4 = vk * (T)a.ho[c + k * P] + (vkm1 - vk) * aob;
+        }
         if (ea2) a2 = a2 - ea2[c + k * P];
         if (ea4) a4 = a4 + ea4[c + k * P];
         T rk = a1 / a2;
@@ -121,7 +149,14 @@ __global__ void vd_column_kernel(VDArgs<T> a)
             T a3 = -ana;
             a1 = -anb;
             a2 = (T)a.hn[c + k * P] + ana + anb;
-            a4 = vk * (T)a.ho[c + k * P] + (vkp1 - vk) * aoa + (vkm1 - vk) * aob;
+            if constexpr (inc) {
+                xo[k * nthreads + tid] = vk;
+                a4 = vk * (T)(a.ho[c + k * P] - a.hn[c + k * P]) + (vkp1 - vk) * (aoa + ana) +
+                     (vkm1 - vk) * (aob + anb);
+                if (ea2) a4 = a4 + ea2[c + k * P] * vk;
+            } else {
+                a4 = vk * (T)a.ho[c + k * P] + (vkp1 - vk) * aoa + (vkm1 - vk) * aob;
+            }
             if (ea2) a2 = a2 - ea2[c + k * P];
             if (ea4) a4 = a4 + ea4[c + k * P];
             T den = a2 - a3 * rk;
@@ -136,16 +171,29 @@ __global__ void vd_column_kernel(VDArgs<T> a)
         {
             T a3 = -ana;
             a2 = (T)a.hn[c] + ana;
-            a4 = vk * (T)a.ho[c] + (vkp1 - vk) * aoa;
+            if constexpr (inc) {
+                a4 = vk * (T)(a.ho[c] - a.hn[c]) + (vkp1 - vk) * (aoa + ana);
+                if (ea2) a4 = a4 + ea2[c] * vk;
+            } else {
+                a4 = vk * (T)a.ho[c] + (vkp1 - vk) * aoa;
+            }
             if (ea2) a2 = a2 - ea2[c];
             if (ea4) a4 = a4 + ea4[c];
             T q0 = (a4 - a3 * qk) / (a2 - a3 * rk);
             // back substitution :304-307
             T vprev = q0;
-            var[c] = q0;
-            for (k = 1; k < nz; k++) {
-                vprev = qu[k * nthreads + tid] - ru[k * nthreads + tid] * vprev;
-                var[c + k * P] = vprev;
+            if constexpr (inc) {
+                var[c] = vk + q0;
+                for (k = 1; k < nz; k++) {
+                    vprev = qu[k * nthreads + tid] - ru[k * nthreads + tid] * vprev;
+                    var[c + k * P] = xo[k * nthreads + tid] + vprev;
+                }
+            } else {
+                var[c] = q0;
+                for (k = 1; k < nz; k++) {
+                    vprev = qu[k * nthreads + tid] - ru[k * nthreads + tid] * vprev;
+                    var[c + k * P] = vprev;
+                }
             }
         }
     }
@@ -171,8 +219,9 @@ template <typename T>
 static int vd_launch(VDArgs<T>& a, cudaStream_t stream)
 {
     int threads = 128;
-    while (threads > 32 && (size_t)2 * a.nz * threads * sizeof(T) > 160 * 1024) threads /= 2;
-    size_t smem = (size_t)2 * a.nz * threads * sizeof(T);
+    const size_t per = (size_t)vd_smem_arrays<T> * a.nz * sizeof(T);
+    while (threads > 32 && per * threads > 160 * 1024) threads /= 2;
+    size_t smem = per * threads;
     if (smem > 200 * 1024) return GETM_ERR_NZ;
     static bool attr_set = false;
     if (!attr_set) {

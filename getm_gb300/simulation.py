@@ -101,9 +101,10 @@ class Simulation:
                  Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
                  nuh: float = 0.0, precision: str = "fp64", device="cuda"):
         """``precision``: "fp64" (the plain form) or "mixed" (float32 tracers,
-        3D velocities and their tendencies, diffusivities, buoyancy and
-        internal pressure; float64 elevations, depths, layer thicknesses, 2D
-        transports and their accumulation)."""
+        3D velocities and their tendencies and diffusivities; float64
+        elevations, depths, layer thicknesses, 2D transports and their
+        accumulation, density, buoyancy, internal pressure and the budget
+        sums of ``totals``)."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
@@ -285,6 +286,38 @@ class Simulation:
             _pygetm.blumberg_mellor(self.buoy, self.idpdx, self.idpdy)
         else:
             _pygetm.shchepetkin_mcwilliams(self.buoy, self.idpdx, self.idpdy, self._P_work)
+
+    def totals_device(self) -> torch.Tensor:
+        """Device tensor [total volume, total of each tracer] (compensated
+        FP64 sums, see ``totals``); no host synchronisation."""
+        from ._lib import GETM_TOTALS_BLOCKS, call, ptr_array
+        from .core import _sfx
+
+        T = self.T
+        trs = list(self.tracers._tracers) if self.runtype > RunType.BAROTROPIC_2D else []
+        n = 1 + len(trs)
+        if getattr(self, "_tot_out", None) is None or self._tot_out.numel() != n:
+            self._tot_out = torch.zeros(n, dtype=torch.float64, device=T.device)
+            self._tot_work = torch.zeros(2 * GETM_TOTALS_BLOCKS * n, dtype=torch.float64, device=T.device)
+        hn = T.hn.all_values if trs else T.D.all_values
+        sfx = _sfx(*[t.all_values for t in trs]) if trs else ""
+        call("getm_domain_totals" + sfx, T.nx_, T.ny_, max(T.nz, 1), T.halox, T.haloy, T.nx, T.ny,
+             T.mask.all_values.data_ptr(), T.area.all_values.data_ptr(), T.D.all_values.data_ptr(), hn.data_ptr(),
+             len(trs),
+             ptr_array([t.all_values.data_ptr() for t in trs]), self._tot_work.data_ptr(), self._tot_out.data_ptr(),
+             torch.cuda.current_stream().cuda_stream)
+        return self._tot_out
+
+    @property
+    def totals(self):
+        """python/pygetm/simulation.py:1409-1444: (total volume, [(tracer,
+        total, mean)]) with total volume = sum of D * area and tracer total =
+        sum of c * area * hn over the unmasked interior, mean = total / total
+        volume.  The sums are compensated (double-double) and reproducible."""
+        out = self.totals_device().cpu().tolist()
+        trs = list(self.tracers._tracers) if self.runtype > RunType.BAROTROPIC_2D else []
+        vol = out[0]
+        return vol, [(t, tot, tot / vol) for t, tot in zip(trs, out[1:])]
 
     def advance_surface_elevation(self, timestep: float, U: Array, V: Array, fwf: Array):
         """simulation.py:1468-1486"""

@@ -46,6 +46,10 @@ typedef struct CUstream_st* cudaStream_t;
 /* largest number of layers the column kernels (vertical advection and
  * diffusion) accept */
 #define GETM_MAX_NZ 256
+/* tracers per getm_domain_totals call, and blocks of its first stage (the
+ * work buffer holds 2 * GETM_TOTALS_BLOCKS * (1 + ntracer) doubles) */
+#define GETM_MAX_TOTALS 16
+#define GETM_TOTALS_BLOCKS 608
 
 typedef struct getm_grid getm_grid;
 typedef struct getm_advection getm_advection;
@@ -337,6 +341,26 @@ int getm_shchepetkin_mcwilliams_f32(int nx, int ny, int nz, int imin, int imax, 
                                     cudaStream_t stream);
 int getm_density_buoyancy_f32(int n, const float* salt, const float* temp, const double* p,
                               double* rho, double* buoy, cudaStream_t stream);
+
+/* ---- domain totals (compensated budget sums) -----------------------------
+ * Replaces python/pygetm/simulation.py:1409-1444 (Simulation.totals: total
+ * volume = sum of D*area, tracer total = sum of c*area*hn over unmasked
+ * interior points) and the Array.global_sum it calls
+ * (python/pygetm/core.py:820-839).  Sums are double-double (error-free
+ * transformations) in a fixed reduction order: correctly rounded to a few
+ * ulps and bitwise reproducible.  nx_/ny_: full extents; nx/ny: interior
+ * extents starting at (halox, haloy).  tracers: HOST array of ntracer
+ * device pointers (nz layers each).  work: device buffer of
+ * 2 * GETM_TOTALS_BLOCKS * (1 + ntracer) doubles.  out: device array of
+ * 1 + ntracer doubles (volume, then each tracer).                          */
+int getm_domain_totals(int nx_, int ny_, int nz, int halox, int haloy, int nx, int ny,
+                       const int* mask, const double* area, const double* D, const double* hn,
+                       int ntracer, const double* const* tracers, double* work, double* out,
+                       cudaStream_t stream);
+int getm_domain_totals_f32(int nx_, int ny_, int nz, int halox, int haloy, int nx, int ny,
+                           const int* mask, const double* area, const double* D, const double* hn,
+                           int ntracer, const float* const* tracers, double* work, double* out,
+                           cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,20 @@ def _fill(a, g, value, fill_value=FILL):
     a[..., g.land] = fill_value
 
 
+def totals(T, D, hn, tracers):
+    """Simulation.totals (python/pygetm/simulation.py:1409-1444) with
+    Array.global_sum on one subdomain (python/pygetm/core.py:820-839):
+    [sum of D * area, then per tracer sum of c * area * hn], each over the
+    interior points where mask != 0 (numpy's pairwise sum, as the reference)."""
+    i = T.interior
+    unmasked = T.mask[i] != 0
+    out = [float((D * T.area)[i].sum(where=unmasked))]
+    for c in tracers:
+        tot = np.asarray(c, dtype=float) * T.area * hn
+        out.append(float(tot[i].sum(where=np.broadcast_to(unmasked, tot[i].shape))))
+    return out
+
+
 def seos_buoyancy(S, T, z):
     """Device EOS restated (simplified nonlinear EOS of Roquet et al. 2015);
     buoyancy -g/rho0 (rho - rho0) as python/pygetm/simulation.py:1184."""

@@ -8,12 +8,20 @@ pytestmark = pytest.mark.gpu
 
 
 def _members(n=3, seed=11):
-    from getm_gb300 import workloads
-
     import numpy as np
+
+    from getm_gb300 import workloads
 
     rng = np.random.default_rng(seed)
     return [workloads.ensemble_member(rng, nmin=24, nmax=40, nzmin=5, nzmax=8) for _ in range(n)]
+
+
+def _differences(a, b):
+    """Points where a and b differ (NaN equals NaN)."""
+    import torch
+
+    diff = ~((a == b) | (torch.isnan(a) & torch.isnan(b)))
+    return int(diff.sum()), diff.nonzero()[:4].tolist()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -29,16 +37,18 @@ def test_alone_equals_in_mix(precision):
     for _ in range(2):
         ens.step_period()
     torch.cuda.synchronize()
-    nsteps = {id(m): m for m in ens.members}
-    for w, m in zip(wls, ens.members):
+    bad = []
+    for n, (w, m) in enumerate(zip(wls, ens.members)):
         alone = make_member(w, precision)
-        # warm-up period + capture period + 2 replays = 4 periods of 2 3D steps
-        for _ in range(4 * Ensemble.period * alone.split_factor):
+        # warm-up period + 2 replays = 3 periods of 2 3D steps (capture
+        # records the kernels of a period without running them)
+        for _ in range(3 * Ensemble.period * alone.split_factor):
             alone.advance()
         torch.cuda.synchronize()
-        for name in ("temp", "salt"):
-            assert torch.equal(getattr(alone, name).all_values, getattr(m, name).all_values), name
-        assert torch.equal(alone.T.z.all_values, m.T.z.all_values)
-        assert torch.equal(alone.momentum.U.all_values, m.momentum.U.all_values)
-        assert torch.equal(alone.momentum.uk.all_values, m.momentum.uk.all_values)
-    del nsteps
+        fields = {"temp": (alone.temp, m.temp), "salt": (alone.salt, m.salt), "z": (alone.T.z, m.T.z),
+                  "U": (alone.momentum.U, m.momentum.U), "uk": (alone.momentum.uk, m.momentum.uk)}
+        for name, (x, y) in fields.items():
+            count, where = _differences(x.all_values, y.all_values)
+            if count:
+                bad.append(f"member {n} {name}: {count} points differ, e.g. {where}")
+    assert not bad, "\n".join(bad)

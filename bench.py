@@ -49,6 +49,11 @@ def _args():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--error-steps", type=int, default=1000,
                     help="3D steps after which the mixed form is compared with FP64 (0: skip)")
+    ap.add_argument("--ensemble", type=int, default=256, help="members of the batched ensemble (0: skip)")
+    ap.add_argument("--ensemble-steps", type=int, default=4)
+    ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson request rate, 1/s (0: skip)")
+    ap.add_argument("--serve-duration", type=float, default=15.0, help="seconds of arrivals per form")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     return ap.parse_args()
 
 
@@ -190,18 +195,19 @@ class Runner:
 
     period = 2
 
-    def __init__(self, sim, warmup, use_graph):
+    def __init__(self, sim, warmup, use_graph, hook=None):
         import torch
 
         from getm_gb300 import _lib
 
         self.sim = sim
+        self.hook = hook
         self.totals0 = sim.totals_device().clone()
         split = sim.split_factor
         nwarm = max(warmup, 3)
         nwarm += nwarm % self.period  # captured periods start on an even 3D step
-        for _ in range(nwarm * split):
-            sim.advance()
+        for _ in range(nwarm):
+            self._step3d()
         self.steps_done = nwarm  # 3D steps run on the device so far
         torch.cuda.synchronize()
         n0 = _lib.launch_count()
@@ -212,26 +218,32 @@ class Runner:
             self.graph = torch.cuda.CUDAGraph()
             with torch.cuda.stream(stream):
                 with torch.cuda.graph(self.graph, stream=stream):
-                    for _ in range(self.period * split):
-                        sim.advance()
+                    for _ in range(self.period):
+                        self._step3d()
             torch.cuda.current_stream().wait_stream(stream)
             self.launches_per_period = _lib.launch_count() - n0
             for _ in range(2):
                 self.graph.replay()
             self.steps_done += 2 * self.period  # the capture itself runs nothing
         else:
-            for _ in range(self.period * split):
-                sim.advance()
+            for _ in range(self.period):
+                self._step3d()
             self.launches_per_period = _lib.launch_count() - n0
             self.steps_done += self.period
         torch.cuda.synchronize()
+
+    def _step3d(self):
+        for _ in range(self.sim.split_factor):
+            self.sim.advance()
+        if self.hook is not None:
+            self.hook(self.sim)
 
     def run_period(self):
         if self.graph is not None:
             self.graph.replay()
         else:
-            for _ in range(self.period * self.sim.split_factor):
-                self.sim.advance()
+            for _ in range(self.period):
+                self._step3d()
         self.steps_done += self.period
 
     def run_to(self, nsteps):
@@ -302,15 +314,21 @@ def _roofline(sim, peak, peak_kind):
             "bytes_per_launch": alg, "us_per_launch": t_kernel * 1e6, "peak_kind": peak_kind}
 
 
+def _round_tracers(sim):
+    for tr in (sim.temp, sim.salt):
+        tr.all_values.copy_(tr.all_values.float().double())
+
+
 def _errors(wl, runners, args, device):
-    """Advance both forms (and an FP64 run from the unrounded initial
-    temperature, which shows how strongly the flow reacts to float32 rounding
-    of its initial state alone) to the same 3D step and compare fields and
-    compensated domain totals."""
+    """Advance both forms to the same 3D step and compare fields and
+    compensated domain totals.  A third run, FP64 arithmetic whose tracers are
+    rounded to float32 after every 3D step, shows the error that float32
+    storage of the tracers alone causes (the floor for any form that stores
+    them in float32)."""
     import torch
 
     target = max(args.error_steps, max(r.steps_done for r in runners.values()))
-    cond = Runner(_make_sim(wl, "fp64", device, round_to_float32=False), args.warmup, not args.no_graph)
+    cond = Runner(_make_sim(wl, "fp64", device), args.warmup, not args.no_graph, hook=_round_tracers)
     for r in list(runners.values()) + [cond]:
         r.run_to(target)
     torch.cuda.synchronize()
@@ -340,7 +358,98 @@ def _errors(wl, runners, args, device):
     out["totals_drift"] = {f: {n: float((x - y) / y) for n, x, y in
                                zip(names, r.sim.totals_device().tolist(), r.totals0.tolist())}
                            for f, r in (("mixed", a), ("fp64", b))}
-    out["fp64_from_unrounded_initial_state"] = compare(cond.sim, b.sim)
+    out["fp64_with_float32_tracer_storage"] = compare(cond.sim, b.sim)
+    return out
+
+
+def _pcts(deltas):
+    import numpy as np
+
+    d = np.asarray([x for x in deltas if x > 0.0])
+    if not d.size:
+        return None, None
+    return float(np.percentile(d, 50) * 1e3), float(np.percentile(d, 99) * 1e3)
+
+
+def _ensemble_leg(args, device):
+    """Batched ensemble of independent domains (mixed form): every member's
+    3D step is one graph replay on one of 16 lane streams.  Throughput of the
+    lane-concurrent replay against the same members replayed one after
+    another on one stream, and the per-member step latency."""
+    import torch
+
+    from getm_gb300 import workloads
+    from getm_gb300.ensemble import Ensemble, make_member
+
+    t_setup = time.perf_counter()
+    wls = workloads.ensemble(args.ensemble, seed=4)
+    ens = Ensemble([make_member(w, "mixed", device) for w in wls], lanes=16)
+    ens.prepare()
+    t_setup = time.perf_counter() - t_setup
+    n = len(ens.runners)
+    main = torch.cuda.current_stream()
+
+    def timed(steps, sequential):
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n)] for _ in range(steps)]
+        torch.cuda.synchronize()
+        start.record(main)
+        for s in range(steps):
+            ens.step(sequential=sequential, events=evs[s])
+        end.record(main)
+        torch.cuda.synchronize()
+        deltas = []
+        for m in range(n):
+            times = [start.elapsed_time(evs[s][m]) / 1000.0 for s in range(steps)]
+            deltas += [b - a for a, b in zip(times, times[1:])]
+        return start.elapsed_time(end) / 1000.0, deltas
+
+    ens.step()  # one untimed replay of every graph
+    steps = max(args.ensemble_steps, 2)
+    t_conc, d_conc = timed(steps, False)
+    t_seq, d_seq = timed(2, True)
+    cells = ens.cells
+    conc = cells * steps / t_conc
+    seq = cells * 2 / t_seq
+    p50, p99 = _pcts(d_conc)
+    out = {"members": n, "cells": cells, "lanes": 16, "steps": steps, "value": conc, "unit": "cell-updates/s",
+           "sequential_value": seq, "speedup_vs_sequential": conc / seq,
+           "member_step_latency_p50_ms": p50, "member_step_latency_p99_ms": p99,
+           "setup_s": t_setup, "precision": "mixed",
+           "workload": "256-type ensemble: sides log-uniform 64-256, nz 20-40, 20-40 substeps, seed 4"}
+    del ens
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
+
+
+def _serving_leg(args, device):
+    """Continuous batching of a Poisson request stream (both forms, one after
+    the other, same requests): per-step latency p50/p99 and throughput."""
+    import torch
+
+    from getm_gb300 import workloads
+    from getm_gb300.serving import GB, Server, summarize
+
+    out = {"rate_per_s": args.serve_rate, "arrival_window_s": args.serve_duration,
+           "deadline_s": 3.0 * args.serve_duration,
+           "budget_gb": args.serve_budget_gb, "lanes": 16,
+           "requests": "sides log-uniform 64-512, nz 20-40, 10-200 3D steps, seed 5"}
+    for prec in ("mixed", "fp64"):
+        reqs = workloads.serving_requests(args.serve_rate, args.serve_duration, seed=5, precision=prec)
+        srv = Server(budget_bytes=args.serve_budget_gb * GB, lanes=16, device=device)
+        t0 = time.perf_counter()
+        res = srv.run(reqs, duration=3.0 * args.serve_duration, admit_until=args.serve_duration)
+        wall = time.perf_counter() - t0
+        s = summarize(res, wall)
+        s["requests_arrived"] = len(reqs)
+        s["peak_budget_used_gb"] = srv.peak_used / GB
+        s["admission_host_ms_mean"] = 1e3 * sum(srv.admission_host_s) / max(len(srv.admission_host_s), 1)
+        out[prec] = s
+        del srv, res
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
     return out
 
 
@@ -436,6 +545,10 @@ def run_ours(args):
             line[f] = {"value": values[f], "ms_per_step": ms[f] / nsteps, "e2e": e2e[f]["value"]}
     if err is not None:
         line["error_vs_fp64"] = err
+    if rank == 0 and args.ensemble > 0:
+        line["ensemble"] = _ensemble_leg(args, device)
+    if rank == 0 and args.serve_rate > 0:
+        line["serving"] = _serving_leg(args, device)
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
         v, dt = cpu_reference(args, 2, threads)

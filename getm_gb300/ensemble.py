@@ -1,11 +1,13 @@
 """Batched ensembles of independent domains on one GPU.
 
-Each member is a full ``Simulation`` with its own CUDA stream.  One CUDA graph
-captures a period of steps of every member, each on its stream (fork from and
-join back to the capture stream), so replaying the graph issues all members'
-kernels with a single launch and the GPU runs the small kernels of different
-members concurrently.  Members are independent: a member's results are the
-same alone and in the ensemble (same kernels, same inputs, no shared state).
+Each member is a full ``Simulation`` whose state stays resident in HBM.  A
+``DomainRunner`` records the member's 3D steps into CUDA graphs after a short
+eager warm-up: two graphs, one per parity of the 3D step (the 3D momentum
+update alternates its u/v order every step and the 2D one every substep), so
+a replay advances the member by exactly one 3D step with a single launch.
+``Ensemble`` replays every member's graph on one of a few "lane" streams, so
+the small kernels of different members run concurrently on the GPU; members
+share no state, so a member's results are the same alone and in the ensemble.
 """
 
 from __future__ import annotations
@@ -19,7 +21,8 @@ from .workloads import Workload
 
 
 def make_member(wl: Workload, precision: str = "mixed", device="cuda") -> Simulation:
-    """Build and start a simulation for one ensemble member."""
+    """Build and start a simulation for one ensemble member (rest state,
+    linear temperature drop ``dT`` per 100 m from 20 degC at the surface)."""
     p = wl.params
     sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device,
                      airsea=Fluxes(taux=p.get("taux", 0.0)))
@@ -31,51 +34,98 @@ def make_member(wl: Workload, precision: str = "mixed", device="cuda") -> Simula
     return sim
 
 
+class DomainRunner:
+    """Warm-up, per-step CUDA graphs and replay of one resident domain."""
+
+    def __init__(self, sim: Simulation, warmup_steps: int = 2, use_graph: bool = True):
+        self.sim = sim
+        self.graphs: Optional[List[torch.cuda.CUDAGraph]] = None
+        self.steps_done = 0  # 3D steps completed on the device (as issued)
+        self._use_graph = use_graph
+        self._warmup = warmup_steps + warmup_steps % 2
+
+    @property
+    def cells(self) -> int:
+        T = self.sim.T
+        return T.nx * T.ny * T.nz
+
+    def _eager_step(self):
+        for _ in range(self.sim.split_factor):
+            self.sim.advance()
+
+    def prepare(self, capture_stream: Optional[torch.cuda.Stream] = None):
+        """Run the eager warm-up steps (allocating every work buffer) and
+        record the two step graphs.  Call on an idle device section: capture
+        requires that no other thread launches work meanwhile."""
+        for _ in range(self._warmup):
+            self._eager_step()
+        self.steps_done = self._warmup
+        if not self._use_graph:
+            return
+        dev = self.sim.T.device
+        stream = capture_stream or torch.cuda.Stream(device=dev)
+        stream.wait_stream(torch.cuda.current_stream(dev))
+        graphs = []
+        for _ in range(2):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(stream):
+                with torch.cuda.graph(g, stream=stream):
+                    self._eager_step()
+            graphs.append(g)
+        torch.cuda.current_stream(dev).wait_stream(stream)
+        self.graphs = graphs
+
+    def step(self):
+        """Issue one 3D step on the current stream."""
+        if self.graphs is None:
+            self._eager_step()
+        else:
+            self.graphs[(self.steps_done - self._warmup) % 2].replay()
+        self.steps_done += 1
+
+
 class Ensemble:
-    """Advance many members together through one multi-stream CUDA graph."""
+    """Advance many members together: each member's step graph is replayed on
+    one of ``lanes`` streams (round robin), one 3D step per member per call."""
 
-    period = 2  # 3D steps per graph replay (the 3D momentum order alternates)
-
-    def __init__(self, members: List[Simulation], device="cuda"):
-        self.members = members
+    def __init__(self, members: List[Simulation], lanes: int = 16, use_graph: bool = True, device="cuda"):
         self.device = torch.device(device)
-        self.streams = [torch.cuda.Stream(device=self.device) for _ in members]
-        self.graph: Optional[torch.cuda.CUDAGraph] = None
+        self.runners = [DomainRunner(m, use_graph=use_graph) for m in members]
+        self.lanes = [torch.cuda.Stream(device=self.device) for _ in range(max(1, min(lanes, len(members))))]
+
+    @property
+    def members(self) -> List[Simulation]:
+        return [r.sim for r in self.runners]
 
     @property
     def cells(self) -> int:
         """Interior cells of all members (the cell-update unit per 3D step)."""
-        return sum(m.T.nx * m.T.ny * m.T.nz for m in self.members)
+        return sum(r.cells for r in self.runners)
 
-    def _advance_period(self):
-        main = torch.cuda.current_stream(self.device)
-        for sim, s in zip(self.members, self.streams):
-            s.wait_stream(main)
-            with torch.cuda.stream(s):
-                for _ in range(self.period * sim.split_factor):
-                    sim.advance()
-        for s in self.streams:
-            main.wait_stream(s)
-
-    def warmup(self, periods: int = 1):
-        """Eager periods: allocate every work buffer before capture."""
-        for _ in range(periods):
-            self._advance_period()
-        torch.cuda.synchronize(self.device)
-
-    def capture(self):
+    def prepare(self):
         capture_stream = torch.cuda.Stream(device=self.device)
-        capture_stream.wait_stream(torch.cuda.current_stream(self.device))
-        self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.stream(capture_stream):
-            with torch.cuda.graph(self.graph, stream=capture_stream):
-                self._advance_period()
-        torch.cuda.current_stream(self.device).wait_stream(capture_stream)
+        for r in self.runners:
+            r.prepare(capture_stream)
         torch.cuda.synchronize(self.device)
 
-    def step_period(self):
-        """Advance every member by ``period`` 3D steps."""
-        if self.graph is None:
-            self._advance_period()
-        else:
-            self.graph.replay()
+    def step(self, sequential: bool = False, events: Optional[List[torch.cuda.Event]] = None):
+        """One 3D step of every member.  ``sequential``: all members on the
+        current stream, one after the other (the single-domain reference).
+        ``events``: one event per member, recorded after its step."""
+        main = torch.cuda.current_stream(self.device)
+        if sequential:
+            for n, r in enumerate(self.runners):
+                r.step()
+                if events is not None:
+                    events[n].record(main)
+            return
+        for s in self.lanes:
+            s.wait_stream(main)
+        for n, r in enumerate(self.runners):
+            s = self.lanes[n % len(self.lanes)]
+            with torch.cuda.stream(s):
+                r.step()
+                if events is not None:
+                    events[n].record(s)
+        for s in self.lanes:
+            main.wait_stream(s)

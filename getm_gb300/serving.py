@@ -1,0 +1,235 @@
+"""Serving loop: continuous batching of simulation requests on one GPU.
+
+A request is a domain plus a number of 3D steps.  Requests arrive over time;
+one is admitted as soon as its estimated device memory fits the HBM budget
+(first come, first served), built, warmed up and recorded into step graphs
+(``ensemble.DomainRunner``), and from then on advanced one 3D step at a time
+by graph replay on one of a few lane streams, interleaved with every other
+active request, so requests that arrive while others run join the mix and
+their work overlaps on the device.  A finished request leaves the mix and
+its memory returns to the budget.  Its state stays resident in HBM for its
+whole life.
+
+Every step's completion is timed on the device (a CUDA event per step,
+measured against a start event), which gives the per-step latency: the time
+between consecutive completed 3D steps of a request.
+"""
+
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Dict, List, Optional
+
+import numpy as np
+import torch
+
+from .ensemble import DomainRunner, make_member
+from .workloads import Workload
+
+GB = 1e9
+
+
+@dataclass
+class Request:
+    rid: int
+    make_workload: Callable[[], Workload]  # built at admission
+    nsteps: int
+    arrival: float                         # seconds after the start of the run
+    precision: str = "mixed"
+    cells_hint: int = 0                    # nx * ny * (nz + 1), for the memory estimate
+
+
+@dataclass
+class Result:
+    rid: int
+    cells: int
+    nsteps: int
+    arrival: float
+    admitted: float = float("nan")
+    step_done: List[float] = field(default_factory=list)  # device time of each completed step (s)
+    final_state: Optional[Dict[str, torch.Tensor]] = None
+
+    @property
+    def finished(self) -> bool:
+        return len(self.step_done) >= self.nsteps
+
+
+class _Active:
+    def __init__(self, req: Request, runner: DomainRunner, estimate: float, lane: torch.cuda.Stream):
+        self.req = req
+        self.runner = runner
+        self.estimate = estimate
+        self.lane = lane
+        self.inflight: List[torch.cuda.Event] = []
+
+
+class Server:
+    """Continuous-batching server for one GPU.
+
+    ``budget_bytes``: device memory the resident requests may use (estimated
+    per request from its cell count, calibrated on the first admissions).
+    ``lanes``: streams the active requests are spread over.
+    ``max_inflight``: steps a request may have queued on the device at once.
+    ``keep``: request ids whose final state is copied out for inspection.
+    """
+
+    STATE_FIELDS = ("temp", "salt")
+
+    def __init__(self, budget_bytes: float = 150 * GB, lanes: int = 16, max_inflight: int = 3,
+                 device="cuda", keep=()):
+        self.device = torch.device(device)
+        self.budget = float(budget_bytes)
+        self.lanes = [torch.cuda.Stream(device=self.device) for _ in range(lanes)]
+        self.max_inflight = max_inflight
+        self.keep = set(keep)
+        self.bytes_per_cell: Dict[str, float] = {}
+        self.default_bytes_per_cell = 2000.0
+        self.used = 0.0
+        self.peak_used = 0.0
+        self._capture_stream = torch.cuda.Stream(device=self.device)
+        self._lane_next = 0
+
+    def estimate(self, req: Request) -> float:
+        bpc = self.bytes_per_cell.get(req.precision, self.default_bytes_per_cell)
+        return 1.1 * bpc * max(req.cells_hint, 1)
+
+    def _admit(self, req: Request, wl: Workload, t_run: float, start: torch.cuda.Event) -> _Active:
+        before = torch.cuda.memory_allocated(self.device)
+        sim = make_member(wl, req.precision, device=self.device)
+        runner = DomainRunner(sim)
+        res = Result(req.rid, runner.cells, req.nsteps, req.arrival, admitted=t_run)
+        # warm-up steps run eagerly inside prepare(); time them as one block
+        runner.prepare(self._capture_stream)
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record()
+        ev.synchronize()
+        t_done = start.elapsed_time(ev) / 1000.0
+        res.step_done.extend([t_done] * min(runner.steps_done, req.nsteps))
+        grown = torch.cuda.memory_allocated(self.device) - before
+        cells = wl.T.nx_ * wl.T.ny_ * (wl.T.nz + 1)
+        bpc = grown / cells
+        self.bytes_per_cell[req.precision] = max(self.bytes_per_cell.get(req.precision, 0.0), bpc)
+        lane = self.lanes[self._lane_next % len(self.lanes)]
+        self._lane_next += 1
+        a = _Active(req, runner, max(self.estimate(req), 1.05 * grown), lane)
+        a.result = res
+        return a
+
+    def run(self, requests: List[Request], duration: float, admit_until: Optional[float] = None,
+            poll_sleep: float = 0.0) -> List[Result]:
+        """Serve ``requests`` until all admitted ones are done or ``duration``
+        seconds have passed (unfinished work is then abandoned; its completed
+        steps still count).  Requests are admitted until ``admit_until``
+        seconds (default: ``duration``).  At most one request is admitted
+        per pass of the loop, so the steps of the running requests keep
+        being issued while new ones are set up.  Workloads of the next
+        arrivals are generated on a host thread ahead of their admission.
+        Returns one Result per admitted request."""
+        from concurrent.futures import ThreadPoolExecutor
+
+        admit_until = duration if admit_until is None else admit_until
+        pending = sorted(requests, key=lambda r: r.arrival)
+        active: List[_Active] = []
+        results: List[Result] = []
+        prefetch = ThreadPoolExecutor(max_workers=2)
+        futures: Dict[int, object] = {}
+
+        def prefetch_ahead():
+            for r in pending[:4]:
+                if r.rid not in futures:
+                    futures[r.rid] = prefetch.submit(r.make_workload)
+
+        start = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(self.device)
+        start.record()
+        t0 = time.perf_counter()
+        self.admission_host_s = []
+        try:
+            while True:
+                now = time.perf_counter() - t0
+                if now > duration:
+                    break
+                prefetch_ahead()
+                # admission: first come, first served, while the budget allows
+                if pending and pending[0].arrival <= now and now <= admit_until:
+                    est = self.estimate(pending[0])
+                    if self.used + est <= self.budget or not active:
+                        req = pending.pop(0)
+                        fut = futures.pop(req.rid, None)
+                        wl = fut.result() if fut is not None else req.make_workload()
+                        ta = time.perf_counter()
+                        a = self._admit(req, wl, ta - t0, start)
+                        self.admission_host_s.append(time.perf_counter() - ta)
+                        self.used += a.estimate
+                        self.peak_used = max(self.peak_used, self.used)
+                        active.append(a)
+                        results.append(a.result)
+                # completion of issued steps, then issue the next ones
+                progressed = False
+                for a in active:
+                    while a.inflight and a.inflight[0].query():
+                        ev = a.inflight.pop(0)
+                        a.result.step_done.append(start.elapsed_time(ev) / 1000.0)
+                        progressed = True
+                    issued = len(a.result.step_done) + len(a.inflight)
+                    while issued < a.req.nsteps and len(a.inflight) < self.max_inflight:
+                        with torch.cuda.stream(a.lane):
+                            a.runner.step()
+                            ev = torch.cuda.Event(enable_timing=True)
+                            ev.record(a.lane)
+                        a.inflight.append(ev)
+                        issued += 1
+                        progressed = True
+                # retire finished requests
+                keep_active = []
+                for a in active:
+                    if a.result.finished and not a.inflight:
+                        if a.req.rid in self.keep:
+                            sim = a.runner.sim
+                            a.result.final_state = {n: getattr(sim, n).all_values.clone() for n in self.STATE_FIELDS}
+                            a.result.final_state["z"] = sim.T.z.all_values.clone()
+                            a.result.final_state["U"] = sim.momentum.U.all_values.clone()
+                        self.used -= a.estimate
+                        a.runner = None
+                    else:
+                        keep_active.append(a)
+                active = keep_active
+                if not active and (not pending or now > admit_until):
+                    break
+                if not progressed and poll_sleep > 0:
+                    time.sleep(poll_sleep)
+        finally:
+            prefetch.shutdown(wait=True, cancel_futures=True)
+        torch.cuda.synchronize(self.device)
+        for a in active:  # abandoned at the deadline: count what completed
+            for ev in a.inflight:
+                a.result.step_done.append(start.elapsed_time(ev) / 1000.0)
+            a.runner = None
+        return results
+
+
+def summarize(results: List[Result], wall: float) -> dict:
+    """Per-step latency percentiles and aggregate throughput of a run."""
+    deltas = []
+    cell_updates = 0
+    first, last = float("inf"), 0.0
+    for r in results:
+        t = r.step_done
+        cell_updates += r.cells * len(t)
+        deltas.extend(np.diff(np.asarray(t)).tolist())
+        if t:
+            first = min(first, r.admitted)
+            last = max(last, t[-1])
+    d = np.asarray([x for x in deltas if x > 0.0])
+    span = max(last - (first if first < float("inf") else 0.0), 1e-9)
+    return {
+        "requests_admitted": len(results),
+        "requests_finished": sum(r.finished for r in results),
+        "steps_completed": int(sum(len(r.step_done) for r in results)),
+        "step_latency_p50_ms": float(np.percentile(d, 50) * 1e3) if d.size else None,
+        "step_latency_p99_ms": float(np.percentile(d, 99) * 1e3) if d.size else None,
+        "cell_updates_per_s": cell_updates / span,
+        "wall_s": wall,
+        "admission_wait_p50_s": float(np.median([r.admitted - r.arrival for r in results])) if results else None,
+    }

@@ -252,3 +252,37 @@ def member_temperature(zc: np.ndarray, dT: float) -> np.ndarray:
 def land_fraction(wl: Workload) -> float:
     m = wl.T.mask[wl.T.interior[1:]]
     return float((m == 0).mean())
+
+
+def serving_requests(rate: float, duration: float, seed: int = 5, nmin: int = 64, nmax: int = 512,
+                     nzmin: int = 20, nzmax: int = 40, steps=(10, 200), precision: str = "mixed"):
+    """Poisson request stream: arrivals at ``rate`` per second over
+    ``duration`` seconds; each request is an ensemble-type domain with sides
+    log-uniform in [nmin, nmax] and nz in [nzmin, nzmax], asking for a
+    uniform number of 3D steps in ``steps``.  Domains are generated at
+    admission (``make_workload``); ``cells_hint`` is known up front."""
+    from .serving import Request
+
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    reqs = []
+    rid = 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        member_seed = int(rng.integers(0, 2**31 - 1))
+        sub = np.random.default_rng(member_seed)
+        # the domain's sizes are the first draws of its own generator
+        nx = int(round(np.exp(sub.uniform(np.log(nmin), np.log(nmax)))))
+        ny = int(round(np.exp(sub.uniform(np.log(nmin), np.log(nmax)))))
+        nz = int(round(np.exp(sub.uniform(np.log(nzmin), np.log(nzmax)))))
+        nsteps = int(rng.integers(steps[0], steps[1] + 1))
+
+        def make(member_seed=member_seed):
+            return ensemble_member(np.random.default_rng(member_seed), nmin=nmin, nmax=nmax, nzmin=nzmin,
+                                   nzmax=nzmax)
+
+        reqs.append(Request(rid, make, nsteps, t, precision, (nx + 4) * (ny + 4) * (nz + 1)))
+        rid += 1
+    return reqs

@@ -31,18 +31,15 @@ def test_alone_equals_in_mix(precision):
     from getm_gb300.ensemble import Ensemble, make_member
 
     wls = _members()
-    ens = Ensemble([make_member(w, precision) for w in wls])
-    ens.warmup(1)
-    ens.capture()
-    for _ in range(2):
-        ens.step_period()
+    ens = Ensemble([make_member(w, precision) for w in wls], lanes=2)
+    ens.prepare()  # 2 eager warm-up steps; capture runs nothing
+    for _ in range(3):
+        ens.step()
     torch.cuda.synchronize()
     bad = []
     for n, (w, m) in enumerate(zip(wls, ens.members)):
         alone = make_member(w, precision)
-        # warm-up period + 2 replays = 3 periods of 2 3D steps (capture
-        # records the kernels of a period without running them)
-        for _ in range(3 * Ensemble.period * alone.split_factor):
+        for _ in range(5 * alone.split_factor):  # 2 warm-up + 3 replayed steps, eagerly
             alone.advance()
         torch.cuda.synchronize()
         fields = {"temp": (alone.temp, m.temp), "salt": (alone.salt, m.salt), "z": (alone.T.z, m.T.z),
@@ -52,3 +49,24 @@ def test_alone_equals_in_mix(precision):
             if count:
                 bad.append(f"member {n} {name}: {count} points differ, e.g. {where}")
     assert not bad, "\n".join(bad)
+
+
+def test_sequential_equals_concurrent():
+    """Replaying the members one after another on one stream gives the same
+    results as the lane-concurrent replay."""
+    import torch
+
+    from getm_gb300.ensemble import Ensemble, make_member
+
+    wls = _members(n=2, seed=12)
+    a = Ensemble([make_member(w, "mixed") for w in wls], lanes=2)
+    b = Ensemble([make_member(w, "mixed") for w in wls], lanes=2)
+    a.prepare()
+    b.prepare()
+    for _ in range(2):
+        a.step()
+        b.step(sequential=True)
+    torch.cuda.synchronize()
+    for x, y in zip(a.members, b.members):
+        assert _differences(x.temp.all_values, y.temp.all_values)[0] == 0
+        assert _differences(x.T.z.all_values, y.T.z.all_values)[0] == 0

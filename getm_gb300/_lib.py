@@ -46,6 +46,7 @@ _SIGS = {
     "getm_advection_w_calculate": "ppppdpps",
     "getm_advection_apply_3d_batch": "ppppippppppdpppips",
     "getm_advection_2d": "ppppiippppdpppps",
+    "getm_advection_2d_mixed": "ppppiippppdpppps",
     "getm_advection_get_status": "ps",
     "getm_advection_2d_noalloc": "ipppiippppdpppps",
     "getm_advection_uv_pass": "iipppppdpppipps",
@@ -69,6 +70,7 @@ _SIGS = {
     "getm_surface_pressure_gradient": "iiiiiippppppppdpps",
     "getm_horizontal_diffusion": "iiiiiippppppppppdpps",
     "getm_bottom_friction": "iippppppdpis",
+    "getm_bottom_friction_mixed": "iippppppdpis",
     "getm_collect_3d_momentum_sources": "iiiiipppppppppppdpps",
     "getm_advance_2d_transport": "iiiippppppppppppppdps",
     "getm_w_momentum_3d": "iiiiiiippppppppdps",

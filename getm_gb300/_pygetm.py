@@ -85,14 +85,16 @@ def horizontal_diffusion(f, Ah_u, Ah_v, dt, out):
          _p(vg.idy), _p(vg.dx), _p(Ah_u), _p(Ah_v), _p(g.mask), _p(g.iarea), float(dt), _p(f), _p(out), _s())
 
 
-def bottom_friction(u, v, D, avmmol, out, update_z0b):
-    """pyx:392-402"""
+def bottom_friction(u, v, D, avmmol, out, update_z0b, arithmetic="float64"):
+    """pyx:392-402; ``arithmetic="float32"`` evaluates the drag coefficient
+    in float (the mixed form), storage stays float64."""
     g = u.grid
     assert not u.z
     assert v.grid is g and not v.z
     assert D.grid is g and not D.z
     assert out.grid is g and not out.z
-    call("getm_bottom_friction", g.nx_, g.ny_, _p(g.mask), _p(u), _p(v), _p(D), _p(g.z0b), _p(g.z0b_min), float(avmmol),
+    fn = "getm_bottom_friction" if arithmetic == "float64" else "getm_bottom_friction_mixed"
+    call(fn, g.nx_, g.ny_, _p(g.mask), _p(u), _p(v), _p(D), _p(g.z0b), _p(g.z0b_min), float(avmmol),
          _p(out), 1 if update_z0b else 0, _s())
 
 

@@ -205,7 +205,9 @@ struct HPassArgs {
     double dt;
     int scheme;
     int ntracer;
-    // mixed form: float copies of dt and of the metrics above
+    // mixed form: float copies of dt and of the metrics above; increment != 0
+    // selects the increment-form kernels for double fields (2D momentum)
+    int increment;
     float dtf;
     const float* idx_f;
     const float* dy_f;
@@ -378,165 +380,262 @@ __global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs<T> a)
 // change of the field, a field at rest is reproduced exactly, and the only
 // FP64 operations per cell are the thickness update hnew = hold - dh.
 // ---------------------------------------------------------------------------
-struct FaceGeomF {
-    float QU, cfl;
-    bool active, up, uu_ok;
-};
-
-__device__ __forceinline__ FaceGeomF face_geom_f32(const HPassArgs<float>& a, long long p2, long long p3,
-                                                    long long s, bool in_range)
+// Storage type S of the advected field and of the velocities: float (the 3D
+// fields of the mixed form) or double (the 2D depth-averaged momentum of the
+// mixed form, whose state stays FP64 while its increments are evaluated in
+// float).  Differences of neighbouring values are formed in S and then
+// narrowed, so they keep their accuracy when the values are close.
+template <typename S>
+__device__ __forceinline__ float inc_f(S x)
 {
-    FaceGeomF g;
-    g.QU = 0.f; g.cfl = 0.f; g.active = false; g.up = false; g.uu_ok = false;
-    if (!in_range) return g;
-    int m = a.umask[p2];
-    if (!getm_flux_point(m)) return g;
-    float uu = a.u[p3];
-    g.active = true;
-    g.QU = uu * (float)a.hu[p3] * a.dy_f[p2];
-    g.cfl = fabsf(uu * a.dtf * a.idx_f[p2]);
-    g.up = uu > 0.f;
-    g.uu_ok = getm_flux_point(g.up ? a.umask[p2 - s] : a.umask[p2 + s]);
-    return g;
+    if constexpr (std::is_same<S, double>::value) return getm_d2f_approx(x);
+    else return x;
 }
 
-// Face between cells p and p+s: el = QU (face - f[p]), er = QU (face - f[p+s]),
-// the diffusive flux (when Ah is given) added to both.
-__device__ __forceinline__ void face_dev_f32(const HPassArgs<float>& a, const FaceGeomF& g,
-                                             const float* __restrict__ f, long long p2, long long p3,
-                                             long long s, float& el, float& er)
+template <typename S>
+__device__ __forceinline__ S inc_add(S x, float dx)
 {
-    el = 0.f; er = 0.f;
-    if (!g.active) return;
-    const float f0 = f[p3], f1 = f[p3 + s];
-    const float d = f1 - f0;
-    float dev;
-    if (g.up) dev = getm_tvd_dev<float>(a.scheme, g.uu_ok ? f[p3 - s] : f0, f0, f1, g.cfl);
-    else dev = getm_tvd_dev<float>(a.scheme, g.uu_ok ? f[p3 + 2 * s] : f1, f1, f0, g.cfl);
-    el = g.QU * (g.up ? dev : d + dev);
-    er = g.QU * (g.up ? dev - d : dev);
-    if (a.Ah) {
-        float fdiff = -(float)a.Ah[p2] * (float)a.hu[p3] * d * a.idx_f[p2] * a.dy_f[p2];
-        el += fdiff;
-        er += fdiff;
-    }
+    if constexpr (std::is_same<S, double>::value) return x + getm_f2d(dx);
+    else return x + dx;
 }
 
-// x-direction pass, float fields.  Launch geometry as hpass_x_kernel.
-__global__ void __launch_bounds__(256) hpass_x_f32_kernel(HPassArgs<float> a)
+// Limited face deviation from the upwind cell, given d = f[b] - f[a] across
+// the face and the differences on either side, dprev = f[a] - f[a-1] and
+// dnext = f[b+1] - f[b].
+__device__ __forceinline__ float hx_dev(int scheme, bool up, bool uu_ok, float dprev, float d, float dnext,
+                                        float cfl)
 {
+    return up ? getm_tvd_dev_d<float>(scheme, d, uu_ok ? dprev : 0.f, cfl)
+              : getm_tvd_dev_d<float>(scheme, -d, uu_ok ? -dnext : 0.f, cfl);
+}
+
+// x-direction pass in increment form.  A warp owns one row segment: lane L
+// computes the face at U point a = i0 - 1 + L (between cells a and a+1) and,
+// for L < 31, updates cell a + 1, whose east face comes from lane L + 1 by a
+// shuffle; segments therefore advance by 31 cells.  Every lane runs the same
+// instructions (no per-lane special paths): each field is read with one
+// coalesced load per warp plus one load of the three values just outside
+// the segment (lanes 0-2), and all loads of a lane are independent.
+constexpr int HX_STRIDE = 31;
+
+template <typename S>
+__global__ void __launch_bounds__(256) hpass_x_inc_kernel(HPassArgs<S> a)
+{
+    constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x;
-    const int i = blockIdx.x * 32 + lane;
+    const int i0 = blockIdx.x * HX_STRIDE;
+    const int ia = i0 - 1 + lane;  // this lane's face (U point) and its west cell
+    const int ib = ia + 1;         // the cell this lane updates (lanes 0-30)
     const long long row = (long long)blockIdx.y * blockDim.y + threadIdx.y;
     if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
     const int k = (int)(row / a.ny_);
     const int j = (int)(row - (long long)k * a.ny_);
-    const bool inx = i < a.nx_;
-    const long long p2 = (long long)j * a.nx_ + i;
-    const long long p3 = (long long)k * a.plane + p2;
+    const long long r2 = (long long)j * a.nx_;
+    const long long r3 = (long long)k * a.plane + r2;
     const bool jrow = j >= a.jlo && j <= a.jhi;
+    const bool ain = ia >= 0 && ia < a.nx_;
+    // lanes 0-2 address the points i0-2, i0+31, i0+32 just outside the lanes' range
+    const int ix = lane == 0 ? i0 - 2 : i0 + 30 + lane;
+    const bool xin = lane < 3 && ix >= 0 && ix < a.nx_;
 
-    FaceGeomF gr = face_geom_f32(a, p2, p3, 1, inx && jrow && i >= a.ilo - 1 && i <= a.ihi);
-    FaceGeomF gl = face_geom_f32(a, p2 - 1, p3 - 1, 1, lane == 0 && jrow && i - 1 >= a.ilo - 1 && i - 1 <= a.ihi);
-    float QUl = __shfl_up_sync(0xffffffffu, gr.QU, 1);
-    if (lane == 0) QUl = gl.QU;
-    const bool upd = inx && jrow && i >= a.ilo && i <= a.ihi && a.tmask[p2] == 1;
+    // face geometry
+    const bool f_in = ain && jrow && ia >= a.ilo - 1 && ia <= a.ihi;
+    const int um = ain ? a.umask[r2 + ia] : 0;
+    const int umx = xin ? a.umask[r2 + ix] : 0;
+    int um_w = __shfl_up_sync(FULL, um, 1), um_e = __shfl_down_sync(FULL, um, 1);
+    const int umx0 = __shfl_sync(FULL, umx, 0), umx1 = __shfl_sync(FULL, umx, 1);
+    if (lane == 0) um_w = umx0;
+    if (lane == 31) um_e = umx1;
+    float QU = 0.f, cfl = 0.f, ahd = 0.f;
+    bool up = false, uu_ok = false;
+    const bool act = f_in && getm_flux_point(um);
+    if (act) {
+        const float uu = inc_f<S>(a.u[r3 + ia]);
+        const float huf = getm_d2f_approx(a.hu[r3 + ia]);
+        const float dyf = a.dy_f[r2 + ia], idxf = a.idx_f[r2 + ia];
+        QU = uu * huf * dyf;
+        cfl = fabsf(uu * a.dtf * idxf);
+        up = uu > 0.f;
+        uu_ok = getm_flux_point(up ? um_w : um_e);
+        if (a.Ah) ahd = -getm_d2f_approx(a.Ah[r2 + ia]) * huf * idxf * dyf;
+    }
+    const float QUe = __shfl_down_sync(FULL, QU, 1);  // east face of cell ib
 
+    // thickness update of cell ib
+    const bool bin = lane < HX_STRIDE && ib < a.nx_;
+    const bool upd = bin && jrow && ib >= a.ilo && ib <= a.ihi && a.tmask[r2 + ib] == 1;
     float coef = 0.f;  // dt iA / hnew
-    if (inx) {
-        const double hold = a.h_in[p3];
+    if (bin) {
+        const double hold = a.h_in[r3 + ib];
         double hnew = hold;
         if (upd) {
-            const float ia = a.iA_f[p2];
-            const float dh = a.dtf * (gr.QU - QUl) * ia;
-            hnew = hold - (double)dh;
-            coef = a.dtf * ia / (float)hnew;
+            const float iaf = a.iA_f[r2 + ib];
+            const float dh = a.dtf * (QUe - QU) * iaf;
+            hnew = hold - getm_f2d(dh);
+            coef = a.dtf * iaf / (getm_d2f_approx(hold) - dh);
         }
-        a.h_out[p3] = hnew;
+        a.h_out[r3 + ib] = hnew;
     }
     for (int t = 0; t < a.ntracer; t++) {
-        const float* __restrict__ f = a.fin[t];
+        const S* __restrict__ f = a.fin[t] + r3;
+        const S fa = ain ? f[ia] : S(0);
+        const S fx = xin ? f[ix] : S(0);
+        S fb = __shfl_down_sync(FULL, fa, 1);  // f[ia+1]
+        const S x0 = __shfl_sync(FULL, fx, 0), x1 = __shfl_sync(FULL, fx, 1), x2 = __shfl_sync(FULL, fx, 2);
+        if (lane == 31) fb = x1;
+        const float d = inc_f<S>(fb - fa);
+        float dprev = __shfl_up_sync(FULL, d, 1), dnext = __shfl_down_sync(FULL, d, 1);
+        // the two differences the shuffles cannot supply, in one operation
+        const float e = inc_f<S>(lane == 0 ? fa - x0 : x2 - x1);
+        if (lane == 0) dprev = e;
+        if (lane == 31) dnext = e;
+        // el = QU (face - f[ia]) (east side of cell ia), er = QU (face - f[ib])
         float el = 0.f, er = 0.f;
-        if (inx) face_dev_f32(a, gr, f, p2, p3, 1, el, er);
-        float erw = __shfl_up_sync(0xffffffffu, er, 1);
-        if (lane == 0) {
-            float elw;
-            face_dev_f32(a, gl, f, p2 - 1, p3 - 1, 1, elw, erw);
+        if (act) {
+            const float dev = hx_dev(a.scheme, up, uu_ok, dprev, d, dnext, cfl);
+            const float fd = ahd * d;
+            el = QU * (up ? dev : d + dev) + fd;
+            er = QU * (up ? dev - d : dev) + fd;
         }
-        if (inx) {
-            const float fo = f[p3];
-            a.fout[t][p3] = upd ? fo - coef * (el - erw) : fo;
-        }
+        const float el_e = __shfl_down_sync(FULL, el, 1);  // east face of cell ib, seen from ib
+        if (bin) a.fout[t][r3 + ib] = upd ? inc_add<S>(fb, -coef * (el_e - er)) : fb;
     }
 }
 
-// y-direction pass, float fields.  Launch geometry as hpass_y_kernel.
-__global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_f32_kernel(HPassArgs<float> a)
+// y-direction pass in increment form: the transpose of hpass_x_inc_kernel.
+// A block of 32 x HY_BY threads covers 32 columns; thread row ty computes the
+// face at V point ja = j0 - 1 + ty and, for ty < HY_BY - 1, updates cell
+// ja + 1, whose north face comes from thread row ty + 1 through shared
+// memory; blocks therefore advance by HY_BY - 1 rows.  The rows of each
+// tracer a block needs are staged in shared memory once (one coalesced load
+// per row), so every value is read from global memory once per block.
+constexpr int HY_BY = 16;
+constexpr int HY_STRIDE = HY_BY - 1;
+
+template <typename S>
+__global__ void __launch_bounds__(32 * HY_BY) hpass_y_inc_kernel(HPassArgs<S> a)
 {
-    __shared__ float sQ[GETM_V_BY][32];
-    __shared__ float sE[GETM_V_BY][32];
+    __shared__ S sf[HY_BY + 3][32];       // rows j0-2 .. j0+HY_BY
+    __shared__ float sd[HY_BY + 2][32];   // differences f[j+1] - f[j], rows j0-2 .. j0+HY_BY-1
+    __shared__ float sx[HY_BY][32];       // per-face exchange (QU, then el)
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i = blockIdx.x * 32 + tx;
-    const int j = blockIdx.y * GETM_V_BY + ty;
+    const int j0 = blockIdx.y * HY_STRIDE;
+    const int ja = j0 - 1 + ty;  // this thread's face (V point) and its south cell
+    const int jb = ja + 1;       // the cell this thread updates (ty < HY_STRIDE)
     const int k = blockIdx.z;
-    const bool in = i < a.nx_ && j < a.ny_;
     const long long s = a.nx_;
-    const long long p2 = (long long)j * a.nx_ + i;
-    const long long p3 = (long long)k * a.plane + p2;
-    const bool icol = i >= a.ilo && i <= a.ihi;
+    const long long base = (long long)k * a.plane + i;  // + j * s
+    const bool icol = i < a.nx_;
+    const bool ain = icol && ja >= 0 && ja < a.ny_;
+    const bool iint = i >= a.ilo && i <= a.ihi;
 
-    FaceGeomF gt = face_geom_f32(a, p2, p3, s, in && icol && j >= a.jlo - 1 && j <= a.jhi);
-    FaceGeomF gb = face_geom_f32(a, p2 - s, p3 - s, s, in && ty == 0 && icol && j - 1 >= a.jlo - 1 && j - 1 <= a.jhi);
-    sQ[ty][tx] = gt.QU;
+    // face geometry
+    const bool f_in = ain && iint && ja >= a.jlo - 1 && ja <= a.jhi;
+    float QU = 0.f, cfl = 0.f, ahd = 0.f;
+    bool up = false, uu_ok = false, act = false;
+    if (f_in) {
+        const long long q2 = (long long)ja * s + i;
+        act = getm_flux_point(a.umask[q2]);
+        if (act) {
+            const int m_s = ja > 0 ? a.umask[q2 - s] : 0;
+            const int m_n = ja + 1 < a.ny_ ? a.umask[q2 + s] : 0;
+            const float vv = inc_f<S>(a.u[base + ja * s]);
+            const float hvf = getm_d2f_approx(a.hu[base + ja * s]);
+            const float dxf = a.dy_f[q2], idyf = a.idx_f[q2];
+            QU = vv * hvf * dxf;
+            cfl = fabsf(vv * a.dtf * idyf);
+            up = vv > 0.f;
+            uu_ok = getm_flux_point(up ? m_s : m_n);
+            if (a.Ah) ahd = -getm_d2f_approx(a.Ah[q2]) * hvf * idyf * dxf;
+        }
+    }
+    sx[ty][tx] = QU;
     __syncthreads();
-    const float QUb = ty > 0 ? sQ[ty - 1][tx] : gb.QU;
-    const bool upd = in && icol && j >= a.jlo && j <= a.jhi && a.tmask[p2] == 1;
+    const float QUn = ty + 1 < HY_BY ? sx[ty + 1][tx] : 0.f;  // north face of cell jb
 
+    const bool bin = ty < HY_STRIDE && icol && jb < a.ny_;
+    const bool upd = bin && iint && jb >= a.jlo && jb <= a.jhi && a.tmask[(long long)jb * s + i] == 1;
     float coef = 0.f;
-    if (in) {
-        const double hold = a.h_in[p3];
+    if (bin) {
+        const double hold = a.h_in[base + jb * s];
         double hnew = hold;
         if (upd) {
-            const float ia = a.iA_f[p2];
-            const float dh = a.dtf * (gt.QU - QUb) * ia;
-            hnew = hold - (double)dh;
-            coef = a.dtf * ia / (float)hnew;
+            const float iaf = a.iA_f[(long long)jb * s + i];
+            const float dh = a.dtf * (QUn - QU) * iaf;
+            hnew = hold - getm_f2d(dh);
+            coef = a.dtf * iaf / (getm_d2f_approx(hold) - dh);
         }
-        a.h_out[p3] = hnew;
+        a.h_out[base + jb * s] = hnew;
     }
+    // staging rows: thread row ty loads row ja (smem row ty + 1); rows 0-2
+    // also load rows j0-2, j0+HY_BY-1 and j0+HY_BY (smem rows 0, HY_BY+1, HY_BY+2)
+    const int jx = ty == 0 ? j0 - 2 : j0 + HY_BY - 2 + ty;
+    const int sxrow = ty == 0 ? 0 : HY_BY + ty;
+    const bool xin = ty < 3 && icol && jx >= 0 && jx < a.ny_;
     for (int t = 0; t < a.ntracer; t++) {
-        const float* __restrict__ f = a.fin[t];
-        float el = 0.f, er = 0.f, ers = 0.f;
-        if (in) face_dev_f32(a, gt, f, p2, p3, s, el, er);
-        if (ty == 0 && in) {
-            float els;
-            face_dev_f32(a, gb, f, p2 - s, p3 - s, s, els, ers);
-        }
-        __syncthreads();  // previous tracer's reads of sE are done
-        sE[ty][tx] = er;
+        const S* __restrict__ f = a.fin[t] + base;
+        __syncthreads();  // previous tracer's reads of sf, sd and sx are done
+        sf[ty + 1][tx] = ain ? f[ja * s] : S(0);
+        if (ty < 3) sf[sxrow][tx] = xin ? f[jx * s] : S(0);
         __syncthreads();
-        if (ty > 0) ers = sE[ty - 1][tx];
-        if (in) {
-            const float fo = f[p3];
-            a.fout[t][p3] = upd ? fo - coef * (el - ers) : fo;
+        // difference across this thread's face (smem row ty + 1 of sd); rows
+        // 0 and 1 also form the differences below and above the block's faces
+        sd[ty + 1][tx] = inc_f<S>(sf[ty + 2][tx] - sf[ty + 1][tx]);
+        if (ty == 0) sd[0][tx] = inc_f<S>(sf[1][tx] - sf[0][tx]);
+        if (ty == 1) sd[HY_BY + 1][tx] = inc_f<S>(sf[HY_BY + 2][tx] - sf[HY_BY + 1][tx]);
+        __syncthreads();
+        const float dprev = sd[ty][tx], d = sd[ty + 1][tx], dnext = sd[ty + 2][tx];
+        const S fb = sf[ty + 2][tx];
+        float el = 0.f, er = 0.f;
+        if (act) {
+            const float dev = hx_dev(a.scheme, up, uu_ok, dprev, d, dnext, cfl);
+            const float fd = ahd * d;
+            el = QU * (up ? dev : d + dev) + fd;
+            er = QU * (up ? dev - d : dev) + fd;
         }
+        sx[ty][tx] = el;
+        __syncthreads();
+        const float el_n = ty + 1 < HY_BY ? sx[ty + 1][tx] : 0.f;
+        if (bin) a.fout[t][base + jb * s] = upd ? inc_add<S>(fb, -coef * (el_n - er)) : fb;
     }
+}
+
+// Launch one horizontal pass in increment form (any storage type S).
+template <typename S>
+static int launch_hpass_inc(int direction, HPassArgs<S>& a, cudaStream_t stream)
+{
+    if (direction == 1) {
+        dim3 block(32, 8);
+        // lane 0 of the first segment handles the face west of cell 0
+        dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up((long long)a.ny_ * a.nk, 8));
+        hpass_x_inc_kernel<S><<<grid, block, 0, stream>>>(a);
+    } else {
+        dim3 block(32, HY_BY);
+        dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_ + 1, HY_STRIDE), a.nk);
+        hpass_y_inc_kernel<S><<<grid, block, 0, stream>>>(a);
+    }
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 template <typename T>
 static int launch_hpass(int direction, HPassArgs<T>& a, cudaStream_t stream)
 {
+    if constexpr (getm_increment_form<T>) {
+        return launch_hpass_inc<T>(direction, a, stream);
+    } else {
+        if (a.increment) return launch_hpass_inc<T>(direction, a, stream);
+    }
     if (direction == 1) {
         const int BY = 8;
         dim3 block(32, BY);
         dim3 grid(getm_div_up(a.nx_, 32), getm_div_up((long long)a.ny_ * a.nk, BY));
-        if constexpr (getm_increment_form<T>) hpass_x_f32_kernel<<<grid, block, 0, stream>>>(a);
-        else hpass_x_kernel<T><<<grid, block, 0, stream>>>(a);
+        hpass_x_kernel<T><<<grid, block, 0, stream>>>(a);
     } else {
         dim3 block(32, GETM_V_BY);
         dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, GETM_V_BY), a.nk);
-        if constexpr (getm_increment_form<T>) hpass_y_f32_kernel<<<grid, block, 0, stream>>>(a);
-        else hpass_y_kernel<T><<<grid, block, 0, stream>>>(a);
+        hpass_y_kernel<T><<<grid, block, 0, stream>>>(a);
     }
     GETM_CHECK_LAUNCH();
     return GETM_OK;
@@ -547,7 +646,8 @@ static int launch_hpass(int direction, HPassArgs<T>& a, cudaStream_t stream)
 // mask/dx/idy).
 template <typename T>
 static int hpass_setup(HPassArgs<T>& a, int direction, const getm_advection* adv, const getm_grid* tg,
-                       const getm_grid* vg, int nk, const T* u, const double* Ah, double dt, const double* hu)
+                       const getm_grid* vg, int nk, const T* u, const double* Ah, double dt, const double* hu,
+                       int increment = 0)
 {
     if (!tg || !vg || !u || !hu) return GETM_ERR_ARG;
     if (tg->halox < 2 || tg->haloy < 2) return GETM_ERR_ARG;
@@ -564,7 +664,8 @@ static int hpass_setup(HPassArgs<T>& a, int direction, const getm_advection* adv
     a.tmask = tg->mask; a.iA = tg->iarea; a.Ah = Ah; a.u = u; a.hu = hu; a.dt = dt;
     a.scheme = adv->scheme;
     a.dtf = (float)dt;
-    if constexpr (getm_increment_form<T>) {
+    if (getm_increment_form<T> || increment) {
+        a.increment = 1;
         int rc = getm_grid_f32_metrics(const_cast<getm_grid*>(tg), 0);
         if (!rc) rc = getm_grid_f32_metrics(const_cast<getm_grid*>(vg), 0);
         if (rc) return rc;
@@ -669,7 +770,7 @@ __device__ void w_substep(const WPassArgs<T>& a, long long c, const T* wv, const
 }
 
 // Mixed form of w_substep: the increment form of the horizontal passes in
-// the vertical (see hpass_x_f32_kernel).  With flux_k = W_k f + e_k at the
+// the vertical (see hpass_x_inc_kernel).  With flux_k = W_k f + e_k at the
 // interface above level k (W_k = w_var there, 0 at the surface) and
 // dh = dtk (w_k - w_{k-1}), the reference update equals
 //     f + dtk ((w_k - W_k - w_{k-1} + W_{k-1}) f - e_k + e'_{k-1}) / hn
@@ -682,7 +783,7 @@ __device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const floa
     const float dtkf = (float)dtk, itf = (float)itersm1, dtf = (float)a.dt;
     float fkm1 = 0.f, fk = fs[c], fk1 = (nz > 1) ? fs[c + P] : 0.f;
     double hk = hs[c], hk1 = (nz > 1) ? hs[c + P] : 0.0;
-    float hkf = (float)hk, hk1f = (float)hk1;
+    float hkf = getm_d2f_approx(hk), hk1f = getm_d2f_approx(hk1);
     float erm = 0.f;   // e'_{k-1}: interface below, deviation from level k
     float Wm = 0.f;    // W_{k-1} (0 below the bottom level)
     float wkm1 = a.w[c];
@@ -703,13 +804,13 @@ __device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const floa
         }
         const float wk = a.w[c + (k + 1) * P];
         const float dh = dtkf * (wk - wkm1);
-        const double hn = hk - (double)dh;
+        const double hn = hk - getm_f2d(dh);
         hd[c + k * P] = hn;
-        fdst[c + k * P] = fk + dtkf * (((wk - W) - (wkm1 - Wm)) * fk - el + erm) / (float)hn;
+        fdst[c + k * P] = fk + dtkf * (((wk - W) - (wkm1 - Wm)) * fk - el + erm) / (hkf - dh);
         erm = er; Wm = W; wkm1 = wk;
         fkm1 = fk; fk = fk1; fk1 = fk2;
         hk = hk1; hk1 = hk2;
-        hkf = hk1f; hk1f = (float)hk2;
+        hkf = hk1f; hk1f = getm_d2f_approx(hk2);
     }
 }
 
@@ -722,9 +823,9 @@ __device__ double w_maxcfl(const WPassArgs<T>& a, long long c, const T* wv, cons
     T cmax = T(-1);
     if constexpr (getm_increment_form<T>) {
         const float dtf = (float)a.dt;
-        float hk = (float)hs[c];
+        float hk = getm_d2f_approx(hs[c]);
         for (int k = 1; k < a.nz; k++) {
-            const float hk1 = (float)hs[c + k * P];
+            const float hk1 = getm_d2f_approx(hs[c + k * P]);
             const float cfl = fabsf(wv[c + k * P]) * dtf / fminf(hk, hk1);
             if (k == 1 || cfl > cmax) cmax = cfl;
             hk = hk1;
@@ -990,18 +1091,17 @@ extern "C" int getm_advection_uv_pass_f32(int direction, int nk, getm_advection*
                                var_out, stream);
 }
 
-extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
-                                 getm_grid* vgrid, int ufirst, int split, const double* u,
-                                 const double* v, const double* Ah_u, const double* Ah_v,
-                                 double timestep, double* D, const double* DU, const double* DV,
-                                 double* var, cudaStream_t stream)
+static int advection_2d_impl(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
+                             int ufirst, int split, const double* u, const double* v, const double* Ah_u,
+                             const double* Ah_v, double timestep, double* D, const double* DU,
+                             const double* DV, double* var, int increment, cudaStream_t stream)
 {
     if (!adv) return GETM_OK;
     if (!D || !var || split < 1 || split > 3) return GETM_ERR_ARG;
     HPassArgs<double> ax, ay;
-    int rc = hpass_setup(ax, 1, adv, tgrid, ugrid, 1, u, Ah_u, timestep, DU);
+    int rc = hpass_setup(ax, 1, adv, tgrid, ugrid, 1, u, Ah_u, timestep, DU, increment);
     if (rc) return rc;
-    if ((rc = hpass_setup(ay, 2, adv, tgrid, vgrid, 1, v, Ah_v, timestep, DV))) return rc;
+    if ((rc = hpass_setup(ay, 2, adv, tgrid, vgrid, 1, v, Ah_v, timestep, DV, increment))) return rc;
     const size_t n2 = (size_t)ax.plane;
     if ((rc = adv_reserve(adv, n2, 1))) return rc;
     HPassArgs<double>* p1 = ufirst ? &ax : &ay;
@@ -1039,6 +1139,7 @@ extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_gri
         double* hdst = (s == seq_n - 1) ? D : ((s % 2 == 0) ? A : B);
         double* fdst = (fsrc == var) ? T : var;
         seq_a[s]->dt = seq_dt[s];
+        seq_a[s]->dtf = (float)seq_dt[s];
         fin[0] = fsrc; fout[0] = fdst;
         if ((rc = run_hstage(*seq_a[s], seq_dir[s], hsrc, hdst, 1, fin, fout, stream))) return rc;
         hsrc = hdst;
@@ -1048,6 +1149,26 @@ extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_gri
         if (cudaMemcpyAsync(var, fsrc, n2 * sizeof(double), cudaMemcpyDeviceToDevice, stream) != cudaSuccess) return GETM_ERR_CUDA;
     }
     return GETM_OK;
+}
+
+extern "C" int getm_advection_2d(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
+                                 getm_grid* vgrid, int ufirst, int split, const double* u,
+                                 const double* v, const double* Ah_u, const double* Ah_v,
+                                 double timestep, double* D, const double* DU, const double* DV,
+                                 double* var, cudaStream_t stream)
+{
+    return advection_2d_impl(adv, tgrid, ugrid, vgrid, ufirst, split, u, v, Ah_u, Ah_v, timestep, D, DU, DV, var,
+                             0, stream);
+}
+
+extern "C" int getm_advection_2d_mixed(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
+                                       getm_grid* vgrid, int ufirst, int split, const double* u,
+                                       const double* v, const double* Ah_u, const double* Ah_v,
+                                       double timestep, double* D, const double* DU, const double* DV,
+                                       double* var, cudaStream_t stream)
+{
+    return advection_2d_impl(adv, tgrid, ugrid, vgrid, ufirst, split, u, v, Ah_u, Ah_v, timestep, D, DU, DV, var,
+                             1, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -56,6 +56,38 @@ extern "C" unsigned long long getm_launch_counter_add(void);
 
 static inline unsigned int getm_div_up(long long a, long long b) { return (unsigned int)((a + b - 1) / b); }
 
+// ---------------------------------------------------------------------------
+// double <-> float conversions on the integer pipe.  GB300 runs FP64
+// instructions, conversions between double and float included, at a small
+// fraction of its FP32/integer rate, so the mixed form's kernels convert the
+// FP64 thickness fields by rearranging IEEE-754 bit fields instead.
+// getm_f2d: exact float -> double for normal numbers and zeros.
+// getm_d2f_approx: double -> float with the mantissa truncated to 23 bits
+// (relative error below 2^-23; used only where a float approximation of a
+// thickness is needed, e.g. as a divisor of an increment), for doubles in the
+// normal float range.  Values outside those ranges take the hardware path.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double getm_f2d(float x)
+{
+    const unsigned int b = __float_as_uint(x);
+    const unsigned int e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;  // zero, subnormal, inf, nan
+    const unsigned long long s = (unsigned long long)(b >> 31) << 63;
+    const unsigned long long m = (unsigned long long)(b & 0x7fffffu) << 29;
+    const unsigned long long de = (unsigned long long)(e + (1023u - 127u)) << 52;
+    return __longlong_as_double((long long)(s | de | m));
+}
+
+__device__ __forceinline__ float getm_d2f_approx(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
+    if (e <= 0 || e >= 0xff) return (float)x;  // outside the normal float range
+    const unsigned int s = (unsigned int)(b >> 63) << 31;
+    const unsigned int m = (unsigned int)((b >> 29) & 0x7fffffu);
+    return __uint_as_float(s | ((unsigned int)e << 23) | m);
+}
+
 // True for the mixed form's float bulk type.  Its update kernels use the
 // increment form x_new = x_old + dx, with dx formed from small differences,
 // so a field that does not change is reproduced exactly and float32 rounding
@@ -120,19 +152,24 @@ __device__ __forceinline__ T getm_tvd_face(int scheme, T fuu, T fu, T fd, T cfl)
 }
 
 // The limited part of the TVD face value, face - fu (0 where the limiter is
-// inactive): the same arithmetic as getm_tvd_face without the final sum, so
-// the increment form can work with deviations from cell values.
+// inactive), from the differences deltaf = fd - fu and deltafu = fu - fuu:
+// the same arithmetic as getm_tvd_face without the final sum, so the
+// increment form can work with deviations from cell values.
 template <typename T>
-__device__ __forceinline__ T getm_tvd_dev(int scheme, T fuu, T fu, T fd, T cfl)
+__device__ __forceinline__ T getm_tvd_dev_d(int scheme, T deltaf, T deltafu, T cfl)
 {
-    T deltaf = fd - fu;
-    T deltafu = fu - fuu;
     if (deltaf * deltafu > T(0)) {
         T ratio = deltafu / deltaf;
         T limiter = getm_limiter<T>(scheme, ratio, cfl);
         return T(0.5) * limiter * (T(1) - cfl) * deltaf;
     }
     return T(0);
+}
+
+template <typename T>
+__device__ __forceinline__ T getm_tvd_dev(int scheme, T fuu, T fu, T fd, T cfl)
+{
+    return getm_tvd_dev_d<T>(scheme, fd - fu, fu - fuu, cfl);
 }
 
 __device__ __forceinline__ bool getm_flux_point(int m) { return m == 1 || m == 2; }

@@ -48,33 +48,52 @@ extern "C" int getm_horizontal_diffusion(int imin, int imax, int jmin, int jmax,
     return GETM_OK;
 }
 
-// momentum.F90:79-101
+// momentum.F90:79-101.  C: arithmetic type of the drag coefficient (double:
+// the reference arithmetic; float: the mixed form, which evaluates the
+// logarithm and square roots of this coefficient in float and stores the
+// result in double).
+template <typename C>
 __global__ void bottom_friction_kernel(int n, const int* mask, const double* u, const double* v,
                                        const double* D, double* z0b, const double* z0b_min,
                                        double avmmol, double* ru, int iterate)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n || mask[p] != 1) return;
-    double uu = u[p], vv = v[p], DD = D[p];
-    double z0 = z0b[p];
-    double sqrtcd = GETM_KAPPA / log(1.0 + 0.5 * DD / z0);
+    C uu = (C)u[p], vv = (C)v[p], DD = (C)D[p];
+    C z0 = (C)z0b[p];
+    C sqrtcd = C(GETM_KAPPA) / log(C(1) + C(0.5) * DD / z0);
     if (iterate != 0) {
-        z0 = fmin(DD, z0b_min[p] + 0.1 * avmmol / fmax(avmmol, sqrtcd * sqrt(uu * uu + vv * vv)));
+        z0 = fmin(DD, (C)z0b_min[p] + C(0.1) * (C)avmmol / fmax((C)avmmol, sqrtcd * sqrt(uu * uu + vv * vv)));
         z0b[p] = z0;
-        sqrtcd = GETM_KAPPA / log(1.0 + 0.5 * DD / z0);
+        sqrtcd = C(GETM_KAPPA) / log(C(1) + C(0.5) * DD / z0);
     }
     ru[p] = sqrtcd * sqrtcd * sqrt(uu * uu + vv * vv);
+}
+
+template <typename C>
+static int bottom_friction_impl(int nx, int ny, const int* mask, const double* u, const double* v, const double* D,
+                                double* z0b, const double* z0b_in, double avmmol, double* ru, int iterate,
+                                cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || !mask || !u || !v || !D || !z0b || !ru || (iterate && !z0b_in)) return GETM_ERR_ARG;
+    int n = nx * ny;
+    bottom_friction_kernel<C><<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(n, mask, u, v, D, z0b, z0b_in, avmmol, ru, iterate);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 extern "C" int getm_bottom_friction(int nx, int ny, const int* mask, const double* u, const double* v,
                                     const double* D, double* z0b, const double* z0b_in, double avmmol,
                                     double* ru, int iterate, cudaStream_t stream)
 {
-    if (nx < 1 || ny < 1 || !mask || !u || !v || !D || !z0b || !ru || (iterate && !z0b_in)) return GETM_ERR_ARG;
-    int n = nx * ny;
-    bottom_friction_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(n, mask, u, v, D, z0b, z0b_in, avmmol, ru, iterate);
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
+    return bottom_friction_impl<double>(nx, ny, mask, u, v, D, z0b, z0b_in, avmmol, ru, iterate, stream);
+}
+
+extern "C" int getm_bottom_friction_mixed(int nx, int ny, const int* mask, const double* u, const double* v,
+                                          const double* D, double* z0b, const double* z0b_in, double avmmol,
+                                          double* ru, int iterate, cudaStream_t stream)
+{
+    return bottom_friction_impl<float>(nx, ny, mask, u, v, D, z0b, z0b_in, avmmol, ru, iterate, stream);
 }
 
 // momentum.F90:103-145: rows haloy..ny-haloy-1, every i, every k (mask unused).

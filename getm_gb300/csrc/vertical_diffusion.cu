@@ -49,6 +49,15 @@ struct VDArgs {
     const T* ea4[VD_MAX_BATCH];
 };
 
+// A layer thickness in the solve's type (the mixed form converts on the
+// integer pipe, see getm_d2f_approx).
+template <typename T>
+__device__ __forceinline__ T vd_h(double h)
+{
+    if constexpr (getm_increment_form<T>) return getm_d2f_approx(h);
+    else return h;
+}
+
 // Coupling coefficients of the interface above C level k (between levels k and
 // k+1): diffusion.F90:166-168 with Fortran k = C k + 1.
 template <typename T>
@@ -61,8 +70,15 @@ __device__ __forceinline__ void vd_aux(const VDArgs<T>& a, long long c, int k, d
         return;
     }
     T x = (T)(2.0 * a.dt) * (a.nuh[c + (k + 1) * P] + (T)mol);
-    auxo = (T)(1.0 - a.cnpar) * x / ((T)a.ho[c + (k + 1) * P] + (T)a.ho[c + k * P]);
-    auxn = (T)a.cnpar * x / ((T)a.hn[c + (k + 1) * P] + (T)a.hn[c + k * P]);
+    auxo = (T)(1.0 - a.cnpar) * x / (vd_h<T>(a.ho[c + (k + 1) * P]) + vd_h<T>(a.ho[c + k * P]));
+    auxn = (T)a.cnpar * x / (vd_h<T>(a.hn[c + (k + 1) * P]) + vd_h<T>(a.hn[c + k * P]));
+}
+
+// Increment form: (ho - hn) of one layer as float, exact-difference first;
+// zero without FP64 work when the solve uses one thickness (ho == hn).
+__device__ __forceinline__ float vd_dh(const double* ho, const double* hn, long long q)
+{
+    return ho == hn ? 0.f : getm_d2f_approx(ho[q] - hn[q]);
 }
 
 // Thread per column; dynamic shared memory holds ru/qu (and, in the
@@ -93,15 +109,15 @@ __global__ void vd_column_kernel(VDArgs<T> a)
     if (nz == 1) {  // diffusion.F90:224-231: every point, mask not consulted
         for (int t = 0; t < a.ntracer; t++) {
             T x = a.var[t][c];
-            T a2 = (T)a.hn[c];
+            T a2 = vd_h<T>(a.hn[c]);
             if (a.ea2[t]) a2 = a2 - a.ea2[t][c];
             if constexpr (inc) {
-                T r = x * (T)(a.ho[c] - a.hn[c]);
+                T r = x * vd_dh(a.ho, a.hn, c);
                 if (a.ea4[t]) r = r + a.ea4[t][c];
                 if (a.ea2[t]) r = r + a.ea2[t][c] * x;
                 a.var[t][c] = x + r / a2;
             } else {
-                T a4 = (T)a.ho[c] * x;
+                T a4 = vd_h<T>(a.ho[c]) * x;
                 if (a.ea4[t]) a4 = a4 + a.ea4[t][c];
                 a.var[t][c] = a4 / a2;
             }
@@ -124,11 +140,11 @@ __global__ void vd_column_kernel(VDArgs<T> a)
         T vk = var[c + k * P];
         T vkm1 = var[c + (k - 1) * P];
         T a1 = -anb;
-        T a2 = (T)a.hn[c + k * P] + anb;
+        T a2 = vd_h<T>(a.hn[c + k * P]) + anb;
         T a4;
         if constexpr (inc) {
             xo[k * nthreads + tid] = vk;
-            a4 = vk * (T)(a.ho[c + k * P] - a.hn[c + k * P]) + (vkm1 - vk) * (aob + anb);
+            a4 = vk * vd_dh(a.ho, a.hn, c + k * P) + (vkm1 - vk) * (aob + anb);
             if (ea2) a4 = a4 + ea2[c + k * P] * vk;
         } else {
             a4 = vk * (T)a.ho[c + k * P] + (vkm1 - vk) * aob;
@@ -148,10 +164,10 @@ __global__ void vd_column_kernel(VDArgs<T> a)
             vkm1 = var[c + (k - 1) * P];
             T a3 = -ana;
             a1 = -anb;
-            a2 = (T)a.hn[c + k * P] + ana + anb;
+            a2 = vd_h<T>(a.hn[c + k * P]) + ana + anb;
             if constexpr (inc) {
                 xo[k * nthreads + tid] = vk;
-                a4 = vk * (T)(a.ho[c + k * P] - a.hn[c + k * P]) + (vkp1 - vk) * (aoa + ana) +
+                a4 = vk * vd_dh(a.ho, a.hn, c + k * P) + (vkp1 - vk) * (aoa + ana) +
                      (vkm1 - vk) * (aob + anb);
                 if (ea2) a4 = a4 + ea2[c + k * P] * vk;
             } else {
@@ -170,9 +186,9 @@ __global__ void vd_column_kernel(VDArgs<T> a)
         // bottom layer, diffusion.F90:260-267 and :291-292
         {
             T a3 = -ana;
-            a2 = (T)a.hn[c] + ana;
+            a2 = vd_h<T>(a.hn[c]) + ana;
             if constexpr (inc) {
-                a4 = vk * (T)(a.ho[c] - a.hn[c]) + (vkp1 - vk) * (aoa + ana);
+                a4 = vk * vd_dh(a.ho, a.hn, c) + (vkp1 - vk) * (aoa + ana);
                 if (ea2) a4 = a4 + ea2[c] * vk;
             } else {
                 a4 = vk * (T)a.ho[c] + (vkp1 - vk) * aoa;

@@ -121,8 +121,9 @@ class Momentum:
             self.corqk.all_values[:, -1, :] = 0.0
         if self.advection_scheme is None:
             self.advection_scheme = default_advection_scheme
-        self.uadv = Advection(ug, scheme=self.advection_scheme, split_2d=self.advection_split_2d)
-        self.vadv = Advection(vg, scheme=self.advection_scheme, split_2d=self.advection_split_2d)
+        inc2d = "float32" if self.dtype3d == torch.float32 else "float64"
+        self.uadv = Advection(ug, scheme=self.advection_scheme, split_2d=self.advection_split_2d, increments_2d=inc2d)
+        self.vadv = Advection(vg, scheme=self.advection_scheme, split_2d=self.advection_split_2d, increments_2d=inc2d)
         if three_d:
             self.hU_bot = ug.hn.isel(z=0)
             self.hV_bot = vg.hn.isel(z=0)
@@ -222,8 +223,9 @@ class Momentum:
         """momentum.py:1099-1125"""
         u_V = u.interp(v.grid._work)
         v_U = v.interp(u.grid._work)
-        _pygetm.bottom_friction(u, v_U, DU, self.avmmol, ru, update_z0b)
-        _pygetm.bottom_friction(u_V, v, DV, self.avmmol, rv, update_z0b)
+        ar = "float32" if self.dtype3d == torch.float32 else "float64"
+        _pygetm.bottom_friction(u, v_U, DU, self.avmmol, ru, update_z0b, ar)
+        _pygetm.bottom_friction(u_V, v, DV, self.avmmol, rv, update_z0b, ar)
 
     def coriolis(self, U: Array, out: Array, x_direction: bool):
         """momentum.py:1127-1148 (DEFAULT scheme)"""

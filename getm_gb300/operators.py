@@ -62,7 +62,13 @@ class Advection:
     """pygetm.operators.Advection (operators.py:27-193, pyx:198-261)."""
 
     def __init__(self, grid: Grid, scheme: AdvectionScheme = AdvectionScheme.DEFAULT,
-                 split_2d: AdvectionSplit = AdvectionSplit.HALF):
+                 split_2d: AdvectionSplit = AdvectionSplit.HALF, increments_2d: str = "float64"):
+        """``increments_2d``: arithmetic of ``__call__`` (2D advection of a
+        float64 field): "float64", the reference arithmetic, or "float32",
+        the mixed form's increment form (float64 storage and updates)."""
+        if increments_2d not in ("float64", "float32"):
+            raise ValueError(f"increments_2d must be 'float64' or 'float32', not {increments_2d!r}")
+        self._call_2d = "getm_advection_2d" if increments_2d == "float64" else "getm_advection_2d_mixed"
         self.grid = grid
         self.ugrid = grid.ugrid
         self.vgrid = grid.vgrid
@@ -128,7 +134,7 @@ class Advection:
         assert Ah_u is None or (Ah_u.grid is self.ugrid and not Ah_u.z)
         assert Ah_v is None or (Ah_v.grid is self.vgrid and not Ah_v.z)
         self.D.copy_(self.grid.D.all_values)
-        call("getm_advection_2d", self.p, self.grid.handle, self.ugrid.handle, self.vgrid.handle, int(self._ufirst),
+        call(self._call_2d, self.p, self.grid.handle, self.ugrid.handle, self.vgrid.handle, int(self._ufirst),
              self.split_2d.value, _p(u), _p(v), _p(Ah_u), _p(Ah_v), float(timestep), self.D.data_ptr(),
              _p(self.ugrid.D), _p(self.vgrid.D), _p(var), _s())
 

@@ -342,6 +342,24 @@ int getm_shchepetkin_mcwilliams_f32(int nx, int ny, int nz, int imin, int imax, 
 int getm_density_buoyancy_f32(int n, const float* salt, const float* temp, const double* p,
                               double* rho, double* buoy, cudaStream_t stream);
 
+/* bottom friction (momentum.F90:79-101, getm_bottom_friction) with the drag
+ * coefficient's logarithm and square roots evaluated in float; inputs and
+ * outputs stay double.                                                     */
+int getm_bottom_friction_mixed(int nx, int ny, const int* mask, const double* u, const double* v,
+                               const double* D, double* z0b, const double* z0b_in, double avmmol,
+                               double* ru, int iterate, cudaStream_t stream);
+
+/* 2D advection of a double field (the depth-averaged momentum of the mixed
+ * form) with the same interface as getm_advection_2d (operators.py:52-93)
+ * and the same storage, whose increments are evaluated in float in
+ * increment form: face deviations are formed from double differences of
+ * neighbouring values, the field and the column heights are updated in
+ * double.                                                                  */
+int getm_advection_2d_mixed(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
+                            int ufirst, int split, const double* u, const double* v, const double* Ah_u,
+                            const double* Ah_v, double timestep, double* D, const double* DU,
+                            const double* DV, double* var, cudaStream_t stream);
+
 /* ---- domain totals (compensated budget sums) -----------------------------
  * Replaces python/pygetm/simulation.py:1409-1444 (Simulation.totals: total
  * volume = sum of D*area, tracer total = sum of c*area*hn over unmasked

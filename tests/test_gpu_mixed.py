@@ -128,3 +128,31 @@ def test_mixed_simulation_error_vs_fp64():
     # error is dominated by float32 rounding of the density field (compare
     # e_cond); the absolute elevation error stays below 0.1 mm.
     assert e_mixed["z_abs"] < 1e-4
+
+
+@pytest.mark.parametrize("split", [1, 2, 3])
+def test_advection_2d_mixed(split):
+    """2D advection of a float64 field with float32 increments: the change of
+    the field matches the FP64 oracle to float32 accuracy (1e-5 of the largest
+    change), the column heights to 1e-6."""
+    import oracle.oracle as O
+    from getm_gb300 import operators
+    from tests.test_gpu_operators import wrap
+
+    Th, To, Td, rng = setup(seed=70 + split)
+    u = velocity(Th.ugrid, rng, 1, 0.5)[0]
+    v = velocity(Th.vgrid, rng, 1, 0.5)[0]
+    # a large mean plus a small signal: the increments are what float32 must resolve
+    t = 100.0 + rng.uniform(0.0, 1.0, (Th.ny_, Th.nx_))
+    ao = O.Advection(To, 5, O.AdvectionSplit(split))
+    to = t.copy()
+    ao(u, v, 600.0, to)
+    ad = operators.Advection(Td, operators.AdvectionScheme.SUPERBEE, operators.AdvectionSplit(split),
+                             increments_2d="float32")
+    td = wrap(Td, t, False)
+    ad(wrap(Td.ugrid, u, False), wrap(Td.vgrid, v, False), 600.0, td)
+    wet = Th.mask == 1
+    change_gpu = host(td.all_values) - t
+    change_ref = to - t
+    assert rel(change_gpu, change_ref, wet) < 1e-5
+    assert rel(host(ad.D), ao.D, wet) < 1e-6

@@ -71,6 +71,13 @@ _SIGS = {
     "getm_horizontal_diffusion": "iiiiiippppppppppdpps",
     "getm_bottom_friction": "iippppppdpis",
     "getm_bottom_friction_mixed": "iippppppdpis",
+    "getm_update_depth_2d": "iidd" + "p" * 25 + "s",
+    "getm_momentum_2d_velocities": "iii" + "p" * 16 + "s",
+    "getm_momentum_2d_friction": "iii" + "p" * 12 + "s",
+    "getm_coriolis_2d": "iiiipppis",
+    "getm_advance_2d_transport_mixed": "iiiippppppppppppppdps",
+    "getm_accumulate_2d": "lpppps",
+    "getm_surface_elevation_fused": "iiiipppppppppds",
     "getm_collect_3d_momentum_sources": "iiiiipppppppppppdpps",
     "getm_advance_2d_transport": "iiiippppppppppppppdps",
     "getm_w_momentum_3d": "iiiiiiippppppppdps",
@@ -98,7 +105,7 @@ _SIGS = {
     "getm_domain_totals": "iiiiiiippppippps",
     "getm_domain_totals_f32": "iiiiiiippppippps",
 }
-_CT = {"i": c_int, "d": c_double, "p": c_void_p, "s": c_void_p, "c": ctypes.c_char_p}
+_CT = {"i": c_int, "l": ctypes.c_longlong, "d": c_double, "p": c_void_p, "s": c_void_p, "c": ctypes.c_char_p}
 
 for _name, _sig in _SIGS.items():
     _f = getattr(lib, _name)
@@ -114,8 +121,40 @@ class GetmError(RuntimeError):
         self.code = code
 
 
+# Handles whose owner was garbage-collected.  Their finalizers free device
+# memory, which must not happen while a CUDA graph is being captured (on any
+# thread, in the default capture mode), and a destructor can run at any
+# allocation, on any thread.  So they are queued and released by the next
+# library call made on a stream that is not capturing.
+_pending_release = []
+
+
+def _capturing() -> bool:
+    try:
+        import torch
+
+        return torch.cuda.is_available() and torch.cuda.is_current_stream_capturing()
+    except Exception:
+        return False
+
+
+def release(finalizer: str, handle) -> None:
+    """Queue a library handle for finalization (see _pending_release)."""
+    _pending_release.append((finalizer, handle))
+
+
+def _flush_releases() -> None:
+    if _capturing():
+        return
+    while _pending_release:
+        finalizer, handle = _pending_release.pop()
+        getattr(lib, finalizer)(handle)
+
+
 def call(name: str, *args) -> int:
     """Call an entry point; raise GetmError on a non-zero status."""
+    if _pending_release:
+        _flush_releases()
     rc = getattr(lib, name)(*args)
     if rc != GETM_OK:
         raise GetmError(name, rc)

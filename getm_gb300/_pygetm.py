@@ -117,13 +117,13 @@ def collect_3d_momentum_sources(dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4)
          _p(g.hn), _p(dp), _p(cor), _p(adv), _p(diff), _p(idp), _p(taus), _p(rr), float(dt), _p(ea2), _p(ea4), _s())
 
 
-def advance_2d_transport(U, dp, taus, cor, adv, diff, damp, SA, SB, SD, SF, r, dt):
-    """pyx:423-441"""
+def advance_2d_transport(U, dp, taus, cor, adv, diff, damp, SA, SB, SD, SF, r, dt, mixed=False):
+    """pyx:423-441; ``mixed``: tendency in float, transport update in double."""
     g = U.grid
     for a, n in ((dp, "dp"), (taus, "taus"), (cor, "cor"), (adv, "adv"), (diff, "diff"), (damp, "damp"), (SA, "SA"),
                  (SB, "SB"), (SD, "SD"), (SF, "SF"), (r, "rr")):
         assert a.grid is g and not a.z, n
-    call("getm_advance_2d_transport", g.nx_, g.ny_, g.halox, g.haloy, _p(g.mask), _p(g.alpha), _p(g.D), _p(dp), _p(taus),
+    call("getm_advance_2d_transport_mixed" if mixed else "getm_advance_2d_transport", g.nx_, g.ny_, g.halox, g.haloy, _p(g.mask), _p(g.alpha), _p(g.D), _p(dp), _p(taus),
          _p(cor), _p(adv), _p(diff), _p(damp), _p(SA), _p(SB), _p(SD), _p(SF), _p(r), float(dt), _p(U), _s())
 
 
@@ -242,3 +242,59 @@ def multiply_add(tgt: torch.Tensor, add: torch.Tensor, scale_factor: float):
 
 def new_handle():
     return ctypes.c_void_p()
+
+
+# ---------------------------------------------------------------------------
+# fused sequences of the 2D substep (no single counterpart in the reference;
+# each replaces the operations named in its docstring with one launch)
+# ---------------------------------------------------------------------------
+def update_depth_2d(T, z, zo, Dmin, Dcrit):
+    """Simulation.update_depth, 2D part (simulation.py:1498-1586):
+    elevation2depth on T, Dclip, z_T_half and its interpolation to U, V, X,
+    depths and alpha there, D_T_half and the UU/VV/UV/VU depth copies."""
+    U, V, X = T.ugrid, T.vgrid, T.xgrid
+    call("getm_update_depth_2d", T.nx_, T.ny_, float(Dmin), float(Dcrit), _p(z), _p(zo), _p(T.H), _p(U.H), _p(V.H),
+         _p(X.H), _p(T.mask), _p(U.mask), _p(V.mask), _p(X.mask), _p(T.D), _p(T.Dclip), _p(T._work), _p(U._work),
+         _p(U.D), _p(U.alpha), _p(V._work), _p(V.D), _p(V.alpha), _p(X._work), _p(X.D), _p(U.ugrid.D),
+         _p(V.vgrid.D), _p(U.vgrid.D), _p(V.ugrid.D), _s())
+
+
+def momentum_2d_velocities(U, V, u1, v1, advU, advV, uua, uva, vua, vva, mixed=False):
+    """momentum.py:1017-1040 (Am = 0 part): u1 = U/D, v1 = V/D, the advected
+    copies and the advection velocities on the UU, UV, VU, VV grids."""
+    g = U.grid
+    call("getm_momentum_2d_velocities", g.nx_, g.ny_, int(bool(mixed)), _p(U), _p(V), _p(U.grid.D), _p(V.grid.D),
+         _p(uua.grid.D), _p(uva.grid.D), _p(vua.grid.D), _p(vva.grid.D), _p(u1), _p(v1), _p(advU), _p(advV),
+         _p(uua), _p(uva), _p(vua), _p(vva), _s())
+
+
+def momentum_2d_friction(u1, v1, ru, rv, mixed=False):
+    """Momentum.bottom_friction on the U and V grids (momentum.py:1099-1125,
+    momentum.F90:79-101 without z0b iteration)."""
+    ug, vg = u1.grid, v1.grid
+    call("getm_momentum_2d_friction", ug.nx_, ug.ny_, int(bool(mixed)), _p(ug.mask), _p(vg.mask), _p(u1), _p(v1),
+         _p(ug.D), _p(vg.D), _p(ug.z0b), _p(vg.z0b), _p(ug._work), _p(vg._work), _p(ru), _p(rv), _s())
+
+
+def coriolis_2d(U, out, x_direction):
+    """Momentum.coriolis, DEFAULT scheme, for 2D transports (momentum.py:1127-1148)."""
+    a, b = U.grid, out.grid
+    if a.ioffset == b.ioffset + 1 and a.joffset == b.joffset - 1:
+        io, jo = 1, 0
+    elif a.ioffset == b.ioffset - 1 and a.joffset == b.joffset + 1:
+        io, jo = 0, 1
+    else:
+        raise NotImplementedError("coriolis_2d expects U -> V or V -> U")
+    call("getm_coriolis_2d", b.nx_, b.ny_, io, jo, _p(U), _p(b.cor), _p(out), int(bool(x_direction)), _s())
+
+
+def accumulate_2d(U, V, Ucum, Vcum):
+    """_U_cum += U; _V_cum += V (momentum.py:716-718)."""
+    call("getm_accumulate_2d", U.all_values.numel(), _p(U), _p(V), Ucum.data_ptr(), Vcum.data_ptr(), _s())
+
+
+def surface_elevation_fused(timestep, z, zo, U, V, fwf):
+    """zo = z, then advance_surface_elevation (simulation.py:1468-1486)."""
+    g = z.grid
+    call("getm_surface_elevation_fused", g.nx_, g.ny_, g.halox, g.haloy, _p(g.mask), _p(U.grid.dy), _p(V.grid.dx),
+         _p(g.iarea), _p(z), _p(zo), _p(U), _p(V), _p(fwf), float(timestep), _s())

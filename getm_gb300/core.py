@@ -198,7 +198,7 @@ class Grid:
         h = getattr(self, "handle", None)
         if h is not None and h.value:
             try:
-                _lib.lib.getm_grid_finalize(h)
+                _lib.release("getm_grid_finalize", h)
             except Exception:
                 pass
 

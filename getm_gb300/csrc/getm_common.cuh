@@ -173,3 +173,8 @@ __device__ __forceinline__ T getm_tvd_dev(int scheme, T fuu, T fu, T fd, T cfl)
 }
 
 __device__ __forceinline__ bool getm_flux_point(int m) { return m == 1 || m == 2; }
+
+// u*u + v*v rounded after each operation (no contraction into an FMA), so
+// every kernel that forms a speed from two components gets the same bits.
+__device__ __forceinline__ double getm_speed2(double u, double v) { return __dadd_rn(__dmul_rn(u, u), __dmul_rn(v, v)); }
+__device__ __forceinline__ float getm_speed2(float u, float v) { return __fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)); }

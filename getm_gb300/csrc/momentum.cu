@@ -63,11 +63,11 @@ __global__ void bottom_friction_kernel(int n, const int* mask, const double* u, 
     C z0 = (C)z0b[p];
     C sqrtcd = C(GETM_KAPPA) / log(C(1) + C(0.5) * DD / z0);
     if (iterate != 0) {
-        z0 = fmin(DD, (C)z0b_min[p] + C(0.1) * (C)avmmol / fmax((C)avmmol, sqrtcd * sqrt(uu * uu + vv * vv)));
+        z0 = fmin(DD, (C)z0b_min[p] + C(0.1) * (C)avmmol / fmax((C)avmmol, sqrtcd * sqrt(getm_speed2(uu, vv))));
         z0b[p] = z0;
         sqrtcd = C(GETM_KAPPA) / log(C(1) + C(0.5) * DD / z0);
     }
-    ru[p] = sqrtcd * sqrtcd * sqrt(uu * uu + vv * vv);
+    ru[p] = sqrtcd * sqrtcd * sqrt(getm_speed2(uu, vv));
 }
 
 template <typename C>

@@ -48,6 +48,9 @@ class Momentum:
         self.coriolis_scheme = coriolis_scheme
         self.avmmol = avmmol
         self.dtype3d = dtype
+        # fused 2D substep kernels (one launch per sequence of operations);
+        # False runs each operation as its own kernel
+        self.fused_2d = True
 
     # ------------------------------------------------------------------ setup
     def _create_arrays(self, tgrid: Grid, three_d: bool):
@@ -161,14 +164,16 @@ class Momentum:
     def advance_depth_integrated(self, timestep: float, tausx: Array, tausy: Array, dpdx: Array, dpdy: Array):
         """momentum.py:644-718"""
 
+        mixed = self.fused_2d and self.dtype3d == torch.float32
+
         def u():
             _pygetm.advance_2d_transport(self.U, dpdx, tausx, self.corU, self.advU, self.diffU, self.dampU,
-                                         self.SxA, self.SxB, self.SxD, self.SxF, self.ru, timestep)
+                                         self.SxA, self.SxB, self.SxD, self.SxF, self.ru, timestep, mixed)
             self.coriolis(self.U, self.corV, True)
 
         def v():
             _pygetm.advance_2d_transport(self.V, dpdy, tausy, self.corV, self.advV, self.diffV, self.dampV,
-                                         self.SyA, self.SyB, self.SyD, self.SyF, self.rv, timestep)
+                                         self.SyA, self.SyB, self.SyD, self.SyF, self.rv, timestep, mixed)
             self.coriolis(self.V, self.corU, False)
 
         if self._ufirst:
@@ -179,8 +184,11 @@ class Momentum:
             u()
         self._ufirst = not self._ufirst
         if self.runtype > 1:
-            self._U_cum += self.U.all_values
-            self._V_cum += self.V.all_values
+            if self.fused_2d:
+                _pygetm.accumulate_2d(self.U, self.V, self._U_cum, self._V_cum)
+            else:
+                self._U_cum += self.U.all_values
+                self._V_cum += self.V.all_values
 
     def update_depth_integrated_diagnostics(self, timestep: float, skip_coriolis: bool = False,
                                             update_z0b: bool = False):
@@ -196,6 +204,9 @@ class Momentum:
     def _transport_2d_momentum(self, U: Array, V: Array, timestep: float, advU: Array, advV: Array,
                                diffU: Array, diffV: Array, update_z0b: bool):
         """momentum.py:1017-1097"""
+        if self.fused_2d and not update_z0b:
+            self._transport_2d_momentum_fused(U, V, timestep, advU, advV, diffU, diffV)
+            return
         torch.div(U.all_values, U.grid.D.all_values, out=self.u1.all_values)
         torch.div(V.all_values, V.grid.D.all_values, out=self.v1.all_values)
         if self.diffuse_momentum:
@@ -218,6 +229,22 @@ class Momentum:
         self.vadv(self.vua, self.vva, timestep, advV, skip_initial_halo_exchange=True)
         _pygetm.reconstruct_transport_change(advV, self.vadv.D, V, timestep)
 
+    def _transport_2d_momentum_fused(self, U, V, timestep, advU, advV, diffU, diffV):
+        """The same sequence with two fused kernels for everything before the
+        advection calls (velocities and copies; drag coefficients)."""
+        mixed = self.dtype3d == torch.float32
+        _pygetm.momentum_2d_velocities(U, V, self.u1, self.v1, advU, advV, self.uua, self.uva, self.vua, self.vva,
+                                       mixed)
+        if self.diffuse_momentum:
+            _pygetm.momentum_diffusion(self.uua.grid.D, self.uva.grid.D, self.vua.grid.D, self.vva.grid.D,
+                                       self.u1, self.v1, self._Am_const, diffU, diffV)
+        if self.apply_bottom_friction:
+            _pygetm.momentum_2d_friction(self.u1, self.v1, self.ru, self.rv, mixed)
+        self.uadv(self.uua, self.uva, timestep, advU, skip_initial_halo_exchange=True)
+        _pygetm.reconstruct_transport_change(advU, self.uadv.D, U, timestep)
+        self.vadv(self.vua, self.vva, timestep, advV, skip_initial_halo_exchange=True)
+        _pygetm.reconstruct_transport_change(advV, self.vadv.D, V, timestep)
+
     def bottom_friction(self, u: Array, v: Array, DU: Array, DV: Array, ru: Array, rv: Array,
                         update_z0b: bool = False):
         """momentum.py:1099-1125"""
@@ -232,6 +259,9 @@ class Momentum:
         assert U.grid is not out.grid
         if self.coriolis_scheme == CoriolisScheme.ESPELID:
             raise NotImplementedError("Espelid Coriolis interpolation is not implemented")
+        if self.fused_2d and not U.z:
+            _pygetm.coriolis_2d(U, out, x_direction)
+            return
         U.interp(out)
         out.all_values.mul_(out.grid.cor.all_values)
         if x_direction:

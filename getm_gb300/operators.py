@@ -87,7 +87,7 @@ class Advection:
         p = getattr(self, "p", None)
         if p is not None and p.value:
             try:
-                _lib.lib.getm_advection_finalize(p)
+                _lib.release("getm_advection_finalize", p)
             except Exception:
                 pass
 
@@ -199,7 +199,7 @@ class VerticalAdvection:
         p = getattr(self, "p", None)
         if p is not None and p.value:
             try:
-                _lib.lib.getm_advection_finalize(p)
+                _lib.release("getm_advection_finalize", p)
             except Exception:
                 pass
 
@@ -228,7 +228,7 @@ class VerticalDiffusion:
         p = getattr(self, "p", None)
         if p is not None and p.value:
             try:
-                _lib.lib.getm_vertical_diffusion_finalize(p)
+                _lib.release("getm_vertical_diffusion_finalize", p)
             except Exception:
                 pass
 

@@ -94,8 +94,21 @@ class Server:
         bpc = self.bytes_per_cell.get(req.precision, self.default_bytes_per_cell)
         return 1.1 * bpc * max(req.cells_hint, 1)
 
+    @staticmethod
+    def resident_bytes(sim) -> int:
+        """Device bytes of a simulation's fields (every state tensor once)."""
+        from .checkpoint import state_tensors
+
+        seen, total = set(), 0
+        for t in state_tensors(sim).values():
+            s = t.untyped_storage()
+            if t.device.type != "cuda" or s.data_ptr() in seen:
+                continue
+            seen.add(s.data_ptr())
+            total += s.nbytes()
+        return total
+
     def _admit(self, req: Request, wl: Workload, t_run: float, start: torch.cuda.Event) -> _Active:
-        before = torch.cuda.memory_allocated(self.device)
         sim = make_member(wl, req.precision, device=self.device)
         runner = DomainRunner(sim)
         res = Result(req.rid, runner.cells, req.nsteps, req.arrival, admitted=t_run)
@@ -106,7 +119,8 @@ class Server:
         ev.synchronize()
         t_done = start.elapsed_time(ev) / 1000.0
         res.step_done.extend([t_done] * min(runner.steps_done, req.nsteps))
-        grown = torch.cuda.memory_allocated(self.device) - before
+        # fields plus operator work buffers and graph pools (about a third more)
+        grown = 1.35 * self.resident_bytes(sim)
         cells = wl.T.nx_ * wl.T.ny_ * (wl.T.nz + 1)
         bpc = grown / cells
         self.bytes_per_cell[req.precision] = max(self.bytes_per_cell.get(req.precision, 0.0), bpc)

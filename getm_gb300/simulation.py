@@ -99,7 +99,7 @@ class Simulation:
                  advection_scheme: AdvectionScheme = AdvectionScheme.DEFAULT, momentum: Optional[Momentum] = None,
                  airsea: Optional[Fluxes] = None, internal_pressure: str = "shchepetkin_mcwilliams",
                  Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
-                 nuh: float = 0.0, precision: str = "fp64", device="cuda"):
+                 nuh: float = 0.0, precision: str = "fp64", fused_2d: bool = True, device="cuda"):
         """``precision``: "fp64" (the plain form) or "mixed" (float32 tracers,
         3D velocities and their tendencies and diffusivities; float64
         elevations, depths, layer thicknesses, 2D transports and their
@@ -108,6 +108,7 @@ class Simulation:
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
+        self.fused_2d = fused_2d
         d3 = torch.float32 if precision == "mixed" else torch.float64
         self.dtype3d = d3
         if Dmin <= 0.0:
@@ -135,6 +136,7 @@ class Simulation:
             self.h_T_half = T.array(fill=float("nan"), z=CENTERS)
             self.depth = T.array(z=CENTERS, name="pres")
         self.momentum = momentum or Momentum(dtype=d3)
+        self.momentum.fused_2d = fused_2d
         self.momentum.initialize(T, int(self.runtype), advection_scheme)
         self.airsea = airsea or Fluxes()
         self.airsea.initialize(T)
@@ -321,6 +323,9 @@ class Simulation:
 
     def advance_surface_elevation(self, timestep: float, U: Array, V: Array, fwf: Array):
         """simulation.py:1468-1486"""
+        if self.fused_2d:
+            _pygetm.surface_elevation_fused(timestep, self.T.z, self.T.zo, U, V, fwf)
+            return
         self.T.zo.all_values.copy_(self.T.z.all_values)
         _pygetm.advance_surface_elevation(timestep, self.T.z, U, V, fwf)
 
@@ -344,6 +349,16 @@ class Simulation:
             z_T, zo_T = T.zin, T.zio
         else:
             z_T, zo_T = T.z, T.zo
+        if self.fused_2d:
+            _pygetm.update_depth_2d(T, z_T, zo_T, self.Dmin, self.Dcrit)
+        else:
+            self._update_depth_2d_ops(z_T, zo_T)
+        if _3d:
+            self._update_depth_3d()
+
+    def _update_depth_2d_ops(self, z_T, zo_T):
+        """The 2D part of update_depth as separate operations."""
+        T, U, V, X = self.T, self.U, self.V, self.X
         z_U, z_V, z_X, z_T_half = U._work, V._work, X._work, T._work
         _pygetm.elevation2depth(z_T, T.H, -1000.0, T.D)
         torch.clamp(T.D.all_values, min=self.Dmin, out=T.Dclip.all_values)
@@ -363,19 +378,22 @@ class Simulation:
         V.vgrid.D.all_values[:-1, :] = D_T_half.all_values[1:, :]
         U.vgrid.D.all_values[:, :] = X.D.all_values[1:, 1:]
         V.ugrid.D.all_values[:, :] = U.vgrid.D.all_values
-        if _3d:
-            T.ho.all_values.copy_(T.hn.all_values)
-            U.ho.all_values.copy_(U.hn.all_values)
-            V.ho.all_values.copy_(V.hn.all_values)
-            for g in (T, U, V, X):
-                self._sigma(g)
-            for g in (T, U, V):
-                _pygetm.thickness2vertical_coordinates(g.mask, g.H, g.hn, g.zc, g.zf)
-            torch.add(T.ho.all_values, T.hn.all_values, out=self.h_T_half.all_values)
-            self.h_T_half.all_values.mul_(0.5)
-            U.ugrid.hn.all_values[:, :, :-1] = self.h_T_half.all_values[:, :, 1:]
-            V.vgrid.hn.all_values[:, :-1, :] = self.h_T_half.all_values[:, 1:, :]
-            U.vgrid.hn.all_values[:, :, :] = X.hn.all_values[:, 1:, 1:]
-            V.ugrid.hn.all_values[:, :, :] = U.vgrid.hn.all_values
-            if self.runtype == RunType.BAROCLINIC:
-                _pygetm.thickness2center_depth(T.mask, T.hn, self.depth)
+
+    def _update_depth_3d(self):
+        """The 3D part of update_depth (simulation.py:1588-1630)."""
+        T, U, V, X = self.T, self.U, self.V, self.X
+        T.ho.all_values.copy_(T.hn.all_values)
+        U.ho.all_values.copy_(U.hn.all_values)
+        V.ho.all_values.copy_(V.hn.all_values)
+        for g in (T, U, V, X):
+            self._sigma(g)
+        for g in (T, U, V):
+            _pygetm.thickness2vertical_coordinates(g.mask, g.H, g.hn, g.zc, g.zf)
+        torch.add(T.ho.all_values, T.hn.all_values, out=self.h_T_half.all_values)
+        self.h_T_half.all_values.mul_(0.5)
+        U.ugrid.hn.all_values[:, :, :-1] = self.h_T_half.all_values[:, :, 1:]
+        V.vgrid.hn.all_values[:, :-1, :] = self.h_T_half.all_values[:, 1:, :]
+        U.vgrid.hn.all_values[:, :, :] = X.hn.all_values[:, 1:, 1:]
+        V.ugrid.hn.all_values[:, :, :] = U.vgrid.hn.all_values
+        if self.runtype == RunType.BAROCLINIC:
+            _pygetm.thickness2center_depth(T.mask, T.hn, self.depth)

@@ -360,6 +360,61 @@ int getm_advection_2d_mixed(getm_advection* adv, getm_grid* tgrid, getm_grid* ug
                             const double* Ah_v, double timestep, double* D, const double* DU,
                             const double* DV, double* var, cudaStream_t stream);
 
+/* ---- fused sequences of the split-explicit 2D substep ---------------------
+ * No single counterpart in the reference: each replaces a sequence of the
+ * reference's operations with one launch and, with FP64 arithmetic, gives
+ * bitwise the same results as running them one by one (points that a
+ * separate interpolation does not write keep their previous values).  All
+ * fields are [j][i] with the full extents of their grid (nx, ny of the T
+ * grid; X fields nx+1, ny+1).                                              */
+/* Simulation.update_depth, 2D part (python/pygetm/simulation.py:1498-1586):
+ * elevation2depth of z on T (Dmin -1000), Dclip = max(D, Dmin), z_T_half =
+ * (zo + z)/2 and its interpolation to U, V, X (work arrays), depths and
+ * alpha there, D_T_half into workT and the UU/VV/UV/VU depth copies.       */
+int getm_update_depth_2d(int nx, int ny, double Dmin, double Dcrit, const double* z, const double* zo,
+                         const double* HT, const double* HU, const double* HV, const double* HX,
+                         const int* mT, const int* mU, const int* mV, const int* mX, double* DT,
+                         double* DclipT, double* workT, double* workU, double* DU, double* alphaU,
+                         double* workV, double* DV, double* alphaV, double* workX, double* DX,
+                         double* DUU, double* DVV, double* DUV, double* DVU, cudaStream_t stream);
+/* Momentum._transport_2d_momentum up to its advection calls
+ * (python/pygetm/momentum.py:1017-1040): u1 = U/DU, v1 = V/DV, advU = u1,
+ * advV = v1, and uua, uva, vua, vva = interpolated transports over the
+ * depth of their grid (mixed != 0: these four quotients in float).         */
+int getm_momentum_2d_velocities(int nx, int ny, int mixed, const double* U, const double* V,
+                                const double* DU, const double* DV, const double* DUU,
+                                const double* DUV, const double* DVU, const double* DVV, double* u1,
+                                double* v1, double* advU, double* advV, double* uua, double* uva,
+                                double* vua, double* vva, cudaStream_t stream);
+/* Momentum.bottom_friction (momentum.py:1099-1125): v1 -> U and u1 -> V
+ * interpolation into the work arrays, then bottom_friction on both grids
+ * (momentum.F90:79-101, no z0b iteration; mixed != 0: float coefficient).  */
+int getm_momentum_2d_friction(int nx, int ny, int mixed, const int* mU, const int* mV, const double* u1,
+                              const double* v1, const double* DU, const double* DV, const double* z0bU,
+                              const double* z0bV, double* workU, double* workV, double* ru, double* rv,
+                              cudaStream_t stream);
+/* Momentum.coriolis, DEFAULT scheme, 2D (momentum.py:1127-1148): out =
+ * (-1 if negate) * f * interp_xy(src, ioffset, joffset).                  */
+int getm_coriolis_2d(int nx, int ny, int ioffset, int joffset, const double* src, const double* cor,
+                     double* out, int negate, cudaStream_t stream);
+/* advance_2d_transport (momentum.F90:147-189) in the mixed form: tendency
+ * summed in float, transport updated in double; same arguments as
+ * getm_advance_2d_transport.                                               */
+int getm_advance_2d_transport_mixed(int nx, int ny, int halox, int haloy, const int* mask,
+                                    const double* alpha, const double* D, const double* dp,
+                                    const double* taus, const double* cor, const double* adv,
+                                    const double* diff, const double* damp, const double* SA,
+                                    const double* SB, const double* SD, const double* SF,
+                                    const double* r, double dt, double* U, cudaStream_t stream);
+/* _U_cum += U; _V_cum += V (momentum.py:716-718), n points                 */
+int getm_accumulate_2d(long long n, const double* U, const double* V, double* Ucum, double* Vcum,
+                       cudaStream_t stream);
+/* zo = z, then advance_surface_elevation (simulation.py:1468-1486)         */
+int getm_surface_elevation_fused(int nx, int ny, int halox, int haloy, const int* mask,
+                                 const double* dyu, const double* dxv, const double* iarea, double* z,
+                                 double* zo, const double* U, const double* V, const double* fwf,
+                                 double dt, cudaStream_t stream);
+
 /* ---- domain totals (compensated budget sums) -----------------------------
  * Replaces python/pygetm/simulation.py:1409-1444 (Simulation.totals: total
  * volume = sum of D*area, tracer total = sum of c*area*hn over unmasked

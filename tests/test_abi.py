@@ -22,6 +22,8 @@ def header_signatures():
                 codes += "p"
             elif a.startswith("double"):
                 codes += "d"
+            elif a.startswith("long long"):
+                codes += "l"
             elif a.startswith("int"):
                 codes += "i"
             else:

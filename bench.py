@@ -309,8 +309,11 @@ def _roofline(sim, peak, peak_kind):
     # u, hu, h in + h out + per tracer in + out (each 3D field read or written once)
     alg = n3 * (sz + 8 + 8 + 8 + len(fin) * 2 * sz)
     achieved = alg / t_kernel / 1e9
+    # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
+    # of the float x pass on this workload, from an ncu capture of this bench
+    traffic = 152.93e6 if sz == 4 else None
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": f"{'hpass_x_f32_kernel' if sz == 4 else 'hpass_x_kernel<double>'} (2 tracers)",
+            "traffic": traffic, "kernel": f"{'hpass_x_inc_kernel<float>' if sz == 4 else 'hpass_x_kernel<double>'} (2 tracers)",
             "bytes_per_launch": alg, "us_per_launch": t_kernel * 1e6, "peak_kind": peak_kind}
 
 

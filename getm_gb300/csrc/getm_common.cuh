@@ -67,11 +67,21 @@ static inline unsigned int getm_div_up(long long a, long long b) { return (unsig
 // thickness is needed, e.g. as a divisor of an increment), for doubles in the
 // normal float range.  Values outside those ranges take the hardware path.
 // ---------------------------------------------------------------------------
+// Out-of-line fallbacks: keeping the hardware conversions out of the common
+// path stops the compiler from issuing them predicated on every call.
+static __device__ __noinline__ double getm_f2d_hw(float x) { return (double)x; }
+static __device__ __noinline__ float getm_d2f_hw(double x) { return (float)x; }
+
 __device__ __forceinline__ double getm_f2d(float x)
 {
     const unsigned int b = __float_as_uint(x);
     const unsigned int e = (b >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)x;  // zero, subnormal, inf, nan
+    if (e == 0u) {
+        if ((b & 0x7fffffu) == 0u)  // signed zero
+            return __longlong_as_double((long long)((unsigned long long)(b >> 31) << 63));
+        return getm_f2d_hw(x);  // subnormal
+    }
+    if (e == 0xffu) return getm_f2d_hw(x);  // inf, nan
     const unsigned long long s = (unsigned long long)(b >> 31) << 63;
     const unsigned long long m = (unsigned long long)(b & 0x7fffffu) << 29;
     const unsigned long long de = (unsigned long long)(e + (1023u - 127u)) << 52;
@@ -82,7 +92,10 @@ __device__ __forceinline__ float getm_d2f_approx(double x)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const int e = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
-    if (e <= 0 || e >= 0xff) return (float)x;  // outside the normal float range
+    if (e <= 0 || e >= 0xff) {
+        if ((b << 1) == 0ull) return __uint_as_float((unsigned int)(b >> 63) << 31);  // signed zero
+        return getm_d2f_hw(x);  // outside the normal float range
+    }
     const unsigned int s = (unsigned int)(b >> 63) << 31;
     const unsigned int m = (unsigned int)((b >> 29) & 0x7fffffu);
     return __uint_as_float(s | ((unsigned int)e << 23) | m);

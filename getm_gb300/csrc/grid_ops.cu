@@ -172,12 +172,14 @@ __global__ void elevation2depth_kernel(int n, const double* z, const double* H, 
     if (p < n && mask[p] != 0) D[p] = fmax(H[p] + z[p], Dmin);  // wrapper.F90:444
 }
 
-__global__ void alpha_kernel(int n, const double* D, double Dmin, double Dcrit, const int* mask,
+// wrapper.F90:428-436, with the constant divisor 1/(Dcrit - Dmin) formed once
+// (ialpha) and applied as a product: FP64 division is costly on GB300.
+__global__ void alpha_kernel(int n, const double* D, double Dmin, double ialpha, const int* mask,
                              double* alpha)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < n && mask[p] != 0)  // wrapper.F90:434
-        alpha[p] = fmax(0.0, fmin(1.0, (D[p] - Dmin) / (Dcrit - Dmin)));
+        alpha[p] = fmax(0.0, fmin(1.0, (D[p] - Dmin) * ialpha));
 }
 
 __global__ void multiply_add_kernel(int n, double* tgt, const double* add, double s)
@@ -201,7 +203,7 @@ extern "C" int getm_alpha(int n, const double* D, double Dmin, double Dcrit, con
 {
     if (n < 0 || !D || !mask || !alpha) return GETM_ERR_ARG;
     if (n == 0) return GETM_OK;
-    alpha_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(n, D, Dmin, Dcrit, mask, alpha);
+    alpha_kernel<<<getm_div_up(n, EW_THREADS), EW_THREADS, 0, stream>>>(n, D, Dmin, 1.0 / (Dcrit - Dmin), mask, alpha);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

@@ -98,7 +98,8 @@ extern "C" int getm_bottom_friction_mixed(int nx, int ny, const int* mask, const
 
 // momentum.F90:103-145: rows haloy..ny-haloy-1, every i, every k (mask unused).
 // T: type of the 3D tendency fields and of ea2/ea4; the internal pressure
-// gradient idp is double in both forms; the sum is formed in FP64.
+// gradient idp is double in both forms; the FP64 form sums in FP64, the
+// mixed form (float sources) in float.
 template <typename T>
 __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const double* alpha,
                                        const double* ho, const double* hn, const double* dp,
@@ -113,6 +114,21 @@ __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const 
     long long p = (long long)j * nx + i;
     const double al = alpha[p], dpp = dp[p];
     const double rho0i = 1.0 / GETM_RHO0;
+    if constexpr (getm_increment_form<T>) {
+        // mixed form: the sources are stored in float, so they are summed
+        // in float (each term to float precision)
+        const float alf = getm_d2f_approx(al), dtf = (float)dt;
+        const float gdp = (float)(-0.5 * GETM_G) * getm_d2f_approx(dpp);
+        for (int k = 0; k < nz; k++) {
+            long long q = p + k * plane;
+            float e = dtf * (gdp * (getm_d2f_approx(ho[q]) + getm_d2f_approx(hn[q])) +
+                             alf * (cor[q] + adv[q] + diff[q] + getm_d2f_approx(idp[q])));
+            if (k == nz - 1) e = e + dtf * alf * getm_d2f_approx(taus[p]) * (float)rho0i;
+            ea4[q] = e;
+        }
+        ea2[p] = -dtf * getm_d2f_approx(rr[p]);
+        return;
+    }
     for (int k = 0; k < nz; k++) {
         long long q = p + k * plane;
         double e = dt * (-0.5 * (ho[q] + hn[q]) * GETM_G * dpp

@@ -28,7 +28,7 @@ __device__ __forceinline__ double clamp_min(double x, double lo) { return isnan(
 
 struct DepthArgs {
     int nx, ny;                 // T-grid extents (halos included)
-    double Dmin, Dcrit;
+    double Dmin, Dcrit, ialpha; // ialpha = 1 / (Dcrit - 2 Dmin)
     const double *z, *zo;       // elevations (T)
     const double *HT, *HU, *HV, *HX;
     const int *mT, *mU, *mV, *mX;
@@ -39,93 +39,102 @@ struct DepthArgs {
     double *DUU, *DVV, *DUV, *DVU;
 };
 
-__device__ __forceinline__ double zhalf(const DepthArgs& a, long long p) { return (a.zo[p] + a.z[p]) * 0.5; }
+constexpr int UD_BX = 32, UD_BY = 4;
 
-// D_T_half at a T point: elevation2depth(z_T_half, H, Dmin) in place over z_T_half
-__device__ __forceinline__ double dthalf(const DepthArgs& a, long long p)
+// alpha (wrapper.F90:428-436) with the constant divisor as a reciprocal
+__device__ __forceinline__ double alpha_of(double d, double twoDmin, double ialpha)
 {
-    const double zh = zhalf(a, p);
-    return a.mT[p] != 0 ? fmax(a.HT[p] + zh, a.Dmin) : zh;
-}
-
-// z_X at X point (jx, ix) (interp_xy T->X, offsets 1, 1) or the previous
-// X._work value where that interpolation does not write
-__device__ __forceinline__ double zx_at(const DepthArgs& a, int jx, int ix)
-{
-    const long long px = (long long)jx * (a.nx + 1) + ix;
-    if (jx >= 1 && jx <= a.ny - 1 && ix >= 1 && ix <= a.nx - 1) {
-        const long long q = (long long)(jx - 1) * a.nx + (ix - 1);
-        return 0.25 * (zhalf(a, q) + zhalf(a, q + 1) + zhalf(a, q + a.nx) + zhalf(a, q + a.nx + 1));
-    }
-    return a.workX[px];
-}
-
-__device__ __forceinline__ double dx_at(const DepthArgs& a, int jx, int ix)
-{
-    const long long px = (long long)jx * (a.nx + 1) + ix;
-    return a.mX[px] != 0 ? fmax(a.HX[px] + zx_at(a, jx, ix), a.Dmin) : a.DX[px];
+    return fmax(0.0, fmin(1.0, (d - twoDmin) * ialpha));
 }
 
 // Simulation.update_depth, 2D part (simulation.py:1498-1586 without the
-// halo exchanges and mirroring of a single closed domain): one thread per
-// point of the X extents.
-__global__ void __launch_bounds__(S2_THREADS) update_depth_2d_kernel(DepthArgs a)
+// halo exchanges and mirroring of a single closed domain).  A 32 x 4 block
+// covers X points (j, i) of its tile and the T, U, V points with the same
+// indices; z_T_half of the tile plus a one-point halo is formed once into
+// shared memory.  Copies between grids are scattered by the point that
+// owns the source value (UU.D(j, i-1) = D_T_half(j, i), VV.D(j-1, i) =
+// D_T_half(j, i), UV.D(j-1, i-1) = VU.D(j-1, i-1) = X.D(j, i)).
+__global__ void __launch_bounds__(UD_BX * UD_BY) update_depth_2d_kernel(DepthArgs a)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i > a.nx || j > a.ny) return;
-    // X grid point (j, i): its own outputs; reads only inputs and points
-    // nobody writes (masked or edge points keep their previous values)
-    {
-        const long long px = (long long)j * (a.nx + 1) + i;
-        const double zx = zx_at(a, j, i);
-        if (j >= 1 && j <= a.ny - 1 && i >= 1 && i <= a.nx - 1) a.workX[px] = zx;
-        if (a.mX[px] != 0) a.DX[px] = fmax(a.HX[px] + zx, a.Dmin);
+    __shared__ double szh[UD_BY + 2][UD_BX + 2];  // z_T_half at rows j0-1.., cols i0-1..
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * UD_BX, j0 = blockIdx.y * UD_BY;
+    const int i = i0 + tx, j = j0 + ty;
+    const int nx = a.nx, ny = a.ny;
+    for (int q = ty * UD_BX + tx; q < (UD_BY + 2) * (UD_BX + 2); q += UD_BX * UD_BY) {
+        const int sj = q / (UD_BX + 2), si = q - sj * (UD_BX + 2);
+        const int gj = j0 - 1 + sj, gi = i0 - 1 + si;
+        double v = 0.0;
+        if (gj >= 0 && gj < ny && gi >= 0 && gi < nx) {
+            const long long g = (long long)gj * nx + gi;
+            v = (a.zo[g] + a.z[g]) * 0.5;
+        }
+        szh[sj][si] = v;
     }
-    if (i >= a.nx || j >= a.ny) return;
-    const long long p = (long long)j * a.nx + i;
-    // T: elevation2depth(z, H, -1000) then Dclip = clamp(D, Dmin)
+    __syncthreads();
+    if (i > nx || j > ny) return;
+    const int sj = ty + 1, si = tx + 1;  // (j, i) in the tile
+    // X point (j, i): interp_xy T->X (offsets 1, 1) where it writes, else the
+    // previous X._work value
+    {
+        const long long px = (long long)j * (nx + 1) + i;
+        double zx;
+        if (j >= 1 && j <= ny - 1 && i >= 1 && i <= nx - 1) {
+            zx = 0.25 * (szh[sj - 1][si - 1] + szh[sj - 1][si] + szh[sj][si - 1] + szh[sj][si]);
+            a.workX[px] = zx;
+        } else {
+            zx = a.workX[px];
+        }
+        double dx = a.DX[px];
+        if (a.mX[px] != 0) {
+            dx = fmax(a.HX[px] + zx, a.Dmin);
+            a.DX[px] = dx;
+        }
+        if (j >= 1 && i >= 1 && j - 1 < ny && i - 1 < nx) {  // UV.D = X.D[1:, 1:]; VU.D = UV.D
+            const long long q = (long long)(j - 1) * nx + (i - 1);
+            a.DUV[q] = dx;
+            a.DVU[q] = dx;
+        }
+    }
+    if (i >= nx || j >= ny) return;
+    const long long p = (long long)j * nx + i;
+    const double zh = szh[sj][si];
+    // T: elevation2depth(z, H, -1000), Dclip = clamp(D, Dmin), D_T_half
     double DT = a.DT[p];
     if (a.mT[p] != 0) DT = fmax(a.HT[p] + a.z[p], -1000.0);
     a.DT[p] = DT;
     a.DclipT[p] = clamp_min(DT, a.Dmin);
-    // T._work ends as D_T_half (z_T_half on land)
-    a.workT[p] = dthalf(a, p);
+    const double dth = a.mT[p] != 0 ? fmax(a.HT[p] + zh, a.Dmin) : zh;
+    a.workT[p] = dth;
+    if (i >= 1) a.DUU[p - 1] = dth;   // UU.D[:, :-1] = D_T_half[:, 1:]
+    if (j >= 1) a.DVV[p - nx] = dth;  // VV.D[:-1, :] = D_T_half[1:, :]
     const double twoDmin = 2 * a.Dmin;
-    // U: z_U = interp_x(z_T_half, ioffset 0); D; alpha
-    if (i < a.nx - 1) {
-        const double zu = 0.5 * (zhalf(a, p) + zhalf(a, p + 1));
+    // U: z_U = interp_x(z_T_half, ioffset 0) for i < nx-1, else the old value
+    double zu;
+    if (i < nx - 1) {
+        zu = 0.5 * (zh + szh[sj][si + 1]);
         a.workU[p] = zu;
-        if (a.mU[p] != 0) {
-            const double d = fmax(a.HU[p] + zu, a.Dmin);
-            a.DU[p] = d;
-            a.alphaU[p] = fmax(0.0, fmin(1.0, (d - twoDmin) / (a.Dcrit - twoDmin)));
-        }
-        a.DUU[p] = dthalf(a, p + 1);  // UU.D[:, :-1] = D_T_half[:, 1:]
-    } else if (a.mU[p] != 0) {
-        const double d = fmax(a.HU[p] + a.workU[p], a.Dmin);
+    } else {
+        zu = a.workU[p];
+    }
+    if (a.mU[p] != 0) {
+        const double d = fmax(a.HU[p] + zu, a.Dmin);
         a.DU[p] = d;
-        a.alphaU[p] = fmax(0.0, fmin(1.0, (d - twoDmin) / (a.Dcrit - twoDmin)));
+        a.alphaU[p] = alpha_of(d, twoDmin, a.ialpha);
     }
-    // V: z_V = interp_y(z_T_half, joffset 0); D; alpha
-    if (j < a.ny - 1) {
-        const double zv = 0.5 * (zhalf(a, p) + zhalf(a, p + a.nx));
+    // V: z_V = interp_y(z_T_half, joffset 0) for j < ny-1
+    double zv;
+    if (j < ny - 1) {
+        zv = 0.5 * (zh + szh[sj + 1][si]);
         a.workV[p] = zv;
-        if (a.mV[p] != 0) {
-            const double d = fmax(a.HV[p] + zv, a.Dmin);
-            a.DV[p] = d;
-            a.alphaV[p] = fmax(0.0, fmin(1.0, (d - twoDmin) / (a.Dcrit - twoDmin)));
-        }
-        a.DVV[p] = dthalf(a, p + a.nx);  // VV.D[:-1, :] = D_T_half[1:, :]
-    } else if (a.mV[p] != 0) {
-        const double d = fmax(a.HV[p] + a.workV[p], a.Dmin);
-        a.DV[p] = d;
-        a.alphaV[p] = fmax(0.0, fmin(1.0, (d - twoDmin) / (a.Dcrit - twoDmin)));
+    } else {
+        zv = a.workV[p];
     }
-    // UV.D = X.D[1:, 1:]; VU.D = UV.D
-    const double duv = dx_at(a, j + 1, i + 1);
-    a.DUV[p] = duv;
-    a.DVU[p] = duv;
+    if (a.mV[p] != 0) {
+        const double d = fmax(a.HV[p] + zv, a.Dmin);
+        a.DV[p] = d;
+        a.alphaV[p] = alpha_of(d, twoDmin, a.ialpha);
+    }
 }
 
 // Momentum._transport_2d_momentum up to the advection calls
@@ -306,9 +315,11 @@ extern "C" int getm_update_depth_2d(int nx, int ny, double Dmin, double Dcrit, c
                           workV, DV, alphaV, workX, DX, DUU, DVV, DUV, DVU};
     for (const void* q : ptrs)
         if (!q) return GETM_ERR_ARG;
-    DepthArgs a{nx, ny, Dmin, Dcrit, z, zo, HT, HU, HV, HX, mT, mU, mV, mX, DT, DclipT, workT,
-                workU, DU, alphaU, workV, DV, alphaV, workX, DX, DUU, DVV, DUV, DVU};
-    update_depth_2d_kernel<<<plane_grid(nx + 1, ny + 1), S2_THREADS, 0, stream>>>(a);
+    DepthArgs a{nx, ny, Dmin, Dcrit, 1.0 / (Dcrit - 2 * Dmin), z, zo, HT, HU, HV, HX, mT, mU, mV, mX, DT, DclipT,
+                workT, workU, DU, alphaU, workV, DV, alphaV, workX, DX, DUU, DVV, DUV, DVU};
+    dim3 block(UD_BX, UD_BY);
+    dim3 grid(getm_div_up(nx + 1, UD_BX), getm_div_up(ny + 1, UD_BY));
+    update_depth_2d_kernel<<<grid, block, 0, stream>>>(a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

@@ -285,8 +285,8 @@ int getm_density_buoyancy(int n, const double* salt, const double* temp, const d
  * the tridiagonal solves.  Layer thicknesses, elevations, water depths,
  * metrics, 2D transports, density, buoyancy and the internal pressure
  * gradient stay double (the gradient is a small difference of large column
- * integrals of buoyancy); the thickness updates, the w recursion and the
- * momentum sources are evaluated in FP64.  The *_f32 internal-pressure
+ * integrals of buoyancy); the thickness updates and the w recursion are
+ * evaluated in FP64, the momentum sources in float.  The *_f32 internal-pressure
  * entry points (float buoyancy and gradients) remain available.           */
 int getm_advection_apply_3d_batch_f32(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
                                       getm_grid* vgrid, int ufirst, const float* u, const float* v,

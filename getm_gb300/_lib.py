@@ -78,6 +78,12 @@ _SIGS = {
     "getm_advance_2d_transport_mixed": "iiiippppppppppppppdps",
     "getm_accumulate_2d": "lpppps",
     "getm_surface_elevation_fused": "iiiipppppppppds",
+    "getm_open_boundary_elevation": "iiipppppppppppppdps",
+    "getm_open_boundary_tracers": "iiiiiiippppppipps",
+    "getm_open_boundary_tracers_f32": "iiiiiiippppppipps",
+    "getm_mirror": "ippilpps",
+    "getm_mirror_f32": "ippilpps",
+    "getm_open_boundary_depth": "ippppppddppps",
     "getm_collect_3d_momentum_sources": "iiiiipppppppppppdpps",
     "getm_advance_2d_transport": "iiiippppppppppppppdps",
     "getm_w_momentum_3d": "iiiiiiippppppppdps",

@@ -263,6 +263,9 @@ class Domain:
         self._dx = np.hypot(dx_x, dy_x)
         self._dy = np.hypot(dx_y, dy_y)
         self._area = self._dx * self._dy
+        from .open_boundaries import OpenBoundaries
+
+        self.open_boundaries = OpenBoundaries(nx, ny)
 
     @property
     def mask(self):
@@ -347,6 +350,7 @@ class Domain:
         if self._H is None:
             raise Exception("Water depth at rest (H) has not been provided")
         self.infer_UVX_masks2()
+        self.open_boundaries.adjust_mask(self._mask)
 
         def make(postfix, ioffset, joffset, overlap=0):
             g = HostGrid(self.nx, self.ny, nz, halox, haloy, postfix, ioffset, joffset, overlap)
@@ -373,8 +377,13 @@ class Domain:
         if velocity_grids > 1:
             U.close_flux_interfaces()
             V.close_flux_interfaces()
+            # no transport between velocity points just outside an open
+            # boundary (python/pygetm/domain.py:752-762)
+            UV.mask[:-1, :][(U.mask[:-1, :] == 4) & (U.mask[1:, :] == 4)] = 0
+            VU.mask[:, :-1][(V.mask[:, :-1] == 4) & (V.mask[:, 1:] == 4)] = 0
         for g in T.all_grids():
             g.freeze()
+        self.open_boundaries.initialize(T)
         return T
 
     def cfl_check(self) -> float:

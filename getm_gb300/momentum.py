@@ -51,6 +51,7 @@ class Momentum:
         # fused 2D substep kernels (one launch per sequence of operations);
         # False runs each operation as its own kernel
         self.fused_2d = True
+        self._ob = None  # open-boundary operations (set by the simulation)
 
     # ------------------------------------------------------------------ setup
     def _create_arrays(self, tgrid: Grid, three_d: bool):
@@ -169,11 +170,15 @@ class Momentum:
         def u():
             _pygetm.advance_2d_transport(self.U, dpdx, tausx, self.corU, self.advU, self.diffU, self.dampU,
                                          self.SxA, self.SxB, self.SxD, self.SxF, self.ru, timestep, mixed)
+            if self._ob is not None:
+                self._ob.mirror("U", self.U)
             self.coriolis(self.U, self.corV, True)
 
         def v():
             _pygetm.advance_2d_transport(self.V, dpdy, tausy, self.corV, self.advV, self.diffV, self.dampV,
                                          self.SyA, self.SyB, self.SyD, self.SyF, self.rv, timestep, mixed)
+            if self._ob is not None:
+                self._ob.mirror("V", self.V)
             self.coriolis(self.V, self.corU, False)
 
         if self._ufirst:
@@ -349,3 +354,5 @@ class Momentum:
         dev.all_values.sub_(tp2d.all_values)
         dev.all_values.div_(grid.D.all_values)
         tp3d.all_values.sub_(dev.all_values * grid.hn.all_values)
+        if self._ob is not None:  # momentum.py:1211-1212
+            self._ob.mirror("U" if tp3d is self.pk else "V", tp3d)

@@ -137,6 +137,13 @@ class Simulation:
             self.depth = T.array(z=CENTERS, name="pres")
         self.momentum = momentum or Momentum(dtype=d3)
         self.momentum.fused_2d = fused_2d
+        # open boundaries (python/pygetm/open_boundaries.py) and model time
+        from .open_boundaries import DeviceBoundaries
+
+        ob = getattr(T_host, "open_boundaries", None)
+        self._ob = DeviceBoundaries(ob, T, d3) if ob is not None and ob.np > 0 else None
+        self.momentum._ob = self._ob
+        self._time = torch.zeros((), dtype=torch.float64, device=T.device)
         self.momentum.initialize(T, int(self.runtype), advection_scheme)
         self.airsea = airsea or Fluxes()
         self.airsea.initialize(T)
@@ -184,12 +191,16 @@ class Simulation:
         self.split_factor = int(split_factor)
         self.macrotimestep = self.timestep * self.split_factor
         self.istep = 0
+        self._time.zero_()
+        if self._ob is not None:
+            self._ob.init_tracer_values(self.tracers._tracers)
         self._start()
         self._update_forcing_and_diagnostics(macro_active=True)
 
     def advance(self):
         """python/pygetm/simulation.py:291-325"""
         self.istep += 1
+        self._time.add_(self.timestep)
         macro_active = self.istep % self.split_factor == 0
         self._advance_state(macro_active)
         self._update_forcing_and_diagnostics(macro_active)
@@ -251,6 +262,9 @@ class Simulation:
         update_z0b = self.runtype == RunType.BAROTROPIC_2D and not starting
         update_3d = self.runtype > RunType.BAROTROPIC_2D and macro_active
         update_baroclinic = self.runtype == RunType.BAROCLINIC and macro_active
+        if update_3d and self._ob is not None:
+            # tracers at the open boundaries (simulation.py:1160-1168)
+            self._ob.update_tracers(self.tracers._tracers)
         if update_baroclinic:
             self.update_density()
             self.update_internal_pressure()
@@ -261,6 +275,11 @@ class Simulation:
         self.momentum.update_depth_integrated_diagnostics(self.timestep, skip_coriolis=not starting,
                                                          update_z0b=update_z0b)
         self.fwf.all_values.copy_(self.airsea.pe.all_values)
+        if self._ob is not None:
+            # elevation at the open boundaries, before the surface pressure
+            # gradient (simulation.py:1252-1257)
+            self._ob.prescribe(self._time)
+            self._ob.update_elevation(self)
         self.update_surface_pressure_gradient(self.T.z, self.airsea.sp)
         self.airsea.taux.interp(self.tausx)
         self.airsea.tauy.interp(self.tausy)
@@ -353,6 +372,9 @@ class Simulation:
             _pygetm.update_depth_2d(T, z_T, zo_T, self.Dmin, self.Dcrit)
         else:
             self._update_depth_2d_ops(z_T, zo_T)
+        if self._ob is not None:
+            # z_T_half.mirror(z_U), z_T_half.mirror(z_V) (simulation.py:1545-1550)
+            self._ob.update_depth(self, z_T, zo_T)
         if _3d:
             self._update_depth_3d()
 

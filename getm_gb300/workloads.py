@@ -286,3 +286,41 @@ def serving_requests(rate: float, duration: float, seed: int = 5, nmin: int = 64
         reqs.append(Request(rid, make, nsteps, t, precision, (nx + 4) * (ny + 4) * (nz + 1)))
         rid += 1
     return reqs
+
+
+M2_PERIOD = 44712.0  # s (M2 tidal constituent)
+
+
+def tidal_channel(nx: int = 60, ny: int = 30, nz: int = 8, dx: float = 2000.0, seed: int = 7,
+                  amplitude: float = 1.0) -> Workload:
+    """A channel with three open boundaries of different kinds: west Flather
+    (elevation) forced by an M2 tide of ``amplitude`` metres, tracers zero
+    gradient; east clamped elevation (the same tide, lagged by 30 degrees),
+    tracers sponge; north Flather (transport) with zero prescribed values,
+    tracers clamped; south coast closed.  Smoothed bathymetry 20-50 m,
+    f = 1e-4, z0 giving a drag coefficient of 2.5e-3 at 30 m."""
+    from .open_boundaries import CLAMPED, FLATHER_ELEV, FLATHER_TRANSPORT, SPONGE, ZERO_GRADIENT
+
+    rng = np.random.default_rng(seed)
+    H = 20.0 + 30.0 * _norm01(gaussian_filter(rng.standard_normal((ny, nx)), sigma=4))
+    x = dx * (np.arange(nx) + 0.5)
+    y = dx * (np.arange(ny) + 0.5)
+    kappa, cd = 0.4, 2.5e-3
+    z0 = 0.5 * 30.0 / (np.exp(kappa / np.sqrt(cd)) - 1.0)
+    dom = create_cartesian(x, y, H=H, f=1e-4, z0=z0)
+    ob = dom.open_boundaries
+    ob.add_left_boundary("W", 0, 0, ny, FLATHER_ELEV, ZERO_GRADIENT)
+    ob.add_right_boundary("E", nx - 1, 0, ny, CLAMPED, SPONGE)
+    ob.add_top_boundary("N", ny - 1, 1, nx - 1, FLATHER_TRANSPORT, CLAMPED)
+    T = dom.create_grids(nz, halox=2, haloy=2, velocity_grids=2)
+    omega = 2.0 * np.pi / M2_PERIOD
+    amp = np.zeros(ob.np)
+    phase = np.zeros(ob.np)
+    for b in ob:
+        if b.name in ("W", "E"):
+            amp[b.start:b.stop] = amplitude
+            phase[b.start:b.stop] = 0.0 if b.name == "W" else -np.pi / 6
+    ob.set_tide(omega, amp, phase)
+    dga = calculate_sigma(nz)
+    params = dict(timestep=5.0, split_factor=10, num=1e-4, nuh=1e-4, z0=z0, scheme=5)
+    return Workload("tidal_channel", T, dga, {}, params)

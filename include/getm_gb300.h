@@ -415,6 +415,46 @@ int getm_surface_elevation_fused(int nx, int ny, int halox, int haloy, const int
                                  double* zo, const double* U, const double* V, const double* fwf,
                                  double dt, cudaStream_t stream);
 
+/* ---- open boundaries (python/pygetm/open_boundaries.py) ------------------
+ * Point tables (halo-inclusive T indices i, j; condition type; inward
+ * direction di, dj; side 1..4 = W, N, E, S; inflow sign) come from the host
+ * collection.  The reference updates its boundaries one after another, so a
+ * call covers the contiguous point range [start, stop) of one boundary.    */
+/* elevation: ZeroGradient (:338-356), Clamped (:358-375), Flather on
+ * elevation or transport (:377-416); result clipped to Dmin - H
+ * (simulation.py:580-582, :1252-1257).  z_ext, flow_ext: per point.        */
+int getm_open_boundary_elevation(int start, int stop, int nx, const int* i, const int* j,
+                                 const int* type, const int* di, const int* dj, const int* side,
+                                 const double* inflow_sign, const double* H, const double* Dclip,
+                                 const double* U, const double* V, const double* z_ext,
+                                 const double* flow_ext, double Dmin, double* z, cudaStream_t stream);
+/* tracers (simulation.py:1160-1168): ZeroGradient, Clamped, Sponge with
+ * nsponge points (:195-336, fixed relaxation).  vars, bdy: HOST arrays of
+ * ntracer (<= 16) device pointers; bdy[t] holds nz x np prescribed values. */
+int getm_open_boundary_tracers(int start, int stop, int np, int nx, int ny, int nz, int nsponge,
+                               const int* i, const int* j, const int* type, const int* di,
+                               const int* dj, const int* mask, int ntracer, double* const* vars,
+                               const double* const* bdy, cudaStream_t stream);
+int getm_open_boundary_tracers_f32(int start, int stop, int np, int nx, int ny, int nz, int nsponge,
+                                   const int* i, const int* j, const int* type, const int* di,
+                                   const int* dj, const int* mask, int ntracer, float* const* vars,
+                                   const float* const* bdy, cudaStream_t stream);
+/* core.Array.mirror (python/pygetm/core.py:723-728): field[tgt] = field[src]
+ * for n pairs of flat [j][i] indices, every one of nlev levels of size plane,
+ * with every source read before any target is written (a point may be the
+ * target of one pair and the source of another); work: device buffer of
+ * n * nlev elements.                                                       */
+int getm_mirror(int n, const int* src, const int* tgt, int nlev, long long plane, double* field,
+                double* work, cudaStream_t stream);
+int getm_mirror_f32(int n, const int* src, const int* tgt, int nlev, long long plane, float* field,
+                    float* work, cudaStream_t stream);
+/* depths at the velocity points just outside boundaries after
+ * getm_update_depth_2d: z_T_half.mirror(z_U), elevation2depth, alpha
+ * (simulation.py:1545-1552); srcT: boundary T points, tgt: outer points.   */
+int getm_open_boundary_depth(int n, const int* srcT, const int* tgt, const double* z, const double* zo,
+                             const double* H, const int* mask, double Dmin, double Dcrit, double* work,
+                             double* D, double* alpha, cudaStream_t stream);
+
 /* ---- domain totals (compensated budget sums) -----------------------------
  * Replaces python/pygetm/simulation.py:1409-1444 (Simulation.totals: total
  * volume = sum of D*area, tracer total = sum of c*area*hn over unmasked

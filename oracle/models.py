@@ -153,6 +153,7 @@ class Momentum:
         self._grids = grids
         self._ufirst = False
         self._u3dfirst = False
+        self.ob = None  # open-boundary operations (set by the simulation)
 
     def start(self):
         for n, g in self._grids.items():
@@ -171,11 +172,15 @@ class Momentum:
         def u():
             O.advance_2d_transport(ug, self.U, dpdx, tausx, self.corU, self.advU, self.diffU, self.dampU, self.SxA,
                                    self.SxB, self.SxD, self.SxF, self.ru, timestep)
+            if self.ob is not None:
+                self.ob.mirror("U", self.U)
             self.coriolis(ug, self.U, vg, self.corV, True)
 
         def v():
             O.advance_2d_transport(vg, self.V, dpdy, tausy, self.corV, self.advV, self.diffV, self.dampV, self.SyA,
                                    self.SyB, self.SyD, self.SyF, self.rv, timestep)
+            if self.ob is not None:
+                self.ob.mirror("V", self.V)
             self.coriolis(vg, self.V, ug, self.corU, False)
 
         if self._ufirst:
@@ -301,6 +306,84 @@ class Momentum:
             dev -= tp2d
             dev /= grid.D
             tp3d -= dev * grid.hn
+        if self.ob is not None:
+            self.ob.mirror("U" if tp3d is self.pk else "V", tp3d)
+
+
+class BoundaryOps:
+    """Open-boundary conditions and mirroring restated in numpy
+    (python/pygetm/open_boundaries.py: ZeroGradient :338-356, Clamped
+    :358-375, Flather :377-416, Sponge :195-336 without flow-dependent
+    relaxation; core.Array.mirror, core.py:723-728).  Boundaries are updated
+    one after another, as ArrayOpenBoundaries.update does (:494-497)."""
+
+    def __init__(self, ob, T):
+        self.ob = ob
+        self.T = T
+        self.ranges = [(b.start, b.stop) for b in ob]
+        self.z = np.zeros(ob.np)
+        self.flow = np.zeros(ob.np)
+        self.tracer_values = {}
+
+    def prescribe(self, time):
+        if self.ob.constituents:
+            self.z[...] = 0.0
+            for om, amp, ph in self.ob.constituents:
+                self.z += amp * np.cos(time * om + ph)
+
+    def update_elevation(self, sim):
+        ob, T = self.ob, self.T
+        z = T.z
+        for s, e in self.ranges:
+            i, j = ob.i[s:e], ob.j[s:e]
+            ty = ob.type_2d[s]
+            if ty == 1:  # ZERO_GRADIENT
+                v = z[j + ob.dj[s:e], i + ob.di[s:e]]
+            elif ty == 3:  # CLAMPED
+                v = self.z[s:e]
+            else:
+                side = ob.side[s]
+                U, V = sim.momentum.U, sim.momentum.V
+                tp = {1: U[j, i], 3: U[j, i - 1], 4: V[j, i], 2: V[j - 1, i]}[side]
+                D = T.Dclip[j, i]
+                ext = self.flow[s:e] * D if ty == 4 else self.flow[s:e]
+                v = self.z[s:e] - ob.inflow_sign[s:e] * (tp - ext) / np.sqrt(D * O.GRAVITY)
+            z[j, i] = np.maximum(sim.Dmin - T.H[j, i], v)
+
+    def mirror(self, name, field):
+        src, tgt = getattr(self.ob, "mirror_" + name)
+        if src.size:
+            flat = field.reshape(field.shape[:-2] + (-1,))
+            flat[..., tgt] = flat[..., src]
+
+    def mirror_to(self, name, source, target):
+        src, tgt = getattr(self.ob, "mirror_" + name)
+        if src.size:
+            target.reshape(target.shape[:-2] + (-1,))[..., tgt] = source.reshape(source.shape[:-2] + (-1,))[..., src]
+
+    def init_tracer_values(self, tracers):
+        ob = self.ob
+        for n, tr in enumerate(tracers):
+            self.tracer_values[n] = tr[:, ob.j, ob.i].copy()
+
+    def update_tracers(self, tracers):
+        ob, T = self.ob, self.T
+        n_sp = ob.sponge_n
+        for n, tr in enumerate(tracers):
+            bdyv = self.tracer_values[n]
+            for s, e in self.ranges:
+                i, j, di, dj = ob.i[s:e], ob.j[s:e], ob.di[s:e], ob.dj[s:e]
+                ty = ob.type_3d[s]
+                if ty == 1:
+                    tr[:, j, i] = tr[:, j + dj, i + di]
+                    continue
+                b = bdyv[:, s:e]
+                tr[:, j, i] = b
+                if ty == 5:
+                    for m in range(n_sp):
+                        jj, ii = j + (m + 1) * dj, i + (m + 1) * di
+                        sp = ((n_sp - m) / (n_sp + 1.0)) ** 2 * (T.mask[jj, ii] == 1)
+                        tr[:, jj, ii] += sp * (b - tr[:, jj, ii])
 
 
 class Simulation:
@@ -353,6 +436,10 @@ class Simulation:
         self.internal_pressure_method = internal_pressure
         self.idpdx = _arr(self.U, T.nz); _fill(self.idpdx, self.U, 0.0)
         self.idpdy = _arr(self.V, T.nz); _fill(self.idpdy, self.V, 0.0)
+        ob = getattr(T_host, "open_boundaries", None)
+        self.ob = BoundaryOps(ob, T) if ob is not None and ob.np > 0 else None
+        self.momentum.ob = self.ob
+        self.time = 0.0
         self.update_depth(True)
         self.update_depth(True)
 
@@ -360,11 +447,15 @@ class Simulation:
         self.timestep, self.split_factor = timestep, split_factor
         self.macrotimestep = timestep * split_factor
         self.istep = 0
+        self.time = 0.0
+        if self.ob is not None:
+            self.ob.init_tracer_values(self.tracers)
         self._start()
         self._update_forcing_and_diagnostics(True)
 
     def advance(self):
         self.istep += 1
+        self.time += self.timestep
         macro_active = self.istep % self.split_factor == 0
         self._advance_state(macro_active)
         self._update_forcing_and_diagnostics(macro_active)
@@ -415,6 +506,8 @@ class Simulation:
     def _update_forcing_and_diagnostics(self, macro_active):
         T, m = self.T, self.momentum
         starting = self.istep == 0
+        if macro_active and self.ob is not None:
+            self.ob.update_tracers(self.tracers)
         if self.runtype == 4 and macro_active:
             with np.errstate(all="ignore"):
                 self.rho[...], self.buoy[...] = seos_buoyancy(self.salt, self.temp, self.depth)
@@ -427,6 +520,9 @@ class Simulation:
         self.update_depth(False)
         m.update_depth_integrated_diagnostics(T, self.timestep, skip_coriolis=not starting)
         self.fwf[...] = self.pe
+        if self.ob is not None:
+            self.ob.prescribe(self.time)
+            self.ob.update_elevation(self)
         O.surface_pressure_gradient(T, T.z, self.sp, self.dpdx, self.dpdy, self.Dmin)
         O.interpolate(T, self.U, self.taux, self.tausx)
         O.interpolate(T, self.V, self.tauy, self.tausy)
@@ -450,8 +546,10 @@ class Simulation:
         zh = T._work
         np.add(zo_T, z_T, out=zh)
         zh *= 0.5
-        for g in (U, V, X):
+        for g, mname in ((U, "TU"), (V, "TV"), (X, None)):
             O.interpolate(T, g, zh, g._work)
+            if self.ob is not None and mname:
+                self.ob.mirror_to(mname, zh, g._work)
             O.elevation2depth(g, g._work, g.H, self.Dmin, g.D)
         with np.errstate(all="ignore"):
             O.alpha(U, U.D, 2 * self.Dmin, self.Dcrit, U.alpha)

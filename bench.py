@@ -54,6 +54,9 @@ def _args():
     ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson request rate, 1/s (0: skip)")
     ap.add_argument("--serve-duration", type=float, default=15.0, help="seconds of arrivals per form")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--shelf-steps", type=int, default=0,
+                    help="3D steps of the 20-tracer shelf sea, both forms, for its error report (0: skip)")
+    ap.add_argument("--shelf-size", default="1000x800x30")
     return ap.parse_args()
 
 
@@ -456,6 +459,49 @@ def _serving_leg(args, device):
     return out
 
 
+def _shelf_leg(args, device):
+    """The many-tracer shelf sea (20 passive tracers, tidal open boundaries):
+    step time of both forms and, after ``--shelf-steps`` 3D steps, the
+    per-tracer error and the compensated tracer totals of the mixed form
+    against FP64."""
+    import numpy as np
+    import torch
+
+    from getm_gb300 import workloads
+
+    nx, ny, nz = (int(v) for v in args.shelf_size.split("x"))
+    wl = workloads.shelf_sea(nx=nx, ny=ny, nz=nz, ntracer=20)
+    cells = nx * ny * nz
+    out = {"workload": f"shelf sea {nx}x{ny}x{nz}, 20 passive tracers, M2 tide on open boundaries, "
+                       f"{wl.params['split_factor']} substeps per 3D step", "steps": args.shelf_steps}
+    runners = {}
+    for f in ("mixed", "fp64"):
+        r = Runner(workloads.start_shelf_sea(wl, f, device), 3, not args.no_graph)
+        ms, _ = r.timed(5)
+        out[f] = {"ms_per_step": ms / (5 * Runner.period), "value": cells * 5 * Runner.period / (ms / 1000.0)}
+        runners[f] = r
+    for r in runners.values():
+        r.run_to(args.shelf_steps)
+    torch.cuda.synchronize()
+    a, b = runners["mixed"].sim, runners["fp64"].sim
+    wet = torch.from_numpy(wl.T.mask == 1).to(device)
+    errs = []
+    for x, y in zip(a.tracers._tracers, b.tracers._tracers):
+        xv, yv = x.all_values.double()[..., wet], y.all_values[..., wet]
+        errs.append(float((xv - yv).abs().max() / yv.abs().max()))
+    ta, tb = a.totals_device().tolist(), b.totals_device().tolist()
+    za, zb = a.T.z.all_values[wet], b.T.z.all_values[wet]
+    out.update({"steps_done": runners["mixed"].steps_done, "tracer_error_max": max(errs),
+                "tracer_error_median": float(np.median(errs)),
+                "tracer_totals_vs_fp64_max": max(abs(x - y) / abs(y) for x, y in zip(ta[1:], tb[1:])),
+                "volume_vs_fp64": (ta[0] - tb[0]) / tb[0],
+                "z_error_m": float((za - zb).abs().max()), "z_max_m": float(zb.abs().max())})
+    del runners, a, b
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -552,6 +598,8 @@ def run_ours(args):
         line["ensemble"] = _ensemble_leg(args, device)
     if rank == 0 and args.serve_rate > 0:
         line["serving"] = _serving_leg(args, device)
+    if rank == 0 and args.shelf_steps > 0:
+        line["shelf_sea"] = _shelf_leg(args, device)
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
         v, dt = cpu_reference(args, 2, threads)

@@ -314,19 +314,29 @@ class Simulation:
         from ._lib import GETM_TOTALS_BLOCKS, call, ptr_array
         from .core import _sfx
 
+        from ._lib import GETM_MAX_TOTALS
+
         T = self.T
         trs = list(self.tracers._tracers) if self.runtype > RunType.BAROTROPIC_2D else []
         n = 1 + len(trs)
+        chunk = GETM_MAX_TOTALS
         if getattr(self, "_tot_out", None) is None or self._tot_out.numel() != n:
             self._tot_out = torch.zeros(n, dtype=torch.float64, device=T.device)
-            self._tot_work = torch.zeros(2 * GETM_TOTALS_BLOCKS * n, dtype=torch.float64, device=T.device)
+            self._tot_work = torch.zeros(2 * GETM_TOTALS_BLOCKS * (1 + chunk), dtype=torch.float64, device=T.device)
+            self._tot_part = torch.zeros(1 + chunk, dtype=torch.float64, device=T.device)
         hn = T.hn.all_values if trs else T.D.all_values
-        sfx = _sfx(*[t.all_values for t in trs]) if trs else ""
-        call("getm_domain_totals" + sfx, T.nx_, T.ny_, max(T.nz, 1), T.halox, T.haloy, T.nx, T.ny,
-             T.mask.all_values.data_ptr(), T.area.all_values.data_ptr(), T.D.all_values.data_ptr(), hn.data_ptr(),
-             len(trs),
-             ptr_array([t.all_values.data_ptr() for t in trs]), self._tot_work.data_ptr(), self._tot_out.data_ptr(),
-             torch.cuda.current_stream().cuda_stream)
+        groups = [trs[c:c + chunk] for c in range(0, len(trs), chunk)] or [[]]
+        for g, grp in enumerate(groups):
+            sfx = _sfx(*[t.all_values for t in grp]) if grp else ""
+            out = self._tot_out if len(groups) == 1 else self._tot_part
+            call("getm_domain_totals" + sfx, T.nx_, T.ny_, max(T.nz, 1), T.halox, T.haloy, T.nx, T.ny,
+                 T.mask.all_values.data_ptr(), T.area.all_values.data_ptr(), T.D.all_values.data_ptr(), hn.data_ptr(),
+                 len(grp), ptr_array([t.all_values.data_ptr() for t in grp]), self._tot_work.data_ptr(),
+                 out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+            if len(groups) > 1:
+                if g == 0:
+                    self._tot_out[0] = self._tot_part[0]
+                self._tot_out[1 + g * chunk:1 + g * chunk + len(grp)] = self._tot_part[1:1 + len(grp)]
         return self._tot_out
 
     @property

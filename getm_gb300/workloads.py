@@ -324,3 +324,121 @@ def tidal_channel(nx: int = 60, ny: int = 30, nz: int = 8, dx: float = 2000.0, s
     dga = calculate_sigma(nz)
     params = dict(timestep=5.0, split_factor=10, num=1e-4, nuh=1e-4, z0=z0, scheme=5)
     return Workload("tidal_channel", T, dga, {}, params)
+
+
+def _fractal(rng, ny, nx, slope=1.5):
+    """Field with a power-law amplitude spectrum k^-slope and random phases
+    (spectral synthesis), scaled to [0, 1]."""
+    ky = np.fft.fftfreq(ny)[:, None]
+    kx = np.fft.rfftfreq(nx)[None, :]
+    k = np.sqrt(kx**2 + ky**2)
+    k[0, 0] = np.inf
+    amp = k ** (-slope)
+    spec = amp * np.exp(2j * np.pi * rng.uniform(size=amp.shape))
+    return _norm01(np.fft.irfft2(spec, s=(ny, nx)))
+
+
+def _water_runs(line):
+    """(start, stop) of the runs of True in a 1D boolean array."""
+    runs, start = [], None
+    for n, w in enumerate(line):
+        if w and start is None:
+            start = n
+        elif not w and start is not None:
+            runs.append((start, n))
+            start = None
+    if start is not None:
+        runs.append((start, len(line)))
+    return runs
+
+
+def shelf_sea(nx: int = 1000, ny: int = 800, nz: int = 30, dx: float = 1500.0, seed: int = 3,
+              ntracer: int = 20, umax: float = 1.2, tide: float = 1.0) -> Workload:
+    """The many-tracer shelf sea (1000 x 800 x 30 by default, dx 1.5 km):
+    fractal bathymetry (amplitude spectrum k^-1.5) mapped to 5-200 m, land
+    where a smoothed random field exceeds its 65th percentile (~35 %), open
+    boundaries on every water run of the west edge (Flather elevation with an
+    M2 tide of ``tide`` metres; tracers zero gradient) and of the south edge
+    (clamped elevation, the tide lagged 60 degrees; tracers sponge).  The
+    initial depth-integrated flow comes from a streamfunction of 8 seeded
+    Fourier modes on X points (zero on land, so the discrete flow is
+    non-divergent with no flow through the coast), scaled to a largest speed
+    of ``umax`` m/s.  ``params['tracers']`` holds the ``ntracer`` initial
+    passive-tracer fields, log-uniform in [1e-3, 10] (smoothed)."""
+    from .open_boundaries import CLAMPED, FLATHER_ELEV, SPONGE, ZERO_GRADIENT
+
+    rng = np.random.default_rng(seed)
+    H = 5.0 + 195.0 * _fractal(rng, ny, nx)
+    q = gaussian_filter(rng.standard_normal((ny, nx)), sigma=8)
+    mask = (q <= np.quantile(q, 0.65)).astype(int)
+    x = dx * (np.arange(nx) + 0.5)
+    y = dx * (np.arange(ny) + 0.5)
+    kappa, cd = 0.4, 2.5e-3
+    z0 = 0.5 * 50.0 / (np.exp(kappa / np.sqrt(cd)) - 1.0)
+    dom = create_cartesian(x, y, mask=mask, H=H, f=1.2e-4, z0=z0)
+    ob = dom.open_boundaries
+    for n, (s, e) in enumerate(_water_runs(mask[:, 0] == 1)):
+        ob.add_left_boundary(f"W{n}", 0, s, e, FLATHER_ELEV, ZERO_GRADIENT)
+    for n, (s, e) in enumerate(_water_runs(mask[0, 1:] == 1)):
+        ob.add_bottom_boundary(f"S{n}", 0, s + 1, e + 1, CLAMPED, SPONGE)
+    T = dom.create_grids(nz, halox=2, haloy=2, velocity_grids=2)
+    omega = 2.0 * np.pi / M2_PERIOD
+    phase = np.zeros(ob.np)
+    for b in ob:
+        if b.name.startswith("S"):
+            phase[b.start:b.stop] = -np.pi / 3
+    ob.set_tide(omega, tide, phase)
+    # streamfunction on X points (ny_+1, nx_+1): 8 Fourier modes, zero at X
+    # points that touch land (X mask 0)
+    X = T.xgrid
+    xs = np.where(X.mask != 0, X.x, 0.0)
+    ys = np.where(X.mask != 0, X.y, 0.0)
+    psi = np.zeros(X.mask.shape)
+    Lx, Ly = nx * dx, ny * dx
+    for _ in range(8):
+        kx = 2 * np.pi * rng.integers(1, 6) / Lx
+        ky = 2 * np.pi * rng.integers(1, 6) / Ly
+        psi += rng.uniform(0.5, 1.0) * np.sin(kx * xs + ky * ys + rng.uniform(0, 2 * np.pi))
+    psi[X.mask == 0] = 0.0
+    U = np.zeros((T.ny_, T.nx_))
+    V = np.zeros((T.ny_, T.nx_))
+    # U(j, i) between X(j, i+1) [south] and X(j+1, i+1) [north]; V(j, i)
+    # between X(j+1, i) [west] and X(j+1, i+1) [east]
+    U[:, :] = -(psi[1:, 1:] - psi[:-1, 1:])
+    V[:, :] = psi[1:, 1:] - psi[1:, :-1]
+    U[T.ugrid.mask != 1] = 0.0
+    V[T.vgrid.mask != 1] = 0.0
+    speed = max(np.abs(U[T.ugrid.mask == 1] / T.ugrid.H[T.ugrid.mask == 1]).max(),
+                np.abs(V[T.vgrid.mask == 1] / T.vgrid.H[T.vgrid.mask == 1]).max())
+    U *= umax / speed
+    V *= umax / speed
+    tracers = []
+    for _ in range(ntracer):
+        f = 10.0 ** (-3.0 + 4.0 * _norm01(gaussian_filter(rng.uniform(size=(T.ny_, T.nx_)), sigma=4)))
+        tracers.append(f)
+    dga = calculate_sigma(nz)
+    params = dict(timestep=10.0, split_factor=6, num=1e-4, nuh=1e-4, z0=z0, scheme=5, U=U, V=V, tracers=tracers)
+    return Workload(f"shelf_sea {nx}x{ny}x{nz}", T, dga, {}, params)
+
+
+def start_shelf_sea(wl: Workload, precision: str = "mixed", device="cuda"):
+    """A BAROTROPIC_3D simulation of ``shelf_sea`` with its passive tracers,
+    initial flow (uniform over depth) and tide, started."""
+    import torch
+
+    from .simulation import RunType, Simulation
+
+    p = wl.params
+    sim = Simulation(wl.T, wl.dga, runtype=RunType.BAROTROPIC_3D, num=p["num"], nuh=p["nuh"], precision=precision,
+                     device=device)
+    trs = [sim.tracers.add(f"tracer{n:02d}") for n in range(len(p["tracers"]))]
+    for tr, f in zip(trs, p["tracers"]):
+        tr.all_values.copy_(torch.from_numpy(np.broadcast_to(f, tr.all_values.shape).copy()))
+    m = sim.momentum
+    for tp2, tp3, g in ((m.U, m.pk, sim.U), (m.V, m.qk, sim.V)):
+        src = torch.from_numpy(p["U"] if tp2 is m.U else p["V"]).to(tp2.all_values)
+        tp2.all_values.copy_(src)
+        frac = torch.where(g.D.all_values > 0, g.hn.all_values / g.D.all_values, torch.zeros_like(g.hn.all_values))
+        tp3.all_values.copy_((src * frac).to(tp3.all_values.dtype))
+    sim.start(p["timestep"], p["split_factor"])
+    return sim

@@ -93,6 +93,7 @@ _SIGS = {
     "getm_reconstruct_transport_change": "iiiiiiipppds",
     "getm_blumberg_mellor": "iiiiiiipppppppppps",
     "getm_shchepetkin_mcwilliams": "iiiiiiipppppppppppps",
+    "getm_shchepetkin_mcwilliams_mixed": "iiiiiiipppppppppppps",
     "getm_density_buoyancy": "ippppps",
     "getm_launch_count": "p",
     "getm_advection_apply_3d_batch_f32": "ppppippppppdpppips",

@@ -217,9 +217,10 @@ def blumberg_mellor(buoy, idpdx, idpdy):
 _P_WORK = {}
 
 
-def shchepetkin_mcwilliams(buoy, idpdx, idpdy, P_work=None):
+def shchepetkin_mcwilliams(buoy, idpdx, idpdy, P_work=None, arithmetic="float64"):
     """pyx:555-568.  ``P_work`` (optional) is the 3D pressure work array; by
-    default one per grid is kept."""
+    default one per grid is kept.  ``arithmetic="float32"`` (float64 fields)
+    evaluates the slope corrections in float (the mixed form)."""
     g = buoy.grid
     assert buoy.z == CENTERS, "buoy"
     assert idpdx.grid is g.ugrid and idpdx.z == CENTERS, "idpdx"
@@ -229,7 +230,10 @@ def shchepetkin_mcwilliams(buoy, idpdx, idpdy, P_work=None):
         if P_work is None or P_work.shape != buoy.all_values.shape:
             P_work = torch.zeros(buoy.all_values.shape, dtype=torch.float64, device=buoy.all_values.device)
             _P_WORK[id(g)] = P_work
-    call("getm_shchepetkin_mcwilliams" + _sfx(buoy.all_values, idpdx.all_values, idpdy.all_values), g.nx_, g.ny_, g.nz_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+    sfx = _sfx(buoy.all_values, idpdx.all_values, idpdy.all_values)
+    if arithmetic == "float32" and sfx == "":
+        sfx = "_mixed"
+    call("getm_shchepetkin_mcwilliams" + sfx, g.nx_, g.ny_, g.nz_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
          _p(g.mask), _p(idpdx.grid.mask), _p(idpdy.grid.mask), _p(idpdx.grid.idx), _p(idpdy.grid.idy), _p(g.hn),
          _p(g.zin), _p(g.zc), _p(buoy), _p(idpdx), _p(idpdy), P_work.data_ptr(), _s())
 

@@ -196,6 +196,123 @@ __global__ void smcw_gradient_kernel(int nx, int ny, int nz, int ilo, int ihi, i
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-form SMcW: double buoyancy, heights, pressure and gradients; the main
+// terms (column sums of b dz, pressure differences, the hydrostatic
+// correction) in FP64, the harmonic-mean slope corrections of
+// internal_pressure.F90:93-99, :143-166 in float from FP64 differences.  The
+// slopes are the divisions of the scheme, so this removes nearly all of its
+// FP64 work while keeping the large, nearly cancelling terms in FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float smcw_harm_f(float a, float b)
+{
+    const float cff = 2.f * a * b;
+    return (cff > (float)SMCW_EPS) ? cff / (a + b) : 0.f;
+}
+
+__global__ void smcw_column_mixed_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
+                                         const int* mask, const double* h, const double* zc,
+                                         const double* buoy, double* Pw)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + jlo;
+    if (i < ilo || i > ihi + 1 || j > jhi + 1) return;
+    const long long P = (long long)nx * ny;
+    const long long p = (long long)j * nx + i;
+    if (mask[p] <= 0) return;
+    const float x = 1.f / 12.f;
+#define B(k) buoy[p + (long long)((k) - 1) * P]
+#define Z(k) zc[p + (long long)((k) - 1) * P]
+    double cff = 0.0;
+    if (nz > 1) cff = 0.5 * (B(nz) - B(nz - 1)) * 0.5 * h[p + (long long)(nz - 1) * P] / (Z(nz) - Z(nz - 1));
+    double Pk = (B(nz) + cff) * 0.5 * h[p + (long long)(nz - 1) * P];
+    Pw[p + (long long)(nz - 1) * P] = Pk;
+    if (nz == 1) return;
+    double bk1 = B(nz), zk1 = Z(nz);
+    double bk = B(nz - 1), zk = Z(nz - 1);
+    float dRk = getm_d2f_approx(bk1 - bk), dZk = getm_d2f_approx(zk1 - zk);
+    float HR1 = smcw_harm_f(dRk, dRk);
+    float HZ1 = 2.f * dZk * dZk / (dZk + dZk);
+    for (int k = nz - 1; k >= 1; k--) {
+        float dRm, dZm;
+        double bkm1 = 0.0, zkm1 = 0.0;
+        if (k > 1) {
+            bkm1 = B(k - 1); zkm1 = Z(k - 1);
+            dRm = getm_d2f_approx(bk - bkm1); dZm = getm_d2f_approx(zk - zkm1);
+        } else {
+            dRm = dRk; dZm = dZk;
+        }
+        const float HR0 = smcw_harm_f(dRk, dRm);
+        const float HZ0 = 2.f * dZk * dZm / (dZk + dZm);
+        const float corr = 0.2f * ((HR1 - HR0) * (dZk - x * (HZ1 + HZ0)) - (HZ1 - HZ0) * (dRk - x * (HR1 + HR0)));
+        Pk = Pk + 0.5 * ((bk1 + bk) * (zk1 - zk) - getm_f2d(corr));
+        Pw[p + (long long)(k - 1) * P] = Pk;
+        HR1 = HR0; HZ1 = HZ0;
+        bk1 = bk; zk1 = zk; bk = bkm1; zk = zkm1;
+        dRk = dRm; dZk = dZm;
+    }
+#undef B
+#undef Z
+}
+
+__global__ void smcw_gradient_mixed_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
+                                           const int* umask, const int* vmask, const double* idxu,
+                                           const double* idyv, const double* h, const double* z,
+                                           const double* zc, const double* buoy, const double* Pw,
+                                           double* idpdx, double* idpdy)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y + jlo;
+    int k = blockIdx.z;
+    if (i < ilo || i > ihi || j > jhi) return;
+    const long long P = (long long)nx * ny;
+    const long long p = (long long)j * nx + i;
+    const long long q = p + (long long)k * P;
+    const long long qtop = p + (long long)(nz - 1) * P;
+    const float x = 1.f / 12.f;
+    for (int dir = 0; dir < 2; dir++) {
+        const int* m = dir ? vmask : umask;
+        if (m[p] != 1) continue;
+        const long long s = dir ? nx : 1;
+        float rZ0 = 0.f, rR0 = 0.f, rZ1 = 0.f, rR1 = 0.f, rZ2 = 0.f, rR2 = 0.f;
+        if (m[p - s] > 0) { rZ0 = getm_d2f_approx(zc[q] - zc[q - s]); rR0 = getm_d2f_approx(buoy[q] - buoy[q - s]); }
+        const double dzc = zc[q + s] - zc[q];
+        const double dbq = buoy[q + s] - buoy[q];
+        if (m[p] > 0) { rZ1 = getm_d2f_approx(dzc); rR1 = getm_d2f_approx(dbq); }
+        if (m[p + s] > 0) { rZ2 = getm_d2f_approx(zc[q + 2 * s] - zc[q + s]); rR2 = getm_d2f_approx(buoy[q + 2 * s] - buoy[q + s]); }
+        const float dZx0 = smcw_harm_f(rZ0, rZ1), dZx1 = smcw_harm_f(rZ1, rZ2);
+        const float dRx0 = smcw_harm_f(rR0, rR1), dRx1 = smcw_harm_f(rR1, rR2);
+        const float corr = 0.2f * ((dRx1 - dRx0) * (getm_d2f_approx(dzc) - x * (dZx1 + dZx0)) -
+                                   (dZx1 - dZx0) * (getm_d2f_approx(dbq) - x * (dRx1 + dRx0)));
+        const double FC = 0.5 * ((buoy[q + s] + buoy[q]) * dzc - getm_f2d(corr));
+        const double id = dir ? idyv[p] : idxu[p];
+        double* out = dir ? idpdy : idpdx;
+        out[q] = 0.5 * (h[q] + h[q + s]) * id
+                 * ((Pw[q + s] - Pw[q]) + FC - (z[p + s] - z[p]) * 0.5 * (buoy[qtop + s] + buoy[qtop]));
+    }
+}
+
+extern "C" int getm_shchepetkin_mcwilliams_mixed(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                                 const int* mask, const int* umask, const int* vmask,
+                                                 const double* idxu, const double* idyv, const double* h,
+                                                 const double* z, const double* zc, const double* buoy,
+                                                 double* idpdx, double* idpdy, double* P_work,
+                                                 cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax + 2 > nx || jmax + 2 > ny || jmax < jmin) return GETM_ERR_ARG;
+    if (!mask || !umask || !vmask || !idxu || !idyv || !h || !z || !zc || !buoy || !idpdx || !idpdy || !P_work)
+        return GETM_ERR_ARG;
+    dim3 g1(getm_div_up(nx, 128), jmax - jmin + 2);
+    smcw_column_mixed_kernel<<<g1, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, h, zc,
+                                                     buoy, P_work);
+    GETM_CHECK_LAUNCH();
+    dim3 g2(getm_div_up(nx, 128), jmax - jmin + 1, nz);
+    smcw_gradient_mixed_kernel<<<g2, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask,
+                                                       idxu, idyv, h, z, zc, buoy, P_work, idpdx, idpdy);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
 template <typename T>
 static int smcw_impl(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* mask,
                      const int* umask, const int* vmask, const double* idxu, const double* idyv, const double* h,

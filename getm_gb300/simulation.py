@@ -104,7 +104,8 @@ class Simulation:
         3D velocities and their tendencies and diffusivities; float64
         elevations, depths, layer thicknesses, 2D transports and their
         accumulation, density, buoyancy, internal pressure and the budget
-        sums of ``totals``)."""
+        sums of ``totals``; increments, tendencies, limiters, drag and the
+        internal-pressure slope corrections are evaluated in float)."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
@@ -306,7 +307,8 @@ class Simulation:
         if self.internal_pressure_method == "blumberg_mellor":
             _pygetm.blumberg_mellor(self.buoy, self.idpdx, self.idpdy)
         else:
-            _pygetm.shchepetkin_mcwilliams(self.buoy, self.idpdx, self.idpdy, self._P_work)
+            _pygetm.shchepetkin_mcwilliams(self.buoy, self.idpdx, self.idpdy, self._P_work,
+                                           "float32" if self.precision == "mixed" else "float64")
 
     def totals_device(self) -> torch.Tensor:
         """Device tensor [total volume, total of each tracer] (compensated

@@ -349,6 +349,17 @@ int getm_bottom_friction_mixed(int nx, int ny, const int* mask, const double* u,
                                const double* D, double* z0b, const double* z0b_in, double avmmol,
                                double* ru, int iterate, cudaStream_t stream);
 
+/* Shchepetkin-McWilliams internal pressure (internal_pressure.F90:63-217)
+ * for the mixed form: same arguments and storage as the FP64 entry point;
+ * the column sums of b dz, the pressure differences and the hydrostatic
+ * correction in FP64, the harmonic-mean slope corrections in float from
+ * FP64 differences.                                                        */
+int getm_shchepetkin_mcwilliams_mixed(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                      const int* mask, const int* umask, const int* vmask,
+                                      const double* idxu, const double* idyv, const double* h,
+                                      const double* z, const double* zc, const double* buoy,
+                                      double* idpdx, double* idpdy, double* P_work, cudaStream_t stream);
+
 /* 2D advection of a double field (the depth-averaged momentum of the mixed
  * form) with the same interface as getm_advection_2d (operators.py:52-93)
  * and the same storage, whose increments are evaluated in float in

@@ -75,9 +75,11 @@ _SIGS = {
     "getm_momentum_2d_velocities": "iii" + "p" * 16 + "s",
     "getm_momentum_2d_friction": "iii" + "p" * 12 + "s",
     "getm_coriolis_2d": "iiiipppis",
+    "getm_coriolis_2d_mixed": "iiiipppis",
     "getm_advance_2d_transport_mixed": "iiiippppppppppppppdps",
     "getm_accumulate_2d": "lpppps",
     "getm_surface_elevation_fused": "iiiipppppppppds",
+    "getm_split2d_substep": "piiiiiiiidddppppippppis",
     "getm_open_boundary_elevation": "iiipppppppppppppdps",
     "getm_open_boundary_tracers": "iiiiiiippppppipps",
     "getm_open_boundary_tracers_f32": "iiiiiiippppppipps",

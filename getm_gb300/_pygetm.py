@@ -280,8 +280,9 @@ def momentum_2d_friction(u1, v1, ru, rv, mixed=False):
          _p(ug.D), _p(vg.D), _p(ug.z0b), _p(vg.z0b), _p(ug._work), _p(vg._work), _p(ru), _p(rv), _s())
 
 
-def coriolis_2d(U, out, x_direction):
-    """Momentum.coriolis, DEFAULT scheme, for 2D transports (momentum.py:1127-1148)."""
+def coriolis_2d(U, out, x_direction, mixed=False):
+    """Momentum.coriolis, DEFAULT scheme, for 2D transports (momentum.py:1127-1148);
+    ``mixed``: in float arithmetic."""
     a, b = U.grid, out.grid
     if a.ioffset == b.ioffset + 1 and a.joffset == b.joffset - 1:
         io, jo = 1, 0
@@ -289,7 +290,8 @@ def coriolis_2d(U, out, x_direction):
         io, jo = 0, 1
     else:
         raise NotImplementedError("coriolis_2d expects U -> V or V -> U")
-    call("getm_coriolis_2d", b.nx_, b.ny_, io, jo, _p(U), _p(b.cor), _p(out), int(bool(x_direction)), _s())
+    call("getm_coriolis_2d_mixed" if mixed else "getm_coriolis_2d", b.nx_, b.ny_, io, jo, _p(U), _p(b.cor), _p(out),
+         int(bool(x_direction)), _s())
 
 
 def accumulate_2d(U, V, Ucum, Vcum):
@@ -302,3 +304,45 @@ def surface_elevation_fused(timestep, z, zo, U, V, fwf):
     g = z.grid
     call("getm_surface_elevation_fused", g.nx_, g.ny_, g.halox, g.haloy, _p(g.mask), _p(U.grid.dy), _p(V.grid.dx),
          _p(g.iarea), _p(z), _p(zo), _p(U), _p(V), _p(fwf), float(timestep), _s())
+
+
+# ---- one 2D substep as one launch -----------------------------------------
+# field order of getm_split2d_fields (include/getm_gb300.h); every member is
+# a device pointer
+SPLIT2D_FIELDS = (
+    "mask_t", "H_t", "iarea_t", "z", "zo", "D_t", "Dclip_t", "work_t", "fwf", "pe", "sp", "taux", "tauy",
+    "mask_u", "H_u", "dy_u", "idx_u", "cor_u", "z0b_u", "D_u", "alpha_u", "work_u",
+    "U", "dpdx", "tausx", "corU", "advU", "diffU", "dampU", "SxA", "SxB", "SxD", "SxF",
+    "ru", "u1", "Ucum", "advD_u", "uua", "uva",
+    "mask_v", "H_v", "dx_v", "idy_v", "cor_v", "z0b_v", "D_v", "alpha_v", "work_v",
+    "V", "dpdy", "tausy", "corV", "advV", "diffV", "dampV", "SyA", "SyB", "SyD", "SyF",
+    "rv", "v1", "Vcum", "advD_v", "vua", "vva",
+    "mask_x", "H_x", "D_x", "work_x", "D_uu", "D_uv", "D_vu", "D_vv", "time", "sync",
+)
+
+
+class Split2DFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in SPLIT2D_FIELDS]
+
+
+def split2d_fields(**arrays) -> Split2DFields:
+    """The fields struct from Arrays or tensors (every name of SPLIT2D_FIELDS;
+    ``time`` may be None)."""
+    missing = set(SPLIT2D_FIELDS) - set(arrays) - {"time"}
+    if missing:
+        raise ValueError(f"split2d_fields: missing {sorted(missing)}")
+    f = Split2DFields()
+    for n in SPLIT2D_FIELDS:
+        a = arrays.get(n)
+        setattr(f, n, None if a is None else (a.data_ptr() if isinstance(a, torch.Tensor) else _p(a)))
+    return f
+
+
+def split2d_substep(fields: Split2DFields, T, mixed, ufirst, accumulate, friction, timestep, Dmin, Dcrit, uadv, vadv):
+    """One non-macro 2D substep (simulation.py:1033-1304 with update_3d
+    false) as one launch; ``uadv``/``vadv``: the momentum Advection objects."""
+    U, V = T.ugrid, T.vgrid
+    call("getm_split2d_substep", ctypes.byref(fields), T.nx_, T.ny_, T.halox, T.haloy, int(bool(mixed)),
+         int(bool(ufirst)), int(bool(accumulate)), int(bool(friction)), float(timestep), float(Dmin), float(Dcrit),
+         uadv.p, U.handle, U.ugrid.handle, U.vgrid.handle, int(uadv.ufirst),
+         vadv.p, V.handle, V.ugrid.handle, V.vgrid.handle, int(vadv.ufirst), _s())

@@ -1,0 +1,447 @@
+// Horizontal advection passes as device functions (shared by the one-pass
+// kernels of advection.cu and the fused 2D-substep kernel of split2d.cu).
+// Reference: src/operators/advection_schemes/advection.F90.template
+// (u2d :23-121, v2d :123-221) and limiters.h.
+#pragma once
+
+#include "getm_common.cuh"
+
+#define GETM_MAX_BATCH 32
+#define GETM_V_BY 16
+
+// ---------------------------------------------------------------------------
+// horizontal pass kernels
+// ---------------------------------------------------------------------------
+// T is the type of the advected fields and of the velocities: double for the
+// FP64 form, float for the mixed form.  Layer thicknesses, the transports QU
+// that update them and all grid metrics are double in both forms.  For
+// T = double every expression below is the FP64 reference arithmetic.
+template <typename T>
+struct HPassArgs {
+    int nx_, ny_, nk;
+    long long plane;            // nx_ * ny_
+    int ilo, ihi, jlo, jhi;     // C interior bounds (inclusive) of the T grid
+    const int* umask;           // mask of the velocity grid of this direction
+    const double* idx;          // x: idx of U grid; y: idy of V grid (Courant number)
+    const double* dy;           // x: dy of U grid;  y: dx of V grid (face length)
+    const int* tmask;
+    const double* iA;
+    const double* Ah;           // 2D horizontal diffusivity on the velocity grid, or NULL
+    const T* u;                 // velocity (nk layers)
+    const double* hu;           // layer thickness on the velocity grid (nk layers)
+    const double* h_in;
+    double* h_out;
+    double dt;
+    int scheme;
+    int ntracer;
+    // mixed form: float copies of dt and of the metrics above; increment != 0
+    // selects the increment-form kernels for double fields (2D momentum)
+    int increment;
+    float dtf;
+    const float* idx_f;
+    const float* dy_f;
+    const float* iA_f;
+    const T* fin[GETM_MAX_BATCH];
+    T* fout[GETM_MAX_BATCH];
+};
+
+template <typename T>
+struct FaceGeom {
+    double QU;
+    T cfl;
+    bool active, up, uu_ok;
+};
+
+// Face quantities that do not depend on the advected field
+// (template :63-65, :70, :77).
+template <typename T>
+__device__ __forceinline__ FaceGeom<T> face_geom(const HPassArgs<T>& a, long long p2, long long p3,
+                                                 long long s, bool in_range)
+{
+    FaceGeom<T> g;
+    g.QU = 0.0; g.cfl = T(0); g.active = false; g.up = false; g.uu_ok = false;
+    if (!in_range) return g;
+    int m = a.umask[p2];
+    if (!getm_flux_point(m)) return g;
+    T uu = a.u[p3];
+    g.active = true;
+    g.QU = (double)uu * a.hu[p3] * a.dy[p2];
+    g.cfl = fabs(uu * (T)a.dt * (T)a.idx[p2]);
+    g.up = uu > T(0);
+    g.uu_ok = getm_flux_point(g.up ? a.umask[p2 - s] : a.umask[p2 + s]);
+    return g;
+}
+
+// Tracer flux through one face (template :66-104).
+template <typename T>
+__device__ __forceinline__ T face_flux(const HPassArgs<T>& a, const FaceGeom<T>& g, const T* __restrict__ f,
+                                       long long p2, long long p3, long long s)
+{
+    if (!g.active) return T(0);
+    T fu, fuu, fd;
+    if (g.up) {
+        fu = f[p3];
+        fuu = g.uu_ok ? f[p3 - s] : fu;
+        fd = f[p3 + s];
+    } else {
+        fu = f[p3 + s];
+        fuu = g.uu_ok ? f[p3 + 2 * s] : fu;
+        fd = f[p3];
+    }
+    fu = getm_tvd_face<T>(a.scheme, fuu, fu, fd, g.cfl);
+    T flux = (T)g.QU * fu;
+    if (a.Ah) flux = flux - (T)a.Ah[p2] * (T)a.hu[p3] * (f[p3 + s] - f[p3]) * (T)a.idx[p2] * (T)a.dy[p2];
+    return flux;
+}
+
+// x-direction pass.  blockDim = (32, BYX); grid = (ceil(nx_/32), ceil(ny_*nk/BYX)).
+template <typename T>
+__device__ __forceinline__ void hpass_x_body(const HPassArgs<T>& a, int bx, long long row, int lane)
+{
+    const int i = bx * 32 + lane;
+    if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
+    const int k = (int)(row / a.ny_);
+    const int j = (int)(row - (long long)k * a.ny_);
+    const bool inx = i < a.nx_;
+    const long long p2 = (long long)j * a.nx_ + i;
+    const long long p3 = (long long)k * a.plane + p2;
+    const bool jrow = j >= a.jlo && j <= a.jhi;
+
+    FaceGeom<T> gr = face_geom(a, p2, p3, 1, inx && jrow && i >= a.ilo - 1 && i <= a.ihi);
+    FaceGeom<T> gl = face_geom(a, p2 - 1, p3 - 1, 1, lane == 0 && jrow && i - 1 >= a.ilo - 1 && i - 1 <= a.ihi);
+    double QUl = __shfl_up_sync(0xffffffffu, gr.QU, 1);
+    if (lane == 0) QUl = gl.QU;
+    const bool upd = inx && jrow && i >= a.ilo && i <= a.ihi && a.tmask[p2] == 1;
+
+    double hold = 0.0, hnew = 0.0, iA = 0.0;
+    if (inx) {
+        hold = a.h_in[p3];
+        hnew = hold;
+        if (upd) {
+            iA = a.iA[p2];
+            hnew = hold - a.dt * (gr.QU - QUl) * iA;
+        }
+        a.h_out[p3] = hnew;
+    }
+    for (int t = 0; t < a.ntracer; t++) {
+        const T* __restrict__ f = a.fin[t];
+        T fr = inx ? face_flux(a, gr, f, p2, p3, 1) : T(0);
+        T fl = __shfl_up_sync(0xffffffffu, fr, 1);
+        if (lane == 0) fl = face_flux(a, gl, f, p2 - 1, p3 - 1, 1);
+        if (inx) {
+            T fo = f[p3];
+            T fn = fo;
+            if (upd) {
+                T hfo = (T)hold * fo;
+                T advn = (fr - fl) * (T)iA;
+                fn = (hfo - (T)a.dt * advn) / (T)hnew;
+            }
+            a.fout[t][p3] = fn;
+        }
+    }
+}
+
+// y-direction pass.  blockDim = (32, GETM_V_BY); grid = (ceil(nx_/32), ceil(ny_/BY), nk).
+template <typename T>
+__device__ __forceinline__ void hpass_y_body(const HPassArgs<T>& a, int bx, int by, int k, int tx, int ty,
+                                             double (&sQ)[GETM_V_BY][32], T (&sF)[GETM_V_BY][32])
+{
+    const int i = bx * 32 + tx;
+    const int j = by * GETM_V_BY + ty;
+    const bool in = i < a.nx_ && j < a.ny_;
+    const long long s = a.nx_;
+    const long long p2 = (long long)j * a.nx_ + i;
+    const long long p3 = (long long)k * a.plane + p2;
+    const bool icol = i >= a.ilo && i <= a.ihi;
+
+    FaceGeom<T> gt = face_geom(a, p2, p3, s, in && icol && j >= a.jlo - 1 && j <= a.jhi);
+    FaceGeom<T> gb = face_geom(a, p2 - s, p3 - s, s, in && ty == 0 && icol && j - 1 >= a.jlo - 1 && j - 1 <= a.jhi);
+    sQ[ty][tx] = gt.QU;
+    __syncthreads();
+    double QUb = ty > 0 ? sQ[ty - 1][tx] : gb.QU;
+    const bool upd = in && icol && j >= a.jlo && j <= a.jhi && a.tmask[p2] == 1;
+
+    double hold = 0.0, hnew = 0.0, iA = 0.0;
+    if (in) {
+        hold = a.h_in[p3];
+        hnew = hold;
+        if (upd) {
+            iA = a.iA[p2];
+            hnew = hold - a.dt * (gt.QU - QUb) * iA;
+        }
+        a.h_out[p3] = hnew;
+    }
+    for (int t = 0; t < a.ntracer; t++) {
+        const T* __restrict__ f = a.fin[t];
+        T ft = in ? face_flux(a, gt, f, p2, p3, s) : T(0);
+        T fb = (ty == 0 && in) ? face_flux(a, gb, f, p2 - s, p3 - s, s) : T(0);
+        __syncthreads();  // previous tracer's reads of sF are done
+        sF[ty][tx] = ft;
+        __syncthreads();
+        if (ty > 0) fb = sF[ty - 1][tx];
+        if (in) {
+            T fo = f[p3];
+            T fn = fo;
+            if (upd) {
+                T hfo = (T)hold * fo;
+                T advn = (ft - fb) * (T)iA;
+                fn = (hfo - (T)a.dt * advn) / (T)hnew;
+            }
+            a.fout[t][p3] = fn;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed form (float fields): increment form of the same passes.
+//
+// With hold - hnew = dt iA (QU_e - QU_w), the reference update
+// (hold f - dt iA (QU_e f_e - QU_w f_w)) / hnew equals
+//     f - dt iA (QU_e (f_e - f) - QU_w (f_w - f)) / hnew
+// exactly, where f_e, f_w are the limited face values.  Each face therefore
+// provides QU (face - left cell) and QU (face - right cell), formed from
+// differences of neighbouring values, so float32 rounding scales with the
+// change of the field, a field at rest is reproduced exactly, and the only
+// FP64 operations per cell are the thickness update hnew = hold - dh.
+// ---------------------------------------------------------------------------
+// Storage type S of the advected field and of the velocities: float (the 3D
+// fields of the mixed form) or double (the 2D depth-averaged momentum of the
+// mixed form, whose state stays FP64 while its increments are evaluated in
+// float).  Differences of neighbouring values are formed in S and then
+// narrowed, so they keep their accuracy when the values are close.
+template <typename S>
+__device__ __forceinline__ float inc_f(S x)
+{
+    if constexpr (std::is_same<S, double>::value) return getm_d2f_approx(x);
+    else return x;
+}
+
+template <typename S>
+__device__ __forceinline__ S inc_add(S x, float dx)
+{
+    if constexpr (std::is_same<S, double>::value) return x + getm_f2d(dx);
+    else return x + dx;
+}
+
+// Limited face deviation from the upwind cell, given d = f[b] - f[a] across
+// the face and the differences on either side, dprev = f[a] - f[a-1] and
+// dnext = f[b+1] - f[b].
+__device__ __forceinline__ float hx_dev(int scheme, bool up, bool uu_ok, float dprev, float d, float dnext,
+                                        float cfl)
+{
+    return up ? getm_tvd_dev_d<float>(scheme, d, uu_ok ? dprev : 0.f, cfl)
+              : getm_tvd_dev_d<float>(scheme, -d, uu_ok ? -dnext : 0.f, cfl);
+}
+
+// x-direction pass in increment form.  A warp owns one row segment: lane L
+// computes the face at U point a = i0 - 1 + L (between cells a and a+1) and,
+// for L < 31, updates cell a + 1, whose east face comes from lane L + 1 by a
+// shuffle; segments therefore advance by 31 cells.  Every lane runs the same
+// instructions (no per-lane special paths): each field is read with one
+// coalesced load per warp plus one load of the three values just outside
+// the segment (lanes 0-2), and all loads of a lane are independent.
+constexpr int HX_STRIDE = 31;
+
+template <typename S>
+__device__ __forceinline__ void hpass_x_inc_body(const HPassArgs<S>& a, int bx, long long row, int lane)
+{
+    constexpr unsigned FULL = 0xffffffffu;
+    const int i0 = bx * HX_STRIDE;
+    const int ia = i0 - 1 + lane;  // this lane's face (U point) and its west cell
+    const int ib = ia + 1;         // the cell this lane updates (lanes 0-30)
+    if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
+    const int k = (int)(row / a.ny_);
+    const int j = (int)(row - (long long)k * a.ny_);
+    const long long r2 = (long long)j * a.nx_;
+    const long long r3 = (long long)k * a.plane + r2;
+    const bool jrow = j >= a.jlo && j <= a.jhi;
+    const bool ain = ia >= 0 && ia < a.nx_;
+    // lanes 0-2 address the points i0-2, i0+31, i0+32 just outside the lanes' range
+    const int ix = lane == 0 ? i0 - 2 : i0 + 30 + lane;
+    const bool xin = lane < 3 && ix >= 0 && ix < a.nx_;
+
+    // face geometry
+    const bool f_in = ain && jrow && ia >= a.ilo - 1 && ia <= a.ihi;
+    const int um = ain ? a.umask[r2 + ia] : 0;
+    const int umx = xin ? a.umask[r2 + ix] : 0;
+    int um_w = __shfl_up_sync(FULL, um, 1), um_e = __shfl_down_sync(FULL, um, 1);
+    const int umx0 = __shfl_sync(FULL, umx, 0), umx1 = __shfl_sync(FULL, umx, 1);
+    if (lane == 0) um_w = umx0;
+    if (lane == 31) um_e = umx1;
+    float QU = 0.f, cfl = 0.f, ahd = 0.f;
+    bool up = false, uu_ok = false;
+    const bool act = f_in && getm_flux_point(um);
+    if (act) {
+        const float uu = inc_f<S>(a.u[r3 + ia]);
+        const float huf = getm_d2f_approx(a.hu[r3 + ia]);
+        const float dyf = a.dy_f[r2 + ia], idxf = a.idx_f[r2 + ia];
+        QU = uu * huf * dyf;
+        cfl = fabsf(uu * a.dtf * idxf);
+        up = uu > 0.f;
+        uu_ok = getm_flux_point(up ? um_w : um_e);
+        if (a.Ah) ahd = -getm_d2f_approx(a.Ah[r2 + ia]) * huf * idxf * dyf;
+    }
+    const float QUe = __shfl_down_sync(FULL, QU, 1);  // east face of cell ib
+
+    // thickness update of cell ib
+    const bool bin = lane < HX_STRIDE && ib < a.nx_;
+    const bool upd = bin && jrow && ib >= a.ilo && ib <= a.ihi && a.tmask[r2 + ib] == 1;
+    float coef = 0.f;  // dt iA / hnew
+    if (bin) {
+        const double hold = a.h_in[r3 + ib];
+        double hnew = hold;
+        if (upd) {
+            const float iaf = a.iA_f[r2 + ib];
+            const float dh = a.dtf * (QUe - QU) * iaf;
+            hnew = hold - getm_f2d(dh);
+            coef = a.dtf * iaf / (getm_d2f_approx(hold) - dh);
+        }
+        a.h_out[r3 + ib] = hnew;
+    }
+    for (int t = 0; t < a.ntracer; t++) {
+        const S* __restrict__ f = a.fin[t] + r3;
+        const S fa = ain ? f[ia] : S(0);
+        const S fx = xin ? f[ix] : S(0);
+        S fb = __shfl_down_sync(FULL, fa, 1);  // f[ia+1]
+        const S x0 = __shfl_sync(FULL, fx, 0), x1 = __shfl_sync(FULL, fx, 1), x2 = __shfl_sync(FULL, fx, 2);
+        if (lane == 31) fb = x1;
+        const float d = inc_f<S>(fb - fa);
+        float dprev = __shfl_up_sync(FULL, d, 1), dnext = __shfl_down_sync(FULL, d, 1);
+        // the two differences the shuffles cannot supply, in one operation
+        const float e = inc_f<S>(lane == 0 ? fa - x0 : x2 - x1);
+        if (lane == 0) dprev = e;
+        if (lane == 31) dnext = e;
+        // el = QU (face - f[ia]) (east side of cell ia), er = QU (face - f[ib])
+        float el = 0.f, er = 0.f;
+        if (act) {
+            const float dev = hx_dev(a.scheme, up, uu_ok, dprev, d, dnext, cfl);
+            const float fd = ahd * d;
+            el = QU * (up ? dev : d + dev) + fd;
+            er = QU * (up ? dev - d : dev) + fd;
+        }
+        const float el_e = __shfl_down_sync(FULL, el, 1);  // east face of cell ib, seen from ib
+        if (bin) a.fout[t][r3 + ib] = upd ? inc_add<S>(fb, -coef * (el_e - er)) : fb;
+    }
+}
+
+// y-direction pass in increment form: the transpose of hpass_x_inc_kernel.
+// A block of 32 x HY_BY threads covers 32 columns; thread row ty computes the
+// face at V point ja = j0 - 1 + ty and, for ty < HY_BY - 1, updates cell
+// ja + 1, whose north face comes from thread row ty + 1 through shared
+// memory; blocks therefore advance by HY_BY - 1 rows.  The rows of each
+// tracer a block needs are staged in shared memory once (one coalesced load
+// per row), so every value is read from global memory once per block.
+constexpr int HY_BY = 16;
+constexpr int HY_STRIDE = HY_BY - 1;
+
+template <typename S>
+struct YIncSmem {
+    S sf[HY_BY + 3][32];       // rows j0-2 .. j0+HY_BY
+    float sd[HY_BY + 2][32];   // differences f[j+1] - f[j], rows j0-2 .. j0+HY_BY-1
+    float sx[HY_BY][32];       // per-face exchange (QU, then el)
+};
+
+template <typename S>
+__device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, int by, int k, int tx, int ty,
+                                                 YIncSmem<S>& sm)
+{
+    auto& sf = sm.sf;
+    auto& sd = sm.sd;
+    auto& sx = sm.sx;
+    const int i = bx * 32 + tx;
+    const int j0 = by * HY_STRIDE;
+    const int ja = j0 - 1 + ty;  // this thread's face (V point) and its south cell
+    const int jb = ja + 1;       // the cell this thread updates (ty < HY_STRIDE)
+    const long long s = a.nx_;
+    const long long base = (long long)k * a.plane + i;  // + j * s
+    const bool icol = i < a.nx_;
+    const bool ain = icol && ja >= 0 && ja < a.ny_;
+    const bool iint = i >= a.ilo && i <= a.ihi;
+
+    // face geometry
+    const bool f_in = ain && iint && ja >= a.jlo - 1 && ja <= a.jhi;
+    float QU = 0.f, cfl = 0.f, ahd = 0.f;
+    bool up = false, uu_ok = false, act = false;
+    if (f_in) {
+        const long long q2 = (long long)ja * s + i;
+        act = getm_flux_point(a.umask[q2]);
+        if (act) {
+            const int m_s = ja > 0 ? a.umask[q2 - s] : 0;
+            const int m_n = ja + 1 < a.ny_ ? a.umask[q2 + s] : 0;
+            const float vv = inc_f<S>(a.u[base + ja * s]);
+            const float hvf = getm_d2f_approx(a.hu[base + ja * s]);
+            const float dxf = a.dy_f[q2], idyf = a.idx_f[q2];
+            QU = vv * hvf * dxf;
+            cfl = fabsf(vv * a.dtf * idyf);
+            up = vv > 0.f;
+            uu_ok = getm_flux_point(up ? m_s : m_n);
+            if (a.Ah) ahd = -getm_d2f_approx(a.Ah[q2]) * hvf * idyf * dxf;
+        }
+    }
+    sx[ty][tx] = QU;
+    __syncthreads();
+    const float QUn = ty + 1 < HY_BY ? sx[ty + 1][tx] : 0.f;  // north face of cell jb
+
+    const bool bin = ty < HY_STRIDE && icol && jb < a.ny_;
+    const bool upd = bin && iint && jb >= a.jlo && jb <= a.jhi && a.tmask[(long long)jb * s + i] == 1;
+    float coef = 0.f;
+    if (bin) {
+        const double hold = a.h_in[base + jb * s];
+        double hnew = hold;
+        if (upd) {
+            const float iaf = a.iA_f[(long long)jb * s + i];
+            const float dh = a.dtf * (QUn - QU) * iaf;
+            hnew = hold - getm_f2d(dh);
+            coef = a.dtf * iaf / (getm_d2f_approx(hold) - dh);
+        }
+        a.h_out[base + jb * s] = hnew;
+    }
+    // staging rows: thread row ty loads row ja (smem row ty + 1); rows 0-2
+    // also load rows j0-2, j0+HY_BY-1 and j0+HY_BY (smem rows 0, HY_BY+1, HY_BY+2)
+    const int jx = ty == 0 ? j0 - 2 : j0 + HY_BY - 2 + ty;
+    const int sxrow = ty == 0 ? 0 : HY_BY + ty;
+    const bool xin = ty < 3 && icol && jx >= 0 && jx < a.ny_;
+    for (int t = 0; t < a.ntracer; t++) {
+        const S* __restrict__ f = a.fin[t] + base;
+        __syncthreads();  // previous tracer's reads of sf, sd and sx are done
+        sf[ty + 1][tx] = ain ? f[ja * s] : S(0);
+        if (ty < 3) sf[sxrow][tx] = xin ? f[jx * s] : S(0);
+        __syncthreads();
+        // difference across this thread's face (smem row ty + 1 of sd); rows
+        // 0 and 1 also form the differences below and above the block's faces
+        sd[ty + 1][tx] = inc_f<S>(sf[ty + 2][tx] - sf[ty + 1][tx]);
+        if (ty == 0) sd[0][tx] = inc_f<S>(sf[1][tx] - sf[0][tx]);
+        if (ty == 1) sd[HY_BY + 1][tx] = inc_f<S>(sf[HY_BY + 2][tx] - sf[HY_BY + 1][tx]);
+        __syncthreads();
+        const float dprev = sd[ty][tx], d = sd[ty + 1][tx], dnext = sd[ty + 2][tx];
+        const S fb = sf[ty + 2][tx];
+        float el = 0.f, er = 0.f;
+        if (act) {
+            const float dev = hx_dev(a.scheme, up, uu_ok, dprev, d, dnext, cfl);
+            const float fd = ahd * d;
+            el = QU * (up ? dev : d + dev) + fd;
+            er = QU * (up ? dev - d : dev) + fd;
+        }
+        sx[ty][tx] = el;
+        __syncthreads();
+        const float el_n = ty + 1 < HY_BY ? sx[ty + 1][tx] : 0.f;
+        if (bin) a.fout[t][base + jb * s] = upd ? inc_add<S>(fb, -coef * (el_n - er)) : fb;
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// The two passes of a FULL-split 2D advection (advection_2d_impl with split
+// 1, no horizontal diffusion), set up for kernels that run them themselves:
+// first: var -> scratch, D -> scratch thickness; second: back into var and
+// D.  Implemented in advection.cu (it owns the scratch buffers).
+// ---------------------------------------------------------------------------
+struct Advection2DPasses {
+    HPassArgs<double> pass[2];
+    int dir[2];  // 1: x pass, 2: y pass
+};
+
+int getm_advection_2d_passes(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
+                             int ufirst, const double* u, const double* v, double timestep, double* D,
+                             const double* DU, const double* DV, double* var, int increment,
+                             Advection2DPasses* out);

@@ -101,6 +101,21 @@ __device__ __forceinline__ float getm_d2f_approx(double x)
     return __uint_as_float(s | ((unsigned int)e << 23) | m);
 }
 
+// num / den in FP64 to about 2^-46 relative (not correctly rounded), for the
+// mixed form: the float reciprocal of den refined by one Newton-Raphson step
+// (q0 = num r, q = q0 + r (num - q0 den)), three FP64 instructions instead of
+// a correctly rounded division.  den zero, not finite or outside the normal
+// float range: the correctly rounded division.
+__device__ __forceinline__ double getm_div_refined(double num, double den)
+{
+    const float df = getm_d2f_approx(den);
+    const float adf = fabsf(df);
+    if (!(adf > 1e-30f && adf < 1e30f)) return num / den;
+    const double r = getm_f2d(__frcp_rn(df));
+    const double q0 = num * r;
+    return fma(fma(-q0, den, num), r, q0);
+}
+
 // True for the mixed form's float bulk type.  Its update kernels use the
 // increment form x_new = x_old + dx, with dx formed from small differences,
 // so a field that does not change is reproduced exactly and float32 rounding

@@ -5,7 +5,7 @@
 // These are elementwise or single-pass column kernels; each thread owns one
 // output point (or one column for the vertical recursions), reads its inputs
 // once, and warps run along i so every access is coalesced.
-#include "getm_common.cuh"
+#include "split2d_ops.cuh"
 
 #define EW_THREADS 256
 
@@ -33,7 +33,7 @@ __global__ void interp_x_kernel(int nx, int ny, int nz, const T* s, T* t, int io
     if (p >= n) return;
     int i = (int)(p % nx);
     if (i >= nx - 1) return;
-    t[p + ioff] = T(0.5) * (s[p] + s[p + 1]);
+    interp_pair_point<T>(s, t, p, 1, ioff);
 }
 
 template <typename T>
@@ -44,7 +44,7 @@ __global__ void interp_y_kernel(int nx, int ny, int nz, const T* s, T* t, int jo
     if (p >= n) return;
     int j = (int)((p / nx) % ny);
     if (j >= ny - 1) return;
-    t[p + (long long)joff * nx] = T(0.5) * (s[p] + s[p + nx]);
+    interp_pair_point<T>(s, t, p, nx, (long long)joff * nx);
 }
 
 template <typename T>
@@ -311,26 +311,12 @@ extern "C" int getm_advance_surface_elevation(int nx, int ny, int halox, int hal
 }
 
 // wrapper.F90:525-565; C bounds from Fortran 1-based imin..jmax
-__global__ void spg_kernel(int nx, int ny, int ilo, int ihi, int jlo, int jhi, const int* umask,
-                           const int* vmask, const double* idxu, const double* idyv,
-                           const double* z, const double* sp, const double* H, const double* D,
-                           double Dmin, double* dpdx, double* dpdy)
+__global__ void spg_kernel(int nx, int ny, int ilo, int ihi, int jlo, int jhi, SpgArgs a)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i < ilo || i > ihi || j < jlo || j > jhi) return;
-    long long p = (long long)j * nx + i;
-    const double gammai = 1.0 / (GETM_G * GETM_RHO0);
-    if (umask[p] == 1) {
-        double zp = fmax(z[p + 1], -H[p] + fmin(Dmin, D[p + 1]));
-        double zm = fmax(z[p], -H[p + 1] + fmin(Dmin, D[p]));
-        dpdx[p] = (zp - zm + (sp[p + 1] - sp[p]) * gammai) * idxu[p];
-    }
-    if (vmask[p] == 1) {
-        double zp = fmax(z[p + nx], -H[p] + fmin(Dmin, D[p + nx]));
-        double zm = fmax(z[p], -H[p + nx] + fmin(Dmin, D[p]));
-        dpdy[p] = (zp - zm + (sp[p + nx] - sp[p]) * gammai) * idyv[p];
-    }
+    spg_point(a, (long long)j * nx + i);
 }
 
 extern "C" int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax, int jmin, int jmax,
@@ -342,7 +328,8 @@ extern "C" int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax
     if (nx < 1 || ny < 1 || imin < 1 || jmin < 1 || imax >= nx || jmax >= ny) return GETM_ERR_ARG;
     if (!umask || !vmask || !idxu || !idyv || !z || !sp || !H || !D || !dpdx || !dpdy) return GETM_ERR_ARG;
     dim3 grid(getm_div_up(nx, 128), ny);
-    spg_kernel<<<grid, 128, 0, stream>>>(nx, ny, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask, idxu, idyv, z, sp, H, D, Dmin, dpdx, dpdy);
+    SpgArgs a{nx, umask, vmask, idxu, idyv, z, sp, H, D, Dmin, dpdx, dpdy};
+    spg_kernel<<<grid, 128, 0, stream>>>(nx, ny, imin - 1, imax - 1, jmin - 1, jmax - 1, a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

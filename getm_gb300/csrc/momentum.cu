@@ -6,7 +6,7 @@
 // recompute the two face fluxes of each point in registers instead of
 // writing a flux array (no intermediate traffic).  Column recursions
 // (w_momentum_3d) use one thread per column.
-#include "getm_common.cuh"
+#include "split2d_ops.cuh"
 
 #define EW_THREADS 256
 
@@ -175,24 +175,12 @@ extern "C" int getm_collect_3d_momentum_sources_f32(int nx, int ny, int nz, int 
 }
 
 // momentum.F90:147-189
-__global__ void advance_2d_transport_kernel(int nx, int ny, int halox, int haloy, const int* mask,
-                                            const double* alpha, const double* D, const double* dp,
-                                            const double* taus, const double* cor, const double* adv,
-                                            const double* diff, const double* damp, const double* SA,
-                                            const double* SB, const double* SD, const double* SF,
-                                            const double* r, double dt, double* U)
+__global__ void advance_2d_transport_kernel(int nx, int ny, int halox, int haloy, Transport2DArgs a, double dt)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i < halox || i >= nx - halox || j < haloy || j >= ny - haloy) return;
-    long long p = (long long)j * nx + i;
-    if (mask[p] != 1) return;
-    const double rho0i = 1.0 / GETM_RHO0;
-    double Up = U[p];
-    double Slr = (Up > 0.0) ? fmin(SF[p], 0.0) : fmax(SF[p], 0.0);
-    double Dp = D[p];
-    U[p] = (Up + dt * (-GETM_G * Dp * dp[p] + alpha[p] * (taus[p] * rho0i + cor[p] + adv[p] + diff[p] + damp[p] + SA[p] + SB[p] + SD[p] + Slr)))
-           / (1.0 + dt * r[p] / Dp);
+    transport_2d_point(a, dt, (long long)j * nx + i);
 }
 
 extern "C" int getm_advance_2d_transport(int nx, int ny, int halox, int haloy, const int* mask,
@@ -205,7 +193,8 @@ extern "C" int getm_advance_2d_transport(int nx, int ny, int halox, int haloy, c
     if (nx < 1 || ny < 1 || !mask || !alpha || !D || !dp || !taus || !cor || !adv || !diff || !damp || !SA || !SB || !SD || !SF || !r || !U)
         return GETM_ERR_ARG;
     dim3 grid(getm_div_up(nx, 128), ny);
-    advance_2d_transport_kernel<<<grid, 128, 0, stream>>>(nx, ny, halox, haloy, mask, alpha, D, dp, taus, cor, adv, diff, damp, SA, SB, SD, SF, r, dt, U);
+    Transport2DArgs a{mask, alpha, D, dp, taus, cor, adv, diff, damp, SA, SB, SD, SF, r, U};
+    advance_2d_transport_kernel<<<grid, 128, 0, stream>>>(nx, ny, halox, haloy, a, dt);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
@@ -388,7 +377,7 @@ __global__ void reconstruct_kernel(int nx, int ny, int nz, int jlo, int jhi, T* 
     if (p >= plane * nz) return;
     int j = (int)((p % plane) / nx);
     if (j < jlo || j > jhi) return;
-    un[p] = (un[p] * (T)hn[p] - Uo[p]) * (T)idt;
+    reconstruct_point<T>(un, hn, Uo, idt, p);
 }
 
 template <typename T>

@@ -1,0 +1,381 @@
+// Point and tile functions of the split-explicit 2D substep, shared by the
+// one-operation kernels (split2d.cu, momentum.cu, grid_ops.cu) and the
+// persistent substep kernel (substep2d.cu), so that every operation has a
+// single definition and both paths give the same results bit for bit.
+//
+// Layout: every field is [j][i] with the full halo-inclusive extents of its
+// grid (nx_, ny_ for T, U, V and their velocity grids, nx_+1, ny_+1 for X).
+#pragma once
+
+#include <math.h>
+
+#include <type_traits>
+
+#include "getm_common.cuh"
+
+
+// torch.clamp(x, min=lo): NaN propagates
+__device__ __forceinline__ double clamp_min(double x, double lo) { return isnan(x) ? x : (x < lo ? lo : x); }
+
+struct DepthArgs {
+    int nx, ny;                 // T-grid extents (halos included)
+    double Dmin, Dcrit, ialpha; // ialpha = 1 / (Dcrit - 2 Dmin)
+    const double *z, *zo;       // elevations (T)
+    const double *HT, *HU, *HV, *HX;
+    const int *mT, *mU, *mV, *mX;
+    double *DT, *DclipT, *workT;
+    double *workU, *DU, *alphaU;
+    double *workV, *DV, *alphaV;
+    double *workX, *DX;         // X extents (nx+1) x (ny+1)
+    double *DUU, *DVV, *DUV, *DVU;
+};
+
+constexpr int UD_BX = 32;  // tile width of update_depth_2d_tile
+
+// alpha (wrapper.F90:428-436) with the constant divisor as a reciprocal
+__device__ __forceinline__ double alpha_of(double d, double twoDmin, double ialpha)
+{
+    return fmax(0.0, fmin(1.0, (d - twoDmin) * ialpha));
+}
+
+// Simulation.update_depth, 2D part (simulation.py:1498-1586 without the
+// halo exchanges and mirroring of a single closed domain).  A 32 x BY block
+// covers X points (j, i) of its tile and the T, U, V points with the same
+// indices; z_T_half of the tile plus a one-point halo is formed once into
+// shared memory.  Copies between grids are scattered by the point that
+// owns the source value (UU.D(j, i-1) = D_T_half(j, i), VV.D(j-1, i) =
+// D_T_half(j, i), UV.D(j-1, i-1) = VU.D(j-1, i-1) = X.D(j, i)).
+template <int BY>
+__device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx, int by, int tx, int ty,
+                                                     double (&szh)[BY + 2][UD_BX + 2])
+{
+    // szh: z_T_half at rows j0-1.., cols i0-1..
+    const int i0 = bx * UD_BX, j0 = by * BY;
+    const int i = i0 + tx, j = j0 + ty;
+    const int nx = a.nx, ny = a.ny;
+    for (int q = ty * UD_BX + tx; q < (BY + 2) * (UD_BX + 2); q += UD_BX * BY) {
+        const int sj = q / (UD_BX + 2), si = q - sj * (UD_BX + 2);
+        const int gj = j0 - 1 + sj, gi = i0 - 1 + si;
+        double v = 0.0;
+        if (gj >= 0 && gj < ny && gi >= 0 && gi < nx) {
+            const long long g = (long long)gj * nx + gi;
+            v = (a.zo[g] + a.z[g]) * 0.5;
+        }
+        szh[sj][si] = v;
+    }
+    __syncthreads();
+    if (i > nx || j > ny) return;
+    const int sj = ty + 1, si = tx + 1;  // (j, i) in the tile
+    // X point (j, i): interp_xy T->X (offsets 1, 1) where it writes, else the
+    // previous X._work value
+    {
+        const long long px = (long long)j * (nx + 1) + i;
+        double zx;
+        if (j >= 1 && j <= ny - 1 && i >= 1 && i <= nx - 1) {
+            zx = 0.25 * (szh[sj - 1][si - 1] + szh[sj - 1][si] + szh[sj][si - 1] + szh[sj][si]);
+            a.workX[px] = zx;
+        } else {
+            zx = a.workX[px];
+        }
+        double dx = a.DX[px];
+        if (a.mX[px] != 0) {
+            dx = fmax(a.HX[px] + zx, a.Dmin);
+            a.DX[px] = dx;
+        }
+        if (j >= 1 && i >= 1 && j - 1 < ny && i - 1 < nx) {  // UV.D = X.D[1:, 1:]; VU.D = UV.D
+            const long long q = (long long)(j - 1) * nx + (i - 1);
+            a.DUV[q] = dx;
+            a.DVU[q] = dx;
+        }
+    }
+    if (i >= nx || j >= ny) return;
+    const long long p = (long long)j * nx + i;
+    const double zh = szh[sj][si];
+    // T: elevation2depth(z, H, -1000), Dclip = clamp(D, Dmin), D_T_half
+    double DT = a.DT[p];
+    if (a.mT[p] != 0) DT = fmax(a.HT[p] + a.z[p], -1000.0);
+    a.DT[p] = DT;
+    a.DclipT[p] = clamp_min(DT, a.Dmin);
+    const double dth = a.mT[p] != 0 ? fmax(a.HT[p] + zh, a.Dmin) : zh;
+    a.workT[p] = dth;
+    if (i >= 1) a.DUU[p - 1] = dth;   // UU.D[:, :-1] = D_T_half[:, 1:]
+    if (j >= 1) a.DVV[p - nx] = dth;  // VV.D[:-1, :] = D_T_half[1:, :]
+    const double twoDmin = 2 * a.Dmin;
+    // U: z_U = interp_x(z_T_half, ioffset 0) for i < nx-1, else the old value
+    double zu;
+    if (i < nx - 1) {
+        zu = 0.5 * (zh + szh[sj][si + 1]);
+        a.workU[p] = zu;
+    } else {
+        zu = a.workU[p];
+    }
+    if (a.mU[p] != 0) {
+        const double d = fmax(a.HU[p] + zu, a.Dmin);
+        a.DU[p] = d;
+        a.alphaU[p] = alpha_of(d, twoDmin, a.ialpha);
+    }
+    // V: z_V = interp_y(z_T_half, joffset 0) for j < ny-1
+    double zv;
+    if (j < ny - 1) {
+        zv = 0.5 * (zh + szh[sj + 1][si]);
+        a.workV[p] = zv;
+    } else {
+        zv = a.workV[p];
+    }
+    if (a.mV[p] != 0) {
+        const double d = fmax(a.HV[p] + zv, a.Dmin);
+        a.DV[p] = d;
+        a.alphaV[p] = alpha_of(d, twoDmin, a.ialpha);
+    }
+}
+
+// Momentum._transport_2d_momentum up to the advection calls
+// (momentum.py:1017-1040 with Am = 0): u1 = U/DU, v1 = V/DV, the advected
+// copies, and the advection velocities on the UU, UV, VU, VV grids.
+// C: arithmetic of the four advection velocities (float in the mixed form).
+struct VelArgs {
+    int nx, ny;
+    const double *U, *V, *DU, *DV, *DUU, *DUV, *DVU, *DVV;
+    double *u1, *v1, *advU, *advV, *uua, *uva, *vua, *vva;
+};
+
+template <typename C>
+__device__ __forceinline__ double vel_div(double num, double den)
+{
+    if constexpr (std::is_same<C, double>::value) return num / den;
+    else return getm_f2d(getm_d2f_approx(num) / getm_d2f_approx(den));
+}
+
+// Mixed form: u1 = U/D to ~2^-46 (getm_div_refined; u1 is advected and its
+// product with the new depth is differenced against U, so it stays FP64) and
+// the advection velocities entirely in float.
+template <typename C>
+__device__ __forceinline__ void momentum_2d_velocities_point(const VelArgs& a, int i, int j)
+{
+    const long long p = (long long)j * a.nx + i;
+    if constexpr (std::is_same<C, double>::value) {
+        const double u1 = a.U[p] / a.DU[p];
+        const double v1 = a.V[p] / a.DV[p];
+        a.u1[p] = u1; a.advU[p] = u1;
+        a.v1[p] = v1; a.advV[p] = v1;
+        // interp_x (ioffset 0) writes i < nx-1; elsewhere the old value is divided
+        const double uu = i < a.nx - 1 ? 0.5 * (a.U[p] + a.U[p + 1]) : a.uua[p];
+        const double uv = i < a.nx - 1 ? 0.5 * (a.V[p] + a.V[p + 1]) : a.uva[p];
+        const double vu = j < a.ny - 1 ? 0.5 * (a.U[p] + a.U[p + a.nx]) : a.vua[p];
+        const double vv = j < a.ny - 1 ? 0.5 * (a.V[p] + a.V[p + a.nx]) : a.vva[p];
+        a.uua[p] = vel_div<C>(uu, a.DUU[p]);
+        a.uva[p] = vel_div<C>(uv, a.DUV[p]);
+        a.vua[p] = vel_div<C>(vu, a.DVU[p]);
+        a.vva[p] = vel_div<C>(vv, a.DVV[p]);
+    } else {
+        const double Up = a.U[p], Vp = a.V[p];
+        const double u1 = getm_div_refined(Up, a.DU[p]);
+        const double v1 = getm_div_refined(Vp, a.DV[p]);
+        a.u1[p] = u1; a.advU[p] = u1;
+        a.v1[p] = v1; a.advV[p] = v1;
+        const float Uf = getm_d2f_approx(Up), Vf = getm_d2f_approx(Vp);
+        const float uu = i < a.nx - 1 ? 0.5f * (Uf + getm_d2f_approx(a.U[p + 1])) : getm_d2f_approx(a.uua[p]);
+        const float uv = i < a.nx - 1 ? 0.5f * (Vf + getm_d2f_approx(a.V[p + 1])) : getm_d2f_approx(a.uva[p]);
+        const float vu = j < a.ny - 1 ? 0.5f * (Uf + getm_d2f_approx(a.U[p + a.nx])) : getm_d2f_approx(a.vua[p]);
+        const float vv = j < a.ny - 1 ? 0.5f * (Vf + getm_d2f_approx(a.V[p + a.nx])) : getm_d2f_approx(a.vva[p]);
+        a.uua[p] = getm_f2d(uu / getm_d2f_approx(a.DUU[p]));
+        a.uva[p] = getm_f2d(uv / getm_d2f_approx(a.DUV[p]));
+        a.vua[p] = getm_f2d(vu / getm_d2f_approx(a.DVU[p]));
+        a.vva[p] = getm_f2d(vv / getm_d2f_approx(a.DVV[p]));
+    }
+}
+
+// Momentum.bottom_friction (momentum.py:1099-1125): u1 -> V grid and v1 -> U
+// grid by interp_xy, then bottom_friction on both grids (momentum.F90:79-101,
+// iterate = 0).  C: arithmetic of the drag coefficient.
+struct FricArgs {
+    int nx, ny;
+    const int *mU, *mV;
+    const double *u1, *v1, *DU, *DV, *z0bU, *z0bV;
+    double *workU, *workV, *ru, *rv;
+};
+
+template <typename C>
+__device__ __forceinline__ C to_c(double x)
+{
+    if constexpr (std::is_same<C, double>::value) return x;
+    else return getm_d2f_approx(x);
+}
+
+template <typename C>
+__device__ __forceinline__ double from_c(C x)
+{
+    if constexpr (std::is_same<C, double>::value) return x;
+    else return getm_f2d(x);
+}
+
+template <typename C>
+__device__ __forceinline__ double drag(C uu, C vv, double D, double z0)
+{
+    const C DD = to_c<C>(D);
+    const C sqrtcd = C(GETM_KAPPA) / log(C(1) + C(0.5) * DD / to_c<C>(z0));
+    return from_c<C>(sqrtcd * sqrtcd * sqrt(getm_speed2(uu, vv)));
+}
+
+template <typename C>
+__device__ __forceinline__ void momentum_2d_friction_point(const FricArgs& a, int i, int j)
+{
+    const long long p = (long long)j * a.nx + i;
+    const int nx = a.nx;
+    // v_U = interp_xy(v1, ioffset 0, joffset 1): written at j >= 1, i <= nx-2
+    // (in arithmetic C: the drag coefficient is evaluated in C)
+    C vU;
+    if (j >= 1 && i <= nx - 2) {
+        const long long q = p - nx;
+        vU = C(0.25) * (to_c<C>(a.v1[q]) + to_c<C>(a.v1[q + 1]) + to_c<C>(a.v1[q + nx]) + to_c<C>(a.v1[q + nx + 1]));
+        a.workU[p] = from_c<C>(vU);
+    } else {
+        vU = to_c<C>(a.workU[p]);
+    }
+    // u_V = interp_xy(u1, ioffset 1, joffset 0): written at i >= 1, j <= ny-2
+    C uV;
+    if (i >= 1 && j <= a.ny - 2) {
+        const long long q = p - 1;
+        uV = C(0.25) * (to_c<C>(a.u1[q]) + to_c<C>(a.u1[q + 1]) + to_c<C>(a.u1[q + nx]) + to_c<C>(a.u1[q + nx + 1]));
+        a.workV[p] = from_c<C>(uV);
+    } else {
+        uV = to_c<C>(a.workV[p]);
+    }
+    if (a.mU[p] == 1) a.ru[p] = drag<C>(to_c<C>(a.u1[p]), vU, a.DU[p], a.z0bU[p]);
+    if (a.mV[p] == 1) a.rv[p] = drag<C>(uV, to_c<C>(a.v1[p]), a.DV[p], a.z0bV[p]);
+}
+
+// Momentum.coriolis, DEFAULT scheme (momentum.py:1127-1148): interp_xy of the
+// transport to the other velocity grid, times f, negated for the V equation.
+// (ioff, joff) are the interp_xy offsets: U -> V (1, 0); V -> U (0, 1).
+// C: arithmetic (float in the mixed form, whose transport update reads the
+// term as a float tendency).
+template <typename C>
+__device__ __forceinline__ void coriolis_2d_point(int nx, int ny, int ioff, int joff, const double* src,
+                                                  const double* cor, double* out, int negate, int i, int j)
+{
+    const long long p = (long long)j * nx + i;
+    const int si = i - ioff, sj = j - joff;
+    C v;
+    if (si >= 0 && sj >= 0 && si <= nx - 2 && sj <= ny - 2) {
+        const long long q = (long long)sj * nx + si;
+        v = C(0.25) * (to_c<C>(src[q]) + to_c<C>(src[q + 1]) + to_c<C>(src[q + nx]) + to_c<C>(src[q + nx + 1]));
+    } else {
+        v = to_c<C>(out[p]);
+    }
+    v = v * to_c<C>(cor[p]);
+    out[p] = from_c<C>(negate ? -v : v);
+}
+
+// Momentum.advance_depth_integrated's transport update (momentum.F90:147-189)
+// at interior point p; a: the fields of one direction (U or V).
+struct Transport2DArgs {
+    const int* mask;
+    const double *alpha, *D, *dp, *taus, *cor, *adv, *diff, *damp, *SA, *SB, *SD, *SF, *r;
+    double* U;
+};
+
+__device__ __forceinline__ void transport_2d_point(const Transport2DArgs& a, double dt, long long p)
+{
+    if (a.mask[p] != 1) return;
+    const double rho0i = 1.0 / GETM_RHO0;
+    double Up = a.U[p];
+    double Slr = (Up > 0.0) ? fmin(a.SF[p], 0.0) : fmax(a.SF[p], 0.0);
+    double Dp = a.D[p];
+    a.U[p] = (Up + dt * (-GETM_G * Dp * a.dp[p] + a.alpha[p] * (a.taus[p] * rho0i + a.cor[p] + a.adv[p] + a.diff[p] + a.damp[p] + a.SA[p] + a.SB[p] + a.SD[p] + Slr)))
+             / (1.0 + dt * a.r[p] / Dp);
+}
+
+// Momentum.advance_depth_integrated's transport update, mixed form
+// (momentum.F90:147-189): the tendency is summed in float, the transport is
+// updated in double, and the implicit friction factor 1/(1 + x), x =
+// dt r / D, is applied as U - U x/(1 + x) with the small correction in float
+// (no FP64 division).
+__device__ __forceinline__ void transport_2d_mixed_point(const Transport2DArgs& a, double dt, long long p)
+{
+    const int* mask = a.mask;
+    const double *alpha = a.alpha, *D = a.D, *dp = a.dp, *taus = a.taus, *cor = a.cor, *adv = a.adv;
+    const double *diff = a.diff, *damp = a.damp, *SA = a.SA, *SB = a.SB, *SD = a.SD, *SF = a.SF, *r = a.r;
+    double* U = a.U;
+    if (mask[p] != 1) return;
+    const float rho0i = (float)(1.0 / GETM_RHO0);
+    const double Up = U[p];
+    const float sf = getm_d2f_approx(SF[p]);
+    const float Slr = (Up > 0.0) ? fminf(sf, 0.f) : fmaxf(sf, 0.f);
+    const float Dp = getm_d2f_approx(D[p]);
+    const float dtf = (float)dt;
+    const float tend = -(float)GETM_G * Dp * getm_d2f_approx(dp[p]) +
+                       getm_d2f_approx(alpha[p]) *
+                           (getm_d2f_approx(taus[p]) * rho0i + getm_d2f_approx(cor[p]) + getm_d2f_approx(adv[p]) +
+                            getm_d2f_approx(diff[p]) + getm_d2f_approx(damp[p]) + getm_d2f_approx(SA[p]) +
+                            getm_d2f_approx(SB[p]) + getm_d2f_approx(SD[p]) + Slr);
+    const double num = Up + getm_f2d(dtf * tend);
+    const float x = dtf * getm_d2f_approx(r[p]) / Dp;
+    U[p] = num - getm_f2d(getm_d2f_approx(num) * (x / (1.f + x)));
+}
+
+// _U_cum += U; _V_cum += V (momentum.py:716-718), every point
+__device__ __forceinline__ void accumulate_2d_point(const double* U, const double* V, double* Uc, double* Vc,
+                                                    long long p)
+{
+    Uc[p] = Uc[p] + U[p];
+    Vc[p] = Vc[p] + V[p];
+}
+
+// zo = z (every point), then the surface elevation update
+// (simulation.py:1468-1486 -> wrapper.F90:496-523)
+__device__ __forceinline__ void surface_elevation_fused_point(int nx, int ny, int halox, int haloy, const int* mask,
+                                                              const double* dyu, const double* dxv,
+                                                              const double* iarea, double* z, double* zo,
+                                                              const double* U, const double* V, const double* fwf,
+                                                              double dt, int i, int j)
+{
+    const long long p = (long long)j * nx + i;
+    const double zp = z[p];
+    zo[p] = zp;
+    if (i < halox || i >= nx - halox || j < haloy || j >= ny - haloy) return;
+    if (mask[p] != 1) return;
+    z[p] = zp + dt * ((U[p - 1] * dyu[p - 1] - U[p] * dyu[p] + V[p - nx] * dxv[p - nx] - V[p] * dxv[p]) * iarea[p] + fwf[p]);
+}
+
+
+// reconstruct_transport_change (momentum.F90:323-340) at point p of a row
+// inside jmin..jmax (T: type of un and Uo)
+template <typename T>
+__device__ __forceinline__ void reconstruct_point(T* un, const double* hn, const T* Uo, double idt, long long p)
+{
+    un[p] = (un[p] * (T)hn[p] - Uo[p]) * (T)idt;
+}
+
+// surface_pressure_gradient (wrapper.F90:525-565) at interior point (i, j)
+struct SpgArgs {
+    int nx;
+    const int *umask, *vmask;
+    const double *idxu, *idyv, *z, *sp, *H, *D;
+    double Dmin;
+    double *dpdx, *dpdy;
+};
+
+__device__ __forceinline__ void spg_point(const SpgArgs& a, long long p)
+{
+    const int nx = a.nx;
+    const double gammai = 1.0 / (GETM_G * GETM_RHO0);
+    if (a.umask[p] == 1) {
+        double zp = fmax(a.z[p + 1], -a.H[p] + fmin(a.Dmin, a.D[p + 1]));
+        double zm = fmax(a.z[p], -a.H[p + 1] + fmin(a.Dmin, a.D[p]));
+        a.dpdx[p] = (zp - zm + (a.sp[p + 1] - a.sp[p]) * gammai) * a.idxu[p];
+    }
+    if (a.vmask[p] == 1) {
+        double zp = fmax(a.z[p + nx], -a.H[p] + fmin(a.Dmin, a.D[p + nx]));
+        double zm = fmax(a.z[p], -a.H[p + nx] + fmin(a.Dmin, a.D[p]));
+        a.dpdy[p] = (zp - zm + (a.sp[p + nx] - a.sp[p]) * gammai) * a.idyv[p];
+    }
+}
+
+// interp_x / interp_y (interpolation.F90:9-40) of one point: t = mean of s
+// at p and its neighbour at +step, stored at p + off (off = 0 or step)
+template <typename T>
+__device__ __forceinline__ void interp_pair_point(const T* s, T* t, long long p, long long step, long long off)
+{
+    t[p + off] = T(0.5) * (s[p] + s[p + step]);
+}

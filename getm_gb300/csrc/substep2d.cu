@@ -1,0 +1,368 @@
+// One split-explicit 2D substep as one persistent kernel for sm_103a.
+//
+// A 2D substep of pygetm's Simulation.advance that is not followed by a 3D
+// (macro) step (python/pygetm/simulation.py:1033-1304: advance_depth_integrated,
+// advance_surface_elevation, update_depth, update_depth_integrated_diagnostics,
+// the surface pressure gradient and the wind-stress interpolation) is some
+// twenty operations on fields of one horizontal plane.  Launched one by one
+// they leave GB300 idle between launches: each reads and writes ~10^5 points,
+// a microsecond of work behind several microseconds of launch and drain.
+//
+// Here one cooperative launch runs the whole substep.  Its blocks (one per
+// SM, 512 threads) walk through eight phases separated by grid-wide
+// barriers; a phase contains operations whose inputs at neighbouring points
+// were completed by an earlier phase:
+//   1  transport update of the first direction (U or V, alternating)
+//   2  Coriolis term from it, then the second direction's update
+//   3  Coriolis term from the second, cumulative transports, zo = z and the
+//      surface elevation update
+//   4  depths (update_depth, 2D part), fwf = pe, wind stress interpolation
+//   5  velocities and advection velocities, copies of the depths advected
+//      by the momentum advection, surface pressure gradient
+//   6  bottom friction, first pass of the U and V momentum advection
+//   7  second pass of both
+//   8  transport change of the momentum advection (reconstruct)
+// Every operation is the same device function the separate kernels run
+// (split2d_ops.cuh, advection_passes.cuh), so results are bitwise the same.
+//
+// The barrier is a counter and a generation word in global memory.  Its wait
+// is bounded: after about a second it sets the error word, every block
+// returns, and later launches return at once until the host clears the word.
+#include <string.h>
+
+#include <type_traits>
+
+#include "advection_passes.cuh"
+#include "split2d_ops.cuh"
+
+namespace {
+
+constexpr int SS_BY = 16;
+constexpr int SS_THREADS = 32 * SS_BY;
+constexpr unsigned SS_SPIN_LIMIT = 1u << 22;
+
+__device__ __forceinline__ int div_up(int a, int b) { return (a + b - 1) / b; }
+
+struct SubstepArgs {
+    int nx, ny, halox, haloy;
+    int ufirst, accumulate, friction;
+    double dt, idt;
+    double* time;
+    Transport2DArgs tr[2];       // [0]: U, [1]: V
+    double* cor_out[2];          // Coriolis terms corU, corV (read by tr[].cor)
+    const double* corf[2];       // Coriolis parameter on U, V
+    double *Ucum, *Vcum;
+    const int* mT;
+    const double *dyU, *dxV, *iareaT;
+    double *z, *zo, *fwf;
+    const double* pe;
+    DepthArgs depth;
+    VelArgs vel;
+    FricArgs fric;
+    SpgArgs spg;
+    const double *taux, *tauy;
+    double *tausx, *tausy;
+    Advection2DPasses adv[2];    // momentum advection of U and V
+    const double* Dsrc[2];       // U.D, V.D
+    double* advD[2];             // the advections' thickness arrays
+    double* advvar[2];           // advU, advV
+    const double* Uo[2];         // U, V
+    unsigned* sync;              // [0] barrier arrivals, [1] blocks done, [2] error
+};
+
+static_assert(SS_BY == GETM_V_BY && SS_BY == HY_BY, "the y passes run on the kernel's 32 x 16 blocks");
+
+union SubstepSmem {
+    double szh[SS_BY + 2][UD_BX + 2];
+    struct {
+        double sQ[GETM_V_BY][32];
+        double sF[GETM_V_BY][32];
+    } y;
+    YIncSmem<double> yi;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier k of a launch: thread 0 of every block adds one arrival
+// and waits until the count reaches k blocks per block; false when the wait
+// gave up or another block reported an error (the caller returns).  The
+// count only grows during a launch; the last block to leave the kernel
+// resets it (grid_exit) for the next launch on the stream.
+__device__ __forceinline__ bool grid_barrier(unsigned* sync, unsigned& target, int& s_ok)
+{
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        target += gridDim.x;
+        __threadfence();
+        atomicAdd(&sync[0], 1u);
+        int ok = 1;
+        unsigned it = 0;
+        while (ld_acquire(&sync[0]) < target) {
+            if (++it > SS_SPIN_LIMIT) {
+                atomicExch(&sync[2], 1u);
+                ok = 0;
+                break;
+            }
+            if ((it & 255u) == 0 && ld_acquire(&sync[2]) != 0) {  // another block gave up
+                ok = 0;
+                break;
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ void grid_exit(unsigned* sync)
+{
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        if (atomicAdd(&sync[1], 1u) == gridDim.x - 1) {
+            atomicExch(&sync[0], 0u);
+            atomicExch(&sync[1], 0u);
+        }
+    }
+}
+
+// One advection pass over the whole plane, distributed over the grid: x
+// passes by warps (one row segment each), y passes by blocks (one tile each).
+template <bool MIXED>
+__device__ __forceinline__ void advection_pass(const HPassArgs<double>& pa, int dir, SubstepSmem& sm, int tx,
+                                               int ty)
+{
+    if (dir == 1) {
+        const int nbx = MIXED ? div_up(pa.nx_ + 1, HX_STRIDE) : div_up(pa.nx_, 32);
+        const long long items = (long long)nbx * pa.ny_;
+        for (long long w = (long long)blockIdx.x * SS_BY + ty; w < items; w += (long long)gridDim.x * SS_BY) {
+            const int bx = (int)(w % nbx);
+            const long long row = w / nbx;
+            if constexpr (MIXED) hpass_x_inc_body<double>(pa, bx, row, tx);
+            else hpass_x_body<double>(pa, bx, row, tx);
+        }
+    } else {
+        const int nbx = div_up(pa.nx_, 32);
+        const int nby = MIXED ? div_up(pa.ny_ + 1, HY_STRIDE) : div_up(pa.ny_, GETM_V_BY);
+        for (int t = blockIdx.x; t < nbx * nby; t += gridDim.x) {
+            if constexpr (MIXED) hpass_y_inc_body<double>(pa, t % nbx, t / nbx, 0, tx, ty, sm.yi);
+            else hpass_y_body<double>(pa, t % nbx, t / nbx, 0, tx, ty, sm.y.sQ, sm.y.sF);
+            __syncthreads();  // shared memory is reused by the next tile
+        }
+    }
+}
+
+template <bool MIXED>
+__device__ __forceinline__ void transport_update(const Transport2DArgs& t, double dt, long long p)
+{
+    if constexpr (MIXED) transport_2d_mixed_point(t, dt, p);
+    else transport_2d_point(t, dt, p);
+}
+
+// Coriolis term on the other velocity grid from the transport of direction
+// d (momentum.py:1127-1148): U -> V with offsets (1, 0), negated; V -> U
+// with offsets (0, 1).
+template <typename C>
+__device__ __forceinline__ void coriolis_from(const SubstepArgs& a, int d, int i, int j)
+{
+    const int o = 1 - d;
+    coriolis_2d_point<C>(a.nx, a.ny, d == 0 ? 1 : 0, d == 0 ? 0 : 1, a.tr[d].U, a.corf[o], a.cor_out[o], d == 0, i,
+                         j);
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(SubstepArgs a)
+{
+    using C = typename std::conditional<MIXED, float, double>::type;
+    __shared__ SubstepSmem sm;
+    __shared__ int s_ok;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int G = gridDim.x * SS_THREADS;
+    const int gt = blockIdx.x * SS_THREADS + ty * 32 + tx;
+    const int nx = a.nx, ny = a.ny;
+    const int n = nx * ny;  // < 2^30 (checked by the host)
+    const int ilo = a.halox, ihi = nx - a.halox - 1, jlo = a.haloy, jhi = ny - a.haloy - 1;
+
+    unsigned target = 0;  // barrier count to wait for (thread 0)
+    if (tx == 0 && ty == 0) s_ok = ld_acquire(&a.sync[2]) == 0;
+    __syncthreads();
+    if (!s_ok) return;
+    if (gt == 0 && a.time) *a.time = *a.time + a.dt;
+
+    const int d1 = a.ufirst ? 0 : 1, d2 = 1 - d1;
+    // 1: first transport update
+    for (int p = gt; p < n; p += G) {
+        const int j = p / nx, i = p - j * nx;
+        if (i >= ilo && i <= ihi && j >= jlo && j <= jhi) transport_update<MIXED>(a.tr[d1], a.dt, p);
+    }
+    if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
+    // 2: Coriolis from the first, second transport update
+    for (int p = gt; p < n; p += G) {
+        const int j = p / nx, i = p - j * nx;
+        coriolis_from<C>(a, d1, i, j);
+        if (i >= ilo && i <= ihi && j >= jlo && j <= jhi) transport_update<MIXED>(a.tr[d2], a.dt, p);
+    }
+    if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
+    // 3: Coriolis from the second, cumulative transports, surface elevation
+    for (int p = gt; p < n; p += G) {
+        const int j = p / nx, i = p - j * nx;
+        coriolis_from<C>(a, d2, i, j);
+        if (a.accumulate) accumulate_2d_point(a.tr[0].U, a.tr[1].U, a.Ucum, a.Vcum, p);
+        surface_elevation_fused_point(nx, ny, a.halox, a.haloy, a.mT, a.dyU, a.dxV, a.iareaT, a.z, a.zo,
+                                      a.tr[0].U, a.tr[1].U, a.fwf, a.dt, i, j);
+    }
+    if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
+    // 4: depths; fwf = pe; wind stress on U and V (interp_x/y, offset 0)
+    {
+        const int ntx = div_up(nx + 1, UD_BX), nty = div_up(ny + 1, SS_BY);
+        for (int t = blockIdx.x; t < ntx * nty; t += gridDim.x) {
+            update_depth_2d_tile<SS_BY>(a.depth, t % ntx, t / ntx, tx, ty, sm.szh);
+            __syncthreads();
+        }
+    }
+    for (int p = gt; p < n; p += G) {
+        const int j = p / nx, i = p - j * nx;
+        a.fwf[p] = a.pe[p];
+        if (i < nx - 1) interp_pair_point<double>(a.taux, a.tausx, p, 1, 0);
+        if (j < ny - 1) interp_pair_point<double>(a.tauy, a.tausy, p, nx, 0);
+    }
+    if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
+    // 5: velocities, advected thicknesses, surface pressure gradient
+    for (int p = gt; p < n; p += G) {
+        const int j = p / nx, i = p - j * nx;
+        momentum_2d_velocities_point<C>(a.vel, i, j);
+        a.advD[0][p] = a.Dsrc[0][p];
+        a.advD[1][p] = a.Dsrc[1][p];
+        if (i >= ilo && i <= ihi && j >= jlo && j <= jhi) spg_point(a.spg, p);
+    }
+    if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
+    // 6: bottom friction; first advection passes
+    if (a.friction) {
+        for (int p = gt; p < n; p += G) {
+            const int j = p / nx, i = p - j * nx;
+            momentum_2d_friction_point<C>(a.fric, i, j);
+        }
+    }
+    advection_pass<MIXED>(a.adv[0].pass[0], a.adv[0].dir[0], sm, tx, ty);
+    advection_pass<MIXED>(a.adv[1].pass[0], a.adv[1].dir[0], sm, tx, ty);
+    if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
+    // 7: second advection passes
+    advection_pass<MIXED>(a.adv[0].pass[1], a.adv[0].dir[1], sm, tx, ty);
+    advection_pass<MIXED>(a.adv[1].pass[1], a.adv[1].dir[1], sm, tx, ty);
+    if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
+    // 8: advection terms from the transport change (rows jlo..jhi, every i)
+    for (int p = gt; p < n; p += G) {
+        const int j = p / nx;
+        if (j < jlo || j > jhi) continue;
+        reconstruct_point<double>(a.advvar[0], a.advD[0], a.Uo[0], a.idt, p);
+        reconstruct_point<double>(a.advvar[1], a.advD[1], a.Uo[1], a.idt, p);
+    }
+    grid_exit(a.sync);
+}
+
+static_assert(sizeof(SubstepArgs) <= 4096, "kernel parameter block");
+
+struct LaunchShape {
+    int blocks = 0;
+};
+
+template <bool MIXED>
+int launch_substep(const SubstepArgs& a, cudaStream_t stream)
+{
+    // co-resident blocks per SM, queried once per process (device 0 of the
+    // process: one process drives one GPU)
+    static LaunchShape shape;
+    if (shape.blocks == 0) {
+        int dev = 0, sms = 0, coop = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return GETM_ERR_CUDA;
+        if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
+            return GETM_ERR_CUDA;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GETM_ERR_CUDA;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, substep_2d_kernel<MIXED>, SS_THREADS, 0) !=
+                cudaSuccess ||
+            per_sm < 1)
+            return GETM_ERR_CUDA;
+        shape.blocks = sms * per_sm;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(shape.blocks);
+    cfg.blockDim = dim3(32, SS_BY);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, substep_2d_kernel<MIXED>, a) != cudaSuccess) return GETM_ERR_CUDA;
+    return GETM_OK;
+}
+
+}  // namespace
+
+extern "C" int getm_split2d_substep(const getm_split2d_fields* f, int nx, int ny, int halox, int haloy, int mixed,
+                                    int ufirst, int accumulate, int friction, double timestep, double Dmin,
+                                    double Dcrit, getm_advection* uadv, getm_grid* ugrid, getm_grid* uugrid,
+                                    getm_grid* uvgrid, int uadv_ufirst, getm_advection* vadv, getm_grid* vgrid,
+                                    getm_grid* vugrid, getm_grid* vvgrid, int vadv_ufirst, cudaStream_t stream)
+{
+    if (!f || nx < 2 || ny < 2 || halox < 1 || haloy < 1 || !(timestep > 0.0) || !uadv || !vadv) return GETM_ERR_ARG;
+    if ((long long)(nx + 1) * (ny + 1) >= (1ll << 30)) return GETM_ERR_ARG;
+    const void* ptrs[] = {f->mask_t, f->H_t, f->iarea_t, f->z, f->zo, f->D_t, f->Dclip_t, f->work_t, f->fwf, f->pe,
+                          f->sp, f->taux, f->tauy,
+                          f->mask_u, f->H_u, f->dy_u, f->idx_u, f->cor_u, f->z0b_u, f->D_u, f->alpha_u, f->work_u,
+                          f->U, f->dpdx, f->tausx, f->corU, f->advU, f->diffU, f->dampU, f->SxA, f->SxB, f->SxD,
+                          f->SxF, f->ru, f->u1, f->Ucum, f->advD_u, f->uua, f->uva,
+                          f->mask_v, f->H_v, f->dx_v, f->idy_v, f->cor_v, f->z0b_v, f->D_v, f->alpha_v, f->work_v,
+                          f->V, f->dpdy, f->tausy, f->corV, f->advV, f->diffV, f->dampV, f->SyA, f->SyB, f->SyD,
+                          f->SyF, f->rv, f->v1, f->Vcum, f->advD_v, f->vua, f->vva,
+                          f->mask_x, f->H_x, f->D_x, f->work_x, f->D_uu, f->D_uv, f->D_vu, f->D_vv, f->sync};
+    for (const void* q : ptrs)
+        if (!q) return GETM_ERR_ARG;
+    SubstepArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nx = nx; a.ny = ny; a.halox = halox; a.haloy = haloy;
+    a.ufirst = ufirst != 0; a.accumulate = accumulate != 0; a.friction = friction != 0;
+    a.dt = timestep; a.idt = 1.0 / timestep;
+    a.time = f->time;
+    a.tr[0] = Transport2DArgs{f->mask_u, f->alpha_u, f->D_u, f->dpdx, f->tausx, f->corU, f->advU, f->diffU,
+                              f->dampU, f->SxA, f->SxB, f->SxD, f->SxF, f->ru, f->U};
+    a.tr[1] = Transport2DArgs{f->mask_v, f->alpha_v, f->D_v, f->dpdy, f->tausy, f->corV, f->advV, f->diffV,
+                              f->dampV, f->SyA, f->SyB, f->SyD, f->SyF, f->rv, f->V};
+    a.cor_out[0] = f->corU; a.cor_out[1] = f->corV;
+    a.corf[0] = f->cor_u; a.corf[1] = f->cor_v;
+    a.Ucum = f->Ucum; a.Vcum = f->Vcum;
+    a.mT = f->mask_t; a.dyU = f->dy_u; a.dxV = f->dx_v; a.iareaT = f->iarea_t;
+    a.z = f->z; a.zo = f->zo; a.fwf = f->fwf; a.pe = f->pe;
+    a.depth = DepthArgs{nx, ny, Dmin, Dcrit, 1.0 / (Dcrit - 2 * Dmin), f->z, f->zo, f->H_t, f->H_u, f->H_v, f->H_x,
+                        f->mask_t, f->mask_u, f->mask_v, f->mask_x, f->D_t, f->Dclip_t, f->work_t, f->work_u,
+                        f->D_u, f->alpha_u, f->work_v, f->D_v, f->alpha_v, f->work_x, f->D_x, f->D_uu, f->D_vv,
+                        f->D_uv, f->D_vu};
+    a.vel = VelArgs{nx, ny, f->U, f->V, f->D_u, f->D_v, f->D_uu, f->D_uv, f->D_vu, f->D_vv, f->u1, f->v1, f->advU,
+                    f->advV, f->uua, f->uva, f->vua, f->vva};
+    a.fric = FricArgs{nx, ny, f->mask_u, f->mask_v, f->u1, f->v1, f->D_u, f->D_v, f->z0b_u, f->z0b_v, f->work_u,
+                      f->work_v, f->ru, f->rv};
+    a.spg = SpgArgs{nx, f->mask_u, f->mask_v, f->idx_u, f->idy_v, f->z, f->sp, f->H_t, f->D_t, Dmin, f->dpdx,
+                    f->dpdy};
+    a.taux = f->taux; a.tauy = f->tauy; a.tausx = f->tausx; a.tausy = f->tausy;
+    int rc = getm_advection_2d_passes(uadv, ugrid, uugrid, uvgrid, uadv_ufirst, f->uua, f->uva, timestep, f->advD_u,
+                                      f->D_uu, f->D_uv, f->advU, mixed != 0, &a.adv[0]);
+    if (rc) return rc;
+    rc = getm_advection_2d_passes(vadv, vgrid, vugrid, vvgrid, vadv_ufirst, f->vua, f->vva, timestep, f->advD_v,
+                                  f->D_vu, f->D_vv, f->advV, mixed != 0, &a.adv[1]);
+    if (rc) return rc;
+    for (int d = 0; d < 2; d++)
+        for (int s = 0; s < 2; s++)
+            if (a.adv[d].pass[s].nx_ != nx || a.adv[d].pass[s].ny_ != ny) return GETM_ERR_ARG;
+    a.Dsrc[0] = f->D_u; a.Dsrc[1] = f->D_v;
+    a.advD[0] = f->advD_u; a.advD[1] = f->advD_v;
+    a.advvar[0] = f->advU; a.advvar[1] = f->advV;
+    a.Uo[0] = f->U; a.Uo[1] = f->V;
+    a.sync = f->sync;
+    return mixed ? launch_substep<true>(a, stream) : launch_substep<false>(a, stream);
+}

@@ -265,7 +265,7 @@ class Momentum:
         if self.coriolis_scheme == CoriolisScheme.ESPELID:
             raise NotImplementedError("Espelid Coriolis interpolation is not implemented")
         if self.fused_2d and not U.z:
-            _pygetm.coriolis_2d(U, out, x_direction)
+            _pygetm.coriolis_2d(U, out, x_direction, mixed=self.dtype3d == torch.float32)
             return
         U.interp(out)
         out.all_values.mul_(out.grid.cor.all_values)

@@ -60,7 +60,8 @@ import enum  # noqa: E402
 
 from . import _pygetm  # noqa: E402
 from .domain import FILL_VALUE, GRAVITY, RHO0  # noqa: E402
-from .momentum import Momentum  # noqa: E402
+from .momentum import CoriolisScheme, Momentum  # noqa: E402
+from .operators import AdvectionSplit  # noqa: E402
 
 
 class RunType(enum.IntEnum):
@@ -85,6 +86,15 @@ class Fluxes:
             setattr(self, n, a)
 
 
+class _Split2DPlan:
+    """Arguments of the one-launch 2D substep: the fields struct and the
+    kernel's barrier words."""
+
+    def __init__(self, fields, sync):
+        self.fields = fields
+        self.sync = sync
+
+
 class Simulation:
     """GPU counterpart of pygetm.Simulation (python/pygetm/simulation.py:477-1630)
     for closed domains with prescribed surface fluxes and prescribed vertical
@@ -99,17 +109,25 @@ class Simulation:
                  advection_scheme: AdvectionScheme = AdvectionScheme.DEFAULT, momentum: Optional[Momentum] = None,
                  airsea: Optional[Fluxes] = None, internal_pressure: str = "shchepetkin_mcwilliams",
                  Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
-                 nuh: float = 0.0, precision: str = "fp64", fused_2d: bool = True, device="cuda"):
+                 nuh: float = 0.0, precision: str = "fp64", fused_2d: bool = True, substep_kernel: bool = True,
+                 device="cuda"):
         """``precision``: "fp64" (the plain form) or "mixed" (float32 tracers,
         3D velocities and their tendencies and diffusivities; float64
         elevations, depths, layer thicknesses, 2D transports and their
         accumulation, density, buoyancy, internal pressure and the budget
         sums of ``totals``; increments, tendencies, limiters, drag and the
-        internal-pressure slope corrections are evaluated in float)."""
+        internal-pressure slope corrections are evaluated in float).
+        ``fused_2d``: the 2D substep's operations run as fused kernels;
+        ``substep_kernel``: in addition, a substep that is not followed by a
+        3D step runs as one persistent kernel launch (closed domains with the
+        default Coriolis scheme, FULL 2D advection split, no horizontal
+        momentum diffusion, 3D run types)."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
         self.fused_2d = fused_2d
+        self.substep_kernel = substep_kernel and fused_2d
+        self._split2d = None
         d3 = torch.float32 if precision == "mixed" else torch.float64
         self.dtype3d = d3
         if Dmin <= 0.0:
@@ -197,14 +215,59 @@ class Simulation:
             self._ob.init_tracer_values(self.tracers._tracers)
         self._start()
         self._update_forcing_and_diagnostics(macro_active=True)
+        self._split2d = self._split2d_plan() if self.substep_kernel else None
 
     def advance(self):
         """python/pygetm/simulation.py:291-325"""
         self.istep += 1
-        self._time.add_(self.timestep)
         macro_active = self.istep % self.split_factor == 0
+        if self._split2d is not None and not macro_active:
+            self._split2d_substep()
+            return
+        self._time.add_(self.timestep)
         self._advance_state(macro_active)
         self._update_forcing_and_diagnostics(macro_active)
+
+    def _split2d_plan(self):
+        """Fields of the one-launch 2D substep, or None where that kernel does
+        not cover the configuration (the substep then runs operation by
+        operation)."""
+        m = self.momentum
+        if (self._ob is not None or self.runtype <= RunType.BAROTROPIC_2D or m.diffuse_momentum
+                or m.An_uu is not None or m.coriolis_scheme != CoriolisScheme.DEFAULT
+                or m.advection_split_2d != AdvectionSplit.FULL or not m.uadv.p.value or not m.vadv.p.value
+                or self.T.device.type != "cuda"):
+            return None
+        T, U, V, X, a = self.T, self.U, self.V, self.X, self.airsea
+        sync = torch.zeros(4, dtype=torch.int32, device=T.device)  # barrier words, not model state
+        fields = _pygetm.split2d_fields(
+            mask_t=T.mask, H_t=T.H, iarea_t=T.iarea, z=T.z, zo=T.zo, D_t=T.D, Dclip_t=T.Dclip, work_t=T._work,
+            fwf=self.fwf, pe=a.pe, sp=a.sp, taux=a.taux, tauy=a.tauy,
+            mask_u=U.mask, H_u=U.H, dy_u=U.dy, idx_u=U.idx, cor_u=U.cor, z0b_u=U.z0b, D_u=U.D, alpha_u=U.alpha,
+            work_u=U._work, U=m.U, dpdx=self.dpdx, tausx=self.tausx, corU=m.corU, advU=m.advU, diffU=m.diffU,
+            dampU=m.dampU, SxA=m.SxA, SxB=m.SxB, SxD=m.SxD, SxF=m.SxF, ru=m.ru, u1=m.u1, Ucum=m._U_cum,
+            advD_u=m.uadv.D, uua=m.uua, uva=m.uva,
+            mask_v=V.mask, H_v=V.H, dx_v=V.dx, idy_v=V.idy, cor_v=V.cor, z0b_v=V.z0b, D_v=V.D, alpha_v=V.alpha,
+            work_v=V._work, V=m.V, dpdy=self.dpdy, tausy=self.tausy, corV=m.corV, advV=m.advV, diffV=m.diffV,
+            dampV=m.dampV, SyA=m.SyA, SyB=m.SyB, SyD=m.SyD, SyF=m.SyF, rv=m.rv, v1=m.v1, Vcum=m._V_cum,
+            advD_v=m.vadv.D, vua=m.vua, vva=m.vva,
+            mask_x=X.mask, H_x=X.H, D_x=X.D, work_x=X._work, D_uu=U.ugrid.D, D_uv=U.vgrid.D, D_vu=V.ugrid.D,
+            D_vv=V.vgrid.D, time=self._time, sync=sync)
+        return _Split2DPlan(fields, sync)
+
+    def _split2d_substep(self):
+        """A substep without 3D step as one launch (the same operations as
+        _advance_state + _update_forcing_and_diagnostics with macro_active
+        false, in the same order, with bitwise the same results)."""
+        m = self.momentum
+        _pygetm.split2d_substep(self._split2d.fields, self.T, self.dtype3d == torch.float32, m._ufirst, True,
+                                m.apply_bottom_friction, self.timestep, self.Dmin, self.Dcrit, m.uadv, m.vadv)
+        m._ufirst = not m._ufirst
+
+    def split2d_status(self) -> int:
+        """Non-zero when a grid barrier of the one-launch substep gave up (the
+        substep did not complete; reads the device word)."""
+        return 0 if self._split2d is None else int(self._split2d.sync[2].item())
 
     def _start(self):
         """python/pygetm/simulation.py:948-1031"""

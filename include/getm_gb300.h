@@ -408,6 +408,10 @@ int getm_momentum_2d_friction(int nx, int ny, int mixed, const int* mU, const in
  * (-1 if negate) * f * interp_xy(src, ioffset, joffset).                  */
 int getm_coriolis_2d(int nx, int ny, int ioffset, int joffset, const double* src, const double* cor,
                      double* out, int negate, cudaStream_t stream);
+/* the same in float arithmetic (mixed form: the transport update reads the
+ * term as a float tendency)                                                */
+int getm_coriolis_2d_mixed(int nx, int ny, int ioffset, int joffset, const double* src, const double* cor,
+                           double* out, int negate, cudaStream_t stream);
 /* advance_2d_transport (momentum.F90:147-189) in the mixed form: tendency
  * summed in float, transport updated in double; same arguments as
  * getm_advance_2d_transport.                                               */
@@ -465,6 +469,56 @@ int getm_mirror_f32(int n, const int* src, const int* tgt, int nlev, long long p
 int getm_open_boundary_depth(int n, const int* srcT, const int* tgt, const double* z, const double* zo,
                              const double* H, const int* mask, double Dmin, double Dcrit, double* work,
                              double* D, double* alpha, cudaStream_t stream);
+
+/* ---- one 2D substep as one launch -----------------------------------------
+ * Replaces, for a substep of python/pygetm/simulation.py:291-325
+ * (Simulation.advance) that is not followed by a 3D step, the sequence
+ * simulation.py:1033-1039 (momentum.advance_depth_integrated, momentum.py
+ * :644-718, and advance_surface_elevation, :1468-1486) and :1138-1304 with
+ * update_3d false: update_depth (2D part, :1498-1586), the momentum
+ * diagnostics with skip_coriolis (momentum.py:720-758, :1017-1125) without
+ * horizontal diffusion and without the z0b iteration, fwf = pe, the surface
+ * pressure gradient and the wind-stress interpolation; plus time += dt.
+ * Closed domains (no open boundaries), DEFAULT Coriolis scheme, FULL 2D
+ * advection split.  Results are bitwise those of the separate operations.
+ * mixed: 0 FP64 form, 1 mixed form (float tendencies, increment-form 2D
+ * advection; getm_advance_2d_transport_mixed, getm_advection_2d_mixed).
+ * ufirst: momentum order of this substep (U then V); accumulate: add U, V to
+ * Ucum, Vcum (3D runs); friction: bottom friction (ru, rv).  uadv/vadv: the
+ * momentum advection handles with their grids (T = U resp. V grid) and their
+ * u-first flags.  sync: 4 words, zero before the first call; sync[2] != 0
+ * after a call means a grid barrier gave up (the call did not complete and
+ * every later call returns at once until the word is cleared).  All fields
+ * are [j][i] with the full extents nx, ny (X fields nx+1, ny+1).            */
+typedef struct getm_split2d_fields {
+    /* T grid */
+    const int* mask_t; const double* H_t; const double* iarea_t;
+    double* z; double* zo; double* D_t; double* Dclip_t; double* work_t;
+    double* fwf; const double* pe; const double* sp; const double* taux; const double* tauy;
+    /* U grid and the U momentum equation */
+    const int* mask_u; const double* H_u; const double* dy_u; const double* idx_u; const double* cor_u;
+    const double* z0b_u; double* D_u; double* alpha_u; double* work_u;
+    double* U; double* dpdx; double* tausx; double* corU; double* advU; const double* diffU;
+    const double* dampU; const double* SxA; const double* SxB; const double* SxD; const double* SxF;
+    double* ru; double* u1; double* Ucum; double* advD_u; double* uua; double* uva;
+    /* V grid and the V momentum equation */
+    const int* mask_v; const double* H_v; const double* dx_v; const double* idy_v; const double* cor_v;
+    const double* z0b_v; double* D_v; double* alpha_v; double* work_v;
+    double* V; double* dpdy; double* tausy; double* corV; double* advV; const double* diffV;
+    const double* dampV; const double* SyA; const double* SyB; const double* SyD; const double* SyF;
+    double* rv; double* v1; double* Vcum; double* advD_v; double* vua; double* vva;
+    /* X grid and the depths of the advection velocity grids */
+    const int* mask_x; const double* H_x; double* D_x; double* work_x;
+    double* D_uu; double* D_uv; double* D_vu; double* D_vv;
+    double* time;          /* may be NULL */
+    unsigned int* sync;
+} getm_split2d_fields;
+
+int getm_split2d_substep(const getm_split2d_fields* f, int nx, int ny, int halox, int haloy, int mixed,
+                         int ufirst, int accumulate, int friction, double timestep, double Dmin, double Dcrit,
+                         getm_advection* uadv, getm_grid* ugrid, getm_grid* uugrid, getm_grid* uvgrid,
+                         int uadv_ufirst, getm_advection* vadv, getm_grid* vgrid, getm_grid* vugrid,
+                         getm_grid* vvgrid, int vadv_ufirst, cudaStream_t stream);
 
 /* ---- domain totals (compensated budget sums) -----------------------------
  * Replaces python/pygetm/simulation.py:1409-1444 (Simulation.totals: total

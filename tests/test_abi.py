@@ -84,3 +84,31 @@ def test_product_path_has_no_fallback(monkeypatch, tmp_path):
             raise AssertionError("import succeeded without the library")
     finally:
         sys.modules["getm_gb300._lib"] = saved
+
+
+def test_split2d_fields_layout_matches_header():
+    """getm_split2d_fields: the ctypes mirror has the header's members in the
+    header's order (all pointers)."""
+    from getm_gb300 import _pygetm
+
+    src = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    body = re.search(r"typedef struct getm_split2d_fields\s*\{(.*?)\}\s*getm_split2d_fields;", src, flags=re.S)
+    assert body
+    names = []
+    for decl in body.group(1).split(";"):
+        decl = decl.strip()
+        if decl:
+            assert "*" in decl, decl
+            names.append(decl.split("*")[-1].strip())
+    assert tuple(names) == _pygetm.SPLIT2D_FIELDS
+    assert ctypes.sizeof(_pygetm.Split2DFields) == 8 * len(names)
+
+
+def test_split2d_substep_rejects_missing_fields():
+    from getm_gb300 import _lib, _pygetm
+
+    f = _pygetm.Split2DFields()
+    args = [ctypes.byref(f), 20, 20, 2, 2, 0, 1, 1, 1, 10.0, 0.02, 0.1] + [None] * 4 + [0] + [None] * 4 + [0, None]
+    assert _lib.lib.getm_split2d_substep(*args) == 1
+    args[0] = None
+    assert _lib.lib.getm_split2d_substep(*args) == 1

@@ -55,7 +55,7 @@ _SIGS = {
     "getm_vertical_diffusion_finalize": "p",
     "getm_vertical_diffusion_prepare": "piiidpddppps",
     "getm_vertical_diffusion_apply": "piiipppppps",
-    "getm_vertical_diffusion_batch": "iiippddppipppps",
+    "getm_vertical_diffusion_batch": "iiippddppippppps",
     "getm_grid_interp_x": "iiippis",
     "getm_grid_interp_y": "iiippis",
     "getm_grid_interp_z": "iiiippis",
@@ -99,7 +99,7 @@ _SIGS = {
     "getm_density_buoyancy": "ippppps",
     "getm_launch_count": "p",
     "getm_advection_apply_3d_batch_f32": "ppppippppppdpppips",
-    "getm_vertical_diffusion_batch_f32": "iiippddppipppps",
+    "getm_vertical_diffusion_batch_f32": "iiippddppippppps",
     "getm_grid_interp_x_f32": "iiippis",
     "getm_grid_interp_y_f32": "iiippis",
     "getm_grid_interp_z_f32": "iiiippis",

@@ -199,11 +199,15 @@ __global__ void __launch_bounds__(256) hpass_x_inc_kernel(HPassArgs<S> a)
     hpass_x_inc_body<S>(a, blockIdx.x, (long long)blockIdx.y * blockDim.y + threadIdx.y, threadIdx.x);
 }
 
-template <typename S>
-__global__ void __launch_bounds__(32 * HY_BY) hpass_y_inc_kernel(HPassArgs<S> a)
+template <typename S, int NT>
+__global__ void __launch_bounds__(256) hpass_y_march_kernel(HPassArgs<S> a, int nchunk)
 {
-    __shared__ YIncSmem<S> sm;
-    hpass_y_inc_body<S>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y, sm);
+    const int w = blockIdx.y * blockDim.y + threadIdx.y;
+    const int chunk = w % nchunk, k = w / nchunk;
+    if (k >= a.nk) return;  // whole warp
+    // one sweep per group of NT tracers; with no tracers one sweep updates h
+    for (int t0 = 0; t0 == 0 || t0 < a.ntracer; t0 += NT)
+        hpass_y_march_body<S, NT>(a, blockIdx.x, chunk, k, threadIdx.x, t0);
 }
 
 // Launch one horizontal pass in increment form (any storage type S).
@@ -216,9 +220,11 @@ static int launch_hpass_inc(int direction, HPassArgs<S>& a, cudaStream_t stream)
         dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up((long long)a.ny_ * a.nk, 8));
         hpass_x_inc_kernel<S><<<grid, block, 0, stream>>>(a);
     } else {
-        dim3 block(32, HY_BY);
-        dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_ + 1, HY_STRIDE), a.nk);
-        hpass_y_inc_kernel<S><<<grid, block, 0, stream>>>(a);
+        const int nchunk = getm_div_up(a.ny_, YM_CH);
+        dim3 block(32, 8);
+        dim3 grid(getm_div_up(a.nx_, 32), getm_div_up((long long)nchunk * a.nk, 8));
+        if (a.ntracer >= 2) hpass_y_march_kernel<S, 2><<<grid, block, 0, stream>>>(a, nchunk);
+        else hpass_y_march_kernel<S, 1><<<grid, block, 0, stream>>>(a, nchunk);
     }
     GETM_CHECK_LAUNCH();
     return GETM_OK;

@@ -242,86 +242,149 @@ __device__ __forceinline__ float hx_dev(int scheme, bool up, bool uu_ok, float d
 // the segment (lanes 0-2), and all loads of a lane are independent.
 constexpr int HX_STRIDE = 31;
 
-template <typename S>
-__device__ __forceinline__ void hpass_x_inc_body(const HPassArgs<S>& a, int bx, long long row, int lane)
+// KB layers k0 .. k0+KB-1 (those below nk) of row j: the 2D fields (masks,
+// metrics) are loaded once for all of them, and every load of the KB layers
+// is issued before any value is used.
+template <typename S, int KB>
+__device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, int j, int k0, int lane)
 {
     constexpr unsigned FULL = 0xffffffffu;
     const int i0 = bx * HX_STRIDE;
     const int ia = i0 - 1 + lane;  // this lane's face (U point) and its west cell
     const int ib = ia + 1;         // the cell this lane updates (lanes 0-30)
-    if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
-    const int k = (int)(row / a.ny_);
-    const int j = (int)(row - (long long)k * a.ny_);
     const long long r2 = (long long)j * a.nx_;
-    const long long r3 = (long long)k * a.plane + r2;
     const bool jrow = j >= a.jlo && j <= a.jhi;
     const bool ain = ia >= 0 && ia < a.nx_;
     // lanes 0-2 address the points i0-2, i0+31, i0+32 just outside the lanes' range
     const int ix = lane == 0 ? i0 - 2 : i0 + 30 + lane;
     const bool xin = lane < 3 && ix >= 0 && ix < a.nx_;
+    const bool bin = lane < HX_STRIDE && ib < a.nx_;
+    // in-bounds copies of the indices for the loads
+    const int iac = min(max(ia, 0), a.nx_ - 1), ixc = min(max(ix, 0), a.nx_ - 1), ibc = min(ib, a.nx_ - 1);
+    const int um_raw = a.umask[r2 + iac];
+    const int umx_raw = a.umask[r2 + ixc];
+    const float dyf = a.dy_f[r2 + iac], idxf = a.idx_f[r2 + iac];
+    const float ahraw = a.Ah ? getm_d2f_approx(a.Ah[r2 + iac]) : 0.f;
+    const int tm = a.tmask[r2 + ibc];
+    const float iaf = a.iA_f[r2 + ibc];
+    S uraw[KB];
+    double huraw[KB], hold[KB];
+#pragma unroll
+    for (int kk = 0; kk < KB; kk++) {
+        const long long r3 = (long long)min(k0 + kk, a.nk - 1) * a.plane + r2;
+        uraw[kk] = a.u[r3 + iac];
+        huraw[kk] = a.hu[r3 + iac];
+        hold[kk] = a.h_in[r3 + ibc];
+    }
+    const int ntg = a.ntracer < 2 ? a.ntracer : 2;  // tracers of the first group
+    S fa_[KB][2], fx_[KB][2];
+#pragma unroll
+    for (int kk = 0; kk < KB; kk++) {
+        const long long r3 = (long long)min(k0 + kk, a.nk - 1) * a.plane + r2;
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            if (q < ntg) {
+                const S* __restrict__ f = a.fin[q] + r3;
+                fa_[kk][q] = f[iac];
+                fx_[kk][q] = f[ixc];
+            } else {
+                fa_[kk][q] = S(0);
+                fx_[kk][q] = S(0);
+            }
+        }
+    }
 
-    // face geometry
+    // face masks (the same for every layer)
     const bool f_in = ain && jrow && ia >= a.ilo - 1 && ia <= a.ihi;
-    const int um = ain ? a.umask[r2 + ia] : 0;
-    const int umx = xin ? a.umask[r2 + ix] : 0;
+    const int um = ain ? um_raw : 0;
+    const int umx = xin ? umx_raw : 0;
     int um_w = __shfl_up_sync(FULL, um, 1), um_e = __shfl_down_sync(FULL, um, 1);
     const int umx0 = __shfl_sync(FULL, umx, 0), umx1 = __shfl_sync(FULL, umx, 1);
     if (lane == 0) um_w = umx0;
     if (lane == 31) um_e = umx1;
-    float QU = 0.f, cfl = 0.f, ahd = 0.f;
-    bool up = false, uu_ok = false;
     const bool act = f_in && getm_flux_point(um);
-    if (act) {
-        const float uu = inc_f<S>(a.u[r3 + ia]);
-        const float huf = getm_d2f_approx(a.hu[r3 + ia]);
-        const float dyf = a.dy_f[r2 + ia], idxf = a.idx_f[r2 + ia];
-        QU = uu * huf * dyf;
-        cfl = fabsf(uu * a.dtf * idxf);
-        up = uu > 0.f;
-        uu_ok = getm_flux_point(up ? um_w : um_e);
-        if (a.Ah) ahd = -getm_d2f_approx(a.Ah[r2 + ia]) * huf * idxf * dyf;
-    }
-    const float QUe = __shfl_down_sync(FULL, QU, 1);  // east face of cell ib
+    const bool upd = bin && jrow && ib >= a.ilo && ib <= a.ihi && tm == 1;
 
-    // thickness update of cell ib
-    const bool bin = lane < HX_STRIDE && ib < a.nx_;
-    const bool upd = bin && jrow && ib >= a.ilo && ib <= a.ihi && a.tmask[r2 + ib] == 1;
-    float coef = 0.f;  // dt iA / hnew
-    if (bin) {
-        const double hold = a.h_in[r3 + ib];
-        double hnew = hold;
-        if (upd) {
-            const float iaf = a.iA_f[r2 + ib];
-            const float dh = a.dtf * (QUe - QU) * iaf;
-            hnew = hold - getm_f2d(dh);
-            coef = a.dtf * iaf / (getm_d2f_approx(hold) - dh);
-        }
-        a.h_out[r3 + ib] = hnew;
-    }
-    for (int t = 0; t < a.ntracer; t++) {
-        const S* __restrict__ f = a.fin[t] + r3;
-        const S fa = ain ? f[ia] : S(0);
-        const S fx = xin ? f[ix] : S(0);
-        S fb = __shfl_down_sync(FULL, fa, 1);  // f[ia+1]
-        const S x0 = __shfl_sync(FULL, fx, 0), x1 = __shfl_sync(FULL, fx, 1), x2 = __shfl_sync(FULL, fx, 2);
-        if (lane == 31) fb = x1;
-        const float d = inc_f<S>(fb - fa);
-        float dprev = __shfl_up_sync(FULL, d, 1), dnext = __shfl_down_sync(FULL, d, 1);
-        // the two differences the shuffles cannot supply, in one operation
-        const float e = inc_f<S>(lane == 0 ? fa - x0 : x2 - x1);
-        if (lane == 0) dprev = e;
-        if (lane == 31) dnext = e;
-        // el = QU (face - f[ia]) (east side of cell ia), er = QU (face - f[ib])
-        float el = 0.f, er = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < KB; kk++) {
+        if (k0 + kk >= a.nk) break;
+        const long long r3 = (long long)(k0 + kk) * a.plane + r2;
+        float QU = 0.f, cfl = 0.f, ahd = 0.f;
+        bool up = false, uu_ok = false;
         if (act) {
-            const float dev = hx_dev(a.scheme, up, uu_ok, dprev, d, dnext, cfl);
-            const float fd = ahd * d;
-            el = QU * (up ? dev : d + dev) + fd;
-            er = QU * (up ? dev - d : dev) + fd;
+            const float uu = inc_f<S>(uraw[kk]);
+            const float huf = getm_d2f_approx(huraw[kk]);
+            QU = uu * huf * dyf;
+            cfl = fabsf(uu * a.dtf * idxf);
+            up = uu > 0.f;
+            uu_ok = getm_flux_point(up ? um_w : um_e);
+            if (a.Ah) ahd = -ahraw * huf * idxf * dyf;
         }
-        const float el_e = __shfl_down_sync(FULL, el, 1);  // east face of cell ib, seen from ib
-        if (bin) a.fout[t][r3 + ib] = upd ? inc_add<S>(fb, -coef * (el_e - er)) : fb;
+        const float QUe = __shfl_down_sync(FULL, QU, 1);  // east face of cell ib
+
+        // thickness update of cell ib
+        float coef = 0.f;  // dt iA / hnew
+        if (bin) {
+            double hnew = hold[kk];
+            if (upd) {
+                const float dh = a.dtf * (QUe - QU) * iaf;
+                hnew = hold[kk] - getm_f2d(dh);
+                coef = a.dtf * iaf / (getm_d2f_approx(hold[kk]) - dh);
+            }
+            a.h_out[r3 + ib] = hnew;
+        }
+        // tracers two at a time (the first two preloaded with the layer)
+        for (int t = 0; t < a.ntracer; t += 2) {
+            const int nt = a.ntracer - t >= 2 ? 2 : 1;
+            S fa2[2], fx2[2];
+            if (t == 0) {
+                fa2[0] = fa_[kk][0]; fa2[1] = fa_[kk][1];
+                fx2[0] = fx_[kk][0]; fx2[1] = fx_[kk][1];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const S* __restrict__ f = a.fin[t + (q < nt ? q : 0)] + r3;
+                    fa2[q] = f[iac];
+                    fx2[q] = f[ixc];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                if (q >= nt) break;
+                const S fa = ain ? fa2[q] : S(0);
+                const S fx = xin ? fx2[q] : S(0);
+                S fb = __shfl_down_sync(FULL, fa, 1);  // f[ia+1]
+                const S x0 = __shfl_sync(FULL, fx, 0), x1 = __shfl_sync(FULL, fx, 1), x2 = __shfl_sync(FULL, fx, 2);
+                if (lane == 31) fb = x1;
+                const float d = inc_f<S>(fb - fa);
+                float dprev = __shfl_up_sync(FULL, d, 1), dnext = __shfl_down_sync(FULL, d, 1);
+                // the two differences the shuffles cannot supply, in one operation
+                const float e = inc_f<S>(lane == 0 ? fa - x0 : x2 - x1);
+                if (lane == 0) dprev = e;
+                if (lane == 31) dnext = e;
+                // el = QU (face - f[ia]) (east side of cell ia), er = QU (face - f[ib])
+                float el = 0.f, er = 0.f;
+                if (act) {
+                    const float dev = hx_dev(a.scheme, up, uu_ok, dprev, d, dnext, cfl);
+                    const float fd = ahd * d;
+                    el = QU * (up ? dev : d + dev) + fd;
+                    er = QU * (up ? dev - d : dev) + fd;
+                }
+                const float el_e = __shfl_down_sync(FULL, el, 1);  // east face of cell ib, seen from ib
+                if (bin) a.fout[t + q][r3 + ib] = upd ? inc_add<S>(fb, -coef * (el_e - er)) : fb;
+            }
+        }
     }
+}
+
+// One row (layer k, row j) of the x pass: row = k ny_ + j.
+template <typename S>
+__device__ __forceinline__ void hpass_x_inc_body(const HPassArgs<S>& a, int bx, long long row, int lane)
+{
+    if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
+    const int k = (int)(row / a.ny_);
+    const int j = (int)(row - (long long)k * a.ny_);
+    hpass_x_inc_rows<S, 1>(a, bx, j, k, lane);
 }
 
 // y-direction pass in increment form: the transpose of hpass_x_inc_kernel.
@@ -429,6 +492,147 @@ __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, 
     }
 }
 
+
+// y-direction pass in increment form, marching north.  A warp owns 32
+// columns of one layer and a chunk of YM_CH cells along y.  Walking the
+// faces j = j0-1 .. j0+YM_CH-1 it keeps the last four rows of every tracer,
+// the three differences around the face and the south face's QU and er in
+// registers, so each step issues one independent load per field and row
+// (no shared memory, no block barriers) and updates cell j from its south
+// face (the previous step) and its north face (this step).  The arithmetic
+// is that of hpass_y_inc_body, operation for operation; NT tracers are
+// marched together, larger batches in groups of NT (the face geometry is
+// reloaded per group).
+constexpr int YM_CH = 32;
+
+template <typename S, int NT>
+__device__ __forceinline__ void hpass_y_march_body(const HPassArgs<S>& a, int bx, int chunk, int k, int lane,
+                                                   int t0)
+{
+    const int i = bx * 32 + lane;
+    const long long s = a.nx_;
+    const bool icol = i < a.nx_;
+    const int ic = icol ? i : a.nx_ - 1;  // in-bounds column for the loads of idle lanes
+    const long long base = (long long)k * a.plane + ic;
+    const bool iint = icol && i >= a.ilo && i <= a.ihi;
+    const int jc0 = chunk * YM_CH;
+    const int jc1 = min(jc0 + YM_CH, a.ny_);
+    const int nt = min(NT, a.ntracer - t0);
+    const bool first_group = t0 == 0;
+    // tracers q >= nt of the group (none when ntracer is 0) read as zero
+    const S* f[NT];
+    S* fo[NT];
+#pragma unroll
+    for (int q = 0; q < NT; q++) {
+        f[q] = q < nt ? a.fin[t0 + q] + base : nullptr;
+        fo[q] = q < nt ? a.fout[t0 + q] + base : nullptr;
+    }
+    auto rowv = [&](const S* p, int j) -> S {
+        return (p && j >= 0 && j < a.ny_ && icol) ? p[(long long)j * s] : S(0);
+    };
+    auto umask_at = [&](int j) -> int { return (j >= 0 && j < a.ny_) ? a.umask[(long long)j * s + ic] : 0; };
+
+    // window at the first face j = jc0 - 1: rows j-1 .. j+1 and d(j-1), d(j)
+    S fm1[NT], f0[NT], f1[NT];
+    float dm1[NT], d0[NT], er_s[NT];
+#pragma unroll
+    for (int q = 0; q < NT; q++) {
+        fm1[q] = rowv(f[q], jc0 - 2);
+        f0[q] = rowv(f[q], jc0 - 1);
+        f1[q] = rowv(f[q], jc0);
+        dm1[q] = inc_f<S>(f0[q] - fm1[q]);
+        d0[q] = inc_f<S>(f1[q] - f0[q]);
+        er_s[q] = 0.f;
+    }
+    int m_m = umask_at(jc0 - 2), m_0 = umask_at(jc0 - 1);
+    float QU_s = 0.f;
+    // every load of step j
+    struct StepLoads {
+        int m_1, tm;
+        S f2[NT];
+        S uraw;
+        double huraw, hold;
+        float dxf, idyf, ahraw, iaf;
+    };
+    auto load_step = [&](int j) -> StepLoads {
+        StepLoads L;
+        L.m_1 = umask_at(j + 1);
+#pragma unroll
+        for (int q = 0; q < NT; q++) L.f2[q] = rowv(f[q], j + 2);
+        const long long jr = (long long)((j >= 0 && j < a.ny_) ? j : 0) * s;
+        L.uraw = a.u[base + jr];
+        L.huraw = a.hu[base + jr];
+        L.dxf = a.dy_f[jr + ic];
+        L.idyf = a.idx_f[jr + ic];
+        L.ahraw = a.Ah ? getm_d2f_approx(a.Ah[jr + ic]) : 0.f;
+        L.hold = a.h_in[base + jr];
+        L.tm = a.tmask[jr + ic];
+        L.iaf = a.iA_f[jr + ic];
+        return L;
+    };
+    // one tracer: prefetch a step ahead (more loads in flight per warp);
+    // two: the registers go to occupancy instead
+    constexpr bool PF = NT == 1;
+    StepLoads nxt = load_step(jc0 - 1);
+    for (int j = jc0 - 1; j < jc1; j++) {
+        const StepLoads cur = PF ? nxt : load_step(j);
+        if (PF) nxt = load_step(min(j + 1, jc1 - 1));
+        const int m_1 = cur.m_1;
+        const S* f2 = cur.f2;
+        const bool jin = j >= 0 && j < a.ny_;
+        const long long jr = (long long)(jin ? j : 0) * s;
+        const S uraw = cur.uraw;
+        const double huraw = cur.huraw;
+        const float dxf = cur.dxf, idyf = cur.idyf, ahraw = cur.ahraw;
+        const double hold = cur.hold;
+        const int tm = cur.tm;
+        const float iaf = cur.iaf;
+
+        // face j (between cells j and j+1)
+        const bool f_in = jin && iint && j >= a.jlo - 1 && j <= a.jhi;
+        float QU = 0.f, cfl = 0.f, ahd = 0.f;
+        bool up = false, uu_ok = false, act = false;
+        if (f_in) {
+            act = getm_flux_point(m_0);
+            if (act) {
+                const float vv = inc_f<S>(uraw);
+                const float hvf = getm_d2f_approx(huraw);
+                QU = vv * hvf * dxf;
+                cfl = fabsf(vv * a.dtf * idyf);
+                up = vv > 0.f;
+                uu_ok = getm_flux_point(up ? m_m : m_1);
+                if (a.Ah) ahd = -ahraw * hvf * idyf * dxf;
+            }
+        }
+        // cell j: south face j-1 (previous step), north face j (this step)
+        const bool upd_cell = j >= jc0 && iint && j >= a.jlo && j <= a.jhi && tm == 1;
+        float coef = 0.f;
+        double hnew = hold;
+        if (upd_cell) {
+            const float dh = a.dtf * (QU - QU_s) * iaf;
+            hnew = hold - getm_f2d(dh);
+            coef = a.dtf * iaf / (getm_d2f_approx(hold) - dh);
+        }
+        if (j >= jc0 && icol && first_group) a.h_out[base + jr] = hnew;
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            const float d1 = inc_f<S>(f2[q] - f1[q]);
+            float el = 0.f, er = 0.f;
+            if (act) {
+                const float dev = hx_dev(a.scheme, up, uu_ok, dm1[q], d0[q], d1, cfl);
+                const float fd = ahd * d0[q];
+                el = QU * (up ? dev : d0[q] + dev) + fd;
+                er = QU * (up ? dev - d0[q] : dev) + fd;
+            }
+            if (j >= jc0 && icol && q < nt) fo[q][jr] = upd_cell ? inc_add<S>(f0[q], -coef * (el - er_s[q])) : f0[q];
+            er_s[q] = er;
+            fm1[q] = f0[q]; f0[q] = f1[q]; f1[q] = f2[q];
+            dm1[q] = d0[q]; d0[q] = d1;
+        }
+        QU_s = QU;
+        m_m = m_0; m_0 = m_1;
+    }
+}
 
 // ---------------------------------------------------------------------------
 // The two passes of a FULL-split 2D advection (advection_2d_impl with split

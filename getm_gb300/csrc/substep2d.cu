@@ -300,6 +300,7 @@ int launch_substep(const SubstepArgs& a, cudaStream_t stream)
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     if (cudaLaunchKernelEx(&cfg, substep_2d_kernel<MIXED>, a) != cudaSuccess) return GETM_ERR_CUDA;
+    GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
 

@@ -47,6 +47,7 @@ struct VDArgs {
     T* var[VD_MAX_BATCH];
     const T* ea2[VD_MAX_BATCH];
     const T* ea4[VD_MAX_BATCH];
+    T* work;               // NULL, or 2 nz plane elements: elimination coefficients in global memory
 };
 
 // A layer thickness in the solve's type (the mixed form converts on the
@@ -93,8 +94,13 @@ __device__ __forceinline__ float vd_dh(const double* ho, const double* hn, long 
 template <typename T>
 constexpr int vd_smem_arrays = getm_increment_form<T> ? 3 : 2;
 
-template <typename T>
-__global__ void vd_column_kernel(VDArgs<T> a)
+// GW: the elimination coefficients ru, qu live in a.work ([k][j][i], so every
+// level is again one coalesced access) instead of shared memory, which then
+// no longer limits the number of resident columns; the increment form
+// re-reads the old values from var during the back substitution (var[k] is
+// overwritten only after it is read).
+template <typename T, bool GW>
+__global__ void __launch_bounds__(128, getm_increment_form<T> ? 8 : 1) vd_column_kernel(VDArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char vd_smem[];
     constexpr bool inc = getm_increment_form<T>;
@@ -125,9 +131,22 @@ __global__ void vd_column_kernel(VDArgs<T> a)
         return;
     }
     if (a.mask[c] != 1) return;
-    T* ru = (T*)vd_smem;                        // ru[k * nthreads + tid]
-    T* qu = ru + (size_t)nz * nthreads;
-    T* xo = qu + (size_t)nz * nthreads;         // increment form: old values
+    // ru[k * rs], qu[k * rs] (and xo[k * rs], increment form in shared memory)
+    T* ru;
+    T* qu;
+    T* xo;
+    long long rs;
+    if constexpr (GW) {
+        ru = a.work + c;
+        qu = ru + P * nz;
+        xo = a.var[0] + c;  // not used: old values are re-read from var
+        rs = P;
+    } else {
+        ru = (T*)vd_smem + tid;
+        qu = ru + (size_t)nz * nthreads;
+        xo = qu + (size_t)nz * nthreads;
+        rs = nthreads;
+    }
     for (int t = 0; t < a.ntracer; t++) {
         T* __restrict__ var = a.var[t];
         const T* ea2 = a.ea2[t];
@@ -143,7 +162,7 @@ __global__ void vd_column_kernel(VDArgs<T> a)
         T a2 = vd_h<T>(a.hn[c + k * P]) + anb;
         T a4;
         if constexpr (inc) {
-            xo[k * nthreads + tid] = vk;
+            if constexpr (!GW) xo[k * rs] = vk;
             a4 = vk * vd_dh(a.ho, a.hn, c + k * P) + (vkm1 - vk) * (aob + anb);
             if (ea2) a4 = a4 + ea2[c + k * P] * vk;
         } else {
@@ -153,8 +172,8 @@ __global__ void vd_column_kernel(VDArgs<T> a)
         if (ea4) a4 = a4 + ea4[c + k * P];
         T rk = a1 / a2;
         T qk = a4 / a2;
-        ru[k * nthreads + tid] = rk;
-        qu[k * nthreads + tid] = qk;
+        ru[k * rs] = rk;
+        qu[k * rs] = qk;
         // inner layers, diffusion.F90:247-258 and elimination :287-290
         T aoa = aob, ana = anb;                 // interface above level k-1
         T vkp1 = vk;
@@ -166,7 +185,7 @@ __global__ void vd_column_kernel(VDArgs<T> a)
             a1 = -anb;
             a2 = vd_h<T>(a.hn[c + k * P]) + ana + anb;
             if constexpr (inc) {
-                xo[k * nthreads + tid] = vk;
+                if constexpr (!GW) xo[k * rs] = vk;
                 a4 = vk * vd_dh(a.ho, a.hn, c + k * P) + (vkp1 - vk) * (aoa + ana) +
                      (vkm1 - vk) * (aob + anb);
                 if (ea2) a4 = a4 + ea2[c + k * P] * vk;
@@ -178,8 +197,8 @@ __global__ void vd_column_kernel(VDArgs<T> a)
             T den = a2 - a3 * rk;
             rk = a1 / den;
             qk = (a4 - a3 * qk) / den;
-            ru[k * nthreads + tid] = rk;
-            qu[k * nthreads + tid] = qk;
+            ru[k * rs] = rk;
+            qu[k * rs] = qk;
             aoa = aob; ana = anb;
             vkp1 = vk; vk = vkm1;
         }
@@ -201,13 +220,14 @@ __global__ void vd_column_kernel(VDArgs<T> a)
             if constexpr (inc) {
                 var[c] = vk + q0;
                 for (k = 1; k < nz; k++) {
-                    vprev = qu[k * nthreads + tid] - ru[k * nthreads + tid] * vprev;
-                    var[c + k * P] = xo[k * nthreads + tid] + vprev;
+                    vprev = qu[k * rs] - ru[k * rs] * vprev;
+                    const T x_old = GW ? var[c + k * P] : xo[k * rs];
+                    var[c + k * P] = x_old + vprev;
                 }
             } else {
                 var[c] = q0;
                 for (k = 1; k < nz; k++) {
-                    vprev = qu[k * nthreads + tid] - ru[k * nthreads + tid] * vprev;
+                    vprev = qu[k * rs] - ru[k * rs] * vprev;
                     var[c + k * P] = vprev;
                 }
             }
@@ -234,6 +254,12 @@ __global__ void vd_prepare_kernel(int nx_, int ny_, int nz, long long plane, dou
 template <typename T>
 static int vd_launch(VDArgs<T>& a, cudaStream_t stream)
 {
+    if (a.work) {
+        dim3 grid(getm_div_up(a.nx_, 128), a.ny_);
+        vd_column_kernel<T, true><<<grid, 128, 0, stream>>>(a);
+        GETM_CHECK_LAUNCH();
+        return GETM_OK;
+    }
     int threads = 128;
     const size_t per = (size_t)vd_smem_arrays<T> * a.nz * sizeof(T);
     while (threads > 32 && per * threads > 160 * 1024) threads /= 2;
@@ -241,11 +267,11 @@ static int vd_launch(VDArgs<T>& a, cudaStream_t stream)
     if (smem > 200 * 1024) return GETM_ERR_NZ;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(vd_column_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(vd_column_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     dim3 grid(getm_div_up(a.nx_, threads), a.ny_);
-    vd_column_kernel<T><<<grid, threads, smem, stream>>>(a);
+    vd_column_kernel<T, false><<<grid, threads, smem, stream>>>(a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
@@ -313,7 +339,7 @@ extern "C" int getm_vertical_diffusion_apply(getm_vertical_diffusion* d, int nx,
 template <typename T>
 static int vd_batch_impl(int nx, int ny, int nz, const int* mask, const T* nuh, double timestep, double cnpar,
                          const double* ho, const double* hn, int ntracer, const double* molecular,
-                         T* const* vars, const T* const* ea2, const T* const* ea4, cudaStream_t stream)
+                         T* const* vars, const T* const* ea2, const T* const* ea4, T* work, cudaStream_t stream)
 {
     if (nx < 1 || ny < 1 || nz < 1 || !mask || !nuh || !ho || !hn || ntracer < 1 || !vars || !molecular)
         return GETM_ERR_ARG;
@@ -322,6 +348,7 @@ static int vd_batch_impl(int nx, int ny, int nz, const int* mask, const T* nuh, 
     memset(&a, 0, sizeof(a));
     a.nx_ = nx; a.ny_ = ny; a.nz = nz; a.plane = (long long)nx * ny;
     a.mask = mask; a.nuh = nuh; a.ho = ho; a.hn = hn; a.dt = timestep; a.cnpar = cnpar;
+    a.work = work;
     int done = 0;
     do {
         int n = ntracer - done;
@@ -345,18 +372,18 @@ extern "C" int getm_vertical_diffusion_batch(int nx, int ny, int nz, const int* 
                                              const double* ho, const double* hn, int ntracer,
                                              const double* molecular, double* const* vars,
                                              const double* const* ea2, const double* const* ea4,
-                                             cudaStream_t stream)
+                                             double* work, cudaStream_t stream)
 {
     return vd_batch_impl<double>(nx, ny, nz, mask, nuh, timestep, cnpar, ho, hn, ntracer, molecular, vars, ea2, ea4,
-                                 stream);
+                                 work, stream);
 }
 
 extern "C" int getm_vertical_diffusion_batch_f32(int nx, int ny, int nz, const int* mask, const float* nuh,
                                                  double timestep, double cnpar, const double* ho,
                                                  const double* hn, int ntracer, const double* molecular,
                                                  float* const* vars, const float* const* ea2,
-                                                 const float* const* ea4, cudaStream_t stream)
+                                                 const float* const* ea4, float* work, cudaStream_t stream)
 {
     return vd_batch_impl<float>(nx, ny, nz, mask, nuh, timestep, cnpar, ho, hn, ntracer, molecular, vars, ea2, ea4,
-                                stream);
+                                work, stream);
 }

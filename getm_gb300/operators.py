@@ -220,6 +220,7 @@ class VerticalDiffusion:
     def __init__(self, grid: Grid, cnpar: float = 1.0):
         self.grid = grid
         self.cnpar = cnpar
+        self._work = {}  # dtype -> workspace of the fused column solve
         h = ctypes.c_void_p()
         call("getm_vertical_diffusion_create", grid.handle, ctypes.byref(h))
         self.p = h
@@ -260,5 +261,11 @@ class VerticalDiffusion:
         e2 = _lib.ptr_array([_p(e) for e in ea2s]) if ea2s is not None and any(e is not None for e in ea2s) else None
         e4 = _lib.ptr_array([_p(e) for e in ea4s]) if ea4s is not None and any(e is not None for e in ea4s) else None
         sfx = _sfx(nuh.all_values, *[v.all_values for v in vars])
+        # elimination coefficients of the column solves (2 nz planes, reused)
+        dt = vars[0].all_values.dtype
+        need = 2 * g.nz_ * g.ny_ * g.nx_
+        w = self._work.get(dt)
+        if w is None or w.numel() < need:
+            w = self._work[dt] = torch.empty(need, dtype=dt, device=nuh.all_values.device)
         call("getm_vertical_diffusion_batch" + sfx, g.nx_, g.ny_, g.nz_, _p(g.mask), _p(nuh), float(timestep),
-             float(self.cnpar), _p(ho), _p(g.hn), n, mol, vv, e2, e4, _s())
+             float(self.cnpar), _p(ho), _p(g.hn), n, mol, vv, e2, e4, w.data_ptr(), _s())

@@ -143,12 +143,14 @@ int getm_vertical_diffusion_apply(getm_vertical_diffusion* diff, int nx, int ny,
 /* prepare + apply fused per column (VerticalDiffusion.__call__,
  * operators.py:218-230) for ntracer fields, each with its own molecular
  * diffusivity and optional ea2/ea4 (arrays of device pointers, entries may be
- * NULL; the arrays themselves may be NULL).                                 */
+ * NULL; the arrays themselves may be NULL).  work: NULL (elimination
+ * coefficients in shared memory) or a device buffer of 2*nx*ny*nz elements
+ * of the field type (more columns resident per SM).                         */
 int getm_vertical_diffusion_batch(int nx, int ny, int nz, const int* mask, const double* nuh,
                                   double timestep, double cnpar, const double* ho,
                                   const double* hn, int ntracer, const double* molecular,
                                   double* const* vars, const double* const* ea2,
-                                  const double* const* ea4, cudaStream_t stream);
+                                  const double* const* ea4, double* work, cudaStream_t stream);
 
 /* ---- python/src/interpolation.F90:9-72 (pyx:28-31) ---------------------- */
 int getm_grid_interp_x(int nx, int ny, int nz, const double* source, double* target, int ioffset,
@@ -302,7 +304,7 @@ int getm_vertical_diffusion_batch_f32(int nx, int ny, int nz, const int* mask, c
                                       double timestep, double cnpar, const double* ho,
                                       const double* hn, int ntracer, const double* molecular,
                                       float* const* vars, const float* const* ea2,
-                                      const float* const* ea4, cudaStream_t stream);
+                                      const float* const* ea4, float* work, cudaStream_t stream);
 int getm_grid_interp_x_f32(int nx, int ny, int nz, const float* source, float* target, int ioffset,
                            cudaStream_t stream);
 int getm_grid_interp_y_f32(int nx, int ny, int nz, const float* source, float* target, int joffset,

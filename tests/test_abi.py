@@ -64,7 +64,7 @@ def test_invalid_extents_are_rejected():
     assert _lib.lib.getm_create_grid(1, 5, 1, 8, 1, 5, 2, 2, None) == 1
     # argument checks happen before any device work
     assert _lib.lib.getm_elevation2depth(10, None, None, 0.1, None, None, None) == 1
-    assert _lib.lib.getm_vertical_diffusion_batch(0, 1, 1, None, None, 1.0, 1.0, None, None, 1, None, None, None, None, None) == 1
+    assert _lib.lib.getm_vertical_diffusion_batch(0, 1, 1, None, None, 1.0, 1.0, None, None, 1, None, None, None, None, None, None) == 1
     assert _lib.lib.getm_surface_pressure_gradient(10, 10, 0, 5, 1, 5, None, None, None, None, None, None, None, None, 0.1, None, None, None) == 1
 
 

@@ -199,6 +199,13 @@ __global__ void __launch_bounds__(256) hpass_x_inc_kernel(HPassArgs<S> a)
     hpass_x_inc_body<S>(a, blockIdx.x, (long long)blockIdx.y * blockDim.y + threadIdx.y, threadIdx.x);
 }
 
+template <typename S>
+__global__ void __launch_bounds__(32 * HY_BY) hpass_y_inc_kernel(HPassArgs<S> a)
+{
+    __shared__ YIncSmem<S> sm;
+    hpass_y_inc_body<S>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y, sm);
+}
+
 template <typename S, int NT>
 __global__ void __launch_bounds__(256) hpass_y_march_kernel(HPassArgs<S> a, int nchunk)
 {
@@ -219,6 +226,12 @@ static int launch_hpass_inc(int direction, HPassArgs<S>& a, cudaStream_t stream)
         // lane 0 of the first segment handles the face west of cell 0
         dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up((long long)a.ny_ * a.nk, 8));
         hpass_x_inc_kernel<S><<<grid, block, 0, stream>>>(a);
+    } else if (a.nk < 4) {
+        // a single plane: too few columns x layers for marching warps to fill
+        // the GPU, so blocks of 32 x HY_BY threads cover tiles instead
+        dim3 block(32, HY_BY);
+        dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_ + 1, HY_STRIDE), a.nk);
+        hpass_y_inc_kernel<S><<<grid, block, 0, stream>>>(a);
     } else {
         const int nchunk = getm_div_up(a.ny_, YM_CH);
         dim3 block(32, 8);

@@ -193,10 +193,13 @@ __global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs<T> a)
     hpass_y_body<T>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y, sQ, sF);
 }
 
+// grid (segments, ceil(ny_ / 8), nk): warp (ty) of block (x, y, k) owns row j = 8 y + ty of layer k
 template <typename S>
 __global__ void __launch_bounds__(256) hpass_x_inc_kernel(HPassArgs<S> a)
 {
-    hpass_x_inc_body<S>(a, blockIdx.x, (long long)blockIdx.y * blockDim.y + threadIdx.y, threadIdx.x);
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= a.ny_) return;  // whole warp
+    hpass_x_inc_rows<S, 1>(a, blockIdx.x, j, blockIdx.z, threadIdx.x);
 }
 
 template <typename S>
@@ -224,7 +227,7 @@ static int launch_hpass_inc(int direction, HPassArgs<S>& a, cudaStream_t stream)
     if (direction == 1) {
         dim3 block(32, 8);
         // lane 0 of the first segment handles the face west of cell 0
-        dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up((long long)a.ny_ * a.nk, 8));
+        dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up(a.ny_, 8), a.nk);
         hpass_x_inc_kernel<S><<<grid, block, 0, stream>>>(a);
     } else if (a.nk < 4) {
         // a single plane: too few columns x layers for marching warps to fill
@@ -420,9 +423,10 @@ __device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const floa
             W = wv[c + (k + 1) * P];
             const float cfl = fabsf(W) * dtf / fminf(hkf, hk1f) * itf;
             const float d = fk1 - fk;
+            const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl);
             float dev;
-            if (W > 0.f) dev = getm_tvd_dev<float>(a.scheme, (k > 0) ? fkm1 : fk, fk, fk1, cfl);
-            else dev = getm_tvd_dev<float>(a.scheme, (k < nz - 2) ? fk2 : fk1, fk1, fk, cfl);
+            if (W > 0.f) dev = getm_tvd_dev_f(tf, fk1 - fk, fk - ((k > 0) ? fkm1 : fk));
+            else dev = getm_tvd_dev_f(tf, fk - fk1, fk1 - ((k < nz - 2) ? fk2 : fk1));
             el = W * (W > 0.f ? dev : d + dev);
             er = W * (W > 0.f ? dev - d : dev);
         }

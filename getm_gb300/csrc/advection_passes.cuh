@@ -225,12 +225,10 @@ __device__ __forceinline__ S inc_add(S x, float dx)
 
 // Limited face deviation from the upwind cell, given d = f[b] - f[a] across
 // the face and the differences on either side, dprev = f[a] - f[a-1] and
-// dnext = f[b+1] - f[b].
-__device__ __forceinline__ float hx_dev(int scheme, bool up, bool uu_ok, float dprev, float d, float dnext,
-                                        float cfl)
+// dnext = f[b+1] - f[b]; tf: the face's limiter constants.
+__device__ __forceinline__ float hx_dev(const TvdFaceF& tf, bool up, bool uu_ok, float dprev, float d, float dnext)
 {
-    return up ? getm_tvd_dev_d<float>(scheme, d, uu_ok ? dprev : 0.f, cfl)
-              : getm_tvd_dev_d<float>(scheme, -d, uu_ok ? -dnext : 0.f, cfl);
+    return up ? getm_tvd_dev_f(tf, d, uu_ok ? dprev : 0.f) : getm_tvd_dev_f(tf, -d, uu_ok ? -dnext : 0.f);
 }
 
 // x-direction pass in increment form.  A warp owns one row segment: lane L
@@ -333,6 +331,7 @@ __device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, 
             }
             a.h_out[r3 + ib] = hnew;
         }
+        const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl);
         // tracers two at a time (the first two preloaded with the layer)
         for (int t = 0; t < a.ntracer; t += 2) {
             const int nt = a.ntracer - t >= 2 ? 2 : 1;
@@ -365,7 +364,7 @@ __device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, 
                 // el = QU (face - f[ia]) (east side of cell ia), er = QU (face - f[ib])
                 float el = 0.f, er = 0.f;
                 if (act) {
-                    const float dev = hx_dev(a.scheme, up, uu_ok, dprev, d, dnext, cfl);
+                    const float dev = hx_dev(tf, up, uu_ok, dprev, d, dnext);
                     const float fd = ahd * d;
                     el = QU * (up ? dev : d + dev) + fd;
                     er = QU * (up ? dev - d : dev) + fd;
@@ -464,6 +463,7 @@ __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, 
     const int jx = ty == 0 ? j0 - 2 : j0 + HY_BY - 2 + ty;
     const int sxrow = ty == 0 ? 0 : HY_BY + ty;
     const bool xin = ty < 3 && icol && jx >= 0 && jx < a.ny_;
+    const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl);
     for (int t = 0; t < a.ntracer; t++) {
         const S* __restrict__ f = a.fin[t] + base;
         __syncthreads();  // previous tracer's reads of sf, sd and sx are done
@@ -480,7 +480,7 @@ __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, 
         const S fb = sf[ty + 2][tx];
         float el = 0.f, er = 0.f;
         if (act) {
-            const float dev = hx_dev(a.scheme, up, uu_ok, dprev, d, dnext, cfl);
+            const float dev = hx_dev(tf, up, uu_ok, dprev, d, dnext);
             const float fd = ahd * d;
             el = QU * (up ? dev : d + dev) + fd;
             er = QU * (up ? dev - d : dev) + fd;
@@ -614,12 +614,13 @@ __device__ __forceinline__ void hpass_y_march_body(const HPassArgs<S>& a, int bx
             coef = a.dtf * iaf / (getm_d2f_approx(hold) - dh);
         }
         if (j >= jc0 && icol && first_group) a.h_out[base + jr] = hnew;
+        const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl);
 #pragma unroll
         for (int q = 0; q < NT; q++) {
             const float d1 = inc_f<S>(f2[q] - f1[q]);
             float el = 0.f, er = 0.f;
             if (act) {
-                const float dev = hx_dev(a.scheme, up, uu_ok, dm1[q], d0[q], d1, cfl);
+                const float dev = hx_dev(tf, up, uu_ok, dm1[q], d0[q], d1);
                 const float fd = ahd * d0[q];
                 el = QU * (up ? dev : d0[q] + dev) + fd;
                 er = QU * (up ? dev - d0[q] : dev) + fd;

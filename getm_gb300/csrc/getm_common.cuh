@@ -200,6 +200,58 @@ __device__ __forceinline__ T getm_tvd_dev(int scheme, T fuu, T fu, T fd, T cfl)
     return getm_tvd_dev_d<T>(scheme, fd - fu, fu - fuu, cfl);
 }
 
+// Float form of the limited deviation without a division per field.  For
+// deltaf and deltafu of the same sign s, phi(r) deltaf with r = deltafu /
+// deltaf equals s phi_a(a, b), a = |deltaf|, b = |deltafu|, where phi_a is
+// the limiter's expression with r replaced by b and every constant term
+// multiplied by a (all five limiters are piecewise linear in r).  The terms
+// that depend only on the Courant number are formed once per face
+// (getm_tvd_face_f) and shared by every field advected through the face.
+struct TvdFaceF {
+    int scheme;
+    float half1mc;     // 0.5 (1 - cfl)
+    float lin0, lin1;  // HSIMT, P2_PDM: phi = lin0 + lin1 r
+    float rcoef, cap;  // P2_PDM: 2 / (cfl + 1e-10), 2 / (1 - cfl)
+};
+
+__device__ __forceinline__ TvdFaceF getm_tvd_face_f(int scheme, float cfl)
+{
+    TvdFaceF f;
+    f.scheme = scheme;
+    f.half1mc = 0.5f * (1.f - cfl);
+    f.lin0 = f.lin1 = 0.f;
+    f.rcoef = f.cap = 2.f;
+    if (scheme == GETM_SCHEME_HSIMT) {
+        const float kappa = 1.f - cfl;
+        const float x = 0.25f * (kappa - 1.f / 3.f / kappa);
+        f.lin0 = 0.5f + x;
+        f.lin1 = 0.5f - x;
+    } else if (scheme == GETM_SCHEME_P2_PDM) {
+        const float x = 1.f / 6.f * (1.f - 2.f * cfl);
+        f.lin0 = 0.5f + x;
+        f.lin1 = 0.5f - x;
+        f.rcoef = 2.f / (cfl + 1.e-10f);
+        f.cap = 2.f / (1.f - cfl);
+    }
+    return f;
+}
+
+__device__ __forceinline__ float getm_tvd_dev_f(const TvdFaceF& tf, float deltaf, float deltafu)
+{
+    if (!(deltaf * deltafu > 0.f)) return 0.f;
+    const float a = fabsf(deltaf), b = fabsf(deltafu);
+    float pa;
+    switch (tf.scheme) {
+    case GETM_SCHEME_HSIMT: pa = fminf(fminf(2.f * b, fmaxf(0.f, tf.lin0 * a + tf.lin1 * b)), 2.f * a); break;
+    case GETM_SCHEME_MUSCL: pa = fminf(fminf(2.f * b, 0.5f * (a + b)), 2.f * a); break;
+    case GETM_SCHEME_P2_PDM: pa = fminf(fminf(tf.rcoef * b, tf.lin0 * a + tf.lin1 * b), tf.cap * a); break;
+    case GETM_SCHEME_SPLMAX13: pa = fminf(fminf(2.f * b, 1.f / 3.f * fmaxf(a + 2.f * b, 2.f * a + b)), 2.f * a); break;
+    case GETM_SCHEME_SUPERBEE: pa = fmaxf(fminf(2.f * b, a), fminf(b, 2.f * a)); break;
+    default: pa = 0.f; break;
+    }
+    return tf.half1mc * copysignf(pa, deltaf);
+}
+
 __device__ __forceinline__ bool getm_flux_point(int m) { return m == 1 || m == 2; }
 
 // u*u + v*v rounded after each operation (no contraction into an FMA), so

@@ -80,6 +80,11 @@ _SIGS = {
     "getm_accumulate_2d": "lpppps",
     "getm_surface_elevation_fused": "iiiipppppppppds",
     "getm_split2d_substep": "piiiiiiiidddppppippppis",
+    "getm_update_depth_3d": "piiis",
+    "getm_transport_3d_finish": "iiipppppps",
+    "getm_transport_3d_finish_f32": "iiipppppps",
+    "getm_velocities_3d": "lpppppps",
+    "getm_velocities_3d_f32": "lpppppps",
     "getm_open_boundary_elevation": "iiipppppppppppppdps",
     "getm_open_boundary_tracers": "iiiiiiippppppipps",
     "getm_open_boundary_tracers_f32": "iiiiiiippppppipps",

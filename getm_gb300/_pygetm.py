@@ -346,3 +346,54 @@ def split2d_substep(fields: Split2DFields, T, mixed, ufirst, accumulate, frictio
          int(bool(ufirst)), int(bool(accumulate)), int(bool(friction)), float(timestep), float(Dmin), float(Dcrit),
          uadv.p, U.handle, U.ugrid.handle, U.vgrid.handle, int(uadv.ufirst),
          vadv.p, V.handle, V.ugrid.handle, V.vgrid.handle, int(vadv.ufirst), _s())
+
+
+def transport_3d_finish(vel3d, hn, tp2d, D, tp3d, dev):
+    """Momentum.advance_3d_transport after the vertical diffusion
+    (momentum.py:1199-1210): tp3d = vel3d hn, dev = (sum_k tp3d - tp2d) / D,
+    tp3d -= dev hn."""
+    g = tp3d.grid
+    sfx = _sfx(vel3d.all_values, tp3d.all_values)
+    call("getm_transport_3d_finish" + sfx, g.nx_, g.ny_, tp3d.all_values.shape[0], _p(vel3d), _p(hn), _p(tp2d), _p(D),
+         _p(tp3d), _p(dev), _s())
+
+
+def velocities_3d(pk, qk, uk, vk):
+    """uk = pk / hn_U, vk = qk / hn_V (momentum.py:909-910)."""
+    sfx = _sfx(pk.all_values, qk.all_values, uk.all_values, vk.all_values)
+    call("getm_velocities_3d" + sfx, pk.all_values.numel(), _p(pk), _p(pk.grid.hn), _p(qk), _p(qk.grid.hn), _p(uk),
+         _p(vk), _s())
+
+
+# field order of getm_depth3d_fields (include/getm_gb300.h)
+DEPTH3D_FIELDS = (
+    "dga", "mask_t", "mask_u", "mask_v", "mask_x", "Dclip_t", "Dclip_u", "Dclip_v", "Dclip_x", "H_t", "H_u", "H_v",
+    "hn_t", "hn_u", "hn_v", "hn_x", "ho_t", "ho_u", "ho_v", "zc_t", "zc_u", "zc_v", "zf_t", "zf_u", "zf_v", "depth",
+    "h_T_half", "hn_uu", "hn_vv", "hn_uv", "hn_vu",
+)
+
+
+class Depth3DFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in DEPTH3D_FIELDS]
+
+
+def depth3d_fields(T, dga, h_T_half, depth=None) -> Depth3DFields:
+    """Fields of getm_update_depth_3d for the grid tree of T (``depth``: the
+    T centre depths, or None)."""
+    U, V, X = T.ugrid, T.vgrid, T.xgrid
+    assert dga.is_contiguous() and dga.dtype == torch.float64
+    arrays = dict(dga=dga, mask_t=T.mask, mask_u=U.mask, mask_v=V.mask, mask_x=X.mask, Dclip_t=T.Dclip,
+                  Dclip_u=U.Dclip, Dclip_v=V.Dclip, Dclip_x=X.Dclip, H_t=T.H, H_u=U.H, H_v=V.H, hn_t=T.hn, hn_u=U.hn,
+                  hn_v=V.hn, hn_x=X.hn, ho_t=T.ho, ho_u=U.ho, ho_v=V.ho, zc_t=T.zc, zc_u=U.zc, zc_v=V.zc, zf_t=T.zf,
+                  zf_u=U.zf, zf_v=V.zf, depth=depth, h_T_half=h_T_half, hn_uu=U.ugrid.hn, hn_vv=V.vgrid.hn,
+                  hn_uv=U.vgrid.hn, hn_vu=V.ugrid.hn)
+    f = Depth3DFields()
+    for n in DEPTH3D_FIELDS:
+        a = arrays[n]
+        setattr(f, n, None if a is None else (a.data_ptr() if isinstance(a, torch.Tensor) else _p(a)))
+    return f
+
+
+def update_depth_3d(fields: Depth3DFields, T):
+    """Simulation.update_depth, 3D part (simulation.py:1588-1630)."""
+    call("getm_update_depth_3d", ctypes.byref(fields), T.nx_, T.ny_, T.nz_, _s())

@@ -8,6 +8,8 @@
 // (w_momentum_3d) use one thread per column.
 #include "split2d_ops.cuh"
 
+#include <type_traits>
+
 #define EW_THREADS 256
 
 // momentum.F90:12-77
@@ -365,6 +367,102 @@ extern "C" int getm_bottom_shear_velocity(int nx, int ny, int imin, int imax, in
     bottom_shear_velocity_kernel<<<grid, 128, 0, stream>>>(nx, ny, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, uk_bot, vk_bot, rru, rrv, taubx, tauby, ustar2_b);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
+}
+
+// Momentum.advance_3d_transport after the vertical diffusion
+// (python/pygetm/momentum.py:1199-1210): tp3d = vel hn, dev = (sum_k tp3d -
+// tp2d) / D, tp3d -= dev hn, as one sweep per column (the sum in FP64 in
+// both forms).  FP64 form (T double): the same roundings as the separate
+// array operations (products and differences not contracted); the sum runs
+// bottom to top.  Mixed form (T float): the products in float from the
+// thickness narrowed on the integer pipe.
+template <typename T>
+__global__ void transport_3d_finish_kernel(long long plane, int nz, const T* vel, const double* hn,
+                                           const double* tp2d, const double* D, T* tp3d, double* dev)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= plane) return;
+    double s = 0.0;
+    for (int k = 0; k < nz; k++) {
+        const long long q = p + k * plane;
+        T x;
+        if constexpr (std::is_same<T, double>::value) x = __dmul_rn(vel[q], hn[q]);
+        else x = vel[q] * getm_d2f_approx(hn[q]);
+        tp3d[q] = x;
+        s = s + (double)x;
+    }
+    const double d = (s - tp2d[p]) / D[p];
+    dev[p] = d;
+    for (int k = 0; k < nz; k++) {
+        const long long q = p + k * plane;
+        if constexpr (std::is_same<T, double>::value) tp3d[q] = __dsub_rn(tp3d[q], __dmul_rn(d, hn[q]));
+        else tp3d[q] = tp3d[q] - getm_d2f_approx(d) * getm_d2f_approx(hn[q]);
+    }
+}
+
+// Momentum.update_diagnostics (momentum.py:909-910): uk = pk / hn, vk = qk /
+// hn over n points (mixed form: in float).
+template <typename T>
+__global__ void velocities_3d_kernel(long long n, const T* pk, const double* hnu, const T* qk, const double* hnv,
+                                     T* uk, T* vk)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    if constexpr (std::is_same<T, double>::value) {
+        uk[q] = pk[q] / hnu[q];
+        vk[q] = qk[q] / hnv[q];
+    } else {
+        uk[q] = pk[q] / getm_d2f_approx(hnu[q]);
+        vk[q] = qk[q] / getm_d2f_approx(hnv[q]);
+    }
+}
+
+template <typename T>
+static int transport_3d_finish_impl(int nx, int ny, int nz, const T* vel, const double* hn, const double* tp2d,
+                                    const double* D, T* tp3d, double* dev, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || !vel || !hn || !tp2d || !D || !tp3d || !dev) return GETM_ERR_ARG;
+    const long long plane = (long long)nx * ny;
+    transport_3d_finish_kernel<T><<<getm_div_up(plane, 128), 128, 0, stream>>>(plane, nz, vel, hn, tp2d, D, tp3d, dev);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_transport_3d_finish(int nx, int ny, int nz, const double* vel, const double* hn,
+                                        const double* tp2d, const double* D, double* tp3d, double* dev,
+                                        cudaStream_t stream)
+{
+    return transport_3d_finish_impl<double>(nx, ny, nz, vel, hn, tp2d, D, tp3d, dev, stream);
+}
+
+extern "C" int getm_transport_3d_finish_f32(int nx, int ny, int nz, const float* vel, const double* hn,
+                                            const double* tp2d, const double* D, float* tp3d, double* dev,
+                                            cudaStream_t stream)
+{
+    return transport_3d_finish_impl<float>(nx, ny, nz, vel, hn, tp2d, D, tp3d, dev, stream);
+}
+
+template <typename T>
+static int velocities_3d_impl(long long n, const T* pk, const double* hnu, const T* qk, const double* hnv, T* uk,
+                              T* vk, cudaStream_t stream)
+{
+    if (n < 0 || (n > 0 && (!pk || !hnu || !qk || !hnv || !uk || !vk))) return GETM_ERR_ARG;
+    if (n == 0) return GETM_OK;
+    velocities_3d_kernel<T><<<getm_div_up(n, 256), 256, 0, stream>>>(n, pk, hnu, qk, hnv, uk, vk);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_velocities_3d(long long n, const double* pk, const double* hnu, const double* qk,
+                                  const double* hnv, double* uk, double* vk, cudaStream_t stream)
+{
+    return velocities_3d_impl<double>(n, pk, hnu, qk, hnv, uk, vk, stream);
+}
+
+extern "C" int getm_velocities_3d_f32(long long n, const float* pk, const double* hnu, const float* qk,
+                                      const double* hnv, float* uk, float* vk, cudaStream_t stream)
+{
+    return velocities_3d_impl<float>(n, pk, hnu, qk, hnv, uk, vk, stream);
 }
 
 // momentum.F90:323-340: rows jmin..jmax, every i (T: type of un and Uo)

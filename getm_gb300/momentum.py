@@ -306,8 +306,7 @@ class Momentum:
             self.coriolis(self.pk, self.corqk, True)
             self.coriolis(self.qk, self.corpk, False)
         _pygetm.w_momentum_3d(self.pk, self.qk, timestep, self.ww)
-        torch.div(self.pk.all_values, self.pk.grid.hn.all_values, out=self.uk.all_values)
-        torch.div(self.qk.all_values, self.qk.grid.hn.all_values, out=self.vk.all_values)
+        _pygetm.velocities_3d(self.pk, self.qk, self.uk, self.vk)
         _pygetm.shear_frequency(self.uk, self.vk, self.SS)
         if self.u_bot is self._u_bot64:
             self._u_bot64.all_values.copy_(self.uk.all_values[0])
@@ -346,13 +345,7 @@ class Momentum:
         visc = viscosity.interp(visc_target if visc_target is not None else grid)
         self._vertical_diffusion(visc, timestep, vel3d, molecular=self.avmmol, ea2=self.ea2, ea4=self.ea4,
                                  use_ho=True)
-        torch.mul(vel3d.all_values, grid.hn.all_values, out=tp3d.all_values)
-        if tp3d.dtype == torch.float64:
-            torch.sum(tp3d.all_values, dim=0, out=dev.all_values)
-        else:
-            dev.all_values.copy_(tp3d.all_values.sum(dim=0, dtype=torch.float64))
-        dev.all_values.sub_(tp2d.all_values)
-        dev.all_values.div_(grid.D.all_values)
-        tp3d.all_values.sub_(dev.all_values * grid.hn.all_values)
+        # tp3d = vel3d hn; dev = (sum_k tp3d - tp2d) / D; tp3d -= dev hn
+        _pygetm.transport_3d_finish(vel3d, grid.hn, tp2d, grid.D, tp3d, dev)
         if self._ob is not None:  # momentum.py:1211-1212
             self._ob.mirror("U" if tp3d is self.pk else "V", tp3d)

@@ -477,7 +477,18 @@ class Simulation:
         V.ugrid.D.all_values[:, :] = U.vgrid.D.all_values
 
     def _update_depth_3d(self):
-        """The 3D part of update_depth (simulation.py:1588-1630)."""
+        """The 3D part of update_depth (simulation.py:1588-1630) as two
+        column sweeps (getm_update_depth_3d)."""
+        if self.fused_2d:
+            if getattr(self, "_depth3d", None) is None:
+                depth = self.depth if self.runtype == RunType.BAROCLINIC else None
+                self._depth3d = _pygetm.depth3d_fields(self.T, self.dga, self.h_T_half, depth)
+            _pygetm.update_depth_3d(self._depth3d, self.T)
+            return
+        self._update_depth_3d_ops()
+
+    def _update_depth_3d_ops(self):
+        """The 3D part of update_depth as separate array operations."""
         T, U, V, X = self.T, self.U, self.V, self.X
         T.ho.all_values.copy_(T.hn.all_values)
         U.ho.all_values.copy_(U.hn.all_values)

@@ -472,6 +472,48 @@ int getm_open_boundary_depth(int n, const int* srcT, const int* tgt, const doubl
                              const double* H, const int* mask, double Dmin, double Dcrit, double* work,
                              double* D, double* alpha, cudaStream_t stream);
 
+/* ---- fused 3D momentum array operations ------------------------------------
+ * Momentum.advance_3d_transport after the vertical diffusion
+ * (python/pygetm/momentum.py:1199-1210) as one sweep per column: tp3d = vel
+ * hn, dev = (sum_k tp3d - tp2d) / D, tp3d -= dev hn (the sum in FP64).  The
+ * FP64 entry rounds every product and difference as the separate array
+ * operations do (the sum runs bottom to top); the _f32 entry (mixed form)
+ * forms the products in float.  nx, ny: full extents; tp2d, D, dev: 2D.   */
+int getm_transport_3d_finish(int nx, int ny, int nz, const double* vel, const double* hn,
+                             const double* tp2d, const double* D, double* tp3d, double* dev,
+                             cudaStream_t stream);
+int getm_transport_3d_finish_f32(int nx, int ny, int nz, const float* vel, const double* hn,
+                                 const double* tp2d, const double* D, float* tp3d, double* dev,
+                                 cudaStream_t stream);
+/* Momentum.update_diagnostics (momentum.py:909-910): uk = pk / hn_U,
+ * vk = qk / hn_V over n points (_f32: the division in float).              */
+int getm_velocities_3d(long long n, const double* pk, const double* hnu, const double* qk,
+                       const double* hnv, double* uk, double* vk, cudaStream_t stream);
+int getm_velocities_3d_f32(long long n, const float* pk, const double* hnu, const float* qk,
+                           const double* hnv, float* uk, float* vk, cudaStream_t stream);
+
+/* Simulation.update_depth, 3D part (python/pygetm/simulation.py:1588-1630)
+ * with Sigma coordinates (vertical_coordinates.py:106-113), in two column
+ * sweeps with the arithmetic of the separate array operations: ho = hn (T,
+ * U, V); hn = dga Dclip where the mask is non-zero (T, U, V, X);
+ * thickness2vertical_coordinates of T, U, V (zc, zf); thickness2center_depth
+ * of T into depth (when not NULL); h_T_half = (ho + hn) / 2 and the
+ * thicknesses of the UU, VV, UV, VU grids.  dga: nz device values.  nx, ny:
+ * full T extents (X fields nx+1 x ny+1).                                    */
+typedef struct getm_depth3d_fields {
+    const double* dga;
+    const int* mask_t; const int* mask_u; const int* mask_v; const int* mask_x;
+    const double* Dclip_t; const double* Dclip_u; const double* Dclip_v; const double* Dclip_x;
+    const double* H_t; const double* H_u; const double* H_v;
+    double* hn_t; double* hn_u; double* hn_v; double* hn_x;
+    double* ho_t; double* ho_u; double* ho_v;
+    double* zc_t; double* zc_u; double* zc_v; double* zf_t; double* zf_u; double* zf_v;
+    double* depth;
+    double* h_T_half; double* hn_uu; double* hn_vv; double* hn_uv; double* hn_vu;
+} getm_depth3d_fields;
+
+int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny, int nz, cudaStream_t stream);
+
 /* ---- one 2D substep as one launch -----------------------------------------
  * Replaces, for a substep of python/pygetm/simulation.py:291-325
  * (Simulation.advance) that is not followed by a 3D step, the sequence

@@ -402,41 +402,57 @@ __device__ void w_substep(const WPassArgs<T>& a, long long c, const T* wv, const
 // dh = dtk (w_k - w_{k-1}), the reference update equals
 //     f + dtk ((w_k - W_k - w_{k-1} + W_{k-1}) f - e_k + e'_{k-1}) / hn
 // with e_k = W_k (face_k - f_k) and e'_{k-1} = W_{k-1} (face_{k-1} - f_k).
+// NT fields advected with the same w_var share every thickness and velocity
+// load and the face constants; each field keeps its own window.
+template <int NT>
 __device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const float* wv, const double* hs,
-                              const float* fs, double* hd, float* fdst, double dtk, double itersm1)
+                              const float* const (&fs)[NT], double* hd, float* const (&fdst)[NT], double dtk,
+                              double itersm1)
 {
     const long long P = a.plane;
     const int nz = a.nz;
     const float dtkf = (float)dtk, itf = (float)itersm1, dtf = (float)a.dt;
-    float fkm1 = 0.f, fk = fs[c], fk1 = (nz > 1) ? fs[c + P] : 0.f;
+    float fkm1[NT], fk[NT], fk1[NT], erm[NT];  // erm: e'_{k-1}, interface below, deviation from level k
+#pragma unroll
+    for (int q = 0; q < NT; q++) {
+        fkm1[q] = 0.f;
+        fk[q] = fs[q][c];
+        fk1[q] = (nz > 1) ? fs[q][c + P] : 0.f;
+        erm[q] = 0.f;
+    }
     double hk = hs[c], hk1 = (nz > 1) ? hs[c + P] : 0.0;
     float hkf = getm_d2f_approx(hk), hk1f = getm_d2f_approx(hk1);
-    float erm = 0.f;   // e'_{k-1}: interface below, deviation from level k
     float Wm = 0.f;    // W_{k-1} (0 below the bottom level)
     float wkm1 = a.w[c];
     for (int k = 0; k < nz; k++) {
-        float fk2 = 0.f;
+        float fk2[NT];
         double hk2 = 0.0;
-        if (k + 2 < nz) { fk2 = fs[c + (k + 2) * P]; hk2 = hs[c + (k + 2) * P]; }
-        float el = 0.f, er = 0.f, W = 0.f;
-        if (k < nz - 1) {
-            W = wv[c + (k + 1) * P];
-            const float cfl = fabsf(W) * dtf / fminf(hkf, hk1f) * itf;
-            const float d = fk1 - fk;
-            const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl);
-            float dev;
-            if (W > 0.f) dev = getm_tvd_dev_f(tf, fk1 - fk, fk - ((k > 0) ? fkm1 : fk));
-            else dev = getm_tvd_dev_f(tf, fk - fk1, fk1 - ((k < nz - 2) ? fk2 : fk1));
-            el = W * (W > 0.f ? dev : d + dev);
-            er = W * (W > 0.f ? dev - d : dev);
-        }
+#pragma unroll
+        for (int q = 0; q < NT; q++) fk2[q] = (k + 2 < nz) ? fs[q][c + (k + 2) * P] : 0.f;
+        if (k + 2 < nz) hk2 = hs[c + (k + 2) * P];
+        const float W = (k < nz - 1) ? wv[c + (k + 1) * P] : 0.f;
         const float wk = a.w[c + (k + 1) * P];
+        const float cfl = fabsf(W) * dtf / fminf(hkf, hk1f) * itf;
+        const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl);
         const float dh = dtkf * (wk - wkm1);
         const double hn = hk - getm_f2d(dh);
         hd[c + k * P] = hn;
-        fdst[c + k * P] = fk + dtkf * (((wk - W) - (wkm1 - Wm)) * fk - el + erm) / (hkf - dh);
-        erm = er; Wm = W; wkm1 = wk;
-        fkm1 = fk; fk = fk1; fk1 = fk2;
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            float el = 0.f, er = 0.f;
+            if (k < nz - 1) {
+                const float d = fk1[q] - fk[q];
+                float dev;
+                if (W > 0.f) dev = getm_tvd_dev_f(tf, fk1[q] - fk[q], fk[q] - ((k > 0) ? fkm1[q] : fk[q]));
+                else dev = getm_tvd_dev_f(tf, fk[q] - fk1[q], fk1[q] - ((k < nz - 2) ? fk2[q] : fk1[q]));
+                el = W * (W > 0.f ? dev : d + dev);
+                er = W * (W > 0.f ? dev - d : dev);
+            }
+            fdst[q][c + k * P] = fk[q] + dtkf * (((wk - W) - (wkm1 - Wm)) * fk[q] - el + erm[q]) / (hkf - dh);
+            erm[q] = er;
+            fkm1[q] = fk[q]; fk[q] = fk1[q]; fk1[q] = fk2[q];
+        }
+        Wm = W; wkm1 = wk;
         hk = hk1; hk1 = hk2;
         hkf = hk1f; hk1f = getm_d2f_approx(hk2);
     }
@@ -479,7 +495,7 @@ __device__ __forceinline__ int w_iters_from(double cfl)
 
 // Thread per column.
 template <typename T>
-__global__ void __launch_bounds__(128) wpass_kernel(WPassArgs<T> a)
+__global__ void __launch_bounds__(128, getm_increment_form<T> ? 8 : 1) wpass_kernel(WPassArgs<T> a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
@@ -487,8 +503,13 @@ __global__ void __launch_bounds__(128) wpass_kernel(WPassArgs<T> a)
     const long long c = (long long)j * a.nx_ + i;
     if (a.tmask[c] != 1) return;
     const int itersmax = 200;
-    const long long P = a.plane;
-    for (int t = 0; t < a.ntracer; t++) {
+    // mixed form: two consecutive fields with the same w_var are stepped
+    // together (the sub-step count depends only on w_var and h); the second
+    // one's intermediate sub-steps use the upper half of the column work
+    // array, which holds n3 doubles
+    constexpr bool inc = getm_increment_form<T>;
+    for (int t = 0; t < a.ntracer;) {
+        const int nt = (inc && t + 1 < a.ntracer && a.wvar[t + 1] == a.wvar[t]) ? 2 : 1;
         const T* wv = a.wvar[t];
         T* f = a.f[t];
         int iters = 1;
@@ -512,15 +533,30 @@ __global__ void __launch_bounds__(128) wpass_kernel(WPassArgs<T> a)
                 }
             }
             // The last sub-step writes the tracer in place and the thickness
-            // into haux (the stage's h_in must survive for the next tracer).
+            // into haux (the stage's h_in must survive for the next tracer);
+            // the last tracer's last sub-step writes the thickness straight
+            // into h_out, the pass's result.
             T* fd = (it == iters) ? f : a.faux;
-            if constexpr (getm_increment_form<T>) w_substep_f32(a, c, wv, hs, fs, a.haux, fd, dtk, itersm1);
-            else w_substep(a, c, wv, hs, fs, a.haux, fd, dtk, itersm1);
+            double* hd = (it == iters && t + nt == a.ntracer) ? a.h_out : a.haux;
+            if constexpr (inc) {
+                if (nt == 2) {
+                    T* f2 = a.f[t + 1];
+                    T* faux2 = a.faux + a.plane * a.nz;
+                    const T* const fs2[2] = {fs, (it == 1) ? f2 : faux2};
+                    T* const fd2[2] = {fd, (it == iters) ? f2 : faux2};
+                    w_substep_f32<2>(a, c, wv, hs, fs2, hd, fd2, dtk, itersm1);
+                } else {
+                    const T* const fs1[1] = {fs};
+                    T* const fd1[1] = {fd};
+                    w_substep_f32<1>(a, c, wv, hs, fs1, hd, fd1, dtk, itersm1);
+                }
+            } else {
+                w_substep(a, c, wv, hs, fs, hd, fd, dtk, itersm1);
+            }
             it++;
         }
+        t += nt;
     }
-    // h after the pass = thickness of the last tracer's final sub-step
-    for (int k = 0; k < a.nz; k++) a.h_out[c + k * P] = a.haux[c + k * P];
 }
 
 // Copy h_in -> h_out for the columns the w pass does not touch, so h_out is a

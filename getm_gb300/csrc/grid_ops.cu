@@ -220,8 +220,9 @@ extern "C" int getm_multiply_add(int n, double* tgt, const double* add, double s
 
 // wrapper.F90:409-426: column recursion, thread per column
 // thickness2vertical_coordinates of the column at p (wrapper.F90:409-426)
-__device__ __forceinline__ void t2vc_column(long long plane, int nz, long long p, const double* bd, const double* h,
-                                            double* zc, double* zf)
+__device__ __forceinline__ void t2vc_column(long long plane, int nz, long long p, const double* __restrict__ bd,
+                                            const double* __restrict__ h, double* __restrict__ zc,
+                                            double* __restrict__ zf)
 {
     double zci = -bd[p] + 0.5 * h[p];
     zc[p] = zci;
@@ -261,7 +262,8 @@ extern "C" int getm_thickness2vertical_coordinates(int nx, int ny, int nz, const
 }
 
 // wrapper.F90:395-407: depth of the layer centres below the surface
-__device__ __forceinline__ void t2cd_column(long long plane, int nz, long long p, const double* h, double* out)
+__device__ __forceinline__ void t2cd_column(long long plane, int nz, long long p, const double* __restrict__ h,
+                                            double* __restrict__ out)
 {
     double hk1 = h[p + (nz - 1) * plane];
     double o = 0.5 * hk1;
@@ -348,14 +350,14 @@ extern "C" int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax
 
 // ---------------------------------------------------------------------------
 // Simulation.update_depth, 3D part (python/pygetm/simulation.py:1588-1630) in
-// two column sweeps.  Sweep 1, per column of the T/U/V grids (and of the X
-// grid): ho = hn; hn = dga Dclip where the mask is non-zero (Sigma
-// coordinates, vertical_coordinates.py:106-113); the vertical coordinates
-// of T, U, V and the T centre depths from the new hn.  Sweep 2 needs the new
-// thicknesses of neighbouring columns: h_T_half = (ho + hn) / 2 on T and the
+// three launches.  1 (one thread per point and level of every grid): ho = hn;
+// hn = dga Dclip where the mask is non-zero (Sigma coordinates,
+// vertical_coordinates.py:106-113).  2 (per point and level, needs the new
+// thicknesses of neighbouring columns): h_T_half = (ho + hn) / 2 on T and the
 // thicknesses of the advection velocity grids (UU from h_T_half at i+1, VV
-// at j+1, UV = VU = X at (j+1, i+1)).  Same arithmetic as the separate array
-// operations.
+// at j+1, UV = VU = X at (j+1, i+1)).  3 (per column): the vertical
+// coordinates of T, U, V and the T centre depths.  Same arithmetic as the
+// separate array operations.
 // ---------------------------------------------------------------------------
 struct Depth3DArgs {
     int nx, ny, nz;
@@ -371,57 +373,61 @@ struct Depth3DArgs {
     double *hhalf, *hnuu, *hnvv, *hnuv, *hnvu;
 };
 
-__device__ __forceinline__ void sigma_column(const Depth3DArgs& a, long long p, long long plane, const int* m,
-                                             const double* D, double* hn, double* ho)
+__device__ __forceinline__ void sigma_point(double dga, long long p, long long q, const int* __restrict__ m,
+                                            const double* __restrict__ D, double* __restrict__ hn,
+                                            double* __restrict__ ho)
 {
-    const bool wet = m[p] != 0;
-    const double Dp = D[p];
-    for (int k = 0; k < a.nz; k++) {
-        const long long q = p + k * plane;
-        const double old = hn[q];
-        if (ho) ho[q] = old;
-        hn[q] = wet ? a.dga[k] * Dp : old;
-    }
+    const double old = hn[q];
+    if (ho) ho[q] = old;
+    hn[q] = m[p] != 0 ? dga * D[p] : old;
 }
 
-__global__ void depth_3d_sweep1_kernel(Depth3DArgs a)
+// grid (ceil((nx + 1) / 128), ny + 1, nz)
+__global__ void depth_3d_sigma_kernel(Depth3DArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const double dga = a.dga[k];
+    if (i <= a.nx && j <= a.ny) {  // X grid: (ny + 1) x (nx + 1)
+        const long long px = (long long)j * (a.nx + 1) + i;
+        sigma_point(dga, px, px + k * a.planex, a.mx, a.Dx, a.hnx, nullptr);
+    }
+    if (i >= a.nx || j >= a.ny) return;
+    const long long p = (long long)j * a.nx + i, q = p + k * a.plane;
+    sigma_point(dga, p, q, a.mt, a.Dt, a.hnt, a.hot);
+    sigma_point(dga, p, q, a.mu, a.Du, a.hnu, a.hou);
+    sigma_point(dga, p, q, a.mv, a.Dv, a.hnv, a.hov);
+}
+
+// grid (ceil(nx / 128), ny, nz)
+__global__ void depth_3d_halves_kernel(Depth3DArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (i >= a.nx || j >= a.ny) return;
+    const long long p = (long long)j * a.nx + i, q = p + k * a.plane;
+    const double hh = (a.hot[q] + a.hnt[q]) * 0.5;
+    a.hhalf[q] = hh;
+    if (i >= 1) a.hnuu[q - 1] = hh;     // UU.hn[:, :, :-1] = h_T_half[:, :, 1:]
+    if (j >= 1) a.hnvv[q - a.nx] = hh;  // VV.hn[:, :-1, :] = h_T_half[:, 1:, :]
+    const double hx = a.hnx[(long long)(j + 1) * (a.nx + 1) + (i + 1) + k * a.planex];
+    a.hnuv[q] = hx;                     // UV.hn = X.hn[:, 1:, 1:]
+    a.hnvu[q] = hx;                     // VU.hn = UV.hn
+}
+
+// one thread per column
+__global__ void depth_3d_coords_kernel(Depth3DArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
-    if (i <= a.nx && j <= a.ny) {  // X grid: (ny + 1) x (nx + 1)
-        const long long px = (long long)j * (a.nx + 1) + i;
-        sigma_column(a, px, a.planex, a.mx, a.Dx, a.hnx, nullptr);
-    }
     if (i >= a.nx || j >= a.ny) return;
     const long long p = (long long)j * a.nx + i;
-    sigma_column(a, p, a.plane, a.mt, a.Dt, a.hnt, a.hot);
-    sigma_column(a, p, a.plane, a.mu, a.Du, a.hnu, a.hou);
-    sigma_column(a, p, a.plane, a.mv, a.Dv, a.hnv, a.hov);
     if (a.mt[p] != 0) {
         t2vc_column(a.plane, a.nz, p, a.Ht, a.hnt, a.zct, a.zft);
         if (a.depth) t2cd_column(a.plane, a.nz, p, a.hnt, a.depth);
     }
     if (a.mu[p] != 0) t2vc_column(a.plane, a.nz, p, a.Hu, a.hnu, a.zcu, a.zfu);
     if (a.mv[p] != 0) t2vc_column(a.plane, a.nz, p, a.Hv, a.hnv, a.zcv, a.zfv);
-}
-
-__global__ void depth_3d_sweep2_kernel(Depth3DArgs a)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i >= a.nx || j >= a.ny) return;
-    const long long p = (long long)j * a.nx + i;
-    const long long px = (long long)(j + 1) * (a.nx + 1) + (i + 1);
-    for (int k = 0; k < a.nz; k++) {
-        const long long q = p + k * a.plane;
-        const double hh = (a.hot[q] + a.hnt[q]) * 0.5;
-        a.hhalf[q] = hh;
-        if (i >= 1) a.hnuu[q - 1] = hh;     // UU.hn[:, :, :-1] = h_T_half[:, :, 1:]
-        if (j >= 1) a.hnvv[q - a.nx] = hh;  // VV.hn[:, :-1, :] = h_T_half[:, 1:, :]
-        const double hx = a.hnx[px + k * a.planex];
-        a.hnuv[q] = hx;                     // UV.hn = X.hn[:, 1:, 1:]
-        a.hnvu[q] = hx;                     // VU.hn = UV.hn
-    }
 }
 
 extern "C" int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny, int nz, cudaStream_t stream)
@@ -438,11 +444,11 @@ extern "C" int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny
                   f->H_t, f->H_u, f->H_v, f->hn_t, f->hn_u, f->hn_v, f->hn_x, f->ho_t, f->ho_u, f->ho_v,
                   f->zc_t, f->zc_u, f->zc_v, f->zf_t, f->zf_u, f->zf_v, f->depth,
                   f->h_T_half, f->hn_uu, f->hn_vv, f->hn_uv, f->hn_vu};
-    dim3 g1(getm_div_up(nx + 1, 128), ny + 1);
-    depth_3d_sweep1_kernel<<<g1, 128, 0, stream>>>(a);
+    depth_3d_sigma_kernel<<<dim3(getm_div_up(nx + 1, 128), ny + 1, nz), 128, 0, stream>>>(a);
     GETM_CHECK_LAUNCH();
-    dim3 g2(getm_div_up(nx, 128), ny);
-    depth_3d_sweep2_kernel<<<g2, 128, 0, stream>>>(a);
+    depth_3d_halves_kernel<<<dim3(getm_div_up(nx, 128), ny, nz), 128, 0, stream>>>(a);
+    GETM_CHECK_LAUNCH();
+    depth_3d_coords_kernel<<<dim3(getm_div_up(nx, 128), ny), 128, 0, stream>>>(a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

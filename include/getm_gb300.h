@@ -493,8 +493,8 @@ int getm_velocities_3d_f32(long long n, const float* pk, const double* hnu, cons
                            const double* hnv, float* uk, float* vk, cudaStream_t stream);
 
 /* Simulation.update_depth, 3D part (python/pygetm/simulation.py:1588-1630)
- * with Sigma coordinates (vertical_coordinates.py:106-113), in two column
- * sweeps with the arithmetic of the separate array operations: ho = hn (T,
+ * with Sigma coordinates (vertical_coordinates.py:106-113), in three
+ * launches with the arithmetic of the separate array operations: ho = hn (T,
  * U, V); hn = dga Dclip where the mask is non-zero (T, U, V, X);
  * thickness2vertical_coordinates of T, U, V (zc, zf); thickness2center_depth
  * of T into depth (when not NULL); h_T_half = (ho + hn) / 2 and the

@@ -53,6 +53,21 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
     const int i0 = bx * UD_BX, j0 = by * BY;
     const int i = i0 + tx, j = j0 + ty;
     const int nx = a.nx, ny = a.ny;
+    // the point's own operands, loaded while the tile is staged
+    const bool xin = i <= nx && j <= ny, tin = i < nx && j < ny;
+    const long long px = (long long)j * (nx + 1) + i;
+    const long long p = (long long)j * nx + i;
+    int mX = 0, mT = 0, mU = 0, mV = 0;
+    double workX0 = 0.0, DX0 = 0.0, HX = 0.0, DT0 = 0.0, HT = 0.0, zT = 0.0, workU0 = 0.0, HU = 0.0;
+    double workV0 = 0.0, HV = 0.0;
+    if (xin) {
+        mX = a.mX[px]; workX0 = a.workX[px]; DX0 = a.DX[px]; HX = a.HX[px];
+    }
+    if (tin) {
+        mT = a.mT[p]; DT0 = a.DT[p]; HT = a.HT[p]; zT = a.z[p];
+        mU = a.mU[p]; workU0 = a.workU[p]; HU = a.HU[p];
+        mV = a.mV[p]; workV0 = a.workV[p]; HV = a.HV[p];
+    }
     for (int q = ty * UD_BX + tx; q < (BY + 2) * (UD_BX + 2); q += UD_BX * BY) {
         const int sj = q / (UD_BX + 2), si = q - sj * (UD_BX + 2);
         const int gj = j0 - 1 + sj, gi = i0 - 1 + si;
@@ -64,22 +79,21 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
         szh[sj][si] = v;
     }
     __syncthreads();
-    if (i > nx || j > ny) return;
+    if (!xin) return;
     const int sj = ty + 1, si = tx + 1;  // (j, i) in the tile
     // X point (j, i): interp_xy T->X (offsets 1, 1) where it writes, else the
     // previous X._work value
     {
-        const long long px = (long long)j * (nx + 1) + i;
         double zx;
         if (j >= 1 && j <= ny - 1 && i >= 1 && i <= nx - 1) {
             zx = 0.25 * (szh[sj - 1][si - 1] + szh[sj - 1][si] + szh[sj][si - 1] + szh[sj][si]);
             a.workX[px] = zx;
         } else {
-            zx = a.workX[px];
+            zx = workX0;
         }
-        double dx = a.DX[px];
-        if (a.mX[px] != 0) {
-            dx = fmax(a.HX[px] + zx, a.Dmin);
+        double dx = DX0;
+        if (mX != 0) {
+            dx = fmax(HX + zx, a.Dmin);
             a.DX[px] = dx;
         }
         if (j >= 1 && i >= 1 && j - 1 < ny && i - 1 < nx) {  // UV.D = X.D[1:, 1:]; VU.D = UV.D
@@ -88,15 +102,14 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
             a.DVU[q] = dx;
         }
     }
-    if (i >= nx || j >= ny) return;
-    const long long p = (long long)j * nx + i;
+    if (!tin) return;
     const double zh = szh[sj][si];
     // T: elevation2depth(z, H, -1000), Dclip = clamp(D, Dmin), D_T_half
-    double DT = a.DT[p];
-    if (a.mT[p] != 0) DT = fmax(a.HT[p] + a.z[p], -1000.0);
+    double DT = DT0;
+    if (mT != 0) DT = fmax(HT + zT, -1000.0);
     a.DT[p] = DT;
     a.DclipT[p] = clamp_min(DT, a.Dmin);
-    const double dth = a.mT[p] != 0 ? fmax(a.HT[p] + zh, a.Dmin) : zh;
+    const double dth = mT != 0 ? fmax(HT + zh, a.Dmin) : zh;
     a.workT[p] = dth;
     if (i >= 1) a.DUU[p - 1] = dth;   // UU.D[:, :-1] = D_T_half[:, 1:]
     if (j >= 1) a.DVV[p - nx] = dth;  // VV.D[:-1, :] = D_T_half[1:, :]
@@ -107,10 +120,10 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
         zu = 0.5 * (zh + szh[sj][si + 1]);
         a.workU[p] = zu;
     } else {
-        zu = a.workU[p];
+        zu = workU0;
     }
-    if (a.mU[p] != 0) {
-        const double d = fmax(a.HU[p] + zu, a.Dmin);
+    if (mU != 0) {
+        const double d = fmax(HU + zu, a.Dmin);
         a.DU[p] = d;
         a.alphaU[p] = alpha_of(d, twoDmin, a.ialpha);
     }
@@ -120,10 +133,10 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
         zv = 0.5 * (zh + szh[sj + 1][si]);
         a.workV[p] = zv;
     } else {
-        zv = a.workV[p];
+        zv = workV0;
     }
-    if (a.mV[p] != 0) {
-        const double d = fmax(a.HV[p] + zv, a.Dmin);
+    if (mV != 0) {
+        const double d = fmax(HV + zv, a.Dmin);
         a.DV[p] = d;
         a.alphaV[p] = alpha_of(d, twoDmin, a.ialpha);
     }
@@ -222,6 +235,9 @@ __device__ __forceinline__ void momentum_2d_friction_point(const FricArgs& a, in
 {
     const long long p = (long long)j * a.nx + i;
     const int nx = a.nx;
+    // the point's own operands, loaded before any mask is tested
+    const int mU = a.mU[p], mV = a.mV[p];
+    const double u1p = a.u1[p], v1p = a.v1[p], DUp = a.DU[p], DVp = a.DV[p], z0bUp = a.z0bU[p], z0bVp = a.z0bV[p];
     // v_U = interp_xy(v1, ioffset 0, joffset 1): written at j >= 1, i <= nx-2
     // (in arithmetic C: the drag coefficient is evaluated in C)
     C vU;
@@ -241,8 +257,8 @@ __device__ __forceinline__ void momentum_2d_friction_point(const FricArgs& a, in
     } else {
         uV = to_c<C>(a.workV[p]);
     }
-    if (a.mU[p] == 1) a.ru[p] = drag<C>(to_c<C>(a.u1[p]), vU, a.DU[p], a.z0bU[p]);
-    if (a.mV[p] == 1) a.rv[p] = drag<C>(uV, to_c<C>(a.v1[p]), a.DV[p], a.z0bV[p]);
+    if (mU == 1) a.ru[p] = drag<C>(to_c<C>(u1p), vU, DUp, z0bUp);
+    if (mV == 1) a.rv[p] = drag<C>(uV, to_c<C>(v1p), DVp, z0bVp);
 }
 
 // Momentum.coriolis, DEFAULT scheme (momentum.py:1127-1148): interp_xy of the
@@ -275,15 +291,19 @@ struct Transport2DArgs {
     double* U;
 };
 
+// Every operand is loaded before the mask is tested (one round of
+// independent loads per point).
 __device__ __forceinline__ void transport_2d_point(const Transport2DArgs& a, double dt, long long p)
 {
-    if (a.mask[p] != 1) return;
+    const int m = a.mask[p];
+    const double Up = a.U[p], SF = a.SF[p], Dp = a.D[p], dp = a.dp[p], alpha = a.alpha[p], taus = a.taus[p];
+    const double cor = a.cor[p], adv = a.adv[p], diff = a.diff[p], damp = a.damp[p];
+    const double SA = a.SA[p], SB = a.SB[p], SD = a.SD[p], r = a.r[p];
+    if (m != 1) return;
     const double rho0i = 1.0 / GETM_RHO0;
-    double Up = a.U[p];
-    double Slr = (Up > 0.0) ? fmin(a.SF[p], 0.0) : fmax(a.SF[p], 0.0);
-    double Dp = a.D[p];
-    a.U[p] = (Up + dt * (-GETM_G * Dp * a.dp[p] + a.alpha[p] * (a.taus[p] * rho0i + a.cor[p] + a.adv[p] + a.diff[p] + a.damp[p] + a.SA[p] + a.SB[p] + a.SD[p] + Slr)))
-             / (1.0 + dt * a.r[p] / Dp);
+    double Slr = (Up > 0.0) ? fmin(SF, 0.0) : fmax(SF, 0.0);
+    a.U[p] = (Up + dt * (-GETM_G * Dp * dp + alpha * (taus * rho0i + cor + adv + diff + damp + SA + SB + SD + Slr)))
+             / (1.0 + dt * r / Dp);
 }
 
 // Momentum.advance_depth_integrated's transport update, mixed form
@@ -297,20 +317,22 @@ __device__ __forceinline__ void transport_2d_mixed_point(const Transport2DArgs& 
     const double *alpha = a.alpha, *D = a.D, *dp = a.dp, *taus = a.taus, *cor = a.cor, *adv = a.adv;
     const double *diff = a.diff, *damp = a.damp, *SA = a.SA, *SB = a.SB, *SD = a.SD, *SF = a.SF, *r = a.r;
     double* U = a.U;
-    if (mask[p] != 1) return;
+    const int m = mask[p];
+    const double Up = U[p], SFp = SF[p], Dd = D[p], dpp = dp[p], alp = alpha[p], tau = taus[p], corp = cor[p];
+    const double advp = adv[p], diffp = diff[p], dampp = damp[p], SAp = SA[p], SBp = SB[p], SDp = SD[p], rp = r[p];
+    if (m != 1) return;
     const float rho0i = (float)(1.0 / GETM_RHO0);
-    const double Up = U[p];
-    const float sf = getm_d2f_approx(SF[p]);
+    const float sf = getm_d2f_approx(SFp);
     const float Slr = (Up > 0.0) ? fminf(sf, 0.f) : fmaxf(sf, 0.f);
-    const float Dp = getm_d2f_approx(D[p]);
+    const float Dp = getm_d2f_approx(Dd);
     const float dtf = (float)dt;
-    const float tend = -(float)GETM_G * Dp * getm_d2f_approx(dp[p]) +
-                       getm_d2f_approx(alpha[p]) *
-                           (getm_d2f_approx(taus[p]) * rho0i + getm_d2f_approx(cor[p]) + getm_d2f_approx(adv[p]) +
-                            getm_d2f_approx(diff[p]) + getm_d2f_approx(damp[p]) + getm_d2f_approx(SA[p]) +
-                            getm_d2f_approx(SB[p]) + getm_d2f_approx(SD[p]) + Slr);
+    const float tend = -(float)GETM_G * Dp * getm_d2f_approx(dpp) +
+                       getm_d2f_approx(alp) *
+                           (getm_d2f_approx(tau) * rho0i + getm_d2f_approx(corp) + getm_d2f_approx(advp) +
+                            getm_d2f_approx(diffp) + getm_d2f_approx(dampp) + getm_d2f_approx(SAp) +
+                            getm_d2f_approx(SBp) + getm_d2f_approx(SDp) + Slr);
     const double num = Up + getm_f2d(dtf * tend);
-    const float x = dtf * getm_d2f_approx(r[p]) / Dp;
+    const float x = dtf * getm_d2f_approx(rp) / Dp;
     U[p] = num - getm_f2d(getm_d2f_approx(num) * (x / (1.f + x)));
 }
 
@@ -334,8 +356,12 @@ __device__ __forceinline__ void surface_elevation_fused_point(int nx, int ny, in
     const double zp = z[p];
     zo[p] = zp;
     if (i < halox || i >= nx - halox || j < haloy || j >= ny - haloy) return;
-    if (mask[p] != 1) return;
-    z[p] = zp + dt * ((U[p - 1] * dyu[p - 1] - U[p] * dyu[p] + V[p - nx] * dxv[p - nx] - V[p] * dxv[p]) * iarea[p] + fwf[p]);
+    // every operand is loaded before the mask is tested
+    const int m = mask[p];
+    const double Uw = U[p - 1], dyw = dyu[p - 1], Ue = U[p], dye = dyu[p], Vs = V[p - nx], dxs = dxv[p - nx];
+    const double Vn = V[p], dxn = dxv[p], ia = iarea[p], fw = fwf[p];
+    if (m != 1) return;
+    z[p] = zp + dt * ((Uw * dyw - Ue * dye + Vs * dxs - Vn * dxn) * ia + fw);
 }
 
 
@@ -360,15 +386,22 @@ __device__ __forceinline__ void spg_point(const SpgArgs& a, long long p)
 {
     const int nx = a.nx;
     const double gammai = 1.0 / (GETM_G * GETM_RHO0);
-    if (a.umask[p] == 1) {
-        double zp = fmax(a.z[p + 1], -a.H[p] + fmin(a.Dmin, a.D[p + 1]));
-        double zm = fmax(a.z[p], -a.H[p + 1] + fmin(a.Dmin, a.D[p]));
-        a.dpdx[p] = (zp - zm + (a.sp[p + 1] - a.sp[p]) * gammai) * a.idxu[p];
+    // every operand is loaded before the masks are tested
+    const int mu = a.umask[p], mv = a.vmask[p];
+    const double z0 = a.z[p], z1 = a.z[p + 1], zn = a.z[p + nx];
+    const double H0 = a.H[p], H1 = a.H[p + 1], Hn = a.H[p + nx];
+    const double D0 = a.D[p], D1 = a.D[p + 1], Dn = a.D[p + nx];
+    const double sp0 = a.sp[p], sp1 = a.sp[p + 1], spn = a.sp[p + nx];
+    const double idx = a.idxu[p], idy = a.idyv[p];
+    if (mu == 1) {
+        double zp = fmax(z1, -H0 + fmin(a.Dmin, D1));
+        double zm = fmax(z0, -H1 + fmin(a.Dmin, D0));
+        a.dpdx[p] = (zp - zm + (sp1 - sp0) * gammai) * idx;
     }
-    if (a.vmask[p] == 1) {
-        double zp = fmax(a.z[p + nx], -a.H[p] + fmin(a.Dmin, a.D[p + nx]));
-        double zm = fmax(a.z[p], -a.H[p + nx] + fmin(a.Dmin, a.D[p]));
-        a.dpdy[p] = (zp - zm + (a.sp[p + nx] - a.sp[p]) * gammai) * a.idyv[p];
+    if (mv == 1) {
+        double zp = fmax(zn, -H0 + fmin(a.Dmin, Dn));
+        double zm = fmax(z0, -Hn + fmin(a.Dmin, D0));
+        a.dpdy[p] = (zp - zm + (spn - sp0) * gammai) * idy;
     }
 }
 

@@ -103,11 +103,11 @@ extern "C" int getm_bottom_friction_mixed(int nx, int ny, const int* mask, const
 // gradient idp is double in both forms; the FP64 form sums in FP64, the
 // mixed form (float sources) in float.
 template <typename T>
-__global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const double* alpha,
-                                       const double* ho, const double* hn, const double* dp,
-                                       const T* cor, const T* adv, const T* diff,
-                                       const double* idp, const double* taus, const double* rr,
-                                       double dt, T* ea2, T* ea4)
+__global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const double* __restrict__ alpha,
+                                       const double* __restrict__ ho, const double* __restrict__ hn, const double* __restrict__ dp,
+                                       const T* __restrict__ cor, const T* __restrict__ adv, const T* __restrict__ diff,
+                                       const double* __restrict__ idp, const double* __restrict__ taus, const double* __restrict__ rr,
+                                       double dt, T* __restrict__ ea2, T* __restrict__ ea4)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + haloy;
@@ -205,9 +205,9 @@ extern "C" int getm_advance_2d_transport(int nx, int ny, int halox, int haloy, c
 // both forms (T: type of pk, qk and w).
 template <typename T>
 __global__ void w_momentum_3d_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
-                                     const int* mask, const double* dyu, const double* dxv,
-                                     const double* iarea, const double* ho, const double* hn,
-                                     const T* pk, const T* qk, double dt, T* w)
+                                     const int* __restrict__ mask, const double* __restrict__ dyu, const double* __restrict__ dxv,
+                                     const double* __restrict__ iarea, const double* __restrict__ ho, const double* __restrict__ hn,
+                                     const T* __restrict__ pk, const T* __restrict__ qk, double dt, T* __restrict__ w)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;
@@ -217,12 +217,28 @@ __global__ void w_momentum_3d_kernel(int nx, int ny, int nz, int ilo, int ihi, i
     long long plane = (long long)nx * ny;
     const double idt = 1.0 / dt;
     const double dyE = dyu[p], dyW = dyu[p - 1], dxN = dxv[p], dxS = dxv[p - nx], ia = iarea[p];
-    double wk = (double)w[p];
-    for (int k = 1; k <= nz - 1; k++) {
-        long long q = p + (k - 1) * plane;
-        wk = wk - (hn[q] - ho[q]) * idt
-             - ((double)pk[q] * dyE - (double)pk[q - 1] * dyW + (double)qk[q] * dxN - (double)qk[q - nx] * dxS) * ia;
-        w[p + k * plane] = (T)wk;
+    if constexpr (std::is_same<T, double>::value) {
+        double wk = (double)w[p];
+        for (int k = 1; k <= nz - 1; k++) {
+            long long q = p + (k - 1) * plane;
+            wk = wk - (hn[q] - ho[q]) * idt
+                 - ((double)pk[q] * dyE - (double)pk[q - 1] * dyW + (double)qk[q] * dxN - (double)qk[q - nx] * dxS) * ia;
+            w[p + k * plane] = (T)wk;
+        }
+    } else {
+        // mixed form: the layer's increment in float (the thickness change
+        // differenced in FP64 first), accumulated up the column in FP64
+        const float idtf = (float)idt;
+        const float dyEf = getm_d2f_approx(dyE), dyWf = getm_d2f_approx(dyW);
+        const float dxNf = getm_d2f_approx(dxN), dxSf = getm_d2f_approx(dxS), iaf = getm_d2f_approx(ia);
+        double wk = getm_f2d(w[p]);
+        for (int k = 1; k <= nz - 1; k++) {
+            long long q = p + (k - 1) * plane;
+            const float inc = getm_d2f_approx(hn[q] - ho[q]) * idtf +
+                              (pk[q] * dyEf - pk[q - 1] * dyWf + qk[q] * dxNf - qk[q - nx] * dxSf) * iaf;
+            wk = wk - getm_f2d(inc);
+            w[p + k * plane] = getm_d2f_approx(wk);
+        }
     }
 }
 
@@ -260,8 +276,8 @@ extern "C" int getm_w_momentum_3d_f32(int nx, int ny, int nz, int imin, int imax
 // momentum.F90:218-241 (T: type of uk, vk, SS and of the arithmetic)
 template <typename T>
 __global__ void shear_frequency_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
-                                       const int* mask, const double* hu, const double* hv,
-                                       const T* uk, const T* vk, T* SS)
+                                       const int* __restrict__ mask, const double* __restrict__ hu, const double* __restrict__ hv,
+                                       const T* __restrict__ uk, const T* __restrict__ vk, T* __restrict__ SS)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;
@@ -377,8 +393,8 @@ extern "C" int getm_bottom_shear_velocity(int nx, int ny, int imin, int imax, in
 // bottom to top.  Mixed form (T float): the products in float from the
 // thickness narrowed on the integer pipe.
 template <typename T>
-__global__ void transport_3d_finish_kernel(long long plane, int nz, const T* vel, const double* hn,
-                                           const double* tp2d, const double* D, T* tp3d, double* dev)
+__global__ void transport_3d_finish_kernel(long long plane, int nz, const T* __restrict__ vel, const double* __restrict__ hn,
+                                           const double* __restrict__ tp2d, const double* __restrict__ D, T* __restrict__ tp3d, double* __restrict__ dev)
 {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= plane) return;

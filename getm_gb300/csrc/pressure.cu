@@ -211,8 +211,8 @@ __device__ __forceinline__ float smcw_harm_f(float a, float b)
 }
 
 __global__ void smcw_column_mixed_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
-                                         const int* mask, const double* h, const double* zc,
-                                         const double* buoy, double* Pw)
+                                         const int* __restrict__ mask, const double* __restrict__ h, const double* __restrict__ zc,
+                                         const double* __restrict__ buoy, double* __restrict__ Pw)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;

@@ -84,6 +84,8 @@ _SIGS = {
     "getm_transport_3d_finish": "iiipppppps",
     "getm_transport_3d_finish_f32": "iiipppppps",
     "getm_velocities_3d": "lpppppps",
+    "getm_column_sums": "iiiipppppppps",
+    "getm_column_sums_f32": "iiiipppppppps",
     "getm_velocities_3d_f32": "lpppppps",
     "getm_open_boundary_elevation": "iiipppppppppppppdps",
     "getm_open_boundary_tracers": "iiiiiiippppppipps",

@@ -397,3 +397,19 @@ def depth3d_fields(T, dga, h_T_half, depth=None) -> Depth3DFields:
 def update_depth_3d(fields: Depth3DFields, T):
     """Simulation.update_depth, 3D part (simulation.py:1588-1630)."""
     call("getm_update_depth_3d", ctypes.byref(fields), T.nx_, T.ny_, T.nz_, _s())
+
+
+def column_sums(pairs, subtract=False):
+    """dst = sum_k src (minus the old dst with ``subtract``) for up to four
+    (src 3D Array, dst 2D Array) pairs on grids of the same extents
+    (momentum.py:989-1012, simulation.py:1186-1192)."""
+    assert 1 <= len(pairs) <= 4
+    src0 = pairs[0][0]
+    g = src0.grid
+    args = []
+    for s, d in pairs:
+        assert d.all_values.dtype == torch.float64 and s.all_values.shape[1:] == d.all_values.shape
+        args += [_p(s), _p(d)]
+    args += [None, None] * (4 - len(pairs))
+    sfx = _sfx(*[s.all_values for s, _ in pairs])
+    call("getm_column_sums" + sfx, g.nx_, g.ny_, src0.all_values.shape[0], int(bool(subtract)), *args, _s())

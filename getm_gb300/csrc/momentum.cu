@@ -416,6 +416,56 @@ __global__ void transport_3d_finish_kernel(long long plane, int nz, const T* __r
     }
 }
 
+// Column sums of up to four 3D fields into 2D FP64 fields (the slow terms of
+// momentum.py:989-1012 and simulation.py:1186-1192): dst = sum_k src
+// (- dst when subtract is set), summed bottom to top in FP64; NULL pairs are
+// skipped.
+template <typename T>
+__global__ void column_sums_kernel(long long plane, int nz, int subtract, const T* __restrict__ a3,
+                                   double* __restrict__ a2, const T* __restrict__ b3, double* __restrict__ b2,
+                                   const T* __restrict__ c3, double* __restrict__ c2, const T* __restrict__ d3,
+                                   double* __restrict__ d2)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= plane) return;
+    const T* src[4] = {a3, b3, c3, d3};
+    double* dst[4] = {a2, b2, c2, d2};
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        if (!src[f]) continue;
+        double s = 0.0;
+        for (int k = 0; k < nz; k++) s = s + (double)src[f][p + k * plane];
+        dst[f][p] = subtract ? s - dst[f][p] : s;
+    }
+}
+
+template <typename T>
+static int column_sums_impl(int nx, int ny, int nz, int subtract, const T* a3, double* a2, const T* b3, double* b2,
+                            const T* c3, double* c2, const T* d3, double* d2, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1) return GETM_ERR_ARG;
+    if (!a3 != !a2 || !b3 != !b2 || !c3 != !c2 || !d3 != !d2) return GETM_ERR_ARG;
+    const long long plane = (long long)nx * ny;
+    column_sums_kernel<T><<<getm_div_up(plane, 128), 128, 0, stream>>>(plane, nz, subtract, a3, a2, b3, b2, c3, c2,
+                                                                        d3, d2);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_column_sums(int nx, int ny, int nz, int subtract, const double* a3, double* a2,
+                                const double* b3, double* b2, const double* c3, double* c2, const double* d3,
+                                double* d2, cudaStream_t stream)
+{
+    return column_sums_impl<double>(nx, ny, nz, subtract, a3, a2, b3, b2, c3, c2, d3, d2, stream);
+}
+
+extern "C" int getm_column_sums_f32(int nx, int ny, int nz, int subtract, const float* a3, double* a2,
+                                    const float* b3, double* b2, const float* c3, double* c2, const float* d3,
+                                    double* d2, cudaStream_t stream)
+{
+    return column_sums_impl<float>(nx, ny, nz, subtract, a3, a2, b3, b2, c3, c2, d3, d2, stream);
+}
+
 // Momentum.update_diagnostics (momentum.py:909-910): uk = pk / hn, vk = qk /
 // hn over n points (mixed form: in float).
 template <typename T>

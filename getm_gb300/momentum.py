@@ -327,11 +327,9 @@ class Momentum:
             _pygetm.momentum_diffusion(self.uua.grid.hn, self.uva.grid.hn, self.vua.grid.hn, self.vva.grid.hn,
                                        self.uk, self.vk, self._Am_const, self.diffpk, self.diffqk)
         self._transport_2d_momentum(self.Ui, self.Vi, timestep, self.SxA, self.SyA, self.SxD, self.SyD, False)
-        f64 = torch.float64
-        torch.sub(self.advpk.all_values.sum(dim=0, dtype=f64), self.SxA.all_values, out=self.SxA.all_values)
-        torch.sub(self.advqk.all_values.sum(dim=0, dtype=f64), self.SyA.all_values, out=self.SyA.all_values)
-        torch.sub(self.diffpk.all_values.sum(dim=0, dtype=f64), self.SxD.all_values, out=self.SxD.all_values)
-        torch.sub(self.diffqk.all_values.sum(dim=0, dtype=f64), self.SyD.all_values, out=self.SyD.all_values)
+        # SxA = sum_k advpk - SxA, ... (the column sums in FP64)
+        _pygetm.column_sums([(self.advpk, self.SxA), (self.advqk, self.SyA), (self.diffpk, self.SxD),
+                             (self.diffqk, self.SyD)], subtract=True)
         if self.apply_bottom_friction:
             torch.add(self.ustar2_bx.all_values, self.ru.all_values * self.u1.all_values, out=self.SxF.all_values)
             torch.add(self.ustar2_by.all_values, self.rv.all_values * self.v1.all_values, out=self.SyF.all_values)

@@ -317,8 +317,7 @@ class Simulation:
                                   self.dpdyo, self.idpdx, self.idpdy, self.num)
             self.tracers.advance(self.macrotimestep, self.momentum.uk, self.momentum.vk, self.momentum.ww, self.nuh)
             if self.runtype == RunType.BAROCLINIC and self.delay_slow_ip:
-                self.momentum.SxB.all_values.copy_(self.idpdx.all_values.sum(dim=0, dtype=torch.float64))
-                self.momentum.SyB.all_values.copy_(self.idpdy.all_values.sum(dim=0, dtype=torch.float64))
+                _pygetm.column_sums([(self.idpdx, self.momentum.SxB), (self.idpdy, self.momentum.SyB)])
 
     def _update_forcing_and_diagnostics(self, macro_active: bool):
         """python/pygetm/simulation.py:1138-1304"""
@@ -333,8 +332,7 @@ class Simulation:
             self.update_density()
             self.update_internal_pressure()
             if not self.delay_slow_ip:
-                self.momentum.SxB.all_values.copy_(self.idpdx.all_values.sum(dim=0, dtype=torch.float64))
-                self.momentum.SyB.all_values.copy_(self.idpdy.all_values.sum(dim=0, dtype=torch.float64))
+                _pygetm.column_sums([(self.idpdx, self.momentum.SxB), (self.idpdy, self.momentum.SyB)])
         self.update_depth()
         self.momentum.update_depth_integrated_diagnostics(self.timestep, skip_coriolis=not starting,
                                                          update_z0b=update_z0b)

@@ -485,6 +485,17 @@ int getm_transport_3d_finish(int nx, int ny, int nz, const double* vel, const do
 int getm_transport_3d_finish_f32(int nx, int ny, int nz, const float* vel, const double* hn,
                                  const double* tp2d, const double* D, float* tp3d, double* dev,
                                  cudaStream_t stream);
+/* Column sums of up to four 3D fields into 2D FP64 fields, for the slow
+ * terms (momentum.py:989-1012: SxA = sum_k advpk - SxA, ...; simulation.py
+ * :1186-1192: SxB = sum_k idpdx): dst = sum_k src, minus the old dst when
+ * subtract is non-zero; summed bottom to top in FP64.  Unused pairs are
+ * NULL.  nx, ny: full extents.                                              */
+int getm_column_sums(int nx, int ny, int nz, int subtract, const double* a3, double* a2,
+                     const double* b3, double* b2, const double* c3, double* c2, const double* d3,
+                     double* d2, cudaStream_t stream);
+int getm_column_sums_f32(int nx, int ny, int nz, int subtract, const float* a3, double* a2,
+                         const float* b3, double* b2, const float* c3, double* c2, const float* d3,
+                         double* d2, cudaStream_t stream);
 /* Momentum.update_diagnostics (momentum.py:909-910): uk = pk / hn_U,
  * vk = qk / hn_V over n points (_f32: the division in float).              */
 int getm_velocities_3d(long long n, const double* pk, const double* hnu, const double* qk,

@@ -413,3 +413,15 @@ def column_sums(pairs, subtract=False):
     args += [None, None] * (4 - len(pairs))
     sfx = _sfx(*[s.all_values for s, _ in pairs])
     call("getm_column_sums" + sfx, g.nx_, g.ny_, src0.all_values.shape[0], int(bool(subtract)), *args, _s())
+
+
+def buoyancy_frequency(salt, temp, p, out):
+    """Density.get_buoyancy_frequency (density.py:22-60) for the device EOS:
+    squared buoyancy frequency at the interior interfaces of ``out``
+    (z=INTERFACES); ``p``: layer-centre depths (thickness2center_depth)."""
+    g = salt.grid
+    assert temp.grid is g and p.grid is g and out.grid is g and out.z == INTERFACES
+    sfx = _sfx(salt.all_values, temp.all_values, out.all_values)
+    call("getm_buoyancy_frequency" + sfx, g.nx_, g.ny_, salt.all_values.shape[0], _p(g.mask), _p(g.hn), _p(p),
+         _p(salt), _p(temp), _p(out), _s())
+    return out

@@ -8,6 +8,8 @@
 // seawater"), with depth (m) standing in for pressure (dbar) as the
 // reference's layer-centre depth does, and returns buoyancy
 // b = -g/rho0 (rho - rho0) exactly as simulation.py:1184 forms it.
+#include <type_traits>
+
 #include "getm_common.cuh"
 
 #define SEOS_RHO0 1026.0
@@ -59,4 +61,70 @@ extern "C" int getm_density_buoyancy_f32(int n, const float* salt, const float* 
     density_kernel<float><<<getm_div_up(n, 256), 256, 0, stream>>>(n, salt, temp, p, rho, buoy);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Squared buoyancy frequency at the interior layer interfaces
+// (Density.get_buoyancy_frequency, python/pygetm/density.py:22-60, called
+// every baroclinic 3D step at simulation.py:1200-1204), for the device EOS:
+// N2 = -g/rho0 (rho(S1, T1, zi) - rho(S0, T0, zi)) / dz between level k
+// (below) and k + 1, both densities at the interface depth zi = (p_k +
+// p_k+1)/2 (locally referenced, as TEOS-10's nsquared evaluates them at the
+// mid pressure), dz = (h_k + h_k+1)/2.  The density difference is formed
+// from the differences of temperature and salinity with the polynomial
+// identities of the EOS, so it keeps the precision of the differences:
+//   f(Ta) = (1 + l1/2 Ta + m1 z) Ta:  f(Ta1) - f(Ta0) = dT (1 + l1/2 (Ta1 + Ta0) + m1 z)
+//   Ta1 Sa1 - Ta0 Sa0 = dT Sa1 + Ta0 dS.
+// Interfaces 1 .. nz-1 of columns with a non-zero mask are written; the
+// surface and bottom interfaces are left as they are (reference: out[1:-1]).
+// R: type of S, T and N2 (float in the mixed form).
+template <typename R>
+__global__ void buoyancy_frequency_kernel(long long plane, int nz, const int* __restrict__ mask,
+                                          const double* __restrict__ h, const double* __restrict__ p,
+                                          const R* __restrict__ S, const R* __restrict__ T, R* __restrict__ NN)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = blockIdx.y;  // interface k + 1
+    if (c >= plane || k >= nz - 1 || mask[c] == 0) return;
+    const long long q0 = c + (long long)k * plane, q1 = q0 + plane;
+    const R T0 = T[q0], T1 = T[q1], S0 = S[q0], S1 = S[q1];
+    const R dT = T1 - T0, dS = S1 - S0;
+    const R Ta0 = T0 - R(10), Ta1 = T1 - R(10), Sa0 = S0 - R(35), Sa1 = S1 - R(35);
+    R zi, dz;
+    if constexpr (std::is_same<R, double>::value) {
+        zi = 0.5 * (p[q0] + p[q1]);
+        dz = 0.5 * (h[q0] + h[q1]);
+    } else {
+        zi = 0.5f * (getm_d2f_approx(p[q0]) + getm_d2f_approx(p[q1]));
+        dz = 0.5f * (getm_d2f_approx(h[q0]) + getm_d2f_approx(h[q1]));
+    }
+    const R drho = -R(SEOS_A0) * dT * (R(1) + R(0.5 * SEOS_LAMBDA1) * (Ta1 + Ta0) + R(SEOS_MU1) * zi)
+                   + R(SEOS_B0) * dS * (R(1) - R(0.5 * SEOS_LAMBDA2) * (Sa1 + Sa0) - R(SEOS_MU2) * zi)
+                   - R(SEOS_NU) * (dT * Sa1 + Ta0 * dS);
+    NN[q1] = R(-GETM_G / GETM_RHO0) * drho / dz;
+}
+
+template <typename R>
+static int buoyancy_frequency_impl(int nx, int ny, int nz, const int* mask, const double* h, const double* p,
+                                   const R* S, const R* T, R* NN, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || !mask || !h || !p || !S || !T || !NN) return GETM_ERR_ARG;
+    if (nz == 1) return GETM_OK;
+    const long long plane = (long long)nx * ny;
+    dim3 grid(getm_div_up(plane, 256), nz - 1);
+    buoyancy_frequency_kernel<R><<<grid, 256, 0, stream>>>(plane, nz, mask, h, p, S, T, NN);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_buoyancy_frequency(int nx, int ny, int nz, const int* mask, const double* h, const double* p,
+                                       const double* salt, const double* temp, double* NN, cudaStream_t stream)
+{
+    return buoyancy_frequency_impl<double>(nx, ny, nz, mask, h, p, salt, temp, NN, stream);
+}
+
+extern "C" int getm_buoyancy_frequency_f32(int nx, int ny, int nz, const int* mask, const double* h, const double* p,
+                                           const float* salt, const float* temp, float* NN, cudaStream_t stream)
+{
+    return buoyancy_frequency_impl<float>(nx, ny, nz, mask, h, p, salt, temp, NN, stream);
 }

@@ -192,6 +192,9 @@ class Simulation:
             # density, buoyancy and internal pressure stay float64 in both forms
             self.rho = T.array(z=CENTERS, name="rho")
             self.buoy = T.array(z=CENTERS, name="buoy")
+            # squared buoyancy frequency (simulation.py:757-767, :1200-1204)
+            self.NN = T.array(z=INTERFACES, name="NN", dtype=d3)
+            self.NN.fill(0.0)
             self.internal_pressure_method = internal_pressure
         if three_d:
             # internal_pressure.Base.initialize (python/pygetm/internal_pressure.py:14-30)
@@ -354,8 +357,9 @@ class Simulation:
 
     # ------------------------------------------------------------ components
     def update_density(self):
-        """density.get_density + buoyancy (simulation.py:1178-1184) with the
-        device equation of state."""
+        """density.get_density + buoyancy (simulation.py:1178-1184) and the
+        squared buoyancy frequency (:1200-1204) with the device equation of
+        state."""
         n = self.rho.all_values.numel()
         from ._lib import call
         from .core import _sfx
@@ -363,6 +367,7 @@ class Simulation:
         call("getm_density_buoyancy" + _sfx(self.salt.all_values, self.temp.all_values), n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
              self.depth.all_values.data_ptr(), self.rho.all_values.data_ptr(), self.buoy.all_values.data_ptr(),
              torch.cuda.current_stream().cuda_stream)
+        _pygetm.buoyancy_frequency(self.salt, self.temp, self.depth, self.NN)
 
     def update_internal_pressure(self):
         if self.internal_pressure_method == "blumberg_mellor":

@@ -343,6 +343,18 @@ int getm_shchepetkin_mcwilliams_f32(int nx, int ny, int nz, int imin, int imax, 
                                     cudaStream_t stream);
 int getm_density_buoyancy_f32(int n, const float* salt, const float* temp, const double* p,
                               double* rho, double* buoy, cudaStream_t stream);
+/* Squared buoyancy frequency (Density.get_buoyancy_frequency,
+ * python/pygetm/density.py:22-60; simulation.py:1200-1204) for the device
+ * EOS: at interfaces 1..nz-1 of columns with a non-zero mask,
+ * N2 = -g/rho0 (rho(S_k+1, T_k+1, zi) - rho(S_k, T_k, zi)) / dz with zi the
+ * mean of the layer-centre depths p and dz the mean thickness; the density
+ * difference is formed from the temperature and salinity differences.
+ * NN: nz+1 interface levels (surface and bottom left unchanged).  The _f32
+ * entry (mixed form) takes float S, T, NN.                                 */
+int getm_buoyancy_frequency(int nx, int ny, int nz, const int* mask, const double* h, const double* p,
+                            const double* salt, const double* temp, double* NN, cudaStream_t stream);
+int getm_buoyancy_frequency_f32(int nx, int ny, int nz, const int* mask, const double* h, const double* p,
+                                const float* salt, const float* temp, float* NN, cudaStream_t stream);
 
 /* bottom friction (momentum.F90:79-101, getm_bottom_friction) with the drag
  * coefficient's logarithm and square roots evaluated in float; inputs and

@@ -93,6 +93,21 @@ def seos_buoyancy(S, T, z):
     return rho, (-O.GRAVITY / O.RHO0) * (rho - O.RHO0)
 
 
+def seos_nsquared(mask, h, p, S, T):
+    """Squared buoyancy frequency of the device EOS at the interior interfaces
+    (Density.get_buoyancy_frequency, python/pygetm/density.py:22-60):
+    -g/rho0 (rho(S1, T1, zi) - rho(S0, T0, zi)) / dz, both densities at the
+    mean depth zi of the two layer centres, dz the mean thickness.  Returns
+    the (nz - 1) interior interfaces; NaN where the mask is zero."""
+    S0, S1, T0, T1 = S[:-1], S[1:], T[:-1], T[1:]
+    zi = 0.5 * (p[:-1] + p[1:])
+    dz = 0.5 * (h[:-1] + h[1:])
+    rho1, _ = seos_buoyancy(S1, T1, zi)
+    rho0, _ = seos_buoyancy(S0, T0, zi)
+    out = (-O.GRAVITY / O.RHO0) * (rho1 - rho0) / dz
+    return np.where(np.asarray(mask)[None] != 0, out, np.nan)
+
+
 class Momentum:
     """python/pygetm/momentum.py:24-1214 (DEFAULT Coriolis, FULL 2D split)."""
 

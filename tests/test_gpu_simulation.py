@@ -52,6 +52,11 @@ def _compare(wl, o, g, rtol):
         errs["temp"] = close(h(g.temp), o.temp, rtol, wetT)
         errs["salt"] = close(h(g.salt), o.salt, rtol, wetT)
         errs["idpdx"] = close(h(g.idpdx), o.idpdx, rtol, wetU)
+        if o.istep > 0:
+            from oracle.models import seos_nsquared
+
+            NN = seos_nsquared(T.mask, o.T.hn, o.depth, o.salt, o.temp)
+            errs["NN"] = close(h(g.NN)[1:-1], NN, rtol, wetT)
     return errs
 
 

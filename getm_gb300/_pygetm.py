@@ -294,6 +294,20 @@ def coriolis_2d(U, out, x_direction, mixed=False):
          int(bool(x_direction)), _s())
 
 
+def coriolis_3d(U, out, x_direction):
+    """Momentum.coriolis, DEFAULT scheme, for 3D transports (momentum.py:1127-1148)."""
+    a, b = U.grid, out.grid
+    if a.ioffset == b.ioffset + 1 and a.joffset == b.joffset - 1:
+        io, jo = 1, 0
+    elif a.ioffset == b.ioffset - 1 and a.joffset == b.joffset + 1:
+        io, jo = 0, 1
+    else:
+        raise NotImplementedError("coriolis_3d expects U -> V or V -> U")
+    sfx = _sfx(U.all_values, out.all_values)
+    call("getm_coriolis_3d" + sfx, b.nx_, b.ny_, out.all_values.shape[0], io, jo, _p(U), _p(b.cor), _p(out),
+         int(bool(x_direction)), _s())
+
+
 def accumulate_2d(U, V, Ucum, Vcum):
     """_U_cum += U; _V_cum += V (momentum.py:716-718)."""
     call("getm_accumulate_2d", U.all_values.numel(), _p(U), _p(V), Ucum.data_ptr(), Vcum.data_ptr(), _s())

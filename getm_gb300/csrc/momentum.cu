@@ -426,17 +426,15 @@ __global__ void column_sums_kernel(long long plane, int nz, int subtract, const 
                                    const T* __restrict__ c3, double* __restrict__ c2, const T* __restrict__ d3,
                                    double* __restrict__ d2)
 {
+    // one field per grid row (blockIdx.y), one column per thread
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= plane) return;
-    const T* src[4] = {a3, b3, c3, d3};
-    double* dst[4] = {a2, b2, c2, d2};
-#pragma unroll
-    for (int f = 0; f < 4; f++) {
-        if (!src[f]) continue;
-        double s = 0.0;
-        for (int k = 0; k < nz; k++) s = s + (double)src[f][p + k * plane];
-        dst[f][p] = subtract ? s - dst[f][p] : s;
-    }
+    const int f = blockIdx.y;
+    const T* src = f == 0 ? a3 : f == 1 ? b3 : f == 2 ? c3 : d3;
+    double* dst = f == 0 ? a2 : f == 1 ? b2 : f == 2 ? c2 : d2;
+    if (p >= plane || !src) return;
+    double s = 0.0;
+    for (int k = 0; k < nz; k++) s = s + (double)src[p + k * plane];
+    dst[p] = subtract ? s - dst[p] : s;
 }
 
 template <typename T>
@@ -446,8 +444,8 @@ static int column_sums_impl(int nx, int ny, int nz, int subtract, const T* a3, d
     if (nx < 1 || ny < 1 || nz < 1) return GETM_ERR_ARG;
     if (!a3 != !a2 || !b3 != !b2 || !c3 != !c2 || !d3 != !d2) return GETM_ERR_ARG;
     const long long plane = (long long)nx * ny;
-    column_sums_kernel<T><<<getm_div_up(plane, 128), 128, 0, stream>>>(plane, nz, subtract, a3, a2, b3, b2, c3, c2,
-                                                                        d3, d2);
+    column_sums_kernel<T><<<dim3(getm_div_up(plane, 128), 4), 128, 0, stream>>>(plane, nz, subtract, a3, a2, b3, b2,
+                                                                                 c3, c2, d3, d2);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

@@ -19,6 +19,8 @@
 
 #include "split2d_ops.cuh"
 
+#include <type_traits>
+
 #define S2_THREADS 128
 
 namespace {
@@ -57,6 +59,34 @@ __global__ void __launch_bounds__(S2_THREADS) coriolis_2d_kernel(int nx, int ny,
     const int j = blockIdx.y;
     if (i >= nx || j >= ny) return;
     coriolis_2d_point<C>(nx, ny, ioff, joff, src, cor, out, negate, i, j);
+}
+
+// Momentum.coriolis for 3D transports (momentum.py:1127-1148, DEFAULT
+// scheme): interp_xy of every layer to the other velocity grid, times f,
+// negated for the V equation, as one launch.  T: storage and arithmetic
+// (float in the mixed form: f narrowed on the integer pipe).
+template <typename T>
+__global__ void __launch_bounds__(S2_THREADS) coriolis_3d_kernel(int nx, int ny, int ioff, int joff,
+                                                                  const T* __restrict__ src,
+                                                                  const double* __restrict__ cor,
+                                                                  T* __restrict__ out, int negate)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    const long long off = (long long)blockIdx.z * nx * ny;
+    if (i >= nx || j >= ny) return;
+    const long long p = (long long)j * nx + i;
+    const int si = i - ioff, sj = j - joff;
+    T v;
+    if (si >= 0 && sj >= 0 && si <= nx - 2 && sj <= ny - 2) {
+        const long long q = off + (long long)sj * nx + si;
+        v = T(0.25) * (src[q] + src[q + 1] + src[q + nx] + src[q + nx + 1]);
+    } else {
+        v = out[off + p];
+    }
+    if constexpr (std::is_same<T, double>::value) v = v * cor[p];
+    else v = v * getm_d2f_approx(cor[p]);
+    out[off + p] = negate ? -v : v;
 }
 
 __global__ void __launch_bounds__(S2_THREADS) advance_2d_transport_mixed_kernel(int nx, int ny, int halox, int haloy,
@@ -205,4 +235,28 @@ extern "C" int getm_surface_elevation_fused(int nx, int ny, int halox, int haloy
                                                                                    iarea, z, zo, U, V, fwf, dt);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
+}
+
+template <typename T>
+static int coriolis_3d_impl(int nx, int ny, int nz, int ioffset, int joffset, const T* src, const double* cor, T* out,
+                            int negate, cudaStream_t stream)
+{
+    if (nx < 2 || ny < 2 || nz < 1 || !src || !cor || !out || ioffset < 0 || ioffset > 1 || joffset < 0 || joffset > 1)
+        return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, S2_THREADS), ny, nz);
+    coriolis_3d_kernel<T><<<grid, S2_THREADS, 0, stream>>>(nx, ny, ioffset, joffset, src, cor, out, negate);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_coriolis_3d(int nx, int ny, int nz, int ioffset, int joffset, const double* src, const double* cor,
+                                double* out, int negate, cudaStream_t stream)
+{
+    return coriolis_3d_impl<double>(nx, ny, nz, ioffset, joffset, src, cor, out, negate, stream);
+}
+
+extern "C" int getm_coriolis_3d_f32(int nx, int ny, int nz, int ioffset, int joffset, const float* src,
+                                    const double* cor, float* out, int negate, cudaStream_t stream)
+{
+    return coriolis_3d_impl<float>(nx, ny, nz, ioffset, joffset, src, cor, out, negate, stream);
 }

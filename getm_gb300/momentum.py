@@ -267,6 +267,9 @@ class Momentum:
         if self.fused_2d and not U.z:
             _pygetm.coriolis_2d(U, out, x_direction, mixed=self.dtype3d == torch.float32)
             return
+        if self.fused_2d:
+            _pygetm.coriolis_3d(U, out, x_direction)
+            return
         U.interp(out)
         out.all_values.mul_(out.grid.cor.all_values)
         if x_direction:

@@ -426,6 +426,12 @@ int getm_coriolis_2d(int nx, int ny, int ioffset, int joffset, const double* src
  * term as a float tendency)                                                */
 int getm_coriolis_2d_mixed(int nx, int ny, int ioffset, int joffset, const double* src, const double* cor,
                            double* out, int negate, cudaStream_t stream);
+/* the same for 3D transports (every layer; nz layers of nx x ny; the _f32
+ * entry takes float transports and terms, mixed form)                      */
+int getm_coriolis_3d(int nx, int ny, int nz, int ioffset, int joffset, const double* src, const double* cor,
+                     double* out, int negate, cudaStream_t stream);
+int getm_coriolis_3d_f32(int nx, int ny, int nz, int ioffset, int joffset, const float* src, const double* cor,
+                         float* out, int negate, cudaStream_t stream);
 /* advance_2d_transport (momentum.F90:147-189) in the mixed form: tendency
  * summed in float, transport updated in double; same arguments as
  * getm_advance_2d_transport.                                               */

@@ -45,6 +45,14 @@ struct HPassArgs {
     T* fout[GETM_MAX_BATCH];
 };
 
+// Epilogue of a pass: called once per updated (or copied) cell with the
+// cell's flat index p3, its row j, the new value of the first field and the
+// new thickness.  The default does nothing; the one-launch 2D substep uses
+// it to form the momentum advection term as each cell is finished.
+struct NoEpi {
+    __device__ __forceinline__ void operator()(long long, int, double, double) const {}
+};
+
 template <typename T>
 struct FaceGeom {
     double QU;
@@ -95,8 +103,9 @@ __device__ __forceinline__ T face_flux(const HPassArgs<T>& a, const FaceGeom<T>&
 }
 
 // x-direction pass.  blockDim = (32, BYX); grid = (ceil(nx_/32), ceil(ny_*nk/BYX)).
-template <typename T>
-__device__ __forceinline__ void hpass_x_body(const HPassArgs<T>& a, int bx, long long row, int lane)
+template <typename T, typename Epi = NoEpi>
+__device__ __forceinline__ void hpass_x_body(const HPassArgs<T>& a, int bx, long long row, int lane,
+                                             const Epi& epi = Epi())
 {
     const int i = bx * 32 + lane;
     if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
@@ -137,14 +146,16 @@ __device__ __forceinline__ void hpass_x_body(const HPassArgs<T>& a, int bx, long
                 fn = (hfo - (T)a.dt * advn) / (T)hnew;
             }
             a.fout[t][p3] = fn;
+            if (t == 0) epi(p3, j, (double)fn, hnew);
         }
     }
 }
 
 // y-direction pass.  blockDim = (32, GETM_V_BY); grid = (ceil(nx_/32), ceil(ny_/BY), nk).
-template <typename T>
+template <typename T, typename Epi = NoEpi>
 __device__ __forceinline__ void hpass_y_body(const HPassArgs<T>& a, int bx, int by, int k, int tx, int ty,
-                                             double (&sQ)[GETM_V_BY][32], T (&sF)[GETM_V_BY][32])
+                                             double (&sQ)[GETM_V_BY][32], T (&sF)[GETM_V_BY][32],
+                                             const Epi& epi = Epi())
 {
     const int i = bx * 32 + tx;
     const int j = by * GETM_V_BY + ty;
@@ -188,6 +199,7 @@ __device__ __forceinline__ void hpass_y_body(const HPassArgs<T>& a, int bx, int 
                 fn = (hfo - (T)a.dt * advn) / (T)hnew;
             }
             a.fout[t][p3] = fn;
+            if (t == 0) epi(p3, j, (double)fn, hnew);
         }
     }
 }
@@ -243,8 +255,9 @@ constexpr int HX_STRIDE = 31;
 // KB layers k0 .. k0+KB-1 (those below nk) of row j: the 2D fields (masks,
 // metrics) are loaded once for all of them, and every load of the KB layers
 // is issued before any value is used.
-template <typename S, int KB>
-__device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, int j, int k0, int lane)
+template <typename S, int KB, typename Epi = NoEpi>
+__device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, int j, int k0, int lane,
+                                                 const Epi& epi = Epi())
 {
     constexpr unsigned FULL = 0xffffffffu;
     const int i0 = bx * HX_STRIDE;
@@ -322,8 +335,8 @@ __device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, 
 
         // thickness update of cell ib
         float coef = 0.f;  // dt iA / hnew
+        double hnew = hold[kk];
         if (bin) {
-            double hnew = hold[kk];
             if (upd) {
                 const float dh = a.dtf * (QUe - QU) * iaf;
                 hnew = hold[kk] - getm_f2d(dh);
@@ -370,20 +383,25 @@ __device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, 
                     er = QU * (up ? dev - d : dev) + fd;
                 }
                 const float el_e = __shfl_down_sync(FULL, el, 1);  // east face of cell ib, seen from ib
-                if (bin) a.fout[t + q][r3 + ib] = upd ? inc_add<S>(fb, -coef * (el_e - er)) : fb;
+                if (bin) {
+                    const S fn = upd ? inc_add<S>(fb, -coef * (el_e - er)) : fb;
+                    a.fout[t + q][r3 + ib] = fn;
+                    if (t + q == 0) epi(r3 + ib, j, (double)fn, hnew);
+                }
             }
         }
     }
 }
 
 // One row (layer k, row j) of the x pass: row = k ny_ + j.
-template <typename S>
-__device__ __forceinline__ void hpass_x_inc_body(const HPassArgs<S>& a, int bx, long long row, int lane)
+template <typename S, typename Epi = NoEpi>
+__device__ __forceinline__ void hpass_x_inc_body(const HPassArgs<S>& a, int bx, long long row, int lane,
+                                                 const Epi& epi = Epi())
 {
     if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
     const int k = (int)(row / a.ny_);
     const int j = (int)(row - (long long)k * a.ny_);
-    hpass_x_inc_rows<S, 1>(a, bx, j, k, lane);
+    hpass_x_inc_rows<S, 1, Epi>(a, bx, j, k, lane, epi);
 }
 
 // y-direction pass in increment form: the transpose of hpass_x_inc_kernel.
@@ -403,9 +421,9 @@ struct YIncSmem {
     float sx[HY_BY][32];       // per-face exchange (QU, then el)
 };
 
-template <typename S>
+template <typename S, typename Epi = NoEpi>
 __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, int by, int k, int tx, int ty,
-                                                 YIncSmem<S>& sm)
+                                                 YIncSmem<S>& sm, const Epi& epi = Epi())
 {
     auto& sf = sm.sf;
     auto& sd = sm.sd;
@@ -447,9 +465,10 @@ __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, 
     const bool bin = ty < HY_STRIDE && icol && jb < a.ny_;
     const bool upd = bin && iint && jb >= a.jlo && jb <= a.jhi && a.tmask[(long long)jb * s + i] == 1;
     float coef = 0.f;
+    double hnew = 0.0;
     if (bin) {
         const double hold = a.h_in[base + jb * s];
-        double hnew = hold;
+        hnew = hold;
         if (upd) {
             const float iaf = a.iA_f[(long long)jb * s + i];
             const float dh = a.dtf * (QUn - QU) * iaf;
@@ -488,7 +507,11 @@ __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, 
         sx[ty][tx] = el;
         __syncthreads();
         const float el_n = ty + 1 < HY_BY ? sx[ty + 1][tx] : 0.f;
-        if (bin) a.fout[t][base + jb * s] = upd ? inc_add<S>(fb, -coef * (el_n - er)) : fb;
+        if (bin) {
+            const S fn = upd ? inc_add<S>(fb, -coef * (el_n - er)) : fb;
+            a.fout[t][base + jb * s] = fn;
+            if (t == 0) epi(base + jb * s, jb, (double)fn, hnew);
+        }
     }
 }
 

@@ -8,8 +8,8 @@
 // they leave GB300 idle between launches: each reads and writes ~10^5 points,
 // a microsecond of work behind several microseconds of launch and drain.
 //
-// Here one cooperative launch runs the whole substep.  Its blocks (one per
-// SM, 512 threads) walk through eight phases separated by grid-wide
+// Here one cooperative launch runs the whole substep.  Its blocks (one or
+// two per SM, 512 threads) walk through seven phases separated by grid-wide
 // barriers; a phase contains operations whose inputs at neighbouring points
 // were completed by an earlier phase:
 //   1  transport update of the first direction (U or V, alternating)
@@ -20,8 +20,8 @@
 //   5  velocities and advection velocities, copies of the depths advected
 //      by the momentum advection, surface pressure gradient
 //   6  bottom friction, first pass of the U and V momentum advection
-//   7  second pass of both
-//   8  transport change of the momentum advection (reconstruct)
+//   7  second pass of both, forming each cell's advection term from its
+//      transport change as the pass finishes the cell (reconstruct)
 // Every operation is the same device function the separate kernels run
 // (split2d_ops.cuh, advection_passes.cuh), so results are bitwise the same.
 //
@@ -133,9 +133,24 @@ __device__ __forceinline__ void grid_exit(unsigned* sync)
 
 // One advection pass over the whole plane, distributed over the grid: x
 // passes by warps (one row segment each), y passes by blocks (one tile each).
-template <bool MIXED>
+// reconstruct_transport_change (momentum.F90:323-340) of a cell as soon as
+// the last advection pass has finished it: un = (un hn - Uo) / dt on rows
+// jlo..jhi (the same expression as reconstruct_point)
+struct ReconstructEpi {
+    double* un;
+    const double* Uo;
+    double idt;
+    int jlo, jhi;
+    __device__ __forceinline__ void operator()(long long p, int j, double fn, double hn) const
+    {
+        if (j < jlo || j > jhi) return;
+        un[p] = (fn * hn - Uo[p]) * idt;
+    }
+};
+
+template <bool MIXED, typename Epi = NoEpi>
 __device__ __forceinline__ void advection_pass(const HPassArgs<double>& pa, int dir, SubstepSmem& sm, int tx,
-                                               int ty)
+                                               int ty, const Epi& epi = Epi())
 {
     if (dir == 1) {
         const int nbx = MIXED ? div_up(pa.nx_ + 1, HX_STRIDE) : div_up(pa.nx_, 32);
@@ -143,15 +158,15 @@ __device__ __forceinline__ void advection_pass(const HPassArgs<double>& pa, int 
         for (long long w = (long long)blockIdx.x * SS_BY + ty; w < items; w += (long long)gridDim.x * SS_BY) {
             const int bx = (int)(w % nbx);
             const long long row = w / nbx;
-            if constexpr (MIXED) hpass_x_inc_body<double>(pa, bx, row, tx);
-            else hpass_x_body<double>(pa, bx, row, tx);
+            if constexpr (MIXED) hpass_x_inc_body<double, Epi>(pa, bx, row, tx, epi);
+            else hpass_x_body<double, Epi>(pa, bx, row, tx, epi);
         }
     } else {
         const int nbx = div_up(pa.nx_, 32);
         const int nby = MIXED ? div_up(pa.ny_ + 1, HY_STRIDE) : div_up(pa.ny_, GETM_V_BY);
         for (int t = blockIdx.x; t < nbx * nby; t += gridDim.x) {
-            if constexpr (MIXED) hpass_y_inc_body<double>(pa, t % nbx, t / nbx, 0, tx, ty, sm.yi);
-            else hpass_y_body<double>(pa, t % nbx, t / nbx, 0, tx, ty, sm.y.sQ, sm.y.sF);
+            if constexpr (MIXED) hpass_y_inc_body<double, Epi>(pa, t % nbx, t / nbx, 0, tx, ty, sm.yi, epi);
+            else hpass_y_body<double, Epi>(pa, t % nbx, t / nbx, 0, tx, ty, sm.y.sQ, sm.y.sF, epi);
             __syncthreads();  // shared memory is reused by the next tile
         }
     }
@@ -251,16 +266,11 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
     advection_pass<MIXED>(a.adv[0].pass[0], a.adv[0].dir[0], sm, tx, ty);
     advection_pass<MIXED>(a.adv[1].pass[0], a.adv[1].dir[0], sm, tx, ty);
     if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
-    // 7: second advection passes
-    advection_pass<MIXED>(a.adv[0].pass[1], a.adv[0].dir[1], sm, tx, ty);
-    advection_pass<MIXED>(a.adv[1].pass[1], a.adv[1].dir[1], sm, tx, ty);
-    if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
-    // 8: advection terms from the transport change (rows jlo..jhi, every i)
-    for (int p = gt; p < n; p += G) {
-        const int j = p / nx;
-        if (j < jlo || j > jhi) continue;
-        reconstruct_point<double>(a.advvar[0], a.advD[0], a.Uo[0], a.idt, p);
-        reconstruct_point<double>(a.advvar[1], a.advD[1], a.Uo[1], a.idt, p);
+    // 7: second advection passes, each cell's advection term formed as the
+    // pass finishes it (reconstruct_transport_change)
+    for (int d = 0; d < 2; d++) {
+        const ReconstructEpi epi{a.advvar[d], a.Uo[d], a.idt, jlo, jhi};
+        advection_pass<MIXED>(a.adv[d].pass[1], a.adv[d].dir[1], sm, tx, ty, epi);
     }
     grid_exit(a.sync);
 }

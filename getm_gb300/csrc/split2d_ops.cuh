@@ -266,21 +266,46 @@ __device__ __forceinline__ void momentum_2d_friction_point(const FricArgs& a, in
 // (ioff, joff) are the interp_xy offsets: U -> V (1, 0); V -> U (0, 1).
 // C: arithmetic (float in the mixed form, whose transport update reads the
 // term as a float tendency).
+// true where the interpolation writes point (i, j) of the target grid
+__device__ __forceinline__ bool coriolis_2d_inside(int nx, int ny, int ioff, int joff, int i, int j)
+{
+    const int si = i - ioff, sj = j - joff;
+    return si >= 0 && sj >= 0 && si <= nx - 2 && sj <= ny - 2;
+}
+
+// The term at (i, j) inside the interpolation range; src(i, j) returns the
+// transport at a source point.
+template <typename C, typename Src>
+__device__ __forceinline__ double coriolis_2d_value(int ioff, int joff, int i, int j, const Src& src, double cor,
+                                                    int negate)
+{
+    const int si = i - ioff, sj = j - joff;
+    C v = C(0.25) * (to_c<C>(src(si, sj)) + to_c<C>(src(si + 1, sj)) + to_c<C>(src(si, sj + 1)) +
+                     to_c<C>(src(si + 1, sj + 1)));
+    v = v * to_c<C>(cor);
+    return from_c<C>(negate ? -v : v);
+}
+
+// ... and outside it (the previous value times f)
+template <typename C>
+__device__ __forceinline__ double coriolis_2d_outside(double old, double cor, int negate)
+{
+    C v = to_c<C>(old);
+    v = v * to_c<C>(cor);
+    return from_c<C>(negate ? -v : v);
+}
+
 template <typename C>
 __device__ __forceinline__ void coriolis_2d_point(int nx, int ny, int ioff, int joff, const double* src,
                                                   const double* cor, double* out, int negate, int i, int j)
 {
     const long long p = (long long)j * nx + i;
-    const int si = i - ioff, sj = j - joff;
-    C v;
-    if (si >= 0 && sj >= 0 && si <= nx - 2 && sj <= ny - 2) {
-        const long long q = (long long)sj * nx + si;
-        v = C(0.25) * (to_c<C>(src[q]) + to_c<C>(src[q + 1]) + to_c<C>(src[q + nx]) + to_c<C>(src[q + nx + 1]));
+    if (coriolis_2d_inside(nx, ny, ioff, joff, i, j)) {
+        auto at = [&](int si, int sj) { return src[(long long)sj * nx + si]; };
+        out[p] = coriolis_2d_value<C>(ioff, joff, i, j, at, cor[p], negate);
     } else {
-        v = to_c<C>(out[p]);
+        out[p] = coriolis_2d_outside<C>(out[p], cor[p], negate);
     }
-    v = v * to_c<C>(cor[p]);
-    out[p] = from_c<C>(negate ? -v : v);
 }
 
 // Momentum.advance_depth_integrated's transport update (momentum.F90:147-189)
@@ -291,19 +316,34 @@ struct Transport2DArgs {
     double* U;
 };
 
+// The transport after the update at interior point p: the new value where
+// the mask is 1, else the old one (upd false).  cor: the Coriolis term at p.
 // Every operand is loaded before the mask is tested (one round of
 // independent loads per point).
-__device__ __forceinline__ void transport_2d_point(const Transport2DArgs& a, double dt, long long p)
+struct TransportNew {
+    double v;
+    bool upd;
+};
+
+__device__ __forceinline__ TransportNew transport_2d_value(const Transport2DArgs& a, double dt, long long p,
+                                                           double cor)
 {
     const int m = a.mask[p];
     const double Up = a.U[p], SF = a.SF[p], Dp = a.D[p], dp = a.dp[p], alpha = a.alpha[p], taus = a.taus[p];
-    const double cor = a.cor[p], adv = a.adv[p], diff = a.diff[p], damp = a.damp[p];
+    const double adv = a.adv[p], diff = a.diff[p], damp = a.damp[p];
     const double SA = a.SA[p], SB = a.SB[p], SD = a.SD[p], r = a.r[p];
-    if (m != 1) return;
+    if (m != 1) return TransportNew{Up, false};
     const double rho0i = 1.0 / GETM_RHO0;
     double Slr = (Up > 0.0) ? fmin(SF, 0.0) : fmax(SF, 0.0);
-    a.U[p] = (Up + dt * (-GETM_G * Dp * dp + alpha * (taus * rho0i + cor + adv + diff + damp + SA + SB + SD + Slr)))
-             / (1.0 + dt * r / Dp);
+    return TransportNew{(Up + dt * (-GETM_G * Dp * dp + alpha * (taus * rho0i + cor + adv + diff + damp + SA + SB + SD + Slr)))
+                            / (1.0 + dt * r / Dp),
+                        true};
+}
+
+__device__ __forceinline__ void transport_2d_point(const Transport2DArgs& a, double dt, long long p)
+{
+    const TransportNew n = transport_2d_value(a, dt, p, a.cor[p]);
+    if (n.upd) a.U[p] = n.v;
 }
 
 // Momentum.advance_depth_integrated's transport update, mixed form
@@ -311,16 +351,16 @@ __device__ __forceinline__ void transport_2d_point(const Transport2DArgs& a, dou
 // updated in double, and the implicit friction factor 1/(1 + x), x =
 // dt r / D, is applied as U - U x/(1 + x) with the small correction in float
 // (no FP64 division).
-__device__ __forceinline__ void transport_2d_mixed_point(const Transport2DArgs& a, double dt, long long p)
+__device__ __forceinline__ TransportNew transport_2d_mixed_value(const Transport2DArgs& a, double dt, long long p,
+                                                                 double corp)
 {
     const int* mask = a.mask;
-    const double *alpha = a.alpha, *D = a.D, *dp = a.dp, *taus = a.taus, *cor = a.cor, *adv = a.adv;
+    const double *alpha = a.alpha, *D = a.D, *dp = a.dp, *taus = a.taus, *adv = a.adv;
     const double *diff = a.diff, *damp = a.damp, *SA = a.SA, *SB = a.SB, *SD = a.SD, *SF = a.SF, *r = a.r;
-    double* U = a.U;
     const int m = mask[p];
-    const double Up = U[p], SFp = SF[p], Dd = D[p], dpp = dp[p], alp = alpha[p], tau = taus[p], corp = cor[p];
+    const double Up = a.U[p], SFp = SF[p], Dd = D[p], dpp = dp[p], alp = alpha[p], tau = taus[p];
     const double advp = adv[p], diffp = diff[p], dampp = damp[p], SAp = SA[p], SBp = SB[p], SDp = SD[p], rp = r[p];
-    if (m != 1) return;
+    if (m != 1) return TransportNew{Up, false};
     const float rho0i = (float)(1.0 / GETM_RHO0);
     const float sf = getm_d2f_approx(SFp);
     const float Slr = (Up > 0.0) ? fminf(sf, 0.f) : fmaxf(sf, 0.f);
@@ -333,7 +373,13 @@ __device__ __forceinline__ void transport_2d_mixed_point(const Transport2DArgs& 
                             getm_d2f_approx(SBp) + getm_d2f_approx(SDp) + Slr);
     const double num = Up + getm_f2d(dtf * tend);
     const float x = dtf * getm_d2f_approx(rp) / Dp;
-    U[p] = num - getm_f2d(getm_d2f_approx(num) * (x / (1.f + x)));
+    return TransportNew{num - getm_f2d(getm_d2f_approx(num) * (x / (1.f + x))), true};
+}
+
+__device__ __forceinline__ void transport_2d_mixed_point(const Transport2DArgs& a, double dt, long long p)
+{
+    const TransportNew n = transport_2d_mixed_value(a, dt, p, a.cor[p]);
+    if (n.upd) a.U[p] = n.v;
 }
 
 // _U_cum += U; _V_cum += V (momentum.py:716-718), every point
@@ -346,6 +392,13 @@ __device__ __forceinline__ void accumulate_2d_point(const double* U, const doubl
 
 // zo = z (every point), then the surface elevation update
 // (simulation.py:1468-1486 -> wrapper.F90:496-523)
+// the elevation update at an interior water point (wrapper.F90:496-523)
+__device__ __forceinline__ double elevation_new(double zp, double dt, double Uw, double dyw, double Ue, double dye,
+                                                double Vs, double dxs, double Vn, double dxn, double ia, double fw)
+{
+    return zp + dt * ((Uw * dyw - Ue * dye + Vs * dxs - Vn * dxn) * ia + fw);
+}
+
 __device__ __forceinline__ void surface_elevation_fused_point(int nx, int ny, int halox, int haloy, const int* mask,
                                                               const double* dyu, const double* dxv,
                                                               const double* iarea, double* z, double* zo,
@@ -361,7 +414,7 @@ __device__ __forceinline__ void surface_elevation_fused_point(int nx, int ny, in
     const double Uw = U[p - 1], dyw = dyu[p - 1], Ue = U[p], dye = dyu[p], Vs = V[p - nx], dxs = dxv[p - nx];
     const double Vn = V[p], dxn = dxv[p], ia = iarea[p], fw = fwf[p];
     if (m != 1) return;
-    z[p] = zp + dt * ((Uw * dyw - Ue * dye + Vs * dxs - Vn * dxn) * ia + fw);
+    z[p] = elevation_new(zp, dt, Uw, dyw, Ue, dye, Vs, dxs, Vn, dxn, ia, fw);
 }
 
 

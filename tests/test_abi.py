@@ -112,3 +112,16 @@ def test_split2d_substep_rejects_missing_fields():
     assert _lib.lib.getm_split2d_substep(*args) == 1
     args[0] = None
     assert _lib.lib.getm_split2d_substep(*args) == 1
+
+
+def test_depth3d_fields_layout_matches_header():
+    """getm_depth3d_fields: the ctypes mirror has the header's members in the
+    header's order (all pointers)."""
+    from getm_gb300 import _pygetm
+
+    src = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    body = re.search(r"typedef struct getm_depth3d_fields\s*\{(.*?)\}\s*getm_depth3d_fields;", src, flags=re.S)
+    assert body
+    names = [d.strip().split("*")[-1].strip() for d in body.group(1).split(";") if d.strip()]
+    assert tuple(names) == _pygetm.DEPTH3D_FIELDS
+    assert ctypes.sizeof(_pygetm.Depth3DFields) == 8 * len(names)

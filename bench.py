@@ -314,7 +314,7 @@ def _roofline(sim, peak, peak_kind):
     achieved = alg / t_kernel / 1e9
     # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
     # of the float x pass on this workload, from an ncu capture of this bench
-    traffic = 152.93e6 if sz == 4 else None
+    traffic = 152.51e6 if sz == 4 else None
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": f"{'hpass_x_inc_kernel<float>' if sz == 4 else 'hpass_x_kernel<double>'} (2 tracers)",
             "bytes_per_launch": alg, "us_per_launch": t_kernel * 1e6, "peak_kind": peak_kind}

@@ -499,9 +499,16 @@ __global__ void __launch_bounds__(128, getm_increment_form<T> ? 8 : 1) wpass_ker
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
-    if (i < a.ilo || i > a.ihi || j < a.jlo || j > a.jhi) return;
+    if (i >= a.nx_) return;
     const long long c = (long long)j * a.nx_ + i;
-    if (a.tmask[c] != 1) return;
+    const bool touched = i >= a.ilo && i <= a.ihi && j >= a.jlo && j <= a.jhi && a.tmask[c] == 1 && a.ntracer > 0;
+    if (!touched) {
+        // a column the pass does not update keeps its thickness (h_out must
+        // be a complete field: it is a ping-pong buffer)
+        if (a.h_out != a.h_in)
+            for (int k = 0; k < a.nz; k++) a.h_out[c + k * a.plane] = a.h_in[c + k * a.plane];
+        return;
+    }
     const int itersmax = 200;
     // mixed form: two consecutive fields with the same w_var are stepped
     // together (the sub-step count depends only on w_var and h); the second
@@ -559,20 +566,6 @@ __global__ void __launch_bounds__(128, getm_increment_form<T> ? 8 : 1) wpass_ker
     }
 }
 
-// Copy h_in -> h_out for the columns the w pass does not touch, so h_out is a
-// complete field (ping-pong buffers must be fully written).
-template <typename T>
-__global__ void copy_untouched_kernel(WPassArgs<T> a)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i >= a.nx_) return;
-    const long long c = (long long)j * a.nx_ + i;
-    bool touched = i >= a.ilo && i <= a.ihi && j >= a.jlo && j <= a.jhi && a.tmask[c] == 1 && a.ntracer > 0;
-    if (touched || a.h_out == a.h_in) return;
-    for (int k = 0; k < a.nz; k++) a.h_out[c + k * a.plane] = a.h_in[c + k * a.plane];
-}
-
 template <typename T>
 static int run_wstage(getm_advection* adv, const getm_grid* tg, const T* w, const T* const* wvar, double dt,
                       const double* h_in, double* h_out, int ntracer, T* const* f, cudaStream_t stream)
@@ -600,8 +593,6 @@ static int run_wstage(getm_advection* adv, const getm_grid* tg, const T* w, cons
         GETM_CHECK_LAUNCH();
         done += n;
     } while (done < ntracer);
-    copy_untouched_kernel<T><<<grid, block, 0, stream>>>(a);
-    GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
 

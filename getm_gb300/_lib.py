@@ -84,6 +84,8 @@ _SIGS = {
     "getm_transport_3d_finish": "iiipppppps",
     "getm_transport_3d_finish_f32": "iiipppppps",
     "getm_velocities_3d": "lpppppps",
+    "getm_momentum_3d_advection_inputs": "iiippppppppppps",
+    "getm_momentum_3d_advection_inputs_f32": "iiippppppppppps",
     "getm_coriolis_3d": "iiiiipppis",
     "getm_coriolis_3d_f32": "iiiiipppis",
     "getm_buoyancy_frequency": "iiipppppps",

@@ -439,3 +439,18 @@ def buoyancy_frequency(salt, temp, p, out):
     call("getm_buoyancy_frequency" + sfx, g.nx_, g.ny_, salt.all_values.shape[0], _p(g.mask), _p(g.hn), _p(p),
          _p(salt), _p(temp), _p(out), _s())
     return out
+
+
+def momentum_3d_advection_inputs(uk, vk, ww, uua, uva, vua, vva, wwu, wwv, advpk, advqk):
+    """The interpolated velocities and advected copies of the 3D momentum
+    advection (momentum.py:989-1003) in one launch."""
+    U, V, T = uk.grid, vk.grid, ww.grid
+    assert uua.grid is U.ugrid and uva.grid is U.vgrid and vua.grid is V.ugrid and vva.grid is V.vgrid
+    assert wwu.grid is U and wwv.grid is V and ww.z == INTERFACES
+    # the interpolations these grids imply (core.Grid.interpolate): +1 in i -> interp_x, +1 in j -> interp_y
+    for s, d, di, dj in ((U, U.ugrid, 1, 0), (V, U.vgrid, 1, 0), (U, V.ugrid, 0, 1), (V, V.vgrid, 0, 1),
+                         (T, U, 1, 0), (T, V, 0, 1)):
+        assert d.ioffset - s.ioffset == di and d.joffset - s.joffset == dj
+    sfx = _sfx(uk.all_values, vk.all_values, ww.all_values)
+    call("getm_momentum_3d_advection_inputs" + sfx, T.nx_, T.ny_, uk.all_values.shape[0], _p(uk), _p(vk), _p(ww),
+         _p(uua), _p(uva), _p(vua), _p(vva), _p(wwu), _p(wwv), _p(advpk), _p(advqk), _s())

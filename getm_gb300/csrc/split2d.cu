@@ -89,6 +89,43 @@ __global__ void __launch_bounds__(S2_THREADS) coriolis_3d_kernel(int nx, int ny,
     out[off + p] = negate ? -v : v;
 }
 
+// Inputs of the 3D momentum advection (momentum.py:989-1003): the velocities
+// interpolated to the UU, UV, VU, VV grids (uk -> UU and vk -> UV by
+// interp_x, uk -> VU and vk -> VV by interp_y), ww interpolated to U and V,
+// and the advected copies of uk and vk, in one launch; grid (x, ny, nz + 1),
+// the top level holds only the interface values of ww.  Each target keeps
+// its previous value where the interpolation does not write (as interp_x/y).
+template <typename T>
+struct Mom3DIn {
+    int nx, ny, nz;
+    long long plane;
+    const T *uk, *vk, *ww;
+    T *uua, *uva, *vua, *vva, *wwu, *wwv, *advpk, *advqk;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(S2_THREADS) momentum_3d_inputs_kernel(Mom3DIn<T> a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (i >= a.nx) return;
+    const long long p = (long long)k * a.plane + (long long)j * a.nx + i;
+    const bool ex = i < a.nx - 1, ey = j < a.ny - 1;
+    if (ex) interp_pair_point<T>(a.ww, a.wwu, p, 1, 0);
+    if (ey) interp_pair_point<T>(a.ww, a.wwv, p, a.nx, 0);
+    if (k == a.nz) return;
+    if (ex) {
+        interp_pair_point<T>(a.uk, a.uua, p, 1, 0);
+        interp_pair_point<T>(a.vk, a.uva, p, 1, 0);
+    }
+    if (ey) {
+        interp_pair_point<T>(a.uk, a.vua, p, a.nx, 0);
+        interp_pair_point<T>(a.vk, a.vva, p, a.nx, 0);
+    }
+    a.advpk[p] = a.uk[p];
+    a.advqk[p] = a.vk[p];
+}
+
 __global__ void __launch_bounds__(S2_THREADS) advance_2d_transport_mixed_kernel(int nx, int ny, int halox, int haloy,
                                                                                  Transport2DArgs a, double dt)
 {
@@ -259,4 +296,35 @@ extern "C" int getm_coriolis_3d_f32(int nx, int ny, int nz, int ioffset, int jof
                                     const double* cor, float* out, int negate, cudaStream_t stream)
 {
     return coriolis_3d_impl<float>(nx, ny, nz, ioffset, joffset, src, cor, out, negate, stream);
+}
+
+template <typename T>
+static int momentum_3d_inputs_impl(int nx, int ny, int nz, const T* uk, const T* vk, const T* ww, T* uua, T* uva,
+                                   T* vua, T* vva, T* wwu, T* wwv, T* advpk, T* advqk, cudaStream_t stream)
+{
+    if (nx < 2 || ny < 2 || nz < 1) return GETM_ERR_ARG;
+    const void* ptrs[] = {uk, vk, ww, uua, uva, vua, vva, wwu, wwv, advpk, advqk};
+    for (const void* q : ptrs)
+        if (!q) return GETM_ERR_ARG;
+    Mom3DIn<T> a{nx, ny, nz, (long long)nx * ny, uk, vk, ww, uua, uva, vua, vva, wwu, wwv, advpk, advqk};
+    dim3 grid(getm_div_up(nx, S2_THREADS), ny, nz + 1);
+    momentum_3d_inputs_kernel<T><<<grid, S2_THREADS, 0, stream>>>(a);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_momentum_3d_advection_inputs(int nx, int ny, int nz, const double* uk, const double* vk,
+                                                 const double* ww, double* uua, double* uva, double* vua,
+                                                 double* vva, double* wwu, double* wwv, double* advpk,
+                                                 double* advqk, cudaStream_t stream)
+{
+    return momentum_3d_inputs_impl<double>(nx, ny, nz, uk, vk, ww, uua, uva, vua, vva, wwu, wwv, advpk, advqk, stream);
+}
+
+extern "C" int getm_momentum_3d_advection_inputs_f32(int nx, int ny, int nz, const float* uk, const float* vk,
+                                                     const float* ww, float* uua, float* uva, float* vua,
+                                                     float* vva, float* wwu, float* wwv, float* advpk,
+                                                     float* advqk, cudaStream_t stream)
+{
+    return momentum_3d_inputs_impl<float>(nx, ny, nz, uk, vk, ww, uua, uva, vua, vva, wwu, wwv, advpk, advqk, stream);
 }

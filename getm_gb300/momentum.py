@@ -318,12 +318,14 @@ class Momentum:
             self.bottom_friction(self.u_bot, self.v_bot, self.hU_bot, self.hV_bot, self.rru, self.rrv)
         _pygetm.bottom_shear_velocity(self.u_bot, self.v_bot, self.rru, self.rrv, self.ustar2_bx, self.ustar2_by,
                                       self.ustar_b)
-        self.advpk.all_values.copy_(self.uk.all_values)
-        self.uadv.apply_3d(self.uk.interp(self.uua3d), self.vk.interp(self.uva3d), self.ww.interp(self._ww_u),
+        # advpk = uk, advqk = vk and the velocities on the advection grids
+        # (the interpolations below, all at once)
+        _pygetm.momentum_3d_advection_inputs(self.uk, self.vk, self.ww, self.uua3d, self.uva3d, self.vua3d,
+                                             self.vva3d, self._ww_u, self._ww_v, self.advpk, self.advqk)
+        self.uadv.apply_3d(self.uua3d, self.uva3d, self._ww_u,
                            timestep, self.advpk, new_h=True, skip_initial_halo_exchange=True)
         _pygetm.reconstruct_transport_change(self.advpk, self.uadv.h, self.pk, timestep)
-        self.advqk.all_values.copy_(self.vk.all_values)
-        self.vadv.apply_3d(self.uk.interp(self.vua3d), self.vk.interp(self.vva3d), self.ww.interp(self._ww_v),
+        self.vadv.apply_3d(self.vua3d, self.vva3d, self._ww_v,
                            timestep, self.advqk, new_h=True, skip_initial_halo_exchange=True)
         _pygetm.reconstruct_transport_change(self.advqk, self.vadv.h, self.qk, timestep)
         if self.diffuse_momentum:

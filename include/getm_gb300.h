@@ -514,6 +514,20 @@ int getm_column_sums(int nx, int ny, int nz, int subtract, const double* a3, dou
 int getm_column_sums_f32(int nx, int ny, int nz, int subtract, const float* a3, double* a2,
                          const float* b3, double* b2, const float* c3, double* c2, const float* d3,
                          double* d2, cudaStream_t stream);
+/* Inputs of the 3D momentum advection (momentum.py:989-1003) in one launch:
+ * uua = interp_x(uk), uva = interp_x(vk), vua = interp_y(uk),
+ * vva = interp_y(vk) (offset 0, nz layers), wwu = interp_x(ww),
+ * wwv = interp_y(ww) (nz+1 interfaces), advpk = uk, advqk = vk.  Targets
+ * keep their values where the interpolation does not write.  nx, ny: full
+ * extents (all grids share them).  _f32: float fields (mixed form).       */
+int getm_momentum_3d_advection_inputs(int nx, int ny, int nz, const double* uk, const double* vk,
+                                      const double* ww, double* uua, double* uva, double* vua, double* vva,
+                                      double* wwu, double* wwv, double* advpk, double* advqk,
+                                      cudaStream_t stream);
+int getm_momentum_3d_advection_inputs_f32(int nx, int ny, int nz, const float* uk, const float* vk,
+                                          const float* ww, float* uua, float* uva, float* vua, float* vva,
+                                          float* wwu, float* wwv, float* advpk, float* advqk,
+                                          cudaStream_t stream);
 /* Momentum.update_diagnostics (momentum.py:909-910): uk = pk / hn_U,
  * vk = qk / hn_V over n points (_f32: the division in float).              */
 int getm_velocities_3d(long long n, const double* pk, const double* hnu, const double* qk,

@@ -38,7 +38,11 @@ __global__ void density_kernel(long long n, const R* S, const R* T, const double
 {
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
-    double r = seos_rho((double)S[q], (double)T[q], p[q]);
+    // float fields widen exactly on the integer pipe (getm_f2d)
+    double s, tt;
+    if constexpr (std::is_same<R, double>::value) { s = S[q]; tt = T[q]; }
+    else { s = getm_f2d(S[q]); tt = getm_f2d(T[q]); }
+    double r = seos_rho(s, tt, p[q]);
     if (rho) rho[q] = r;
     if (buoy) buoy[q] = (-GETM_G / GETM_RHO0) * (r - GETM_RHO0);
 }

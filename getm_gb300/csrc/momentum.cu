@@ -287,10 +287,15 @@ __global__ void shear_frequency_kernel(int nx, int ny, int nz, int ilo, int ihi,
     if (mask[p] <= 0) return;
     long long plane = (long long)nx * ny;
     long long a = p + (k - 1) * plane, b = p + k * plane;
-    T t1 = (uk[b] - uk[a]) / (T(0.5) * ((T)hu[b] + (T)hu[a]));
-    T t2 = (uk[b - 1] - uk[a - 1]) / (T(0.5) * ((T)hu[b - 1] + (T)hu[a - 1]));
-    T t3 = (vk[b] - vk[a]) / (T(0.5) * ((T)hv[b] + (T)hv[a]));
-    T t4 = (vk[b - nx] - vk[a - nx]) / (T(0.5) * ((T)hv[b - nx] + (T)hv[a - nx]));
+    // thicknesses in T (float: narrowed on the integer pipe)
+    auto h = [](double x) -> T {
+        if constexpr (std::is_same<T, double>::value) return x;
+        else return getm_d2f_approx(x);
+    };
+    T t1 = (uk[b] - uk[a]) / (T(0.5) * (h(hu[b]) + h(hu[a])));
+    T t2 = (uk[b - 1] - uk[a - 1]) / (T(0.5) * (h(hu[b - 1]) + h(hu[a - 1])));
+    T t3 = (vk[b] - vk[a]) / (T(0.5) * (h(hv[b]) + h(hv[a])));
+    T t4 = (vk[b - nx] - vk[a - nx]) / (T(0.5) * (h(hv[b - nx]) + h(hv[a - nx])));
     SS[b] = T(0.5) * (t1 * t1 + t2 * t2 + t3 * t3 + t4 * t4);
 }
 

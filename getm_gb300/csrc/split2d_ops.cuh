@@ -423,7 +423,8 @@ __device__ __forceinline__ void surface_elevation_fused_point(int nx, int ny, in
 template <typename T>
 __device__ __forceinline__ void reconstruct_point(T* un, const double* hn, const T* Uo, double idt, long long p)
 {
-    un[p] = (un[p] * (T)hn[p] - Uo[p]) * (T)idt;
+    if constexpr (std::is_same<T, double>::value) un[p] = (un[p] * hn[p] - Uo[p]) * idt;
+    else un[p] = (un[p] * getm_d2f_approx(hn[p]) - Uo[p]) * (T)idt;
 }
 
 // surface_pressure_gradient (wrapper.F90:525-565) at interior point (i, j)

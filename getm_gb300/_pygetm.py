@@ -218,18 +218,24 @@ _P_WORK = {}
 
 
 def shchepetkin_mcwilliams(buoy, idpdx, idpdy, P_work=None, arithmetic="float64"):
-    """pyx:555-568.  ``P_work`` (optional) is the 3D pressure work array; by
-    default one per grid is kept.  ``arithmetic="float32"`` (float64 fields)
+    """pyx:555-568.  ``P_work`` (optional) is the 3D pressure work array (nz
+    planes, nz + 2 for ``arithmetic="float32"``); by default one per grid is
+    kept.  ``arithmetic="float32"`` (float64 fields)
     evaluates the slope corrections in float (the mixed form)."""
     g = buoy.grid
     assert buoy.z == CENTERS, "buoy"
     assert idpdx.grid is g.ugrid and idpdx.z == CENTERS, "idpdx"
     assert idpdy.grid is g.vgrid and idpdy.z == CENTERS, "idpdy"
+    nz, ny, nx = buoy.all_values.shape
+    shape = (nz + 2, ny, nx)  # the mixed form keeps two planes of column terms after P
     if P_work is None:
         P_work = _P_WORK.get(id(g))
-        if P_work is None or P_work.shape != buoy.all_values.shape:
-            P_work = torch.zeros(buoy.all_values.shape, dtype=torch.float64, device=buoy.all_values.device)
+        if P_work is None or P_work.shape != shape:
+            P_work = torch.zeros(shape, dtype=torch.float64, device=buoy.all_values.device)
             _P_WORK[id(g)] = P_work
+    assert P_work.shape[1:] == (ny, nx) and P_work.shape[0] >= nz and P_work.dtype == torch.float64
+    if arithmetic == "float32":
+        assert P_work.shape[0] >= nz + 2, "P_work: nz + 2 planes for the mixed form"
     sfx = _sfx(buoy.all_values, idpdx.all_values, idpdy.all_values)
     if arithmetic == "float32" and sfx == "":
         sfx = "_mixed"

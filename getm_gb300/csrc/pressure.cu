@@ -210,9 +210,13 @@ __device__ __forceinline__ float smcw_harm_f(float a, float b)
     return (cff > (float)SMCW_EPS) ? cff / (a + b) : 0.f;
 }
 
+// Pw: nz + 2 planes; the last two receive the hydrostatic surface term of
+// the x and y gradients of the column, (z_e - z) (b_e + b)/2 at the top
+// layer, formed once per column instead of once per layer.
 __global__ void smcw_column_mixed_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
                                          const int* __restrict__ mask, const double* __restrict__ h, const double* __restrict__ zc,
-                                         const double* __restrict__ buoy, double* __restrict__ Pw)
+                                         const double* __restrict__ buoy, const double* __restrict__ z,
+                                         double* __restrict__ Pw)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y + jlo;
@@ -221,6 +225,11 @@ __global__ void smcw_column_mixed_kernel(int nx, int ny, int nz, int ilo, int ih
     const long long p = (long long)j * nx + i;
     if (mask[p] <= 0) return;
     const float x = 1.f / 12.f;
+    if (i <= ihi && j <= jhi) {
+        const long long ptop = p + (long long)(nz - 1) * P;
+        Pw[p + (long long)nz * P] = (z[p + 1] - z[p]) * 0.5 * (buoy[ptop + 1] + buoy[ptop]);
+        Pw[p + (long long)(nz + 1) * P] = (z[p + nx] - z[p]) * 0.5 * (buoy[ptop + nx] + buoy[ptop]);
+    }
 #define B(k) buoy[p + (long long)((k) - 1) * P]
 #define Z(k) zc[p + (long long)((k) - 1) * P]
     double cff = 0.0;
@@ -268,7 +277,6 @@ __global__ void smcw_gradient_mixed_kernel(int nx, int ny, int nz, int ilo, int 
     const long long P = (long long)nx * ny;
     const long long p = (long long)j * nx + i;
     const long long q = p + (long long)k * P;
-    const long long qtop = p + (long long)(nz - 1) * P;
     const float x = 1.f / 12.f;
     for (int dir = 0; dir < 2; dir++) {
         const int* m = dir ? vmask : umask;
@@ -285,10 +293,14 @@ __global__ void smcw_gradient_mixed_kernel(int nx, int ny, int nz, int ilo, int 
         const float corr = 0.2f * ((dRx1 - dRx0) * (getm_d2f_approx(dzc) - x * (dZx1 + dZx0)) -
                                    (dZx1 - dZx0) * (getm_d2f_approx(dbq) - x * (dRx1 + dRx0)));
         const double FC = 0.5 * ((buoy[q + s] + buoy[q]) * dzc - getm_f2d(corr));
-        const double id = dir ? idyv[p] : idxu[p];
+        // the large, nearly cancelling terms in FP64 (the surface term from
+        // the column sweep), the scaling by the mean thickness and the
+        // inverse spacing in float
+        const double surf = Pw[p + (long long)(nz + dir) * P];
+        const float hm = 0.5f * (getm_d2f_approx(h[q]) + getm_d2f_approx(h[q + s]));
+        const float idf = getm_d2f_approx(dir ? idyv[p] : idxu[p]);
         double* out = dir ? idpdy : idpdx;
-        out[q] = 0.5 * (h[q] + h[q + s]) * id
-                 * ((Pw[q + s] - Pw[q]) + FC - (z[p + s] - z[p]) * 0.5 * (buoy[qtop + s] + buoy[qtop]));
+        out[q] = getm_f2d(hm * idf * getm_d2f_approx((Pw[q + s] - Pw[q]) + FC - surf));
     }
 }
 
@@ -304,7 +316,7 @@ extern "C" int getm_shchepetkin_mcwilliams_mixed(int nx, int ny, int nz, int imi
         return GETM_ERR_ARG;
     dim3 g1(getm_div_up(nx, 128), jmax - jmin + 2);
     smcw_column_mixed_kernel<<<g1, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, h, zc,
-                                                     buoy, P_work);
+                                                     buoy, z, P_work);
     GETM_CHECK_LAUNCH();
     dim3 g2(getm_div_up(nx, 128), jmax - jmin + 1, nz);
     smcw_gradient_mixed_kernel<<<g2, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask,

@@ -202,7 +202,7 @@ class Simulation:
             self.idpdy = self.V.array(z=CENTERS, name="idpdy")
             self.idpdx.fill(0.0)
             self.idpdy.fill(0.0)
-            self._P_work = torch.zeros((T.nz, T.ny_, T.nx_), dtype=torch.float64, device=T.device)
+            self._P_work = torch.zeros((T.nz + 2, T.ny_, T.nx_), dtype=torch.float64, device=T.device)
         self.update_depth(_3d=three_d)
         self.update_depth(_3d=three_d)
 

@@ -364,10 +364,12 @@ int getm_bottom_friction_mixed(int nx, int ny, const int* mask, const double* u,
                                double* ru, int iterate, cudaStream_t stream);
 
 /* Shchepetkin-McWilliams internal pressure (internal_pressure.F90:63-217)
- * for the mixed form: same arguments and storage as the FP64 entry point;
- * the column sums of b dz, the pressure differences and the hydrostatic
- * correction in FP64, the harmonic-mean slope corrections in float from
- * FP64 differences.                                                        */
+ * for the mixed form: same arguments and storage as the FP64 entry point,
+ * except that P_work holds nz + 2 planes; the column sums of b dz, the
+ * pressure differences and the hydrostatic surface term in FP64 (the sum of
+ * the large, nearly cancelling terms), the harmonic-mean slope corrections
+ * and the final scaling by the mean thickness and the inverse spacing in
+ * float.                                                                   */
 int getm_shchepetkin_mcwilliams_mixed(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
                                       const int* mask, const int* umask, const int* vmask,
                                       const double* idxu, const double* idyv, const double* h,

@@ -350,14 +350,16 @@ extern "C" int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax
 
 // ---------------------------------------------------------------------------
 // Simulation.update_depth, 3D part (python/pygetm/simulation.py:1588-1630) in
-// three launches.  1 (one thread per point and level of every grid): ho = hn;
-// hn = dga Dclip where the mask is non-zero (Sigma coordinates,
-// vertical_coordinates.py:106-113).  2 (per point and level, needs the new
-// thicknesses of neighbouring columns): h_T_half = (ho + hn) / 2 on T and the
-// thicknesses of the advection velocity grids (UU from h_T_half at i+1, VV
-// at j+1, UV = VU = X at (j+1, i+1)).  3 (per column): the vertical
-// coordinates of T, U, V and the T centre depths.  Same arithmetic as the
-// separate array operations.
+// one launch, one thread per X-grid column (j, i), 0 <= j <= ny, 0 <= i <= nx,
+// sweeping up from the bottom: hn = dga Dclip where the mask is non-zero
+// (Sigma coordinates, vertical_coordinates.py:106-113) on X and, for j < ny
+// and i < nx, on T, U and V with ho = the previous hn; h_T_half = (ho + hn) / 2
+// on T and the thicknesses of the advection velocity grids, each written by
+// the thread that owns its source value (UU.hn(j, i-1) = VV.hn(j-1, i) =
+// h_T_half(j, i), UV.hn(j-1, i-1) = VU.hn(j-1, i-1) = X.hn(j, i)); the
+// vertical coordinates of T, U and V accumulate in the same sweep and the T
+// centre depths follow in a second, downward sweep over the new T
+// thicknesses.  Same arithmetic as the separate array operations.
 // ---------------------------------------------------------------------------
 struct Depth3DArgs {
     int nx, ny, nz;
@@ -373,61 +375,85 @@ struct Depth3DArgs {
     double *hhalf, *hnuu, *hnvv, *hnuv, *hnvu;
 };
 
-__device__ __forceinline__ void sigma_point(double dga, long long p, long long q, const int* __restrict__ m,
-                                            const double* __restrict__ D, double* __restrict__ hn,
-                                            double* __restrict__ ho)
-{
-    const double old = hn[q];
-    if (ho) ho[q] = old;
-    hn[q] = m[p] != 0 ? dga * D[p] : old;
-}
-
-// grid (ceil((nx + 1) / 128), ny + 1, nz)
-__global__ void depth_3d_sigma_kernel(Depth3DArgs a)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, k = blockIdx.z;
-    const double dga = a.dga[k];
-    if (i <= a.nx && j <= a.ny) {  // X grid: (ny + 1) x (nx + 1)
-        const long long px = (long long)j * (a.nx + 1) + i;
-        sigma_point(dga, px, px + k * a.planex, a.mx, a.Dx, a.hnx, nullptr);
+// one level of the upward coordinate sweep of a column (t2vc_column's
+// arithmetic): zc(k) from zc(k-1) and the mean of the two thicknesses, zf(k+1)
+// = zf(k) + h(k)
+struct CoordSweep {
+    double zc, zf, hprev;
+    __device__ __forceinline__ void level(int k, long long q, long long plane, double H, double hk, double* zcp,
+                                          double* zfp)
+    {
+        if (k == 0) {
+            zc = -H + 0.5 * hk;
+            zf = -H;
+            zfp[q] = zf;
+        } else {
+            zc = zc + 0.5 * (hprev + hk);
+        }
+        zcp[q] = zc;
+        zf = zf + hk;
+        zfp[q + plane] = zf;
+        hprev = hk;
     }
-    if (i >= a.nx || j >= a.ny) return;
-    const long long p = (long long)j * a.nx + i, q = p + k * a.plane;
-    sigma_point(dga, p, q, a.mt, a.Dt, a.hnt, a.hot);
-    sigma_point(dga, p, q, a.mu, a.Du, a.hnu, a.hou);
-    sigma_point(dga, p, q, a.mv, a.Dv, a.hnv, a.hov);
-}
+};
 
-// grid (ceil(nx / 128), ny, nz)
-__global__ void depth_3d_halves_kernel(Depth3DArgs a)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, k = blockIdx.z;
-    if (i >= a.nx || j >= a.ny) return;
-    const long long p = (long long)j * a.nx + i, q = p + k * a.plane;
-    const double hh = (a.hot[q] + a.hnt[q]) * 0.5;
-    a.hhalf[q] = hh;
-    if (i >= 1) a.hnuu[q - 1] = hh;     // UU.hn[:, :, :-1] = h_T_half[:, :, 1:]
-    if (j >= 1) a.hnvv[q - a.nx] = hh;  // VV.hn[:, :-1, :] = h_T_half[:, 1:, :]
-    const double hx = a.hnx[(long long)(j + 1) * (a.nx + 1) + (i + 1) + k * a.planex];
-    a.hnuv[q] = hx;                     // UV.hn = X.hn[:, 1:, 1:]
-    a.hnvu[q] = hx;                     // VU.hn = UV.hn
-}
-
-// one thread per column
-__global__ void depth_3d_coords_kernel(Depth3DArgs a)
+// grid (ceil((nx + 1) / 128), ny + 1)
+__global__ void depth_3d_column_kernel(Depth3DArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
-    if (i >= a.nx || j >= a.ny) return;
-    const long long p = (long long)j * a.nx + i;
-    if (a.mt[p] != 0) {
-        t2vc_column(a.plane, a.nz, p, a.Ht, a.hnt, a.zct, a.zft);
-        if (a.depth) t2cd_column(a.plane, a.nz, p, a.hnt, a.depth);
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    if (i > nx || j > ny) return;
+    const long long plane = a.plane, planex = a.planex;
+    const long long px = (long long)j * (nx + 1) + i;
+    const bool xm = a.mx[px] != 0;
+    const double Dx = xm ? a.Dx[px] : 0.0;
+    const bool xuv = i >= 1 && j >= 1;
+    const long long quv = (long long)(j - 1) * nx + (i - 1);
+    const bool tin = i < nx && j < ny;
+    const long long p = (long long)j * nx + i;
+    bool mt = false, mu = false, mv = false;
+    double Dt = 0.0, Du = 0.0, Dv = 0.0, Ht = 0.0, Hu = 0.0, Hv = 0.0;
+    if (tin) {
+        mt = a.mt[p] != 0; mu = a.mu[p] != 0; mv = a.mv[p] != 0;
+        if (mt) { Dt = a.Dt[p]; Ht = a.Ht[p]; }
+        if (mu) { Du = a.Du[p]; Hu = a.Hu[p]; }
+        if (mv) { Dv = a.Dv[p]; Hv = a.Hv[p]; }
     }
-    if (a.mu[p] != 0) t2vc_column(a.plane, a.nz, p, a.Hu, a.hnu, a.zcu, a.zfu);
-    if (a.mv[p] != 0) t2vc_column(a.plane, a.nz, p, a.Hv, a.hnv, a.zcv, a.zfv);
+    CoordSweep st{0.0, 0.0, 0.0}, su{0.0, 0.0, 0.0}, sv{0.0, 0.0, 0.0};
+    for (int k = 0; k < nz; k++) {
+        const double dga = a.dga[k];
+        const long long qx = px + k * planex;
+        double hx;
+        if (xm) {
+            hx = dga * Dx;
+            a.hnx[qx] = hx;
+        } else {
+            hx = a.hnx[qx];
+        }
+        if (xuv) {
+            a.hnuv[quv + k * plane] = hx;
+            a.hnvu[quv + k * plane] = hx;
+        }
+        if (!tin) continue;
+        const long long q = p + k * plane;
+        const double ot = a.hnt[q], ou = a.hnu[q], ov = a.hnv[q];
+        a.hot[q] = ot;
+        a.hou[q] = ou;
+        a.hov[q] = ov;
+        double nt = ot, nu = ou, nv = ov;
+        if (mt) { nt = dga * Dt; a.hnt[q] = nt; }
+        if (mu) { nu = dga * Du; a.hnu[q] = nu; }
+        if (mv) { nv = dga * Dv; a.hnv[q] = nv; }
+        const double hh = (ot + nt) * 0.5;
+        a.hhalf[q] = hh;
+        if (i >= 1) a.hnuu[q - 1] = hh;
+        if (j >= 1) a.hnvv[q - nx] = hh;
+        if (mt) st.level(k, q, plane, Ht, nt, a.zct, a.zft);
+        if (mu) su.level(k, q, plane, Hu, nu, a.zcu, a.zfu);
+        if (mv) sv.level(k, q, plane, Hv, nv, a.zcv, a.zfv);
+    }
+    if (mt && a.depth) t2cd_column(plane, nz, p, a.hnt, a.depth);
 }
 
 extern "C" int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny, int nz, cudaStream_t stream)
@@ -444,11 +470,7 @@ extern "C" int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny
                   f->H_t, f->H_u, f->H_v, f->hn_t, f->hn_u, f->hn_v, f->hn_x, f->ho_t, f->ho_u, f->ho_v,
                   f->zc_t, f->zc_u, f->zc_v, f->zf_t, f->zf_u, f->zf_v, f->depth,
                   f->h_T_half, f->hn_uu, f->hn_vv, f->hn_uv, f->hn_vu};
-    depth_3d_sigma_kernel<<<dim3(getm_div_up(nx + 1, 128), ny + 1, nz), 128, 0, stream>>>(a);
-    GETM_CHECK_LAUNCH();
-    depth_3d_halves_kernel<<<dim3(getm_div_up(nx, 128), ny, nz), 128, 0, stream>>>(a);
-    GETM_CHECK_LAUNCH();
-    depth_3d_coords_kernel<<<dim3(getm_div_up(nx, 128), ny), 128, 0, stream>>>(a);
+    depth_3d_column_kernel<<<dim3(getm_div_up(nx + 1, 128), ny + 1), 128, 0, stream>>>(a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

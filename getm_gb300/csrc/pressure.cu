@@ -264,30 +264,98 @@ __global__ void smcw_column_mixed_kernel(int nx, int ny, int nz, int ilo, int ih
 #undef Z
 }
 
-__global__ void smcw_gradient_mixed_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
-                                           const int* umask, const int* vmask, const double* idxu,
-                                           const double* idyv, const double* h, const double* z,
-                                           const double* zc, const double* buoy, const double* Pw,
-                                           double* idpdx, double* idpdy)
+// Gradient, both directions, on 32 x SG_BY tiles of one level.  The raw
+// differences between neighbouring points (zc and buoyancy, x and y, each
+// gated by the mask of the velocity point between them) are formed once per
+// face into shared memory instead of three times (once for each of the three
+// points that use them); a point keeps the FP64 differences of its own faces
+// for the density-Jacobian term.  The values are those of the per-point
+// form, operation for operation.
+constexpr int SG_BX = 32, SG_BY = 8;
+
+struct SgFace {
+    float rz, rr;   // gated float differences (zero where the mask is not positive)
+    double dz, db;  // FP64 differences, valid where the mask is positive
+};
+
+__device__ __forceinline__ SgFace smcw_face(const int* __restrict__ m, long long p, long long q, long long s,
+                                            const double* __restrict__ zc, const double* __restrict__ buoy)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y + jlo;
-    int k = blockIdx.z;
-    if (i < ilo || i > ihi || j > jhi) return;
+    SgFace f{0.f, 0.f, 0.0, 0.0};
+    if (m[p] > 0) {
+        f.dz = zc[q + s] - zc[q];
+        f.db = buoy[q + s] - buoy[q];
+        f.rz = getm_d2f_approx(f.dz);
+        f.rr = getm_d2f_approx(f.db);
+    }
+    return f;
+}
+
+__global__ void smcw_gradient_mixed_kernel(
+    int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi, const int* __restrict__ umask,
+    const int* __restrict__ vmask, const double* __restrict__ idxu, const double* __restrict__ idyv,
+    const double* __restrict__ h, const double* __restrict__ zc, const double* __restrict__ buoy,
+    const double* __restrict__ Pw, double* __restrict__ idpdx, double* __restrict__ idpdy)
+{
+    // x faces of columns i0-1 .. i0+SG_BX, y faces of rows j0-1 .. j0+SG_BY
+    __shared__ float sZx[SG_BY][SG_BX + 2], sRx[SG_BY][SG_BX + 2];
+    __shared__ float sZy[SG_BY + 2][SG_BX], sRy[SG_BY + 2][SG_BX];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * SG_BX, j0 = jlo + blockIdx.y * SG_BY;
+    const int i = i0 + tx, j = j0 + ty;
+    const int k = blockIdx.z;
     const long long P = (long long)nx * ny;
+    const long long kP = (long long)k * P;
     const long long p = (long long)j * nx + i;
-    const long long q = p + (long long)k * P;
+    // faces needed: x at columns ilo-1 .. ihi+1 of rows jlo .. jhi, y at
+    // rows jlo-1 .. jhi+1 of columns ilo .. ihi
+    const bool rowin = j <= jhi, colin = i >= ilo && i <= ihi;
+    SgFace fx{0.f, 0.f, 0.0, 0.0}, fy{0.f, 0.f, 0.0, 0.0};
+    if (rowin && i >= ilo - 1 && i <= ihi + 1) fx = smcw_face(umask, p, p + kP, 1, zc, buoy);
+    if (colin && j <= jhi + 1) fy = smcw_face(vmask, p, p + kP, nx, zc, buoy);
+    sZx[ty][tx + 1] = fx.rz; sRx[ty][tx + 1] = fx.rr;
+    sZy[ty + 1][tx] = fy.rz; sRy[ty + 1][tx] = fy.rr;
+    if (tx < 2) {  // x faces at columns i0-1 (tx 0) and i0+SG_BX (tx 1) of row j
+        const int ii = tx == 0 ? i0 - 1 : i0 + SG_BX;
+        SgFace f{0.f, 0.f, 0.0, 0.0};
+        if (rowin && ii >= ilo - 1 && ii <= ihi + 1) {
+            const long long pp = (long long)j * nx + ii;
+            f = smcw_face(umask, pp, pp + kP, 1, zc, buoy);
+        }
+        sZx[ty][tx == 0 ? 0 : SG_BX + 1] = f.rz;
+        sRx[ty][tx == 0 ? 0 : SG_BX + 1] = f.rr;
+    }
+    if (ty < 2) {  // y faces at rows j0-1 (ty 0) and j0+SG_BY (ty 1) of column i
+        const int jj = ty == 0 ? j0 - 1 : j0 + SG_BY;
+        SgFace f{0.f, 0.f, 0.0, 0.0};
+        if (colin && jj <= jhi + 1) {
+            const long long pp = (long long)jj * nx + i;
+            f = smcw_face(vmask, pp, pp + kP, nx, zc, buoy);
+        }
+        sZy[ty == 0 ? 0 : SG_BY + 1][tx] = f.rz;
+        sRy[ty == 0 ? 0 : SG_BY + 1][tx] = f.rr;
+    }
+    __syncthreads();
+    if (!rowin || !colin) return;
+    const long long q = p + kP;
     const float x = 1.f / 12.f;
     for (int dir = 0; dir < 2; dir++) {
         const int* m = dir ? vmask : umask;
         if (m[p] != 1) continue;
         const long long s = dir ? nx : 1;
-        float rZ0 = 0.f, rR0 = 0.f, rZ1 = 0.f, rR1 = 0.f, rZ2 = 0.f, rR2 = 0.f;
-        if (m[p - s] > 0) { rZ0 = getm_d2f_approx(zc[q] - zc[q - s]); rR0 = getm_d2f_approx(buoy[q] - buoy[q - s]); }
-        const double dzc = zc[q + s] - zc[q];
-        const double dbq = buoy[q + s] - buoy[q];
-        if (m[p] > 0) { rZ1 = getm_d2f_approx(dzc); rR1 = getm_d2f_approx(dbq); }
-        if (m[p + s] > 0) { rZ2 = getm_d2f_approx(zc[q + 2 * s] - zc[q + s]); rR2 = getm_d2f_approx(buoy[q + 2 * s] - buoy[q + s]); }
+        float rZ0, rR0, rZ1, rR1, rZ2, rR2;
+        double dzc, dbq;
+        if (dir == 0) {
+            rZ0 = sZx[ty][tx]; rR0 = sRx[ty][tx];
+            rZ1 = sZx[ty][tx + 1]; rR1 = sRx[ty][tx + 1];
+            rZ2 = sZx[ty][tx + 2]; rR2 = sRx[ty][tx + 2];
+            dzc = fx.dz; dbq = fx.db;
+        } else {
+            rZ0 = sZy[ty][tx]; rR0 = sRy[ty][tx];
+            rZ1 = sZy[ty + 1][tx]; rR1 = sRy[ty + 1][tx];
+            rZ2 = sZy[ty + 2][tx]; rR2 = sRy[ty + 2][tx];
+            dzc = fy.dz; dbq = fy.db;
+        }
         const float dZx0 = smcw_harm_f(rZ0, rZ1), dZx1 = smcw_harm_f(rZ1, rZ2);
         const float dRx0 = smcw_harm_f(rR0, rR1), dRx1 = smcw_harm_f(rR1, rR2);
         const float corr = 0.2f * ((dRx1 - dRx0) * (getm_d2f_approx(dzc) - x * (dZx1 + dZx0)) -
@@ -318,9 +386,10 @@ extern "C" int getm_shchepetkin_mcwilliams_mixed(int nx, int ny, int nz, int imi
     smcw_column_mixed_kernel<<<g1, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, h, zc,
                                                      buoy, z, P_work);
     GETM_CHECK_LAUNCH();
-    dim3 g2(getm_div_up(nx, 128), jmax - jmin + 1, nz);
-    smcw_gradient_mixed_kernel<<<g2, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, umask, vmask,
-                                                       idxu, idyv, h, z, zc, buoy, P_work, idpdx, idpdy);
+    dim3 g2(getm_div_up(nx, SG_BX), getm_div_up(jmax - jmin + 1, SG_BY), nz);
+    smcw_gradient_mixed_kernel<<<g2, dim3(SG_BX, SG_BY), 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1,
+                                                                      jmax - 1, umask, vmask, idxu, idyv, h, zc,
+                                                                      buoy, P_work, idpdx, idpdy);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

@@ -88,18 +88,25 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
     return v;
 }
 
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
+
 // Grid-wide barrier k of a launch: thread 0 of every block adds one arrival
 // and waits until the count reaches k blocks per block; false when the wait
 // gave up or another block reported an error (the caller returns).  The
 // count only grows during a launch; the last block to leave the kernel
-// resets it (grid_exit) for the next launch on the stream.
+// resets it (grid_exit) for the next launch on the stream.  Ordering: the
+// block barrier orders the block's writes before thread 0's release
+// arrival, and thread 0's acquire load followed by the block barrier orders
+// the other blocks' writes before every thread's later reads.
 __device__ __forceinline__ bool grid_barrier(unsigned* sync, unsigned& target, int& s_ok)
 {
     __syncthreads();
     if (threadIdx.x == 0 && threadIdx.y == 0) {
         target += gridDim.x;
-        __threadfence();
-        atomicAdd(&sync[0], 1u);
+        red_release_add(&sync[0], 1u);
         int ok = 1;
         unsigned it = 0;
         while (ld_acquire(&sync[0]) < target) {
@@ -113,7 +120,6 @@ __device__ __forceinline__ bool grid_barrier(unsigned* sync, unsigned& target, i
                 break;
             }
         }
-        __threadfence();
         s_ok = ok;
     }
     __syncthreads();

@@ -235,6 +235,162 @@ __global__ void __launch_bounds__(128, getm_increment_form<T> ? 8 : 1) vd_column
     }
 }
 
+// Increment form with the elimination coefficients in global memory (the
+// mixed form's column solve): the same arithmetic as vd_column_kernel<float,
+// true>, restructured for memory-level parallelism.  The loads of the
+// forward elimination do not depend on the elimination itself, so the
+// operands of the next level (thicknesses, nuh, field values, sources) are
+// issued one level ahead of the arithmetic, and those of the back
+// substitution likewise; NT fields share the thickness and nuh loads and
+// sweep together (work: 2 nz planes per field of a group).  SRC: whether a
+// field of the group has ea2 or ea4 (without, no registers are spent on
+// them).
+template <int NT, bool SRC>
+__device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c, int t0)
+{
+    const long long P = a.plane;
+    const int nz = a.nz;
+    const double* __restrict__ ho = a.ho + c;
+    const double* __restrict__ hn = a.hn + c;
+    const float* __restrict__ nuh = a.nuh + c;
+    const bool one_h = a.ho == a.hn;
+    const float co = (float)(1.0 - a.cnpar), cn = (float)a.cnpar, dt2 = (float)(2.0 * a.dt);
+    float* v[NT];
+    const float* e2[NT];
+    const float* e4[NT];
+    float* ru[NT];
+    float* qu[NT];
+    float mol[NT];
+#pragma unroll
+    for (int t = 0; t < NT; t++) {
+        v[t] = a.var[t0 + t] + c;
+        e2[t] = SRC && a.ea2[t0 + t] ? a.ea2[t0 + t] + c : nullptr;
+        e4[t] = SRC && a.ea4[t0 + t] ? a.ea4[t0 + t] + c : nullptr;
+        ru[t] = a.work + c + (long long)(2 * t) * nz * P;
+        qu[t] = ru[t] + (long long)nz * P;
+        mol[t] = (float)a.molecular[t0 + t];
+    }
+    // level k operands (current) and the raw loads of level k-1 (next)
+    int k = nz - 1;
+    double ho_c = ho[k * P], hn_c = hn[k * P];
+    double ho_n = ho[(k - 1) * P], hn_n = hn[(k - 1) * P];
+    float nuh_c = nuh[k * P];  // interface below level k
+    float vk[NT], vn[NT], e2c[NT], e4c[NT];
+#pragma unroll
+    for (int t = 0; t < NT; t++) {
+        vk[t] = v[t][k * P];
+        vn[t] = v[t][(k - 1) * P];
+        e2c[t] = SRC && e2[t] ? e2[t][k * P] : 0.f;
+        e4c[t] = SRC && e4[t] ? e4[t][k * P] : 0.f;
+    }
+    float hoF = vd_h<float>(ho_c), hnF = vd_h<float>(hn_c);
+    float dh = one_h ? 0.f : getm_d2f_approx(ho_c - hn_c);
+    float rk[NT], qk[NT], aoa[NT], ana[NT], vkp1[NT];
+    // surface layer (diffusion.F90:238-245) and the inner layers
+    // (:247-258, elimination :287-290)
+    for (; k >= 1; k--) {
+        // next level's raw operands, one level ahead
+        const int kn = k - 1;
+        double ho_nn = 0.0, hn_nn = 0.0;
+        float nuh_n = 0.f, vnn[NT], e2n[NT], e4n[NT];
+        if (kn >= 1) {
+            ho_nn = ho[(kn - 1) * P];
+            hn_nn = hn[(kn - 1) * P];
+        }
+        nuh_n = nuh[kn * P];
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            vnn[t] = kn >= 1 ? v[t][(kn - 1) * P] : 0.f;
+            e2n[t] = SRC && e2[t] ? e2[t][kn * P] : 0.f;
+            e4n[t] = SRC && e4[t] ? e4[t][kn * P] : 0.f;
+        }
+        // interface below level k (vd_aux with C level k-1)
+        const float hoFn = vd_h<float>(ho_n), hnFn = vd_h<float>(hn_n);
+        const float so = hoF + hoFn, sn = hnF + hnFn;
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            const float x = dt2 * (nuh_c + mol[t]);
+            const float aob = co * x / so;
+            const float anb = cn * x / sn;
+            const float a1 = -anb;
+            float a2, a4;
+            if (k == nz - 1) {
+                a2 = hnF + anb;
+                a4 = vk[t] * dh + (vn[t] - vk[t]) * (aob + anb);
+            } else {
+                a2 = hnF + ana[t] + anb;
+                a4 = vk[t] * dh + (vkp1[t] - vk[t]) * (aoa[t] + ana[t]) + (vn[t] - vk[t]) * (aob + anb);
+            }
+            if (SRC && e2[t]) a4 = a4 + e2c[t] * vk[t];
+            if (SRC && e2[t]) a2 = a2 - e2c[t];
+            if (SRC && e4[t]) a4 = a4 + e4c[t];
+            if (k == nz - 1) {
+                rk[t] = a1 / a2;
+                qk[t] = a4 / a2;
+            } else {
+                const float a3 = -ana[t];
+                const float den = a2 - a3 * rk[t];
+                rk[t] = a1 / den;
+                qk[t] = (a4 - a3 * qk[t]) / den;
+            }
+            ru[t][k * P] = rk[t];
+            qu[t][k * P] = qk[t];
+            aoa[t] = aob; ana[t] = anb;
+            vkp1[t] = vk[t]; vk[t] = vn[t]; vn[t] = vnn[t];
+            e2c[t] = e2n[t]; e4c[t] = e4n[t];
+        }
+        hoF = hoFn; hnF = hnFn;
+        dh = one_h ? 0.f : getm_d2f_approx(ho_n - hn_n);
+        ho_n = ho_nn; hn_n = hn_nn;
+        nuh_c = nuh_n;
+    }
+    // bottom layer (:260-267, :291-292), back substitution (:304-307);
+    // the old values of level k+1 are read before level k is written
+    float vprev[NT], xn[NT], rn[NT], qn[NT];
+#pragma unroll
+    for (int t = 0; t < NT; t++) {
+        const float a3 = -ana[t];
+        float a2 = hnF + ana[t];
+        float a4 = vk[t] * dh + (vkp1[t] - vk[t]) * (aoa[t] + ana[t]);
+        if (SRC && e2[t]) a4 = a4 + e2c[t] * vk[t];
+        if (SRC && e2[t]) a2 = a2 - e2c[t];
+        if (SRC && e4[t]) a4 = a4 + e4c[t];
+        vprev[t] = (a4 - a3 * qk[t]) / (a2 - a3 * rk[t]);
+        xn[t] = v[t][P];
+        rn[t] = ru[t][P];
+        qn[t] = qu[t][P];
+        v[t][0] = vk[t] + vprev[t];
+    }
+    for (k = 1; k < nz; k++) {
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            const float x_old = xn[t], r = rn[t], q = qn[t];
+            if (k + 1 < nz) {
+                xn[t] = v[t][(k + 1) * P];
+                rn[t] = ru[t][(k + 1) * P];
+                qn[t] = qu[t][(k + 1) * P];
+            }
+            vprev[t] = q - r * vprev[t];
+            v[t][k * P] = x_old + vprev[t];
+        }
+    }
+}
+
+// PAIRS: fields in pairs (then an odd last one alone), else one at a time
+template <bool SRC, bool PAIRS>
+__global__ void __launch_bounds__(128, 8) vd_inc_kernel(VDArgs<float> a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= a.nx_) return;
+    const long long c = (long long)j * a.nx_ + i;
+    if (a.mask[c] != 1) return;
+    int t0 = 0;
+    if constexpr (PAIRS)
+        for (; t0 + 2 <= a.ntracer; t0 += 2) vd_inc_sweep<2, SRC>(a, c, t0);
+    for (; t0 < a.ntracer; t0++) vd_inc_sweep<1, SRC>(a, c, t0);
+}
+
 // prepare as a separate call (diffusion.F90:163-171): auxo/auxn at every
 // point of the halo-inclusive extent, Fortran levels kmin..kmax-1.
 __global__ void vd_prepare_kernel(int nx_, int ny_, int nz, long long plane, double molecular,
@@ -256,6 +412,19 @@ static int vd_launch(VDArgs<T>& a, cudaStream_t stream)
 {
     if (a.work) {
         dim3 grid(getm_div_up(a.nx_, 128), a.ny_);
+        if constexpr (getm_increment_form<T>) {
+            if (a.nz > 1 && !a.auxo) {
+                bool src = false;
+                for (int t = 0; t < a.ntracer; t++) src = src || a.ea2[t] || a.ea4[t];
+                const bool pairs = a.ntracer > 1;
+                if (src && pairs) vd_inc_kernel<true, true><<<grid, 128, 0, stream>>>(a);
+                else if (src) vd_inc_kernel<true, false><<<grid, 128, 0, stream>>>(a);
+                else if (pairs) vd_inc_kernel<false, true><<<grid, 128, 0, stream>>>(a);
+                else vd_inc_kernel<false, false><<<grid, 128, 0, stream>>>(a);
+                GETM_CHECK_LAUNCH();
+                return GETM_OK;
+            }
+        }
         vd_column_kernel<T, true><<<grid, 128, 0, stream>>>(a);
         GETM_CHECK_LAUNCH();
         return GETM_OK;

@@ -261,9 +261,10 @@ class VerticalDiffusion:
         e2 = _lib.ptr_array([_p(e) for e in ea2s]) if ea2s is not None and any(e is not None for e in ea2s) else None
         e4 = _lib.ptr_array([_p(e) for e in ea4s]) if ea4s is not None and any(e is not None for e in ea4s) else None
         sfx = _sfx(nuh.all_values, *[v.all_values for v in vars])
-        # elimination coefficients of the column solves (2 nz planes, reused)
+        # elimination coefficients of the column solves (2 nz planes per field
+        # solved at once, reused; the float solve takes its fields in pairs)
         dt = vars[0].all_values.dtype
-        need = 2 * g.nz_ * g.ny_ * g.nx_
+        need = 2 * (2 if n > 1 and dt == torch.float32 else 1) * g.nz_ * g.ny_ * g.nx_
         w = self._work.get(dt)
         if w is None or w.numel() < need:
             w = self._work[dt] = torch.empty(need, dtype=dt, device=nuh.all_values.device)

@@ -480,8 +480,8 @@ class Simulation:
         V.ugrid.D.all_values[:, :] = U.vgrid.D.all_values
 
     def _update_depth_3d(self):
-        """The 3D part of update_depth (simulation.py:1588-1630) in three
-        launches (getm_update_depth_3d)."""
+        """The 3D part of update_depth (simulation.py:1588-1630) in one
+        launch (getm_update_depth_3d)."""
         if self.fused_2d:
             if getattr(self, "_depth3d", None) is None:
                 depth = self.depth if self.runtype == RunType.BAROCLINIC else None

@@ -145,7 +145,8 @@ int getm_vertical_diffusion_apply(getm_vertical_diffusion* diff, int nx, int ny,
  * diffusivity and optional ea2/ea4 (arrays of device pointers, entries may be
  * NULL; the arrays themselves may be NULL).  work: NULL (elimination
  * coefficients in shared memory) or a device buffer of 2*nx*ny*nz elements
- * of the field type (more columns resident per SM).                         */
+ * of the field type (more columns resident per SM); the _f32 form solves
+ * its fields in pairs and needs 4*nx*ny*nz elements when ntracer > 1.       */
 int getm_vertical_diffusion_batch(int nx, int ny, int nz, const int* mask, const double* nuh,
                                   double timestep, double cnpar, const double* ho,
                                   const double* hn, int ntracer, const double* molecular,
@@ -538,8 +539,8 @@ int getm_velocities_3d_f32(long long n, const float* pk, const double* hnu, cons
                            const double* hnv, float* uk, float* vk, cudaStream_t stream);
 
 /* Simulation.update_depth, 3D part (python/pygetm/simulation.py:1588-1630)
- * with Sigma coordinates (vertical_coordinates.py:106-113), in three
- * launches with the arithmetic of the separate array operations: ho = hn (T,
+ * with Sigma coordinates (vertical_coordinates.py:106-113), in one launch
+ * with the arithmetic of the separate array operations: ho = hn (T,
  * U, V); hn = dga Dclip where the mask is non-zero (T, U, V, X);
  * thickness2vertical_coordinates of T, U, V (zc, zf); thickness2center_depth
  * of T into depth (when not NULL); h_T_half = (ho + hn) / 2 and the

@@ -20,7 +20,8 @@ from .simulation import Fluxes, Simulation
 from .workloads import Workload
 
 
-def make_member(wl: Workload, precision: str = "mixed", device="cuda", substep_kernel: bool = False) -> Simulation:
+def make_member(wl: Workload, precision: str = "mixed", device="cuda", substep_kernel: bool = False,
+                concurrent_3d: bool = True) -> Simulation:
     """Build and start a simulation for one ensemble member (rest state,
     linear temperature drop ``dT`` per 100 m from 20 degC at the surface).
     Members replay concurrently on several streams, so by default their 2D
@@ -28,7 +29,8 @@ def make_member(wl: Workload, precision: str = "mixed", device="cuda", substep_k
     that needs every SM of the GPU at once."""
     p = wl.params
     sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device,
-                     airsea=Fluxes(taux=p.get("taux", 0.0)), substep_kernel=substep_kernel)
+                     airsea=Fluxes(taux=p.get("taux", 0.0)), substep_kernel=substep_kernel,
+                     concurrent_3d=concurrent_3d)
     zc = sim.T.zc.all_values
     dT = p.get("dT", 10.0)
     temp0 = torch.where(sim.T.mask.all_values[None] != 0, 20.0 + dT * zc / 100.0, sim.temp.all_values.double())

@@ -277,8 +277,8 @@ class Momentum:
 
     # ------------------------------------------------------------------ 3D
     def advance(self, timestep: float, split_factor: int, tausx: Array, tausy: Array, dpdx: Array, dpdy: Array,
-                idpdx: Array, idpdy: Array, viscosity: Array):
-        """momentum.py:760-858"""
+                idpdx: Array, idpdy: Array, viscosity: Array, side_stream=None):
+        """momentum.py:760-858.  ``side_stream``: see update_diagnostics."""
         torch.mul(self._U_cum, 1.0 / split_factor, out=self.Ui.all_values)
         torch.mul(self._V_cum, 1.0 / split_factor, out=self.Vi.all_values)
         self._U_cum.zero_()
@@ -301,10 +301,15 @@ class Momentum:
             v()
             u()
         self._u3dfirst = not self._u3dfirst
-        self.update_diagnostics(timestep, viscosity, skip_coriolis=True)
+        self.update_diagnostics(timestep, viscosity, skip_coriolis=True, side_stream=side_stream)
 
-    def update_diagnostics(self, timestep: float, viscosity: Array, skip_coriolis: bool = False):
-        """momentum.py:860-1015"""
+    def update_diagnostics(self, timestep: float, viscosity: Array, skip_coriolis: bool = False,
+                           side_stream=None):
+        """momentum.py:860-1015.  ``side_stream``: a CUDA stream on which the
+        advection of the 3D momentum and the slow terms (advpk, advqk, SxA,
+        SyA, SxD, SyD, SxF, SyF) are issued after the velocities; the caller
+        joins it (current_stream().wait_stream) before anything reads them or
+        the momentum advection handles and 2D work arrays they use."""
         if not skip_coriolis:
             self.coriolis(self.pk, self.corqk, True)
             self.coriolis(self.qk, self.corpk, False)
@@ -318,6 +323,16 @@ class Momentum:
             self.bottom_friction(self.u_bot, self.v_bot, self.hU_bot, self.hV_bot, self.rru, self.rrv)
         _pygetm.bottom_shear_velocity(self.u_bot, self.v_bot, self.rru, self.rrv, self.ustar2_bx, self.ustar2_by,
                                       self.ustar_b)
+        if side_stream is None:
+            self._slow_terms(timestep)
+            return
+        side_stream.wait_stream(torch.cuda.current_stream(side_stream.device))
+        with torch.cuda.stream(side_stream):
+            self._slow_terms(timestep)
+
+    def _slow_terms(self, timestep: float):
+        """The tail of update_diagnostics (momentum.py:944-1015): advection of
+        the 3D momentum, its depth-integrated counterpart and the slow terms."""
         # advpk = uk, advqk = vk and the velocities on the advection grids
         # (the interpolations below, all at once)
         _pygetm.momentum_3d_advection_inputs(self.uk, self.vk, self.ww, self.uua3d, self.uva3d, self.vua3d,

@@ -110,7 +110,7 @@ class Simulation:
                  airsea: Optional[Fluxes] = None, internal_pressure: str = "shchepetkin_mcwilliams",
                  Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
                  nuh: float = 0.0, precision: str = "fp64", fused_2d: bool = True, substep_kernel: bool = True,
-                 device="cuda"):
+                 concurrent_3d: bool = True, device="cuda"):
         """``precision``: "fp64" (the plain form) or "mixed" (float32 tracers,
         3D velocities and their tendencies and diffusivities; float64
         elevations, depths, layer thicknesses, 2D transports and their
@@ -121,13 +121,19 @@ class Simulation:
         ``substep_kernel``: in addition, a substep that is not followed by a
         3D step runs as one persistent kernel launch (closed domains with the
         default Coriolis scheme, FULL 2D advection split, no horizontal
-        momentum diffusion, 3D run types)."""
+        momentum diffusion, 3D run types).  ``concurrent_3d``: in a 3D step,
+        the advection of the 3D momentum and the slow terms it feeds run on a
+        second stream, concurrently with the tracers, density and internal
+        pressure (neither reads what the other writes; the streams join
+        before the 2D depth update)."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
         self.fused_2d = fused_2d
         self.substep_kernel = substep_kernel and fused_2d
         self._split2d = None
+        self._side_stream = None
+        self._forked = False
         d3 = torch.float32 if precision == "mixed" else torch.float64
         self.dtype3d = d3
         if Dmin <= 0.0:
@@ -205,6 +211,8 @@ class Simulation:
             self._P_work = torch.zeros((T.nz + 2, T.ny_, T.nx_), dtype=torch.float64, device=T.device)
         self.update_depth(_3d=three_d)
         self.update_depth(_3d=three_d)
+        if concurrent_3d and three_d and T.device.type == "cuda":
+            self._side_stream = torch.cuda.Stream(device=T.device)
 
     # ---------------------------------------------------------------- driver
     def start(self, timestep: float, split_factor: int = 1):
@@ -317,7 +325,8 @@ class Simulation:
             # without rivers and with zero precipitation-evaporation.
             self.update_depth(_3d=True, timestep=self.macrotimestep)
             self.momentum.advance(self.macrotimestep, self.split_factor, self.tausxo, self.tausyo, self.dpdxo,
-                                  self.dpdyo, self.idpdx, self.idpdy, self.num)
+                                  self.dpdyo, self.idpdx, self.idpdy, self.num, side_stream=self._side_stream)
+            self._forked = self._side_stream is not None
             self.tracers.advance(self.macrotimestep, self.momentum.uk, self.momentum.vk, self.momentum.ww, self.nuh)
             if self.runtype == RunType.BAROCLINIC and self.delay_slow_ip:
                 _pygetm.column_sums([(self.idpdx, self.momentum.SxB), (self.idpdy, self.momentum.SyB)])
@@ -336,6 +345,9 @@ class Simulation:
             self.update_internal_pressure()
             if not self.delay_slow_ip:
                 _pygetm.column_sums([(self.idpdx, self.momentum.SxB), (self.idpdy, self.momentum.SyB)])
+        if self._forked:  # the momentum advection and slow terms are done
+            torch.cuda.current_stream(self.T.device).wait_stream(self._side_stream)
+            self._forked = False
         self.update_depth()
         self.momentum.update_depth_integrated_diagnostics(self.timestep, skip_coriolis=not starting,
                                                          update_z0b=update_z0b)

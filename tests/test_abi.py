@@ -125,3 +125,14 @@ def test_depth3d_fields_layout_matches_header():
     names = [d.strip().split("*")[-1].strip() for d in body.group(1).split(";") if d.strip()]
     assert tuple(names) == _pygetm.DEPTH3D_FIELDS
     assert ctypes.sizeof(_pygetm.Depth3DFields) == 8 * len(names)
+
+
+def test_package_modules_import():
+    """Every module of the package imports without a GPU (syntax, names)."""
+    import importlib
+    from pathlib import Path
+
+    import getm_gb300
+
+    for f in sorted(Path(getm_gb300.__path__[0]).glob("*.py")):
+        importlib.import_module("getm_gb300." + f.stem)

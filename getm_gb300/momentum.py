@@ -51,6 +51,7 @@ class Momentum:
         # fused 2D substep kernels (one launch per sequence of operations);
         # False runs each operation as its own kernel
         self.fused_2d = True
+        self._v_stream = None  # see _diagnostics_tail
         self._ob = None  # open-boundary operations (set by the simulation)
 
     # ------------------------------------------------------------------ setup
@@ -305,16 +306,31 @@ class Momentum:
 
     def update_diagnostics(self, timestep: float, viscosity: Array, skip_coriolis: bool = False,
                            side_stream=None):
-        """momentum.py:860-1015.  ``side_stream``: a CUDA stream on which the
-        advection of the 3D momentum and the slow terms (advpk, advqk, SxA,
-        SyA, SxD, SyD, SxF, SyF) are issued after the velocities; the caller
-        joins it (current_stream().wait_stream) before anything reads them or
-        the momentum advection handles and 2D work arrays they use."""
+        """momentum.py:860-1015.  ``side_stream``: a CUDA stream on which
+        everything after the 3D velocities and the vertical velocity is
+        issued (shear frequency SS, bottom drag rru/rrv and shear velocities,
+        the advection of the 3D momentum and the slow terms advpk, advqk,
+        SxA, SyA, SxD, SyD, SxF, SyF); the caller joins it
+        (current_stream().wait_stream) before anything reads those or the
+        momentum advection handles and 2D work arrays they use."""
         if not skip_coriolis:
             self.coriolis(self.pk, self.corqk, True)
             self.coriolis(self.qk, self.corpk, False)
         _pygetm.w_momentum_3d(self.pk, self.qk, timestep, self.ww)
         _pygetm.velocities_3d(self.pk, self.qk, self.uk, self.vk)
+        if side_stream is None:
+            self._diagnostics_tail(timestep)
+            return
+        side_stream.wait_stream(torch.cuda.current_stream(side_stream.device))
+        with torch.cuda.stream(side_stream):
+            self._diagnostics_tail(timestep, self._v_stream)
+
+    def _diagnostics_tail(self, timestep: float, v_stream=None):
+        """update_diagnostics after the velocities (momentum.py:880-1015):
+        shear frequency, bottom stress, advection of the 3D momentum, its
+        depth-integrated counterpart and the slow terms.  ``v_stream``: a
+        stream on which the advection of the V momentum runs beside that of
+        the U momentum (separate handles, inputs and outputs)."""
         _pygetm.shear_frequency(self.uk, self.vk, self.SS)
         if self.u_bot is self._u_bot64:
             self._u_bot64.all_values.copy_(self.uk.all_values[0])
@@ -323,26 +339,27 @@ class Momentum:
             self.bottom_friction(self.u_bot, self.v_bot, self.hU_bot, self.hV_bot, self.rru, self.rrv)
         _pygetm.bottom_shear_velocity(self.u_bot, self.v_bot, self.rru, self.rrv, self.ustar2_bx, self.ustar2_by,
                                       self.ustar_b)
-        if side_stream is None:
-            self._slow_terms(timestep)
-            return
-        side_stream.wait_stream(torch.cuda.current_stream(side_stream.device))
-        with torch.cuda.stream(side_stream):
-            self._slow_terms(timestep)
-
-    def _slow_terms(self, timestep: float):
-        """The tail of update_diagnostics (momentum.py:944-1015): advection of
-        the 3D momentum, its depth-integrated counterpart and the slow terms."""
         # advpk = uk, advqk = vk and the velocities on the advection grids
         # (the interpolations below, all at once)
         _pygetm.momentum_3d_advection_inputs(self.uk, self.vk, self.ww, self.uua3d, self.uva3d, self.vua3d,
                                              self.vva3d, self._ww_u, self._ww_v, self.advpk, self.advqk)
+        def v_advection():
+            self.vadv.apply_3d(self.vua3d, self.vva3d, self._ww_v,
+                               timestep, self.advqk, new_h=True, skip_initial_halo_exchange=True)
+            _pygetm.reconstruct_transport_change(self.advqk, self.vadv.h, self.qk, timestep)
+
+        here = torch.cuda.current_stream(self.uk.all_values.device) if v_stream is not None else None
+        if v_stream is not None:
+            v_stream.wait_stream(here)
+            with torch.cuda.stream(v_stream):
+                v_advection()
         self.uadv.apply_3d(self.uua3d, self.uva3d, self._ww_u,
                            timestep, self.advpk, new_h=True, skip_initial_halo_exchange=True)
         _pygetm.reconstruct_transport_change(self.advpk, self.uadv.h, self.pk, timestep)
-        self.vadv.apply_3d(self.vua3d, self.vva3d, self._ww_v,
-                           timestep, self.advqk, new_h=True, skip_initial_halo_exchange=True)
-        _pygetm.reconstruct_transport_change(self.advqk, self.vadv.h, self.qk, timestep)
+        if v_stream is None:
+            v_advection()
+        else:
+            here.wait_stream(v_stream)
         if self.diffuse_momentum:
             _pygetm.momentum_diffusion(self.uua.grid.hn, self.uva.grid.hn, self.vua.grid.hn, self.vva.grid.hn,
                                        self.uk, self.vk, self._Am_const, self.diffpk, self.diffqk)

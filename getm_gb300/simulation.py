@@ -122,10 +122,12 @@ class Simulation:
         3D step runs as one persistent kernel launch (closed domains with the
         default Coriolis scheme, FULL 2D advection split, no horizontal
         momentum diffusion, 3D run types).  ``concurrent_3d``: in a 3D step,
-        the advection of the 3D momentum and the slow terms it feeds run on a
-        second stream, concurrently with the tracers, density and internal
-        pressure (neither reads what the other writes; the streams join
-        before the 2D depth update)."""
+        the shear frequency, the bottom stress, the advection of the 3D
+        momentum and the slow terms it feeds run on a second stream,
+        concurrently with the tracers, density and internal pressure
+        (neither reads what the other writes; the streams join before the
+        2D depth update), and the advection of the V momentum on a third,
+        beside that of the U momentum."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
@@ -213,6 +215,7 @@ class Simulation:
         self.update_depth(_3d=three_d)
         if concurrent_3d and three_d and T.device.type == "cuda":
             self._side_stream = torch.cuda.Stream(device=T.device)
+            self.momentum._v_stream = torch.cuda.Stream(device=T.device)
 
     # ---------------------------------------------------------------- driver
     def start(self, timestep: float, split_factor: int = 1):

@@ -424,14 +424,20 @@ __device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const floa
     float hkf = getm_d2f_approx(hk), hk1f = getm_d2f_approx(hk1);
     float Wm = 0.f;    // W_{k-1} (0 below the bottom level)
     float wkm1 = a.w[c];
+    // the interface values above level k, loaded one level ahead (the loads
+    // of a level do not depend on the stores of the level before)
+    float Wn = (nz > 1) ? wv[c + P] : 0.f;
+    float wkn = a.w[c + P];
     for (int k = 0; k < nz; k++) {
         float fk2[NT];
         double hk2 = 0.0;
 #pragma unroll
         for (int q = 0; q < NT; q++) fk2[q] = (k + 2 < nz) ? fs[q][c + (k + 2) * P] : 0.f;
         if (k + 2 < nz) hk2 = hs[c + (k + 2) * P];
-        const float W = (k < nz - 1) ? wv[c + (k + 1) * P] : 0.f;
-        const float wk = a.w[c + (k + 1) * P];
+        const float W = Wn;
+        const float wk = wkn;
+        Wn = (k + 1 < nz - 1) ? wv[c + (k + 2) * P] : 0.f;
+        wkn = (k + 1 < nz) ? a.w[c + (k + 2) * P] : 0.f;
         const float cfl = fabsf(W) * dtf / fminf(hkf, hk1f) * itf;
         const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl);
         const float dh = dtkf * (wk - wkm1);
@@ -495,11 +501,13 @@ __device__ __forceinline__ int w_iters_from(double cfl)
 
 // Thread per column.
 template <typename T>
-__global__ void __launch_bounds__(128, getm_increment_form<T> ? 8 : 1) wpass_kernel(WPassArgs<T> a)
+// block (32, 4): 32 columns of 4 rows (row lengths need not be multiples
+// of 128 columns)
+__global__ void __launch_bounds__(128, getm_increment_form<T> ? 7 : 1) wpass_kernel(WPassArgs<T> a)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i >= a.nx_) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 4 + threadIdx.y;
+    if (i >= a.nx_ || j >= a.ny_) return;
     const long long c = (long long)j * a.nx_ + i;
     const bool touched = i >= a.ilo && i <= a.ihi && j >= a.jlo && j <= a.jhi && a.tmask[c] == 1 && a.ntracer > 0;
     if (!touched) {
@@ -579,8 +587,8 @@ static int run_wstage(getm_advection* adv, const getm_grid* tg, const T* w, cons
     a.tmask = tg->mask; a.w = w; a.dt = dt; a.scheme = adv->scheme; a.status = adv->status;
     a.haux = adv->colbuf[0]; a.faux = (T*)adv->colbuf[1];
     if (a.nz < 1) return GETM_ERR_ARG;
-    dim3 block(128);
-    dim3 grid(getm_div_up(a.nx_, 128), a.ny_);
+    dim3 block(32, 4);
+    dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, 4));
     // Chunks: every chunk starts from h_in; the final h is the last chunk's.
     int done = 0;
     do {

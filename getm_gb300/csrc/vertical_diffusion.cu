@@ -377,12 +377,13 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c
 }
 
 // PAIRS: fields in pairs (then an odd last one alone), else one at a time
+// block (32, 4): 32 columns of 4 rows
 template <bool SRC, bool PAIRS>
-__global__ void __launch_bounds__(128, 8) vd_inc_kernel(VDArgs<float> a)
+__global__ void __launch_bounds__(128, 7) vd_inc_kernel(VDArgs<float> a)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i >= a.nx_) return;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 4 + threadIdx.y;
+    if (i >= a.nx_ || j >= a.ny_) return;
     const long long c = (long long)j * a.nx_ + i;
     if (a.mask[c] != 1) return;
     int t0 = 0;
@@ -414,13 +415,14 @@ static int vd_launch(VDArgs<T>& a, cudaStream_t stream)
         dim3 grid(getm_div_up(a.nx_, 128), a.ny_);
         if constexpr (getm_increment_form<T>) {
             if (a.nz > 1 && !a.auxo) {
+                const dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, 4)), block(32, 4);
                 bool src = false;
                 for (int t = 0; t < a.ntracer; t++) src = src || a.ea2[t] || a.ea4[t];
                 const bool pairs = a.ntracer > 1;
-                if (src && pairs) vd_inc_kernel<true, true><<<grid, 128, 0, stream>>>(a);
-                else if (src) vd_inc_kernel<true, false><<<grid, 128, 0, stream>>>(a);
-                else if (pairs) vd_inc_kernel<false, true><<<grid, 128, 0, stream>>>(a);
-                else vd_inc_kernel<false, false><<<grid, 128, 0, stream>>>(a);
+                if (src && pairs) vd_inc_kernel<true, true><<<grid, block, 0, stream>>>(a);
+                else if (src) vd_inc_kernel<true, false><<<grid, block, 0, stream>>>(a);
+                else if (pairs) vd_inc_kernel<false, true><<<grid, block, 0, stream>>>(a);
+                else vd_inc_kernel<false, false><<<grid, block, 0, stream>>>(a);
                 GETM_CHECK_LAUNCH();
                 return GETM_OK;
             }

@@ -127,7 +127,8 @@ class Simulation:
         concurrently with the tracers, density and internal pressure
         (neither reads what the other writes; the streams join before the
         2D depth update), and the advection of the V momentum on a third,
-        beside that of the U momentum."""
+        beside that of the U momentum; the squared buoyancy frequency joins
+        the second stream once the density is known."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
@@ -344,7 +345,7 @@ class Simulation:
             # tracers at the open boundaries (simulation.py:1160-1168)
             self._ob.update_tracers(self.tracers._tracers)
         if update_baroclinic:
-            self.update_density()
+            self.update_density(side_stream=self._side_stream if self._forked else None)
             self.update_internal_pressure()
             if not self.delay_slow_ip:
                 _pygetm.column_sums([(self.idpdx, self.momentum.SxB), (self.idpdy, self.momentum.SyB)])
@@ -371,10 +372,11 @@ class Simulation:
             _pygetm.surface_shear_velocity(self.airsea.taux, self.airsea.tauy, self.ustar_s)
 
     # ------------------------------------------------------------ components
-    def update_density(self):
+    def update_density(self, side_stream=None):
         """density.get_density + buoyancy (simulation.py:1178-1184) and the
         squared buoyancy frequency (:1200-1204) with the device equation of
-        state."""
+        state.  ``side_stream``: the squared buoyancy frequency (read by
+        nothing else in the step) is issued there; the caller joins it."""
         n = self.rho.all_values.numel()
         from ._lib import call
         from .core import _sfx
@@ -382,7 +384,12 @@ class Simulation:
         call("getm_density_buoyancy" + _sfx(self.salt.all_values, self.temp.all_values), n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
              self.depth.all_values.data_ptr(), self.rho.all_values.data_ptr(), self.buoy.all_values.data_ptr(),
              torch.cuda.current_stream().cuda_stream)
-        _pygetm.buoyancy_frequency(self.salt, self.temp, self.depth, self.NN)
+        if side_stream is None:
+            _pygetm.buoyancy_frequency(self.salt, self.temp, self.depth, self.NN)
+            return
+        side_stream.wait_stream(torch.cuda.current_stream(side_stream.device))
+        with torch.cuda.stream(side_stream):
+            _pygetm.buoyancy_frequency(self.salt, self.temp, self.depth, self.NN)
 
     def update_internal_pressure(self):
         if self.internal_pressure_method == "blumberg_mellor":

@@ -56,6 +56,21 @@ extern "C" unsigned long long getm_launch_counter_add(void);
 
 static inline unsigned int getm_div_up(long long a, long long b) { return (unsigned int)((a + b - 1) / b); }
 
+// Thread-per-column kernels launched over a flattened range of rows: thread
+// t of a 1D grid takes column (j0 + t / width, t % width) of rows j0 ..
+// j0 + nrows - 1 (consecutive threads, consecutive points, rows back to back,
+// so every block is full whatever the row length); false past the last
+// column.  Launch getm_div_up(width * nrows, threads) blocks.
+__device__ __forceinline__ bool getm_flat_column(int width, int j0, int nrows, int& i, int& j)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)width * nrows) return false;
+    const int r = (int)(t / width);
+    j = j0 + r;
+    i = (int)(t - (long long)r * width);
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // double <-> float conversions on the integer pipe.  GB300 runs FP64
 // instructions, conversions between double and float included, at a small

@@ -397,13 +397,12 @@ struct CoordSweep {
     }
 };
 
-// grid (ceil((nx + 1) / 128), ny + 1)
+// flattened over the (nx + 1) x (ny + 1) X-grid columns
 __global__ void depth_3d_column_kernel(Depth3DArgs a)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    if (i > nx || j > ny) return;
+    int i, j;
+    if (!getm_flat_column(nx + 1, 0, ny + 1, i, j)) return;
     const long long plane = a.plane, planex = a.planex;
     const long long px = (long long)j * (nx + 1) + i;
     const bool xm = a.mx[px] != 0;
@@ -470,7 +469,7 @@ extern "C" int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny
                   f->H_t, f->H_u, f->H_v, f->hn_t, f->hn_u, f->hn_v, f->hn_x, f->ho_t, f->ho_u, f->ho_v,
                   f->zc_t, f->zc_u, f->zc_v, f->zf_t, f->zf_u, f->zf_v, f->depth,
                   f->h_T_half, f->hn_uu, f->hn_vv, f->hn_uv, f->hn_vu};
-    depth_3d_column_kernel<<<dim3(getm_div_up(nx + 1, 128), ny + 1), 128, 0, stream>>>(a);
+    depth_3d_column_kernel<<<getm_div_up((long long)(nx + 1) * (ny + 1), 128), 128, 0, stream>>>(a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

@@ -109,9 +109,8 @@ __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const 
                                        const double* __restrict__ idp, const double* __restrict__ taus, const double* __restrict__ rr,
                                        double dt, T* __restrict__ ea2, T* __restrict__ ea4)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y + haloy;
-    if (i >= nx) return;
+    int i, j;
+    if (!getm_flat_column(nx, haloy, ny - 2 * haloy, i, j)) return;
     long long plane = (long long)nx * ny;
     long long p = (long long)j * nx + i;
     const double al = alpha[p], dpp = dp[p];
@@ -148,7 +147,7 @@ static int collect_impl(int nx, int ny, int nz, int haloy, const double* alpha, 
 {
     if (nx < 1 || ny <= 2 * haloy || nz < 1 || !alpha || !ho || !hn || !dp || !cor || !adv || !diff || !idp || !taus || !rr || !ea2 || !ea4)
         return GETM_ERR_ARG;
-    dim3 grid(getm_div_up(nx, 128), ny - 2 * haloy);
+    const unsigned grid = getm_div_up((long long)nx * (ny - 2 * haloy), 128);
     collect_sources_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, haloy, alpha, ho, hn, dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
@@ -209,9 +208,8 @@ __global__ void w_momentum_3d_kernel(int nx, int ny, int nz, int ilo, int ihi, i
                                      const double* __restrict__ iarea, const double* __restrict__ ho, const double* __restrict__ hn,
                                      const T* __restrict__ pk, const T* __restrict__ qk, double dt, T* __restrict__ w)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y + jlo;
-    if (i < ilo || i > ihi || j > jhi) return;
+    int i, j;
+    if (!getm_flat_column(nx, jlo, jhi - jlo + 1, i, j) || i < ilo || i > ihi) return;
     long long p = (long long)j * nx + i;
     if (mask[p] != 1) return;
     long long plane = (long long)nx * ny;
@@ -249,7 +247,7 @@ static int w_momentum_impl(int nx, int ny, int nz, int imin, int imax, int jmin,
 {
     if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
     if (!mask || !dyu || !dxv || !iarea || !ho || !hn || !pk || !qk || !w) return GETM_ERR_ARG;
-    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1);
+    const unsigned grid = getm_div_up((long long)nx * (jmax - jmin + 1), 128);
     w_momentum_3d_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, dyu, dxv, iarea, ho, hn, pk, qk, dt, w);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
@@ -279,10 +277,9 @@ __global__ void shear_frequency_kernel(int nx, int ny, int nz, int ilo, int ihi,
                                        const int* __restrict__ mask, const double* __restrict__ hu, const double* __restrict__ hv,
                                        const T* __restrict__ uk, const T* __restrict__ vk, T* __restrict__ SS)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y + jlo;
-    int k = blockIdx.z + 1;  // Fortran interface k = 1..nz-1
-    if (i < ilo || i > ihi || j > jhi) return;
+    int i, j;
+    const int k = blockIdx.y + 1;  // Fortran interface k = 1..nz-1
+    if (!getm_flat_column(nx, jlo, jhi - jlo + 1, i, j) || i < ilo || i > ihi) return;
     long long p = (long long)j * nx + i;
     if (mask[p] <= 0) return;
     long long plane = (long long)nx * ny;
@@ -306,7 +303,7 @@ static int shear_impl(int nx, int ny, int nz, int imin, int imax, int jmin, int 
     if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax > nx || jmax > ny || jmax < jmin) return GETM_ERR_ARG;
     if (!mask || !hu || !hv || !uk || !vk || !SS) return GETM_ERR_ARG;
     if (nz < 2) return GETM_OK;
-    dim3 grid(getm_div_up(nx, 128), jmax - jmin + 1, nz - 1);
+    dim3 grid(getm_div_up((long long)nx * (jmax - jmin + 1), 128), nz - 1);
     shear_frequency_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, hu, hv, uk, vk, SS);
     GETM_CHECK_LAUNCH();
     return GETM_OK;

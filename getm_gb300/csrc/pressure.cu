@@ -218,9 +218,8 @@ __global__ void smcw_column_mixed_kernel(int nx, int ny, int nz, int ilo, int ih
                                          const double* __restrict__ buoy, const double* __restrict__ z,
                                          double* __restrict__ Pw)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y + jlo;
-    if (i < ilo || i > ihi + 1 || j > jhi + 1) return;
+    int i, j;
+    if (!getm_flat_column(nx, jlo, jhi - jlo + 2, i, j) || i < ilo || i > ihi + 1) return;
     const long long P = (long long)nx * ny;
     const long long p = (long long)j * nx + i;
     if (mask[p] <= 0) return;
@@ -382,7 +381,7 @@ extern "C" int getm_shchepetkin_mcwilliams_mixed(int nx, int ny, int nz, int imi
     if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax + 2 > nx || jmax + 2 > ny || jmax < jmin) return GETM_ERR_ARG;
     if (!mask || !umask || !vmask || !idxu || !idyv || !h || !z || !zc || !buoy || !idpdx || !idpdy || !P_work)
         return GETM_ERR_ARG;
-    dim3 g1(getm_div_up(nx, 128), jmax - jmin + 2);
+    const unsigned g1 = getm_div_up((long long)nx * (jmax - jmin + 2), 128);
     smcw_column_mixed_kernel<<<g1, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, h, zc,
                                                      buoy, z, P_work);
     GETM_CHECK_LAUNCH();

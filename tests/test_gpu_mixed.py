@@ -186,3 +186,32 @@ def test_smcw_mixed_arithmetic():
     ey = float((s.idpdy.all_values - ref_y)[..., wv].abs().max() / ref_y[..., wv].abs().max())
     print(f"SMcW float slopes: {ex:.2e} {ey:.2e}")
     assert ex < 2e-4 and ey < 2e-4
+
+
+def test_density_double_float():
+    """Mixed-form density (float S and T, the anomaly rho - rho0 in
+    double-float) against the FP64 evaluation of the oracle on the same
+    float-valued inputs: the double-float anomaly is the more accurate of the
+    two (no cancellation against rho0), so both agree to the FP64 form's own
+    rounding of rho (a few ulps of 1026 kg m-3) and of the buoyancy."""
+    import torch
+
+    from getm_gb300 import _lib
+    from oracle.models import seos_buoyancy
+
+    rng = np.random.default_rng(11)
+    n = 200_000
+    S = rng.uniform(0.0, 40.0, n).astype(np.float32)
+    T = rng.uniform(-2.0, 32.0, n).astype(np.float32)
+    z = rng.uniform(0.0, 6000.0, n)
+    rho_ref, b_ref = seos_buoyancy(S.astype(np.float64), T.astype(np.float64), z)
+    Sd, Td, zd = (torch.from_numpy(a).cuda() for a in (S, T, z))
+    rho = torch.empty(n, dtype=torch.float64, device="cuda")
+    b = torch.empty_like(rho)
+    _lib.call("getm_density_buoyancy_f32", n, Sd.data_ptr(), Td.data_ptr(), zd.data_ptr(), rho.data_ptr(),
+              b.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    drho = np.abs(rho.cpu().numpy() - rho_ref).max()
+    db = np.abs(b.cpu().numpy() - b_ref).max()
+    print(f"double-float density: rho {drho:.2e} kg m-3, buoyancy {db:.2e} m s-2")
+    assert drho < 2e-12 and db < 2e-14

@@ -116,6 +116,25 @@ __device__ __forceinline__ float getm_d2f_approx(double x)
     return __uint_as_float(s | ((unsigned int)e << 23) | m);
 }
 
+// x * 2^-n (n = 1, 2) on the integer pipe: exact, and bitwise the FP64
+// multiply's result, for normal x whose product stays normal (the exponent
+// field decreases by n); zeros, subnormals, infinities and NaNs take the FP64
+// multiply out of line (so that it is not issued predicated on every call).
+static __device__ __noinline__ double getm_scale_hw(double x, double f) { return x * f; }
+
+template <int N>
+__device__ __forceinline__ double getm_pow2_scale_down(double x)
+{
+    static_assert(N == 1 || N == 2, "halving or quartering");
+    const long long b = __double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e > N && e < 0x7ff) return __longlong_as_double(b - ((long long)N << 52));
+    return getm_scale_hw(x, N == 1 ? 0.5 : 0.25);
+}
+
+__device__ __forceinline__ double getm_half(double x) { return getm_pow2_scale_down<1>(x); }
+__device__ __forceinline__ double getm_quarter(double x) { return getm_pow2_scale_down<2>(x); }
+
 // num / den in FP64 to about 2^-46 relative (not correctly rounded), for the
 // mixed form: the float reciprocal of den refined by one Newton-Raphson step
 // (q0 = num r, q = q0 + r (num - q0 den)), three FP64 instructions instead of

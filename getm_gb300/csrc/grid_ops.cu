@@ -444,7 +444,7 @@ __global__ void depth_3d_column_kernel(Depth3DArgs a)
         if (mt) { nt = dga * Dt; a.hnt[q] = nt; }
         if (mu) { nu = dga * Du; a.hnu[q] = nu; }
         if (mv) { nv = dga * Dv; a.hnv[q] = nv; }
-        const double hh = (ot + nt) * 0.5;
+        const double hh = getm_half(ot + nt);
         a.hhalf[q] = hh;
         if (i >= 1) a.hnuu[q - 1] = hh;
         if (j >= 1) a.hnvv[q - nx] = hh;

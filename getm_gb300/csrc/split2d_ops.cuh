@@ -74,7 +74,7 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
         double v = 0.0;
         if (gj >= 0 && gj < ny && gi >= 0 && gi < nx) {
             const long long g = (long long)gj * nx + gi;
-            v = (a.zo[g] + a.z[g]) * 0.5;
+            v = getm_half(a.zo[g] + a.z[g]);
         }
         szh[sj][si] = v;
     }
@@ -86,7 +86,7 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
     {
         double zx;
         if (j >= 1 && j <= ny - 1 && i >= 1 && i <= nx - 1) {
-            zx = 0.25 * (szh[sj - 1][si - 1] + szh[sj - 1][si] + szh[sj][si - 1] + szh[sj][si]);
+            zx = getm_quarter(szh[sj - 1][si - 1] + szh[sj - 1][si] + szh[sj][si - 1] + szh[sj][si]);
             a.workX[px] = zx;
         } else {
             zx = workX0;
@@ -117,7 +117,7 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
     // U: z_U = interp_x(z_T_half, ioffset 0) for i < nx-1, else the old value
     double zu;
     if (i < nx - 1) {
-        zu = 0.5 * (zh + szh[sj][si + 1]);
+        zu = getm_half(zh + szh[sj][si + 1]);
         a.workU[p] = zu;
     } else {
         zu = workU0;
@@ -130,7 +130,7 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
     // V: z_V = interp_y(z_T_half, joffset 0) for j < ny-1
     double zv;
     if (j < ny - 1) {
-        zv = 0.5 * (zh + szh[sj + 1][si]);
+        zv = getm_half(zh + szh[sj + 1][si]);
         a.workV[p] = zv;
     } else {
         zv = workV0;
@@ -172,10 +172,10 @@ __device__ __forceinline__ void momentum_2d_velocities_point(const VelArgs& a, i
         a.u1[p] = u1; a.advU[p] = u1;
         a.v1[p] = v1; a.advV[p] = v1;
         // interp_x (ioffset 0) writes i < nx-1; elsewhere the old value is divided
-        const double uu = i < a.nx - 1 ? 0.5 * (a.U[p] + a.U[p + 1]) : a.uua[p];
-        const double uv = i < a.nx - 1 ? 0.5 * (a.V[p] + a.V[p + 1]) : a.uva[p];
-        const double vu = j < a.ny - 1 ? 0.5 * (a.U[p] + a.U[p + a.nx]) : a.vua[p];
-        const double vv = j < a.ny - 1 ? 0.5 * (a.V[p] + a.V[p + a.nx]) : a.vva[p];
+        const double uu = i < a.nx - 1 ? getm_half(a.U[p] + a.U[p + 1]) : a.uua[p];
+        const double uv = i < a.nx - 1 ? getm_half(a.V[p] + a.V[p + 1]) : a.uva[p];
+        const double vu = j < a.ny - 1 ? getm_half(a.U[p] + a.U[p + a.nx]) : a.vua[p];
+        const double vv = j < a.ny - 1 ? getm_half(a.V[p] + a.V[p + a.nx]) : a.vva[p];
         a.uua[p] = vel_div<C>(uu, a.DUU[p]);
         a.uva[p] = vel_div<C>(uv, a.DUV[p]);
         a.vua[p] = vel_div<C>(vu, a.DVU[p]);

@@ -350,8 +350,9 @@ extern "C" int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax
 
 // ---------------------------------------------------------------------------
 // Simulation.update_depth, 3D part (python/pygetm/simulation.py:1588-1630) in
-// one launch, one thread per X-grid column (j, i), 0 <= j <= ny, 0 <= i <= nx,
-// sweeping up from the bottom: hn = dga Dclip where the mask is non-zero
+// one launch, one thread per column of each grid (X: 0 <= j <= ny,
+// 0 <= i <= nx; T, U, V: j < ny, i < nx), sweeping up from the bottom:
+// hn = dga Dclip where the mask is non-zero
 // (Sigma coordinates, vertical_coordinates.py:106-113) on X and, for j < ny
 // and i < nx, on T, U and V with ho = the previous hn; h_T_half = (ho + hn) / 2
 // on T and the thicknesses of the advection velocity grids, each written by
@@ -397,62 +398,70 @@ struct CoordSweep {
     }
 };
 
-// flattened over the (nx + 1) x (ny + 1) X-grid columns
+// One role per blockIdx.y, flattened over the (nx + 1) x (ny + 1) X-grid
+// columns: 0 the X grid (and the UV/VU thicknesses it feeds), 1 T (with
+// h_T_half, the UU/VV thicknesses and the centre depths), 2 U, 3 V.  The roles
+// share no intermediate value, so splitting them keeps few values live per
+// thread and four times the columns in flight.
 __global__ void depth_3d_column_kernel(Depth3DArgs a)
 {
     const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const int role = blockIdx.y;
     int i, j;
     if (!getm_flat_column(nx + 1, 0, ny + 1, i, j)) return;
-    const long long plane = a.plane, planex = a.planex;
-    const long long px = (long long)j * (nx + 1) + i;
-    const bool xm = a.mx[px] != 0;
-    const double Dx = xm ? a.Dx[px] : 0.0;
-    const bool xuv = i >= 1 && j >= 1;
-    const long long quv = (long long)(j - 1) * nx + (i - 1);
-    const bool tin = i < nx && j < ny;
+    const long long plane = a.plane;
+    if (role == 0) {
+        const long long px = (long long)j * (nx + 1) + i;
+        const bool xm = a.mx[px] != 0;
+        const double Dx = xm ? a.Dx[px] : 0.0;
+        const bool xuv = i >= 1 && j >= 1;
+        const long long quv = (long long)(j - 1) * nx + (i - 1);
+        for (int k = 0; k < nz; k++) {
+            const long long qx = px + k * a.planex;
+            double hx;
+            if (xm) {
+                hx = a.dga[k] * Dx;
+                a.hnx[qx] = hx;
+            } else {
+                hx = a.hnx[qx];
+            }
+            if (xuv) {
+                a.hnuv[quv + k * plane] = hx;
+                a.hnvu[quv + k * plane] = hx;
+            }
+        }
+        return;
+    }
+    if (i >= nx || j >= ny) return;
     const long long p = (long long)j * nx + i;
-    bool mt = false, mu = false, mv = false;
-    double Dt = 0.0, Du = 0.0, Dv = 0.0, Ht = 0.0, Hu = 0.0, Hv = 0.0;
-    if (tin) {
-        mt = a.mt[p] != 0; mu = a.mu[p] != 0; mv = a.mv[p] != 0;
-        if (mt) { Dt = a.Dt[p]; Ht = a.Ht[p]; }
-        if (mu) { Du = a.Du[p]; Hu = a.Hu[p]; }
-        if (mv) { Dv = a.Dv[p]; Hv = a.Hv[p]; }
-    }
-    CoordSweep st{0.0, 0.0, 0.0}, su{0.0, 0.0, 0.0}, sv{0.0, 0.0, 0.0};
+    const int* mask = role == 1 ? a.mt : role == 2 ? a.mu : a.mv;
+    const double* Dc = role == 1 ? a.Dt : role == 2 ? a.Du : a.Dv;
+    const double* Hc = role == 1 ? a.Ht : role == 2 ? a.Hu : a.Hv;
+    double* hn = role == 1 ? a.hnt : role == 2 ? a.hnu : a.hnv;
+    double* ho = role == 1 ? a.hot : role == 2 ? a.hou : a.hov;
+    double* zc = role == 1 ? a.zct : role == 2 ? a.zcu : a.zcv;
+    double* zf = role == 1 ? a.zft : role == 2 ? a.zfu : a.zfv;
+    const bool m = mask[p] != 0;
+    const double D = m ? Dc[p] : 0.0, H = m ? Hc[p] : 0.0;
+    CoordSweep sw{0.0, 0.0, 0.0};
     for (int k = 0; k < nz; k++) {
-        const double dga = a.dga[k];
-        const long long qx = px + k * planex;
-        double hx;
-        if (xm) {
-            hx = dga * Dx;
-            a.hnx[qx] = hx;
-        } else {
-            hx = a.hnx[qx];
-        }
-        if (xuv) {
-            a.hnuv[quv + k * plane] = hx;
-            a.hnvu[quv + k * plane] = hx;
-        }
-        if (!tin) continue;
         const long long q = p + k * plane;
-        const double ot = a.hnt[q], ou = a.hnu[q], ov = a.hnv[q];
-        a.hot[q] = ot;
-        a.hou[q] = ou;
-        a.hov[q] = ov;
-        double nt = ot, nu = ou, nv = ov;
-        if (mt) { nt = dga * Dt; a.hnt[q] = nt; }
-        if (mu) { nu = dga * Du; a.hnu[q] = nu; }
-        if (mv) { nv = dga * Dv; a.hnv[q] = nv; }
-        const double hh = getm_half(ot + nt);
-        a.hhalf[q] = hh;
-        if (i >= 1) a.hnuu[q - 1] = hh;
-        if (j >= 1) a.hnvv[q - nx] = hh;
-        if (mt) st.level(k, q, plane, Ht, nt, a.zct, a.zft);
-        if (mu) su.level(k, q, plane, Hu, nu, a.zcu, a.zfu);
-        if (mv) sv.level(k, q, plane, Hv, nv, a.zcv, a.zfv);
+        const double o = hn[q];
+        ho[q] = o;
+        double n = o;
+        if (m) {
+            n = a.dga[k] * D;
+            hn[q] = n;
+        }
+        if (role == 1) {
+            const double hh = getm_half(o + n);
+            a.hhalf[q] = hh;
+            if (i >= 1) a.hnuu[q - 1] = hh;
+            if (j >= 1) a.hnvv[q - nx] = hh;
+        }
+        if (m) sw.level(k, q, plane, H, n, zc, zf);
     }
-    if (mt && a.depth) t2cd_column(plane, nz, p, a.hnt, a.depth);
+    if (role == 1 && m && a.depth) t2cd_column(plane, nz, p, a.hnt, a.depth);
 }
 
 extern "C" int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny, int nz, cudaStream_t stream)
@@ -469,7 +478,7 @@ extern "C" int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny
                   f->H_t, f->H_u, f->H_v, f->hn_t, f->hn_u, f->hn_v, f->hn_x, f->ho_t, f->ho_u, f->ho_v,
                   f->zc_t, f->zc_u, f->zc_v, f->zf_t, f->zf_u, f->zf_v, f->depth,
                   f->h_T_half, f->hn_uu, f->hn_vv, f->hn_uv, f->hn_vu};
-    depth_3d_column_kernel<<<getm_div_up((long long)(nx + 1) * (ny + 1), 128), 128, 0, stream>>>(a);
+    depth_3d_column_kernel<<<dim3(getm_div_up((long long)(nx + 1) * (ny + 1), 128), 4), 128, 0, stream>>>(a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }

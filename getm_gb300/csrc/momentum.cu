@@ -109,10 +109,13 @@ __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const 
                                        const double* __restrict__ idp, const double* __restrict__ taus, const double* __restrict__ rr,
                                        double dt, T* __restrict__ ea2, T* __restrict__ ea4)
 {
+    // one thread per cell: grid (flattened columns, level)
     int i, j;
     if (!getm_flat_column(nx, haloy, ny - 2 * haloy, i, j)) return;
+    const int k = blockIdx.y;
     long long plane = (long long)nx * ny;
     long long p = (long long)j * nx + i;
+    const long long q = p + k * plane;
     const double al = alpha[p], dpp = dp[p];
     const double rho0i = 1.0 / GETM_RHO0;
     if constexpr (getm_increment_form<T>) {
@@ -120,24 +123,18 @@ __global__ void collect_sources_kernel(int nx, int ny, int nz, int haloy, const 
         // in float (each term to float precision)
         const float alf = getm_d2f_approx(al), dtf = (float)dt;
         const float gdp = (float)(-0.5 * GETM_G) * getm_d2f_approx(dpp);
-        for (int k = 0; k < nz; k++) {
-            long long q = p + k * plane;
-            float e = dtf * (gdp * (getm_d2f_approx(ho[q]) + getm_d2f_approx(hn[q])) +
-                             alf * (cor[q] + adv[q] + diff[q] + getm_d2f_approx(idp[q])));
-            if (k == nz - 1) e = e + dtf * alf * getm_d2f_approx(taus[p]) * (float)rho0i;
-            ea4[q] = e;
-        }
-        ea2[p] = -dtf * getm_d2f_approx(rr[p]);
+        float e = dtf * (gdp * (getm_d2f_approx(ho[q]) + getm_d2f_approx(hn[q])) +
+                         alf * (cor[q] + adv[q] + diff[q] + getm_d2f_approx(idp[q])));
+        if (k == nz - 1) e = e + dtf * alf * getm_d2f_approx(taus[p]) * (float)rho0i;
+        ea4[q] = e;
+        if (k == 0) ea2[p] = -dtf * getm_d2f_approx(rr[p]);
         return;
     }
-    for (int k = 0; k < nz; k++) {
-        long long q = p + k * plane;
-        double e = dt * (-0.5 * (ho[q] + hn[q]) * GETM_G * dpp
-                         + al * ((double)cor[q] + (double)adv[q] + (double)diff[q] + idp[q]));
-        if (k == nz - 1) e = e + dt * al * taus[p] * rho0i;
-        ea4[q] = (T)e;
-    }
-    ea2[p] = (T)(-dt * rr[p]);
+    double e = dt * (-0.5 * (ho[q] + hn[q]) * GETM_G * dpp
+                     + al * ((double)cor[q] + (double)adv[q] + (double)diff[q] + idp[q]));
+    if (k == nz - 1) e = e + dt * al * taus[p] * rho0i;
+    ea4[q] = (T)e;
+    if (k == 0) ea2[p] = (T)(-dt * rr[p]);
 }
 
 template <typename T>
@@ -147,7 +144,7 @@ static int collect_impl(int nx, int ny, int nz, int haloy, const double* alpha, 
 {
     if (nx < 1 || ny <= 2 * haloy || nz < 1 || !alpha || !ho || !hn || !dp || !cor || !adv || !diff || !idp || !taus || !rr || !ea2 || !ea4)
         return GETM_ERR_ARG;
-    const unsigned grid = getm_div_up((long long)nx * (ny - 2 * haloy), 128);
+    const dim3 grid(getm_div_up((long long)nx * (ny - 2 * haloy), 128), nz);
     collect_sources_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, haloy, alpha, ho, hn, dp, cor, adv, diff, idp, taus, rr, dt, ea2, ea4);
     GETM_CHECK_LAUNCH();
     return GETM_OK;

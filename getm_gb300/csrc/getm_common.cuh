@@ -116,6 +116,15 @@ __device__ __forceinline__ float getm_d2f_approx(double x)
     return __uint_as_float(s | ((unsigned int)e << 23) | m);
 }
 
+// A value of the storage type T widened to double: float on the integer pipe
+// (getm_f2d, exact), double as it is.
+template <typename T>
+__device__ __forceinline__ double getm_widen(T x)
+{
+    if constexpr (std::is_same<T, float>::value) return getm_f2d(x);
+    else return x;
+}
+
 // x * 2^-n (n = 1, 2) on the integer pipe: exact, and bitwise the FP64
 // multiply's result, for normal x whose product stays normal (the exponent
 // field decreases by n); zeros, subnormals, infinities and NaNs take the FP64

@@ -404,7 +404,7 @@ __global__ void transport_3d_finish_kernel(long long plane, int nz, const T* __r
         if constexpr (std::is_same<T, double>::value) x = __dmul_rn(vel[q], hn[q]);
         else x = vel[q] * getm_d2f_approx(hn[q]);
         tp3d[q] = x;
-        s = s + (double)x;
+        s = s + getm_widen(x);
     }
     const double d = (s - tp2d[p]) / D[p];
     dev[p] = d;
@@ -432,7 +432,7 @@ __global__ void column_sums_kernel(long long plane, int nz, int subtract, const 
     double* dst = f == 0 ? a2 : f == 1 ? b2 : f == 2 ? c2 : d2;
     if (p >= plane || !src) return;
     double s = 0.0;
-    for (int k = 0; k < nz; k++) s = s + (double)src[p + k * plane];
+    for (int k = 0; k < nz; k++) s = s + getm_widen(src[p + k * plane]);
     dst[p] = subtract ? s - dst[p] : s;
 }
 

@@ -10,7 +10,9 @@
 //   2. thread per (i, j, k) U/V point: horizontal harmonic-mean slopes from
 //      the three raw differences around the point, the density-Jacobian
 //      correction FC and the gradient.  The reference's per-level dZx/dRx
-//      work arrays are recomputed in registers (same operations, same values).
+//      work arrays are recomputed in registers (same operations, same values);
+//      the mixed form forms each raw difference once per 32 x 8 tile in
+//      shared memory.
 #include "getm_common.cuh"
 
 // ---------------------------------------------------------------------------

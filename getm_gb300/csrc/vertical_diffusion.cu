@@ -10,9 +10,11 @@
 // tridiagonal matrix is never stored: its coefficients are formed on the fly
 // from nuh, ho, hn and var while sweeping down from the surface (the Thomas
 // forward elimination of diffusion.F90:285-292), keeping only the two
-// elimination coefficients per level in shared memory for the back
-// substitution (:304-307).  prepare+apply are fused (traffic per field: read
-// nuh, ho, hn, var [+ea2, ea4], write var).  A warp-per-column PCR solve would
+// elimination coefficients per level for the back substitution (:304-307),
+// in shared memory or in a caller-provided global workspace.  prepare+apply
+// are fused (traffic per field: read nuh, ho, hn, var [+ea2, ea4], write
+// var).  The mixed form's solve (vd_inc_kernel) takes fields in pairs and
+// issues each level's loads one level ahead.  A warp-per-column PCR solve would
 // cost O(nz log nz) FP64 divides per column instead of O(nz); GB300's FP64
 // rate makes the serial Thomas sweep the faster choice.
 #include <stdlib.h>

@@ -1,0 +1,53 @@
+"""bench.py's multi-GPU path is N independent replicas (one process per GPU,
+no collective on the data path): the timing is the maximum over ranks and
+the whole-job rate counts every replica's cells.  Checked here with two
+gloo ranks on the CPU, through the same helpers the bench uses; the
+reference arm runs on rank 0 alone."""
+
+import json
+import os
+import socket
+
+import pytest
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out_dir):
+    os.environ.update(WORLD_SIZE=str(world), RANK=str(rank), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    import torch.distributed as dist
+
+    import bench
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        ms = bench._max_over_ranks(10.0 * (rank + 1), "cpu")
+        rate = bench._whole_job_rate(1000, 4, ms)
+        ref = None
+        if rank != 0:
+            # the reference arm: ranks other than 0 return without work
+            class A:
+                steps = 1
+                warmup = 1
+            ref = bench.run_reference(A())
+        with open(os.path.join(out_dir, f"rank{rank}.json"), "w") as f:
+            json.dump({"ms": ms, "rate": rate, "ref": ref}, f)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replicas_time_is_max_over_ranks_and_rate_counts_every_replica(tmp_path):
+    mp = pytest.importorskip("torch.multiprocessing")
+    world = 2
+    mp.start_processes(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True,
+                       start_method="spawn")
+    for r in range(world):
+        d = json.loads((tmp_path / f"rank{r}.json").read_text())
+        assert d["ms"] == 20.0
+        assert d["rate"] == pytest.approx(1000 * 4 * world / 0.020)
+        assert d["ref"] is None

@@ -51,3 +51,25 @@ def test_replicas_time_is_max_over_ranks_and_rate_counts_every_replica(tmp_path)
         assert d["ms"] == 20.0
         assert d["rate"] == pytest.approx(1000 * 4 * world / 0.020)
         assert d["ref"] is None
+
+
+def test_reference_arm_prints_the_contract_line(capsys, monkeypatch):
+    """`bench.py --impl reference` on rank 0: one JSON line with the metric,
+    impl "reference", its CPU baseline and an end-to-end figure without host
+    copies (small domain here; the bench runs the full workload)."""
+    import bench
+
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    # the arm sets these only where unset; set here, they are restored afterwards
+    monkeypatch.setenv("OMP_NUM_THREADS", "1")
+    monkeypatch.setenv("GETM_ORACLE_VARIANT", "serial")
+    monkeypatch.setattr("sys.argv", ["bench.py", "--impl", "reference", "--nx", "24", "--ny", "20", "--nz", "4",
+                                     "--steps", "1", "--warmup", "1"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == "3D cell-updates/s"
+    assert line["value"] > 0 and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}

@@ -152,6 +152,14 @@ def _whole_job_rate(cells: int, nsteps: int, ms: float) -> float:
     return cells * nsteps * ws / (ms / 1000.0)
 
 
+def _host_threads() -> int:
+    """Threads of the CPU legs: OMP_NUM_THREADS where set, else every core."""
+    try:
+        return max(1, int(os.environ["OMP_NUM_THREADS"]))
+    except (KeyError, ValueError):
+        return os.cpu_count() or 1
+
+
 def cpu_reference(args, nmacro: int, threads: int):
     """Time the oracle restatement of the reference's CPU path."""
     import numpy as np
@@ -177,7 +185,7 @@ def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
+    threads = _host_threads()
     steps = max(1, min(args.steps, 3))
     for _ in range(min(args.warmup, 1)):
         pass
@@ -623,7 +631,7 @@ def run_ours(args):
     if rank == 0 and args.shelf_steps > 0:
         line["shelf_sea"] = _shelf_leg(args, device)
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
-        threads = os.cpu_count() or 1
+        threads = _host_threads()
         v, dt = cpu_reference(args, 2, threads)
         line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
                                 "sample": f"2 3D steps of the full workload ({dt:.1f} s)"}

@@ -71,5 +71,6 @@ def test_reference_arm_prints_the_contract_line(capsys, monkeypatch):
     assert line["impl"] == "reference" and line["metric"] == "3D cell-updates/s"
     assert line["value"] > 0 and line["higher_is_better"] is True
     assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
+    assert line["cpu_baseline"]["cores"] == 1  # the threads it ran with
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}

@@ -88,6 +88,8 @@ _SIGS = {
     "getm_momentum_3d_advection_inputs_f32": "iiippppppppppps",
     "getm_coriolis_3d": "iiiiipppis",
     "getm_coriolis_3d_f32": "iiiiipppis",
+    "getm_coriolis_espelid": "iiiiipppppppis",
+    "getm_coriolis_espelid_f32": "iiiiipppppppis",
     "getm_buoyancy_frequency": "iiipppppps",
     "getm_buoyancy_frequency_f32": "iiipppppps",
     "getm_column_sums": "iiiipppppppps",

@@ -314,6 +314,26 @@ def coriolis_3d(U, out, x_direction):
          int(bool(x_direction)), _s())
 
 
+def coriolis_espelid(U, out, x_direction):
+    """Momentum.coriolis, ESPELID scheme (momentum.py:1136-1142), for 2D or 3D
+    transports: f * sqrt(Dout) * interp(U / sqrt(Din)), negated for the V
+    equation, with D the water depths (2D) or layer thicknesses (3D)."""
+    a, b = U.grid, out.grid
+    if a.ioffset == b.ioffset + 1 and a.joffset == b.joffset - 1:
+        io, jo = 1, 0
+    elif a.ioffset == b.ioffset - 1 and a.joffset == b.joffset + 1:
+        io, jo = 0, 1
+    else:
+        raise NotImplementedError("coriolis_espelid expects U -> V or V -> U")
+    if U.z:
+        Din, Dout, nz = a.hn, b.hn, out.all_values.shape[0]
+    else:
+        Din, Dout, nz = a.D, b.D, 1
+    sfx = _sfx(U.all_values, out.all_values)
+    call("getm_coriolis_espelid" + sfx, b.nx_, b.ny_, nz, io, jo, _p(U), _p(Din), _p(a.mask), _p(Dout), _p(b.mask),
+         _p(b.cor), _p(out), int(bool(x_direction)), _s())
+
+
 def accumulate_2d(U, V, Ucum, Vcum):
     """_U_cum += U; _V_cum += V (momentum.py:716-718)."""
     call("getm_accumulate_2d", U.all_values.numel(), _p(U), _p(V), Ucum.data_ptr(), Vcum.data_ptr(), _s())

@@ -961,6 +961,7 @@ extern "C" int getm_advection_2d_noalloc(int scheme, getm_grid* tgrid, getm_grid
         double* hdst = (s == seq_n - 1) ? D : ((s % 2 == 0) ? A : B);
         double* fdst = (fsrc == var) ? T : var;
         seq_a[s]->dt = seq_dt[s];
+        seq_a[s]->dtf = (float)seq_dt[s];
         fin[0] = fsrc;
         fout[0] = fdst;
         if ((rc = run_hstage(*seq_a[s], seq_dir[s], hsrc, hdst, 1, fin, fout, stream))) return rc;

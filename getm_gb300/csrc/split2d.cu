@@ -286,6 +286,77 @@ static int coriolis_3d_impl(int nx, int ny, int nz, int ioffset, int joffset, co
     return GETM_OK;
 }
 
+// Momentum.coriolis, ESPELID scheme (momentum.py:1136-1142), 2D or 3D: the
+// transport is divided by sqrt(D) of its own grid (1 on land) before the
+// interp_xy to the other velocity grid, and the result is multiplied by
+// sqrt(D) of the target grid on water points, then by f and negated for the
+// V equation.  D: water depth (2D) or layer thickness (3D) of each grid.
+// Target points outside the interpolation range keep their old value, as
+// interp leaves them (then scaled like the rest).  On land points of the
+// target the reference multiplies by an unset value (np.sqrt with where=
+// and no out=); here the sqrt(D) factor is left out there.  The transport
+// update never reads the term on land.  FP64 arithmetic, T storage.
+template <typename T>
+__global__ void __launch_bounds__(S2_THREADS) coriolis_espelid_kernel(
+    int nx, int ny, int ioff, int joff, const T* __restrict__ src, const double* __restrict__ Din,
+    const int* __restrict__ mask_in, const double* __restrict__ Dout, const int* __restrict__ mask_out,
+    const double* __restrict__ cor, T* __restrict__ out, int negate)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    const long long off = (long long)blockIdx.z * nx * ny;
+    if (i >= nx || j >= ny) return;
+    const long long p = (long long)j * nx + i;
+    const int si = i - ioff, sj = j - joff;
+    double v;
+    if (si >= 0 && sj >= 0 && si <= nx - 2 && sj <= ny - 2) {
+        const long long q = (long long)sj * nx + si;
+        auto scaled = [&](long long r) {
+            const double s = mask_in[r] != 0 ? sqrt(Din[off + r]) : 1.0;
+            return (double)src[off + r] / s;
+        };
+        v = 0.25 * (scaled(q) + scaled(q + 1) + scaled(q + nx) + scaled(q + nx + 1));
+    } else {
+        v = (double)out[off + p];
+    }
+    if (mask_out[p] != 0) v = v * sqrt(Dout[off + p]);
+    v = v * cor[p];
+    out[off + p] = (T)(negate ? -v : v);
+}
+
+template <typename T>
+static int coriolis_espelid_impl(int nx, int ny, int nz, int ioffset, int joffset, const T* src, const double* Din,
+                                 const int* mask_in, const double* Dout, const int* mask_out, const double* cor,
+                                 T* out, int negate, cudaStream_t stream)
+{
+    if (nx < 2 || ny < 2 || nz < 1 || !src || !Din || !mask_in || !Dout || !mask_out || !cor || !out ||
+        ioffset < 0 || ioffset > 1 || joffset < 0 || joffset > 1)
+        return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, S2_THREADS), ny, nz);
+    coriolis_espelid_kernel<T><<<grid, S2_THREADS, 0, stream>>>(nx, ny, ioffset, joffset, src, Din, mask_in, Dout,
+                                                                mask_out, cor, out, negate);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_coriolis_espelid(int nx, int ny, int nz, int ioffset, int joffset, const double* src,
+                                     const double* Din, const int* mask_in, const double* Dout,
+                                     const int* mask_out, const double* cor, double* out, int negate,
+                                     cudaStream_t stream)
+{
+    return coriolis_espelid_impl<double>(nx, ny, nz, ioffset, joffset, src, Din, mask_in, Dout, mask_out, cor, out,
+                                         negate, stream);
+}
+
+extern "C" int getm_coriolis_espelid_f32(int nx, int ny, int nz, int ioffset, int joffset, const float* src,
+                                         const double* Din, const int* mask_in, const double* Dout,
+                                         const int* mask_out, const double* cor, float* out, int negate,
+                                         cudaStream_t stream)
+{
+    return coriolis_espelid_impl<float>(nx, ny, nz, ioffset, joffset, src, Din, mask_in, Dout, mask_out, cor, out,
+                                        negate, stream);
+}
+
 extern "C" int getm_coriolis_3d(int nx, int ny, int nz, int ioffset, int joffset, const double* src, const double* cor,
                                 double* out, int negate, cudaStream_t stream)
 {

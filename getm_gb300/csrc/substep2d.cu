@@ -30,6 +30,7 @@
 // returns, and later launches return at once until the host clears the word.
 #include <string.h>
 
+#include <mutex>
 #include <type_traits>
 
 #include "advection_passes.cuh"
@@ -213,7 +214,6 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
     if (tx == 0 && ty == 0) s_ok = ld_acquire(&a.sync[2]) == 0;
     __syncthreads();
     if (!s_ok) return;
-    if (gt == 0 && a.time) *a.time = *a.time + a.dt;
 
     const int d1 = a.ufirst ? 0 : 1, d2 = 1 - d1;
     // 1: first transport update
@@ -273,7 +273,10 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
     advection_pass<MIXED>(a.adv[1].pass[0], a.adv[1].dir[0], sm, tx, ty);
     if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
     // 7: second advection passes, each cell's advection term formed as the
-    // pass finishes it (reconstruct_transport_change)
+    // pass finishes it (reconstruct_transport_change).  The model time moves
+    // on only here, after the last barrier: a substep abandoned at a barrier
+    // leaves it unchanged (no phase reads it).
+    if (gt == 0 && a.time) *a.time = *a.time + a.dt;
     for (int d = 0; d < 2; d++) {
         const ReconstructEpi epi{a.advvar[d], a.Uo[d], a.idt, jlo, jhi};
         advection_pass<MIXED>(a.adv[d].pass[1], a.adv[d].dir[1], sm, tx, ty, epi);
@@ -283,19 +286,20 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
 
 static_assert(sizeof(SubstepArgs) <= 4096, "kernel parameter block");
 
-struct LaunchShape {
-    int blocks = 0;
-};
+constexpr int SS_MAX_DEVICES = 64;
 
+// Co-resident blocks of substep_2d_kernel<MIXED> on device `dev` (SMs times
+// blocks per SM), queried once per device and kept under a mutex, so host
+// threads driving different GPUs each get their own device's count.
 template <bool MIXED>
-int launch_substep(const SubstepArgs& a, cudaStream_t stream)
+int substep_blocks(int dev, int* blocks)
 {
-    // co-resident blocks per SM, queried once per process (device 0 of the
-    // process: one process drives one GPU)
-    static LaunchShape shape;
-    if (shape.blocks == 0) {
-        int dev = 0, sms = 0, coop = 0, per_sm = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess) return GETM_ERR_CUDA;
+    static int cache[SS_MAX_DEVICES];
+    static std::mutex mutex;
+    if (dev < 0 || dev >= SS_MAX_DEVICES) return GETM_ERR_ARG;
+    std::lock_guard<std::mutex> lock(mutex);
+    if (cache[dev] == 0) {
+        int sms = 0, coop = 0, per_sm = 0;
         if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
             return GETM_ERR_CUDA;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GETM_ERR_CUDA;
@@ -303,10 +307,20 @@ int launch_substep(const SubstepArgs& a, cudaStream_t stream)
                 cudaSuccess ||
             per_sm < 1)
             return GETM_ERR_CUDA;
-        shape.blocks = sms * per_sm;
+        cache[dev] = sms * per_sm;
     }
+    *blocks = cache[dev];
+    return GETM_OK;
+}
+
+template <bool MIXED>
+int launch_substep(const SubstepArgs& a, cudaStream_t stream)
+{
+    int dev = 0, blocks = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GETM_ERR_CUDA;
+    if (int rc = substep_blocks<MIXED>(dev, &blocks)) return rc;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(shape.blocks);
+    cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(32, SS_BY);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = stream;

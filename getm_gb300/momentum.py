@@ -261,10 +261,11 @@ class Momentum:
         _pygetm.bottom_friction(u_V, v, DV, self.avmmol, rv, update_z0b, ar)
 
     def coriolis(self, U: Array, out: Array, x_direction: bool):
-        """momentum.py:1127-1148 (DEFAULT scheme)"""
+        """momentum.py:1127-1148 (DEFAULT and ESPELID schemes)"""
         assert U.grid is not out.grid
         if self.coriolis_scheme == CoriolisScheme.ESPELID:
-            raise NotImplementedError("Espelid Coriolis interpolation is not implemented")
+            _pygetm.coriolis_espelid(U, out, x_direction)
+            return
         if self.fused_2d and not U.z:
             _pygetm.coriolis_2d(U, out, x_direction, mixed=self.dtype3d == torch.float32)
             return

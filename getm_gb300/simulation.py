@@ -284,6 +284,14 @@ class Simulation:
         substep did not complete; reads the device word)."""
         return 0 if self._split2d is None else int(self._split2d.sync[2].item())
 
+    def clear_split2d_status(self):
+        """Re-arm the one-launch substep after a barrier gave up: zero its
+        barrier words (stream-ordered, so call it with no substep in flight
+        on another stream).  Until then every substep launch returns at once
+        and leaves the fields and the model time unchanged."""
+        if self._split2d is not None:
+            self._split2d.sync.zero_()
+
     def _start(self):
         """python/pygetm/simulation.py:948-1031"""
         T = self.T

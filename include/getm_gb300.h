@@ -435,6 +435,18 @@ int getm_coriolis_3d(int nx, int ny, int nz, int ioffset, int joffset, const dou
                      double* out, int negate, cudaStream_t stream);
 int getm_coriolis_3d_f32(int nx, int ny, int nz, int ioffset, int joffset, const float* src, const double* cor,
                          float* out, int negate, cudaStream_t stream);
+/* Momentum.coriolis, ESPELID scheme (momentum.py:1136-1142), 2D (nz = 1,
+ * D = water depths) or 3D (D = layer thicknesses): out = (-1 if negate) *
+ * f * sqrt(Dout) * interp_xy(src / sqrt(Din)), sqrt(Din) taken as 1 where
+ * mask_in == 0; where mask_out == 0 the sqrt(Dout) factor is left out (the
+ * reference leaves those points unset).  FP64 arithmetic; the _f32 entry
+ * takes float transports and terms.                                        */
+int getm_coriolis_espelid(int nx, int ny, int nz, int ioffset, int joffset, const double* src,
+                          const double* Din, const int* mask_in, const double* Dout, const int* mask_out,
+                          const double* cor, double* out, int negate, cudaStream_t stream);
+int getm_coriolis_espelid_f32(int nx, int ny, int nz, int ioffset, int joffset, const float* src,
+                              const double* Din, const int* mask_in, const double* Dout, const int* mask_out,
+                              const double* cor, float* out, int negate, cudaStream_t stream);
 /* advance_2d_transport (momentum.F90:147-189) in the mixed form: tendency
  * summed in float, transport updated in double; same arguments as
  * getm_advance_2d_transport.                                               */

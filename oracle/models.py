@@ -111,10 +111,12 @@ def seos_nsquared(mask, h, p, S, T):
 class Momentum:
     """python/pygetm/momentum.py:24-1214 (DEFAULT Coriolis, FULL 2D split)."""
 
-    def __init__(self, Am=0.0, An=0.0, cnpar=1.0, advection_scheme=None, avmmol=1.8e-6):
+    def __init__(self, Am=0.0, An=0.0, cnpar=1.0, advection_scheme=None, avmmol=1.8e-6, coriolis_scheme=1):
+        """coriolis_scheme: 1 DEFAULT, 2 ESPELID (momentum.py:14-17)."""
         self._Am_const, self._An_const, self.cnpar = Am, An, cnpar
         self.advection_scheme = advection_scheme
         self.avmmol = avmmol
+        self.coriolis_scheme = coriolis_scheme
 
     def initialize(self, T, runtype, default_scheme):
         ug, vg = T.ugrid, T.vgrid
@@ -169,14 +171,44 @@ class Momentum:
         self._ufirst = False
         self._u3dfirst = False
         self.ob = None  # open-boundary operations (set by the simulation)
+        self._T = T
+        self.An = _arr(T)
+        _fill(self.An, T, self._An_const)
+        self.An_uu = self.An_uv = self.An_vu = self.An_vv = None
 
     def start(self):
         for n, g in self._grids.items():
             a = getattr(self, n)
             a[..., g.land] = 0.0
+        # momentum.py:630-642: numerical damping only where An is non-zero
+        T = self._T
+        self.An[T.land] = FILL
+        if (self.An[T.water] == 0.0).all():
+            self.An_uu = self.An_uv = self.An_vu = self.An_vv = None
+        else:
+            ug, vg = T.ugrid, T.vgrid
+            self.An_uu, self.An_uv = _arr(ug.ugrid, fill=NAN), _arr(ug.vgrid, fill=NAN)
+            self.An_vu, self.An_vv = _arr(vg.ugrid, fill=NAN), _arr(vg.vgrid, fill=NAN)
+            for tgt, g in ((self.An_uu, ug.ugrid), (self.An_uv, ug.vgrid), (self.An_vu, vg.ugrid),
+                           (self.An_vv, vg.vgrid)):
+                O.interpolate(T, g, self.An, tgt)
 
     def coriolis(self, src_grid, U, out_grid, out, x_direction):
-        O.interpolate(src_grid, out_grid, U, out)
+        """momentum.py:1127-1148.  ESPELID: interp(U / sqrt(Din)) * sqrt(Dout),
+        D the water depth (2D) or layer thickness (3D); sqrt(Din) is 1 on
+        land.  The reference leaves the sqrt(Dout) factor unset on land
+        points of the target (np.sqrt with where= and no out=); it is left
+        out there, and nothing reads those points."""
+        if self.coriolis_scheme == 2:
+            Din = src_grid.D if U.ndim == 2 else src_grid.hn
+            Dout = out_grid.D if out.ndim == 2 else out_grid.hn
+            with np.errstate(invalid="ignore"):
+                sqrtDin = np.where(src_grid.mask != 0, np.sqrt(Din), 1.0)
+            O.interpolate(src_grid, out_grid, U / sqrtDin, out)
+            wet = np.broadcast_to(out_grid.mask != 0, out.shape)
+            out[wet] *= np.sqrt(Dout[wet])
+        else:
+            O.interpolate(src_grid, out_grid, U, out)
         out *= out_grid.cor
         if x_direction:
             np.negative(out, out=out)
@@ -211,12 +243,18 @@ class Momentum:
             self.coriolis(T.ugrid, self.U, T.vgrid, self.corV, True)
             self.coriolis(T.vgrid, self.V, T.ugrid, self.corU, False)
         self._transport_2d_momentum(T, self.U, self.V, timestep, self.advU, self.advV, self.diffU, self.diffV)
+        if self.An_uu is not None:  # numerical damping (momentum.py:751-758)
+            O.horizontal_diffusion(T.ugrid, self.U, self.An_uu, self.An_uv, timestep, self.dampU)
+            O.horizontal_diffusion(T.vgrid, self.V, self.An_vu, self.An_vv, timestep, self.dampV)
 
     def _transport_2d_momentum(self, T, U, V, timestep, advU, advV, diffU, diffV):
         ug, vg = T.ugrid, T.vgrid
         with np.errstate(all="ignore"):
             np.divide(U, ug.D, out=self.u1)
             np.divide(V, vg.D, out=self.v1)
+        if self._Am_const > 0.0:  # momentum.py:1051-1064
+            O.momentum_diffusion(ug, vg, ug.ugrid.D, ug.vgrid.D, vg.ugrid.D, vg.vgrid.D, self.u1, self.v1,
+                                 self._Am_const, diffU, diffV)
         if self.apply_bottom_friction:
             self.bottom_friction(T, self.u1, self.v1, ug.D, vg.D, self.ru, self.rv)
         with np.errstate(all="ignore"):
@@ -299,6 +337,9 @@ class Momentum:
             O.interpolate(T, vg, self.ww, ww_v)
             self.vadv.apply_3d(self.vua3d, self.vva3d, ww_v, timestep, self.advqk, new_h=True)
             O.reconstruct_transport_change(vg, self.advqk, self.vadv.h, self.qk, timestep)
+        if self._Am_const > 0.0:  # momentum.py:963-978
+            O.momentum_diffusion(ug, vg, ug.ugrid.hn, ug.vgrid.hn, vg.ugrid.hn, vg.vgrid.hn, self.uk, self.vk,
+                                 self._Am_const, self.diffpk, self.diffqk)
         self._transport_2d_momentum(T, self.Ui, self.Vi, timestep, self.SxA, self.SyA, self.SxD, self.SyD)
         self.SxA[...] = self.advpk.sum(axis=0) - self.SxA
         self.SyA[...] = self.advqk.sum(axis=0) - self.SyA
@@ -406,7 +447,7 @@ class Simulation:
     (BAROCLINIC or BAROTROPIC_3D), matching getm_gb300.simulation.Simulation."""
 
     def __init__(self, T_host, dga, runtype=4, scheme=5, Dmin=0.02, Dcrit=0.1, num=0.0, nuh=0.0, taux=0.0, tauy=0.0,
-                 sp=101325.0, internal_pressure="shchepetkin_mcwilliams"):
+                 sp=101325.0, internal_pressure="shchepetkin_mcwilliams", momentum=None):
         self.runtype = runtype
         self.dga = np.asarray(dga, dtype=float)[:, None, None]
         self.T = T = O.make_grids(T_host)
@@ -423,7 +464,7 @@ class Simulation:
             g._work = _arr(g, fill=NAN)
         self.h_T_half = _arr(T, T.nz, NAN)
         self.depth = _arr(T, T.nz)
-        self.momentum = Momentum()
+        self.momentum = momentum or Momentum()
         self.momentum.initialize(T, runtype, scheme)
         self.taux = _arr(T); _fill(self.taux, T, taux)
         self.tauy = _arr(T); _fill(self.tauy, T, tauy)

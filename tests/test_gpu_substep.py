@@ -94,3 +94,35 @@ def test_substep_kernel_in_cuda_graph():
     assert a.split2d_status() == 0
     bad = _same(a, b)
     assert not bad, bad[:12]
+
+
+def test_substep_error_word_leaves_state_unchanged():
+    """With the error word already set (a grid barrier gave up earlier), a
+    substep launch returns at once: every field and the model time stay as
+    they were and the status stays non-zero, until clear_split2d_status()
+    re-arms the kernel.  The error is planted on the host; no barrier times
+    out."""
+    import torch
+
+    from getm_gb300 import checkpoint
+
+    s = _member("mixed", True, n3d=1)
+    assert s.split2d_status() == 0
+    assert (s.istep + 1) % s.split_factor != 0  # the next advance is a one-launch substep
+    before = {k: v.clone() for k, v in checkpoint.state_tensors(s).items()}
+    t0 = float(s._time)
+    s._split2d.sync[2] = 1
+    s.advance()
+    torch.cuda.synchronize()
+    assert s.split2d_status() != 0
+    after = checkpoint.state_tensors(s)
+    changed = [k for k in before
+               if not bool(((before[k] == after[k]) | (torch.isnan(before[k]) & torch.isnan(after[k]))).all())]
+    assert not changed, changed[:12]
+    assert float(s._time) == t0
+    s.clear_split2d_status()
+    assert s.split2d_status() == 0
+    s.advance()
+    torch.cuda.synchronize()
+    assert s.split2d_status() == 0
+    assert float(s._time) > t0

@@ -37,7 +37,7 @@ sys.path.insert(0, str(ROOT))
 def _args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-graph", action="store_true")
@@ -51,10 +51,13 @@ def _args():
                     help="3D steps after which the mixed form is compared with FP64 (0: skip)")
     ap.add_argument("--ensemble", type=int, default=256, help="members of the batched ensemble (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=4)
-    ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson request rate, 1/s (0: skip)")
-    ap.add_argument("--serve-duration", type=float, default=15.0, help="seconds of arrivals per form")
+    ap.add_argument("--serve-rates", default="50,100,200,400",
+                    help="Poisson request rates, 1/s, comma-separated ('' : skip)")
+    ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate and form")
+    ap.add_argument("--no-c1", dest="c1", action="store_false",
+                    help="skip the 120x100x30 tracer-transport leg")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
-    ap.add_argument("--shelf-steps", type=int, default=0,
+    ap.add_argument("--shelf-steps", type=int, default=100,
                     help="3D steps of the 20-tracer shelf sea, both forms, for its error report (0: skip)")
     ap.add_argument("--shelf-size", default="1000x800x30")
     return ap.parse_args()
@@ -76,7 +79,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
         except Exception:
@@ -181,23 +184,59 @@ def cpu_reference(args, nmacro: int, threads: int):
     return wl.cells * nmacro / dt, dt
 
 
+def _config(wl, ws):
+    """The workload's description, identical in both arms."""
+    return {"workload": f"seamount {wl.T.nx}x{wl.T.ny}x{wl.T.nz} baroclinic split-explicit, "
+                        f"{wl.params['split_factor']} substeps per 3D step",
+            "cells": wl.cells, "wet_cells": wl.wet_cells,
+            "l2": "working set (> 1 GB of 3D fields) exceeds L2; no flush needed",
+            "parallelism": f"replicas x{ws}"}
+
+
+REFERENCE_BUDGET_S = 240.0  # timed CPU work of the reference arm
+
+
 def run_reference(args):
+    """The reference's CPU algorithm (the oracle restatement, OpenMP on every
+    host core) on the same workload: W warm-up 3D steps (at most 2: the CPU
+    has nothing to warm), then K timed 3D steps, stopping early only if the
+    timed work would exceed a few minutes (the line then says how many ran)."""
+    import numpy as np
+
     ws, rank, _ = _dist()
     if rank != 0:
         return
     threads = _host_threads()
-    steps = max(1, min(args.steps, 3))
-    for _ in range(min(args.warmup, 1)):
-        pass
-    value, dt = cpu_reference(args, steps, threads)
-    cfg = {"workload": f"seamount {args.nx}x{args.ny}x{args.nz}, 30 substeps per 3D step, FP64",
-           "sample": f"{steps} 3D steps"}
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    os.environ.setdefault("GETM_ORACLE_VARIANT", "omp" if threads > 1 else "serial")
+    from getm_gb300 import workloads
+    from oracle import models
+
+    wl = workloads.seamount(nx=args.nx, ny=args.ny, nz=args.nz)
+    p = wl.params
+    s = models.Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"])
+    s.temp[...] = np.where(s.T.mask[None] != 0, workloads.seamount_temperature(s.T.zc), s.temp)
+    s.start(p["timestep"], p["split_factor"])
+    nwarm = min(args.warmup, 2)
+    for _ in range(nwarm * p["split_factor"]):
+        s.advance()
+    done, t0 = 0, time.perf_counter()
+    while done < args.steps:
+        for _ in range(p["split_factor"]):
+            s.advance()
+        done += 1
+        el = time.perf_counter() - t0
+        if el * (done + 1) / done > REFERENCE_BUDGET_S:
+            break
+    dt = time.perf_counter() - t0
+    value = wl.cells * done / dt
+    sample = f"{done} of {args.steps} 3D steps timed" if done < args.steps else f"{done} 3D steps"
     line = {"metric": "3D cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
-            "steps": steps, "warmup": 0, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-            "impl": "reference",
+            "steps": done, "warmup": nwarm, "ms_per_step": 1000.0 * dt / done, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": _config(wl, ws), "impl": "reference", "form": "fp64 (CPU restatement, OpenMP)",
             "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": "port",
-                             "sample": f"{steps} 3D steps of the full workload"},
+                             "sample": sample + " of the full workload"},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -223,8 +262,9 @@ def _make_sim(wl, precision, device, round_to_float32=True):
 
 
 class Runner:
-    """Warm-up, CUDA-graph capture and replay of one simulation (two 3D steps
-    per graph: the 3D momentum update alternates its u/v order each step)."""
+    """Warm-up, CUDA-graph capture and replay of one simulation: one graph
+    per 3D step parity (the 3D momentum update alternates its u/v order each
+    step), so every replay is exactly one 3D step with its substeps."""
 
     period = 2
 
@@ -236,34 +276,36 @@ class Runner:
         self.sim = sim
         self.hook = hook
         self.totals0 = sim.totals_device().clone()
-        split = sim.split_factor
         nwarm = max(warmup, 3)
-        nwarm += nwarm % self.period  # captured periods start on an even 3D step
+        nwarm += nwarm % self.period  # captured steps start on an even 3D step
         for _ in range(nwarm):
             self._step3d()
         self.steps_done = nwarm  # 3D steps run on the device so far
         torch.cuda.synchronize()
         n0 = _lib.launch_count()
-        self.graph = None
+        self.graphs = None
         if use_graph:
             stream = torch.cuda.Stream()
             stream.wait_stream(torch.cuda.current_stream())
-            self.graph = torch.cuda.CUDAGraph()
+            self.graphs = []
             with torch.cuda.stream(stream):
-                with torch.cuda.graph(self.graph, stream=stream):
-                    for _ in range(self.period):
+                for _ in range(self.period):
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g, stream=stream):
                         self._step3d()
+                    self.graphs.append(g)
             torch.cuda.current_stream().wait_stream(stream)
             self.launches_per_period = _lib.launch_count() - n0
-            for _ in range(2):
-                self.graph.replay()
-            self.steps_done += 2 * self.period  # the capture itself runs nothing
+            for g in self.graphs:  # capture runs nothing: one untimed replay of each
+                g.replay()
+            self.steps_done += self.period
         else:
             for _ in range(self.period):
                 self._step3d()
             self.launches_per_period = _lib.launch_count() - n0
             self.steps_done += self.period
         torch.cuda.synchronize()
+        self.check()
 
     def _step3d(self):
         for _ in range(self.sim.split_factor):
@@ -271,19 +313,30 @@ class Runner:
         if self.hook is not None:
             self.hook(self.sim)
 
-    def run_period(self):
-        if self.graph is not None:
-            self.graph.replay()
+    def check(self):
+        """Raise if a grid barrier of the one-launch substep gave up (its
+        substeps would then have done no work)."""
+        st = self.sim.split2d_status()
+        if st != 0:
+            raise RuntimeError(f"one-launch substep reported status {st}: a grid barrier gave up")
+
+    def run_step(self):
+        """One 3D step (graph replay of the step's parity)."""
+        if self.graphs is not None:
+            self.graphs[self.steps_done % self.period].replay()
         else:
-            for _ in range(self.period):
-                self._step3d()
-        self.steps_done += self.period
+            self._step3d()
+        self.steps_done += 1
+
+    def run_period(self):
+        for _ in range(self.period):
+            self.run_step()
 
     def run_to(self, nsteps):
         while self.steps_done < nsteps:
-            self.run_period()
+            self.run_step()
 
-    def timed(self, nperiods, clocks_index=None):
+    def timed(self, nsteps, clocks_index=None):
         import torch
 
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -292,12 +345,13 @@ class Runner:
         if sampler:
             sampler.__enter__()
         start.record()
-        for _ in range(nperiods):
-            self.run_period()
+        for _ in range(nsteps):
+            self.run_step()
         end.record()
         torch.cuda.synchronize()
         if sampler:
             sampler.__exit__(None, None, None)
+        self.check()
         return start.elapsed_time(end), (sampler.summary() if sampler else None)
 
 
@@ -461,31 +515,35 @@ def _ensemble_leg(args, device):
 
 
 def _serving_leg(args, device):
-    """Continuous batching of a Poisson request stream (both forms, one after
-    the other, same requests): per-step latency p50/p99 and throughput."""
+    """Continuous batching of Poisson request streams at each rate (both
+    forms, one after the other, the same requests): per-step latency
+    p50/p99, admitted and finished requests and throughput."""
     import torch
 
     from getm_gb300 import workloads
     from getm_gb300.serving import GB, Server, summarize
 
-    out = {"rate_per_s": args.serve_rate, "arrival_window_s": args.serve_duration,
-           "deadline_s": 3.0 * args.serve_duration,
+    rates = [float(x) for x in args.serve_rates.split(",") if x.strip()]
+    out = {"arrival_window_s": args.serve_duration, "deadline_s": 3.0 * args.serve_duration,
            "budget_gb": args.serve_budget_gb, "lanes": 16,
-           "requests": "sides log-uniform 64-512, nz 20-40, 10-200 3D steps, seed 5"}
-    for prec in ("mixed", "fp64"):
-        reqs = workloads.serving_requests(args.serve_rate, args.serve_duration, seed=5, precision=prec)
-        srv = Server(budget_bytes=args.serve_budget_gb * GB, lanes=16, device=device)
-        t0 = time.perf_counter()
-        res = srv.run(reqs, duration=3.0 * args.serve_duration, admit_until=args.serve_duration)
-        wall = time.perf_counter() - t0
-        s = summarize(res, wall)
-        s["requests_arrived"] = len(reqs)
-        s["peak_budget_used_gb"] = srv.peak_used / GB
-        s["admission_host_ms_mean"] = 1e3 * sum(srv.admission_host_s) / max(len(srv.admission_host_s), 1)
-        out[prec] = s
-        del srv, res
-        torch.cuda.synchronize()
-        torch.cuda.empty_cache()
+           "requests": "sides log-uniform 64-512, nz 20-40, 10-200 3D steps, seed 5", "rates": {}}
+    for rate in rates:
+        per = {}
+        for prec in ("mixed", "fp64"):
+            reqs = workloads.serving_requests(rate, args.serve_duration, seed=5, precision=prec)
+            srv = Server(budget_bytes=args.serve_budget_gb * GB, lanes=16, device=device)
+            t0 = time.perf_counter()
+            res = srv.run(reqs, duration=3.0 * args.serve_duration, admit_until=args.serve_duration)
+            wall = time.perf_counter() - t0
+            s = summarize(res, wall)
+            s["requests_arrived"] = len(reqs)
+            s["peak_budget_used_gb"] = srv.peak_used / GB
+            s["admission_host_ms_mean"] = 1e3 * sum(srv.admission_host_s) / max(len(srv.admission_host_s), 1)
+            per[prec] = s
+            del srv, res
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+        out["rates"][str(rate)] = per
     return out
 
 
@@ -507,8 +565,8 @@ def _shelf_leg(args, device):
     runners = {}
     for f in ("mixed", "fp64"):
         r = Runner(workloads.start_shelf_sea(wl, f, device), 3, not args.no_graph)
-        ms, _ = r.timed(5)
-        out[f] = {"ms_per_step": ms / (5 * Runner.period), "value": cells * 5 * Runner.period / (ms / 1000.0)}
+        ms, _ = r.timed(10)
+        out[f] = {"ms_per_step": ms / 10, "value": cells * 10 / (ms / 1000.0)}
         runners[f] = r
     for r in runners.values():
         r.run_to(args.shelf_steps)
@@ -532,8 +590,103 @@ def _shelf_leg(args, device):
     return out
 
 
+def _substep_kernel_leg(runner, peak, peak_kind):
+    """Time the one-launch 2D substep (substep_2d_kernel) on the live state:
+    CUDA events around every substep of two 3D steps that is not followed
+    by a 3D step (one launch each), against the substep's algorithmic bytes
+    (its 2D fields stay resident in L2, so the HBM figure is a reference
+    point, not its bound)."""
+    import torch
+
+    from getm_gb300 import roofline
+
+    sim = runner.sim
+    if sim._split2d is None:
+        return None
+    if runner.steps_done % runner.period:
+        runner.run_step()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(2):
+        for k in range(sim.split_factor):
+            if k == sim.split_factor - 1:
+                sim.advance()
+                continue
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            sim.advance()
+            e1.record()
+            times.append((e0, e1))
+        runner.steps_done += 1
+        if runner.hook is not None:
+            runner.hook(sim)
+    torch.cuda.synchronize()
+    runner.check()
+    us = sorted(a.elapsed_time(b) * 1000.0 for a, b in times)
+    t = us[len(us) // 2] / 1e6
+    T = sim.T
+    b = roofline.substep_bytes(T.nx, T.ny)
+    return {"kernel": f"substep_2d_kernel<{'true' if sim.precision == 'mixed' else 'false'}>",
+            "us_per_launch_median": us[len(us) // 2], "launches_timed": len(us),
+            "bytes_per_launch": b, "achieved_gbs": b / t / 1e9, "peak": peak, "peak_kind": peak_kind,
+            "frac_of_hbm": b / t / 1e9 / peak,
+            "note": "2D fields of one plane are L2-resident; bound by FP64 pipe, barriers and latency"}
+
+
+def _tracer_transport_leg(args, device, threads):
+    """The plain FP64 tracer transport (120 x 100 x 30, superbee, implicit
+    vertical diffusion): 500 steps on the GPU (each step one graph replay)
+    against the oracle on the host cores (a sample of 50 steps)."""
+    import torch
+
+    from getm_gb300 import workloads
+    from getm_gb300.simulation import TracerTransport
+
+    wl = workloads.tracer_transport()
+    nsteps = 500
+    g = TracerTransport(wl, device=device)
+    for _ in range(3):
+        g.step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            g.step()
+    torch.cuda.current_stream().wait_stream(stream)
+    graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(nsteps):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1000.0
+    out = {"workload": "tracer transport 120x100x30, dt 30 s, superbee + implicit vertical diffusion, FP64",
+           "steps": nsteps, "value": wl.cells * nsteps / t, "unit": "cell-updates/s",
+           "ms_per_step": 1000.0 * t / nsteps, "cuda_graph": True}
+    if not args.no_cpu_baseline:
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        os.environ.setdefault("GETM_ORACLE_VARIANT", "omp" if threads > 1 else "serial")
+        from oracle.models import TracerTransport as OT
+
+        o = OT(wl)
+        o.step()
+        n = 50
+        t0 = time.perf_counter()
+        for _ in range(n):
+            o.step()
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": wl.cells * n / tc, "unit": "cell-updates/s", "cores": threads,
+                               "kind": "port", "sample": f"{n} steps"}
+    del g, graph
+    torch.cuda.synchronize()
+    return out
+
+
 def run_ours(args):
-    import numpy as np
     import torch
 
     ws, rank, local = _dist()
@@ -545,19 +698,16 @@ def run_ours(args):
     import __graft_entry__
 
     __graft_entry__.build()
-    from getm_gb300 import workloads
+    from getm_gb300 import roofline, workloads
 
     device = f"cuda:{local}"
     wl = workloads.seamount(nx=args.nx, ny=args.ny, nz=args.nz)
-    split = wl.params["split_factor"]
-    period = Runner.period
-    nsteps = args.steps + (args.steps % period)
-    nper = nsteps // period
+    nsteps = args.steps
     primary = args.precision
     forms = [primary] + ([] if args.no_compare else [f for f in ("fp64", "mixed") if f != primary])
     runners = {f: Runner(_make_sim(wl, f, device), args.warmup, not args.no_graph) for f in forms}
 
-    # device-timed region for each form
+    # device-timed region for each form: exactly nsteps 3D steps
     ms = {}
     clocks = None
     for f in forms:
@@ -565,18 +715,20 @@ def run_ours(args):
             import torch.distributed as dist
 
             dist.barrier()
-        m, c = runners[f].timed(nper, clocks_index=local if f == primary else None)
+        m, c = runners[f].timed(nsteps, clocks_index=local if f == primary else None)
         if f == primary:
             clocks = c
         ms[f] = _max_over_ranks(m, "cuda")
     cells = wl.cells
     values = {f: _whole_job_rate(cells, nsteps, ms[f]) for f in forms}
 
-    # end to end through the public API: per 3D step, upload the surface
-    # forcing (taux, tauy, sp) from pinned host memory and read back z
+    # end to end through the public API: before every 3D step the surface
+    # forcing (taux, tauy, sp) is uploaded from pinned host memory, after
+    # it the surface elevation z is read back
     e2e = {}
     for f in forms:
-        sim = runners[f].sim
+        r = runners[f]
+        sim = r.sim
         forcing = [sim.airsea.taux, sim.airsea.tauy, sim.airsea.sp]
         host_in = [x.all_values.detach().cpu().pin_memory() for x in forcing]
         host_out = torch.empty(sim.T.z.all_values.shape, dtype=torch.float64).pin_memory()
@@ -588,53 +740,66 @@ def run_ours(args):
 
             dist.barrier()
         t0 = time.perf_counter()
-        for _ in range(nper):
-            for _ in range(period):
-                for x, h in zip(forcing, host_in):
-                    x.all_values.copy_(h, non_blocking=True)
-            runners[f].run_period()
+        for _ in range(nsteps):
+            for x, h in zip(forcing, host_in):
+                x.all_values.copy_(h, non_blocking=True)
+            r.run_step()
             host_out.copy_(sim.T.z.all_values, non_blocking=True)
         torch.cuda.synchronize()
         dt = _max_over_ranks(time.perf_counter() - t0, "cuda")
+        r.check()
         e2e[f] = {"value": _whole_job_rate(cells, nsteps, 1000.0 * dt), "unit": "cell-updates/s",
-                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h // period}
+                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     # error of the mixed form against FP64 after the same number of 3D steps
     err = None
     if "mixed" in runners and "fp64" in runners and args.error_steps > 0 and rank == 0:
         err = _errors(wl, runners, args, device)
+        for r in runners.values():
+            r.check()
 
     peak, peak_kind = _peaks()
-    roofline = _roofline(runners[primary].sim, peak, peak_kind)
+    roofline_kernel = _roofline(runners[primary].sim, peak, peak_kind)
+    T = wl.T
+    step_roof = {}
+    for f in forms:
+        b = roofline.step_bytes(T.nx, T.ny, T.nz, f, ntracer=2, split=wl.params["split_factor"])
+        t = ms[f] / nsteps / 1000.0
+        step_roof[f] = {"bytes_per_step": b["total"], "bytes_3d": b["3d"], "bytes_2d_loop": b["2d"],
+                        "achieved_gbs": b["total"] / t / 1e9, "peak": peak, "peak_kind": peak_kind,
+                        "frac": b["total"] / t / 1e9 / peak}
+    substep = _substep_kernel_leg(runners[primary], peak, peak_kind)
     r = runners[primary]
     line = {"metric": "3D cell-updates/s", "value": values[primary], "unit": "cell-updates/s", "n_gpus": ws,
             "steps": nsteps, "warmup": max(args.warmup, 3), "ms_per_step": ms[primary] / nsteps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if primary == "mixed" else "f64", "data": "synthetic",
-            "config": {"workload": f"seamount {wl.T.nx}x{wl.T.ny}x{wl.T.nz} baroclinic split-explicit, "
-                                   f"{split} substeps per 3D step, {primary} form",
-                       "precision": primary, "cells": cells, "wet_cells": wl.wet_cells,
-                       "cuda_graph": r.graph is not None,
-                       "l2": "working set (> 1 GB of 3D fields) exceeds L2; no flush needed",
-                       "parallelism": f"replicas x{ws}"},
-            "e2e": e2e[primary], "roofline": roofline,
-            "gpu_launches": r.launches_per_period * nper, "clocks": clocks}
+            "config": _config(wl, ws), "form": primary, "cuda_graph": r.graphs is not None,
+            "e2e": e2e[primary], "roofline": roofline_kernel, "step_roofline": step_roof,
+            "gpu_launches": r.launches_per_period * nsteps // r.period, "clocks": clocks,
+            "split2d_status": {f: runners[f].sim.split2d_status() for f in forms}}
+    if substep is not None:
+        line["substep_kernel"] = substep
     for f in forms:
         if f != primary:
             line[f] = {"value": values[f], "ms_per_step": ms[f] / nsteps, "e2e": e2e[f]["value"]}
     if err is not None:
         line["error_vs_fp64"] = err
+    threads = _host_threads()
+    if rank == 0 and args.c1:
+        line["tracer_transport"] = _tracer_transport_leg(args, device, threads)
     if rank == 0 and args.ensemble > 0:
         line["ensemble"] = _ensemble_leg(args, device)
-    if rank == 0 and args.serve_rate > 0:
+    if rank == 0 and args.serve_rates:
         line["serving"] = _serving_leg(args, device)
     if rank == 0 and args.shelf_steps > 0:
         line["shelf_sea"] = _shelf_leg(args, device)
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
-        threads = _host_threads()
         v, dt = cpu_reference(args, 2, threads)
         line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
                                 "sample": f"2 3D steps of the full workload ({dt:.1f} s)"}
+        line["speedup_vs_cpu"] = {f"{f}_e2e": e2e[f]["value"] / v for f in forms}
+        line["speedup_vs_cpu"].update({f"{f}_device": values[f] / v for f in forms})
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -5,6 +5,11 @@ Compiles ``getm_oracle.c`` to ``oracle/_build/libgetm_oracle.so`` with
 default code generation on generic x86-64 for the reference Fortran).
 ``variant="omp"`` builds the same source with OpenMP for the timed CPU
 baseline (the per-row loops carry ``omp`` pragmas that are inert otherwise).
+``variant="fma"`` lets the compiler contract multiply-adds into fused
+multiply-adds (``-ffp-contract=fast``; on x86-64 with ``-mfma`` so that the
+instruction exists), as gfortran does by default for the reference on
+aarch64: the two builds are the reference's own spread between two valid
+compilations, against which the GPU's rounding differences are measured.
 """
 
 from __future__ import annotations
@@ -31,6 +36,14 @@ def build(variant: str = "serial", force: bool = False) -> Path:
     flags = ["-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11"]
     if variant == "omp":
         flags = ["-O3", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11", "-fopenmp"]
+    elif variant == "fma":
+        import platform
+
+        flags = ["-O2", "-ffp-contract=fast", "-fPIC", "-shared", "-std=c11"]
+        if platform.machine() in ("x86_64", "AMD64"):
+            flags.append("-mfma")
+    elif variant != "serial":
+        raise ValueError(f"unknown oracle variant {variant!r}")
     tmp = out.with_suffix(".tmp")
     cmd = [os.environ.get("CC", "gcc")] + flags + [str(SRC), "-o", str(tmp), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -41,5 +54,5 @@ def build(variant: str = "serial", force: bool = False) -> Path:
 
 
 if __name__ == "__main__":
-    for v in ("serial", "omp"):
+    for v in ("serial", "omp", "fma"):
         print(build(v, force="--force" in sys.argv))

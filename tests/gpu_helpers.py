@@ -60,3 +60,39 @@ def dev(a, device="cuda"):
 
 def host(t):
     return t.detach().cpu().numpy()
+
+
+def oracle_variant(variant: str):
+    """Context manager: every oracle call inside runs the given build of the
+    C restatement ("serial": no contraction; "fma": multiply-adds contracted
+    as gfortran does on aarch64)."""
+    import contextlib
+
+    import oracle.oracle as O
+
+    @contextlib.contextmanager
+    def cm():
+        old = O._lib
+        O._lib = O.load_variant(variant)
+        try:
+            yield
+        finally:
+            O._lib = old
+
+    return cm()
+
+
+def relative_errors(a: dict, b: dict) -> dict:
+    """max |a - b| / max |b| per field over each field's water points; a and
+    b map names to (array, mask) or (array, mask, scale) with the same keys."""
+    out = {}
+    for k, v in b.items():
+        x, m = v[0], v[1]
+        y = a[k][0]
+        wet = np.broadcast_to(m, x.shape)
+        xs, ys = x[wet], y[wet]
+        # an optional third entry: the scale to measure against (for a field
+        # that is the small difference of two larger terms)
+        scale = v[2] if len(v) > 2 else (np.abs(xs).max() if xs.size else 0.0)
+        out[k] = float(np.abs(ys - xs).max() / scale) if scale > 0 else float(np.abs(ys - xs).max(initial=0.0))
+    return out

@@ -6,23 +6,30 @@ configurations' full sizes.
   first and after the second 3D step, field by field (elevation, transports,
   3D velocities, vertical velocity, layer thicknesses, both tracers, both
   internal-pressure gradients, squared buoyancy and shear frequency, bottom
-  shear velocity, slow terms).
+  shear velocity and drag, slow terms).
 * Tracer transport 120 x 100 x 30 (dx = 1 km, dt = 30 s, superbee, implicit
   vertical diffusion): 500 steps, the error recorded every 50 steps; the
   drift over the run is bounded.
 
-Tolerances (relative to each field's largest magnitude on water points):
-1e-10 after one seamount 3D step and 1e-9 after two (the GPU contracts
-multiply-adds and sums columns in its own order; those last-bit differences
-pass through the dynamics, where the flow is the small residual of the
-sigma-coordinate pressure gradient); 1e-10 for the tracer over all 500
-transport steps.
+Tolerances (relative to each field's largest magnitude on water points).
+Tracers and layer thicknesses: 1e-13 after each seamount 3D step; the
+tracer-transport tracer: 1e-12 over all 500 steps.  The seamount's flow
+fields (elevation, transports, velocities, w, the internal-pressure
+gradient and the terms built from them) are the small residual of large
+cancelling terms (the sigma-coordinate pressure gradient over a 4000 m
+seamount), so one-ulp differences grow far beyond 1e-12 there: the same
+oracle compiled with and without contracted multiply-adds (both valid
+builds of the reference; gfortran contracts on aarch64) already differs by
+up to 2e-7 (internal-pressure gradient) after one 3D step.  Each such field
+must stay within 100 times that spread of the reference itself, and below
+1e-5.
 """
 
 import numpy as np
 import pytest
 
 from tests.test_gpu_operators import close
+from tests.test_gpu_simulation import _gpu_fields, _oracle_fields, check_against_spread
 
 pytestmark = pytest.mark.gpu
 
@@ -31,60 +38,49 @@ def _host(a):
     return a.all_values.detach().cpu().numpy()
 
 
-def _seamount_errors(wl, o, g):
-    """Max relative error of every compared field (no assertion)."""
-    from oracle.models import seos_nsquared
-
-    T = wl.T
-    wetT, wetU, wetV = T.mask == 1, T.ugrid.mask == 1, T.vgrid.mask == 1
-    m, om = g.momentum, o.momentum
-    pairs = {
-        "z": (g.T.z, o.T.z, wetT), "U": (m.U, om.U, wetU), "V": (m.V, om.V, wetV),
-        "uk": (m.uk, om.uk, wetU), "vk": (m.vk, om.vk, wetV), "hn": (g.T.hn, o.T.hn, wetT),
-        "temp": (g.temp, o.temp, wetT), "salt": (g.salt, o.salt, wetT),
-        "idpdx": (g.idpdx, o.idpdx, wetU), "idpdy": (g.idpdy, o.idpdy, wetV),
-        "ustar_b": (m.ustar_b, om.ustar_b, wetT), "SxA": (m.SxA, om.SxA, wetU), "SyA": (m.SyA, om.SyA, wetV),
-        "SxB": (m.SxB, om.SxB, wetU), "SxF": (m.SxF, om.SxF, wetU),
-    }
-    errs = {}
-    for name, (a, b, wet) in pairs.items():
-        errs[name] = close(_host(a), b, 1.0, wet)
-    errs["ww"] = close(_host(m.ww)[1:-1], om.ww[1:-1], 1.0, wetT)
-    errs["SS"] = close(_host(m.SS)[1:-1], om.SS[1:-1], 1.0, wetT)
-    NN = seos_nsquared(T.mask, o.T.hn, o.depth, o.salt, o.temp)
-    errs["NN"] = close(_host(g.NN)[1:-1], NN, 1.0, wetT)
-    return errs
-
-
 def test_seamount_full_size_two_3d_steps():
     import torch
 
     from getm_gb300 import workloads
     from getm_gb300.simulation import Simulation as GS
     from oracle.models import Simulation as OS
+    from tests.gpu_helpers import oracle_variant, relative_errors
 
     wl = workloads.seamount()  # 400 x 300 x 40
     assert (wl.T.nx, wl.T.ny, wl.T.nz) == (400, 300, 40)
     p = wl.params
-    o = OS(wl.T, wl.dga, num=p["num"], nuh=p["nuh"])
+    nstep = 2
+    snaps, temp0 = {}, None
+    for variant in ("serial", "fma"):
+        with oracle_variant(variant):
+            o = OS(wl.T, wl.dga, num=p["num"], nuh=p["nuh"])
+            if temp0 is None:
+                temp0 = np.where(o.T.mask[None] != 0, workloads.seamount_temperature(o.T.zc), o.temp)
+            o.temp[...] = temp0
+            o.start(p["timestep"], p["split_factor"])
+            snaps[variant] = []
+            for _ in range(nstep):
+                for _ in range(p["split_factor"]):
+                    o.advance()
+                snaps[variant].append(_oracle_fields(wl, o))
+            del o
     g = GS(wl.T, wl.dga, num=p["num"], nuh=p["nuh"])
-    temp0 = np.where(o.T.mask[None] != 0, workloads.seamount_temperature(o.T.zc), o.temp)
-    o.temp[...] = temp0
     g.temp.all_values.copy_(torch.from_numpy(temp0))
-    o.start(p["timestep"], p["split_factor"])
     g.start(p["timestep"], p["split_factor"])
     assert g._split2d is not None  # the one-launch substep is on the path
-    for step, rtol in ((1, 1e-10), (2, 1e-9)):
+    for step in range(nstep):
         for _ in range(p["split_factor"]):
-            o.advance()
             g.advance()
         torch.cuda.synchronize()
         assert g.split2d_status() == 0
-        errs = _seamount_errors(wl, o, g)
-        print(f"seamount 400x300x40, after 3D step {step}: "
-              + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
-        bad = {k: v for k, v in errs.items() if not v <= rtol}
-        assert not bad, f"3D step {step}: above {rtol}: {bad}"
+        ref = snaps["serial"][step]
+        spread = relative_errors(snaps["fma"][step], ref)
+        err = relative_errors(_gpu_fields(g, ref), ref)
+        print(f"seamount 400x300x40, 3D step {step + 1}, gpu error / oracle FMA spread: "
+              + ", ".join(f"{k} {err[k]:.1e}/{spread[k]:.1e}" for k in err))
+        for k in ("temp", "salt", "hn"):
+            assert err[k] <= 1e-13, (k, err[k])
+        check_against_spread(err, spread)
 
 
 def test_tracer_transport_full_size_500_steps():
@@ -106,7 +102,7 @@ def test_tracer_transport_full_size_500_steps():
     print("tracer transport 120x100x30, relative error every 50 steps: "
           + ", ".join(f"{n}: {e:.2e}" for n, e in series))
     worst = max(e for _, e in series)
-    assert worst <= 1e-10, series
+    assert worst <= 1e-12, series
     # the tracer stays bounded like the oracle's (no growth of the blob)
     a = _host(g.tracers[0])[..., wet]
     b = o.tracers[0][..., wet]

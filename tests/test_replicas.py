@@ -74,3 +74,8 @@ def test_reference_arm_prints_the_contract_line(capsys, monkeypatch):
     assert line["cpu_baseline"]["cores"] == 1  # the threads it ran with
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    assert line["steps"] == 1 and line["warmup"] == 1
+    # the same workload description as the GPU arm prints
+    from getm_gb300 import workloads
+
+    assert line["config"] == bench._config(workloads.seamount(nx=24, ny=20, nz=4), 1)

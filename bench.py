@@ -50,7 +50,7 @@ def _args():
     ap.add_argument("--error-steps", type=int, default=1000,
                     help="3D steps after which the mixed form is compared with FP64 (0: skip)")
     ap.add_argument("--ensemble", type=int, default=256, help="members of the batched ensemble (0: skip)")
-    ap.add_argument("--ensemble-steps", type=int, default=4)
+    ap.add_argument("--ensemble-steps", type=int, default=8)
     ap.add_argument("--serve-rates", default="50,100,200,400",
                     help="Poisson request rates, 1/s, comma-separated ('' : skip)")
     ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate and form")
@@ -355,6 +355,11 @@ class Runner:
         return start.elapsed_time(end), (sampler.summary() if sampler else None)
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one x-pass launch over both
+# tracers of the 400 x 300 x 40 seamount (ncu, profiles/); None: not captured
+TRAFFIC_X_PASS = {"_f32": 152.51e6}
+
+
 def _roofline(sim, peak, peak_kind):
     """Time the dominant kernel alone on the live state: one x-direction
     advection pass of both tracers (hpass_x_kernel, one launch)."""
@@ -371,7 +376,9 @@ def _roofline(sim, peak, peak_kind):
     h_out = torch.empty_like(h_in)
     fin = [x.all_values for x in tr._tracers]
     fout = [torch.empty_like(x) for x in fin]
-    sfx = "_f32" if u.dtype == torch.float32 else ""
+    from getm_gb300.core import _sfx_storage
+
+    sfx = _sfx_storage([u], fin)
     pin = _lib.ptr_array([x.data_ptr() for x in fin])
     pout = _lib.ptr_array([x.data_ptr() for x in fout])
     stream = torch.cuda.current_stream().cuda_stream
@@ -391,16 +398,20 @@ def _roofline(sim, peak, peak_kind):
     ev1.record()
     torch.cuda.synchronize()
     t_kernel = ev0.elapsed_time(ev1) / reps / 1000.0
-    n3 = h_in.numel()
+    # interior cells of the layers the pass updates (halos excluded)
+    n3 = T.nx * T.ny * T.nz
     sz = u.element_size()
+    fsz = fin[0].element_size()
     # u, hu, h in + h out + per tracer in + out (each 3D field read or written once)
-    alg = n3 * (sz + 8 + 8 + 8 + len(fin) * 2 * sz)
+    alg = n3 * (sz + 8 + 8 + 8 + len(fin) * 2 * fsz)
     achieved = alg / t_kernel / 1e9
+    kernel = {"_f32": "hpass_x_inc_kernel<float>", "_f64s": "hpass_x_inc_kernel<double, float>",
+              "": "hpass_x_kernel<double>"}[sfx]
     # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
-    # of the float x pass on this workload, from an ncu capture of this bench
-    traffic = 152.51e6 if sz == 4 else None
+    # of this kernel on this workload, from an ncu capture of this bench
+    traffic = TRAFFIC_X_PASS.get(sfx)
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": f"{'hpass_x_inc_kernel<float>' if sz == 4 else 'hpass_x_kernel<double>'} (2 tracers)",
+            "traffic": traffic, "kernel": f"{kernel} (2 tracers)",
             "bytes_per_launch": alg, "us_per_launch": t_kernel * 1e6, "peak_kind": peak_kind}
 
 
@@ -462,53 +473,77 @@ def _pcts(deltas):
 
 
 def _ensemble_leg(args, device):
-    """Batched ensemble of independent domains (mixed form): every member's
-    3D step is one graph replay on one of 16 lane streams.  Throughput of the
-    lane-concurrent replay against the same members replayed one after
-    another on one stream, and the per-member step latency."""
+    """Batched ensemble of independent domains (mixed form, each member with
+    the tuned launch shapes of its size), two ways on the same members:
+    (a) every member's 3D step is one graph replay on one of 16 lane
+    streams; (b) the 2D substeps of all members run as one persistent
+    cooperative launch per substep index, then every member's 3D step on the
+    lanes.  Throughput of both against the members replayed one after
+    another, and the per-member step latency.  Set-up happens before the
+    timed regions."""
     import torch
 
     from getm_gb300 import workloads
-    from getm_gb300.ensemble import Ensemble, make_member
+    from getm_gb300.ensemble import BatchedEnsemble, Ensemble, make_member
 
-    t_setup = time.perf_counter()
     wls = workloads.ensemble(args.ensemble, seed=4)
-    ens = Ensemble([make_member(w, "mixed", device) for w in wls], lanes=16)
-    ens.prepare()
-    t_setup = time.perf_counter() - t_setup
-    n = len(ens.runners)
     main = torch.cuda.current_stream()
+    steps = max(args.ensemble_steps, 2)
 
-    def timed(steps, sequential):
+    def timed(step, n, nsteps):
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
-        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n)] for _ in range(steps)]
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n)] for _ in range(nsteps)]
         torch.cuda.synchronize()
         start.record(main)
-        for s in range(steps):
-            ens.step(sequential=sequential, events=evs[s])
+        for q in range(nsteps):
+            step(evs[q])
         end.record(main)
         torch.cuda.synchronize()
         deltas = []
         for m in range(n):
-            times = [start.elapsed_time(evs[s][m]) / 1000.0 for s in range(steps)]
+            times = [start.elapsed_time(evs[q][m]) / 1000.0 for q in range(nsteps)]
             deltas += [b - a for a, b in zip(times, times[1:])]
         return start.elapsed_time(end) / 1000.0, deltas
 
-    ens.step()  # one untimed replay of every graph
-    steps = max(args.ensemble_steps, 2)
-    t_conc, d_conc = timed(steps, False)
-    t_seq, d_seq = timed(2, True)
+    t_setup = time.perf_counter()
+    ens = Ensemble([make_member(w, "mixed", device, tiles="auto") for w in wls], lanes=16)
+    ens.prepare()
+    t_setup = time.perf_counter() - t_setup
+    n = len(ens.runners)
     cells = ens.cells
-    conc = cells * steps / t_conc
-    seq = cells * 2 / t_seq
+    ens.step()  # one untimed replay of every graph
+    t_conc, d_conc = timed(lambda e: ens.step(events=e), n, steps)
+    t_seq, _ = timed(lambda e: ens.step(sequential=True, events=e), n, 2)
+    conc, seq = cells * steps / t_conc, cells * 2 / t_seq
     p50, p99 = _pcts(d_conc)
-    out = {"members": n, "cells": cells, "lanes": 16, "steps": steps, "value": conc, "unit": "cell-updates/s",
-           "sequential_value": seq, "speedup_vs_sequential": conc / seq,
-           "member_step_latency_p50_ms": p50, "member_step_latency_p99_ms": p99,
-           "setup_s": t_setup, "precision": "mixed",
-           "workload": "256-type ensemble: sides log-uniform 64-256, nz 20-40, 20-40 substeps, seed 4"}
     del ens
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+    t_bsetup = time.perf_counter()
+    bat = BatchedEnsemble([make_member(w, "mixed", device, substep_kernel=True, tiles="auto") for w in wls],
+                          lanes=16)
+    bat.prepare()
+    t_bsetup = time.perf_counter() - t_bsetup
+    bat.step()
+    t_bat, d_bat = timed(lambda e: bat.step(events=e), n, steps)
+    torch.cuda.synchronize()
+    if bat.status() != 0:
+        raise RuntimeError("batched substep reported a barrier error")
+    bp50, bp99 = _pcts(d_bat)
+    out = {"members": n, "cells": cells, "lanes": 16, "steps": steps, "unit": "cell-updates/s",
+           "precision": "mixed", "tiles": "tuned per member size (autotune cache)",
+           "workload": "256-type ensemble: sides log-uniform 64-256, nz 20-40, 20-40 substeps, seed 4",
+           "value": max(conc, cells * steps / t_bat),
+           "lane_graphs": {"value": conc, "member_step_latency_p50_ms": p50, "member_step_latency_p99_ms": p99,
+                           "setup_s": t_setup},
+           "batched_substeps": {"value": cells * steps / t_bat, "member_step_latency_p50_ms": bp50,
+                                "member_step_latency_p99_ms": bp99, "setup_s": t_bsetup,
+                                "launches_per_round": max(bat.nsub) + n},
+           "sequential_value": seq}
+    out["speedup_vs_sequential"] = out["value"] / seq
+    del bat
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     return out

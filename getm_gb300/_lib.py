@@ -51,6 +51,7 @@ _SIGS = {
     "getm_advection_2d_noalloc": "ipppiippppdpppps",
     "getm_advection_uv_pass": "iipppppdpppipps",
     "getm_advection_uv_pass_f32": "iipppppdpppipps",
+    "getm_advection_uv_pass_f64s": "iipppppdpppipps",
     "getm_vertical_diffusion_create": "pp",
     "getm_vertical_diffusion_finalize": "p",
     "getm_vertical_diffusion_prepare": "piiidpddppps",
@@ -88,6 +89,14 @@ _SIGS = {
     "getm_momentum_3d_advection_inputs_f32": "iiippppppppppps",
     "getm_coriolis_3d": "iiiiipppis",
     "getm_coriolis_3d_f32": "iiiiipppis",
+    "getm_substep_batch_create": "iip",
+    "getm_substep_batch_set": "piiipiiiiiiidddppppippppi",
+    "getm_substep_batch_upload": "p",
+    "getm_substep_batch_participants": "pip",
+    "getm_substep_batch_launch": "piips",
+    "getm_substep_batch_finalize": "p",
+    "getm_tune_set": "ii",
+    "getm_tune_get": "ip",
     "getm_coriolis_espelid": "iiiiipppppppis",
     "getm_coriolis_espelid_f32": "iiiiipppppppis",
     "getm_buoyancy_frequency": "iiipppppps",
@@ -114,7 +123,9 @@ _SIGS = {
     "getm_density_buoyancy": "ippppps",
     "getm_launch_count": "p",
     "getm_advection_apply_3d_batch_f32": "ppppippppppdpppips",
+    "getm_advection_apply_3d_batch_f64s": "ppppippppppdpppips",
     "getm_vertical_diffusion_batch_f32": "iiippddppippppps",
+    "getm_vertical_diffusion_batch_f64s": "iiippddppippppps",
     "getm_grid_interp_x_f32": "iiippis",
     "getm_grid_interp_y_f32": "iiippis",
     "getm_grid_interp_z_f32": "iiiippis",

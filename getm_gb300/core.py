@@ -110,6 +110,18 @@ def _stream():
     return torch.cuda.current_stream().cuda_stream
 
 
+def _sfx_storage(velocities, fields):
+    """Entry-point suffix from the velocity (or diffusivity) tensors and the
+    field tensors: '' (all FP64), '_f32' (all float) or '_f64s' (float
+    velocities, FP64-stored fields: the mixed form with FP64 tracers)."""
+    v, f = _sfx(*velocities), _sfx(*fields)
+    if v == f:
+        return v
+    if v == "_f32" and f == "":
+        return "_f64s"
+    raise TypeError(f"unsupported combination: velocities {velocities[0].dtype}, fields {fields[0].dtype}")
+
+
 def _sfx(*tensors):
     """Entry-point suffix for the tensors' type: '' (FP64) or '_f32'."""
     dt = tensors[0].dtype

@@ -194,86 +194,89 @@ __global__ void __launch_bounds__(32 * GETM_V_BY) hpass_y_kernel(HPassArgs<T> a)
 }
 
 // grid (segments, ceil(ny_ / 8), nk): warp (ty) of block (x, y, k) owns row j = 8 y + ty of layer k
-template <typename S>
-__global__ void __launch_bounds__(256) hpass_x_inc_kernel(HPassArgs<S> a)
+template <typename S, typename V = S>
+__global__ void __launch_bounds__(256) hpass_x_inc_kernel(HPassArgs<S, V> a)
 {
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (j >= a.ny_) return;  // whole warp
-    hpass_x_inc_rows<S, 1>(a, blockIdx.x, j, blockIdx.z, threadIdx.x);
+    hpass_x_inc_rows<S, 1, NoEpi, V>(a, blockIdx.x, j, blockIdx.z, threadIdx.x);
 }
 
-template <typename S>
-__global__ void __launch_bounds__(32 * HY_BY) hpass_y_inc_kernel(HPassArgs<S> a)
+template <typename S, typename V = S>
+__global__ void __launch_bounds__(32 * HY_BY) hpass_y_inc_kernel(HPassArgs<S, V> a)
 {
     __shared__ YIncSmem<S> sm;
-    hpass_y_inc_body<S>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y, sm);
+    hpass_y_inc_body<S, NoEpi, V>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y, sm);
 }
 
-template <typename S, int NT>
-__global__ void __launch_bounds__(256) hpass_y_march_kernel(HPassArgs<S> a, int nchunk)
+template <typename S, int NT, typename V = S>
+__global__ void __launch_bounds__(256) hpass_y_march_kernel(HPassArgs<S, V> a, int nchunk)
 {
     const int w = blockIdx.y * blockDim.y + threadIdx.y;
     const int chunk = w % nchunk, k = w / nchunk;
     if (k >= a.nk) return;  // whole warp
     // one sweep per group of NT tracers; with no tracers one sweep updates h
     for (int t0 = 0; t0 == 0 || t0 < a.ntracer; t0 += NT)
-        hpass_y_march_body<S, NT>(a, blockIdx.x, chunk, k, threadIdx.x, t0);
+        hpass_y_march_body<S, NT, V>(a, blockIdx.x, chunk, k, threadIdx.x, t0);
 }
 
-// Launch one horizontal pass in increment form (any storage type S).
-template <typename S>
-static int launch_hpass_inc(int direction, HPassArgs<S>& a, cudaStream_t stream)
+// Launch one horizontal pass in increment form (any storage type S,
+// velocity type V).
+template <typename S, typename V = S>
+static int launch_hpass_inc(int direction, HPassArgs<S, V>& a, cudaStream_t stream)
 {
     if (direction == 1) {
-        dim3 block(32, 8);
+        const int rows = getm_tune(GETM_TUNE_XPASS_ROWS);
+        dim3 block(32, rows);
         // lane 0 of the first segment handles the face west of cell 0
-        dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up(a.ny_, 8), a.nk);
-        hpass_x_inc_kernel<S><<<grid, block, 0, stream>>>(a);
+        dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up(a.ny_, rows), a.nk);
+        hpass_x_inc_kernel<S, V><<<grid, block, 0, stream>>>(a);
     } else if (a.nk < 4) {
         // a single plane: too few columns x layers for marching warps to fill
         // the GPU, so blocks of 32 x HY_BY threads cover tiles instead
         dim3 block(32, HY_BY);
         dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_ + 1, HY_STRIDE), a.nk);
-        hpass_y_inc_kernel<S><<<grid, block, 0, stream>>>(a);
+        hpass_y_inc_kernel<S, V><<<grid, block, 0, stream>>>(a);
     } else {
-        const int nchunk = getm_div_up(a.ny_, YM_CH);
+        a.ych = getm_tune(GETM_TUNE_YMARCH_CHUNK);
+        const int nchunk = getm_div_up(a.ny_, a.ych);
         dim3 block(32, 8);
         dim3 grid(getm_div_up(a.nx_, 32), getm_div_up((long long)nchunk * a.nk, 8));
-        if (a.ntracer >= 2) hpass_y_march_kernel<S, 2><<<grid, block, 0, stream>>>(a, nchunk);
-        else hpass_y_march_kernel<S, 1><<<grid, block, 0, stream>>>(a, nchunk);
+        if (a.ntracer >= 2) hpass_y_march_kernel<S, 2, V><<<grid, block, 0, stream>>>(a, nchunk);
+        else hpass_y_march_kernel<S, 1, V><<<grid, block, 0, stream>>>(a, nchunk);
     }
     GETM_CHECK_LAUNCH();
     return GETM_OK;
 }
 
-template <typename T>
-static int launch_hpass(int direction, HPassArgs<T>& a, cudaStream_t stream)
+template <typename T, typename V = T>
+static int launch_hpass(int direction, HPassArgs<T, V>& a, cudaStream_t stream)
 {
-    if constexpr (getm_increment_form<T>) {
-        return launch_hpass_inc<T>(direction, a, stream);
+    if constexpr (getm_increment_form<T> || !std::is_same<T, V>::value) {
+        return launch_hpass_inc<T, V>(direction, a, stream);
     } else {
-        if (a.increment) return launch_hpass_inc<T>(direction, a, stream);
+        if (a.increment) return launch_hpass_inc<T, V>(direction, a, stream);
+        if (direction == 1) {
+            const int BY = 8;
+            dim3 block(32, BY);
+            dim3 grid(getm_div_up(a.nx_, 32), getm_div_up((long long)a.ny_ * a.nk, BY));
+            hpass_x_kernel<T><<<grid, block, 0, stream>>>(a);
+        } else {
+            dim3 block(32, GETM_V_BY);
+            dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, GETM_V_BY), a.nk);
+            hpass_y_kernel<T><<<grid, block, 0, stream>>>(a);
+        }
+        GETM_CHECK_LAUNCH();
+        return GETM_OK;
     }
-    if (direction == 1) {
-        const int BY = 8;
-        dim3 block(32, BY);
-        dim3 grid(getm_div_up(a.nx_, 32), getm_div_up((long long)a.ny_ * a.nk, BY));
-        hpass_x_kernel<T><<<grid, block, 0, stream>>>(a);
-    } else {
-        dim3 block(32, GETM_V_BY);
-        dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, GETM_V_BY), a.nk);
-        hpass_y_kernel<T><<<grid, block, 0, stream>>>(a);
-    }
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
 }
 
 // Fill the direction-dependent fields of HPassArgs from the grid handles
 // (wrapper.F90:240-253: direction 1 passes ugrid mask/idx/dy, 2 passes vgrid
 // mask/dx/idy).
-template <typename T>
-static int hpass_setup(HPassArgs<T>& a, int direction, const getm_advection* adv, const getm_grid* tg,
-                       const getm_grid* vg, int nk, const T* u, const double* Ah, double dt, const double* hu,
+template <typename T, typename V = T>
+static int hpass_setup(HPassArgs<T, V>& a, int direction, const getm_advection* adv, const getm_grid* tg,
+                       const getm_grid* vg, int nk, const V* u, const double* Ah, double dt, const double* hu,
                        int increment = 0)
 {
     if (!tg || !vg || !u || !hu) return GETM_ERR_ARG;
@@ -291,7 +294,7 @@ static int hpass_setup(HPassArgs<T>& a, int direction, const getm_advection* adv
     a.tmask = tg->mask; a.iA = tg->iarea; a.Ah = Ah; a.u = u; a.hu = hu; a.dt = dt;
     a.scheme = adv->scheme;
     a.dtf = (float)dt;
-    if (getm_increment_form<T> || increment) {
+    if (getm_increment_form<T> || !std::is_same<T, V>::value || increment) {
         a.increment = 1;
         int rc = getm_grid_f32_metrics(const_cast<getm_grid*>(tg), 0);
         if (!rc) rc = getm_grid_f32_metrics(const_cast<getm_grid*>(vg), 0);
@@ -305,8 +308,8 @@ static int hpass_setup(HPassArgs<T>& a, int direction, const getm_advection* adv
 }
 
 // Run one horizontal stage for ntracer tracers, chunked by GETM_MAX_BATCH.
-template <typename T>
-static int run_hstage(HPassArgs<T>& a, int direction, const double* h_in, double* h_out, int ntracer,
+template <typename T, typename V = T>
+static int run_hstage(HPassArgs<T, V>& a, int direction, const double* h_in, double* h_out, int ntracer,
                       const T* const* fin, T* const* fout, cudaStream_t stream)
 {
     a.h_in = h_in; a.h_out = h_out;
@@ -316,7 +319,7 @@ static int run_hstage(HPassArgs<T>& a, int direction, const double* h_in, double
         if (n > GETM_MAX_BATCH) n = GETM_MAX_BATCH;
         a.ntracer = n;
         for (int t = 0; t < n; t++) { a.fin[t] = fin[done + t]; a.fout[t] = fout[done + t]; }
-        int rc = launch_hpass<T>(direction, a, stream);
+        int rc = launch_hpass<T, V>(direction, a, stream);
         if (rc) return rc;
         done += n;
     } while (done < ntracer);
@@ -326,13 +329,15 @@ static int run_hstage(HPassArgs<T>& a, int direction, const double* h_in, double
 // ---------------------------------------------------------------------------
 // vertical pass (template w3d :223-374)
 // ---------------------------------------------------------------------------
-template <typename T>
+// T: the advected fields; V: w and w_var (T unless given).  T = double, V =
+// float is the mixed form with FP64 tracer storage (increment form).
+template <typename T, typename V = T>
 struct WPassArgs {
     int nx_, ny_, nz;
     long long plane;
     int ilo, ihi, jlo, jhi;
     const int* tmask;
-    const T* w;                 // nz+1 levels
+    const V* w;                 // nz+1 levels
     const double* h_in;         // layer thickness at stage start (not modified)
     double* h_out;              // layer thickness after the pass (last tracer's)
     double* haux;               // column work arrays for sub-stepping (nz levels)
@@ -341,7 +346,7 @@ struct WPassArgs {
     int scheme;
     int ntracer;
     int* status;
-    const T* wvar[GETM_MAX_BATCH];
+    const V* wvar[GETM_MAX_BATCH];
     T* f[GETM_MAX_BATCH];       // updated in place
 };
 
@@ -404,20 +409,21 @@ __device__ void w_substep(const WPassArgs<T>& a, long long c, const T* wv, const
 // with e_k = W_k (face_k - f_k) and e'_{k-1} = W_{k-1} (face_{k-1} - f_k).
 // NT fields advected with the same w_var share every thickness and velocity
 // load and the face constants; each field keeps its own window.
-template <int NT>
-__device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const float* wv, const double* hs,
-                              const float* const (&fs)[NT], double* hd, float* const (&fdst)[NT], double dtk,
+template <int NT, typename S>
+__device__ void w_substep_inc(const WPassArgs<S, float>& a, long long c, const float* wv, const double* hs,
+                              const S* const (&fs)[NT], double* hd, S* const (&fdst)[NT], double dtk,
                               double itersm1)
 {
     const long long P = a.plane;
     const int nz = a.nz;
     const float dtkf = (float)dtk, itf = (float)itersm1, dtf = (float)a.dt;
-    float fkm1[NT], fk[NT], fk1[NT], erm[NT];  // erm: e'_{k-1}, interface below, deviation from level k
+    S fkm1[NT], fk[NT], fk1[NT];
+    float erm[NT];  // erm: e'_{k-1}, interface below, deviation from level k
 #pragma unroll
     for (int q = 0; q < NT; q++) {
-        fkm1[q] = 0.f;
+        fkm1[q] = S(0);
         fk[q] = fs[q][c];
-        fk1[q] = (nz > 1) ? fs[q][c + P] : 0.f;
+        fk1[q] = (nz > 1) ? fs[q][c + P] : S(0);
         erm[q] = 0.f;
     }
     double hk = hs[c], hk1 = (nz > 1) ? hs[c + P] : 0.0;
@@ -429,10 +435,10 @@ __device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const floa
     float Wn = (nz > 1) ? wv[c + P] : 0.f;
     float wkn = a.w[c + P];
     for (int k = 0; k < nz; k++) {
-        float fk2[NT];
+        S fk2[NT];
         double hk2 = 0.0;
 #pragma unroll
-        for (int q = 0; q < NT; q++) fk2[q] = (k + 2 < nz) ? fs[q][c + (k + 2) * P] : 0.f;
+        for (int q = 0; q < NT; q++) fk2[q] = (k + 2 < nz) ? fs[q][c + (k + 2) * P] : S(0);
         if (k + 2 < nz) hk2 = hs[c + (k + 2) * P];
         const float W = Wn;
         const float wk = wkn;
@@ -447,14 +453,17 @@ __device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const floa
         for (int q = 0; q < NT; q++) {
             float el = 0.f, er = 0.f;
             if (k < nz - 1) {
-                const float d = fk1[q] - fk[q];
+                // differences of neighbouring values in the storage type,
+                // then narrowed (exact for float storage)
+                const float d = inc_f<S>(fk1[q] - fk[q]);
                 float dev;
-                if (W > 0.f) dev = getm_tvd_dev_f(tf, fk1[q] - fk[q], fk[q] - ((k > 0) ? fkm1[q] : fk[q]));
-                else dev = getm_tvd_dev_f(tf, fk[q] - fk1[q], fk1[q] - ((k < nz - 2) ? fk2[q] : fk1[q]));
+                if (W > 0.f) dev = getm_tvd_dev_f(tf, d, inc_f<S>(fk[q] - ((k > 0) ? fkm1[q] : fk[q])));
+                else dev = getm_tvd_dev_f(tf, -d, inc_f<S>(fk1[q] - ((k < nz - 2) ? fk2[q] : fk1[q])));
                 el = W * (W > 0.f ? dev : d + dev);
                 er = W * (W > 0.f ? dev - d : dev);
             }
-            fdst[q][c + k * P] = fk[q] + dtkf * (((wk - W) - (wkm1 - Wm)) * fk[q] - el + erm[q]) / (hkf - dh);
+            fdst[q][c + k * P] =
+                inc_add<S>(fk[q], dtkf * (((wk - W) - (wkm1 - Wm)) * inc_f<S>(fk[q]) - el + erm[q]) / (hkf - dh));
             erm[q] = er;
             fkm1[q] = fk[q]; fk[q] = fk1[q]; fk1[q] = fk2[q];
         }
@@ -466,12 +475,12 @@ __device__ void w_substep_f32(const WPassArgs<float>& a, long long c, const floa
 
 // Largest Courant number over the interior interfaces of a column
 // (template :274, :294, :300).  Returns -1 when nz == 1 (no interfaces).
-template <typename T>
-__device__ double w_maxcfl(const WPassArgs<T>& a, long long c, const T* wv, const double* hs)
+template <typename T, typename V>
+__device__ double w_maxcfl(const WPassArgs<T, V>& a, long long c, const V* wv, const double* hs)
 {
     const long long P = a.plane;
-    T cmax = T(-1);
-    if constexpr (getm_increment_form<T>) {
+    V cmax = V(-1);
+    if constexpr (getm_increment_form<V>) {
         const float dtf = (float)a.dt;
         float hk = getm_d2f_approx(hs[c]);
         for (int k = 1; k < a.nz; k++) {
@@ -485,7 +494,7 @@ __device__ double w_maxcfl(const WPassArgs<T>& a, long long c, const T* wv, cons
     double hk = hs[c];
     for (int k = 1; k < a.nz; k++) {
         double hk1 = hs[c + k * P];
-        T cfl = fabs(wv[c + k * P]) * (T)a.dt / (T)fmin(hk, hk1);
+        V cfl = fabs(wv[c + k * P]) * (V)a.dt / (V)fmin(hk, hk1);
         if (k == 1 || cfl > cmax) cmax = cfl;
         hk = hk1;
     }
@@ -500,13 +509,13 @@ __device__ __forceinline__ int w_iters_from(double cfl)
 }
 
 // Thread per column.
-template <typename T>
-// block (32, 4): 32 columns of 4 rows (row lengths need not be multiples
-// of 128 columns)
-__global__ void __launch_bounds__(128, getm_increment_form<T> ? 7 : 1) wpass_kernel(WPassArgs<T> a)
+// T: fields; V: velocities.  Blocks of 32 columns by GETM_TUNE_COLUMN_ROWS
+// rows (row lengths need not be multiples of 128 columns).
+template <typename T, typename V = T>
+__global__ void __launch_bounds__(128, getm_increment_form<V> ? 7 : 1) wpass_kernel(WPassArgs<T, V> a)
 {
     const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 4 + threadIdx.y;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= a.nx_ || j >= a.ny_) return;
     const long long c = (long long)j * a.nx_ + i;
     const bool touched = i >= a.ilo && i <= a.ihi && j >= a.jlo && j <= a.jhi && a.tmask[c] == 1 && a.ntracer > 0;
@@ -522,10 +531,13 @@ __global__ void __launch_bounds__(128, getm_increment_form<T> ? 7 : 1) wpass_ker
     // together (the sub-step count depends only on w_var and h); the second
     // one's intermediate sub-steps use the upper half of the column work
     // array, which holds n3 doubles
-    constexpr bool inc = getm_increment_form<T>;
+    constexpr bool inc = getm_increment_form<V>;
+    // pairs only for float fields: the second field's intermediate sub-steps
+    // need the upper half of the column work array (n3 doubles)
+    constexpr bool pairs = inc && sizeof(T) == 4;
     for (int t = 0; t < a.ntracer;) {
-        const int nt = (inc && t + 1 < a.ntracer && a.wvar[t + 1] == a.wvar[t]) ? 2 : 1;
-        const T* wv = a.wvar[t];
+        const int nt = (pairs && t + 1 < a.ntracer && a.wvar[t + 1] == a.wvar[t]) ? 2 : 1;
+        const V* wv = a.wvar[t];
         T* f = a.f[t];
         int iters = 1;
         double itersm1 = 1.0, dtk = a.dt;
@@ -554,16 +566,16 @@ __global__ void __launch_bounds__(128, getm_increment_form<T> ? 7 : 1) wpass_ker
             T* fd = (it == iters) ? f : a.faux;
             double* hd = (it == iters && t + nt == a.ntracer) ? a.h_out : a.haux;
             if constexpr (inc) {
-                if (nt == 2) {
+                if (pairs && nt == 2) {
                     T* f2 = a.f[t + 1];
                     T* faux2 = a.faux + a.plane * a.nz;
                     const T* const fs2[2] = {fs, (it == 1) ? f2 : faux2};
                     T* const fd2[2] = {fd, (it == iters) ? f2 : faux2};
-                    w_substep_f32<2>(a, c, wv, hs, fs2, hd, fd2, dtk, itersm1);
+                    w_substep_inc<2, T>(a, c, wv, hs, fs2, hd, fd2, dtk, itersm1);
                 } else {
                     const T* const fs1[1] = {fs};
                     T* const fd1[1] = {fd};
-                    w_substep_f32<1>(a, c, wv, hs, fs1, hd, fd1, dtk, itersm1);
+                    w_substep_inc<1, T>(a, c, wv, hs, fs1, hd, fd1, dtk, itersm1);
                 }
             } else {
                 w_substep(a, c, wv, hs, fs, hd, fd, dtk, itersm1);
@@ -574,11 +586,11 @@ __global__ void __launch_bounds__(128, getm_increment_form<T> ? 7 : 1) wpass_ker
     }
 }
 
-template <typename T>
-static int run_wstage(getm_advection* adv, const getm_grid* tg, const T* w, const T* const* wvar, double dt,
+template <typename T, typename V = T>
+static int run_wstage(getm_advection* adv, const getm_grid* tg, const V* w, const V* const* wvar, double dt,
                       const double* h_in, double* h_out, int ntracer, T* const* f, cudaStream_t stream)
 {
-    WPassArgs<T> a;
+    WPassArgs<T, V> a;
     memset(&a, 0, sizeof(a));
     a.nx_ = tg->nx_; a.ny_ = tg->ny_; a.nz = tg->kmax - tg->kmin + 1;
     a.plane = (long long)tg->nx_ * tg->ny_;
@@ -587,8 +599,9 @@ static int run_wstage(getm_advection* adv, const getm_grid* tg, const T* w, cons
     a.tmask = tg->mask; a.w = w; a.dt = dt; a.scheme = adv->scheme; a.status = adv->status;
     a.haux = adv->colbuf[0]; a.faux = (T*)adv->colbuf[1];
     if (a.nz < 1) return GETM_ERR_ARG;
-    dim3 block(32, 4);
-    dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, 4));
+    const int rows = getm_tune(GETM_TUNE_COLUMN_ROWS);
+    dim3 block(32, rows);
+    dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, rows));
     // Chunks: every chunk starts from h_in; the final h is the last chunk's.
     int done = 0;
     do {
@@ -597,17 +610,18 @@ static int run_wstage(getm_advection* adv, const getm_grid* tg, const T* w, cons
         a.ntracer = n;
         a.h_in = h_in; a.h_out = h_out;
         for (int t = 0; t < n; t++) { a.wvar[t] = wvar[done + t]; a.f[t] = f[done + t]; }
-        wpass_kernel<T><<<grid, block, 0, stream>>>(a);
+        wpass_kernel<T, V><<<grid, block, 0, stream>>>(a);
         GETM_CHECK_LAUNCH();
         done += n;
     } while (done < ntracer);
     return GETM_OK;
 }
 
-// Fused Strang split for either form (see getm_advection_apply_3d_batch).
-template <typename T>
+// Fused Strang split for any form (see getm_advection_apply_3d_batch): T
+// the fields, V the velocities.
+template <typename T, typename V = T>
 static int apply_3d_batch_impl(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,
-                               int ufirst, const T* u, const T* v, const T* w, const T* const* w_var,
+                               int ufirst, const V* u, const V* v, const V* w, const V* const* w_var,
                                const double* Ah_u, const double* Ah_v, double timestep, double* h,
                                const double* hu, const double* hv, int ntracer, T* const* vars,
                                cudaStream_t stream)
@@ -615,14 +629,14 @@ static int apply_3d_batch_impl(getm_advection* adv, getm_grid* tgrid, getm_grid*
     if (!adv) return GETM_OK;
     if (!tgrid || !w || !h || ntracer < 1 || !vars) return GETM_ERR_ARG;
     const int nz = tgrid->kmax - tgrid->kmin + 1;
-    HPassArgs<T> ax, ay;
-    int rc = hpass_setup<T>(ax, 1, adv, tgrid, ugrid, nz, u, Ah_u, 0.5 * timestep, hu);
+    HPassArgs<T, V> ax, ay;
+    int rc = hpass_setup<T, V>(ax, 1, adv, tgrid, ugrid, nz, u, Ah_u, 0.5 * timestep, hu);
     if (rc) return rc;
-    if ((rc = hpass_setup<T>(ay, 2, adv, tgrid, vgrid, nz, v, Ah_v, 0.5 * timestep, hv))) return rc;
+    if ((rc = hpass_setup<T, V>(ay, 2, adv, tgrid, vgrid, nz, v, Ah_v, 0.5 * timestep, hv))) return rc;
     const size_t n3 = (size_t)ax.plane * nz;
     if ((rc = adv_reserve(adv, n3, ntracer))) return rc;
 
-    const T* wv[GETM_MAX_BATCH * 8];
+    const V* wv[GETM_MAX_BATCH * 8];
     const T* fin[GETM_MAX_BATCH * 8];
     T* fout[GETM_MAX_BATCH * 8];
     T* tmp[GETM_MAX_BATCH * 8];
@@ -631,27 +645,27 @@ static int apply_3d_batch_impl(getm_advection* adv, getm_grid* tgrid, getm_grid*
         tmp[t] = (T*)adv->tmp[t];
     }
 
-    HPassArgs<T>* first = ufirst ? &ax : &ay;
+    HPassArgs<T, V>* first = ufirst ? &ax : &ay;
     const int dfirst = ufirst ? 1 : 2;
-    HPassArgs<T>* second = ufirst ? &ay : &ax;
+    HPassArgs<T, V>* second = ufirst ? &ay : &ax;
     const int dsecond = ufirst ? 2 : 1;
     double* A = adv->hbuf[0];
     double* B = adv->hbuf[1];
 
     // adv1(dt/2): vars -> tmp, h -> A   (operators.py:165-170)
     for (int t = 0; t < ntracer; t++) { fin[t] = vars[t]; fout[t] = tmp[t]; }
-    if ((rc = run_hstage<T>(*first, dfirst, h, A, ntracer, fin, fout, stream))) return rc;
+    if ((rc = run_hstage<T, V>(*first, dfirst, h, A, ntracer, fin, fout, stream))) return rc;
     // adv2(dt/2): tmp -> vars, A -> B   (:171-175)
     for (int t = 0; t < ntracer; t++) { fin[t] = tmp[t]; fout[t] = vars[t]; }
-    if ((rc = run_hstage<T>(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
+    if ((rc = run_hstage<T, V>(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
     // w(dt): vars in place, B -> A      (:176-182)
-    if ((rc = run_wstage<T>(adv, tgrid, w, wv, timestep, B, A, ntracer, vars, stream))) return rc;
+    if ((rc = run_wstage<T, V>(adv, tgrid, w, wv, timestep, B, A, ntracer, vars, stream))) return rc;
     // adv2(dt/2): vars -> tmp, A -> B   (:183-188)
     for (int t = 0; t < ntracer; t++) { fin[t] = vars[t]; fout[t] = tmp[t]; }
-    if ((rc = run_hstage<T>(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
+    if ((rc = run_hstage<T, V>(*second, dsecond, A, B, ntracer, fin, fout, stream))) return rc;
     // adv1(dt/2): tmp -> vars, B -> h   (:189-193)
     for (int t = 0; t < ntracer; t++) { fin[t] = tmp[t]; fout[t] = vars[t]; }
-    if ((rc = run_hstage<T>(*first, dfirst, B, h, ntracer, fin, fout, stream))) return rc;
+    if ((rc = run_hstage<T, V>(*first, dfirst, B, h, ntracer, fin, fout, stream))) return rc;
     return GETM_OK;
 }
 
@@ -720,9 +734,21 @@ extern "C" int getm_advection_apply_3d_batch_f32(getm_advection* adv, getm_grid*
                                       hu, hv, ntracer, vars, stream);
 }
 
-template <typename T>
+extern "C" int getm_advection_apply_3d_batch_f64s(getm_advection* adv, getm_grid* tgrid,
+                                                  getm_grid* ugrid, getm_grid* vgrid, int ufirst,
+                                                  const float* u, const float* v, const float* w,
+                                                  const float* const* w_var, const double* Ah_u,
+                                                  const double* Ah_v, double timestep, double* h,
+                                                  const double* hu, const double* hv, int ntracer,
+                                                  double* const* vars, cudaStream_t stream)
+{
+    return apply_3d_batch_impl<double, float>(adv, tgrid, ugrid, vgrid, ufirst, u, v, w, w_var, Ah_u, Ah_v,
+                                              timestep, h, hu, hv, ntracer, vars, stream);
+}
+
+template <typename T, typename V = T>
 static int uv_pass_impl(int direction, int nk, getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
-                        const T* u, const double* Ah, double timestep, const double* h_in, double* h_out,
+                        const V* u, const double* Ah, double timestep, const double* h_in, double* h_out,
                         const double* hu, int ntracer, const T* const* fin, T* const* fout, cudaStream_t stream)
 {
     if (!adv || (direction != 1 && direction != 2) || nk < 1 || !h_in || !h_out || ntracer < 0) return GETM_ERR_ARG;
@@ -730,10 +756,10 @@ static int uv_pass_impl(int direction, int nk, getm_advection* adv, getm_grid* t
     if (h_in == h_out) return GETM_ERR_ARG;
     for (int t = 0; t < ntracer; t++)
         if (!fin[t] || !fout[t] || (const void*)fin[t] == (const void*)fout[t]) return GETM_ERR_ARG;
-    HPassArgs<T> a;
-    int rc = hpass_setup<T>(a, direction, adv, tgrid, ugrid, nk, u, Ah, timestep, hu);
+    HPassArgs<T, V> a;
+    int rc = hpass_setup<T, V>(a, direction, adv, tgrid, ugrid, nk, u, Ah, timestep, hu);
     if (rc) return rc;
-    return run_hstage<T>(a, direction, h_in, h_out, ntracer, fin, fout, stream);
+    return run_hstage<T, V>(a, direction, h_in, h_out, ntracer, fin, fout, stream);
 }
 
 extern "C" int getm_advection_uv_pass(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
@@ -752,6 +778,16 @@ extern "C" int getm_advection_uv_pass_f32(int direction, int nk, getm_advection*
 {
     return uv_pass_impl<float>(direction, nk, adv, tgrid, ugrid, u, Ah, timestep, h_in, h_out, hu, ntracer, var_in,
                                var_out, stream);
+}
+
+extern "C" int getm_advection_uv_pass_f64s(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
+                                           getm_grid* ugrid, const float* u, const double* Ah, double timestep,
+                                           const double* h_in, double* h_out, const double* hu, int ntracer,
+                                           const double* const* var_in, double* const* var_out,
+                                           cudaStream_t stream)
+{
+    return uv_pass_impl<double, float>(direction, nk, adv, tgrid, ugrid, u, Ah, timestep, h_in, h_out, hu, ntracer,
+                                       var_in, var_out, stream);
 }
 
 static int advection_2d_impl(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid, getm_grid* vgrid,

@@ -12,11 +12,14 @@
 // ---------------------------------------------------------------------------
 // horizontal pass kernels
 // ---------------------------------------------------------------------------
-// T is the type of the advected fields and of the velocities: double for the
-// FP64 form, float for the mixed form.  Layer thicknesses, the transports QU
-// that update them and all grid metrics are double in both forms.  For
-// T = double every expression below is the FP64 reference arithmetic.
-template <typename T>
+// T is the type of the advected fields, V that of the velocities (T unless
+// given): double for the FP64 form, float for the mixed form; the mixed form
+// with FP64 tracer storage has T = double, V = float (its increments are
+// still formed in float).  Layer thicknesses, the transports QU that update
+// them and all grid metrics are double in every form.  For T = V = double
+// without increment form every expression below is the FP64 reference
+// arithmetic.
+template <typename T, typename V = T>
 struct HPassArgs {
     int nx_, ny_, nk;
     long long plane;            // nx_ * ny_
@@ -27,7 +30,7 @@ struct HPassArgs {
     const int* tmask;
     const double* iA;
     const double* Ah;           // 2D horizontal diffusivity on the velocity grid, or NULL
-    const T* u;                 // velocity (nk layers)
+    const V* u;                 // velocity (nk layers)
     const double* hu;           // layer thickness on the velocity grid (nk layers)
     const double* h_in;
     double* h_out;
@@ -38,6 +41,7 @@ struct HPassArgs {
     // selects the increment-form kernels for double fields (2D momentum)
     int increment;
     float dtf;
+    int ych;                    // rows a warp marches in the 3D y pass (launch-shape knob)
     const float* idx_f;
     const float* dy_f;
     const float* iA_f;
@@ -221,19 +225,6 @@ __device__ __forceinline__ void hpass_y_body(const HPassArgs<T>& a, int bx, int 
 // mixed form, whose state stays FP64 while its increments are evaluated in
 // float).  Differences of neighbouring values are formed in S and then
 // narrowed, so they keep their accuracy when the values are close.
-template <typename S>
-__device__ __forceinline__ float inc_f(S x)
-{
-    if constexpr (std::is_same<S, double>::value) return getm_d2f_approx(x);
-    else return x;
-}
-
-template <typename S>
-__device__ __forceinline__ S inc_add(S x, float dx)
-{
-    if constexpr (std::is_same<S, double>::value) return x + getm_f2d(dx);
-    else return x + dx;
-}
 
 // Limited face deviation from the upwind cell, given d = f[b] - f[a] across
 // the face and the differences on either side, dprev = f[a] - f[a-1] and
@@ -255,8 +246,8 @@ constexpr int HX_STRIDE = 31;
 // KB layers k0 .. k0+KB-1 (those below nk) of row j: the 2D fields (masks,
 // metrics) are loaded once for all of them, and every load of the KB layers
 // is issued before any value is used.
-template <typename S, int KB, typename Epi = NoEpi>
-__device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, int j, int k0, int lane,
+template <typename S, int KB, typename Epi = NoEpi, typename V = S>
+__device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S, V>& a, int bx, int j, int k0, int lane,
                                                  const Epi& epi = Epi())
 {
     constexpr unsigned FULL = 0xffffffffu;
@@ -278,7 +269,7 @@ __device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, 
     const float ahraw = a.Ah ? getm_d2f_approx(a.Ah[r2 + iac]) : 0.f;
     const int tm = a.tmask[r2 + ibc];
     const float iaf = a.iA_f[r2 + ibc];
-    S uraw[KB];
+    V uraw[KB];
     double huraw[KB], hold[KB];
 #pragma unroll
     for (int kk = 0; kk < KB; kk++) {
@@ -323,7 +314,7 @@ __device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, 
         float QU = 0.f, cfl = 0.f, ahd = 0.f;
         bool up = false, uu_ok = false;
         if (act) {
-            const float uu = inc_f<S>(uraw[kk]);
+            const float uu = inc_f<V>(uraw[kk]);
             const float huf = getm_d2f_approx(huraw[kk]);
             QU = uu * huf * dyf;
             cfl = fabsf(uu * a.dtf * idxf);
@@ -394,14 +385,14 @@ __device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S>& a, int bx, 
 }
 
 // One row (layer k, row j) of the x pass: row = k ny_ + j.
-template <typename S, typename Epi = NoEpi>
-__device__ __forceinline__ void hpass_x_inc_body(const HPassArgs<S>& a, int bx, long long row, int lane,
+template <typename S, typename Epi = NoEpi, typename V = S>
+__device__ __forceinline__ void hpass_x_inc_body(const HPassArgs<S, V>& a, int bx, long long row, int lane,
                                                  const Epi& epi = Epi())
 {
     if (row >= (long long)a.ny_ * a.nk) return;  // whole warp shares one row
     const int k = (int)(row / a.ny_);
     const int j = (int)(row - (long long)k * a.ny_);
-    hpass_x_inc_rows<S, 1, Epi>(a, bx, j, k, lane, epi);
+    hpass_x_inc_rows<S, 1, Epi, V>(a, bx, j, k, lane, epi);
 }
 
 // y-direction pass in increment form: the transpose of hpass_x_inc_kernel.
@@ -421,8 +412,8 @@ struct YIncSmem {
     float sx[HY_BY][32];       // per-face exchange (QU, then el)
 };
 
-template <typename S, typename Epi = NoEpi>
-__device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, int by, int k, int tx, int ty,
+template <typename S, typename Epi = NoEpi, typename V = S>
+__device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S, V>& a, int bx, int by, int k, int tx, int ty,
                                                  YIncSmem<S>& sm, const Epi& epi = Epi())
 {
     auto& sf = sm.sf;
@@ -448,7 +439,7 @@ __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, 
         if (act) {
             const int m_s = ja > 0 ? a.umask[q2 - s] : 0;
             const int m_n = ja + 1 < a.ny_ ? a.umask[q2 + s] : 0;
-            const float vv = inc_f<S>(a.u[base + ja * s]);
+            const float vv = inc_f<V>(a.u[base + ja * s]);
             const float hvf = getm_d2f_approx(a.hu[base + ja * s]);
             const float dxf = a.dy_f[q2], idyf = a.idx_f[q2];
             QU = vv * hvf * dxf;
@@ -517,8 +508,8 @@ __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, 
 
 
 // y-direction pass in increment form, marching north.  A warp owns 32
-// columns of one layer and a chunk of YM_CH cells along y.  Walking the
-// faces j = j0-1 .. j0+YM_CH-1 it keeps the last four rows of every tracer,
+// columns of one layer and a chunk of a.ych cells along y.  Walking the
+// faces j = j0-1 .. j0+a.ych-1 it keeps the last four rows of every tracer,
 // the three differences around the face and the south face's QU and er in
 // registers, so each step issues one independent load per field and row
 // (no shared memory, no block barriers) and updates cell j from its south
@@ -526,10 +517,9 @@ __device__ __forceinline__ void hpass_y_inc_body(const HPassArgs<S>& a, int bx, 
 // is that of hpass_y_inc_body, operation for operation; NT tracers are
 // marched together, larger batches in groups of NT (the face geometry is
 // reloaded per group).
-constexpr int YM_CH = 32;
 
-template <typename S, int NT>
-__device__ __forceinline__ void hpass_y_march_body(const HPassArgs<S>& a, int bx, int chunk, int k, int lane,
+template <typename S, int NT, typename V = S>
+__device__ __forceinline__ void hpass_y_march_body(const HPassArgs<S, V>& a, int bx, int chunk, int k, int lane,
                                                    int t0)
 {
     const int i = bx * 32 + lane;
@@ -538,8 +528,8 @@ __device__ __forceinline__ void hpass_y_march_body(const HPassArgs<S>& a, int bx
     const int ic = icol ? i : a.nx_ - 1;  // in-bounds column for the loads of idle lanes
     const long long base = (long long)k * a.plane + ic;
     const bool iint = icol && i >= a.ilo && i <= a.ihi;
-    const int jc0 = chunk * YM_CH;
-    const int jc1 = min(jc0 + YM_CH, a.ny_);
+    const int jc0 = chunk * a.ych;
+    const int jc1 = min(jc0 + a.ych, a.ny_);
     const int nt = min(NT, a.ntracer - t0);
     const bool first_group = t0 == 0;
     // tracers q >= nt of the group (none when ntracer is 0) read as zero
@@ -573,7 +563,7 @@ __device__ __forceinline__ void hpass_y_march_body(const HPassArgs<S>& a, int bx
     struct StepLoads {
         int m_1, tm;
         S f2[NT];
-        S uraw;
+        V uraw;
         double huraw, hold;
         float dxf, idyf, ahraw, iaf;
     };
@@ -604,7 +594,7 @@ __device__ __forceinline__ void hpass_y_march_body(const HPassArgs<S>& a, int bx
         const S* f2 = cur.f2;
         const bool jin = j >= 0 && j < a.ny_;
         const long long jr = (long long)(jin ? j : 0) * s;
-        const S uraw = cur.uraw;
+        const V uraw = cur.uraw;
         const double huraw = cur.huraw;
         const float dxf = cur.dxf, idyf = cur.idyf, ahraw = cur.ahraw;
         const double hold = cur.hold;
@@ -618,7 +608,7 @@ __device__ __forceinline__ void hpass_y_march_body(const HPassArgs<S>& a, int bx
         if (f_in) {
             act = getm_flux_point(m_0);
             if (act) {
-                const float vv = inc_f<S>(uraw);
+                const float vv = inc_f<V>(uraw);
                 const float hvf = getm_d2f_approx(huraw);
                 QU = vv * hvf * dxf;
                 cfl = fabsf(vv * a.dtf * idyf);

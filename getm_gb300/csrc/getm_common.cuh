@@ -43,6 +43,9 @@ struct getm_grid {
 // capture.
 int getm_grid_f32_metrics(getm_grid* g, cudaStream_t stream);
 
+// Launch-shape knob of the calling host thread (GETM_TUNE_*; getm_tune_set).
+int getm_tune(int knob);
+
 // Host-side count of kernel launches issued by this library (one increment
 // per launch site executed); read with getm_launch_count().
 extern "C" unsigned long long getm_launch_counter_add(void);
@@ -114,6 +117,24 @@ __device__ __forceinline__ float getm_d2f_approx(double x)
     const unsigned int s = (unsigned int)(b >> 63) << 31;
     const unsigned int m = (unsigned int)((b >> 29) & 0x7fffffu);
     return __uint_as_float(s | ((unsigned int)e << 23) | m);
+}
+
+// Increment-form helpers for a field stored as S (float, or double for the
+// FP64 storage of the mixed form's 2D momentum and tracers): a value or a
+// difference of neighbouring values (formed in S) narrowed to the float
+// arithmetic of the increments, and a float increment added in S.
+template <typename S>
+__device__ __forceinline__ float inc_f(S x)
+{
+    if constexpr (std::is_same<S, double>::value) return getm_d2f_approx(x);
+    else return x;
+}
+
+template <typename S>
+__device__ __forceinline__ S inc_add(S x, float dx)
+{
+    if constexpr (std::is_same<S, double>::value) return x + getm_f2d(dx);
+    else return x + dx;
 }
 
 // A value of the storage type T widened to double: float on the integer pipe

@@ -22,6 +22,37 @@ extern "C" int getm_launch_count(unsigned long long* count)
     return GETM_OK;
 }
 
+// Launch-shape knobs, per host thread (a thread that captures a domain's
+// graphs sets its own shapes without disturbing another thread's launches).
+static thread_local int g_tune[GETM_TUNE_NKNOBS] = {8, 32, 4, 0};
+
+static bool tune_valid(int knob, int v)
+{
+    switch (knob) {
+    case GETM_TUNE_XPASS_ROWS: return v == 2 || v == 4 || v == 8;
+    case GETM_TUNE_YMARCH_CHUNK: return v == 16 || v == 32 || v == 64;
+    case GETM_TUNE_COLUMN_ROWS: return v == 1 || v == 2 || v == 4;
+    case GETM_TUNE_SUBSTEP_BLOCKS: return v >= 0 && v <= 2;
+    default: return false;
+    }
+}
+
+int getm_tune(int knob) { return (knob >= 0 && knob < GETM_TUNE_NKNOBS) ? g_tune[knob] : 0; }
+
+extern "C" int getm_tune_set(int knob, int value)
+{
+    if (!tune_valid(knob, value)) return GETM_ERR_ARG;
+    g_tune[knob] = value;
+    return GETM_OK;
+}
+
+extern "C" int getm_tune_get(int knob, int* value)
+{
+    if (!value || knob < 0 || knob >= GETM_TUNE_NKNOBS) return GETM_ERR_ARG;
+    *value = g_tune[knob];
+    return GETM_OK;
+}
+
 // ---------------------------------------------------------------------------
 // interpolation.F90:9-72 (T: double for the FP64 form, float for the mixed form)
 // ---------------------------------------------------------------------------

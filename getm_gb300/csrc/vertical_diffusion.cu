@@ -31,9 +31,11 @@ struct getm_vertical_diffusion {
     double* auxn;
 };
 
-// T: type of the diffused fields, of nuh and of the solve (double: FP64 form;
-// float: mixed form).  Layer thicknesses are double in both forms.
-template <typename T>
+// T: type of nuh and of the solve (double: FP64 form; float: mixed form);
+// S: storage type of the diffused fields (T unless given; double with a
+// float solve: the mixed form with FP64 tracer storage, increment form).
+// Layer thicknesses are double in every form.
+template <typename T, typename S = T>
 struct VDArgs {
     int nx_, ny_, nz;
     long long plane;
@@ -46,7 +48,7 @@ struct VDArgs {
     double dt, cnpar;
     int ntracer;
     double molecular[VD_MAX_BATCH];
-    T* var[VD_MAX_BATCH];
+    S* var[VD_MAX_BATCH];
     const T* ea2[VD_MAX_BATCH];
     const T* ea4[VD_MAX_BATCH];
     T* work;               // NULL, or 2 nz plane elements: elimination coefficients in global memory
@@ -247,8 +249,8 @@ __global__ void __launch_bounds__(128, getm_increment_form<T> ? 8 : 1) vd_column
 // sweep together (work: 2 nz planes per field of a group).  SRC: whether a
 // field of the group has ea2 or ea4 (without, no registers are spent on
 // them).
-template <int NT, bool SRC>
-__device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c, int t0)
+template <int NT, bool SRC, typename S>
+__device__ __forceinline__ void vd_inc_sweep(const VDArgs<float, S>& a, long long c, int t0)
 {
     const long long P = a.plane;
     const int nz = a.nz;
@@ -257,7 +259,7 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c
     const float* __restrict__ nuh = a.nuh + c;
     const bool one_h = a.ho == a.hn;
     const float co = (float)(1.0 - a.cnpar), cn = (float)a.cnpar, dt2 = (float)(2.0 * a.dt);
-    float* v[NT];
+    S* v[NT];
     const float* e2[NT];
     const float* e4[NT];
     float* ru[NT];
@@ -277,7 +279,8 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c
     double ho_c = ho[k * P], hn_c = hn[k * P];
     double ho_n = ho[(k - 1) * P], hn_n = hn[(k - 1) * P];
     float nuh_c = nuh[k * P];  // interface below level k
-    float vk[NT], vn[NT], e2c[NT], e4c[NT];
+    S vk[NT], vn[NT];
+    float e2c[NT], e4c[NT];
 #pragma unroll
     for (int t = 0; t < NT; t++) {
         vk[t] = v[t][k * P];
@@ -287,14 +290,16 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c
     }
     float hoF = vd_h<float>(ho_c), hnF = vd_h<float>(hn_c);
     float dh = one_h ? 0.f : getm_d2f_approx(ho_c - hn_c);
-    float rk[NT], qk[NT], aoa[NT], ana[NT], vkp1[NT];
+    float rk[NT], qk[NT], aoa[NT], ana[NT];
+    S vkp1[NT];
     // surface layer (diffusion.F90:238-245) and the inner layers
     // (:247-258, elimination :287-290)
     for (; k >= 1; k--) {
         // next level's raw operands, one level ahead
         const int kn = k - 1;
         double ho_nn = 0.0, hn_nn = 0.0;
-        float nuh_n = 0.f, vnn[NT], e2n[NT], e4n[NT];
+        float nuh_n = 0.f, e2n[NT], e4n[NT];
+        S vnn[NT];
         if (kn >= 1) {
             ho_nn = ho[(kn - 1) * P];
             hn_nn = hn[(kn - 1) * P];
@@ -302,7 +307,7 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c
         nuh_n = nuh[kn * P];
 #pragma unroll
         for (int t = 0; t < NT; t++) {
-            vnn[t] = kn >= 1 ? v[t][(kn - 1) * P] : 0.f;
+            vnn[t] = kn >= 1 ? v[t][(kn - 1) * P] : S(0);
             e2n[t] = SRC && e2[t] ? e2[t][kn * P] : 0.f;
             e4n[t] = SRC && e4[t] ? e4[t][kn * P] : 0.f;
         }
@@ -315,15 +320,18 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c
             const float aob = co * x / so;
             const float anb = cn * x / sn;
             const float a1 = -anb;
+            // differences of neighbouring values in the storage type, then
+            // narrowed (exact for float storage)
+            const float xk = inc_f<S>(vk[t]);
             float a2, a4;
             if (k == nz - 1) {
                 a2 = hnF + anb;
-                a4 = vk[t] * dh + (vn[t] - vk[t]) * (aob + anb);
+                a4 = xk * dh + inc_f<S>(vn[t] - vk[t]) * (aob + anb);
             } else {
                 a2 = hnF + ana[t] + anb;
-                a4 = vk[t] * dh + (vkp1[t] - vk[t]) * (aoa[t] + ana[t]) + (vn[t] - vk[t]) * (aob + anb);
+                a4 = xk * dh + inc_f<S>(vkp1[t] - vk[t]) * (aoa[t] + ana[t]) + inc_f<S>(vn[t] - vk[t]) * (aob + anb);
             }
-            if (SRC && e2[t]) a4 = a4 + e2c[t] * vk[t];
+            if (SRC && e2[t]) a4 = a4 + e2c[t] * xk;
             if (SRC && e2[t]) a2 = a2 - e2c[t];
             if (SRC && e4[t]) a4 = a4 + e4c[t];
             if (k == nz - 1) {
@@ -348,50 +356,84 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float>& a, long long c
     }
     // bottom layer (:260-267, :291-292), back substitution (:304-307);
     // the old values of level k+1 are read before level k is written
-    float vprev[NT], xn[NT], rn[NT], qn[NT];
+    float vprev[NT], rn[NT], qn[NT];
+    S xn[NT];
 #pragma unroll
     for (int t = 0; t < NT; t++) {
         const float a3 = -ana[t];
+        const float xk = inc_f<S>(vk[t]);
         float a2 = hnF + ana[t];
-        float a4 = vk[t] * dh + (vkp1[t] - vk[t]) * (aoa[t] + ana[t]);
-        if (SRC && e2[t]) a4 = a4 + e2c[t] * vk[t];
+        float a4 = xk * dh + inc_f<S>(vkp1[t] - vk[t]) * (aoa[t] + ana[t]);
+        if (SRC && e2[t]) a4 = a4 + e2c[t] * xk;
         if (SRC && e2[t]) a2 = a2 - e2c[t];
         if (SRC && e4[t]) a4 = a4 + e4c[t];
         vprev[t] = (a4 - a3 * qk[t]) / (a2 - a3 * rk[t]);
         xn[t] = v[t][P];
         rn[t] = ru[t][P];
         qn[t] = qu[t][P];
-        v[t][0] = vk[t] + vprev[t];
+        v[t][0] = inc_add<S>(vk[t], vprev[t]);
     }
     for (k = 1; k < nz; k++) {
 #pragma unroll
         for (int t = 0; t < NT; t++) {
-            const float x_old = xn[t], r = rn[t], q = qn[t];
+            const S x_old = xn[t];
+            const float r = rn[t], q = qn[t];
             if (k + 1 < nz) {
                 xn[t] = v[t][(k + 1) * P];
                 rn[t] = ru[t][(k + 1) * P];
                 qn[t] = qu[t][(k + 1) * P];
             }
             vprev[t] = q - r * vprev[t];
-            v[t][k * P] = x_old + vprev[t];
+            v[t][k * P] = inc_add<S>(x_old, vprev[t]);
         }
     }
 }
 
-// PAIRS: fields in pairs (then an odd last one alone), else one at a time
-// block (32, 4): 32 columns of 4 rows
-template <bool SRC, bool PAIRS>
-__global__ void __launch_bounds__(128, 7) vd_inc_kernel(VDArgs<float> a)
+// PAIRS: fields in pairs (then an odd last one alone), else one at a time.
+// Blocks of 32 columns by GETM_TUNE_COLUMN_ROWS rows.  S: storage type of
+// the fields (float, or double for FP64 tracer storage).
+template <bool SRC, bool PAIRS, typename S = float>
+__global__ void __launch_bounds__(128, 7) vd_inc_kernel(VDArgs<float, S> a)
 {
     const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 4 + threadIdx.y;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= a.nx_ || j >= a.ny_) return;
     const long long c = (long long)j * a.nx_ + i;
+    if (a.nz == 1) {  // diffusion.F90:224-231: every point, mask not consulted
+        for (int t = 0; t < a.ntracer; t++) {
+            const S x = a.var[t][c];
+            const float xf = inc_f<S>(x);
+            float a2 = vd_h<float>(a.hn[c]);
+            float r = xf * vd_dh(a.ho, a.hn, c);
+            if (a.ea2[t]) { a2 = a2 - a.ea2[t][c]; r = r + a.ea2[t][c] * xf; }
+            if (a.ea4[t]) r = r + a.ea4[t][c];
+            a.var[t][c] = inc_add<S>(x, r / a2);
+        }
+        return;
+    }
     if (a.mask[c] != 1) return;
     int t0 = 0;
     if constexpr (PAIRS)
-        for (; t0 + 2 <= a.ntracer; t0 += 2) vd_inc_sweep<2, SRC>(a, c, t0);
-    for (; t0 < a.ntracer; t0++) vd_inc_sweep<1, SRC>(a, c, t0);
+        for (; t0 + 2 <= a.ntracer; t0 += 2) vd_inc_sweep<2, SRC, S>(a, c, t0);
+    for (; t0 < a.ntracer; t0++) vd_inc_sweep<1, SRC, S>(a, c, t0);
+}
+
+// The increment-form solve for FP64-stored fields (float solve, nuh and
+// sources; work: 2 nz planes of floats per field of a pair).
+static int vd_launch_f64s(VDArgs<float, double>& a, cudaStream_t stream)
+{
+    if (!a.work) return GETM_ERR_ARG;
+    const int rows = getm_tune(GETM_TUNE_COLUMN_ROWS);
+    const dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, rows)), block(32, rows);
+    bool src = false;
+    for (int t = 0; t < a.ntracer; t++) src = src || a.ea2[t] || a.ea4[t];
+    const bool pairs = a.ntracer > 1;
+    if (src && pairs) vd_inc_kernel<true, true, double><<<grid, block, 0, stream>>>(a);
+    else if (src) vd_inc_kernel<true, false, double><<<grid, block, 0, stream>>>(a);
+    else if (pairs) vd_inc_kernel<false, true, double><<<grid, block, 0, stream>>>(a);
+    else vd_inc_kernel<false, false, double><<<grid, block, 0, stream>>>(a);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 // prepare as a separate call (diffusion.F90:163-171): auxo/auxn at every
@@ -417,7 +459,8 @@ static int vd_launch(VDArgs<T>& a, cudaStream_t stream)
         dim3 grid(getm_div_up(a.nx_, 128), a.ny_);
         if constexpr (getm_increment_form<T>) {
             if (a.nz > 1 && !a.auxo) {
-                const dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, 4)), block(32, 4);
+                const int rows = getm_tune(GETM_TUNE_COLUMN_ROWS);
+                const dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, rows)), block(32, rows);
                 bool src = false;
                 for (int t = 0; t < a.ntracer; t++) src = src || a.ea2[t] || a.ea4[t];
                 const bool pairs = a.ntracer > 1;
@@ -509,15 +552,15 @@ extern "C" int getm_vertical_diffusion_apply(getm_vertical_diffusion* d, int nx,
     return vd_launch(a, stream);
 }
 
-template <typename T>
+template <typename T, typename S = T>
 static int vd_batch_impl(int nx, int ny, int nz, const int* mask, const T* nuh, double timestep, double cnpar,
                          const double* ho, const double* hn, int ntracer, const double* molecular,
-                         T* const* vars, const T* const* ea2, const T* const* ea4, T* work, cudaStream_t stream)
+                         S* const* vars, const T* const* ea2, const T* const* ea4, T* work, cudaStream_t stream)
 {
     if (nx < 1 || ny < 1 || nz < 1 || !mask || !nuh || !ho || !hn || ntracer < 1 || !vars || !molecular)
         return GETM_ERR_ARG;
     if (nz > GETM_MAX_NZ) return GETM_ERR_NZ;
-    VDArgs<T> a;
+    VDArgs<T, S> a;
     memset(&a, 0, sizeof(a));
     a.nx_ = nx; a.ny_ = ny; a.nz = nz; a.plane = (long long)nx * ny;
     a.mask = mask; a.nuh = nuh; a.ho = ho; a.hn = hn; a.dt = timestep; a.cnpar = cnpar;
@@ -533,7 +576,9 @@ static int vd_batch_impl(int nx, int ny, int nz, const int* mask, const T* nuh, 
             a.ea2[t] = ea2 ? ea2[done + t] : NULL;
             a.ea4[t] = ea4 ? ea4[done + t] : NULL;
         }
-        int rc = vd_launch<T>(a, stream);
+        int rc;
+        if constexpr (std::is_same<T, S>::value) rc = vd_launch<T>(a, stream);
+        else rc = vd_launch_f64s(a, stream);
         if (rc) return rc;
         done += n;
     } while (done < ntracer);
@@ -559,4 +604,14 @@ extern "C" int getm_vertical_diffusion_batch_f32(int nx, int ny, int nz, const i
 {
     return vd_batch_impl<float>(nx, ny, nz, mask, nuh, timestep, cnpar, ho, hn, ntracer, molecular, vars, ea2, ea4,
                                 work, stream);
+}
+
+extern "C" int getm_vertical_diffusion_batch_f64s(int nx, int ny, int nz, const int* mask, const float* nuh,
+                                                  double timestep, double cnpar, const double* ho,
+                                                  const double* hn, int ntracer, const double* molecular,
+                                                  double* const* vars, const float* const* ea2,
+                                                  const float* const* ea4, float* work, cudaStream_t stream)
+{
+    return vd_batch_impl<float, double>(nx, ny, nz, mask, nuh, timestep, cnpar, ho, hn, ntracer, molecular, vars,
+                                        ea2, ea4, work, stream);
 }

@@ -21,16 +21,17 @@ from .workloads import Workload
 
 
 def make_member(wl: Workload, precision: str = "mixed", device="cuda", substep_kernel: bool = False,
-                concurrent_3d: bool = True) -> Simulation:
+                concurrent_3d: bool = True, tiles=None) -> Simulation:
     """Build and start a simulation for one ensemble member (rest state,
     linear temperature drop ``dT`` per 100 m from 20 degC at the surface).
     Members replay concurrently on several streams, so by default their 2D
     substeps run as separate kernels rather than as one cooperative launch
-    that needs every SM of the GPU at once."""
+    that needs every SM of the GPU at once.  ``tiles``: launch shapes
+    (``Simulation``), e.g. "auto" for the tuned shapes of the member's size."""
     p = wl.params
     sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device,
                      airsea=Fluxes(taux=p.get("taux", 0.0)), substep_kernel=substep_kernel,
-                     concurrent_3d=concurrent_3d)
+                     concurrent_3d=concurrent_3d, tiles=tiles)
     zc = sim.T.zc.all_values
     dT = p.get("dT", 10.0)
     temp0 = torch.where(sim.T.mask.all_values[None] != 0, 20.0 + dT * zc / 100.0, sim.temp.all_values.double())
@@ -58,10 +59,12 @@ class DomainRunner:
         for _ in range(self.sim.split_factor):
             self.sim.advance()
 
-    def prepare(self, capture_stream: Optional[torch.cuda.Stream] = None):
+    def prepare(self, capture_stream: Optional[torch.cuda.Stream] = None, capture_error_mode: str = "global"):
         """Run the eager warm-up steps (allocating every work buffer) and
-        record the two step graphs.  Call on an idle device section: capture
-        requires that no other thread launches work meanwhile."""
+        record the two step graphs.  ``capture_error_mode="thread_local"``
+        lets other host threads keep launching work (graph replays, event
+        queries) while this one captures; with "global" no other thread may
+        make CUDA calls during the capture."""
         for _ in range(self._warmup):
             self._eager_step()
         self.steps_done = self._warmup
@@ -74,7 +77,7 @@ class DomainRunner:
         for _ in range(2):
             g = torch.cuda.CUDAGraph()
             with torch.cuda.stream(stream):
-                with torch.cuda.graph(g, stream=stream):
+                with torch.cuda.graph(g, stream=stream, capture_error_mode=capture_error_mode):
                     self._eager_step()
             graphs.append(g)
         torch.cuda.current_stream(dev).wait_stream(stream)
@@ -134,3 +137,153 @@ class Ensemble:
                     events[n].record(s)
         for s in self.lanes:
             main.wait_stream(s)
+
+
+class BatchedEnsemble:
+    """Advance many members together with the 2D substeps of all members in
+    one persistent kernel: per 3D step (a "round"), one cooperative launch
+    per substep index k advances every member with more than k substeps left
+    before its 3D step (``getm_substep_batch_launch``), then every member's
+    last substep and its 3D step run on one of ``lanes`` streams.  Members
+    may differ in size and in their number of substeps.  Each round is
+    replayed from CUDA graphs: one graph of the batched launches per parity
+    of the round, and one graph of each member's 3D substep per parity.
+
+    Members must be built with ``substep_kernel=True`` (each then carries the
+    fields of the one-launch substep) and share one precision form; their
+    results are bitwise those of advancing each alone."""
+
+    def __init__(self, members: List[Simulation], lanes: int = 16, warmup_rounds: int = 2, device="cuda"):
+        import ctypes
+
+        from ._lib import call
+
+        self.device = torch.device(device)
+        self.members = list(members)
+        if not self.members:
+            raise ValueError("empty ensemble")
+        forms = {m.precision for m in self.members}
+        if len(forms) != 1:
+            raise ValueError(f"members of one precision form only, not {sorted(forms)}")
+        for m in self.members:
+            if m._split2d is None:
+                raise ValueError("every member needs the one-launch substep (substep_kernel=True and a "
+                                 "configuration it covers)")
+        self.mixed = forms.pop() == "mixed"
+        self.lanes = [torch.cuda.Stream(device=self.device) for _ in range(max(1, min(lanes, len(self.members))))]
+        self.sync = torch.zeros(4, dtype=torch.int32, device=self.device)
+        h = ctypes.c_void_p()
+        call("getm_substep_batch_create", len(self.members), int(self.mixed), ctypes.byref(h))
+        self._h = h
+        self._warmup = warmup_rounds + warmup_rounds % 2
+        self.rounds_done = 0
+        self.graphs = None
+        self.nsub = [m.split_factor - 1 for m in self.members]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            from ._lib import release
+
+            try:
+                release("getm_substep_batch_finalize", h)
+            except Exception:
+                pass
+
+    @property
+    def cells(self) -> int:
+        return sum(m.T.nx * m.T.ny * m.T.nz for m in self.members)
+
+    def status(self) -> int:
+        """Non-zero when a grid barrier of the batched substep gave up."""
+        return int(self.sync[2].item())
+
+    def _register(self):
+        """The members' fields and orders at the start of an even round."""
+        import ctypes
+
+        from ._lib import call
+
+        for q, s in enumerate(self.members):
+            T, U, V, m = s.T, s.U, s.V, s.momentum
+            call("getm_substep_batch_set", self._h, q, self.nsub[q], s.split_factor, ctypes.byref(s._split2d.fields),
+                 T.nx_, T.ny_, T.halox, T.haloy, int(bool(m._ufirst)), 1, int(bool(m.apply_bottom_friction)),
+                 float(s.timestep), float(s.Dmin), float(s.Dcrit),
+                 m.uadv.p, U.handle, U.ugrid.handle, U.vgrid.handle, int(m.uadv.ufirst),
+                 m.vadv.p, V.handle, V.ugrid.handle, V.vgrid.handle, int(m.vadv.ufirst))
+        call("getm_substep_batch_upload", self._h)
+
+    def _batched_substeps(self, round_parity: int):
+        """The launches of one round, with the members' host-side counters
+        moved on as advance() would."""
+        from ._lib import call
+
+        for k in range(max(self.nsub)):
+            call("getm_substep_batch_launch", self._h, k, round_parity, self.sync.data_ptr(),
+                 torch.cuda.current_stream(self.device).cuda_stream)
+        for s, n in zip(self.members, self.nsub):
+            s.istep += n
+            if n % 2:
+                s.momentum._ufirst = not s.momentum._ufirst
+
+    def _macro(self, main, events=None):
+        """Every member's last substep (with its 3D step) on the lanes."""
+        for st in self.lanes:
+            st.wait_stream(main)
+        for q, s in enumerate(self.members):
+            st = self.lanes[q % len(self.lanes)]
+            with torch.cuda.stream(st):
+                s.advance()
+                if events is not None:
+                    events[q].record(st)
+        for st in self.lanes:
+            main.wait_stream(st)
+
+    def prepare(self):
+        """Warm-up rounds member by member (allocating every work buffer),
+        the device table, and the round graphs (one per round parity)."""
+        for s in self.members:
+            for _ in range(self._warmup * s.split_factor):
+                s.advance()
+        torch.cuda.synchronize(self.device)
+        self._register()
+        self.rounds_done = 0
+        main = torch.cuda.Stream(device=self.device)
+        main.wait_stream(torch.cuda.current_stream(self.device))
+        self.graphs = []
+        with torch.cuda.stream(main):
+            for r in range(2):
+                gb = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(gb, stream=main):
+                    self._batched_substeps(r)
+                gm = []
+                for s in self.members:
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g, stream=main):
+                        s.advance()
+                    gm.append(g)
+                self.graphs.append((gb, gm))
+        torch.cuda.current_stream(self.device).wait_stream(main)
+        torch.cuda.synchronize(self.device)
+
+    def step(self, events: Optional[List[torch.cuda.Event]] = None):
+        """One round: every member advances by one 3D step.  ``events``: one
+        per member, recorded after its 3D step."""
+        main = torch.cuda.current_stream(self.device)
+        if self.graphs is None:
+            self._batched_substeps(self.rounds_done % 2)
+            self._macro(main, events)
+        else:
+            gb, gm = self.graphs[self.rounds_done % 2]
+            gb.replay()
+            for st in self.lanes:
+                st.wait_stream(main)
+            for q, g in enumerate(gm):
+                st = self.lanes[q % len(self.lanes)]
+                with torch.cuda.stream(st):
+                    g.replay()
+                    if events is not None:
+                        events[q].record(st)
+            for st in self.lanes:
+                main.wait_stream(st)
+        self.rounds_done += 1

@@ -18,7 +18,7 @@ import torch
 
 from . import _lib
 from ._lib import call
-from .core import CENTERS, INTERFACES, Array, Grid, _sfx
+from .core import CENTERS, INTERFACES, Array, Grid, _sfx, _sfx_storage  # noqa: F401
 
 
 class AdvectionScheme(enum.IntEnum):
@@ -175,7 +175,8 @@ class Advection:
         self.h.copy_((self.grid.hn if new_h else self.grid.ho).all_values)
         wv = _lib.ptr_array([_p(x) for x in w_vars])
         vv = _lib.ptr_array([_p(x) for x in vars])
-        sfx = _sfx(*([u.all_values, v.all_values, w.all_values] + [x.all_values for x in list(w_vars) + list(vars)]))
+        sfx = _sfx_storage([u.all_values, v.all_values, w.all_values] + [x.all_values for x in w_vars],
+                           [x.all_values for x in vars])
         call("getm_advection_apply_3d_batch" + sfx, self.p, self.grid.handle, self.ugrid.handle, self.vgrid.handle,
              int(self._ufirst), _p(u), _p(v), _p(w), wv, _p(Ah_u), _p(Ah_v), float(timestep), self.h.data_ptr(),
              _p(self.ugrid.hn), _p(self.vgrid.hn), len(vars), vv, _s())
@@ -260,10 +261,11 @@ class VerticalDiffusion:
         vv = _lib.ptr_array([_p(v) for v in vars])
         e2 = _lib.ptr_array([_p(e) for e in ea2s]) if ea2s is not None and any(e is not None for e in ea2s) else None
         e4 = _lib.ptr_array([_p(e) for e in ea4s]) if ea4s is not None and any(e is not None for e in ea4s) else None
-        sfx = _sfx(nuh.all_values, *[v.all_values for v in vars])
+        sfx = _sfx_storage([nuh.all_values], [v.all_values for v in vars])
         # elimination coefficients of the column solves (2 nz planes per field
-        # solved at once, reused; the float solve takes its fields in pairs)
-        dt = vars[0].all_values.dtype
+        # solved at once, reused; the float solve takes its fields in pairs),
+        # in the solve's type (that of nuh)
+        dt = nuh.all_values.dtype
         need = 2 * (2 if n > 1 and dt == torch.float32 else 1) * g.nz_ * g.ny_ * g.nx_
         w = self._work.get(dt)
         if w is None or w.numel() < need:

@@ -10,6 +10,12 @@ their work overlaps on the device.  A finished request leaves the mix and
 its memory returns to the budget.  Its state stays resident in HBM for its
 whole life.
 
+Admission runs on a worker thread with its own stream: building a domain,
+its eager warm-up steps and the capture of its step graphs (in thread-local
+capture mode) overlap with the main loop, which only decides admissions,
+issues graph replays and polls completions, so issuing the steps of running
+requests never waits for a request being set up.
+
 Every step's completion is timed on the device (a CUDA event per step,
 measured against a start event), which gives the per-step latency: the time
 between consecutive completed 3D steps of a request.
@@ -77,7 +83,10 @@ class Server:
     STATE_FIELDS = ("temp", "salt")
 
     def __init__(self, budget_bytes: float = 150 * GB, lanes: int = 16, max_inflight: int = 3,
-                 device="cuda", keep=()):
+                 device="cuda", keep=(), admission_thread: bool = True, max_building: int = 2):
+        """``admission_thread``: set requests up on a worker thread (False:
+        in the main loop, between step issues); ``max_building``: requests
+        handed to the worker and not yet ready."""
         self.device = torch.device(device)
         self.budget = float(budget_bytes)
         self.lanes = [torch.cuda.Stream(device=self.device) for _ in range(lanes)]
@@ -88,7 +97,11 @@ class Server:
         self.used = 0.0
         self.peak_used = 0.0
         self._capture_stream = torch.cuda.Stream(device=self.device)
+        self._build_stream = torch.cuda.Stream(device=self.device)
         self._lane_next = 0
+        self.admission_thread = admission_thread
+        self.max_building = max(1, max_building)
+        self.admission_host_s: List[float] = []
 
     def estimate(self, req: Request) -> float:
         bpc = self.bytes_per_cell.get(req.precision, self.default_bytes_per_cell)
@@ -108,12 +121,13 @@ class Server:
             total += s.nbytes()
         return total
 
-    def _admit(self, req: Request, wl: Workload, t_run: float, start: torch.cuda.Event) -> _Active:
+    def _admit(self, req: Request, wl: Workload, t_run: float, start: torch.cuda.Event,
+               capture_error_mode: str = "global") -> _Active:
         sim = make_member(wl, req.precision, device=self.device)
         runner = DomainRunner(sim)
         res = Result(req.rid, runner.cells, req.nsteps, req.arrival, admitted=t_run)
         # warm-up steps run eagerly inside prepare(); time them as one block
-        runner.prepare(self._capture_stream)
+        runner.prepare(self._capture_stream, capture_error_mode)
         ev = torch.cuda.Event(enable_timing=True)
         ev.record()
         ev.synchronize()
@@ -130,16 +144,37 @@ class Server:
         a.result = res
         return a
 
+    def _worker(self, inbox: "queue.Queue", ready: "queue.Queue", start: torch.cuda.Event, t0: float):
+        """Admission worker: build, warm up and capture each handed request
+        on the worker's own stream; hand the result (or the exception) back."""
+        while True:
+            item = inbox.get()
+            if item is None:
+                return
+            req, fut, t_adm = item
+            try:
+                wl = fut.result() if fut is not None else req.make_workload()
+                ta = time.perf_counter()
+                with torch.cuda.stream(self._build_stream):
+                    a = self._admit(req, wl, t_adm, start, capture_error_mode="thread_local")
+                self.admission_host_s.append(time.perf_counter() - ta)
+                ready.put(a)
+            except BaseException as e:  # surfaced by the main loop
+                ready.put(e)
+
     def run(self, requests: List[Request], duration: float, admit_until: Optional[float] = None,
             poll_sleep: float = 0.0) -> List[Result]:
         """Serve ``requests`` until all admitted ones are done or ``duration``
         seconds have passed (unfinished work is then abandoned; its completed
         steps still count).  Requests are admitted until ``admit_until``
-        seconds (default: ``duration``).  At most one request is admitted
-        per pass of the loop, so the steps of the running requests keep
-        being issued while new ones are set up.  Workloads of the next
-        arrivals are generated on a host thread ahead of their admission.
-        Returns one Result per admitted request."""
+        seconds (default: ``duration``).  Workloads of the next arrivals are
+        generated on a host thread ahead of their admission; with
+        ``admission_thread`` the set-up runs on a worker thread, otherwise at
+        most one request is set up per pass of the loop.  Returns one Result
+        per admitted request."""
+        import queue
+        import sys
+        import threading
         from concurrent.futures import ThreadPoolExecutor
 
         admit_until = duration if admit_until is None else admit_until
@@ -159,26 +194,54 @@ class Server:
         start.record()
         t0 = time.perf_counter()
         self.admission_host_s = []
+        inbox: "queue.Queue" = queue.Queue()
+        ready: "queue.Queue" = queue.Queue()
+        reserved: Dict[int, float] = {}
+        worker = None
+        switch = sys.getswitchinterval()
+        if self.admission_thread:
+            # the main loop's short bursts of step issue should not wait a
+            # whole default switch interval behind the worker's set-up
+            sys.setswitchinterval(5e-4)
+            worker = threading.Thread(target=self._worker, args=(inbox, ready, start, t0), daemon=True)
+            worker.start()
+
+        def take(a: _Active):
+            self.used += a.estimate - reserved.pop(a.req.rid, 0.0)
+            self.peak_used = max(self.peak_used, self.used)
+            active.append(a)
+            results.append(a.result)
+
         try:
             while True:
                 now = time.perf_counter() - t0
                 if now > duration:
                     break
                 prefetch_ahead()
+                # requests the worker finished setting up join the mix
+                while not ready.empty():
+                    a = ready.get_nowait()
+                    if isinstance(a, BaseException):
+                        raise a
+                    take(a)
                 # admission: first come, first served, while the budget allows
-                if pending and pending[0].arrival <= now and now <= admit_until:
+                if pending and pending[0].arrival <= now and now <= admit_until and len(reserved) < (
+                        self.max_building if worker is not None else 1):
                     est = self.estimate(pending[0])
-                    if self.used + est <= self.budget or not active:
+                    if self.used + est <= self.budget or (not active and not reserved):
                         req = pending.pop(0)
                         fut = futures.pop(req.rid, None)
-                        wl = fut.result() if fut is not None else req.make_workload()
-                        ta = time.perf_counter()
-                        a = self._admit(req, wl, ta - t0, start)
-                        self.admission_host_s.append(time.perf_counter() - ta)
-                        self.used += a.estimate
+                        reserved[req.rid] = est
+                        self.used += est
                         self.peak_used = max(self.peak_used, self.used)
-                        active.append(a)
-                        results.append(a.result)
+                        if worker is not None:
+                            inbox.put((req, fut, now))
+                        else:
+                            wl = fut.result() if fut is not None else req.make_workload()
+                            ta = time.perf_counter()
+                            a = self._admit(req, wl, ta - t0, start)
+                            self.admission_host_s.append(time.perf_counter() - ta)
+                            take(a)
                 # completion of issued steps, then issue the next ones
                 progressed = False
                 for a in active:
@@ -209,11 +272,19 @@ class Server:
                     else:
                         keep_active.append(a)
                 active = keep_active
-                if not active and (not pending or now > admit_until):
+                if not active and not reserved and (not pending or now > admit_until):
                     break
                 if not progressed and poll_sleep > 0:
                     time.sleep(poll_sleep)
         finally:
+            if worker is not None:
+                inbox.put(None)
+                worker.join()
+                sys.setswitchinterval(switch)
+                while not ready.empty():  # set up but never joined the mix
+                    a = ready.get_nowait()
+                    if not isinstance(a, BaseException):
+                        a.runner = None
             prefetch.shutdown(wait=True, cancel_futures=True)
         torch.cuda.synchronize(self.device)
         for a in active:  # abandoned at the deadline: count what completed

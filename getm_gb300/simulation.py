@@ -110,7 +110,7 @@ class Simulation:
                  airsea: Optional[Fluxes] = None, internal_pressure: str = "shchepetkin_mcwilliams",
                  Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
                  nuh: float = 0.0, precision: str = "fp64", fused_2d: bool = True, substep_kernel: bool = True,
-                 concurrent_3d: bool = True, device="cuda"):
+                 concurrent_3d: bool = True, tiles=None, tracer_storage: Optional[str] = None, device="cuda"):
         """``precision``: "fp64" (the plain form) or "mixed" (float32 tracers,
         3D velocities and their tendencies and diffusivities; float64
         elevations, depths, layer thicknesses, 2D transports and their
@@ -128,7 +128,17 @@ class Simulation:
         (neither reads what the other writes; the streams join before the
         2D depth update), and the advection of the V momentum on a third,
         beside that of the U momentum; the squared buoyancy frequency joins
-        the second stream once the density is known."""
+        the second stream once the density is known.  ``tiles``: launch
+        shapes of the hot kernels (``autotune``): a dict of knob values,
+        "auto" for the tuned shapes of this domain's size bucket, or None to
+        leave the calling thread's shapes as they are; applied on every
+        ``advance`` (and so captured into the step's CUDA graphs).
+        ``tracer_storage`` (mixed form): "float64" (the default) keeps the
+        tracers (and the buoyancy frequency computed from them) in FP64
+        while their advection and diffusion increments, fluxes, limiters and
+        solves stay float: float32 rounding of the stored tracers would
+        otherwise perturb the density, and through it the flow, by up to half
+        an ulp of the tracer every step; "float32" stores them in float."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
@@ -139,6 +149,13 @@ class Simulation:
         self._forked = False
         d3 = torch.float32 if precision == "mixed" else torch.float64
         self.dtype3d = d3
+        if tracer_storage is None:
+            tracer_storage = "float64"
+        if tracer_storage not in ("float64", "float32"):
+            raise ValueError(f"tracer_storage must be 'float64' or 'float32', not {tracer_storage!r}")
+        self.tracer_storage = tracer_storage
+        dtr = torch.float64 if precision == "fp64" or tracer_storage == "float64" else torch.float32
+        self.dtype_tracer = dtr
         if Dmin <= 0.0:
             raise Exception("Dmin<=0")
         if Dcrit < 2.5 * Dmin:
@@ -147,6 +164,11 @@ class Simulation:
         self.dga = torch.as_tensor(dga, dtype=torch.float64, device=device)[:, None, None]
         self.T = T = make_grids(T_host, device)
         self.U, self.V, self.X = T.ugrid, T.vgrid, T.xgrid
+        if tiles == "auto":
+            from . import autotune
+
+            tiles = autotune.lookup(T.nx, T.ny, T.nz, precision)
+        self.tiles = tiles
         self.Dmin, self.Dcrit = Dmin, Dcrit
         self.delay_slow_ip = delay_slow_ip
         three_d = self.runtype > RunType.BAROTROPIC_2D
@@ -181,7 +203,7 @@ class Simulation:
         self.tausy = self.V.array(name="tausyv")
         self.fwf = T.array(name="fwf")
         self.fwf.fill(0.0)
-        self.tracers = TracerCollection(T, advection_scheme, dtype=d3)
+        self.tracers = TracerCollection(T, advection_scheme, dtype=dtr)
         if three_d:
             self.num = T.array(z=INTERFACES, name="num", dtype=d3)
             self.nuh = T.array(z=INTERFACES, name="nuh", dtype=d3)
@@ -202,7 +224,7 @@ class Simulation:
             self.rho = T.array(z=CENTERS, name="rho")
             self.buoy = T.array(z=CENTERS, name="buoy")
             # squared buoyancy frequency (simulation.py:757-767, :1200-1204)
-            self.NN = T.array(z=INTERFACES, name="NN", dtype=d3)
+            self.NN = T.array(z=INTERFACES, name="NN", dtype=dtr)
             self.NN.fill(0.0)
             self.internal_pressure_method = internal_pressure
         if three_d:
@@ -234,6 +256,10 @@ class Simulation:
 
     def advance(self):
         """python/pygetm/simulation.py:291-325"""
+        if self.tiles is not None:
+            from . import autotune
+
+            autotune.apply(self.tiles)
         self.istep += 1
         macro_active = self.istep % self.split_factor == 0
         if self._split2d is not None and not macro_active:

@@ -37,7 +37,8 @@ class TracerCollection:
 
     def __init__(self, grid: Grid, advection_scheme: AdvectionScheme = AdvectionScheme.DEFAULT, cnpar: float = 1.0,
                  dtype: torch.dtype = torch.float64):
-        """``dtype``: float64 (FP64 form) or float32 (mixed form) tracers."""
+        """``dtype``: storage of the tracers: float64 (FP64 form, and the mixed
+        form's FP64 tracer storage) or float32 (mixed form)."""
         self.grid = grid
         self.dtype = dtype
         self._tracers: List[Tracer] = []
@@ -74,7 +75,8 @@ class TracerCollection:
         ea4s = []
         for tracer in self._tracers:
             if tracer.source is not None or tracer.surface_flux is not None:
-                src = torch.zeros_like(tracer.all_values)
+                # in the solve's type (that of the diffusivity)
+                src = torch.zeros_like(tracer.all_values, dtype=diffusivity.all_values.dtype)
                 if tracer.source is not None:
                     src.copy_(tracer.source.all_values)
                 if tracer.surface_flux is not None:

@@ -273,6 +273,25 @@ int getm_shchepetkin_mcwilliams(int nx, int ny, int nz, int imin, int imax, int 
  * counted once, at capture).                                                */
 int getm_launch_count(unsigned long long* count);
 
+/* ---- launch-shape knobs (the autotuner's search space) -----------------
+ * No counterpart in the reference.  Launch shapes of the hot kernels, read
+ * on the calling host thread at every launch (a CUDA graph keeps the shapes
+ * it was captured with).  The table is per host thread and starts at the
+ * defaults; a value outside the knob's set returns GETM_ERR_ARG.
+ *   GETM_TUNE_XPASS_ROWS      rows (warps) per block of the x pass: 2, 4, 8 (default 8)
+ *   GETM_TUNE_YMARCH_CHUNK    rows a warp marches in the 3D y pass: 16, 32, 64 (default 32)
+ *   GETM_TUNE_COLUMN_ROWS     rows of 32 columns per block of the w pass and
+ *                             the float column solve: 1, 2, 4 (default 4)
+ *   GETM_TUNE_SUBSTEP_BLOCKS  blocks per SM of the one-launch 2D substep:
+ *                             0 = as many as fit (default), 1, 2 (capped at what fits) */
+#define GETM_TUNE_XPASS_ROWS 0
+#define GETM_TUNE_YMARCH_CHUNK 1
+#define GETM_TUNE_COLUMN_ROWS 2
+#define GETM_TUNE_SUBSTEP_BLOCKS 3
+#define GETM_TUNE_NKNOBS 4
+int getm_tune_set(int knob, int value);
+int getm_tune_get(int knob, int* value);
+
 /* ---- equation of state --------------------------------------------------
  * No counterpart in the reference's Fortran: pygetm takes density from the
  * external TEOS-10 package pygsw (python/pygetm/density.py:62-95).  This
@@ -306,6 +325,28 @@ int getm_vertical_diffusion_batch_f32(int nx, int ny, int nz, const int* mask, c
                                       const double* hn, int ntracer, const double* molecular,
                                       float* const* vars, const float* const* ea2,
                                       const float* const* ea4, float* work, cudaStream_t stream);
+/* The mixed form with FP64 tracer storage: fields (tracers) double, every
+ * other operand as in the _f32 entries (float velocities, w, nuh, sources
+ * and work); the increments, fluxes, limiters and the solve are float, the
+ * differences of neighbouring values are formed in FP64 before they are
+ * narrowed, and each field is updated in FP64 (value + float increment).
+ * Same arguments as getm_advection_apply_3d_batch_f32 and
+ * getm_vertical_diffusion_batch_f32 otherwise.                             */
+int getm_advection_apply_3d_batch_f64s(getm_advection* adv, getm_grid* tgrid, getm_grid* ugrid,
+                                       getm_grid* vgrid, int ufirst, const float* u, const float* v,
+                                       const float* w, const float* const* w_var, const double* Ah_u,
+                                       const double* Ah_v, double timestep, double* h,
+                                       const double* hu, const double* hv, int ntracer,
+                                       double* const* vars, cudaStream_t stream);
+int getm_advection_uv_pass_f64s(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
+                                getm_grid* ugrid, const float* u, const double* Ah, double timestep,
+                                const double* h_in, double* h_out, const double* hu, int ntracer,
+                                const double* const* var_in, double* const* var_out, cudaStream_t stream);
+int getm_vertical_diffusion_batch_f64s(int nx, int ny, int nz, const int* mask, const float* nuh,
+                                       double timestep, double cnpar, const double* ho,
+                                       const double* hn, int ntracer, const double* molecular,
+                                       double* const* vars, const float* const* ea2,
+                                       const float* const* ea4, float* work, cudaStream_t stream);
 int getm_grid_interp_x_f32(int nx, int ny, int nz, const float* source, float* target, int ioffset,
                            cudaStream_t stream);
 int getm_grid_interp_y_f32(int nx, int ny, int nz, const float* source, float* target, int joffset,
@@ -621,6 +662,40 @@ int getm_split2d_substep(const getm_split2d_fields* f, int nx, int ny, int halox
                          getm_advection* uadv, getm_grid* ugrid, getm_grid* uugrid, getm_grid* uvgrid,
                          int uadv_ufirst, getm_advection* vadv, getm_grid* vgrid, getm_grid* vugrid,
                          getm_grid* vvgrid, int vadv_ufirst, cudaStream_t stream);
+
+/* ---- substeps of many domains in one launch ------------------------------
+ * No single counterpart in the reference, which advances each domain in its
+ * own process: for an ensemble of independent domains (each one
+ * Simulation.advance substep sequence, python/pygetm/simulation.py:291-325),
+ * the substeps that are not followed by a 3D step run for all members
+ * together, one cooperative launch per substep index k, with the operations
+ * and results of getm_split2d_substep per member.
+ *   create(nmember, mixed): a table for nmember domains of one form;
+ *   set(member, nsub, split, <getm_split2d_substep's arguments>): member's
+ *     fields at the start of a round of `split` substeps, nsub of which (the
+ *     ones without 3D step, split - 1 in a split-explicit run) run here; its
+ *     transport order `ufirst` is the order of its first substep in a round
+ *     of even parity;
+ *   upload(b): builds the device table (cudaMalloc and synchronous copies:
+ *     call before any stream capture; set() is closed afterwards);
+ *   launch(b, k, round_parity, sync): substep k of the round for every member
+ *     with nsub > k (round_parity: the round's index mod 2; a member's order
+ *     then is its recorded order flipped k + round_parity * split times);
+ *     sync: 4 zeroed barrier words owned by the caller, as for
+ *     getm_split2d_substep (its bounded waits and error word).
+ *   participants(b, k, count): members that take part in launch k.          */
+typedef struct getm_substep_batch getm_substep_batch;
+int getm_substep_batch_create(int nmember, int mixed, getm_substep_batch** out);
+int getm_substep_batch_set(getm_substep_batch* b, int member, int nsub, int split, const getm_split2d_fields* f,
+                           int nx, int ny, int halox, int haloy, int ufirst, int accumulate, int friction,
+                           double timestep, double Dmin, double Dcrit, getm_advection* uadv, getm_grid* ugrid,
+                           getm_grid* uugrid, getm_grid* uvgrid, int uadv_ufirst, getm_advection* vadv,
+                           getm_grid* vgrid, getm_grid* vugrid, getm_grid* vvgrid, int vadv_ufirst);
+int getm_substep_batch_upload(getm_substep_batch* b);
+int getm_substep_batch_participants(const getm_substep_batch* b, int k, int* count);
+int getm_substep_batch_launch(getm_substep_batch* b, int k, int round_parity, unsigned int* sync,
+                              cudaStream_t stream);
+int getm_substep_batch_finalize(getm_substep_batch* b);
 
 /* ---- domain totals (compensated budget sums) -----------------------------
  * Replaces python/pygetm/simulation.py:1409-1444 (Simulation.totals: total

@@ -80,6 +80,119 @@ def test_vertical_diffusion_f32():
     assert rel(host(td.all_values), to, Th.mask == 1) < 2e-6
 
 
+@pytest.mark.parametrize("scheme", [1, 5, 6])
+def test_apply_3d_batch_f64s(scheme):
+    """FP64-stored tracers with float velocities and float increments
+    (getm_advection_apply_3d_batch_f64s): fields of a large mean plus a small
+    signal, where float32 storage could not even hold the change; the change
+    matches the FP64 oracle to float32 accuracy (1e-5 of its largest value;
+    HSIMT 2e-5), the thicknesses to 1e-6."""
+    import oracle.oracle as O
+    from getm_gb300 import operators
+    from getm_gb300.core import Array, CENTERS, INTERFACES
+
+    Th, To, Td, rng = setup(seed=80 + scheme)
+    nz = Th.nz
+    u = velocity(Th.ugrid, rng, nz, 0.3)
+    v = velocity(Th.vgrid, rng, nz, 0.3)
+    w = rng.uniform(-5e-4, 5e-4, (nz + 1, Th.ny_, Th.nx_))
+    w[0] = w[-1] = 0.0
+    u, v, w = (x.astype(np.float32).astype(np.float64) for x in (u, v, w))
+    tr = [1000.0 + rng.uniform(0.0, 1.0, (nz, Th.ny_, Th.nx_)) for _ in range(3)]
+    ao = O.Advection(To, scheme)
+    tro = [t.copy() for t in tr]
+    ao.apply_3d_batch(u, v, w, 600.0, tro)
+    ad = operators.Advection(Td, operators.AdvectionScheme(scheme))
+    trd = [Array(Td, dev(t), z=CENTERS) for t in tr]
+    ad.apply_3d_batch(wrap32(Td.ugrid, u, CENTERS), wrap32(Td.vgrid, v, CENTERS), wrap32(Td, w, INTERFACES), 600.0, trd)
+    wet = Th.mask == 1
+    tol = 2e-5 if scheme == 1 else 1e-5
+    for a, b, t0 in zip(trd, tro, tr):
+        assert a.all_values.dtype == __import__("torch").float64
+        assert rel(host(a.all_values) - t0, b - t0, wet) < tol
+    assert rel(host(ad.h), ao.h, wet) < 1e-6
+
+
+@pytest.mark.parametrize("sources", [False, True])
+def test_vertical_diffusion_f64s(sources):
+    """FP64-stored fields diffused with a float solve (getm_vertical_diffusion_
+    batch_f64s): the change matches the FP64 oracle to 2e-6 of its largest
+    value, for a field of a large mean plus a small signal."""
+    import oracle.oracle as O
+    from getm_gb300 import operators
+    from getm_gb300.core import Array, CENTERS, INTERFACES
+
+    Th, To, Td, rng = setup(seed=90 + sources, nz=12)
+    nz = Th.nz
+    nuh = (10.0 ** rng.uniform(-6, -1, (nz + 1, Th.ny_, Th.nx_))).astype(np.float32).astype(np.float64)
+    t = 500.0 + rng.uniform(0, 1, (nz, Th.ny_, Th.nx_))
+    ea4 = rng.uniform(0, 1e-3, t.shape).astype(np.float32).astype(np.float64) if sources else None
+    vo = O.VerticalDiffusion(To, 1.0)
+    to = t.copy()
+    vo(nuh, 600.0, to, molecular=1e-6, ea4=ea4)
+    vd = operators.VerticalDiffusion(Td, 1.0)
+    td = Array(Td, dev(t), z=CENTERS)
+    vd(wrap32(Td, nuh, INTERFACES), 600.0, td, molecular=1e-6, ea4=None if ea4 is None else wrap32(Td, ea4, CENTERS))
+    wet = Th.mask == 1
+    assert rel(host(td.all_values) - t, to - t, wet) < 2e-6
+
+
+def test_mixed_seamount_1000_steps():
+    """The full 400 x 300 x 40 seamount for 1000 3D steps in the mixed form
+    (FP64 tracer storage, float increments, velocities and solves) against
+    the FP64 form: temperature within 1e-5 of its largest value, salinity
+    within 1e-10.  (The elevation of this unforced box is a residual signal
+    of 2e-6 m; its error is reported, not bounded relative to that signal:
+    FP64 itself, restarted from a temperature moved by one ulp, differs by
+    1e-4 of it after 1000 steps.)"""
+    import torch
+
+    from getm_gb300 import workloads
+    from getm_gb300.simulation import Simulation
+
+    wl = workloads.seamount()
+    p = wl.params
+    sims = {}
+    for prec in ("fp64", "mixed"):
+        s = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=prec)
+        zc = s.T.zc.all_values
+        temp0 = torch.where(s.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
+                            s.temp.all_values.double()).float().double()
+        s.temp.all_values.copy_(temp0)
+        s.start(p["timestep"], p["split_factor"])
+        sims[prec] = s
+    n = 1000 * p["split_factor"]
+    for prec, s in sims.items():
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        graphs = []
+        with torch.cuda.stream(stream):
+            for _ in range(2 * p["split_factor"]):  # warm-up: allocate work buffers
+                s.advance()
+            for _ in range(2):  # one graph per parity of the 3D step (captures run nothing)
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=stream):
+                    for _ in range(p["split_factor"]):
+                        s.advance()
+                graphs.append(g)
+        torch.cuda.current_stream().wait_stream(stream)
+        done = 2 * p["split_factor"]  # substeps run by the warm-up
+        while done < n:
+            graphs[(done // p["split_factor"]) % 2].replay()
+            done += p["split_factor"]
+        torch.cuda.synchronize()
+        assert s.split2d_status() == 0
+    a, b = sims["mixed"], sims["fp64"]
+    assert a.temp.all_values.dtype == torch.float64
+    wet = wl.T.mask == 1
+    e = {"temp": rel(host(a.temp.all_values), host(b.temp.all_values), wet),
+         "salt": rel(host(a.salt.all_values), host(b.salt.all_values), wet),
+         "z_abs_m": float(np.abs(host(a.T.z.all_values) - host(b.T.z.all_values))[wet].max())}
+    print("mixed vs fp64 after 1000 3D steps:", {k: f"{v:.2e}" for k, v in e.items()})
+    assert e["temp"] < 1e-5
+    assert e["salt"] < 1e-10
+
+
 def test_mixed_simulation_error_vs_fp64():
     """Several 3D steps of the seamount box in both forms from identical
     (float32-representable) initial fields.  Tracer errors of the mixed form

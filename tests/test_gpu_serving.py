@@ -25,15 +25,18 @@ def _requests(n, arrivals, steps=6, seed=21, precision="mixed"):
     return reqs
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_alone_equals_in_mix(precision):
+@pytest.mark.parametrize("precision,admission_thread", [("fp64", True), ("mixed", True), ("mixed", False)])
+def test_alone_equals_in_mix(precision, admission_thread):
+    """Admitted on the worker thread (graphs captured while other requests'
+    steps replay) or in the main loop: the same result alone and in the mix."""
     import torch
 
     from getm_gb300.serving import Server
 
-    alone = Server(lanes=2, keep={0}).run(_requests(1, [0.0], precision=precision), duration=120.0)
-    mix = Server(lanes=2, keep={0}).run(_requests(4, [0.0, 0.0, 0.01, 0.02], precision=precision),
-                                        duration=120.0)
+    alone = Server(lanes=2, keep={0}, admission_thread=admission_thread).run(
+        _requests(1, [0.0], precision=precision), duration=120.0)
+    mix = Server(lanes=2, keep={0}, admission_thread=admission_thread).run(
+        _requests(4, [0.0, 0.0, 0.01, 0.02], precision=precision), duration=120.0)
     a = next(r for r in alone if r.rid == 0)
     m = next(r for r in mix if r.rid == 0)
     assert a.finished and m.finished

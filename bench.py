@@ -250,7 +250,7 @@ def _make_sim(wl, precision, device, round_to_float32=True):
     from getm_gb300.simulation import Simulation
 
     p = wl.params
-    sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device)
+    sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device, tiles="auto")
     zc = sim.T.zc.all_values
     temp0 = torch.where(sim.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
                         sim.temp.all_values.double())
@@ -809,7 +809,8 @@ def run_ours(args):
             "steps": nsteps, "warmup": max(args.warmup, 3), "ms_per_step": ms[primary] / nsteps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if primary == "mixed" else "f64", "data": "synthetic",
-            "config": _config(wl, ws), "form": primary, "cuda_graph": r.graphs is not None,
+            "config": _config(wl, ws), "form": primary, "tracer_storage": str(r.sim.dtype_tracer).replace("torch.", ""),
+            "tiles": r.sim.tiles, "cuda_graph": r.graphs is not None,
             "e2e": e2e[primary], "roofline": roofline_kernel, "step_roofline": step_roof,
             "gpu_launches": r.launches_per_period * nsteps // r.period, "clocks": clocks,
             "split2d_status": {f: runners[f].sim.split2d_status() for f in forms}}

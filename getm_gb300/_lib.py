@@ -95,6 +95,9 @@ _SIGS = {
     "getm_substep_batch_participants": "pip",
     "getm_substep_batch_launch": "piips",
     "getm_substep_batch_finalize": "p",
+    "getm_mean_transports": "lppdpps",
+    "getm_slow_friction": "lpppppppps",
+    "getm_velocities_3d_bottom_f32": "llpppppppps",
     "getm_tune_set": "ii",
     "getm_tune_get": "ip",
     "getm_coriolis_espelid": "iiiiipppppppis",

@@ -398,11 +398,30 @@ def transport_3d_finish(vel3d, hn, tp2d, D, tp3d, dev):
          _p(tp3d), _p(dev), _s())
 
 
-def velocities_3d(pk, qk, uk, vk):
-    """uk = pk / hn_U, vk = qk / hn_V (momentum.py:909-910)."""
+def velocities_3d(pk, qk, uk, vk, ubot=None, vbot=None):
+    """uk = pk / hn_U, vk = qk / hn_V (momentum.py:909-910); with ``ubot``,
+    ``vbot`` (mixed form) also their bottom layers widened to FP64."""
     sfx = _sfx(pk.all_values, qk.all_values, uk.all_values, vk.all_values)
+    if ubot is not None:
+        if sfx != "_f32":
+            raise TypeError("bottom velocities are written by the float form only")
+        call("getm_velocities_3d_bottom_f32", pk.all_values.numel(), ubot.all_values.numel(), _p(pk),
+             _p(pk.grid.hn), _p(qk), _p(qk.grid.hn), _p(uk), _p(vk), _p(ubot), _p(vbot), _s())
+        return
     call("getm_velocities_3d" + sfx, pk.all_values.numel(), _p(pk), _p(pk.grid.hn), _p(qk), _p(qk.grid.hn), _p(uk),
          _p(vk), _s())
+
+
+def mean_transports(Ucum, Vcum, scale, Ui, Vi):
+    """Ui = U_cum scale, Vi = V_cum scale, then U_cum = V_cum = 0
+    (momentum.py:790-793); U_cum, V_cum are tensors."""
+    call("getm_mean_transports", Ucum.numel(), Ucum.data_ptr(), Vcum.data_ptr(), float(scale), _p(Ui), _p(Vi), _s())
+
+
+def slow_friction(ustar2x, ru, u1, SxF, ustar2y, rv, v1, SyF):
+    """SxF = ustar2_bx + ru u1, SyF = ustar2_by + rv v1 (momentum.py:1003-1015)."""
+    call("getm_slow_friction", SxF.all_values.numel(), _p(ustar2x), _p(ru), _p(u1), _p(SxF), _p(ustar2y), _p(rv),
+         _p(v1), _p(SyF), _s())
 
 
 # field order of getm_depth3d_fields (include/getm_gb300.h)

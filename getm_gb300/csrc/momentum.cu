@@ -467,16 +467,24 @@ extern "C" int getm_column_sums_f32(int nx, int ny, int nz, int subtract, const 
 // hn over n points (mixed form: in float).
 template <typename T>
 __global__ void velocities_3d_kernel(long long n, const T* pk, const double* hnu, const T* qk, const double* hnv,
-                                     T* uk, T* vk)
+                                     T* uk, T* vk, long long plane = 0, double* ubot = nullptr,
+                                     double* vbot = nullptr)
 {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
+    T u, v;
     if constexpr (std::is_same<T, double>::value) {
-        uk[q] = pk[q] / hnu[q];
-        vk[q] = qk[q] / hnv[q];
+        u = pk[q] / hnu[q];
+        v = qk[q] / hnv[q];
     } else {
-        uk[q] = pk[q] / getm_d2f_approx(hnu[q]);
-        vk[q] = qk[q] / getm_d2f_approx(hnv[q]);
+        u = pk[q] / getm_d2f_approx(hnu[q]);
+        v = qk[q] / getm_d2f_approx(hnv[q]);
+    }
+    uk[q] = u;
+    vk[q] = v;
+    if (ubot && q < plane) {  // the bottom layer widened to FP64 (exact)
+        ubot[q] = getm_widen(u);
+        vbot[q] = getm_widen(v);
     }
 }
 
@@ -526,6 +534,66 @@ extern "C" int getm_velocities_3d_f32(long long n, const float* pk, const double
                                       const double* hnv, float* uk, float* vk, cudaStream_t stream)
 {
     return velocities_3d_impl<float>(n, pk, hnu, qk, hnv, uk, vk, stream);
+}
+
+extern "C" int getm_velocities_3d_bottom_f32(long long n, long long plane, const float* pk, const double* hnu,
+                                             const float* qk, const double* hnv, float* uk, float* vk, double* ubot,
+                                             double* vbot, cudaStream_t stream)
+{
+    if (n < 0 || plane < 0 || plane > n || (n > 0 && (!pk || !hnu || !qk || !hnv || !uk || !vk || !ubot || !vbot)))
+        return GETM_ERR_ARG;
+    if (n == 0) return GETM_OK;
+    velocities_3d_kernel<float><<<getm_div_up(n, 256), 256, 0, stream>>>(n, pk, hnu, qk, hnv, uk, vk, plane, ubot,
+                                                                          vbot);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// Momentum.advance (momentum.py:790-793): the mean transports of the
+// substeps, Ui = U_cum / split_factor (as a product with the reciprocal,
+// like the reference's numpy expression), then U_cum = 0.
+__global__ void mean_transports_kernel(long long n, double* Ucum, double* Vcum, double scale, double* Ui, double* Vi)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    Ui[q] = Ucum[q] * scale;
+    Vi[q] = Vcum[q] * scale;
+    Ucum[q] = 0.0;
+    Vcum[q] = 0.0;
+}
+
+extern "C" int getm_mean_transports(long long n, double* Ucum, double* Vcum, double scale, double* Ui, double* Vi,
+                                    cudaStream_t stream)
+{
+    if (n < 0 || (n > 0 && (!Ucum || !Vcum || !Ui || !Vi))) return GETM_ERR_ARG;
+    if (n == 0) return GETM_OK;
+    mean_transports_kernel<<<getm_div_up(n, 256), 256, 0, stream>>>(n, Ucum, Vcum, scale, Ui, Vi);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// Momentum.update_diagnostics (momentum.py:1003-1015): the slow bottom
+// friction SxF = ustar2_bx + ru u1 (SyF likewise), product and sum rounded
+// separately as in the reference's numpy expression (no contraction).
+__global__ void slow_friction_kernel(long long n, const double* ustar2x, const double* ru, const double* u1,
+                                     double* SxF, const double* ustar2y, const double* rv, const double* v1,
+                                     double* SyF)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    SxF[q] = __dadd_rn(ustar2x[q], __dmul_rn(ru[q], u1[q]));
+    SyF[q] = __dadd_rn(ustar2y[q], __dmul_rn(rv[q], v1[q]));
+}
+
+extern "C" int getm_slow_friction(long long n, const double* ustar2x, const double* ru, const double* u1,
+                                  double* SxF, const double* ustar2y, const double* rv, const double* v1, double* SyF,
+                                  cudaStream_t stream)
+{
+    if (n < 0 || (n > 0 && (!ustar2x || !ru || !u1 || !SxF || !ustar2y || !rv || !v1 || !SyF))) return GETM_ERR_ARG;
+    if (n == 0) return GETM_OK;
+    slow_friction_kernel<<<getm_div_up(n, 256), 256, 0, stream>>>(n, ustar2x, ru, u1, SxF, ustar2y, rv, v1, SyF);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 // momentum.F90:323-340: rows jmin..jmax, every i (T: type of un and Uo)

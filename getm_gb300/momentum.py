@@ -281,10 +281,7 @@ class Momentum:
     def advance(self, timestep: float, split_factor: int, tausx: Array, tausy: Array, dpdx: Array, dpdy: Array,
                 idpdx: Array, idpdy: Array, viscosity: Array, side_stream=None):
         """momentum.py:760-858.  ``side_stream``: see update_diagnostics."""
-        torch.mul(self._U_cum, 1.0 / split_factor, out=self.Ui.all_values)
-        torch.mul(self._V_cum, 1.0 / split_factor, out=self.Vi.all_values)
-        self._U_cum.zero_()
-        self._V_cum.zero_()
+        _pygetm.mean_transports(self._U_cum, self._V_cum, 1.0 / split_factor, self.Ui, self.Vi)
 
         def u():
             self.advance_3d_transport(self.pk, self.Ui, self.uk, dpdx, self.corpk, self.advpk, self.diffpk, idpdx,
@@ -318,7 +315,10 @@ class Momentum:
             self.coriolis(self.pk, self.corqk, True)
             self.coriolis(self.qk, self.corpk, False)
         _pygetm.w_momentum_3d(self.pk, self.qk, timestep, self.ww)
-        _pygetm.velocities_3d(self.pk, self.qk, self.uk, self.vk)
+        if self.u_bot is self._u_bot64:  # mixed form: the FP64 bottom velocities in the same launch
+            _pygetm.velocities_3d(self.pk, self.qk, self.uk, self.vk, self._u_bot64, self._v_bot64)
+        else:
+            _pygetm.velocities_3d(self.pk, self.qk, self.uk, self.vk)
         if side_stream is None:
             self._diagnostics_tail(timestep)
             return
@@ -333,9 +333,6 @@ class Momentum:
         stream on which the advection of the V momentum runs beside that of
         the U momentum (separate handles, inputs and outputs)."""
         _pygetm.shear_frequency(self.uk, self.vk, self.SS)
-        if self.u_bot is self._u_bot64:
-            self._u_bot64.all_values.copy_(self.uk.all_values[0])
-            self._v_bot64.all_values.copy_(self.vk.all_values[0])
         if self.apply_bottom_friction:
             self.bottom_friction(self.u_bot, self.v_bot, self.hU_bot, self.hV_bot, self.rru, self.rrv)
         _pygetm.bottom_shear_velocity(self.u_bot, self.v_bot, self.rru, self.rrv, self.ustar2_bx, self.ustar2_by,
@@ -369,8 +366,8 @@ class Momentum:
         _pygetm.column_sums([(self.advpk, self.SxA), (self.advqk, self.SyA), (self.diffpk, self.SxD),
                              (self.diffqk, self.SyD)], subtract=True)
         if self.apply_bottom_friction:
-            torch.add(self.ustar2_bx.all_values, self.ru.all_values * self.u1.all_values, out=self.SxF.all_values)
-            torch.add(self.ustar2_by.all_values, self.rv.all_values * self.v1.all_values, out=self.SyF.all_values)
+            _pygetm.slow_friction(self.ustar2_bx, self.ru, self.u1, self.SxF, self.ustar2_by, self.rv, self.v1,
+                                  self.SyF)
 
     def advance_3d_transport(self, tp3d: Array, tp2d: Array, vel3d: Array, dp: Array, cor: Array, adv: Array,
                              diff: Array, idp: Array, taus: Array, rr: Array, viscosity: Array, dev: Array,

@@ -163,21 +163,27 @@ class Server:
                 ready.put(e)
 
     def run(self, requests: List[Request], duration: float, admit_until: Optional[float] = None,
-            poll_sleep: float = 0.0) -> List[Result]:
+            poll_sleep: Optional[float] = None) -> List[Result]:
         """Serve ``requests`` until all admitted ones are done or ``duration``
         seconds have passed (unfinished work is then abandoned; its completed
         steps still count).  Requests are admitted until ``admit_until``
         seconds (default: ``duration``).  Workloads of the next arrivals are
         generated on a host thread ahead of their admission; with
         ``admission_thread`` the set-up runs on a worker thread, otherwise at
-        most one request is set up per pass of the loop.  Returns one Result
-        per admitted request."""
+        most one request is set up per pass of the loop.  ``poll_sleep``:
+        seconds the loop sleeps when a pass found nothing to do (default:
+        100 us with the admission thread, which then gets the interpreter:
+        a loop that only polls would otherwise hold it while the worker's
+        every library call gives it up; 0 without).  Returns one Result per
+        admitted request."""
         import queue
         import sys
         import threading
         from concurrent.futures import ThreadPoolExecutor
 
         admit_until = duration if admit_until is None else admit_until
+        if poll_sleep is None:
+            poll_sleep = 1e-4 if self.admission_thread else 0.0
         pending = sorted(requests, key=lambda r: r.arrival)
         active: List[_Active] = []
         results: List[Result] = []

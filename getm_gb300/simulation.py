@@ -110,7 +110,8 @@ class Simulation:
                  airsea: Optional[Fluxes] = None, internal_pressure: str = "shchepetkin_mcwilliams",
                  Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
                  nuh: float = 0.0, precision: str = "fp64", fused_2d: bool = True, substep_kernel: bool = True,
-                 concurrent_3d: bool = True, tiles=None, tracer_storage: Optional[str] = None, device="cuda"):
+                 concurrent_3d: bool = True, tiles=None, tracer_storage: Optional[str] = None,
+                 internal_pressure_arithmetic: Optional[str] = None, device="cuda"):
         """``precision``: "fp64" (the plain form) or "mixed" (float32 tracers,
         3D velocities and their tendencies and diffusivities; float64
         elevations, depths, layer thicknesses, 2D transports and their
@@ -138,7 +139,10 @@ class Simulation:
         while their advection and diffusion increments, fluxes, limiters and
         solves stay float: float32 rounding of the stored tracers would
         otherwise perturb the density, and through it the flow, by up to half
-        an ulp of the tracer every step; "float32" stores them in float."""
+        an ulp of the tracer every step; "float32" stores them in float.
+        ``internal_pressure_arithmetic``: "float32" (mixed-form default: FP64
+        column integrals and differences, float slope corrections) or
+        "float64"."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
@@ -154,6 +158,9 @@ class Simulation:
         if tracer_storage not in ("float64", "float32"):
             raise ValueError(f"tracer_storage must be 'float64' or 'float32', not {tracer_storage!r}")
         self.tracer_storage = tracer_storage
+        if internal_pressure_arithmetic is None:
+            internal_pressure_arithmetic = "float32" if precision == "mixed" else "float64"
+        self.internal_pressure_arithmetic = internal_pressure_arithmetic
         dtr = torch.float64 if precision == "fp64" or tracer_storage == "float64" else torch.float32
         self.dtype_tracer = dtr
         if Dmin <= 0.0:
@@ -430,7 +437,7 @@ class Simulation:
             _pygetm.blumberg_mellor(self.buoy, self.idpdx, self.idpdy)
         else:
             _pygetm.shchepetkin_mcwilliams(self.buoy, self.idpdx, self.idpdy, self._P_work,
-                                           "float32" if self.precision == "mixed" else "float64")
+                                           self.internal_pressure_arithmetic)
 
     def totals_device(self) -> torch.Tensor:
         """Device tensor [total volume, total of each tracer] (compensated

@@ -301,6 +301,16 @@ int getm_tune_get(int knob, int* value);
 int getm_density_buoyancy(int n, const double* salt, const double* temp, const double* p, double* rho,
                           double* buoy, cudaStream_t stream);
 
+/* Momentum.advance (momentum.py:790-793): Ui = U_cum * scale, Vi = V_cum *
+ * scale (scale = 1 / split_factor), then U_cum = V_cum = 0; n points.      */
+int getm_mean_transports(long long n, double* Ucum, double* Vcum, double scale, double* Ui, double* Vi,
+                         cudaStream_t stream);
+/* Momentum.update_diagnostics (momentum.py:1003-1015): SxF = ustar2_bx +
+ * ru * u1 and SyF = ustar2_by + rv * v1 (product and sum rounded
+ * separately), n points.                                                   */
+int getm_slow_friction(long long n, const double* ustar2x, const double* ru, const double* u1, double* SxF,
+                       const double* ustar2y, const double* rv, const double* v1, double* SyF, cudaStream_t stream);
+
 /* ---- mixed-precision form ------------------------------------------------
  * Same routines with float bulk fields (tracers, 3D velocities/transports,
  * their tendencies, nuh/num) and float arithmetic for fluxes, limiters and
@@ -338,6 +348,12 @@ int getm_advection_apply_3d_batch_f64s(getm_advection* adv, getm_grid* tgrid, ge
                                        const double* Ah_v, double timestep, double* h,
                                        const double* hu, const double* hv, int ntracer,
                                        double* const* vars, cudaStream_t stream);
+/* getm_velocities_3d_f32, also writing the bottom layer (the first `plane`
+ * points) of uk and vk widened to double into ubot, vbot (the FP64 bottom
+ * velocities of the mixed form's 2D friction).                             */
+int getm_velocities_3d_bottom_f32(long long n, long long plane, const float* pk, const double* hnu,
+                                  const float* qk, const double* hnv, float* uk, float* vk, double* ubot,
+                                  double* vbot, cudaStream_t stream);
 int getm_advection_uv_pass_f64s(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
                                 getm_grid* ugrid, const float* u, const double* Ah, double timestep,
                                 const double* h_in, double* h_out, const double* hu, int ntracer,

@@ -104,6 +104,7 @@ _SIGS = {
     "getm_coriolis_espelid_f32": "iiiiipppppppis",
     "getm_buoyancy_frequency": "iiipppppps",
     "getm_buoyancy_frequency_f32": "iiipppppps",
+    "getm_buoyancy_frequency_f64s": "iiipppppps",
     "getm_column_sums": "iiiipppppppps",
     "getm_column_sums_f32": "iiiipppppppps",
     "getm_velocities_3d_f32": "lpppppps",
@@ -140,15 +141,33 @@ _SIGS = {
     "getm_blumberg_mellor_f32": "iiiiiiipppppppppps",
     "getm_shchepetkin_mcwilliams_f32": "iiiiiiipppppppppppps",
     "getm_density_buoyancy_f32": "ippppps",
+    "getm_density_buoyancy_f64s": "ippppps",
     "getm_domain_totals": "iiiiiiippppippps",
     "getm_domain_totals_f32": "iiiiiiippppippps",
 }
 _CT = {"i": c_int, "l": ctypes.c_longlong, "d": c_double, "p": c_void_p, "s": c_void_p, "c": ctypes.c_char_p}
 
+# The same library bound a second time with the interpreter lock held during
+# the call.  Almost every entry point only checks arguments and enqueues
+# work on a stream (microseconds); releasing and re-taking the lock around
+# each of them lets another Python thread (the serving loop's step issue, or
+# its admission worker) take the lock, and the caller then waits up to a
+# whole switch interval to continue: thousands of such calls in a domain's
+# set-up cost seconds.  Calls that may block (device synchronisation,
+# allocation, synchronous copies) release the lock as usual.
+_plib = ctypes.PyDLL(str(LIB_PATH))
+_BLOCKING = frozenset({
+    "getm_advection_create", "getm_advection_finalize", "getm_vertical_diffusion_create",
+    "getm_vertical_diffusion_finalize", "getm_grid_finalize", "getm_advection_get_status",
+    "getm_substep_batch_create", "getm_substep_batch_upload", "getm_substep_batch_finalize",
+})
+
 for _name, _sig in _SIGS.items():
-    _f = getattr(lib, _name)
-    _f.argtypes = [_CT[c] for c in _sig]
-    _f.restype = c_int
+    for _l in (lib, _plib):
+        _f = getattr(_l, _name)
+        _f.argtypes = [_CT[c] for c in _sig]
+        _f.restype = c_int
+_CALL = {n: getattr(lib if n in _BLOCKING else _plib, n) for n in _SIGS}
 
 EXPORTED = tuple(_SIGS)
 
@@ -193,7 +212,7 @@ def call(name: str, *args) -> int:
     """Call an entry point; raise GetmError on a non-zero status."""
     if _pending_release:
         _flush_releases()
-    rc = getattr(lib, name)(*args)
+    rc = _CALL[name](*args)
     if rc != GETM_OK:
         raise GetmError(name, rc)
     return rc

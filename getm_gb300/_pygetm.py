@@ -13,7 +13,7 @@ import ctypes
 import torch
 
 from . import _lib
-from .core import CENTERS, INTERFACES, Array, _sfx, interp_x, interp_xy, interp_y, interp_z  # noqa: F401
+from .core import CENTERS, INTERFACES, Array, _sfx, _sfx_storage, interp_x, interp_xy, interp_y, interp_z  # noqa: F401
 from ._lib import call
 
 
@@ -480,7 +480,7 @@ def buoyancy_frequency(salt, temp, p, out):
     (z=INTERFACES); ``p``: layer-centre depths (thickness2center_depth)."""
     g = salt.grid
     assert temp.grid is g and p.grid is g and out.grid is g and out.z == INTERFACES
-    sfx = _sfx(salt.all_values, temp.all_values, out.all_values)
+    sfx = _sfx_storage([out.all_values], [salt.all_values, temp.all_values])
     call("getm_buoyancy_frequency" + sfx, g.nx_, g.ny_, salt.all_values.shape[0], _p(g.mask), _p(g.hn), _p(p),
          _p(salt), _p(temp), _p(out), _s())
     return out

@@ -111,7 +111,7 @@ struct getm_advection {
     getm_grid* tgrid;
     size_t n3;                 // elements of one 3D field the buffers are sized for
     double* hbuf[2];           // layer-thickness ping-pong buffers
-    double* colbuf[2];         // vertical sub-stepping work arrays (haux, faux)
+    double* colbuf[2];         // vertical sub-stepping work arrays (haux: n3, faux: 2 n3 doubles)
     double* tmp[GETM_MAX_BATCH * 8];  // per-tracer ping-pong buffers
     int ntmp;
     int* status;               // device status word (GETM_ERR_ITERS)
@@ -136,8 +136,10 @@ static int adv_reserve(getm_advection* a, size_t n3, int ntracer)
         adv_free_buffers(a);
         for (int i = 0; i < 2; i++)
             if (cudaMalloc(&a->hbuf[i], n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
-        for (int i = 0; i < 2; i++)
-            if (cudaMalloc(&a->colbuf[i], n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
+        // colbuf[1] holds the intermediate sub-steps of a pair of fields
+        // stepped together by the w pass (two fields of up to 8 bytes)
+        if (cudaMalloc(&a->colbuf[0], n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
+        if (cudaMalloc(&a->colbuf[1], 2 * n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
         a->n3 = n3;
     }
     while (a->ntmp < ntracer) {
@@ -528,13 +530,11 @@ __global__ void __launch_bounds__(128, getm_increment_form<V> ? 7 : 1) wpass_ker
     }
     const int itersmax = 200;
     // mixed form: two consecutive fields with the same w_var are stepped
-    // together (the sub-step count depends only on w_var and h); the second
-    // one's intermediate sub-steps use the upper half of the column work
-    // array, which holds n3 doubles
+    // together (the sub-step count depends only on w_var and h)
     constexpr bool inc = getm_increment_form<V>;
-    // pairs only for float fields: the second field's intermediate sub-steps
-    // need the upper half of the column work array (n3 doubles)
-    constexpr bool pairs = inc && sizeof(T) == 4;
+    // the second field's intermediate sub-steps use the upper half of the
+    // column work array colbuf[1] (2 n3 doubles)
+    constexpr bool pairs = inc;
     for (int t = 0; t < a.ntracer;) {
         const int nt = (pairs && t + 1 < a.ntracer && a.wvar[t + 1] == a.wvar[t]) ? 2 : 1;
         const V* wv = a.wvar[t];

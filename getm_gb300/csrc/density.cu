@@ -102,6 +102,49 @@ __device__ __forceinline__ DF seos_anomaly_df(float S, float T, double z)
     return df_add(df_add(DF{-tA.hi, -tA.lo}, tB), DF{-tN.hi, -tN.lo});
 }
 
+// The same anomaly from FP64 S and T (the mixed form's FP64 tracer storage):
+// each is split into a truncated float head and the float of the rest (one
+// FP64 subtraction each), which the double-float sums take in.
+__device__ __forceinline__ DF seos_anomaly_df2(double S, double T, double z)
+{
+    constexpr DFConst A0(SEOS_A0), B0(SEOS_B0), L1(0.5 * SEOS_LAMBDA1), L2(0.5 * SEOS_LAMBDA2);
+    constexpr DFConst M1(SEOS_MU1), M2(SEOS_MU2), NU(SEOS_NU);
+    const float zh = getm_d2f_approx(z), Th = getm_d2f_approx(T), Sh = getm_d2f_approx(S);
+    const DF zd{zh, getm_d2f_approx(z - getm_f2d(zh))};
+    const float Tl = getm_d2f_approx(T - getm_f2d(Th)), Sl = getm_d2f_approx(S - getm_f2d(Sh));
+    const DF Ta = df_add(df_two_sum(Th, -10.f), DF{Tl, 0.f});
+    const DF Sa = df_add(df_two_sum(Sh, -35.f), DF{Sl, 0.f});
+    const DF one{1.f, 0.f};
+    const DF u = df_add(one, df_add(df_mul(df_of(L1), Ta), df_mul(df_of(M1), zd)));
+    DF v = df_add(df_mul(df_of(L2), Sa), df_mul(df_of(M2), zd));
+    v = df_add(one, DF{-v.hi, -v.lo});
+    const DF tA = df_mul(df_of(A0), df_mul(u, Ta));
+    const DF tB = df_mul(df_of(B0), df_mul(v, Sa));
+    const DF tN = df_mul(df_of(NU), df_mul(Ta, Sa));
+    return df_add(df_add(DF{-tA.hi, -tA.lo}, tB), DF{-tN.hi, -tN.lo});
+}
+
+__global__ void density_f64s_kernel(long long n, const double* S, const double* T, const double* p, double* rho,
+                                    double* buoy)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const DF a = seos_anomaly_df2(S[q], T[q], p[q]);
+    const double ad = getm_f2d(a.hi) + getm_f2d(a.lo);
+    if (rho) rho[q] = SEOS_RHO0 + ad;
+    if (buoy) buoy[q] = (-GETM_G / GETM_RHO0) * (ad + (SEOS_RHO0 - GETM_RHO0));
+}
+
+extern "C" int getm_density_buoyancy_f64s(int n, const double* salt, const double* temp, const double* p,
+                                          double* rho, double* buoy, cudaStream_t stream)
+{
+    if (n < 0 || (n > 0 && (!salt || !temp || !p || (!rho && !buoy)))) return GETM_ERR_ARG;
+    if (n == 0) return GETM_OK;
+    density_f64s_kernel<<<getm_div_up(n, 256), 256, 0, stream>>>(n, salt, temp, p, rho, buoy);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
 // R: type of salinity and temperature.  Density and buoyancy are stored in
 // FP64 in both forms (the internal pressure gradient is a small difference
 // of large column integrals of buoyancy).  The FP64 form evaluates seos_rho
@@ -161,18 +204,28 @@ extern "C" int getm_density_buoyancy_f32(int n, const float* salt, const float* 
 //   Ta1 Sa1 - Ta0 Sa0 = dT Sa1 + Ta0 dS.
 // Interfaces 1 .. nz-1 of columns with a non-zero mask are written; the
 // surface and bottom interfaces are left as they are (reference: out[1:-1]).
-// R: type of S, T and N2 (float in the mixed form).
-template <typename R>
+// R: arithmetic and the type of N2 (float in the mixed form); X: type of S
+// and T (R, or double with float arithmetic for the mixed form's FP64
+// tracers: the differences dT, dS are formed in FP64 and narrowed).
+template <typename R, typename X = R>
 __global__ void buoyancy_frequency_kernel(long long plane, int nz, const int* __restrict__ mask,
                                           const double* __restrict__ h, const double* __restrict__ p,
-                                          const R* __restrict__ S, const R* __restrict__ T, R* __restrict__ NN)
+                                          const X* __restrict__ S, const X* __restrict__ T, R* __restrict__ NN)
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int k = blockIdx.y;  // interface k + 1
     if (c >= plane || k >= nz - 1 || mask[c] == 0) return;
     const long long q0 = c + (long long)k * plane, q1 = q0 + plane;
-    const R T0 = T[q0], T1 = T[q1], S0 = S[q0], S1 = S[q1];
-    const R dT = T1 - T0, dS = S1 - S0;
+    R T0, T1, S0, S1, dT, dS;
+    if constexpr (std::is_same<R, X>::value) {
+        T0 = T[q0]; T1 = T[q1]; S0 = S[q0]; S1 = S[q1];
+        dT = T1 - T0; dS = S1 - S0;
+    } else {
+        const X T0x = T[q0], T1x = T[q1], S0x = S[q0], S1x = S[q1];
+        T0 = getm_d2f_approx(T0x); T1 = getm_d2f_approx(T1x);
+        S0 = getm_d2f_approx(S0x); S1 = getm_d2f_approx(S1x);
+        dT = getm_d2f_approx(T1x - T0x); dS = getm_d2f_approx(S1x - S0x);
+    }
     const R Ta0 = T0 - R(10), Ta1 = T1 - R(10), Sa0 = S0 - R(35), Sa1 = S1 - R(35);
     R zi, dz;
     if constexpr (std::is_same<R, double>::value) {
@@ -211,4 +264,17 @@ extern "C" int getm_buoyancy_frequency_f32(int nx, int ny, int nz, const int* ma
                                            const float* salt, const float* temp, float* NN, cudaStream_t stream)
 {
     return buoyancy_frequency_impl<float>(nx, ny, nz, mask, h, p, salt, temp, NN, stream);
+}
+
+extern "C" int getm_buoyancy_frequency_f64s(int nx, int ny, int nz, const int* mask, const double* h,
+                                            const double* p, const double* salt, const double* temp, float* NN,
+                                            cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || !mask || !h || !p || !salt || !temp || !NN) return GETM_ERR_ARG;
+    if (nz == 1) return GETM_OK;
+    const long long plane = (long long)nx * ny;
+    dim3 grid(getm_div_up(plane, 256), nz - 1);
+    buoyancy_frequency_kernel<float, double><<<grid, 256, 0, stream>>>(plane, nz, mask, h, p, salt, temp, NN);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }

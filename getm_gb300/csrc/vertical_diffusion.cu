@@ -290,8 +290,7 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float, S>& a, long lon
     }
     float hoF = vd_h<float>(ho_c), hnF = vd_h<float>(hn_c);
     float dh = one_h ? 0.f : getm_d2f_approx(ho_c - hn_c);
-    float rk[NT], qk[NT], aoa[NT], ana[NT];
-    S vkp1[NT];
+    float rk[NT], qk[NT], aoa[NT], ana[NT], dprev[NT];
     // surface layer (diffusion.F90:238-245) and the inner layers
     // (:247-258, elimination :287-290)
     for (; k >= 1; k--) {
@@ -321,16 +320,19 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float, S>& a, long lon
             const float anb = cn * x / sn;
             const float a1 = -anb;
             // differences of neighbouring values in the storage type, then
-            // narrowed (exact for float storage)
+            // narrowed (exact for float storage); the difference to the
+            // level above is minus the level above's difference to this one
             const float xk = inc_f<S>(vk[t]);
+            const float ddn = inc_f<S>(vn[t] - vk[t]);
             float a2, a4;
             if (k == nz - 1) {
                 a2 = hnF + anb;
-                a4 = xk * dh + inc_f<S>(vn[t] - vk[t]) * (aob + anb);
+                a4 = xk * dh + ddn * (aob + anb);
             } else {
                 a2 = hnF + ana[t] + anb;
-                a4 = xk * dh + inc_f<S>(vkp1[t] - vk[t]) * (aoa[t] + ana[t]) + inc_f<S>(vn[t] - vk[t]) * (aob + anb);
+                a4 = xk * dh + (-dprev[t]) * (aoa[t] + ana[t]) + ddn * (aob + anb);
             }
+            dprev[t] = ddn;
             if (SRC && e2[t]) a4 = a4 + e2c[t] * xk;
             if (SRC && e2[t]) a2 = a2 - e2c[t];
             if (SRC && e4[t]) a4 = a4 + e4c[t];
@@ -346,7 +348,7 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float, S>& a, long lon
             ru[t][k * P] = rk[t];
             qu[t][k * P] = qk[t];
             aoa[t] = aob; ana[t] = anb;
-            vkp1[t] = vk[t]; vk[t] = vn[t]; vn[t] = vnn[t];
+            vk[t] = vn[t]; vn[t] = vnn[t];
             e2c[t] = e2n[t]; e4c[t] = e4n[t];
         }
         hoF = hoFn; hnF = hnFn;
@@ -363,7 +365,7 @@ __device__ __forceinline__ void vd_inc_sweep(const VDArgs<float, S>& a, long lon
         const float a3 = -ana[t];
         const float xk = inc_f<S>(vk[t]);
         float a2 = hnF + ana[t];
-        float a4 = xk * dh + inc_f<S>(vkp1[t] - vk[t]) * (aoa[t] + ana[t]);
+        float a4 = xk * dh + (-dprev[t]) * (aoa[t] + ana[t]);
         if (SRC && e2[t]) a4 = a4 + e2c[t] * xk;
         if (SRC && e2[t]) a2 = a2 - e2c[t];
         if (SRC && e4[t]) a4 = a4 + e4c[t];

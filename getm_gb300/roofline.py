@@ -9,10 +9,11 @@ arrays a kernel keeps to itself (fluxes, Thomas coefficients) do not count.
 Interior cells only (nx ny nz; columns nx ny), halos excluded.
 
 Storage: the FP64 form stores everything in 8 bytes.  The mixed form
-stores tracers, 3D velocities and transports and their tendencies,
-diffusivities, w and the shear and buoyancy frequencies in 4 bytes, and
-keeps layer thicknesses, vertical coordinates, density, buoyancy, the
-internal-pressure gradients and every 2D field in 8 bytes.
+stores 3D velocities and transports and their tendencies, diffusivities, w
+and the shear frequency in 4 bytes, the tracers and the buoyancy frequency
+in 8 bytes (4 with ``tracer_storage="float32"``), and keeps layer
+thicknesses, vertical coordinates, density, buoyancy, the internal-pressure
+gradients and every 2D field in 8 bytes.
 
 The call list follows Simulation.advance for a closed baroclinic domain
 with prescribed surface fluxes and vertical mixing, default Coriolis, FULL
@@ -76,11 +77,13 @@ def _substep_2d() -> List[Call]:
     return c
 
 
-def step_calls(precision: str = "mixed", ntracer: int = 2, split: int = 30) -> List[Call]:
+def step_calls(precision: str = "mixed", ntracer: int = 2, split: int = 30,
+               tracer_storage: str = "float64") -> List[Call]:
     """Every call of one 3D step with its substeps, for the given form."""
-    if precision not in ("fp64", "mixed"):
-        raise ValueError(precision)
+    if precision not in ("fp64", "mixed") or tracer_storage not in ("float64", "float32"):
+        raise ValueError((precision, tracer_storage))
     S = 4 if precision == "mixed" else 8  # bytes of a float-stored 3D field
+    F = 4 if precision == "mixed" and tracer_storage == "float32" else 8  # bytes of a tracer
     H = D                                 # thicknesses, coordinates: float64 in both forms
     calls = [dataclasses.replace(c, count=split) for c in _substep_2d()]
     # --- 3D step (macro substep) ---
@@ -102,7 +105,10 @@ def step_calls(precision: str = "mixed", ntracer: int = 2, split: int = 30) -> L
     # w), apply_3d (four u/v passes of var, u, hu, h in and h, var out; the w
     # pass of w, h, var in and h, var out) and reconstruct_transport_change;
     # the column sums of advpk, advqk, diffpk, diffqk
-    apply3d = 4 * (S + S + H + H + H + S) + (S + H + S + H + S)
+    def apply3d_of(f):  # f: bytes of the advected field
+        return 4 * (f + S + H + H + H + f) + (S + H + f + H + f)
+
+    apply3d = apply3d_of(S)
     adv_dir = 2 * S + 3 * 2 * S + apply3d + (S + H + S + S)
     # 2D: bottom friction on the bottom layer (two interps, two drag
     # coefficients), bottom_shear_velocity (three masks, u, v, rru, rrv in;
@@ -114,23 +120,23 @@ def step_calls(precision: str = "mixed", ntracer: int = 2, split: int = 30) -> L
     # TracerCollection.advance (tracer.py:193-276): per tracer apply_3d (as
     # above with float u/v/w) and VerticalDiffusion (nuh, ho, hn, var in; var out)
     calls.append(Call("TracerCollection.advance (tracer.py:193-276)",
-                      ntracer * (apply3d + (S + 2 * H + S + S)), 0))
+                      ntracer * (apply3d_of(F) + (S + 2 * H + F + F)), 0))
     # density and buoyancy (simulation.py:1178-1184): S, T, pressure in; rho,
     # then buoy; internal pressure (buoy, h, zc in; idpdx, idpdy out);
     # SxB, SyB column sums; NN (S, T, h, pressure in; NN out)
     calls.append(Call("density, buoyancy, internal pressure, NN (simulation.py:1178-1204)",
-                      (2 * S + H + D) + 2 * D + 5 * D + 2 * D + (2 * S + 2 * H + S), 2 * D))
+                      (2 * F + H + D) + 2 * D + 5 * D + 2 * D + (2 * F + 2 * H + F), 2 * D))
     return calls
 
 
 def step_bytes(nx: int, ny: int, nz: int, precision: str = "mixed", ntracer: int = 2,
-               split: int = 30) -> Dict[str, float]:
+               split: int = 30, tracer_storage: str = "float64") -> Dict[str, float]:
     """Algorithmic bytes of one 3D step: per call and in total, with the 2D
     substep loop and the 3D part apart."""
     cells, cols = nx * ny * nz, nx * ny
     out: Dict[str, float] = {}
     b2d = b3d = 0.0
-    for c in step_calls(precision, ntracer, split):
+    for c in step_calls(precision, ntracer, split, tracer_storage):
         b = c.count * (c.per_cell * cells + c.per_column * cols)
         out[c.name] = b
         if c.per_cell:

@@ -231,7 +231,7 @@ class Simulation:
             self.rho = T.array(z=CENTERS, name="rho")
             self.buoy = T.array(z=CENTERS, name="buoy")
             # squared buoyancy frequency (simulation.py:757-767, :1200-1204)
-            self.NN = T.array(z=INTERFACES, name="NN", dtype=dtr)
+            self.NN = T.array(z=INTERFACES, name="NN", dtype=d3)
             self.NN.fill(0.0)
             self.internal_pressure_method = internal_pressure
         if three_d:
@@ -422,7 +422,10 @@ class Simulation:
         from ._lib import call
         from .core import _sfx
 
-        call("getm_density_buoyancy" + _sfx(self.salt.all_values, self.temp.all_values), n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
+        # the mixed form's FP64 tracers: the double-float anomaly from split inputs
+        sfx = "_f64s" if self.precision == "mixed" and self.dtype_tracer == torch.float64 else \
+            _sfx(self.salt.all_values, self.temp.all_values)
+        call("getm_density_buoyancy" + sfx, n, self.salt.all_values.data_ptr(), self.temp.all_values.data_ptr(),
              self.depth.all_values.data_ptr(), self.rho.all_values.data_ptr(), self.buoy.all_values.data_ptr(),
              torch.cuda.current_stream().cuda_stream)
         if side_stream is None:

@@ -354,6 +354,15 @@ int getm_advection_apply_3d_batch_f64s(getm_advection* adv, getm_grid* tgrid, ge
 int getm_velocities_3d_bottom_f32(long long n, long long plane, const float* pk, const double* hnu,
                                   const float* qk, const double* hnv, float* uk, float* vk, double* ubot,
                                   double* vbot, cudaStream_t stream);
+/* Density and buoyancy from FP64 S and T with the mixed form's arithmetic
+ * (the double-float anomaly of getm_density_buoyancy_f32, each input split
+ * into two floats); the squared buoyancy frequency from FP64 S and T in
+ * float arithmetic (temperature and salinity differences formed in FP64),
+ * float NN.                                                                 */
+int getm_density_buoyancy_f64s(int n, const double* salt, const double* temp, const double* p, double* rho,
+                               double* buoy, cudaStream_t stream);
+int getm_buoyancy_frequency_f64s(int nx, int ny, int nz, const int* mask, const double* h, const double* p,
+                                 const double* salt, const double* temp, float* NN, cudaStream_t stream);
 int getm_advection_uv_pass_f64s(int direction, int nk, getm_advection* adv, getm_grid* tgrid,
                                 getm_grid* ugrid, const float* u, const double* Ah, double timestep,
                                 const double* h_in, double* h_out, const double* hu, int ntracer,

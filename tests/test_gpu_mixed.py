@@ -331,3 +331,55 @@ def test_density_double_float():
     db = np.abs(b.cpu().numpy() - b_ref).max()
     print(f"double-float density: rho {drho:.2e} kg m-3, buoyancy {db:.2e} m s-2")
     assert drho < 2e-12 and db < 2e-14
+
+
+def test_density_and_nn_from_fp64_tracers():
+    """Mixed form with FP64 tracers: density from FP64 S and T split into
+    float pairs (double-float anomaly) against the oracle's FP64 evaluation,
+    to FP64 rounding of rho (and 2e-14 m s-2 in buoyancy); the squared
+    buoyancy frequency in float arithmetic (differences in FP64) against the
+    FP64 kernel to 1e-5 of its largest value."""
+    import torch
+
+    from getm_gb300 import _lib
+    from oracle.models import seos_buoyancy
+
+    rng = np.random.default_rng(12)
+    n = 200_000
+    S = rng.uniform(0.0, 40.0, n)
+    T = rng.uniform(-2.0, 32.0, n)
+    z = rng.uniform(0.0, 6000.0, n)
+    rho_ref, b_ref = seos_buoyancy(S, T, z)
+    Sd, Td, zd = (torch.from_numpy(a).cuda() for a in (S, T, z))
+    rho = torch.empty(n, dtype=torch.float64, device="cuda")
+    b = torch.empty_like(rho)
+    s = torch.cuda.current_stream().cuda_stream
+    _lib.call("getm_density_buoyancy_f64s", n, Sd.data_ptr(), Td.data_ptr(), zd.data_ptr(), rho.data_ptr(),
+              b.data_ptr(), s)
+    torch.cuda.synchronize()
+    drho = np.abs(rho.cpu().numpy() - rho_ref).max()
+    db = np.abs(b.cpu().numpy() - b_ref).max()
+    print(f"density from FP64 tracers: rho {drho:.2e} kg m-3, buoyancy {db:.2e} m s-2")
+    assert drho < 2e-12 and db < 2e-14
+
+    # stratified columns: NN from FP64 tracers, float arithmetic vs FP64
+    nz, ny, nx = 30, 40, 50
+    plane = nx * ny
+    h = torch.from_numpy(rng.uniform(1.0, 20.0, (nz, ny, nx))).cuda()
+    p = torch.cumsum(h.flip(0), 0).flip(0) - 0.5 * h
+    zc = -p
+    temp = (10.0 + 10.0 * torch.exp(zc / 200.0) + 0.01 * torch.from_numpy(rng.standard_normal((nz, ny, nx))).cuda())
+    salt = 35.0 + 0.5 * torch.tanh(zc / 300.0)
+    mask = torch.from_numpy((rng.random((ny, nx)) > 0.2).astype(np.int32)).cuda()
+    nn64 = torch.zeros((nz + 1, ny, nx), dtype=torch.float64, device="cuda")
+    nn32 = torch.zeros((nz + 1, ny, nx), dtype=torch.float32, device="cuda")
+    _lib.call("getm_buoyancy_frequency", nx, ny, nz, mask.data_ptr(), h.data_ptr(), p.data_ptr(), salt.data_ptr(),
+              temp.data_ptr(), nn64.data_ptr(), s)
+    _lib.call("getm_buoyancy_frequency_f64s", nx, ny, nz, mask.data_ptr(), h.data_ptr(), p.data_ptr(),
+              salt.data_ptr(), temp.data_ptr(), nn32.data_ptr(), s)
+    torch.cuda.synchronize()
+    wet = mask.bool().cpu().numpy()
+    e = rel(host(nn32)[1:-1].astype(np.float64), host(nn64)[1:-1], wet)
+    print(f"NN from FP64 tracers in float arithmetic: {e:.2e}")
+    assert e < 1e-5
+    assert plane > 0

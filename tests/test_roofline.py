@@ -22,7 +22,13 @@ def test_fp64_3d_bytes_per_cell_match_the_per_call_rule():
 def test_mixed_form_stores_less_and_2d_loop_is_form_independent():
     f = roofline.step_bytes(400, 300, 40, "fp64")
     m = roofline.step_bytes(400, 300, 40, "mixed")
-    assert m["3d"] < f["3d"]
+    m32 = roofline.step_bytes(400, 300, 40, "mixed", tracer_storage="float32")
+    assert m32["3d"] < m["3d"] < f["3d"]
+    # FP64 tracer storage: 8 more bytes per tracer read and write in each of
+    # the five advection passes and the diffusion, plus the tracers and NN of
+    # the density and buoyancy-frequency calls
+    cells = 400 * 300 * 40
+    assert (m["3d"] - m32["3d"]) / cells == pytest.approx(2 * (5 * 8 + 8) + 2 * 4 + 3 * 4)
     assert m["2d"] == f["2d"]  # every 2D field is float64 in both forms
     assert m["total"] == pytest.approx(m["3d"] + m["2d"])
     # the substep loop: split copies of the per-substep 2D bytes

@@ -98,6 +98,9 @@ _SIGS = {
     "getm_mean_transports": "lppdpps",
     "getm_slow_friction": "lpppppppps",
     "getm_velocities_3d_bottom_f32": "llpppppppps",
+    "getm_keps_default_params": "p",
+    "getm_keps_advance": "iiiiipdpppppppppppppps",
+    "getm_keps_advance_f32": "iiiiipdpppppppppppppps",
     "getm_tune_set": "ii",
     "getm_tune_get": "ip",
     "getm_coriolis_espelid": "iiiiipppppppis",

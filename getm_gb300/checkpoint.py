@@ -58,7 +58,10 @@ def state_tensors(sim) -> Dict[str, torch.Tensor]:
     for g in sim.T.all_grids():
         for k, t in _tensors_of(g, f"grid{g.postfix or 't'}.", seen):
             out[k] = t
-    for prefix, obj in (("sim.", sim), ("momentum.", sim.momentum), ("airsea.", sim.airsea)):
+    objs = [("sim.", sim), ("momentum.", sim.momentum), ("airsea.", sim.airsea)]
+    if getattr(sim, "vertical_mixing", None) is not None:
+        objs.append(("vertical_mixing.", sim.vertical_mixing))
+    for prefix, obj in objs:
         for k, t in _tensors_of(obj, prefix, seen):
             out[k] = t
     for tr in sim.tracers._tracers:

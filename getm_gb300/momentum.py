@@ -52,6 +52,7 @@ class Momentum:
         # False runs each operation as its own kernel
         self.fused_2d = True
         self._v_stream = None  # see _diagnostics_tail
+        self._bottom_event = torch.cuda.Event() if torch.cuda.is_available() else None
         self._ob = None  # open-boundary operations (set by the simulation)
 
     # ------------------------------------------------------------------ setup
@@ -337,6 +338,9 @@ class Momentum:
             self.bottom_friction(self.u_bot, self.v_bot, self.hU_bot, self.hV_bot, self.rru, self.rrv)
         _pygetm.bottom_shear_velocity(self.u_bot, self.v_bot, self.rru, self.rrv, self.ustar2_bx, self.ustar2_by,
                                       self.ustar_b)
+        # SS and ustar_b are ready: a turbulence closure on another stream
+        # may start from here
+        self._bottom_event.record()
         # advpk = uk, advqk = vk and the velocities on the advection grids
         # (the interpolations below, all at once)
         _pygetm.momentum_3d_advection_inputs(self.uk, self.vk, self.ww, self.uua3d, self.uva3d, self.vua3d,

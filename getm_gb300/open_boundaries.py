@@ -286,6 +286,7 @@ class DeviceBoundaries:
         self.np = ob.np
         self.i, self.j = it(ob.i), it(ob.j)
         self.type_2d, self.type_3d = it(ob.type_2d), it(ob.type_3d)
+        self.type_zero_gradient = it(np.full(ob.np, ZERO_GRADIENT))
         self.di, self.dj, self.side = it(ob.di), it(ob.dj), it(ob.side)
         self.sign = torch.from_numpy(ob.inflow_sign.astype(float)).to(dev)
         self.ranges = [(b.start, b.stop) for b in ob]
@@ -363,6 +364,24 @@ class DeviceBoundaries:
             if n:
                 _lib.call("getm_open_boundary_depth", n, src.data_ptr(), tgt.data_ptr(), _p(z), _p(zo), _p(g.H),
                           _p(g.mask), float(sim.Dmin), float(sim.Dcrit), _p(g._work), _p(g.D), _p(g.alpha), _s())
+
+    def update_zero_gradient(self, field):
+        """ArrayOpenBoundaries.update of an array whose boundaries are all
+        ZERO_GRADIENT (the turbulent viscosity, python/pygetm/vertical_mixing.py:120,186):
+        each boundary point takes the value of its inward neighbour at every
+        level, one boundary after another."""
+        from . import _lib
+        from ._pygetm import _p, _s
+        import torch
+
+        T = self.T
+        t = field.all_values
+        fn = "getm_open_boundary_tracers_f32" if t.dtype == torch.float32 else "getm_open_boundary_tracers"
+        ptr = _lib.ptr_array([t.data_ptr()])
+        for s, e in self.ranges:
+            _lib.call(fn, s, e, self.np, T.nx_, T.ny_, t.shape[0], 0, self.i.data_ptr(), self.j.data_ptr(),
+                      self.type_zero_gradient.data_ptr(), self.di.data_ptr(), self.dj.data_ptr(), _p(T.mask), 1,
+                      ptr, ptr, _s())
 
     def update_tracers(self, tracers):
         from . import _lib

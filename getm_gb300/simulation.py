@@ -111,7 +111,7 @@ class Simulation:
                  Dmin: float = 0.02, Dcrit: float = 0.1, delay_slow_ip: bool = False, num: float = 0.0,
                  nuh: float = 0.0, precision: str = "fp64", fused_2d: bool = True, substep_kernel: bool = True,
                  concurrent_3d: bool = True, tiles=None, tracer_storage: Optional[str] = None,
-                 internal_pressure_arithmetic: Optional[str] = None, device="cuda"):
+                 internal_pressure_arithmetic: Optional[str] = None, vertical_mixing=None, device="cuda"):
         """``precision``: "fp64" (the plain form) or "mixed" (float32 tracers,
         3D velocities and their tendencies and diffusivities; float64
         elevations, depths, layer thicknesses, 2D transports and their
@@ -142,7 +142,12 @@ class Simulation:
         an ulp of the tracer every step; "float32" stores them in float.
         ``internal_pressure_arithmetic``: "float32" (mixed-form default: FP64
         column integrals and differences, float slope corrections) or
-        "float64"."""
+        "float64".  ``vertical_mixing``: None (prescribed ``num``/``nuh``
+        from the arguments of those names) or a
+        ``vertical_mixing.VerticalMixing`` instance such as ``GOTM()`` (the
+        k-epsilon closure), advanced every 3D step after the 3D momentum
+        and before the tracers, as python/pygetm/simulation.py:1107-1115
+        does."""
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.precision = precision
@@ -211,7 +216,16 @@ class Simulation:
         self.fwf = T.array(name="fwf")
         self.fwf.fill(0.0)
         self.tracers = TracerCollection(T, advection_scheme, dtype=dtr)
-        if three_d:
+        self.vertical_mixing = vertical_mixing
+        if three_d and vertical_mixing is not None:
+            vertical_mixing.initialize(T, dtype=d3)
+            vertical_mixing._ob = self._ob
+            self.num, self.nuh = vertical_mixing.num, vertical_mixing.nuh
+            # surface roughness for the turbulence closure (simulation.py:777-784)
+            self.z0s = T.array(name="z0s")
+            self.z0s.fill(0.1)
+            self._NN_zero = T.array(z=INTERFACES, name="NN", dtype=d3, fill=0.0)  # without density
+        elif three_d:
             self.num = T.array(z=INTERFACES, name="num", dtype=d3)
             self.nuh = T.array(z=INTERFACES, name="nuh", dtype=d3)
             self.num.fill(num)
@@ -372,6 +386,15 @@ class Simulation:
             self.momentum.advance(self.macrotimestep, self.split_factor, self.tausxo, self.tausyo, self.dpdxo,
                                   self.dpdyo, self.idpdx, self.idpdy, self.num, side_stream=self._side_stream)
             self._forked = self._side_stream is not None
+            if self.vertical_mixing is not None:
+                # turbulence from ustar_s, z0s, NN at the start of the step and
+                # ustar_b, z0b, SS of the new 3D velocities (simulation.py:1107-1115);
+                # SS and ustar_b come from the side stream
+                if self._forked:
+                    torch.cuda.current_stream(self.T.device).wait_event(self.momentum._bottom_event)
+                NN = self.NN if self.runtype == RunType.BAROCLINIC else self._NN_zero
+                self.vertical_mixing.advance(self.macrotimestep, self.ustar_s, self.momentum.ustar_b, self.z0s,
+                                             self.T.z0b, NN, self.momentum.SS)
             self.tracers.advance(self.macrotimestep, self.momentum.uk, self.momentum.vk, self.momentum.ww, self.nuh)
             if self.runtype == RunType.BAROCLINIC and self.delay_slow_ip:
                 _pygetm.column_sums([(self.idpdx, self.momentum.SxB), (self.idpdy, self.momentum.SyB)])

@@ -688,6 +688,36 @@ int getm_split2d_substep(const getm_split2d_fields* f, int nx, int ny, int halox
                          int uadv_ufirst, getm_advection* vadv, getm_grid* vgrid, getm_grid* vugrid,
                          getm_grid* vvgrid, int vadv_ufirst, cudaStream_t stream);
 
+/* ---- turbulence closure -----------------------------------------------
+ * Replaces the GOTM call of python/pygetm/vertical_mixing.py:150-188
+ * (VerticalMixing GOTM.advance: tke, eps, L, num, nuh at the interfaces
+ * from ustar_s, ustar_b, z0s, z0b, NN and SS, once per 3D step).  GOTM is
+ * external to the reference; this is the buoyancy-extended k-epsilon model
+ * of Rodi (1987) with constant stability functions (num = cm0^4 k^2/eps,
+ * nuh = num/prandtl), log-law Dirichlet values at the bottom and surface
+ * interfaces (k = ustar^2/cm0^2, eps = cm0^3 k^1.5/(kappa z0)), implicit
+ * diffusion of k (num/sig_k) and eps (num/sig_e) with Patankar-linearised
+ * sources, k >= k_min, eps >= eps_min and the Galperin limit L <= galp
+ * sqrt(2k/NN) where NN > 0.  FP64; one thread per water column (mask == 1,
+ * interior); fields are nz + 1 interface planes of nx x ny (halos
+ * included), h has nz layers; work: 2 (nz + 1) nx ny doubles.              */
+typedef struct getm_keps_params {
+    double cm0, kappa, sig_k, sig_e, c1, c2, c3_minus, c3_plus, galp, prandtl, k_min, eps_min;
+} getm_keps_params;
+int getm_keps_default_params(getm_keps_params* p);
+int getm_keps_advance(int nx, int ny, int nz, int halox, int haloy, const getm_keps_params* params,
+                      double timestep, const int* mask, const double* h, const double* ustar_s,
+                      const double* ustar_b, const double* z0s, const double* z0b, const double* NN,
+                      const double* SS, double* tke, double* eps, double* L, double* num, double* nuh,
+                      double* work, cudaStream_t stream);
+/* the mixed form: NN, SS, num and nuh in float (k, eps, L and the
+ * arithmetic stay FP64)                                                     */
+int getm_keps_advance_f32(int nx, int ny, int nz, int halox, int haloy, const getm_keps_params* params,
+                          double timestep, const int* mask, const double* h, const double* ustar_s,
+                          const double* ustar_b, const double* z0s, const double* z0b, const float* NN,
+                          const float* SS, double* tke, double* eps, double* L, float* num, float* nuh,
+                          double* work, cudaStream_t stream);
+
 /* ---- substeps of many domains in one launch ------------------------------
  * No single counterpart in the reference, which advances each domain in its
  * own process: for an ensemble of independent domains (each one

@@ -10,6 +10,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import oracle as O
+from . import turbulence
 
 
 class TracerTransport:
@@ -422,6 +423,14 @@ class BoundaryOps:
         for n, tr in enumerate(tracers):
             self.tracer_values[n] = tr[:, ob.j, ob.i].copy()
 
+    def update_zero_gradient(self, field):
+        """ArrayOpenBoundaries.update of an array whose boundaries are all
+        ZERO_GRADIENT (num, python/pygetm/vertical_mixing.py:120,186)."""
+        ob = self.ob
+        for s, e in self.ranges:
+            i, j, di, dj = ob.i[s:e], ob.j[s:e], ob.di[s:e], ob.dj[s:e]
+            field[:, j, i] = field[:, j + dj, i + di]
+
     def update_tracers(self, tracers):
         ob, T = self.ob, self.T
         n_sp = ob.sponge_n
@@ -447,7 +456,11 @@ class Simulation:
     (BAROCLINIC or BAROTROPIC_3D), matching getm_gb300.simulation.Simulation."""
 
     def __init__(self, T_host, dga, runtype=4, scheme=5, Dmin=0.02, Dcrit=0.1, num=0.0, nuh=0.0, taux=0.0, tauy=0.0,
-                 sp=101325.0, internal_pressure="shchepetkin_mcwilliams", momentum=None):
+                 sp=101325.0, internal_pressure="shchepetkin_mcwilliams", momentum=None, keps=None):
+        """keps: None (prescribed num and nuh) or a dict of k-epsilon
+        parameters (empty for the defaults): num and nuh from the closure of
+        turbulence.keps_advance, advanced after the 3D momentum
+        (python/pygetm/simulation.py:1107-1115)."""
         self.runtype = runtype
         self.dga = np.asarray(dga, dtype=float)[:, None, None]
         self.T = T = O.make_grids(T_host)
@@ -476,6 +489,16 @@ class Simulation:
         self.num = _arr(T, T.nz + 1); _fill(self.num, T, num)
         self.nuh = _arr(T, T.nz + 1); _fill(self.nuh, T, nuh)
         self.ustar_s = _arr(T, fill=0.0)
+        self.keps = None if keps is None else dict(keps)
+        if self.keps is not None:
+            # GOTM-style start: k = k_min, eps = eps_min everywhere
+            self.tke, self.eps, self.L, nu_m, nu_h = turbulence.initial_state(T.nz, T.mask.shape, self.keps)
+            for a in (self.tke, self.eps, self.L):  # Array.fill: land gets the fill value
+                a[..., T.land] = FILL
+            _fill(self.num, T, nu_m)
+            _fill(self.nuh, T, nu_h)
+            self.z0s = _arr(T, fill=0.1)
+            self.NN = _arr(T, T.nz + 1, 0.0)
         self.tausxo, self.tausyo = np.zeros_like(self.tausx), np.zeros_like(self.tausy)
         self.dpdxo, self.dpdyo = np.zeros_like(self.dpdx), np.zeros_like(self.dpdy)
         self.adv = O.Advection(T, scheme)
@@ -550,6 +573,11 @@ class Simulation:
             self.update_depth(True)
             m.advance(T, self.macrotimestep, self.split_factor, self.tausxo, self.tausyo, self.dpdxo, self.dpdyo,
                       self.idpdx, self.idpdy, self.num)
+            if self.keps is not None:
+                turbulence.keps_advance(T, self.macrotimestep, T.hn, self.ustar_s, m.ustar_b, self.z0s, T.z0b,
+                                        self.NN, m.SS, self.tke, self.eps, self.L, self.num, self.nuh, self.keps)
+                if self.ob is not None:
+                    self.ob.update_zero_gradient(self.num)
             if self.tracers:
                 self.adv.apply_3d_batch(m.uk, m.vk, m.ww, self.macrotimestep, self.tracers)
                 avmol = -1.0
@@ -567,6 +595,9 @@ class Simulation:
         if self.runtype == 4 and macro_active:
             with np.errstate(all="ignore"):
                 self.rho[...], self.buoy[...] = seos_buoyancy(self.salt, self.temp, self.depth)
+                if self.keps is not None:
+                    N2 = seos_nsquared(T.mask, T.hn, self.depth, self.salt, self.temp)
+                    self.NN[1:T.nz] = np.where(T.mask[None] != 0, N2, self.NN[1:T.nz])
             if self.internal_pressure_method == "blumberg_mellor":
                 O.blumberg_mellor(T, self.buoy, self.idpdx, self.idpdy)
             else:

@@ -69,10 +69,12 @@ _SIGS = {
     "getm_multiply_add": "ippds",
     "getm_advance_surface_elevation": "iiiippppppppds",
     "getm_surface_pressure_gradient": "iiiiiippppppppdpps",
+    "getm_surface_pressure_gradient_mixed": "iiiiiippppppppdpps",
     "getm_horizontal_diffusion": "iiiiiippppppppppdpps",
     "getm_bottom_friction": "iippppppdpis",
     "getm_bottom_friction_mixed": "iippppppdpis",
     "getm_update_depth_2d": "iidd" + "p" * 25 + "s",
+    "getm_update_depth_2d_mixed": "iidd" + "p" * 25 + "s",
     "getm_momentum_2d_velocities": "iii" + "p" * 16 + "s",
     "getm_momentum_2d_friction": "iii" + "p" * 12 + "s",
     "getm_coriolis_2d": "iiiipppis",

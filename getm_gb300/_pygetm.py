@@ -191,14 +191,15 @@ def advance_surface_elevation(timestep, z, U, V, fwf):
          _p(g.iarea), _p(z), _p(U), _p(V), _p(fwf), float(timestep), _s())
 
 
-def surface_pressure_gradient(z, sp, dpdx, dpdy, Dmin):
-    """pyx:525-539"""
+def surface_pressure_gradient(z, sp, dpdx, dpdy, Dmin, mixed=False):
+    """pyx:525-539 (mixed: the mixed-form arithmetic, getm_surface_pressure_gradient_mixed)"""
     g = z.grid
     assert not z.z, "z"
     assert sp.grid is g and not sp.z, "sp"
     assert dpdx.grid is g.ugrid and not dpdx.z, "dpdx"
     assert dpdy.grid is g.vgrid and not dpdy.z, "dpdy"
-    call("getm_surface_pressure_gradient", g.nx_, g.ny_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
+    fn = "getm_surface_pressure_gradient_mixed" if mixed else "getm_surface_pressure_gradient"
+    call(fn, g.nx_, g.ny_, g.halox + 1, g.halox + g.nx, g.haloy + 1, g.haloy + g.ny,
          _p(dpdx.grid.mask), _p(dpdy.grid.mask), _p(dpdx.grid.idx), _p(dpdy.grid.idy), _p(z), _p(sp), _p(g.H), _p(g.D),
          float(Dmin), _p(dpdx), _p(dpdy), _s())
 
@@ -258,12 +259,14 @@ def new_handle():
 # fused sequences of the 2D substep (no single counterpart in the reference;
 # each replaces the operations named in its docstring with one launch)
 # ---------------------------------------------------------------------------
-def update_depth_2d(T, z, zo, Dmin, Dcrit):
+def update_depth_2d(T, z, zo, Dmin, Dcrit, mixed=False):
     """Simulation.update_depth, 2D part (simulation.py:1498-1586):
     elevation2depth on T, Dclip, z_T_half and its interpolation to U, V, X,
-    depths and alpha there, D_T_half and the UU/VV/UV/VU depth copies."""
+    depths and alpha there, D_T_half and the UU/VV/UV/VU depth copies
+    (mixed: alpha in float, getm_update_depth_2d_mixed)."""
     U, V, X = T.ugrid, T.vgrid, T.xgrid
-    call("getm_update_depth_2d", T.nx_, T.ny_, float(Dmin), float(Dcrit), _p(z), _p(zo), _p(T.H), _p(U.H), _p(V.H),
+    fn = "getm_update_depth_2d_mixed" if mixed else "getm_update_depth_2d"
+    call(fn, T.nx_, T.ny_, float(Dmin), float(Dcrit), _p(z), _p(zo), _p(T.H), _p(U.H), _p(V.H),
          _p(X.H), _p(T.mask), _p(U.mask), _p(V.mask), _p(X.mask), _p(T.D), _p(T.Dclip), _p(T._work), _p(U._work),
          _p(U.D), _p(U.alpha), _p(V._work), _p(V.D), _p(V.alpha), _p(X._work), _p(X.D), _p(U.ugrid.D),
          _p(V.vgrid.D), _p(U.vgrid.D), _p(V.ugrid.D), _s())

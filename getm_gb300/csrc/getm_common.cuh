@@ -165,6 +165,59 @@ __device__ __forceinline__ double getm_pow2_scale_down(double x)
 __device__ __forceinline__ double getm_half(double x) { return getm_pow2_scale_down<1>(x); }
 __device__ __forceinline__ double getm_quarter(double x) { return getm_pow2_scale_down<2>(x); }
 
+// The rest x - getm_f2d(getm_d2f_approx(x)) as a float, on the integer pipe:
+// the truncated head keeps the top 24 significant bits of x, so the rest is
+// the low 29 bits of the mantissa at the scale of x's last bit (rounded to 24
+// bits by the conversion).  |x| below 2^-74 or beyond the float range: the
+// FP64 subtraction.
+__device__ __forceinline__ float getm_d2f_rest(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ffu) - 1023;
+    if (e < -74 || e > 127) return getm_d2f_approx(x - getm_f2d(getm_d2f_approx(x)));
+    const float r = __uint2float_rn((unsigned int)b & 0x1fffffffu) * __uint_as_float((unsigned int)(e + 75) << 23);
+    return (b >> 63) ? -r : r;
+}
+
+// Comparisons of doubles on the integer pipe, for the mixed form: GB300
+// issues an FP64 instruction (compare, min and max included) at a small
+// fraction of the integer rate, and these give the same values.
+// getm_dkey maps a double to a signed 64-bit key whose order is the numeric
+// order of all non-NaN doubles (-0 orders below +0): the magnitude bits of
+// a negative value are inverted.
+__device__ __forceinline__ long long getm_dkey(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b ^ (long long)((unsigned long long)(b >> 63) >> 1);
+}
+
+__device__ __forceinline__ bool getm_isnan_i(double x)
+{
+    return ((unsigned long long)__double_as_longlong(x) << 1) > (0x7ff0000000000000ull << 1);
+}
+
+// fmax / fmin semantics (a NaN operand yields the other one)
+__device__ __forceinline__ double getm_fmax_i(double a, double b)
+{
+    if (getm_isnan_i(a)) return b;
+    if (getm_isnan_i(b)) return a;
+    return getm_dkey(a) >= getm_dkey(b) ? a : b;
+}
+
+__device__ __forceinline__ double getm_fmin_i(double a, double b)
+{
+    if (getm_isnan_i(a)) return b;
+    if (getm_isnan_i(b)) return a;
+    return getm_dkey(a) <= getm_dkey(b) ? a : b;
+}
+
+// x > 0.0 (false for NaN)
+__device__ __forceinline__ bool getm_positive_i(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7ff0000000000000ll;
+}
+
 // num / den in FP64 to about 2^-46 relative (not correctly rounded), for the
 // mixed form: the float reciprocal of den refined by one Newton-Raphson step
 // (q0 = num r, q = q0 + r (num - q0 den)), three FP64 instructions instead of

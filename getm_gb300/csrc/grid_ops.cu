@@ -356,12 +356,27 @@ extern "C" int getm_advance_surface_elevation(int nx, int ny, int halox, int hal
 }
 
 // wrapper.F90:525-565; C bounds from Fortran 1-based imin..jmax
+template <bool MIXED>
 __global__ void spg_kernel(int nx, int ny, int ilo, int ihi, int jlo, int jhi, SpgArgs a)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i < ilo || i > ihi || j < jlo || j > jhi) return;
-    spg_point(a, (long long)j * nx + i);
+    spg_point<MIXED>(a, (long long)j * nx + i);
+}
+
+template <bool MIXED>
+static int spg_impl(int nx, int ny, int imin, int imax, int jmin, int jmax, const int* umask, const int* vmask,
+                    const double* idxu, const double* idyv, const double* z, const double* sp, const double* H,
+                    const double* D, double Dmin, double* dpdx, double* dpdy, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || imin < 1 || jmin < 1 || imax >= nx || jmax >= ny) return GETM_ERR_ARG;
+    if (!umask || !vmask || !idxu || !idyv || !z || !sp || !H || !D || !dpdx || !dpdy) return GETM_ERR_ARG;
+    dim3 grid(getm_div_up(nx, 128), ny);
+    SpgArgs a{nx, umask, vmask, idxu, idyv, z, sp, H, D, Dmin, dpdx, dpdy};
+    spg_kernel<MIXED><<<grid, 128, 0, stream>>>(nx, ny, imin - 1, imax - 1, jmin - 1, jmax - 1, a);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
 }
 
 extern "C" int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax, int jmin, int jmax,
@@ -370,13 +385,18 @@ extern "C" int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax
                                               const double* H, const double* D, double Dmin,
                                               double* dpdx, double* dpdy, cudaStream_t stream)
 {
-    if (nx < 1 || ny < 1 || imin < 1 || jmin < 1 || imax >= nx || jmax >= ny) return GETM_ERR_ARG;
-    if (!umask || !vmask || !idxu || !idyv || !z || !sp || !H || !D || !dpdx || !dpdy) return GETM_ERR_ARG;
-    dim3 grid(getm_div_up(nx, 128), ny);
-    SpgArgs a{nx, umask, vmask, idxu, idyv, z, sp, H, D, Dmin, dpdx, dpdy};
-    spg_kernel<<<grid, 128, 0, stream>>>(nx, ny, imin - 1, imax - 1, jmin - 1, jmax - 1, a);
-    GETM_CHECK_LAUNCH();
-    return GETM_OK;
+    return spg_impl<false>(nx, ny, imin, imax, jmin, jmax, umask, vmask, idxu, idyv, z, sp, H, D, Dmin, dpdx, dpdy,
+                           stream);
+}
+
+extern "C" int getm_surface_pressure_gradient_mixed(int nx, int ny, int imin, int imax, int jmin, int jmax,
+                                                    const int* umask, const int* vmask, const double* idxu,
+                                                    const double* idyv, const double* z, const double* sp,
+                                                    const double* H, const double* D, double Dmin,
+                                                    double* dpdx, double* dpdy, cudaStream_t stream)
+{
+    return spg_impl<true>(nx, ny, imin, imax, jmin, jmax, umask, vmask, idxu, idyv, z, sp, H, D, Dmin, dpdx, dpdy,
+                          stream);
 }
 
 // ---------------------------------------------------------------------------

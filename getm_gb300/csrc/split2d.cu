@@ -25,11 +25,11 @@
 
 namespace {
 
-template <int BY>
+template <int BY, bool MIXED>
 __global__ void __launch_bounds__(UD_BX * BY) update_depth_2d_kernel(DepthArgs a)
 {
     __shared__ double szh[BY + 2][UD_BX + 2];
-    update_depth_2d_tile<BY>(a, blockIdx.x, blockIdx.y, threadIdx.x, threadIdx.y, szh);
+    update_depth_2d_tile<BY, MIXED>(a, blockIdx.x, blockIdx.y, threadIdx.x, threadIdx.y, szh);
 }
 
 template <typename C>
@@ -156,12 +156,13 @@ __global__ void __launch_bounds__(S2_THREADS) surface_elevation_fused_kernel(
 
 static inline dim3 plane_grid(int nx, int ny) { return dim3(getm_div_up(nx, S2_THREADS), ny); }
 
-extern "C" int getm_update_depth_2d(int nx, int ny, double Dmin, double Dcrit, const double* z, const double* zo,
-                                    const double* HT, const double* HU, const double* HV, const double* HX,
-                                    const int* mT, const int* mU, const int* mV, const int* mX, double* DT,
-                                    double* DclipT, double* workT, double* workU, double* DU, double* alphaU,
-                                    double* workV, double* DV, double* alphaV, double* workX, double* DX,
-                                    double* DUU, double* DVV, double* DUV, double* DVU, cudaStream_t stream)
+template <bool MIXED>
+static int update_depth_2d_impl(int nx, int ny, double Dmin, double Dcrit, const double* z, const double* zo,
+                                const double* HT, const double* HU, const double* HV, const double* HX, const int* mT,
+                                const int* mU, const int* mV, const int* mX, double* DT, double* DclipT,
+                                double* workT, double* workU, double* DU, double* alphaU, double* workV, double* DV,
+                                double* alphaV, double* workX, double* DX, double* DUU, double* DVV, double* DUV,
+                                double* DVU, cudaStream_t stream)
 {
     if (nx < 2 || ny < 2) return GETM_ERR_ARG;
     const void* ptrs[] = {z, zo, HT, HU, HV, HX, mT, mU, mV, mX, DT, DclipT, workT, workU, DU, alphaU,
@@ -173,9 +174,32 @@ extern "C" int getm_update_depth_2d(int nx, int ny, double Dmin, double Dcrit, c
     constexpr int BY = 4;
     dim3 block(UD_BX, BY);
     dim3 grid(getm_div_up(nx + 1, UD_BX), getm_div_up(ny + 1, BY));
-    update_depth_2d_kernel<BY><<<grid, block, 0, stream>>>(a);
+    update_depth_2d_kernel<BY, MIXED><<<grid, block, 0, stream>>>(a);
     GETM_CHECK_LAUNCH();
     return GETM_OK;
+}
+
+extern "C" int getm_update_depth_2d(int nx, int ny, double Dmin, double Dcrit, const double* z, const double* zo,
+                                    const double* HT, const double* HU, const double* HV, const double* HX,
+                                    const int* mT, const int* mU, const int* mV, const int* mX, double* DT,
+                                    double* DclipT, double* workT, double* workU, double* DU, double* alphaU,
+                                    double* workV, double* DV, double* alphaV, double* workX, double* DX,
+                                    double* DUU, double* DVV, double* DUV, double* DVU, cudaStream_t stream)
+{
+    return update_depth_2d_impl<false>(nx, ny, Dmin, Dcrit, z, zo, HT, HU, HV, HX, mT, mU, mV, mX, DT, DclipT, workT,
+                                       workU, DU, alphaU, workV, DV, alphaV, workX, DX, DUU, DVV, DUV, DVU, stream);
+}
+
+extern "C" int getm_update_depth_2d_mixed(int nx, int ny, double Dmin, double Dcrit, const double* z,
+                                          const double* zo, const double* HT, const double* HU, const double* HV,
+                                          const double* HX, const int* mT, const int* mU, const int* mV,
+                                          const int* mX, double* DT, double* DclipT, double* workT, double* workU,
+                                          double* DU, double* alphaU, double* workV, double* DV, double* alphaV,
+                                          double* workX, double* DX, double* DUU, double* DVV, double* DUV,
+                                          double* DVU, cudaStream_t stream)
+{
+    return update_depth_2d_impl<true>(nx, ny, Dmin, Dcrit, z, zo, HT, HU, HV, HX, mT, mU, mV, mX, DT, DclipT, workT,
+                                      workU, DU, alphaU, workV, DV, alphaV, workX, DX, DUU, DVV, DUV, DVU, stream);
 }
 
 extern "C" int getm_momentum_2d_velocities(int nx, int ny, int mixed, const double* U, const double* V,

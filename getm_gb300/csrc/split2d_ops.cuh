@@ -17,6 +17,29 @@
 // torch.clamp(x, min=lo): NaN propagates
 __device__ __forceinline__ double clamp_min(double x, double lo) { return isnan(x) ? x : (x < lo ? lo : x); }
 
+// The same values with the comparisons on the integer pipe (I: the mixed
+// form) or on the FP64 pipe (the FP64 form, as written in the reference)
+template <bool I>
+__device__ __forceinline__ double dmax(double a, double b)
+{
+    if constexpr (I) return getm_fmax_i(a, b);
+    else return fmax(a, b);
+}
+
+template <bool I>
+__device__ __forceinline__ double dmin(double a, double b)
+{
+    if constexpr (I) return getm_fmin_i(a, b);
+    else return fmin(a, b);
+}
+
+template <bool I>
+__device__ __forceinline__ double dclamp_min(double x, double lo)
+{
+    if constexpr (I) return getm_isnan_i(x) ? x : (getm_dkey(x) < getm_dkey(lo) ? lo : x);
+    else return clamp_min(x, lo);
+}
+
 struct DepthArgs {
     int nx, ny;                 // T-grid extents (halos included)
     double Dmin, Dcrit, ialpha; // ialpha = 1 / (Dcrit - 2 Dmin)
@@ -38,6 +61,13 @@ __device__ __forceinline__ double alpha_of(double d, double twoDmin, double ialp
     return fmax(0.0, fmin(1.0, (d - twoDmin) * ialpha));
 }
 
+// ... in float, for the mixed form: alpha is a weight between 0 and 1 that
+// the mixed transport update reads as a float
+__device__ __forceinline__ double alpha_of_f(double d, float twoDmin, float ialpha)
+{
+    return getm_f2d(fmaxf(0.f, fminf(1.f, (getm_d2f_approx(d) - twoDmin) * ialpha)));
+}
+
 // Simulation.update_depth, 2D part (simulation.py:1498-1586 without the
 // halo exchanges and mirroring of a single closed domain).  A 32 x BY block
 // covers X points (j, i) of its tile and the T, U, V points with the same
@@ -45,7 +75,9 @@ __device__ __forceinline__ double alpha_of(double d, double twoDmin, double ialp
 // shared memory.  Copies between grids are scattered by the point that
 // owns the source value (UU.D(j, i-1) = D_T_half(j, i), VV.D(j-1, i) =
 // D_T_half(j, i), UV.D(j-1, i-1) = VU.D(j-1, i-1) = X.D(j, i)).
-template <int BY>
+// MIXED: minima, maxima and clamps on the integer pipe (the same values) and
+// alpha in float (alpha_of_f); the sums stay FP64.
+template <int BY, bool MIXED = false>
 __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx, int by, int tx, int ty,
                                                      double (&szh)[BY + 2][UD_BX + 2])
 {
@@ -93,7 +125,7 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
         }
         double dx = DX0;
         if (mX != 0) {
-            dx = fmax(HX + zx, a.Dmin);
+            dx = dmax<MIXED>(HX + zx, a.Dmin);
             a.DX[px] = dx;
         }
         if (j >= 1 && i >= 1 && j - 1 < ny && i - 1 < nx) {  // UV.D = X.D[1:, 1:]; VU.D = UV.D
@@ -106,14 +138,15 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
     const double zh = szh[sj][si];
     // T: elevation2depth(z, H, -1000), Dclip = clamp(D, Dmin), D_T_half
     double DT = DT0;
-    if (mT != 0) DT = fmax(HT + zT, -1000.0);
+    if (mT != 0) DT = dmax<MIXED>(HT + zT, -1000.0);
     a.DT[p] = DT;
-    a.DclipT[p] = clamp_min(DT, a.Dmin);
-    const double dth = mT != 0 ? fmax(HT + zh, a.Dmin) : zh;
+    a.DclipT[p] = dclamp_min<MIXED>(DT, a.Dmin);
+    const double dth = mT != 0 ? dmax<MIXED>(HT + zh, a.Dmin) : zh;
     a.workT[p] = dth;
     if (i >= 1) a.DUU[p - 1] = dth;   // UU.D[:, :-1] = D_T_half[:, 1:]
     if (j >= 1) a.DVV[p - nx] = dth;  // VV.D[:-1, :] = D_T_half[1:, :]
     const double twoDmin = 2 * a.Dmin;
+    const float twoDmin_f = 2.f * getm_d2f_approx(a.Dmin), ialpha_f = getm_d2f_approx(a.ialpha);
     // U: z_U = interp_x(z_T_half, ioffset 0) for i < nx-1, else the old value
     double zu;
     if (i < nx - 1) {
@@ -123,9 +156,9 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
         zu = workU0;
     }
     if (mU != 0) {
-        const double d = fmax(HU + zu, a.Dmin);
+        const double d = dmax<MIXED>(HU + zu, a.Dmin);
         a.DU[p] = d;
-        a.alphaU[p] = alpha_of(d, twoDmin, a.ialpha);
+        a.alphaU[p] = MIXED ? alpha_of_f(d, twoDmin_f, ialpha_f) : alpha_of(d, twoDmin, a.ialpha);
     }
     // V: z_V = interp_y(z_T_half, joffset 0) for j < ny-1
     double zv;
@@ -136,9 +169,9 @@ __device__ __forceinline__ void update_depth_2d_tile(const DepthArgs& a, int bx,
         zv = workV0;
     }
     if (mV != 0) {
-        const double d = fmax(HV + zv, a.Dmin);
+        const double d = dmax<MIXED>(HV + zv, a.Dmin);
         a.DV[p] = d;
-        a.alphaV[p] = alpha_of(d, twoDmin, a.ialpha);
+        a.alphaV[p] = MIXED ? alpha_of_f(d, twoDmin_f, ialpha_f) : alpha_of(d, twoDmin, a.ialpha);
     }
 }
 
@@ -363,7 +396,7 @@ __device__ __forceinline__ TransportNew transport_2d_mixed_value(const Transport
     if (m != 1) return TransportNew{Up, false};
     const float rho0i = (float)(1.0 / GETM_RHO0);
     const float sf = getm_d2f_approx(SFp);
-    const float Slr = (Up > 0.0) ? fminf(sf, 0.f) : fmaxf(sf, 0.f);
+    const float Slr = getm_positive_i(Up) ? fminf(sf, 0.f) : fmaxf(sf, 0.f);
     const float Dp = getm_d2f_approx(Dd);
     const float dtf = (float)dt;
     const float tend = -(float)GETM_G * Dp * getm_d2f_approx(dpp) +
@@ -436,6 +469,10 @@ struct SpgArgs {
     double *dpdx, *dpdy;
 };
 
+// MIXED: the elevation bounds on the integer pipe, the two differences in
+// FP64 and the rest in float (the mixed transport update reads the gradient
+// as a float).
+template <bool MIXED = false>
 __device__ __forceinline__ void spg_point(const SpgArgs& a, long long p)
 {
     const int nx = a.nx;
@@ -447,6 +484,22 @@ __device__ __forceinline__ void spg_point(const SpgArgs& a, long long p)
     const double D0 = a.D[p], D1 = a.D[p + 1], Dn = a.D[p + nx];
     const double sp0 = a.sp[p], sp1 = a.sp[p + 1], spn = a.sp[p + nx];
     const double idx = a.idxu[p], idy = a.idyv[p];
+    if constexpr (MIXED) {
+        const float gi = (float)(1.0 / (GETM_G * GETM_RHO0));
+        if (mu == 1) {
+            const double zp = getm_fmax_i(z1, -H0 + getm_fmin_i(a.Dmin, D1));
+            const double zm = getm_fmax_i(z0, -H1 + getm_fmin_i(a.Dmin, D0));
+            const float g = getm_d2f_approx(zp - zm) + getm_d2f_approx(sp1 - sp0) * gi;
+            a.dpdx[p] = getm_f2d(g * getm_d2f_approx(idx));
+        }
+        if (mv == 1) {
+            const double zp = getm_fmax_i(zn, -H0 + getm_fmin_i(a.Dmin, Dn));
+            const double zm = getm_fmax_i(z0, -Hn + getm_fmin_i(a.Dmin, D0));
+            const float g = getm_d2f_approx(zp - zm) + getm_d2f_approx(spn - sp0) * gi;
+            a.dpdy[p] = getm_f2d(g * getm_d2f_approx(idy));
+        }
+        return;
+    }
     if (mu == 1) {
         double zp = fmax(z1, -H0 + fmin(a.Dmin, D1));
         double zm = fmax(z0, -H1 + fmin(a.Dmin, D0));

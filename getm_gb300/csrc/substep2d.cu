@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
     {
         const int ntx = div_up(nx + 1, UD_BX), nty = div_up(ny + 1, SS_BY);
         for (int t = blockIdx.x; t < ntx * nty; t += gridDim.x) {
-            update_depth_2d_tile<SS_BY>(a.depth, t % ntx, t / ntx, tx, ty, sm.szh);
+            update_depth_2d_tile<SS_BY, MIXED>(a.depth, t % ntx, t / ntx, tx, ty, sm.szh);
             __syncthreads();
         }
     }
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
         momentum_2d_velocities_point<C>(a.vel, i, j);
         a.advD[0][p] = a.Dsrc[0][p];
         a.advD[1][p] = a.Dsrc[1][p];
-        if (i >= ilo && i <= ihi && j >= jlo && j <= jhi) spg_point(a.spg, p);
+        if (i >= ilo && i <= ihi && j >= jlo && j <= jhi) spg_point<MIXED>(a.spg, p);
     }
     if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
     // 6: bottom friction; first advection passes
@@ -535,7 +535,7 @@ __device__ void batch_item(const BatchMember& m, int ph, int q, int ufirst, Subs
         break;
     case 3:
         if (q < m.dtiles) {
-            update_depth_2d_tile<SS_BY>(a.depth, q % m.dntx, q / m.dntx, tx, ty, sm.szh);
+            update_depth_2d_tile<SS_BY, MIXED>(a.depth, q % m.dntx, q / m.dntx, tx, ty, sm.szh);
             __syncthreads();
         } else if (point(q - m.dtiles, p, i, j)) {
             a.fwf[p] = a.pe[p];
@@ -548,7 +548,7 @@ __device__ void batch_item(const BatchMember& m, int ph, int q, int ufirst, Subs
             momentum_2d_velocities_point<C>(a.vel, i, j);
             a.advD[0][p] = a.Dsrc[0][p];
             a.advD[1][p] = a.Dsrc[1][p];
-            if (interior(i, j)) spg_point(a.spg, p);
+            if (interior(i, j)) spg_point<MIXED>(a.spg, p);
         }
         break;
     case 5: {

@@ -230,6 +230,7 @@ class Simulation:
             self.nuh = T.array(z=INTERFACES, name="nuh", dtype=d3)
             self.num.fill(num)
             self.nuh.fill(nuh)
+        if three_d:
             self.ustar_s = T.array(fill=0.0, name="ustar_s")
             self.tausxo = self.U.array(fill_value=None)
             self.tausyo = self.V.array(fill_value=None)
@@ -517,7 +518,8 @@ class Simulation:
 
     def update_surface_pressure_gradient(self, z: Array, sp: Array):
         """simulation.py:1488-1489"""
-        _pygetm.surface_pressure_gradient(z, sp, self.dpdx, self.dpdy, self.Dmin)
+        _pygetm.surface_pressure_gradient(z, sp, self.dpdx, self.dpdy, self.Dmin,
+                                          mixed=self.precision == "mixed")
 
     def _sigma(self, grid):
         """Sigma.__call__ on one grid (vertical_coordinates.py:106-113)."""
@@ -536,7 +538,7 @@ class Simulation:
         else:
             z_T, zo_T = T.z, T.zo
         if self.fused_2d:
-            _pygetm.update_depth_2d(T, z_T, zo_T, self.Dmin, self.Dcrit)
+            _pygetm.update_depth_2d(T, z_T, zo_T, self.Dmin, self.Dcrit, mixed=self.precision == "mixed")
         else:
             self._update_depth_2d_ops(z_T, zo_T)
         if self._ob is not None:

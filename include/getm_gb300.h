@@ -198,6 +198,14 @@ int getm_surface_pressure_gradient(int nx, int ny, int imin, int imax, int jmin,
                                    const double* idyv, const double* z, const double* sp,
                                    const double* H, const double* D, double Dmin, double* dpdx,
                                    double* dpdy, cudaStream_t stream);
+/* The same, mixed form: elevation bounds compared on the integer pipe, the
+ * elevation and air-pressure differences in FP64, the rest in float (the
+ * mixed transport update reads the gradient as a float).                   */
+int getm_surface_pressure_gradient_mixed(int nx, int ny, int imin, int imax, int jmin, int jmax,
+                                         const int* umask, const int* vmask, const double* idxu,
+                                         const double* idyv, const double* z, const double* sp,
+                                         const double* H, const double* D, double Dmin, double* dpdx,
+                                         double* dpdy, cudaStream_t stream);
 
 /* ---- python/src/momentum.F90 --------------------------------------------- */
 /* c_horizontal_diffusion: momentum.F90:12-77 (pyx:50) */
@@ -471,6 +479,14 @@ int getm_update_depth_2d(int nx, int ny, double Dmin, double Dcrit, const double
                          double* DclipT, double* workT, double* workU, double* DU, double* alphaU,
                          double* workV, double* DV, double* alphaV, double* workX, double* DX,
                          double* DUU, double* DVV, double* DUV, double* DVU, cudaStream_t stream);
+/* The same, mixed form: the same depths (minima, maxima and clamps on the
+ * integer pipe) and alpha evaluated in float.                              */
+int getm_update_depth_2d_mixed(int nx, int ny, double Dmin, double Dcrit, const double* z, const double* zo,
+                               const double* HT, const double* HU, const double* HV, const double* HX,
+                               const int* mT, const int* mU, const int* mV, const int* mX, double* DT,
+                               double* DclipT, double* workT, double* workU, double* DU, double* alphaU,
+                               double* workV, double* DV, double* alphaV, double* workX, double* DX,
+                               double* DUU, double* DVV, double* DUV, double* DVU, cudaStream_t stream);
 /* Momentum._transport_2d_momentum up to its advection calls
  * (python/pygetm/momentum.py:1017-1040): u1 = U/DU, v1 = V/DV, advU = u1,
  * advV = v1, and uua, uva, vua, vva = interpolated transports over the

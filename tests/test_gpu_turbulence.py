@@ -1,9 +1,11 @@
 """The k-epsilon closure on the GPU (getm_keps_advance) against its CPU
-restatement (oracle/turbulence.py) on random columns, FP64 (1e-11 relative
-per field after several steps: the GPU contracts multiply-adds) and with
-float NN, SS, num, nuh (1e-5); and a wind-driven simulation with the
-closure: finite, positive viscosity, and the same state, bit for bit, with
-the 3D step on one stream or three."""
+restatement (oracle/turbulence.py) on random columns, FP64 (within 100 times
+the oracle's own response to a 2-ulp input perturbation: the GPU contracts
+multiply-adds) and with float NN, SS, num, nuh (1e-5); a wind-driven,
+stratified tidal channel with the closure against the oracle simulation;
+and a wind-driven simulation with the closure: finite, positive viscosity,
+and the same state, bit for bit, with the 3D step on one stream or
+three."""
 
 import numpy as np
 import pytest
@@ -56,20 +58,32 @@ def test_keps_matches_oracle(dtype):
     def arr(x, z):
         return Array(Td, dev(x).to(td) if z else dev(x), z=z)
 
+    # the same oracle run from a viscosity perturbed by two units in the last
+    # place: these random columns (unstable, strongly sheared) grow k by up to
+    # six orders of magnitude in five steps, which amplifies last-bit
+    # differences such as the GPU's contracted multiply-adds
+    p = {n: x.copy() for n, x in o.items()}
+    p["num"] = p["num"] * (1.0 + 4.4e-16)
     for _ in range(5):
         vm.advance(600.0, arr(us, False), arr(ub, False), arr(z0s, False), arr(z0b, False), arr(NN, INTERFACES),
                    arr(SS, INTERFACES))
-        K.keps_advance(Th, 600.0, h, us, ub, z0s, z0b, NN, SS, o["tke"], o["eps"], o["L"], o["num"], o["nuh"])
-        if dtype == "float32":  # the stored viscosities are float on the GPU
-            o["num"] = o["num"].astype(np.float32).astype(np.float64)
-            o["nuh"] = o["nuh"].astype(np.float32).astype(np.float64)
+        for st in (o, p):
+            K.keps_advance(Th, 600.0, h, us, ub, z0s, z0b, NN, SS, st["tke"], st["eps"], st["L"], st["num"],
+                           st["nuh"])
+            if dtype == "float32":  # the stored viscosities are float on the GPU
+                st["num"] = st["num"].astype(np.float32).astype(np.float64)
+                st["nuh"] = st["nuh"].astype(np.float32).astype(np.float64)
     torch.cuda.synchronize()
     sel = np.zeros((Th.ny_, Th.nx_), dtype=bool)
     sel[2:-2, 2:-2] = Th.mask[2:-2, 2:-2] == 1
-    rtol = 1e-11 if dtype == "float64" else 1e-5
     for n in ("tke", "eps", "L", "num", "nuh"):
+        a, b = o[n][:, sel], p[n][:, sel]
+        spread = float(np.abs(a - b).max() / np.abs(a).max())
+        # FP64: 100 times the oracle's own response to the perturbation (at
+        # least 1e-12); float NN, SS, num and nuh: 1e-5
+        rtol = max(1e-12, 100.0 * spread) if dtype == "float64" else 1e-5
         e = close(host(getattr(vm, n).all_values).astype(np.float64), o[n], rtol, sel)
-        print(f"{n}: {e:.2e}")
+        print(f"{n}: {e:.2e} (oracle 2-ulp spread {spread:.1e})")
 
 
 def _member_sim(concurrent, precision="fp64"):
@@ -156,7 +170,9 @@ def _channel(precision):
     from getm_gb300.vertical_mixing import GOTM
 
     g = Simulation(wl.T, wl.dga, precision=precision, airsea=Fluxes(taux=0.2), vertical_mixing=GOTM())
-    g.temp.all_values.copy_(torch.from_numpy(temp0(wl.T.zc, host(g.temp.all_values).astype(np.float64))))
+    zc = host(g.T.zc.all_values).astype(np.float64)
+    t = torch.from_numpy(temp0(zc, host(g.temp.all_values).astype(np.float64)))
+    g.temp.all_values.copy_(t.to(g.temp.all_values.dtype))
     vm = g.vertical_mixing
     for n, v in dev_state.items():
         a = getattr(vm, n).all_values

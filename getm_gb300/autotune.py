@@ -1,10 +1,10 @@
 """Launch-shape autotuner for the hot kernels.
 
-The library reads four launch-shape knobs at every launch (``getm_tune_set``,
+The library reads five launch-shape knobs at every launch (``getm_tune_set``,
 per host thread): the rows per block of the x advection pass, the rows a warp
 marches in the 3D y pass, the rows of 32 columns per block of the column
-kernels (w pass, float column solve) and the blocks per SM of the one-launch
-2D substep.  The best shapes depend on the domain: a 64 x 64 x 20 member has
+kernels (w pass, float column solve), the blocks per SM of the one-launch
+2D substep and the form of the 3D x pass (four cells or one cell per lane).  The best shapes depend on the domain: a 64 x 64 x 20 member has
 too few columns to fill 152 SMs with 8-row blocks, a 400 x 300 x 40 box has
 plenty.
 
@@ -32,8 +32,10 @@ KNOBS: Dict[str, Tuple[int, Tuple[int, ...]]] = {
     "ymarch_chunk": (1, (16, 32, 64)),
     "column_rows": (2, (1, 2, 4)),
     "substep_blocks_per_sm": (3, (0, 1)),
+    "xpass_vec": (4, (1, 0)),
 }
-DEFAULTS: Dict[str, int] = {"xpass_rows": 8, "ymarch_chunk": 32, "column_rows": 4, "substep_blocks_per_sm": 0}
+DEFAULTS: Dict[str, int] = {"xpass_rows": 8, "ymarch_chunk": 32, "column_rows": 4, "substep_blocks_per_sm": 0,
+                            "xpass_vec": 1}
 CACHE_PATH = Path(__file__).resolve().parent / "tiles.json"
 
 _applied = threading.local()

@@ -204,6 +204,30 @@ __global__ void __launch_bounds__(256) hpass_x_inc_kernel(HPassArgs<S, V> a)
     hpass_x_inc_rows<S, 1, NoEpi, V>(a, blockIdx.x, j, blockIdx.z, threadIdx.x);
 }
 
+// grid (1, ceil(ny_ / rows), nk): warp (ty) of block (0, y, k) sweeps row j = rows y + ty of layer k
+template <typename S, typename V = S>
+__global__ void __launch_bounds__(256) hpass_x_vec_kernel(HPassArgs<S, V> a)
+{
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= a.ny_) return;  // whole warp
+    hpass_x_vec_row<S, V>(a, j, blockIdx.z, threadIdx.x);
+}
+
+// The four-cells-per-lane x pass applies: rows of whole 16-byte vectors and
+// every pointer it reads or writes 16-byte aligned.
+template <typename S, typename V>
+static bool xpass_vec_ok(const HPassArgs<S, V>& a)
+{
+    if (a.nk < 2 || a.nx_ % 4 != 0 || a.ntracer > GETM_MAX_BATCH) return false;
+    auto al = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+    if (!al(a.umask) || !al(a.tmask) || !al(a.dy_f) || !al(a.idx_f) || !al(a.iA_f) || !al(a.u) || !al(a.hu) ||
+        !al(a.h_in) || !al(a.h_out) || (a.Ah && !al(a.Ah)))
+        return false;
+    for (int t = 0; t < a.ntracer; t++)
+        if (!al(a.fin[t]) || !al(a.fout[t])) return false;
+    return true;
+}
+
 template <typename S, typename V = S>
 __global__ void __launch_bounds__(32 * HY_BY) hpass_y_inc_kernel(HPassArgs<S, V> a)
 {
@@ -230,9 +254,14 @@ static int launch_hpass_inc(int direction, HPassArgs<S, V>& a, cudaStream_t stre
     if (direction == 1) {
         const int rows = getm_tune(GETM_TUNE_XPASS_ROWS);
         dim3 block(32, rows);
-        // lane 0 of the first segment handles the face west of cell 0
-        dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up(a.ny_, rows), a.nk);
-        hpass_x_inc_kernel<S, V><<<grid, block, 0, stream>>>(a);
+        if (getm_tune(GETM_TUNE_XPASS_VEC) && xpass_vec_ok(a)) {
+            dim3 grid(1, getm_div_up(a.ny_, rows), a.nk);
+            hpass_x_vec_kernel<S, V><<<grid, block, 0, stream>>>(a);
+        } else {
+            // lane 0 of the first segment handles the face west of cell 0
+            dim3 grid(getm_div_up(a.nx_ + 1, HX_STRIDE), getm_div_up(a.ny_, rows), a.nk);
+            hpass_x_inc_kernel<S, V><<<grid, block, 0, stream>>>(a);
+        }
     } else if (a.nk < 4) {
         // a single plane: too few columns x layers for marching warps to fill
         // the GPU, so blocks of 32 x HY_BY threads cover tiles instead
@@ -419,13 +448,19 @@ __device__ void w_substep_inc(const WPassArgs<S, float>& a, long long c, const f
     const long long P = a.plane;
     const int nz = a.nz;
     const float dtkf = (float)dtk, itf = (float)itersm1, dtf = (float)a.dt;
-    S fkm1[NT], fk[NT], fk1[NT];
+    S fk[NT], fk1[NT];
     float erm[NT];  // erm: e'_{k-1}, interface below, deviation from level k
+    // the differences f[k+1] - f[k] (dk) and f[k] - f[k-1] (dkm1), narrowed:
+    // each is formed once, as the level above's is needed next (the
+    // downwind-side difference f[k+1] - f[k+2] is -(f[k+2] - f[k+1]), the
+    // same bits up to the sign of a zero, which the limiter ignores)
+    float dk[NT], dkm1[NT];
 #pragma unroll
     for (int q = 0; q < NT; q++) {
-        fkm1[q] = S(0);
         fk[q] = fs[q][c];
         fk1[q] = (nz > 1) ? fs[q][c + P] : S(0);
+        dk[q] = (nz > 1) ? inc_f<S>(fk1[q] - fk[q]) : 0.f;
+        dkm1[q] = 0.f;
         erm[q] = 0.f;
     }
     double hk = hs[c], hk1 = (nz > 1) ? hs[c + P] : 0.0;
@@ -453,21 +488,23 @@ __device__ void w_substep_inc(const WPassArgs<S, float>& a, long long c, const f
         hd[c + k * P] = hn;
 #pragma unroll
         for (int q = 0; q < NT; q++) {
+            // differences of neighbouring values in the storage type, then
+            // narrowed (exact for float storage)
+            const float dn = (k + 2 < nz) ? inc_f<S>(fk2[q] - fk1[q]) : 0.f;
             float el = 0.f, er = 0.f;
             if (k < nz - 1) {
-                // differences of neighbouring values in the storage type,
-                // then narrowed (exact for float storage)
-                const float d = inc_f<S>(fk1[q] - fk[q]);
+                const float d = dk[q];
                 float dev;
-                if (W > 0.f) dev = getm_tvd_dev_f(tf, d, inc_f<S>(fk[q] - ((k > 0) ? fkm1[q] : fk[q])));
-                else dev = getm_tvd_dev_f(tf, -d, inc_f<S>(fk1[q] - ((k < nz - 2) ? fk2[q] : fk1[q])));
+                if (W > 0.f) dev = getm_tvd_dev_f(tf, d, dkm1[q]);
+                else dev = getm_tvd_dev_f(tf, -d, -dn);
                 el = W * (W > 0.f ? dev : d + dev);
                 er = W * (W > 0.f ? dev - d : dev);
             }
             fdst[q][c + k * P] =
                 inc_add<S>(fk[q], dtkf * (((wk - W) - (wkm1 - Wm)) * inc_f<S>(fk[q]) - el + erm[q]) / (hkf - dh));
             erm[q] = er;
-            fkm1[q] = fk[q]; fk[q] = fk1[q]; fk1[q] = fk2[q];
+            dkm1[q] = dk[q]; dk[q] = dn;
+            fk[q] = fk1[q]; fk1[q] = fk2[q];
         }
         Wm = W; wkm1 = wk;
         hk = hk1; hk1 = hk2;

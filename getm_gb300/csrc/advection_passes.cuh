@@ -384,6 +384,193 @@ __device__ __forceinline__ void hpass_x_inc_rows(const HPassArgs<S, V>& a, int b
     }
 }
 
+// x pass in increment form with four cells per lane, for the 3D passes.  A
+// warp sweeps one row (layer k, row j) from west to east in chunks of 128
+// cells; lane L of a chunk owns cells i0 + 4L .. i0 + 4L + 3 and their east
+// faces, so every load and store of the lane is one 16-byte vector (two for
+// doubles) at an aligned address (the caller checks nx_ % 4 == 0 and the
+// pointers' alignment).  A face needs the values of the lanes beside it
+// (shuffles), the chunk to the west hands its last face over in registers,
+// and the last lane reads the two cells east of the chunk.  Each difference
+// of neighbouring values is formed once (it serves the face and, in the
+// limiter, both faces beside it: one FP64 subtraction per cell and field
+// instead of two for FP64 storage).  Every face and cell is evaluated with
+// the same expressions as hpass_x_inc_rows, so both give the same bits.
+// Fields are swept two at a time (the thickness is written by the first
+// sweep).
+template <typename T>
+__device__ __forceinline__ void xv_load4(const T* p, T (&o)[4])
+{
+    if constexpr (sizeof(T) == 8) {
+        const double2 a = *reinterpret_cast<const double2*>(p);
+        const double2 b = *reinterpret_cast<const double2*>(p + 2);
+        o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+    } else if constexpr (std::is_same<T, int>::value) {
+        const int4 a = *reinterpret_cast<const int4*>(p);
+        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    } else {
+        const float4 a = *reinterpret_cast<const float4*>(p);
+        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void xv_store4(T* p, const T (&v)[4])
+{
+    if constexpr (sizeof(T) == 8) {
+        *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+        *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+    } else {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+constexpr int XV_CHUNK = 128;
+
+template <typename S, typename V = S>
+__device__ __forceinline__ void hpass_x_vec_row(const HPassArgs<S, V>& a, int j, int k, int lane)
+{
+    constexpr unsigned FULL = 0xffffffffu;
+    const int nx = a.nx_;
+    const long long r2 = (long long)j * nx;
+    const long long r3 = (long long)k * a.plane + r2;
+    const bool jrow = j >= a.jlo && j <= a.jhi;
+    const int ngroup = a.ntracer > 0 ? (a.ntracer + 1) / 2 : 1;
+    for (int g = 0; g < ngroup; g++) {
+        const int t0 = 2 * g;
+        const int nt = a.ntracer - t0 >= 2 ? 2 : a.ntracer - t0;  // 0 with no fields
+        // the west face of the chunk's first cell: the chunk to the west's
+        // last face (nothing west of the row: an inactive face)
+        float cQU = 0.f;
+        int cum = 0;
+        float cd[2] = {0.f, 0.f}, cer[2] = {0.f, 0.f};
+        for (int i0 = 0; i0 < nx; i0 += XV_CHUNK) {
+            const int ib = i0 + 4 * lane;  // the lane's first cell and its east face
+            const bool lin = ib < nx;      // all four cells or none
+            const int ie = i0 + XV_CHUNK;  // the first cell east of the chunk
+            int um[4] = {0, 0, 0, 0}, tm[4] = {0, 0, 0, 0};
+            float dyf[4] = {0.f, 0.f, 0.f, 0.f}, idxf[4] = {0.f, 0.f, 0.f, 0.f}, iaf[4] = {0.f, 0.f, 0.f, 0.f};
+            float ahraw[4] = {0.f, 0.f, 0.f, 0.f};
+            V uraw[4] = {V(0), V(0), V(0), V(0)};
+            double huraw[4] = {0.0, 0.0, 0.0, 0.0}, hold[4] = {0.0, 0.0, 0.0, 0.0};
+            if (lin) {
+                xv_load4(a.umask + r2 + ib, um);
+                xv_load4(a.tmask + r2 + ib, tm);
+                xv_load4(a.dy_f + r2 + ib, dyf);
+                xv_load4(a.idx_f + r2 + ib, idxf);
+                xv_load4(a.iA_f + r2 + ib, iaf);
+                xv_load4(a.u + r3 + ib, uraw);
+                xv_load4(a.hu + r3 + ib, huraw);
+                xv_load4(a.h_in + r3 + ib, hold);
+                if (a.Ah) {
+                    double ah[4];
+                    xv_load4(a.Ah + r2 + ib, ah);
+#pragma unroll
+                    for (int m = 0; m < 4; m++) ahraw[m] = getm_d2f_approx(ah[m]);
+                }
+            }
+            // masks of the velocity points beside the lane's first and last faces
+            int umW = __shfl_up_sync(FULL, um[3], 1), umE = __shfl_down_sync(FULL, um[0], 1);
+            if (lane == 0) umW = cum;
+            if (lane == 31) umE = ie < nx ? a.umask[r2 + ie] : 0;
+
+            // face geometry (the same expressions as hpass_x_inc_rows)
+            float QU[4], cfl[4], ahd[4];
+            bool up[4], uu_ok[4], act[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                const int ia = ib + m;
+                const bool f_in = lin && jrow && ia >= a.ilo - 1 && ia <= a.ihi;
+                act[m] = f_in && getm_flux_point(um[m]);
+                QU[m] = 0.f; cfl[m] = 0.f; ahd[m] = 0.f;
+                up[m] = false; uu_ok[m] = false;
+                if (act[m]) {
+                    const float uu = inc_f<V>(uraw[m]);
+                    const float huf = getm_d2f_approx(huraw[m]);
+                    QU[m] = uu * huf * dyf[m];
+                    cfl[m] = fabsf(uu * a.dtf * idxf[m]);
+                    up[m] = uu > 0.f;
+                    const int mw = m > 0 ? um[m - 1] : umW, me = m < 3 ? um[m + 1] : umE;
+                    uu_ok[m] = getm_flux_point(up[m] ? mw : me);
+                    if (a.Ah) ahd[m] = -ahraw[m] * huf * idxf[m] * dyf[m];
+                }
+            }
+            float QUw0 = __shfl_up_sync(FULL, QU[3], 1);  // west face of the lane's first cell
+            if (lane == 0) QUw0 = cQU;
+
+            // thickness update of the lane's cells
+            float coef[4];
+            bool upd[4];
+            double hnew[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                const int c = ib + m;
+                upd[m] = lin && jrow && c >= a.ilo && c <= a.ihi && tm[m] == 1;
+                coef[m] = 0.f;
+                hnew[m] = hold[m];
+                if (upd[m]) {
+                    const float QUw = m > 0 ? QU[m - 1] : QUw0;
+                    const float dh = a.dtf * (QU[m] - QUw) * iaf[m];
+                    hnew[m] = hold[m] - getm_f2d(dh);
+                    coef[m] = a.dtf * iaf[m] / (getm_d2f_approx(hold[m]) - dh);
+                }
+            }
+            if (g == 0 && lin) xv_store4(a.h_out + r3 + ib, hnew);
+
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                if (q >= nt) break;
+                const S* __restrict__ f = a.fin[t0 + q] + r3;
+                S fv[4] = {S(0), S(0), S(0), S(0)};
+                if (lin) xv_load4(f + ib, fv);
+                S fE0 = S(0), fE1 = S(0);  // the two cells east of the chunk (last lane)
+                if (lane == 31) {
+                    if (ie < nx) fE0 = f[ie];
+                    if (ie + 1 < nx) fE1 = f[ie + 1];
+                }
+                S fn0 = __shfl_down_sync(FULL, fv[0], 1);
+                if (lane == 31) fn0 = fE0;
+                // differences of neighbouring values in the storage type, then
+                // narrowed (d[m]: across face m)
+                float d[4];
+                d[0] = inc_f<S>(fv[1] - fv[0]);
+                d[1] = inc_f<S>(fv[2] - fv[1]);
+                d[2] = inc_f<S>(fv[3] - fv[2]);
+                d[3] = inc_f<S>(fn0 - fv[3]);
+                float dW = __shfl_up_sync(FULL, d[3], 1), dE = __shfl_down_sync(FULL, d[0], 1);
+                if (lane == 0) dW = cd[q];
+                if (lane == 31) dE = inc_f<S>(fE1 - fE0);
+                float el[4], er[4];
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    el[m] = 0.f; er[m] = 0.f;
+                    if (act[m]) {
+                        const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl[m]);
+                        const float dprev = m > 0 ? d[m - 1] : dW, dnext = m < 3 ? d[m + 1] : dE;
+                        const float dev = hx_dev(tf, up[m], uu_ok[m], dprev, d[m], dnext);
+                        const float fd = ahd[m] * d[m];
+                        el[m] = QU[m] * (up[m] ? dev : d[m] + dev) + fd;
+                        er[m] = QU[m] * (up[m] ? dev - d[m] : dev) + fd;
+                    }
+                }
+                float erW = __shfl_up_sync(FULL, er[3], 1);  // west face of the lane's first cell
+                if (lane == 0) erW = cer[q];
+                S out[4];
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    const float ew = m > 0 ? er[m - 1] : erW;
+                    out[m] = upd[m] ? inc_add<S>(fv[m], -coef[m] * (el[m] - ew)) : fv[m];
+                }
+                if (lin) xv_store4(a.fout[t0 + q] + r3 + ib, out);
+                cd[q] = __shfl_sync(FULL, d[3], 31);
+                cer[q] = __shfl_sync(FULL, er[3], 31);
+            }
+            cQU = __shfl_sync(FULL, QU[3], 31);
+            cum = __shfl_sync(FULL, um[3], 31);
+        }
+    }
+}
+
 // One row (layer k, row j) of the x pass: row = k ny_ + j.
 template <typename S, typename Epi = NoEpi, typename V = S>
 __device__ __forceinline__ void hpass_x_inc_body(const HPassArgs<S, V>& a, int bx, long long row, int lane,

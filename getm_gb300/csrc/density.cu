@@ -103,15 +103,15 @@ __device__ __forceinline__ DF seos_anomaly_df(float S, float T, double z)
 }
 
 // The same anomaly from FP64 S and T (the mixed form's FP64 tracer storage):
-// each is split into a truncated float head and the float of the rest (one
-// FP64 subtraction each), which the double-float sums take in.
+// each is split into a truncated float head and the float of the rest (both
+// on the integer pipe), which the double-float sums take in.
 __device__ __forceinline__ DF seos_anomaly_df2(double S, double T, double z)
 {
     constexpr DFConst A0(SEOS_A0), B0(SEOS_B0), L1(0.5 * SEOS_LAMBDA1), L2(0.5 * SEOS_LAMBDA2);
     constexpr DFConst M1(SEOS_MU1), M2(SEOS_MU2), NU(SEOS_NU);
     const float zh = getm_d2f_approx(z), Th = getm_d2f_approx(T), Sh = getm_d2f_approx(S);
-    const DF zd{zh, getm_d2f_approx(z - getm_f2d(zh))};
-    const float Tl = getm_d2f_approx(T - getm_f2d(Th)), Sl = getm_d2f_approx(S - getm_f2d(Sh));
+    const DF zd{zh, getm_d2f_rest(z)};
+    const float Tl = getm_d2f_rest(T), Sl = getm_d2f_rest(S);
     const DF Ta = df_add(df_two_sum(Th, -10.f), DF{Tl, 0.f});
     const DF Sa = df_add(df_two_sum(Sh, -35.f), DF{Sl, 0.f});
     const DF one{1.f, 0.f};
@@ -130,9 +130,15 @@ __global__ void density_f64s_kernel(long long n, const double* S, const double* 
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     const DF a = seos_anomaly_df2(S[q], T[q], p[q]);
-    const double ad = getm_f2d(a.hi) + getm_f2d(a.lo);
-    if (rho) rho[q] = SEOS_RHO0 + ad;
-    if (buoy) buoy[q] = (-GETM_G / GETM_RHO0) * (ad + (SEOS_RHO0 - GETM_RHO0));
+    if (rho) rho[q] = SEOS_RHO0 + (getm_f2d(a.hi) + getm_f2d(a.lo));
+    if (buoy) {
+        // -g/rho0 (anomaly + (SEOS_RHO0 - rho0)) in double-float: one FP64
+        // addition to widen it
+        constexpr DFConst GB(-GETM_G / GETM_RHO0);
+        const DF t = df_add(a, DF{(float)(SEOS_RHO0 - GETM_RHO0), 0.f});
+        const DF m = df_mul(df_of(GB), t);
+        buoy[q] = getm_f2d(m.hi) + getm_f2d(m.lo);
+    }
 }
 
 extern "C" int getm_density_buoyancy_f64s(int n, const double* salt, const double* temp, const double* p,

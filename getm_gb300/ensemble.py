@@ -12,6 +12,8 @@ share no state, so a member's results are the same alone and in the ensemble.
 
 from __future__ import annotations
 
+import contextlib
+
 from typing import List, Optional
 
 import torch
@@ -59,12 +61,15 @@ class DomainRunner:
         for _ in range(self.sim.split_factor):
             self.sim.advance()
 
-    def prepare(self, capture_stream: Optional[torch.cuda.Stream] = None, capture_error_mode: str = "global"):
+    def prepare(self, capture_stream: Optional[torch.cuda.Stream] = None, capture_error_mode: str = "global",
+                capture_lock=None):
         """Run the eager warm-up steps (allocating every work buffer) and
         record the two step graphs.  ``capture_error_mode="thread_local"``
-        lets other host threads keep launching work (graph replays, event
-        queries) while this one captures; with "global" no other thread may
-        make CUDA calls during the capture."""
+        lets other host threads keep launching work (event queries, kernels)
+        while this one captures; with "global" no other thread may make CUDA
+        calls during the capture.  ``capture_lock``: held during each
+        capture; another thread that replays graphs must hold it too (torch
+        refuses a replay while any graph is being captured)."""
         for _ in range(self._warmup):
             self._eager_step()
         self.steps_done = self._warmup
@@ -76,9 +81,16 @@ class DomainRunner:
         graphs = []
         for _ in range(2):
             g = torch.cuda.CUDAGraph()
-            with torch.cuda.stream(stream):
-                with torch.cuda.graph(g, stream=stream, capture_error_mode=capture_error_mode):
+            with torch.cuda.stream(stream), (capture_lock or contextlib.nullcontext()):
+                # capture_begin/end rather than the torch.cuda.graph context,
+                # which synchronizes the whole device, collects garbage and
+                # empties the allocator's cache first: with other domains'
+                # steps queued (serving) that waits for all of them
+                g.capture_begin(capture_error_mode=capture_error_mode)
+                try:
                     self._eager_step()
+                finally:
+                    g.capture_end()
             graphs.append(g)
         torch.cuda.current_stream(dev).wait_stream(stream)
         self.graphs = graphs

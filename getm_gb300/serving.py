@@ -23,6 +23,7 @@ between consecutive completed 3D steps of a request.
 
 from __future__ import annotations
 
+import threading
 import time
 from dataclasses import dataclass, field
 from typing import Callable, Dict, List, Optional
@@ -96,9 +97,15 @@ class Server:
         self.default_bytes_per_cell = 2000.0
         self.used = 0.0
         self.peak_used = 0.0
-        self._capture_stream = torch.cuda.Stream(device=self.device)
-        self._build_stream = torch.cuda.Stream(device=self.device)
+        # set-up work (eager warm-up steps) on high-priority streams: its
+        # kernels go ahead of the queued step replays of running requests
+        self._capture_stream = torch.cuda.Stream(device=self.device, priority=-1)
+        self._build_stream = torch.cuda.Stream(device=self.device, priority=-1)
         self._lane_next = 0
+        # held by the admission worker while it captures a graph and by the
+        # main loop while it issues replays (torch refuses a replay while any
+        # graph is being captured)
+        self._capture_lock = threading.Lock()
         self.admission_thread = admission_thread
         self.max_building = max(1, max_building)
         self.admission_host_s: List[float] = []
@@ -127,7 +134,8 @@ class Server:
         runner = DomainRunner(sim)
         res = Result(req.rid, runner.cells, req.nsteps, req.arrival, admitted=t_run)
         # warm-up steps run eagerly inside prepare(); time them as one block
-        runner.prepare(self._capture_stream, capture_error_mode)
+        runner.prepare(self._capture_stream, capture_error_mode,
+                       capture_lock=self._capture_lock if capture_error_mode == "thread_local" else None)
         ev = torch.cuda.Event(enable_timing=True)
         ev.record()
         ev.synchronize()
@@ -248,22 +256,28 @@ class Server:
                             a = self._admit(req, wl, ta - t0, start)
                             self.admission_host_s.append(time.perf_counter() - ta)
                             take(a)
-                # completion of issued steps, then issue the next ones
+                # completion of issued steps, then issue the next ones (not
+                # while the worker captures a graph: this pass skips them)
                 progressed = False
-                for a in active:
-                    while a.inflight and a.inflight[0].query():
-                        ev = a.inflight.pop(0)
-                        a.result.step_done.append(start.elapsed_time(ev) / 1000.0)
-                        progressed = True
-                    issued = len(a.result.step_done) + len(a.inflight)
-                    while issued < a.req.nsteps and len(a.inflight) < self.max_inflight:
-                        with torch.cuda.stream(a.lane):
-                            a.runner.step()
-                            ev = torch.cuda.Event(enable_timing=True)
-                            ev.record(a.lane)
-                        a.inflight.append(ev)
-                        issued += 1
-                        progressed = True
+                may_issue = self._capture_lock.acquire(blocking=False)
+                try:
+                    for a in active:
+                        while a.inflight and a.inflight[0].query():
+                            ev = a.inflight.pop(0)
+                            a.result.step_done.append(start.elapsed_time(ev) / 1000.0)
+                            progressed = True
+                        issued = len(a.result.step_done) + len(a.inflight)
+                        while may_issue and issued < a.req.nsteps and len(a.inflight) < self.max_inflight:
+                            with torch.cuda.stream(a.lane):
+                                a.runner.step()
+                                ev = torch.cuda.Event(enable_timing=True)
+                                ev.record(a.lane)
+                            a.inflight.append(ev)
+                            issued += 1
+                            progressed = True
+                finally:
+                    if may_issue:
+                        self._capture_lock.release()
                 # retire finished requests
                 keep_active = []
                 for a in active:

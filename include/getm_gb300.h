@@ -291,12 +291,16 @@ int getm_launch_count(unsigned long long* count);
  *   GETM_TUNE_COLUMN_ROWS     rows of 32 columns per block of the w pass and
  *                             the float column solve: 1, 2, 4 (default 4)
  *   GETM_TUNE_SUBSTEP_BLOCKS  blocks per SM of the one-launch 2D substep:
- *                             0 = as many as fit (default), 1, 2 (capped at what fits) */
+ *                             0 = as many as fit (default), 1, 2 (capped at what fits)
+ *   GETM_TUNE_XPASS_VEC       3D x pass in increment form: 1 = four cells per lane
+ *                             where rows allow 16-byte vectors (default), 0 = one
+ *                             cell per lane (both give the same bits)            */
 #define GETM_TUNE_XPASS_ROWS 0
 #define GETM_TUNE_YMARCH_CHUNK 1
 #define GETM_TUNE_COLUMN_ROWS 2
 #define GETM_TUNE_SUBSTEP_BLOCKS 3
-#define GETM_TUNE_NKNOBS 4
+#define GETM_TUNE_XPASS_VEC 4
+#define GETM_TUNE_NKNOBS 5
 int getm_tune_set(int knob, int value);
 int getm_tune_get(int knob, int* value);
 

@@ -43,6 +43,8 @@ def _args():
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--tracer-storage", choices=["float64", "float32"], default=None,
+                    help="tracer type of the mixed form (default float64)")
     ap.add_argument("--no-compare", action="store_true", help="skip the other precision form")
     ap.add_argument("--nx", type=int, default=400)
     ap.add_argument("--ny", type=int, default=300)
@@ -241,16 +243,18 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _make_sim(wl, precision, device, round_to_float32=True):
+def _make_sim(wl, precision, device, round_to_float32=True, tracer_storage=None):
     """Seamount simulation from rest; the initial temperature (20 -> 4 degC,
     linear in depth) is rounded to float32 unless told otherwise, so both
-    forms start from identical fields."""
+    forms start from identical fields.  ``tracer_storage``: the mixed form's
+    tracer type (default float64)."""
     import torch
 
     from getm_gb300.simulation import Simulation
 
     p = wl.params
-    sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device, tiles="auto")
+    sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device, tiles="auto",
+                     tracer_storage=tracer_storage)
     zc = sim.T.zc.all_values
     temp0 = torch.where(sim.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
                         sim.temp.all_values.double())
@@ -743,7 +747,8 @@ def run_ours(args):
     nsteps = args.steps
     primary = args.precision
     forms = [primary] + ([] if args.no_compare else [f for f in ("fp64", "mixed") if f != primary])
-    runners = {f: Runner(_make_sim(wl, f, device), args.warmup, not args.no_graph) for f in forms}
+    runners = {f: Runner(_make_sim(wl, f, device, tracer_storage=args.tracer_storage if f == "mixed" else None),
+                         args.warmup, not args.no_graph) for f in forms}
 
     # device-timed region for each form: exactly nsteps 3D steps
     ms = {}

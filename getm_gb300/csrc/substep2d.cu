@@ -162,7 +162,10 @@ __device__ __forceinline__ void advection_pass(const HPassArgs<double>& pa, int 
     if (dir == 1) {
         const int nbx = MIXED ? div_up(pa.nx_ + 1, HX_STRIDE) : div_up(pa.nx_, 32);
         const long long items = (long long)nbx * pa.ny_;
-        for (long long w = (long long)blockIdx.x * SS_BY + ty; w < items; w += (long long)gridDim.x * SS_BY) {
+        // equal contiguous runs of row segments per block (every SM busy)
+        const long long per = (items + gridDim.x - 1) / gridDim.x;
+        const long long wb = (long long)blockIdx.x * per, we = wb + per < items ? wb + per : items;
+        for (long long w = wb + ty; w < we; w += SS_BY) {
             const int bx = (int)(w % nbx);
             const long long row = w / nbx;
             if constexpr (MIXED) hpass_x_inc_body<double, Epi>(pa, bx, row, tx, epi);
@@ -204,10 +207,17 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
     __shared__ SubstepSmem sm;
     __shared__ int s_ok;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int G = gridDim.x * SS_THREADS;
     const int gt = blockIdx.x * SS_THREADS + ty * 32 + tx;
+    // pointwise phases: the plane in equal contiguous chunks, one per block,
+    // so every SM gets the same number of points (a grid-stride loop over
+    // fewer points than threads would leave the last blocks idle and give
+    // the first SMs a third more work); consecutive threads take
+    // consecutive points
+    const int tid = ty * 32 + tx;
     const int nx = a.nx, ny = a.ny;
     const int n = nx * ny;  // < 2^30 (checked by the host)
+    const int chunk = (n + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int pb = (int)blockIdx.x * chunk, pe = min(pb + chunk, n);
     const int ilo = a.halox, ihi = nx - a.halox - 1, jlo = a.haloy, jhi = ny - a.haloy - 1;
 
     unsigned target = 0;  // barrier count to wait for (thread 0)
@@ -217,20 +227,20 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
 
     const int d1 = a.ufirst ? 0 : 1, d2 = 1 - d1;
     // 1: first transport update
-    for (int p = gt; p < n; p += G) {
+    for (int p = pb + tid; p < pe; p += SS_THREADS) {
         const int j = p / nx, i = p - j * nx;
         if (i >= ilo && i <= ihi && j >= jlo && j <= jhi) transport_update<MIXED>(a.tr[d1], a.dt, p);
     }
     if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
     // 2: Coriolis from the first, second transport update
-    for (int p = gt; p < n; p += G) {
+    for (int p = pb + tid; p < pe; p += SS_THREADS) {
         const int j = p / nx, i = p - j * nx;
         coriolis_from<C>(a, d1, i, j);
         if (i >= ilo && i <= ihi && j >= jlo && j <= jhi) transport_update<MIXED>(a.tr[d2], a.dt, p);
     }
     if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
     // 3: Coriolis from the second, cumulative transports, surface elevation
-    for (int p = gt; p < n; p += G) {
+    for (int p = pb + tid; p < pe; p += SS_THREADS) {
         const int j = p / nx, i = p - j * nx;
         coriolis_from<C>(a, d2, i, j);
         if (a.accumulate) accumulate_2d_point(a.tr[0].U, a.tr[1].U, a.Ucum, a.Vcum, p);
@@ -246,7 +256,7 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
             __syncthreads();
         }
     }
-    for (int p = gt; p < n; p += G) {
+    for (int p = pb + tid; p < pe; p += SS_THREADS) {
         const int j = p / nx, i = p - j * nx;
         a.fwf[p] = a.pe[p];
         if (i < nx - 1) interp_pair_point<double>(a.taux, a.tausx, p, 1, 0);
@@ -254,7 +264,7 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
     }
     if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
     // 5: velocities, advected thicknesses, surface pressure gradient
-    for (int p = gt; p < n; p += G) {
+    for (int p = pb + tid; p < pe; p += SS_THREADS) {
         const int j = p / nx, i = p - j * nx;
         momentum_2d_velocities_point<C>(a.vel, i, j);
         a.advD[0][p] = a.Dsrc[0][p];
@@ -264,7 +274,7 @@ __global__ void __launch_bounds__(SS_THREADS, MIXED ? 2 : 1) substep_2d_kernel(S
     if (!grid_barrier(a.sync, target, s_ok)) return grid_exit(a.sync);
     // 6: bottom friction; first advection passes
     if (a.friction) {
-        for (int p = gt; p < n; p += G) {
+        for (int p = pb + tid; p < pe; p += SS_THREADS) {
             const int j = p / nx, i = p - j * nx;
             momentum_2d_friction_point<C>(a.fric, i, j);
         }

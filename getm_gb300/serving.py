@@ -179,11 +179,12 @@ class Server:
         generated on a host thread ahead of their admission; with
         ``admission_thread`` the set-up runs on a worker thread, otherwise at
         most one request is set up per pass of the loop.  ``poll_sleep``:
-        seconds the loop sleeps when a pass found nothing to do (default:
-        100 us with the admission thread, which then gets the interpreter:
-        a loop that only polls would otherwise hold it while the worker's
-        every library call gives it up; 0 without).  Returns one Result per
-        admitted request."""
+        seconds the loop sleeps when a pass found nothing to do, doubled
+        after each idle pass up to 20 times that, reset when a step completes
+        or is issued (default: 100 us with the admission thread, which then
+        gets the interpreter: a loop that only polls would otherwise hold it
+        while the worker's every library call gives it up; 0 without).
+        Returns one Result per admitted request."""
         import queue
         import sys
         import threading
@@ -192,6 +193,7 @@ class Server:
         admit_until = duration if admit_until is None else admit_until
         if poll_sleep is None:
             poll_sleep = 1e-4 if self.admission_thread else 0.0
+        idle_sleep = poll_sleep
         pending = sorted(requests, key=lambda r: r.arrival)
         active: List[_Active] = []
         results: List[Result] = []
@@ -294,8 +296,15 @@ class Server:
                 active = keep_active
                 if not active and not reserved and (not pending or now > admit_until):
                     break
-                if not progressed and poll_sleep > 0:
-                    time.sleep(poll_sleep)
+                if progressed:
+                    idle_sleep = poll_sleep
+                elif poll_sleep > 0:
+                    # back off while nothing completes (a pass that wakes every
+                    # 100 us would hold the interpreter half the time and
+                    # starve the admission worker); every request keeps
+                    # max_inflight steps queued, so the device does not wait
+                    time.sleep(idle_sleep)
+                    idle_sleep = min(2.0 * idle_sleep, 20.0 * poll_sleep)
         finally:
             if worker is not None:
                 inbox.put(None)

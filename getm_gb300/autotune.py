@@ -242,6 +242,20 @@ def _tune_main(argv: Optional[Iterable[str]] = None) -> None:
     args = ap.parse_args(list(argv) if argv is not None else None)
     cache = TileCache.load(args.out)
     dev = "cuda"
+    sides = [int(s) for s in args.sides.split(",") if s]
+    nzs = [int(s) for s in args.nzs.split(",") if s]
+    rng = np.random.default_rng(11)
+    for n in sides:
+        for nz in nzs:
+            wl = workloads.ensemble_member(rng, nmin=n, nmax=n, nzmin=nz, nzmax=nz)
+            sim = make_member(wl, "mixed", device=dev)
+            best, t, t0, _ = tune(sim, replays=4)
+            cache.store(wl.T.nx, wl.T.ny, wl.T.nz, "mixed", best, t, t0, "ensemble member")
+            print(f"member {wl.T.nx}x{wl.T.ny}x{wl.T.nz}: {best} {t:.3f} ms/step (defaults {t0:.3f})", flush=True)
+            del sim
+            torch.cuda.empty_cache()
+    # the benchmark domains last: a member of the same size bucket must not
+    # overwrite their shapes
     if not args.no_seamount:
         wl = workloads.seamount()
         p = wl.params
@@ -254,18 +268,6 @@ def _tune_main(argv: Optional[Iterable[str]] = None) -> None:
             best, t, t0, _ = tune(sim, replays=3 if prec == "fp64" else 6)
             cache.store(wl.T.nx, wl.T.ny, wl.T.nz, prec, best, t, t0, "seamount")
             print(f"seamount {prec}: {best} {t:.3f} ms/step (defaults {t0:.3f})", flush=True)
-            del sim
-            torch.cuda.empty_cache()
-    sides = [int(s) for s in args.sides.split(",") if s]
-    nzs = [int(s) for s in args.nzs.split(",") if s]
-    rng = np.random.default_rng(11)
-    for n in sides:
-        for nz in nzs:
-            wl = workloads.ensemble_member(rng, nmin=n, nmax=n, nzmin=nz, nzmax=nz)
-            sim = make_member(wl, "mixed", device=dev)
-            best, t, t0, _ = tune(sim, replays=4)
-            cache.store(wl.T.nx, wl.T.ny, wl.T.nz, "mixed", best, t, t0, "ensemble member")
-            print(f"member {wl.T.nx}x{wl.T.ny}x{wl.T.nz}: {best} {t:.3f} ms/step (defaults {t0:.3f})", flush=True)
             del sim
             torch.cuda.empty_cache()
     cache.save(args.out)

@@ -27,6 +27,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <cuda_pipeline.h>
+
 #include "advection_passes.cuh"
 
 
@@ -440,10 +442,50 @@ __device__ void w_substep(const WPassArgs<T>& a, long long c, const T* wv, const
 // with e_k = W_k (face_k - f_k) and e'_{k-1} = W_{k-1} (face_{k-1} - f_k).
 // NT fields advected with the same w_var share every thickness and velocity
 // load and the face constants; each field keeps its own window.
+// The operands of the levels a column sweep will need are staged W_STAGE
+// levels ahead into a per-thread ring in shared memory by asynchronous
+// copies (cp.async): the loads of W_STAGE levels are in flight without
+// holding registers, where register prefetch reached two levels.  Each
+// thread reads back only the slots it filled, so no block barrier is
+// involved; a slot is refilled only after its level was read.
+constexpr int W_STAGE = 6;
+constexpr int W_RING = W_STAGE + 1;
+
+template <typename S>
+struct WRing {
+    double* h;  // h of level L at h[(L % W_RING) * 32]
+    S* f;       // field q of level L at f[((L % W_RING) * 2 + q) * 32]
+    float* W;   // the field's vertical velocity (w_var) of level L
+    float* w;   // w of level L (nz + 1 interfaces)
+};
+
+template <typename S>
+constexpr size_t w_ring_bytes_per_thread()
+{
+    return (size_t)W_RING * (sizeof(double) + 2 * sizeof(S) + 2 * sizeof(float));
+}
+
+// the ring of thread (lane, warp) in the block's dynamic shared memory
+// (doubles first, so every slot is naturally aligned)
+template <typename S>
+__device__ __forceinline__ WRing<S> w_ring(unsigned char* smem, int nwarps, int warp, int lane)
+{
+    WRing<S> r;
+    double* hb = reinterpret_cast<double*>(smem);
+    S* fb = reinterpret_cast<S*>(hb + (size_t)nwarps * W_RING * 32);
+    float* Wb = reinterpret_cast<float*>(fb + (size_t)nwarps * W_RING * 64);
+    float* wb = Wb + (size_t)nwarps * W_RING * 32;
+    r.h = hb + (size_t)warp * W_RING * 32 + lane;
+    r.f = fb + (size_t)warp * W_RING * 64 + lane;
+    r.W = Wb + (size_t)warp * W_RING * 32 + lane;
+    r.w = wb + (size_t)warp * W_RING * 32 + lane;
+    return r;
+}
+
 template <int NT, typename S>
 __device__ void w_substep_inc(const WPassArgs<S, float>& a, long long c, const float* wv, const double* hs,
                               const S* const (&fs)[NT], double* hd, S* const (&fdst)[NT], double dtk,
-                              double itersm1)
+                              double itersm1, const WRing<S>& ring)
 {
     const long long P = a.plane;
     const int nz = a.nz;
@@ -467,20 +509,38 @@ __device__ void w_substep_inc(const WPassArgs<S, float>& a, long long c, const f
     float hkf = getm_d2f_approx(hk), hk1f = getm_d2f_approx(hk1);
     float Wm = 0.f;    // W_{k-1} (0 below the bottom level)
     float wkm1 = a.w[c];
-    // the interface values above level k, loaded one level ahead (the loads
-    // of a level do not depend on the stores of the level before)
+    // the interface values above level k, one level ahead
     float Wn = (nz > 1) ? wv[c + P] : 0.f;
     float wkn = a.w[c + P];
+    // level L's operands into its slot (nothing past the column), one
+    // commit group per level
+    auto stage = [&](int L) {
+        const int s = L % W_RING;
+        if (L < nz) {
+#pragma unroll
+            for (int q = 0; q < NT; q++)
+                __pipeline_memcpy_async(&ring.f[(s * 2 + q) * 32], &fs[q][c + (long long)L * P], sizeof(S));
+            __pipeline_memcpy_async(&ring.h[s * 32], &hs[c + (long long)L * P], sizeof(double));
+            __pipeline_memcpy_async(&ring.W[s * 32], &wv[c + (long long)L * P], sizeof(float));
+        }
+        if (L <= nz) __pipeline_memcpy_async(&ring.w[s * 32], &a.w[c + (long long)L * P], sizeof(float));
+        __pipeline_commit();
+    };
+    for (int L = 2; L < 2 + W_STAGE; L++) stage(L);
     for (int k = 0; k < nz; k++) {
+        // level k + 2: its group is the oldest of the W_STAGE in flight
+        __pipeline_wait_prior(W_STAGE - 1);
+        const int s2 = (k + 2) % W_RING;
         S fk2[NT];
         double hk2 = 0.0;
 #pragma unroll
-        for (int q = 0; q < NT; q++) fk2[q] = (k + 2 < nz) ? fs[q][c + (k + 2) * P] : S(0);
-        if (k + 2 < nz) hk2 = hs[c + (k + 2) * P];
+        for (int q = 0; q < NT; q++) fk2[q] = (k + 2 < nz) ? ring.f[(s2 * 2 + q) * 32] : S(0);
+        if (k + 2 < nz) hk2 = ring.h[s2 * 32];
         const float W = Wn;
         const float wk = wkn;
-        Wn = (k + 1 < nz - 1) ? wv[c + (k + 2) * P] : 0.f;
-        wkn = (k + 1 < nz) ? a.w[c + (k + 2) * P] : 0.f;
+        Wn = (k + 1 < nz - 1) ? ring.W[s2 * 32] : 0.f;
+        wkn = (k + 1 < nz) ? ring.w[s2 * 32] : 0.f;
+        stage(k + 2 + W_STAGE);  // into the slot of level k + 1, read at k - 1
         const float cfl = fabsf(W) * dtf / fminf(hkf, hk1f) * itf;
         const TvdFaceF tf = getm_tvd_face_f(a.scheme, cfl);
         const float dh = dtkf * (wk - wkm1);
@@ -510,6 +570,7 @@ __device__ void w_substep_inc(const WPassArgs<S, float>& a, long long c, const f
         hk = hk1; hk1 = hk2;
         hkf = hk1f; hk1f = getm_d2f_approx(hk2);
     }
+    __pipeline_wait_prior(0);  // the ring is free for the next sweep
 }
 
 // Largest Courant number over the interior interfaces of a column
@@ -553,6 +614,7 @@ __device__ __forceinline__ int w_iters_from(double cfl)
 template <typename T, typename V = T>
 __global__ void __launch_bounds__(128, getm_increment_form<V> ? 7 : 1) wpass_kernel(WPassArgs<T, V> a)
 {
+    extern __shared__ __align__(16) unsigned char w_smem[];
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= a.nx_ || j >= a.ny_) return;
@@ -608,11 +670,13 @@ __global__ void __launch_bounds__(128, getm_increment_form<V> ? 7 : 1) wpass_ker
                     T* faux2 = a.faux + a.plane * a.nz;
                     const T* const fs2[2] = {fs, (it == 1) ? f2 : faux2};
                     T* const fd2[2] = {fd, (it == iters) ? f2 : faux2};
-                    w_substep_inc<2, T>(a, c, wv, hs, fs2, hd, fd2, dtk, itersm1);
+                    w_substep_inc<2, T>(a, c, wv, hs, fs2, hd, fd2, dtk, itersm1,
+                                        w_ring<T>(w_smem, blockDim.y, threadIdx.y, threadIdx.x));
                 } else {
                     const T* const fs1[1] = {fs};
                     T* const fd1[1] = {fd};
-                    w_substep_inc<1, T>(a, c, wv, hs, fs1, hd, fd1, dtk, itersm1);
+                    w_substep_inc<1, T>(a, c, wv, hs, fs1, hd, fd1, dtk, itersm1,
+                                        w_ring<T>(w_smem, blockDim.y, threadIdx.y, threadIdx.x));
                 }
             } else {
                 w_substep(a, c, wv, hs, fs, hd, fd, dtk, itersm1);
@@ -639,6 +703,19 @@ static int run_wstage(getm_advection* adv, const getm_grid* tg, const V* w, cons
     const int rows = getm_tune(GETM_TUNE_COLUMN_ROWS);
     dim3 block(32, rows);
     dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, rows));
+    // the increment form's staging rings (w_substep_inc); the largest
+    // carve-out of shared memory, so seven blocks of four rows fit per SM
+    size_t smem = 0;
+    if constexpr (getm_increment_form<V>) {
+        smem = (size_t)32 * rows * w_ring_bytes_per_thread<T>();
+        static bool carveout_set = false;  // a per-function attribute: once per process
+        if (!carveout_set) {
+            if (cudaFuncSetAttribute(wpass_kernel<T, V>, cudaFuncAttributePreferredSharedMemoryCarveout, 100) !=
+                cudaSuccess)
+                return GETM_ERR_CUDA;
+            carveout_set = true;
+        }
+    }
     // Chunks: every chunk starts from h_in; the final h is the last chunk's.
     int done = 0;
     do {
@@ -647,7 +724,7 @@ static int run_wstage(getm_advection* adv, const getm_grid* tg, const V* w, cons
         a.ntracer = n;
         a.h_in = h_in; a.h_out = h_out;
         for (int t = 0; t < n; t++) { a.wvar[t] = wvar[done + t]; a.f[t] = f[done + t]; }
-        wpass_kernel<T, V><<<grid, block, 0, stream>>>(a);
+        wpass_kernel<T, V><<<grid, block, smem, stream>>>(a);
         GETM_CHECK_LAUNCH();
         done += n;
     } while (done < ntracer);

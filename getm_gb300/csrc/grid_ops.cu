@@ -496,22 +496,34 @@ __global__ void depth_3d_column_kernel(Depth3DArgs a)
     const bool m = mask[p] != 0;
     const double D = m ? Dc[p] : 0.0, H = m ? Hc[p] : 0.0;
     CoordSweep sw{0.0, 0.0, 0.0};
-    for (int k = 0; k < nz; k++) {
-        const long long q = p + k * plane;
-        const double o = hn[q];
-        ho[q] = o;
-        double n = o;
-        if (m) {
-            n = a.dga[k] * D;
-            hn[q] = n;
+    // the old thicknesses of DEPTH3D_CHUNK levels are loaded before any of
+    // their stores (the stores may alias as far as the compiler knows, which
+    // would serialise each level's load behind the previous level's stores)
+    constexpr int DEPTH3D_CHUNK = 8;
+    for (int k0 = 0; k0 < nz; k0 += DEPTH3D_CHUNK) {
+        double ov[DEPTH3D_CHUNK];
+#pragma unroll
+        for (int u = 0; u < DEPTH3D_CHUNK; u++) ov[u] = k0 + u < nz ? hn[p + (k0 + u) * plane] : 0.0;
+#pragma unroll
+        for (int u = 0; u < DEPTH3D_CHUNK; u++) {
+            const int k = k0 + u;
+            if (k >= nz) break;
+            const long long q = p + k * plane;
+            const double o = ov[u];
+            ho[q] = o;
+            double n = o;
+            if (m) {
+                n = a.dga[k] * D;
+                hn[q] = n;
+            }
+            if (role == 1) {
+                const double hh = getm_half(o + n);
+                a.hhalf[q] = hh;
+                if (i >= 1) a.hnuu[q - 1] = hh;
+                if (j >= 1) a.hnvv[q - nx] = hh;
+            }
+            if (m) sw.level(k, q, plane, H, n, zc, zf);
         }
-        if (role == 1) {
-            const double hh = getm_half(o + n);
-            a.hhalf[q] = hh;
-            if (i >= 1) a.hnuu[q - 1] = hh;
-            if (j >= 1) a.hnvv[q - nx] = hh;
-        }
-        if (m) sw.level(k, q, plane, H, n, zc, zf);
     }
     if (role == 1 && m && a.depth) t2cd_column(plane, nz, p, a.hnt, a.depth);
 }

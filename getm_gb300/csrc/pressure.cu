@@ -316,15 +316,20 @@ __global__ void smcw_gradient_mixed_kernel(
     if (colin && j <= jhi + 1) fy = smcw_face(vmask, p, p + kP, nx, zc, buoy);
     sZx[ty][tx + 1] = fx.rz; sRx[ty][tx + 1] = fx.rr;
     sZy[ty + 1][tx] = fy.rz; sRy[ty + 1][tx] = fy.rr;
-    if (tx < 2) {  // x faces at columns i0-1 (tx 0) and i0+SG_BX (tx 1) of row j
-        const int ii = tx == 0 ? i0 - 1 : i0 + SG_BX;
+    if (ty == SG_BY - 1 && tx < 2 * SG_BY) {
+        // x faces at columns i0-1 and i0+SG_BX of every row of the tile, all
+        // by the last warp (lane 2r + side: row r): one warp's FP64
+        // differences instead of one per row
+        const int r = tx >> 1, side = tx & 1;
+        const int jr = j0 + r;
+        const int ii = side == 0 ? i0 - 1 : i0 + SG_BX;
         SgFace f{0.f, 0.f, 0.0, 0.0};
-        if (rowin && ii >= ilo - 1 && ii <= ihi + 1) {
-            const long long pp = (long long)j * nx + ii;
+        if (jr <= jhi && ii >= ilo - 1 && ii <= ihi + 1) {
+            const long long pp = (long long)jr * nx + ii;
             f = smcw_face(umask, pp, pp + kP, 1, zc, buoy);
         }
-        sZx[ty][tx == 0 ? 0 : SG_BX + 1] = f.rz;
-        sRx[ty][tx == 0 ? 0 : SG_BX + 1] = f.rr;
+        sZx[r][side == 0 ? 0 : SG_BX + 1] = f.rz;
+        sRx[r][side == 0 ? 0 : SG_BX + 1] = f.rr;
     }
     if (ty < 2) {  // y faces at rows j0-1 (ty 0) and j0+SG_BY (ty 1) of column i
         const int jj = ty == 0 ? j0 - 1 : j0 + SG_BY;
@@ -361,7 +366,7 @@ __global__ void smcw_gradient_mixed_kernel(
         const float dRx0 = smcw_harm_f(rR0, rR1), dRx1 = smcw_harm_f(rR1, rR2);
         const float corr = 0.2f * ((dRx1 - dRx0) * (getm_d2f_approx(dzc) - x * (dZx1 + dZx0)) -
                                    (dZx1 - dZx0) * (getm_d2f_approx(dbq) - x * (dRx1 + dRx0)));
-        const double FC = 0.5 * ((buoy[q + s] + buoy[q]) * dzc - getm_f2d(corr));
+        const double FC = getm_half((buoy[q + s] + buoy[q]) * dzc - getm_f2d(corr));  // 0.5 x, exactly
         // the large, nearly cancelling terms in FP64 (the surface term from
         // the column sweep), the scaling by the mean thickness and the
         // inverse spacing in float

@@ -69,6 +69,10 @@ _SIGS = {
     "getm_multiply_add": "ippds",
     "getm_advance_surface_elevation": "iiiippppppppds",
     "getm_surface_pressure_gradient": "iiiiiippppppppdpps",
+    "getm_shear_frequency2": "iiiiiiipppppppps",
+    "getm_shear_frequency2_f32": "iiiiiiipppppppps",
+    "getm_vertical_advection_to_sources": "iiiiipppppps",
+    "getm_update_gvc": "iiidpdippps",
     "getm_surface_pressure_gradient_mixed": "iiiiiippppppppdpps",
     "getm_horizontal_diffusion": "iiiiiippppppppppdpps",
     "getm_bottom_friction": "iippppppdpis",

@@ -147,6 +147,18 @@ def shear_frequency(uk, vk, SS):
          _p(g.mask), _p(uk.grid.hn), _p(vk.grid.hn), _p(uk), _p(vk), _p(SS), _s())
 
 
+def shear_frequency2(uk, vk, num, SS):
+    """pyx:468-479"""
+    g = SS.grid
+    assert SS.z == INTERFACES, "w"
+    assert uk.grid is g.ugrid and uk.z == CENTERS, "uk"
+    assert vk.grid is g.vgrid and vk.z == CENTERS, "vk"
+    assert num.grid is g and num.z == INTERFACES, "num"
+    sfx = _sfx(uk.all_values, vk.all_values, num.all_values, SS.all_values)
+    call("getm_shear_frequency2" + sfx, g.nx_, g.ny_, g.nz, g.halox + 1, g.halox + g.nx, g.haloy + 1,
+         g.haloy + g.ny, _p(g.mask), _p(g.hn), _p(uk.grid.hn), _p(vk.grid.hn), _p(uk), _p(vk), _p(num), _p(SS), _s())
+
+
 def surface_shear_velocity(taux, tauy, ustar):
     """pyx:481-488"""
     g = ustar.grid
@@ -249,6 +261,38 @@ def multiply_add(tgt: torch.Tensor, add: torch.Tensor, scale_factor: float):
     """pyx:570-572"""
     if tgt.numel() != 0:
         call("getm_multiply_add", tgt.numel(), tgt.data_ptr(), add.data_ptr(), float(scale_factor), _s())
+
+
+_flags = {}
+
+
+def vertical_advection_to_sources(halox: int, haloy: int, mask: torch.Tensor, c: torch.Tensor, w: torch.Tensor,
+                                  h: torch.Tensor, s: torch.Tensor):
+    """pyx:574-575: (nz, ny, nx) device tensors, mask int32, the rest float64."""
+    nz, ny, nx = c.shape
+    for name, t, dt in (("mask", mask, torch.int32), ("w", w, torch.float64), ("h", h, torch.float64),
+                        ("s", s, torch.float64), ("c", c, torch.float64)):
+        assert t.shape == (nz, ny, nx) and t.dtype == dt and t.is_contiguous(), name
+    flag = _flags.get(c.device)
+    if flag is None:
+        flag = _flags[c.device] = torch.zeros(1, dtype=torch.int32, device=c.device)
+    call("getm_vertical_advection_to_sources", nx, ny, nz, halox, haloy, mask.data_ptr(), c.data_ptr(), w.data_ptr(),
+         h.data_ptr(), s.data_ptr(), flag.data_ptr(), _s())
+
+
+def update_gvc(dsigma: float, dbeta: torch.Tensor, Dgamma: float, kk: int, D: torch.Tensor, mask: torch.Tensor,
+               h: torch.Tensor):
+    """pyx:577-585: dbeta (nz,), D (ny, nx) float64 and mask (ny, nx) int32
+    device tensors; h (nz, ny, nx) float64; kk < 0 counts from the top."""
+    ny, nx = D.shape
+    nz = dbeta.shape[0]
+    assert mask.shape == (ny, nx) and mask.dtype == torch.int32
+    assert h.shape == (nz, ny, nx) and h.dtype == torch.float64 and h.is_contiguous()
+    assert D.dtype == torch.float64 and dbeta.dtype == torch.float64
+    if kk < 0:
+        kk = nz + kk
+    call("getm_update_gvc", nx, ny, nz, float(dsigma), dbeta.data_ptr(), float(Dgamma), 1 + kk, D.data_ptr(),
+         mask.data_ptr(), h.data_ptr(), _s())
 
 
 def new_handle():

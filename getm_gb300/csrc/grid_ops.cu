@@ -528,6 +528,95 @@ __global__ void depth_3d_column_kernel(Depth3DArgs a)
     if (role == 1 && m && a.depth) t2cd_column(plane, nz, p, a.hnt, a.depth);
 }
 
+// c_vertical_advection_to_sources (wrapper.F90:447-485): first-order upstream
+// fluxes of c between the levels of a column (for sinking or floating, with
+// the vertical velocity w at the layer centres, positive upwards, levels
+// ordered surface to bottom), added to the source term s: at interface
+// k | k+1 of two wet levels the flux upward * (w_k + w_k+1) / 2 times the
+// upstream c leaves level k and enters level k+1, in level order.  Nothing
+// changes when w is zero at every interior point (the routine returns
+// early then): a first kernel reduces that test into a flag.
+__global__ void vadv_sources_active_kernel(int nx, int ny, int nz, int halox, int haloy, const double* w, int* flag)
+{
+    const long long plane = (long long)nx * ny;
+    const long long n = plane * nz;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        const long long c = p % plane;
+        const int j = (int)(c / nx), i = (int)(c - (long long)j * nx);
+        if (i >= halox && i < nx - halox && j >= haloy && j < ny - haloy && w[p] != 0.0) {
+            *flag = 1;  // any writer: all write 1
+            return;
+        }
+    }
+}
+
+__global__ void vadv_sources_kernel(int nx, int ny, int nz, int halox, int haloy, const int* mask, const double* c,
+                                    const double* w, const double* h, double* s, const int* flag)
+{
+    if (*flag == 0) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y + haloy;
+    if (i < halox || i >= nx - halox || j >= ny - haloy) return;
+    const long long plane = (long long)nx * ny;
+    const long long p = (long long)j * nx + i;
+    const double upward = -1.0;  // levels ordered surface to bottom
+    for (int k = 0; k < nz - 1; k++) {
+        const long long a = p + k * plane, b = a + plane;
+        if (mask[a] == 1 && mask[b] == 1) {
+            const double local_w = upward * 0.5 * (w[a] + w[b]);
+            const double flux = local_w > 0.0 ? local_w * c[a] : local_w * c[b];
+            s[a] = s[a] - flux / h[a];
+            s[b] = s[b] + flux / h[b];
+        }
+    }
+}
+
+extern "C" int getm_vertical_advection_to_sources(int nx, int ny, int nz, int halox, int haloy, const int* mask,
+                                                  const double* c, const double* w, const double* h, double* s,
+                                                  int* work, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || halox < 0 || haloy < 0 || 2 * halox >= nx || 2 * haloy >= ny)
+        return GETM_ERR_ARG;
+    if (!mask || !c || !w || !h || !s || !work) return GETM_ERR_ARG;
+    if (cudaMemsetAsync(work, 0, sizeof(int), stream) != cudaSuccess) return GETM_ERR_CUDA;
+    const long long n = (long long)nx * ny * nz;
+    const int blocks = (int)(getm_div_up(n, 256) < 4096 ? getm_div_up(n, 256) : 4096);
+    vadv_sources_active_kernel<<<blocks, 256, 0, stream>>>(nx, ny, nz, halox, haloy, w, work);
+    GETM_CHECK_LAUNCH();
+    vadv_sources_kernel<<<dim3(getm_div_up(nx, 128), ny - 2 * haloy), 128, 0, stream>>>(nx, ny, nz, halox, haloy,
+                                                                                      mask, c, w, h, s, work);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// c_update_gvc (wrapper.F90:567-600): general vertical coordinates, layer
+// thicknesses D (dbeta_k + alpha (dsigma - dbeta_k)) where the mask is
+// non-zero, with alpha = (min(Dgamma / D, 1) dsigma - dbeta_kk) /
+// (dsigma - dbeta_kk) giving the reference layer kk (1-based) the thickness
+// min(Dgamma, D) dsigma.
+__global__ void update_gvc_kernel(int nx, int ny, int nz, double dsigma, const double* dbeta, double Dgamma, int kk,
+                                  const double* D, const int* mask, double* h)
+{
+    const long long plane = (long long)nx * ny;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= plane) return;
+    if (mask[p] == 0) return;
+    const double Dp = D[p], db = dbeta[kk - 1];
+    const double alpha = (fmin(Dgamma / Dp, 1.0) * dsigma - db) / (dsigma - db);
+    for (int k = 0; k < nz; k++) h[p + k * plane] = Dp * (dbeta[k] + alpha * (dsigma - dbeta[k]));
+}
+
+extern "C" int getm_update_gvc(int nx, int ny, int nz, double dsigma, const double* dbeta, double Dgamma, int kk,
+                               const double* D, const int* mask, double* h, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || kk < 1 || kk > nz) return GETM_ERR_ARG;
+    if (!dbeta || !D || !mask || !h) return GETM_ERR_ARG;
+    update_gvc_kernel<<<getm_div_up((long long)nx * ny, 128), 128, 0, stream>>>(nx, ny, nz, dsigma, dbeta, Dgamma, kk,
+                                                                                  D, mask, h);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
 extern "C" int getm_update_depth_3d(const getm_depth3d_fields* f, int nx, int ny, int nz, cudaStream_t stream)
 {
     if (!f || nx < 2 || ny < 2 || nz < 1) return GETM_ERR_ARG;

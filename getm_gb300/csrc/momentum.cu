@@ -306,6 +306,69 @@ static int shear_impl(int nx, int ny, int nz, int imin, int imax, int jmin, int 
     return GETM_OK;
 }
 
+// c_shear_frequency2 (momentum.F90:244-268): the squared shear frequency
+// weighted by the viscosity at the four neighbouring velocity points,
+// normalised by the viscosity of the T point; interfaces k = 1..nz-1 of the
+// interior T points with mask > 0.  The same expression and operation order.
+template <typename T>
+__global__ void shear_frequency2_kernel(int nx, int ny, int nz, int ilo, int ihi, int jlo, int jhi,
+                                        const int* __restrict__ mask, const double* __restrict__ h,
+                                        const double* __restrict__ hu, const double* __restrict__ hv,
+                                        const T* __restrict__ uk, const T* __restrict__ vk,
+                                        const T* __restrict__ num, T* __restrict__ SS)
+{
+    int i, j;
+    const int k = blockIdx.y + 1;  // Fortran interface k = 1..nz-1
+    if (!getm_flat_column(nx, jlo, jhi - jlo + 1, i, j) || i < ilo || i > ihi) return;
+    const long long p = (long long)j * nx + i;
+    if (mask[p] <= 0) return;
+    const long long plane = (long long)nx * ny;
+    const long long a = p + (k - 1) * plane, b = p + k * plane;  // layers Fortran k, k+1
+    const long long q = p + k * plane;                            // interface k
+    auto c = [](double x) -> T {
+        if constexpr (std::is_same<T, double>::value) return x;
+        else return getm_d2f_approx(x);
+    };
+    const T due = uk[b] - uk[a], duw = uk[b - 1] - uk[a - 1];
+    const T dvn = vk[b] - vk[a], dvs = vk[b - nx] - vk[a - nx];
+    const T s = due * due / (c(hu[b]) + c(hu[a])) * (num[q] + num[q + 1])
+                + duw * duw / (c(hu[b - 1]) + c(hu[a - 1])) * (num[q - 1] + num[q])
+                + dvn * dvn / (c(hv[b]) + c(hv[a])) * (num[q] + num[q + nx])
+                + dvs * dvs / (c(hv[b - nx]) + c(hv[a - nx])) * (num[q - nx] + num[q]);
+    SS[q] = T(0.5) * s / (T(0.5) * (c(h[a]) + c(h[b]))) / num[q];
+}
+
+template <typename T>
+static int shear2_impl(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* mask,
+                       const double* h, const double* hu, const double* hv, const T* uk, const T* vk, const T* num,
+                       T* SS, cudaStream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || imin < 2 || jmin < 2 || imax >= nx || jmax >= ny || jmax < jmin)
+        return GETM_ERR_ARG;
+    if (!mask || !h || !hu || !hv || !uk || !vk || !num || !SS) return GETM_ERR_ARG;
+    if (nz < 2) return GETM_OK;
+    dim3 grid(getm_div_up((long long)nx * (jmax - jmin + 1), 128), nz - 1);
+    shear_frequency2_kernel<T><<<grid, 128, 0, stream>>>(nx, ny, nz, imin - 1, imax - 1, jmin - 1, jmax - 1, mask, h,
+                                                          hu, hv, uk, vk, num, SS);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+extern "C" int getm_shear_frequency2(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* mask,
+                                     const double* h, const double* hu, const double* hv, const double* uk,
+                                     const double* vk, const double* num, double* SS, cudaStream_t stream)
+{
+    return shear2_impl<double>(nx, ny, nz, imin, imax, jmin, jmax, mask, h, hu, hv, uk, vk, num, SS, stream);
+}
+
+extern "C" int getm_shear_frequency2_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
+                                         const int* mask, const double* h, const double* hu, const double* hv,
+                                         const float* uk, const float* vk, const float* num, float* SS,
+                                         cudaStream_t stream)
+{
+    return shear2_impl<float>(nx, ny, nz, imin, imax, jmin, jmax, mask, h, hu, hv, uk, vk, num, SS, stream);
+}
+
 extern "C" int getm_shear_frequency(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
                                     const int* mask, const double* hu, const double* hv, const double* uk,
                                     const double* vk, double* SS, cudaStream_t stream)

@@ -6,9 +6,11 @@ one is admitted as soon as its estimated device memory fits the HBM budget
 (``ensemble.DomainRunner``), and from then on advanced one 3D step at a time
 by graph replay on one of a few lane streams, interleaved with every other
 active request, so requests that arrive while others run join the mix and
-their work overlaps on the device.  A finished request leaves the mix and
-its memory returns to the budget.  Its state stays resident in HBM for its
-whole life.
+their work overlaps on the device.  A finished request leaves the mix; its
+memory returns to the budget when no request is running (releasing a
+domain's library buffers waits for all work on the device, so it is not
+done while other requests' steps are queued).  Its state stays resident in
+HBM for its whole life.
 
 Admission runs on a worker thread with its own stream: building a domain,
 its eager warm-up steps and the capture of its step graphs (in thread-local
@@ -83,7 +85,7 @@ class Server:
 
     STATE_FIELDS = ("temp", "salt")
 
-    def __init__(self, budget_bytes: float = 150 * GB, lanes: int = 16, max_inflight: int = 3,
+    def __init__(self, budget_bytes: float = 150 * GB, lanes: int = 16, max_inflight: int = 2,
                  device="cuda", keep=(), admission_thread: bool = True, max_building: int = 2):
         """``admission_thread``: set requests up on a worker thread (False:
         in the main loop, between step issues); ``max_building``: requests
@@ -180,10 +182,11 @@ class Server:
         ``admission_thread`` the set-up runs on a worker thread, otherwise at
         most one request is set up per pass of the loop.  ``poll_sleep``:
         seconds the loop sleeps when a pass found nothing to do, doubled
-        after each idle pass up to 20 times that, reset when a step completes
-        or is issued (default: 100 us with the admission thread, which then
-        gets the interpreter: a loop that only polls would otherwise hold it
-        while the worker's every library call gives it up; 0 without).
+        after each idle pass up to 8 times that, reset when a step completes
+        or is issued (default: 0.5 ms with the admission thread, which then
+        gets the interpreter: a loop that polls every 100 us held it half the
+        time and slowed the worker's set-up tenfold; every request keeps
+        max_inflight steps queued, milliseconds of device work; 0 without).
         Returns one Result per admitted request."""
         import queue
         import sys
@@ -192,12 +195,12 @@ class Server:
 
         admit_until = duration if admit_until is None else admit_until
         if poll_sleep is None:
-            poll_sleep = 1e-4 if self.admission_thread else 0.0
+            poll_sleep = 5e-4 if self.admission_thread else 0.0
         idle_sleep = poll_sleep
         pending = sorted(requests, key=lambda r: r.arrival)
         active: List[_Active] = []
         results: List[Result] = []
-        prefetch = ThreadPoolExecutor(max_workers=2)
+        prefetch = ThreadPoolExecutor(max_workers=1)  # one host thread keeps ahead of admission
         futures: Dict[int, object] = {}
 
         def prefetch_ahead():
@@ -221,6 +224,14 @@ class Server:
             sys.setswitchinterval(5e-4)
             worker = threading.Thread(target=self._worker, args=(inbox, ready, start, t0), daemon=True)
             worker.start()
+
+        retired: List[_Active] = []
+
+        def release_retired():
+            for a in retired:
+                self.used -= a.estimate
+                a.runner = None
+            retired.clear()
 
         def take(a: _Active):
             self.used += a.estimate - reserved.pop(a.req.rid, 0.0)
@@ -289,11 +300,16 @@ class Server:
                             a.result.final_state = {n: getattr(sim, n).all_values.clone() for n in self.STATE_FIELDS}
                             a.result.final_state["z"] = sim.T.z.all_values.clone()
                             a.result.final_state["U"] = sim.momentum.U.all_values.clone()
-                        self.used -= a.estimate
-                        a.runner = None
+                        # released later, with the device idle: freeing a
+                        # domain's library buffers (cudaFree) waits for all
+                        # work on the device, every other request's queued
+                        # steps included
+                        retired.append(a)
                     else:
                         keep_active.append(a)
                 active = keep_active
+                if retired and not active and not reserved:
+                    release_retired()
                 if not active and not reserved and (not pending or now > admit_until):
                     break
                 if progressed:
@@ -304,7 +320,7 @@ class Server:
                     # starve the admission worker); every request keeps
                     # max_inflight steps queued, so the device does not wait
                     time.sleep(idle_sleep)
-                    idle_sleep = min(2.0 * idle_sleep, 20.0 * poll_sleep)
+                    idle_sleep = min(2.0 * idle_sleep, 8.0 * poll_sleep)
         finally:
             if worker is not None:
                 inbox.put(None)
@@ -316,6 +332,7 @@ class Server:
                         a.runner = None
             prefetch.shutdown(wait=True, cancel_futures=True)
         torch.cuda.synchronize(self.device)
+        release_retired()
         for a in active:  # abandoned at the deadline: count what completed
             for ev in a.inflight:
                 a.result.step_done.append(start.elapsed_time(ev) / 1000.0)

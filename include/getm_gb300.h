@@ -184,6 +184,21 @@ int getm_alpha(int n, const double* D, double Dmin, double Dcrit, const int* mas
 /* c_elevation2depth: wrapper.F90:437-445 (pyx:49) */
 int getm_elevation2depth(int n, const double* z, const double* H, double Dmin, const int* mask,
                          double* D, cudaStream_t stream);
+/* c_vertical_advection_to_sources: wrapper.F90:447-485 (pyx:65, 574-575):
+ * first-order upstream vertical fluxes of c (w at the layer centres, levels
+ * surface to bottom, mask 3D) added to the source term s; nothing changes
+ * when w is zero at every interior point.  work: one int of device memory
+ * (the test's flag).                                                      */
+int getm_vertical_advection_to_sources(int nx, int ny, int nz, int halox, int haloy, const int* mask,
+                                       const double* c, const double* w, const double* h, double* s,
+                                       int* work, cudaStream_t stream);
+/* c_update_gvc: wrapper.F90:567-600 (pyx:66, 577-585): general vertical
+ * coordinates; layer thicknesses h (nz x ny x nx) where mask != 0 from the
+ * water depth D, the equidistant fraction dsigma, the zoomed fractions
+ * dbeta (nz values, device memory), Dgamma and the 1-based reference
+ * layer kk.                                                               */
+int getm_update_gvc(int nx, int ny, int nz, double dsigma, const double* dbeta, double Dgamma, int kk,
+                    const double* D, const int* mask, double* h, cudaStream_t stream);
 /* c_multiply_add: wrapper.F90:488-494 (pyx:60) */
 int getm_multiply_add(int n, double* tgt, const double* add, double scale_factor,
                       cudaStream_t stream);
@@ -243,6 +258,16 @@ int getm_w_momentum_3d(int nx, int ny, int nz, int imin, int imax, int jmin, int
 int getm_shear_frequency(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax,
                          const int* mask, const double* hu, const double* hv, const double* uk,
                          const double* vk, double* SS, cudaStream_t stream);
+/* c_shear_frequency2: momentum.F90:244-268 (pyx:56, 468-479): the squared
+ * shear frequency weighted by the viscosity num at the four neighbouring
+ * velocity points, over num at the T point; h, hu, hv layer thicknesses of
+ * the T, U, V grids.  _f32: float uk, vk, num, SS.                          */
+int getm_shear_frequency2(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* mask,
+                          const double* h, const double* hu, const double* hv, const double* uk,
+                          const double* vk, const double* num, double* SS, cudaStream_t stream);
+int getm_shear_frequency2_f32(int nx, int ny, int nz, int imin, int imax, int jmin, int jmax, const int* mask,
+                              const double* h, const double* hu, const double* hv, const float* uk,
+                              const float* vk, const float* num, float* SS, cudaStream_t stream);
 /* c_surface_shear_velocity: momentum.F90:270-284 (pyx:57) */
 int getm_surface_shear_velocity(int nx, int ny, int imin, int imax, int jmin, int jmax,
                                 const int* mask, const double* tausx, const double* tausy,

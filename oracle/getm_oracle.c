@@ -747,6 +747,66 @@ void oracle_shear_frequency(int nx_, int ny_, int nz, int imin, int imax, int jm
             }
 }
 
+/* momentum.F90:244-268: interfaces k = 1..nz-1 (the layers Fortran k, k+1 are
+   0-based k-1, k; interface k is 0-based k), left-to-right evaluation */
+void oracle_shear_frequency2(int nx_, int ny_, int nz, int imin, int imax, int jmin, int jmax, const int *mask,
+                             const double *h, const double *hu, const double *hv, const double *uk,
+                             const double *vk, const double *num, double *SS)
+{
+    for (int k = 1; k <= nz - 1; k++)
+        for (int j = jmin - 1; j <= jmax - 1; j++)
+            for (int i = imin - 1; i <= imax - 1; i++) {
+                size_t p = IDX2(i, j);
+                if (mask[p] <= 0) continue;
+                size_t a = IDX3(i, j, k - 1), b = IDX3(i, j, k), q = IDX3(i, j, k);
+                double due = uk[b] - uk[a], duw = uk[b - 1] - uk[a - 1];
+                double dvn = vk[b] - vk[a], dvs = vk[b - nx_] - vk[a - nx_];
+                double s = due * due / (hu[b] + hu[a]) * (num[q] + num[q + 1])
+                           + duw * duw / (hu[b - 1] + hu[a - 1]) * (num[q - 1] + num[q])
+                           + dvn * dvn / (hv[b] + hv[a]) * (num[q] + num[q + nx_])
+                           + dvs * dvs / (hv[b - nx_] + hv[a - nx_]) * (num[q - nx_] + num[q]);
+                SS[q] = 0.5 * s / (0.5 * (h[a] + h[b])) / num[q];
+            }
+}
+
+/* wrapper.F90:447-485: nothing when w is zero at every interior point */
+void oracle_vertical_advection_to_sources(int nx_, int ny_, int nz, int halox, int haloy, const int *mask,
+                                          const double *c, const double *w, const double *h, double *s)
+{
+    int active = 0;
+    for (int k = 0; k < nz && !active; k++)
+        for (int j = haloy; j < ny_ - haloy && !active; j++)
+            for (int i = halox; i < nx_ - halox; i++)
+                if (w[IDX3(i, j, k)] != 0.0) { active = 1; break; }
+    if (!active) return;
+    const double upward = -1.0;
+    for (int k = 0; k < nz - 1; k++)
+        for (int j = haloy; j < ny_ - haloy; j++)
+            for (int i = halox; i < nx_ - halox; i++) {
+                size_t a = IDX3(i, j, k), b = IDX3(i, j, k + 1);
+                if (mask[a] == 1 && mask[b] == 1) {
+                    double local_w = upward * 0.5 * (w[a] + w[b]);
+                    double flux = local_w > 0.0 ? local_w * c[a] : local_w * c[b];
+                    s[a] = s[a] - flux / h[a];
+                    s[b] = s[b] + flux / h[b];
+                }
+            }
+}
+
+/* wrapper.F90:567-600 (kk 1-based) */
+void oracle_update_gvc(int nx_, int ny_, int nz, double dsigma, const double *dbeta, double Dgamma, int kk,
+                       const double *D, const int *mask, double *h)
+{
+    for (int j = 0; j < ny_; j++)
+        for (int i = 0; i < nx_; i++) {
+            size_t p = IDX2(i, j);
+            double r = Dgamma / D[p];
+            double alpha = ((r < 1.0 ? r : 1.0) * dsigma - dbeta[kk - 1]) / (dsigma - dbeta[kk - 1]);
+            if (mask[p] == 0) continue;
+            for (int k = 0; k < nz; k++) h[IDX3(i, j, k)] = D[p] * (dbeta[k] + alpha * (dsigma - dbeta[k]));
+        }
+}
+
 /* momentum.F90:270-284 */
 void oracle_surface_shear_velocity(int nx_, int ny_, int imin, int imax, int jmin, int jmax,
                                    const int *mask, const double *taux, const double *tauy,

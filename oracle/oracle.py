@@ -427,6 +427,31 @@ def shear_frequency(T: OGrid, uk, vk, SS):
     )
 
 
+def shear_frequency2(T: OGrid, uk, vk, num, SS):
+    """pyx:468-479"""
+    _lib.oracle_shear_frequency2(
+        c_int(T.nx_), c_int(T.ny_), c_int(T.nz), c_int(T.halox + 1), c_int(T.halox + T.nx), c_int(T.haloy + 1),
+        c_int(T.haloy + T.ny), _pi(T.mask), _p(T.hn), _p(T.ugrid.hn), _p(T.vgrid.hn), _p(uk), _p(vk), _p(num), _p(SS),
+    )
+
+
+def vertical_advection_to_sources(halox, haloy, mask, c, w, h, s):
+    """pyx:574-575 ((nz, ny, nx) arrays; mask int)"""
+    nz, ny, nx = c.shape
+    _lib.oracle_vertical_advection_to_sources(c_int(nx), c_int(ny), c_int(nz), c_int(halox), c_int(haloy),
+                                              _pi(mask), _p(c), _p(w), _p(h), _p(s))
+
+
+def update_gvc(dsigma, dbeta, Dgamma, kk, D, mask, h):
+    """pyx:577-585"""
+    nz = dbeta.shape[0]
+    ny, nx = D.shape
+    if kk < 0:
+        kk = nz + kk
+    _lib.oracle_update_gvc(c_int(nx), c_int(ny), c_int(nz), c_double(dsigma), _p(np.ascontiguousarray(dbeta)),
+                           c_double(Dgamma), c_int(1 + kk), _p(D), _pi(mask), _p(h))
+
+
 def surface_shear_velocity(T: OGrid, taux, tauy, ustar):
     _lib.oracle_surface_shear_velocity(
         c_int(T.nx_), c_int(T.ny_), c_int(T.halox + 1), c_int(T.halox + T.nx), c_int(T.haloy + 1), c_int(T.haloy + T.ny),

@@ -1,9 +1,10 @@
 """Per-call parity of the momentum-side kernels with the oracle on identical
 seeded inputs: momentum_diffusion (2D and 3D), horizontal_diffusion,
-shear_frequency, surface_shear_velocity, bottom_shear_velocity,
-thickness2center_depth and the Coriolis terms (DEFAULT and ESPELID, 2D and
-3D).  These are the _pygetm calls of python/_pygetm.pyx:318-504 behind
-python/src/wrapper.F90:275-393 and python/src/momentum.F90:12-321, and
+shear_frequency, shear_frequency2, surface_shear_velocity,
+bottom_shear_velocity, thickness2center_depth, the Coriolis terms (DEFAULT
+and ESPELID, 2D and 3D), vertical_advection_to_sources and update_gvc.
+These are the _pygetm calls of python/_pygetm.pyx:318-585 behind
+python/src/wrapper.F90:275-600 and python/src/momentum.F90:12-321, and
 python/pygetm/momentum.py:1127-1148.
 
 Tolerance: FP64, 1e-12 relative to the field's magnitude (the GPU contracts
@@ -12,7 +13,7 @@ multiply-adds, the oracle does not)."""
 import numpy as np
 import pytest
 
-from tests.gpu_helpers import host
+from tests.gpu_helpers import dev, host
 from tests.test_gpu_operators import close, setup, velocity, wrap
 
 pytestmark = pytest.mark.gpu
@@ -184,3 +185,90 @@ def test_coriolis(scheme, three_d):
         wet = dst_h.mask != 0
         _report(f"coriolis scheme {scheme} {'3D' if three_d else '2D'} x={xdir}",
                 close(host(out_d.all_values), out_o, mask=wet))
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_shear_frequency2(dtype):
+    """momentum.F90:244-268: the viscosity-weighted squared shear frequency
+    (pyx:468-479); FP64 to 1e-12 of the field's magnitude, float uk, vk,
+    num, SS to 1e-5."""
+    import torch
+
+    import oracle.oracle as O
+    from getm_gb300 import _pygetm
+    from getm_gb300.core import CENTERS, INTERFACES, Array
+
+    Th, To, Td, rng = setup(seed=64, nz=10)
+    nz = Th.nz
+    uk = velocity(Th.ugrid, rng, nz, 0.5)
+    vk = velocity(Th.vgrid, rng, nz, 0.5)
+    num = rng.uniform(1e-5, 1e-2, (nz + 1, Th.ny_, Th.nx_))
+    if dtype == "float32":
+        uk, vk, num = (x.astype(np.float32).astype(np.float64) for x in (uk, vk, num))
+    SS0 = rng.uniform(0, 1e-3, (nz + 1, Th.ny_, Th.nx_))
+    SS_o = SS0.copy()
+    O.shear_frequency2(To, uk, vk, num, SS_o)
+    td = torch.float64 if dtype == "float64" else torch.float32
+    wrapt = lambda g, a, z: Array(g, dev(a).to(td), z=z)  # noqa: E731
+    SS_d = wrapt(Td, SS0, INTERFACES)
+    _pygetm.shear_frequency2(wrapt(Td.ugrid, uk, CENTERS), wrapt(Td.vgrid, vk, CENTERS), wrapt(Td, num, INTERFACES),
+                             SS_d)
+    assert np.abs(SS_o - SS0).max() > 0.0
+    _report("SS2 " + dtype, close(host(SS_d.all_values).astype(np.float64), SS_o,
+                                  1e-12 if dtype == "float64" else 1e-5))
+
+
+def test_vertical_advection_to_sources():
+    """wrapper.F90:447-485 (pyx:574-575): upstream vertical fluxes of a
+    sinking or floating field into its source term, against the oracle; and
+    no change at all when w is zero at every interior point."""
+    import torch
+
+    import oracle.oracle as O
+    from getm_gb300 import _pygetm
+
+    rng = np.random.default_rng(65)
+    nz, ny, nx = 12, 30, 41
+    mask = (rng.uniform(size=(nz, ny, nx)) > 0.1).astype(np.int32)
+    c = rng.uniform(0.5, 2.0, (nz, ny, nx))
+    h = rng.uniform(1.0, 3.0, (nz, ny, nx))
+    w = rng.uniform(-1e-3, 1e-3, (nz, ny, nx))
+    s0 = rng.uniform(-1e-6, 1e-6, (nz, ny, nx))
+    s_o = s0.copy()
+    O.vertical_advection_to_sources(2, 3, mask, c, w, h, s_o)
+    s_d = dev(s0)
+    _pygetm.vertical_advection_to_sources(2, 3, dev(mask), dev(c), dev(w), dev(h), s_d)
+    _report("vadv sources", close(host(s_d), s_o, 1e-14))
+    # w zero in the interior (non-zero in the halos), NaN in c: unchanged
+    w2 = np.zeros_like(w)
+    w2[:, :3] = 1.0
+    c[3, 10, 10] = np.nan
+    s_d = dev(s0)
+    _pygetm.vertical_advection_to_sources(2, 3, dev(mask), dev(c), dev(w2), dev(h), s_d)
+    torch.cuda.synchronize()
+    assert np.array_equal(host(s_d), s0)
+
+
+def test_update_gvc():
+    """wrapper.F90:567-600 (pyx:577-585): general vertical coordinates
+    against the oracle (1e-14: the GPU contracts the blend into a fused
+    multiply-add)."""
+    import torch
+
+    import oracle.oracle as O
+    from getm_gb300 import _pygetm
+    from getm_gb300.domain import calculate_sigma
+
+    rng = np.random.default_rng(66)
+    nz, ny, nx = 20, 33, 47
+    dbeta = calculate_sigma(nz, 2.0, 1.0)
+    D = rng.uniform(2.0, 400.0, (ny, nx))
+    mask = (rng.uniform(size=(ny, nx)) > 0.2).astype(np.int32)
+    h0 = rng.uniform(size=(nz, ny, nx))
+    for kk in (-1, 0):
+        h_o = h0.copy()
+        O.update_gvc(1.0 / nz, dbeta, 30.0, kk, D, mask, h_o)
+        h_d = dev(h0)
+        _pygetm.update_gvc(1.0 / nz, dev(dbeta), 30.0, kk, dev(D), dev(mask), h_d)
+        torch.cuda.synchronize()
+        _report(f"gvc kk={kk}", close(host(h_d), h_o, 1e-14))

@@ -62,6 +62,8 @@ def _args():
     ap.add_argument("--shelf-steps", type=int, default=100,
                     help="3D steps of the 20-tracer shelf sea, both forms, for its error report (0: skip)")
     ap.add_argument("--shelf-size", default="1000x800x30")
+    ap.add_argument("--no-column-solve", dest="column_solve", action="store_false",
+                    help="skip timing the two float column solves")
     return ap.parse_args()
 
 
@@ -361,10 +363,13 @@ class Runner:
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch on the
 # 400 x 300 x 40 seamount, from ncu captures of this bench (profiles/); None:
-# not captured.  The x pass over both tracers, by storage suffix:
-TRAFFIC_X_PASS = {"_f32": 152.51e6}
-# one one-launch substep, by form:
-TRAFFIC_SUBSTEP = {}
+# not captured.  The x pass over both tracers, by (storage suffix, four
+# cells per lane): profiles/hpass_x_f64s_seamount_400x300x40.md (184.0 +
+# 83.0 MB), and the float-storage one-cell pass of an earlier capture.
+TRAFFIC_X_PASS = {("_f32", 0): 152.51e6, ("_f64s", 1): 267.0e6, ("_f64s", 0): 263.9e6}
+# one one-launch substep, by form: profiles/substep_2d_seamount_400x300.md
+# (60.8 + 5.3 MB; the plane's fields stay in L2)
+TRAFFIC_SUBSTEP = {"mixed": 66.1e6}
 
 
 def _roofline(sim, peak, peak_kind):
@@ -412,14 +417,67 @@ def _roofline(sim, peak, peak_kind):
     # u, hu, h in + h out + per tracer in + out (each 3D field read or written once)
     alg = n3 * (sz + 8 + 8 + 8 + len(fin) * 2 * fsz)
     achieved = alg / t_kernel / 1e9
-    kernel = {"_f32": "hpass_x_inc_kernel<float>", "_f64s": "hpass_x_inc_kernel<double, float>",
-              "": "hpass_x_kernel<double>"}[sfx]
+    # the four-cells-per-lane form runs where the knob asks for it and rows
+    # are whole 16-byte vectors
+    from getm_gb300 import autotune
+
+    vec = int(sfx != "" and autotune.current()["xpass_vec"] == 1 and T.nx_ % 4 == 0)
+    kernel = {("_f32", 0): "hpass_x_inc_kernel<float, float>", ("_f32", 1): "hpass_x_vec_kernel<float, float>",
+              ("_f64s", 0): "hpass_x_inc_kernel<double, float>", ("_f64s", 1): "hpass_x_vec_kernel<double, float>",
+              ("", 0): "hpass_x_kernel<double>"}[(sfx, vec)]
     # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
     # of this kernel on this workload, from an ncu capture of this bench
-    traffic = TRAFFIC_X_PASS.get(sfx)
+    traffic = TRAFFIC_X_PASS.get((sfx, vec))
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": f"{kernel} (2 tracers)",
             "bytes_per_launch": alg, "us_per_launch": t_kernel * 1e6, "peak_kind": peak_kind}
+
+
+def _column_solve_leg(sim, device):
+    """The mixed form's float column solve of both FP64-stored tracers (one
+    getm_vertical_diffusion_batch_f64s call) timed with CUDA events, one
+    thread per column against the segmented solve (GETM_TUNE_COLUMN_SOLVE),
+    on copies of the live seamount tracers and on small seamounts of
+    ensemble-member size."""
+    import torch
+
+    from getm_gb300 import autotune, workloads
+    from getm_gb300.core import Array, CENTERS
+
+    def time_solves(s):
+        T = s.T
+        vd = s.tracers._vertical_diffusion
+        fields = [Array(T, t.all_values.clone(), z=CENTERS) for t in s.tracers._tracers]
+        mol = [t.molecular_diffusivity for t in s.tracers._tracers]
+        n3 = T.nx * T.ny * T.nz
+        out = {"domain": f"{T.nx}x{T.ny}x{T.nz}"}
+        for name, knob in (("thread_per_column", 0), ("segmented", 1)):
+            autotune.apply(dict(s.tiles or {}, column_solve=knob))
+            for _ in range(3):
+                vd.batch(s.nuh, s.macrotimestep, fields, mol, None, [None] * len(fields))
+            torch.cuda.synchronize()
+            reps = 20
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                vd.batch(s.nuh, s.macrotimestep, fields, mol, None, [None] * len(fields))
+            e1.record()
+            torch.cuda.synchronize()
+            us = e0.elapsed_time(e1) / reps * 1000.0
+            # nuh (float) and both thicknesses read, two FP64 fields read and written
+            alg = n3 * (4 + 8 + 8 + len(fields) * 16)
+            out[name] = {"us": us, "gbs": alg / us / 1e3}
+        autotune.apply(s.tiles)
+        out["speedup"] = out["thread_per_column"]["us"] / out["segmented"]["us"]
+        return out
+
+    res = [time_solves(sim)]
+    for nx, ny, nz in ((64, 64, 20), (128, 128, 30), (256, 192, 40)):
+        s = _make_sim(workloads.seamount(nx=nx, ny=ny, nz=nz, dx=2000.0 * 400 / nx), "mixed", device)
+        s.advance()
+        res.append(time_solves(s))
+        del s
+    return res
 
 
 def _round_tracers(sim):
@@ -841,6 +899,8 @@ def run_ours(args):
             "split2d_status": {f: runners[f].sim.split2d_status() for f in forms}}
     if substep is not None:
         line["substep_kernel"] = substep
+    if primary == "mixed" and args.column_solve:
+        line["column_solve"] = _column_solve_leg(runners[primary].sim, device)
     for f in forms:
         if f != primary:
             line[f] = {"value": values[f], "ms_per_step": ms[f] / nsteps, "e2e": e2e[f]["value"]}

@@ -33,9 +33,10 @@ KNOBS: Dict[str, Tuple[int, Tuple[int, ...]]] = {
     "column_rows": (2, (1, 2, 4)),
     "substep_blocks_per_sm": (3, (0, 1)),
     "xpass_vec": (4, (1, 0)),
+    "column_solve": (5, (0, 1)),
 }
 DEFAULTS: Dict[str, int] = {"xpass_rows": 8, "ymarch_chunk": 32, "column_rows": 4, "substep_blocks_per_sm": 0,
-                            "xpass_vec": 1}
+                            "xpass_vec": 1, "column_solve": 0}
 CACHE_PATH = Path(__file__).resolve().parent / "tiles.json"
 
 _applied = threading.local()

@@ -24,7 +24,7 @@ extern "C" int getm_launch_count(unsigned long long* count)
 
 // Launch-shape knobs, per host thread (a thread that captures a domain's
 // graphs sets its own shapes without disturbing another thread's launches).
-static thread_local int g_tune[GETM_TUNE_NKNOBS] = {8, 32, 4, 0, 1};
+static thread_local int g_tune[GETM_TUNE_NKNOBS] = {8, 32, 4, 0, 1, 0};
 
 static bool tune_valid(int knob, int v)
 {
@@ -34,6 +34,7 @@ static bool tune_valid(int knob, int v)
     case GETM_TUNE_COLUMN_ROWS: return v == 1 || v == 2 || v == 4;
     case GETM_TUNE_SUBSTEP_BLOCKS: return v >= 0 && v <= 2;
     case GETM_TUNE_XPASS_VEC: return v == 0 || v == 1;
+    case GETM_TUNE_COLUMN_SOLVE: return v == 0 || v == 1;
     default: return false;
     }
 }

@@ -420,10 +420,321 @@ __global__ void __launch_bounds__(128, 7) vd_inc_kernel(VDArgs<float, S> a)
     for (; t0 < a.ntracer; t0++) vd_inc_sweep<1, SRC, S>(a, c, t0);
 }
 
+// ---------------------------------------------------------------------------
+// Segmented column solve (mixed form): VD_NSEG warps share 32 columns
+// ---------------------------------------------------------------------------
+// The partition method for tridiagonal systems (H. H. Wang, ACM Trans. Math.
+// Softw. 7 (1981) 170-183), in the thread-per-segment form of the hybrid
+// Thomas/PCR solvers (A. Laszlo, M. Giles, J. Appleyard, ACM Trans. Math.
+// Softw. 42 (2016) 31).  Warp s of a block owns levels klo..khi (about
+// nz / VD_NSEG of them) of the block's 32 columns; lane i is column i, so
+// every load and store is still a coalesced 128- or 256-byte row of a level.
+// Each thread
+//   1. forms the rows of its levels with the arithmetic of vd_inc_sweep
+//      (the increment form: A dx = a4 - A x) and, sweeping up, eliminates
+//      each row's coupling to the level below in favour of the segment's
+//      first unknown, then, sweeping down through shared memory, the
+//      coupling to the level above in favour of its last unknown, so that
+//      dx_i = d_i - a_i dx_first - g_i dx_last inside the segment;
+//   2. adds the rows of its first and last unknown to a reduced tridiagonal
+//      system of 2 VD_NSEG unknowns per column, which warp 0 solves by
+//      Thomas elimination in shared memory;
+//   3. substitutes the two back into its levels and adds the increments to
+//      the stored values.
+// A column's chain of dependent steps is VD_NSEG times shorter than the
+// serial sweep's, and the elimination coefficients stay in shared memory
+// (no global workspace).  It costs one reciprocal and about twice the
+// multiply-adds per row and level; the rounding differs from the serial
+// sweep's by float rounding of the increments.  Used for 2 VD_NSEG <= nz <=
+// VD_NSEG * VD_SEG_MAXM when the GETM_TUNE_COLUMN_SOLVE knob asks for it.
+constexpr int VD_NSEG = 4;
+constexpr int VD_SEG_MAXM = 16;
+constexpr int VD_SEG_THREADS = 32 * VD_NSEG;
+
+// Shared memory of one launch: 3 NT (maxm - 2) per-level coefficients per
+// thread (levels strictly inside a segment), and the reduced systems of the
+// block's 32 columns (lower, diagonal, upper, right-hand side; the solution
+// overwrites the right-hand side).
+static size_t vd_seg_smem(int nz, int nt)
+{
+    const int maxm = (nz + VD_NSEG - 1) / VD_NSEG;
+    return sizeof(float) * ((size_t)3 * nt * (maxm > 2 ? maxm - 2 : 0) * VD_SEG_THREADS +
+                            (size_t)4 * nt * 2 * VD_NSEG * 32);
+}
+
+template <int NT, bool SRC, typename S>
+__device__ __forceinline__ void vd_seg_group(const VDArgs<float, S>& a, long long c, bool act, int t0, int s,
+                                             int klo, int m, int slots, float* __restrict__ rows,
+                                             float* __restrict__ red, int tid, int tx)
+{
+    constexpr int R = 2 * VD_NSEG;
+    const long long P = a.plane;
+    const int nz = a.nz;
+    // coefficient q (0: a, 1: g, 2: d) of field t at inner level ii (1..m-2)
+#define VD_ROW(t, q, ii) rows[(((t) * 3 + (q)) * slots + (ii) - 1) * VD_SEG_THREADS + tid]
+    // reduced system of this column: q 0 lower, 1 diagonal, 2 upper, 3 rhs
+#define VD_RED(t, q, r) red[(((t) * 4 + (q)) * R + (r)) * 32 + tx]
+    if (act) {
+        const double* __restrict__ ho = a.ho + c;
+        const double* __restrict__ hn = a.hn + c;
+        const float* __restrict__ nuh = a.nuh + c;
+        const bool one_h = a.ho == a.hn;
+        const float co = (float)(1.0 - a.cnpar), cn = (float)a.cnpar, dt2 = (float)(2.0 * a.dt);
+        S* v[NT];
+        const float* e2[NT];
+        const float* e4[NT];
+        float mol[NT];
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            v[t] = a.var[t0 + t] + c;
+            e2[t] = SRC && a.ea2[t0 + t] ? a.ea2[t0 + t] + c : nullptr;
+            e4[t] = SRC && a.ea4[t0 + t] ? a.ea4[t0 + t] + c : nullptr;
+            mol[t] = (float)a.molecular[t0 + t];
+        }
+        // level k = klo; the interface below it (k >= 1)
+        int k = klo;
+        float hoF = vd_h<float>(ho[k * P]), hnF = vd_h<float>(hn[k * P]);
+        float dh = one_h ? 0.f : getm_d2f_approx(ho[k * P] - hn[k * P]);
+        S xc[NT];
+        float aob[NT], anb[NT], ddn[NT];
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            xc[t] = v[t][k * P];
+            aob[t] = anb[t] = ddn[t] = 0.f;
+        }
+        if (k >= 1) {
+            const float hoFb = vd_h<float>(ho[(k - 1) * P]), hnFb = vd_h<float>(hn[(k - 1) * P]);
+            const float nb = nuh[k * P];
+#pragma unroll
+            for (int t = 0; t < NT; t++) {
+                const float x = dt2 * (nb + mol[t]);
+                aob[t] = co * x / (hoF + hoFb);
+                anb[t] = cn * x / (hnF + hnFb);
+                ddn[t] = inc_f<S>(v[t][(k - 1) * P] - xc[t]);
+            }
+        }
+        // operands of the level above (k + 1), one level ahead of the arithmetic
+        double ho_a = 0.0, hn_a = 0.0;
+        float nuh_a = 0.f, e2c[NT], e4c[NT];
+        S xa[NT];
+        if (k + 1 < nz) {
+            ho_a = ho[(k + 1) * P];
+            hn_a = hn[(k + 1) * P];
+            nuh_a = nuh[(k + 1) * P];
+        }
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            xa[t] = k + 1 < nz ? v[t][(k + 1) * P] : S(0);
+            e2c[t] = SRC && e2[t] ? e2[t][k * P] : 0.f;
+            e4c[t] = SRC && e4[t] ? e4[t][k * P] : 0.f;
+        }
+        float L0[NT], D0[NT], U0[NT], R0[NT], al[NT], ga[NT], de[NT];
+        for (int ii = 0; ii < m; ii++, k++) {
+            const bool top = k == nz - 1, bot = k == 0;
+            // raw operands of level k + 2 and the sources of level k + 1
+            double ho_n = 0.0, hn_n = 0.0;
+            float nuh_n = 0.f, e2n[NT], e4n[NT];
+            S xn[NT];
+            if (k + 2 < nz) {
+                ho_n = ho[(k + 2) * P];
+                hn_n = hn[(k + 2) * P];
+                nuh_n = nuh[(k + 2) * P];
+            }
+#pragma unroll
+            for (int t = 0; t < NT; t++) {
+                xn[t] = k + 2 < nz ? v[t][(k + 2) * P] : S(0);
+                e2n[t] = SRC && e2[t] && k + 1 < nz ? e2[t][(k + 1) * P] : 0.f;
+                e4n[t] = SRC && e4[t] && k + 1 < nz ? e4[t][(k + 1) * P] : 0.f;
+            }
+            const float hoFa = top ? 0.f : vd_h<float>(ho_a), hnFa = top ? 0.f : vd_h<float>(hn_a);
+            const float dha = (one_h || top) ? 0.f : getm_d2f_approx(ho_a - hn_a);
+#pragma unroll
+            for (int t = 0; t < NT; t++) {
+                // interface above level k (vd_aux with C level k) and the
+                // difference to the level above, as in vd_inc_sweep
+                float aoa = 0.f, ana = 0.f, dup = 0.f;
+                if (!top) {
+                    const float x = dt2 * (nuh_a + mol[t]);
+                    aoa = co * x / (hoFa + hoF);
+                    ana = cn * x / (hnFa + hnF);
+                    dup = inc_f<S>(xa[t] - xc[t]);
+                }
+                const float xk = inc_f<S>(xc[t]);
+                float dg, rh;
+                if (top) {
+                    dg = hnF + anb[t];
+                    rh = xk * dh + ddn[t] * (aob[t] + anb[t]);
+                } else if (bot) {
+                    dg = hnF + ana;
+                    rh = xk * dh + dup * (aoa + ana);
+                } else {
+                    dg = hnF + ana + anb[t];
+                    rh = xk * dh + dup * (aoa + ana) + ddn[t] * (aob[t] + anb[t]);
+                }
+                if (SRC && e2[t]) rh = rh + e2c[t] * xk;
+                if (SRC && e2[t]) dg = dg - e2c[t];
+                if (SRC && e4[t]) rh = rh + e4c[t];
+                const float lw = bot ? 0.f : -anb[t];
+                const float up = top ? 0.f : -ana;
+                if (ii == 0) {
+                    L0[t] = lw; D0[t] = dg; U0[t] = up; R0[t] = rh;
+                } else if (ii == 1) {
+                    const float inv = 1.f / dg;
+                    al[t] = lw * inv; ga[t] = up * inv; de[t] = rh * inv;
+                } else {
+                    const float inv = 1.f / (dg - lw * ga[t]);
+                    al[t] = -(lw * al[t]) * inv;
+                    ga[t] = up * inv;
+                    de[t] = (rh - lw * de[t]) * inv;
+                }
+                if (ii >= 1 && ii < m - 1) {
+                    VD_ROW(t, 0, ii) = al[t];
+                    VD_ROW(t, 1, ii) = ga[t];
+                    VD_ROW(t, 2, ii) = de[t];
+                }
+                aob[t] = aoa; anb[t] = ana; ddn[t] = -dup;
+                xc[t] = xa[t]; xa[t] = xn[t];
+                e2c[t] = e2n[t]; e4c[t] = e4n[t];
+            }
+            hoF = hoFa; hnF = hnFa; dh = dha;
+            ho_a = ho_n; hn_a = hn_n; nuh_a = nuh_n;
+        }
+        // down through the inner levels: dx_ii = d - a dx_first - g dx_last
+        float as[NT], gs[NT], ds[NT];
+#pragma unroll
+        for (int t = 0; t < NT; t++) { as[t] = 0.f; gs[t] = -1.f; ds[t] = 0.f; }
+        for (int ii = m - 2; ii >= 1; ii--) {
+#pragma unroll
+            for (int t = 0; t < NT; t++) {
+                const float a_ = VD_ROW(t, 0, ii), g_ = VD_ROW(t, 1, ii), d_ = VD_ROW(t, 2, ii);
+                ds[t] = d_ - g_ * ds[t];
+                as[t] = a_ - g_ * as[t];
+                gs[t] = -(g_ * gs[t]);
+                VD_ROW(t, 0, ii) = as[t];
+                VD_ROW(t, 1, ii) = gs[t];
+                VD_ROW(t, 2, ii) = ds[t];
+            }
+        }
+        // the segment's rows of the reduced system
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            VD_RED(t, 0, 2 * s) = L0[t];
+            VD_RED(t, 1, 2 * s) = D0[t] - U0[t] * as[t];
+            VD_RED(t, 2, 2 * s) = -(U0[t] * gs[t]);
+            VD_RED(t, 3, 2 * s) = R0[t] - U0[t] * ds[t];
+            VD_RED(t, 0, 2 * s + 1) = al[t];
+            VD_RED(t, 1, 2 * s + 1) = 1.f;
+            VD_RED(t, 2, 2 * s + 1) = ga[t];
+            VD_RED(t, 3, 2 * s + 1) = de[t];
+        }
+    }
+    __syncthreads();
+    if (s == 0 && act) {
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            float cp[R], dp[R];
+            cp[0] = VD_RED(t, 2, 0) / VD_RED(t, 1, 0);
+            dp[0] = VD_RED(t, 3, 0) / VD_RED(t, 1, 0);
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                const float lw = VD_RED(t, 0, r);
+                const float inv = 1.f / (VD_RED(t, 1, r) - lw * cp[r - 1]);
+                cp[r] = VD_RED(t, 2, r) * inv;
+                dp[r] = (VD_RED(t, 3, r) - lw * dp[r - 1]) * inv;
+            }
+            float x = dp[R - 1];
+            VD_RED(t, 3, R - 1) = x;
+#pragma unroll
+            for (int r = R - 2; r >= 0; r--) {
+                x = dp[r] - cp[r] * x;
+                VD_RED(t, 3, r) = x;
+            }
+        }
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            S* __restrict__ vt = a.var[t0 + t] + c;
+            const float xF = VD_RED(t, 3, 2 * s), xL = VD_RED(t, 3, 2 * s + 1);
+            S xo = vt[klo * P];
+            for (int ii = 0; ii < m; ii++) {
+                const int k = klo + ii;
+                const S xnext = ii + 1 < m ? vt[(k + 1) * P] : S(0);
+                const float dx = ii == 0 ? xF
+                                 : ii == m - 1 ? xL
+                                               : VD_ROW(t, 2, ii) - VD_ROW(t, 0, ii) * xF - VD_ROW(t, 1, ii) * xL;
+                vt[k * P] = inc_add<S>(xo, dx);
+                xo = xnext;
+            }
+        }
+    }
+    __syncthreads();  // shared memory is reused by the next group of fields
+#undef VD_ROW
+#undef VD_RED
+}
+
+// One row j of 32 columns per block (blockIdx.x: 32-column strip, blockIdx.y:
+// row); fields in groups of NT (then an odd last one alone).
+template <int NT, bool SRC, typename S>
+__global__ void __launch_bounds__(VD_SEG_THREADS, 4) vd_seg_kernel(VDArgs<float, S> a)
+{
+    extern __shared__ __align__(16) unsigned char vd_smem[];
+    const int tx = threadIdx.x, s = threadIdx.y, tid = s * 32 + tx;
+    const int i = blockIdx.x * 32 + tx, j = blockIdx.y;
+    const long long c = (long long)j * a.nx_ + i;
+    const bool act = i < a.nx_ && a.mask[c] == 1;
+    const int nz = a.nz;
+    const int klo = s * nz / VD_NSEG, m = (s + 1) * nz / VD_NSEG - klo;
+    const int maxm = (nz + VD_NSEG - 1) / VD_NSEG;
+    const int slots = maxm > 2 ? maxm - 2 : 0;
+    float* rows = (float*)vd_smem;
+    float* red = rows + (size_t)3 * NT * slots * VD_SEG_THREADS;
+    int t0 = 0;
+    for (; t0 + NT <= a.ntracer; t0 += NT) vd_seg_group<NT, SRC, S>(a, c, act, t0, s, klo, m, slots, rows, red, tid, tx);
+    if constexpr (NT > 1)
+        for (; t0 < a.ntracer; t0++) vd_seg_group<1, SRC, S>(a, c, act, t0, s, klo, m, slots, rows, red, tid, tx);
+}
+
+template <int NT, bool SRC, typename S>
+static int vd_seg_launch_one(VDArgs<float, S>& a, cudaStream_t stream)
+{
+    const size_t smem = vd_seg_smem(a.nz, NT);
+    if (smem > 48 * 1024) {
+        // nz up to VD_NSEG * VD_SEG_MAXM needs at most ~60 KB
+        if (cudaFuncSetAttribute(vd_seg_kernel<NT, SRC, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return GETM_ERR_CUDA;
+    }
+    const dim3 grid(getm_div_up(a.nx_, 32), a.ny_), block(32, VD_NSEG);
+    vd_seg_kernel<NT, SRC, S><<<grid, block, smem, stream>>>(a);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
+// Whether the segmented solve takes this call (knob set, nz in range).
+static bool vd_seg_applies(int nz)
+{
+    return getm_tune(GETM_TUNE_COLUMN_SOLVE) == 1 && nz >= 2 * VD_NSEG && nz <= VD_NSEG * VD_SEG_MAXM;
+}
+
+template <typename S>
+static int vd_seg_launch(VDArgs<float, S>& a, cudaStream_t stream)
+{
+    bool src = false;
+    for (int t = 0; t < a.ntracer; t++) src = src || a.ea2[t] || a.ea4[t];
+    const bool pairs = a.ntracer > 1;
+    if (src && pairs) return vd_seg_launch_one<2, true, S>(a, stream);
+    if (src) return vd_seg_launch_one<1, true, S>(a, stream);
+    if (pairs) return vd_seg_launch_one<2, false, S>(a, stream);
+    return vd_seg_launch_one<1, false, S>(a, stream);
+}
+
 // The increment-form solve for FP64-stored fields (float solve, nuh and
 // sources; work: 2 nz planes of floats per field of a pair).
 static int vd_launch_f64s(VDArgs<float, double>& a, cudaStream_t stream)
 {
+    if (a.nz > 1 && vd_seg_applies(a.nz)) return vd_seg_launch(a, stream);
     if (!a.work) return GETM_ERR_ARG;
     const int rows = getm_tune(GETM_TUNE_COLUMN_ROWS);
     const dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, rows)), block(32, rows);
@@ -460,6 +771,7 @@ static int vd_launch(VDArgs<T>& a, cudaStream_t stream)
     if (a.work) {
         dim3 grid(getm_div_up(a.nx_, 128), a.ny_);
         if constexpr (getm_increment_form<T>) {
+            if (a.nz > 1 && !a.auxo && vd_seg_applies(a.nz)) return vd_seg_launch(a, stream);
             if (a.nz > 1 && !a.auxo) {
                 const int rows = getm_tune(GETM_TUNE_COLUMN_ROWS);
                 const dim3 grid(getm_div_up(a.nx_, 32), getm_div_up(a.ny_, rows)), block(32, rows);

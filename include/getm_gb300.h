@@ -319,13 +319,19 @@ int getm_launch_count(unsigned long long* count);
  *                             0 = as many as fit (default), 1, 2 (capped at what fits)
  *   GETM_TUNE_XPASS_VEC       3D x pass in increment form: 1 = four cells per lane
  *                             where rows allow 16-byte vectors (default), 0 = one
- *                             cell per lane (both give the same bits)            */
+ *                             cell per lane (both give the same bits)
+ *   GETM_TUNE_COLUMN_SOLVE    float column solve (mixed form): 0 = one thread per
+ *                             column (default), 1 = four warps per 32 columns, each
+ *                             owning a quarter of the levels (partition method),
+ *                             for 8 <= nz <= 64.  Unlike the other knobs this one
+ *                             changes the rounding of the solve's increments.   */
 #define GETM_TUNE_XPASS_ROWS 0
 #define GETM_TUNE_YMARCH_CHUNK 1
 #define GETM_TUNE_COLUMN_ROWS 2
 #define GETM_TUNE_SUBSTEP_BLOCKS 3
 #define GETM_TUNE_XPASS_VEC 4
-#define GETM_TUNE_NKNOBS 5
+#define GETM_TUNE_COLUMN_SOLVE 5
+#define GETM_TUNE_NKNOBS 6
 int getm_tune_set(int knob, int value);
 int getm_tune_get(int knob, int* value);
 

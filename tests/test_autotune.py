@@ -12,12 +12,13 @@ def _model(opt):
     """A separable step-time model with its minimum at ``opt``."""
     def measure(t):
         return 1.0 + sum(abs(autotune.KNOBS[k][1].index(t[k]) - autotune.KNOBS[k][1].index(opt[k])) * w
-                         for w, k in zip((0.3, 0.2, 0.1, 0.05, 0.02), autotune.KNOBS))
+                         for w, k in zip((0.3, 0.2, 0.1, 0.05, 0.02, 0.01), autotune.KNOBS))
     return measure
 
 
 def test_search_finds_the_optimum_of_a_separable_model():
-    opt = {"xpass_rows": 2, "ymarch_chunk": 64, "column_rows": 1, "substep_blocks_per_sm": 1, "xpass_vec": 0}
+    opt = {"xpass_rows": 2, "ymarch_chunk": 64, "column_rows": 1, "substep_blocks_per_sm": 1, "xpass_vec": 0,
+           "column_solve": 1}
     best, t, trials = autotune.search(_model(opt))
     assert best == opt and t == pytest.approx(1.0)
     # coordinate descent: one pass over the candidates of every knob, then a

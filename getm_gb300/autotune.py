@@ -37,6 +37,8 @@ KNOBS: Dict[str, Tuple[int, Tuple[int, ...]]] = {
 }
 DEFAULTS: Dict[str, int] = {"xpass_rows": 8, "ymarch_chunk": 32, "column_rows": 4, "substep_blocks_per_sm": 0,
                             "xpass_vec": 1, "column_solve": 0}
+# knobs of kernels that only the mixed form runs
+FLOAT_ONLY = frozenset({"column_solve"})
 CACHE_PATH = Path(__file__).resolve().parent / "tiles.json"
 
 _applied = threading.local()
@@ -203,10 +205,13 @@ def step_timer(sim, replays: int = 4) -> Callable[[Dict[str, int]], float]:
     return measure
 
 
-def tune(sim, rounds: int = 2, replays: int = 4) -> Tuple[Dict[str, int], float, float, list]:
+def tune(sim, rounds: int = 2, replays: int = 4, only: Optional[Iterable[str]] = None,
+         start: Optional[Dict[str, int]] = None) -> Tuple[Dict[str, int], float, float, list]:
     """Tune the shapes on a started simulation (warmed up here with two eager
-    3D steps).  Returns (shapes, ms per step, ms per step with the defaults,
-    trials).  Leaves the defaults applied."""
+    3D steps).  ``only``: search just these knobs; ``start``: the shapes to
+    start from (default: DEFAULTS), e.g. a bucket's cached shapes when a knob
+    is added.  Returns (shapes, ms per step, ms per step with the starting
+    shapes, trials).  Leaves the defaults applied."""
     import torch
 
     apply(None)
@@ -214,13 +219,23 @@ def tune(sim, rounds: int = 2, replays: int = 4) -> Tuple[Dict[str, int], float,
         sim.advance()
     torch.cuda.synchronize(sim.T.device)
     measure = step_timer(sim, replays)
-    knobs = dict(KNOBS)
+    knobs = {k: v for k, v in KNOBS.items() if only is None or k in set(only)}
     if sim._split2d is None:  # no one-launch substep in this configuration
-        knobs.pop("substep_blocks_per_sm")
-    best, t, trials = search(measure, knobs=knobs, rounds=rounds)
-    default_t = next(tt for tl, tt in trials if tl == DEFAULTS)
+        knobs.pop("substep_blocks_per_sm", None)
+    if sim.precision != "mixed":
+        for k in FLOAT_ONLY:
+            knobs.pop(k, None)
+    first = dict(DEFAULTS, **(start or {}))
+    best, t, trials = search(measure, knobs=knobs, start=first, rounds=rounds)
+    first_t = next(tt for tl, tt in trials if tl == first)
     apply(None)
-    return best, t, default_t, trials
+    return best, t, first_t, trials
+
+
+def _applies(precision: str, only: Optional[Iterable[str]]) -> bool:
+    """Whether a search over the knobs ``only`` (None: all) has anything to
+    tune in a domain of this precision."""
+    return only is None or precision == "mixed" or any(k not in FLOAT_ONLY for k in only)
 
 
 def _tune_main(argv: Optional[Iterable[str]] = None) -> None:
@@ -240,8 +255,25 @@ def _tune_main(argv: Optional[Iterable[str]] = None) -> None:
     ap.add_argument("--sides", default="64,96,128,192,256,384,512")
     ap.add_argument("--nzs", default="20,30,40")
     ap.add_argument("--no-seamount", action="store_true")
+    ap.add_argument("--knobs", default="", help="search only these knobs (comma-separated)")
+    ap.add_argument("--refine", action="store_true",
+                    help="start each bucket from its cached shapes (and keep its reference time)")
     args = ap.parse_args(list(argv) if argv is not None else None)
     cache = TileCache.load(args.out)
+    only = [k for k in args.knobs.split(",") if k] or None
+    for k in only or ():
+        if k not in KNOBS:
+            raise SystemExit(f"unknown knob {k!r}")
+
+    def run(sim, nx, ny, nz, prec, domain, replays):
+        key = bucket(nx, ny, nz, prec)
+        old = cache.entries.get(key) if args.refine else None
+        best, t, t0, _ = tune(sim, replays=replays, only=only, start=old["tiles"] if old else None)
+        # the time with the defaults stays the one measured in the full search
+        default_t = old["default_ms_per_step"] if old else t0
+        cache.store(nx, ny, nz, prec, best, t, default_t, domain)
+        return best, t, t0
+
     dev = "cuda"
     sides = [int(s) for s in args.sides.split(",") if s]
     nzs = [int(s) for s in args.nzs.split(",") if s]
@@ -250,9 +282,8 @@ def _tune_main(argv: Optional[Iterable[str]] = None) -> None:
         for nz in nzs:
             wl = workloads.ensemble_member(rng, nmin=n, nmax=n, nzmin=nz, nzmax=nz)
             sim = make_member(wl, "mixed", device=dev)
-            best, t, t0, _ = tune(sim, replays=4)
-            cache.store(wl.T.nx, wl.T.ny, wl.T.nz, "mixed", best, t, t0, "ensemble member")
-            print(f"member {wl.T.nx}x{wl.T.ny}x{wl.T.nz}: {best} {t:.3f} ms/step (defaults {t0:.3f})", flush=True)
+            best, t, t0 = run(sim, wl.T.nx, wl.T.ny, wl.T.nz, "mixed", "ensemble member", 4)
+            print(f"member {wl.T.nx}x{wl.T.ny}x{wl.T.nz}: {best} {t:.3f} ms/step (start {t0:.3f})", flush=True)
             del sim
             torch.cuda.empty_cache()
     # the benchmark domains last: a member of the same size bucket must not
@@ -260,15 +291,14 @@ def _tune_main(argv: Optional[Iterable[str]] = None) -> None:
     if not args.no_seamount:
         wl = workloads.seamount()
         p = wl.params
-        for prec in ("mixed", "fp64"):
+        for prec in [p for p in ("mixed", "fp64") if _applies(p, only)]:
             sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=prec, device=dev)
             zc = sim.T.zc.all_values
             sim.temp.all_values.copy_(torch.where(sim.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
                                                   sim.temp.all_values.double()))
             sim.start(p["timestep"], p["split_factor"])
-            best, t, t0, _ = tune(sim, replays=3 if prec == "fp64" else 6)
-            cache.store(wl.T.nx, wl.T.ny, wl.T.nz, prec, best, t, t0, "seamount")
-            print(f"seamount {prec}: {best} {t:.3f} ms/step (defaults {t0:.3f})", flush=True)
+            best, t, t0 = run(sim, wl.T.nx, wl.T.ny, wl.T.nz, prec, "seamount", 3 if prec == "fp64" else 6)
+            print(f"seamount {prec}: {best} {t:.3f} ms/step (start {t0:.3f})", flush=True)
             del sim
             torch.cuda.empty_cache()
     cache.save(args.out)

@@ -77,3 +77,17 @@ def test_knob_table_of_the_c_abi():
     with pytest.raises(KeyError):
         autotune.apply({"no_such_knob": 1})
     assert autotune.current() == autotune.DEFAULTS
+
+
+def test_refining_one_knob_from_cached_shapes():
+    """A knob added later is searched alone, starting from a bucket's cached
+    shapes (``python -m getm_gb300.autotune --knobs column_solve --refine``);
+    knobs that only the mixed form's kernels read are not searched for FP64."""
+    cached = dict(autotune.DEFAULTS, xpass_rows=2, ymarch_chunk=64)
+    opt = dict(cached, column_solve=1, column_rows=1)
+    best, t, trials = autotune.search(_model(opt), knobs={"column_solve": autotune.KNOBS["column_solve"]},
+                                      start=cached)
+    assert best == dict(cached, column_solve=1)
+    assert {k for x, _ in trials for k in x if x[k] != cached[k]} == {"column_solve"}
+    assert not autotune._applies("fp64", ["column_solve"])
+    assert autotune._applies("fp64", ["column_solve", "xpass_rows"]) and autotune._applies("mixed", ["column_solve"])

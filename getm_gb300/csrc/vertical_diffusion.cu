@@ -16,7 +16,9 @@
 // var).  The mixed form's solve (vd_inc_kernel) takes fields in pairs and
 // issues each level's loads one level ahead.  A warp-per-column PCR solve would
 // cost O(nz log nz) FP64 divides per column instead of O(nz); GB300's FP64
-// rate makes the serial Thomas sweep the faster choice.
+// rate makes the serial Thomas sweep the faster choice for the FP64 form.
+// For domains with few columns the mixed form can instead split each column
+// into four segments, one warp each (vd_seg_kernel, the partition method).
 #include <stdlib.h>
 #include <string.h>
 

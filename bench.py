@@ -245,18 +245,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _make_sim(wl, precision, device, round_to_float32=True, tracer_storage=None):
+def _make_sim(wl, precision, device, round_to_float32=True, tracer_storage=None, ip_arithmetic=None):
     """Seamount simulation from rest; the initial temperature (20 -> 4 degC,
     linear in depth) is rounded to float32 unless told otherwise, so both
     forms start from identical fields.  ``tracer_storage``: the mixed form's
-    tracer type (default float64)."""
+    tracer type (default float64); ``ip_arithmetic``: its internal-pressure
+    arithmetic (default float32 slope corrections)."""
     import torch
 
     from getm_gb300.simulation import Simulation
 
     p = wl.params
     sim = Simulation(wl.T, wl.dga, num=p["num"], nuh=p["nuh"], precision=precision, device=device, tiles="auto",
-                     tracer_storage=tracer_storage)
+                     tracer_storage=tracer_storage, internal_pressure_arithmetic=ip_arithmetic)
     zc = sim.T.zc.all_values
     temp0 = torch.where(sim.T.mask.all_values[None] != 0, 4.0 + 16.0 * (zc + 4500.0) / 4500.0,
                         sim.temp.all_values.double())
@@ -490,15 +491,25 @@ def _errors(wl, runners, args, device):
     compensated domain totals.  A third run, FP64 arithmetic whose tracers are
     rounded to float32 after every 3D step, shows the error that float32
     storage of the tracers alone causes (the floor for any form that stores
-    them in float32)."""
+    them in float32).  A fourth, the mixed form with its internal pressure
+    gradient evaluated in FP64, shows how much of the flow's error the float
+    slope corrections cause, and what removing it costs per 3D step."""
     import torch
 
     target = max(args.error_steps, max(r.steps_done for r in runners.values()))
     cond = Runner(_make_sim(wl, "fp64", device), args.warmup, not args.no_graph, hook=_round_tracers)
+    ip64 = Runner(_make_sim(wl, "mixed", device, ip_arithmetic="float64"), args.warmup, not args.no_graph)
     for r in list(runners.values()) + [cond]:
         r.run_to(target)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = ip64.steps_done
+    e0.record()
+    ip64.run_to(target)
+    e1.record()
     torch.cuda.synchronize()
-    steps = {r.steps_done for r in list(runners.values()) + [cond]}
+    ip64_ms = e0.elapsed_time(e1) / max(target - n0, 1)
+    ip64.check()
+    steps = {r.steps_done for r in list(runners.values()) + [cond, ip64]}
     assert len(steps) == 1, steps
     wet = torch.from_numpy(wl.T.mask == 1).to(device)
     uwet = torch.from_numpy(wl.T.ugrid.mask == 1).to(device)
@@ -528,6 +539,7 @@ def _errors(wl, runners, args, device):
                                zip(names, r.sim.totals_device().tolist(), r.totals0.tolist())}
                            for f, r in (("mixed", a), ("fp64", b))}
     out["fp64_with_float32_tracer_storage"] = compare(cond.sim, b.sim)
+    out["mixed_with_fp64_internal_pressure"] = dict(compare(ip64.sim, b.sim), ms_per_step=ip64_ms)
     return out
 
 

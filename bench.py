@@ -33,6 +33,15 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+# CUDA settings read when the process creates its context (before torch
+# touches the GPU): every kernel loaded with the context instead of at its
+# first launch (a first launch on a busy device holds up the other threads'
+# CUDA calls: the serving loop's step issue while a request is set up), and
+# 32 hardware work queues, one per lane stream of the serving and ensemble
+# legs (with the default 8, lanes that share a queue wait on each other).
+os.environ.setdefault("CUDA_MODULE_LOADING", "EAGER")
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 
 def _args():
     ap = argparse.ArgumentParser()
@@ -640,13 +649,13 @@ def _serving_leg(args, device):
 
     rates = [float(x) for x in args.serve_rates.split(",") if x.strip()]
     out = {"arrival_window_s": args.serve_duration, "deadline_s": 3.0 * args.serve_duration,
-           "budget_gb": args.serve_budget_gb, "lanes": 16,
+           "budget_gb": args.serve_budget_gb, "lanes": 32,
            "requests": "sides log-uniform 64-512, nz 20-40, 10-200 3D steps, seed 5", "rates": {}}
     for rate in rates:
         per = {}
         for prec in ("mixed", "fp64"):
             reqs = workloads.serving_requests(rate, args.serve_duration, seed=5, precision=prec)
-            srv = Server(budget_bytes=args.serve_budget_gb * GB, lanes=16, device=device)
+            srv = Server(budget_bytes=args.serve_budget_gb * GB, lanes=32, device=device)
             t0 = time.perf_counter()
             res = srv.run(reqs, duration=3.0 * args.serve_duration, admit_until=args.serve_duration)
             wall = time.perf_counter() - t0

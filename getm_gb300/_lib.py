@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import threading
 from ctypes import c_double, c_int, c_void_p
 from pathlib import Path
 
@@ -40,6 +41,7 @@ _SIGS = {
     "getm_create_grid": "iiiiiiiip",
     "getm_grid_finalize": "p",
     "getm_grid_set_array": "pcp",
+    "getm_grid_float_metrics": "ps",
     "getm_advection_create": "ipp",
     "getm_advection_finalize": "p",
     "getm_advection_uv_calculate": "iipppppdppps",
@@ -135,6 +137,9 @@ _SIGS = {
     "getm_shchepetkin_mcwilliams_mixed": "iiiiiiipppppppppppps",
     "getm_density_buoyancy": "ippppps",
     "getm_launch_count": "p",
+    "getm_graph_launch": "ps",
+    "getm_stream_create": "is",
+    "getm_stream_destroy": "s",
     "getm_advection_apply_3d_batch_f32": "ppppippppppdpppips",
     "getm_advection_apply_3d_batch_f64s": "ppppippppppdpppips",
     "getm_vertical_diffusion_batch_f32": "iiippddppippppps",
@@ -169,6 +174,7 @@ _BLOCKING = frozenset({
     "getm_advection_create", "getm_advection_finalize", "getm_vertical_diffusion_create",
     "getm_vertical_diffusion_finalize", "getm_grid_finalize", "getm_advection_get_status",
     "getm_substep_batch_create", "getm_substep_batch_upload", "getm_substep_batch_finalize",
+    "getm_grid_float_metrics", "getm_stream_create", "getm_stream_destroy",
 })
 
 for _name, _sig in _SIGS.items():
@@ -195,7 +201,29 @@ class GetmError(RuntimeError):
 _pending_release = []
 
 
+# Graph captures in progress on any host thread (capture_started/ended),
+# e.g. a serving admission worker recording a new request while the main
+# loop keeps issuing steps: no handle is finalized meanwhile (freeing device
+# memory waits for the whole device, which an ongoing capture forbids).
+_captures = 0
+_captures_lock = threading.Lock()
+
+
+def capture_started() -> None:
+    global _captures
+    with _captures_lock:
+        _captures += 1
+
+
+def capture_ended() -> None:
+    global _captures
+    with _captures_lock:
+        _captures -= 1
+
+
 def _capturing() -> bool:
+    if _captures:
+        return True
     try:
         import torch
 
@@ -217,14 +245,53 @@ def _flush_releases() -> None:
         getattr(lib, finalizer)(handle)
 
 
+# Threads whose library calls release the interpreter lock whatever the entry
+# point (a serving admission worker): a call there can block (first-use
+# allocation, module loading on a busy device) while another thread must
+# keep issuing steps.
+_tls = threading.local()
+
+
+def release_gil_in_this_thread(flag: bool = True) -> None:
+    """Make every library call of the calling thread release the interpreter
+    lock (``flag``) or use the default per entry point."""
+    _tls.release = flag
+
+
 def call(name: str, *args) -> int:
     """Call an entry point; raise GetmError on a non-zero status."""
     if _pending_release:
         _flush_releases()
-    rc = _CALL[name](*args)
+    f = getattr(lib, name) if getattr(_tls, "release", False) else _CALL[name]
+    rc = f(*args)
     if rc != GETM_OK:
         raise GetmError(name, rc)
     return rc
+
+
+def graph_launch(graph_exec: int, stream: int) -> None:
+    """Launch an instantiated CUDA graph on a stream (getm_graph_launch).  No
+    queued handle is finalized here: this is the call a loop makes while
+    another thread may be capturing."""
+    rc = _CALL["getm_graph_launch"](graph_exec, stream)
+    if rc != GETM_OK:
+        raise GetmError("getm_graph_launch", rc)
+
+
+def own_stream(device, priority: int = 0):
+    """A torch stream (ExternalStream) over a CUDA stream created for the
+    caller alone (getm_stream_create), never one of torch's pooled streams;
+    destroyed when the returned object is collected."""
+    import torch
+
+    with torch.cuda.device(device):
+        h = c_void_p()
+        call("getm_stream_create", int(priority), ctypes.byref(h))
+    s = torch.cuda.ExternalStream(h.value, device=device)
+    import weakref
+
+    weakref.finalize(s, lib.getm_stream_destroy, h.value)
+    return s
 
 
 def ptr(t) -> int | None:

@@ -206,6 +206,12 @@ class Grid:
         for name in ("mask", "dx", "dy", "idx", "idy", "iarea", "area"):
             _lib.call("getm_grid_set_array", h, name.encode(), getattr(self, name).all_values.data_ptr())
 
+    def float_metrics(self):
+        """Make the float copies of the metrics (read by the mixed form's
+        kernels) on the current stream, after the uploads above, waiting for
+        that stream only."""
+        _lib.call("getm_grid_float_metrics", self.handle, torch.cuda.current_stream(self.device).cuda_stream)
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h is not None and h.value:

@@ -66,14 +66,12 @@ __global__ void to_float_kernel(long long n, const double* src, float* dst)
     if (p < n) dst[p] = (float)src[p];
 }
 
-int getm_grid_f32_metrics(getm_grid* g, cudaStream_t stream)
+// The float copies of a grid's metrics, converted on `stream` after every
+// earlier write of the metrics on that stream, and complete on return (the
+// wait is for `stream` only).
+static int grid_float_metrics_on(getm_grid* g, cudaStream_t stream)
 {
-    if (!g) return GETM_ERR_ARG;
-    if (g->iarea_f) return GETM_OK;  // built last: its presence means all are there
     const long long n = (long long)g->nx_ * g->ny_;
-    // one-time setup: order it after every earlier write of the metrics on
-    // any stream, and complete it before returning
-    if (cudaDeviceSynchronize() != cudaSuccess) return GETM_ERR_CUDA;
     const double* src[5] = {g->dx, g->dy, g->idx, g->idy, g->iarea};
     float** dst[5] = {&g->dx_f, &g->dy_f, &g->idx_f, &g->idy_f, &g->iarea_f};
     for (int q = 0; q < 5; q++) {
@@ -89,6 +87,24 @@ int getm_grid_f32_metrics(getm_grid* g, cudaStream_t stream)
     }
     if (cudaStreamSynchronize(stream) != cudaSuccess) return GETM_ERR_CUDA;
     return GETM_OK;
+}
+
+// First use by a float kernel of a grid whose copies were not made with
+// getm_grid_float_metrics: the metrics may have been written on any stream,
+// so the conversion is ordered after all work on the device.
+int getm_grid_f32_metrics(getm_grid* g, cudaStream_t stream)
+{
+    if (!g) return GETM_ERR_ARG;
+    if (g->iarea_f) return GETM_OK;  // built last: its presence means all are there
+    if (cudaDeviceSynchronize() != cudaSuccess) return GETM_ERR_CUDA;
+    return grid_float_metrics_on(g, stream);
+}
+
+extern "C" int getm_grid_float_metrics(getm_grid* g, cudaStream_t stream)
+{
+    if (!g) return GETM_ERR_ARG;
+    if (g->iarea_f) return GETM_OK;
+    return grid_float_metrics_on(g, stream);
 }
 
 extern "C" int getm_grid_set_array(getm_grid* g, const char* name, void* p)
@@ -121,9 +137,10 @@ struct getm_advection {
 
 static void adv_free_buffers(getm_advection* a)
 {
-    for (int i = 0; i < 2; i++) { cudaFree(a->hbuf[i]); a->hbuf[i] = NULL; }
-    for (int i = 0; i < 2; i++) { cudaFree(a->colbuf[i]); a->colbuf[i] = NULL; }
-    for (int i = 0; i < a->ntmp; i++) { cudaFree(a->tmp[i]); a->tmp[i] = NULL; }
+    // (cudaFree waits for the whole device: never called without a buffer)
+    for (int i = 0; i < 2; i++) if (a->hbuf[i]) { cudaFree(a->hbuf[i]); a->hbuf[i] = NULL; }
+    for (int i = 0; i < 2; i++) if (a->colbuf[i]) { cudaFree(a->colbuf[i]); a->colbuf[i] = NULL; }
+    for (int i = 0; i < a->ntmp; i++) if (a->tmp[i]) { cudaFree(a->tmp[i]); a->tmp[i] = NULL; }
     a->ntmp = 0;
     a->n3 = 0;
 }

@@ -22,6 +22,24 @@ extern "C" int getm_launch_count(unsigned long long* count)
     return GETM_OK;
 }
 
+extern "C" int getm_stream_create(int priority, cudaStream_t* stream)
+{
+    if (!stream) return GETM_ERR_ARG;
+    return cudaStreamCreateWithPriority(stream, cudaStreamNonBlocking, priority) == cudaSuccess ? GETM_OK
+                                                                                              : GETM_ERR_CUDA;
+}
+
+extern "C" int getm_stream_destroy(cudaStream_t stream)
+{
+    return cudaStreamDestroy(stream) == cudaSuccess ? GETM_OK : GETM_ERR_CUDA;
+}
+
+extern "C" int getm_graph_launch(void* graph_exec, cudaStream_t stream)
+{
+    if (!graph_exec) return GETM_ERR_ARG;
+    return cudaGraphLaunch((cudaGraphExec_t)graph_exec, stream) == cudaSuccess ? GETM_OK : GETM_ERR_CUDA;
+}
+
 // Launch-shape knobs, per host thread (a thread that captures a domain's
 // graphs sets its own shapes without disturbing another thread's launches).
 static thread_local int g_tune[GETM_TUNE_NKNOBS] = {8, 32, 4, 0, 1, 0};

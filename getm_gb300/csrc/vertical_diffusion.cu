@@ -840,7 +840,8 @@ extern "C" int getm_vertical_diffusion_prepare(getm_vertical_diffusion* d, int n
     const long long plane = (long long)nx * ny;
     const size_t n3 = (size_t)plane * nz;
     if (n3 > d->n3) {
-        cudaFree(d->auxo); cudaFree(d->auxn);
+        if (d->auxo) cudaFree(d->auxo);  // (cudaFree waits for the whole device)
+        if (d->auxn) cudaFree(d->auxn);
         d->auxo = d->auxn = NULL;
         if (cudaMalloc(&d->auxo, n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;
         if (cudaMalloc(&d->auxn, n3 * sizeof(double)) != cudaSuccess) return GETM_ERR_ALLOC;

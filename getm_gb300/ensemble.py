@@ -18,6 +18,7 @@ from typing import List, Optional
 
 import torch
 
+from . import _lib
 from .simulation import Fluxes, Simulation
 from .workloads import Workload
 
@@ -42,12 +43,19 @@ def make_member(wl: Workload, precision: str = "mixed", device="cuda", substep_k
     return sim
 
 
+# PyTorch exposes the instantiated graph (cudaGraphExec_t): replays then go
+# through the library's getm_graph_launch, which another host thread may
+# call while one captures (torch's CUDAGraph.replay refuses that)
+RAW_LAUNCH = hasattr(torch.cuda.CUDAGraph, "raw_cuda_graph_exec")
+
+
 class DomainRunner:
     """Warm-up, per-step CUDA graphs and replay of one resident domain."""
 
     def __init__(self, sim: Simulation, warmup_steps: int = 2, use_graph: bool = True):
         self.sim = sim
         self.graphs: Optional[List[torch.cuda.CUDAGraph]] = None
+        self._execs: Optional[List[int]] = None  # the graphs' cudaGraphExec_t (RAW_LAUNCH)
         self.steps_done = 0  # 3D steps completed on the device (as issued)
         self._use_graph = use_graph
         self._warmup = warmup_steps + warmup_steps % 2
@@ -86,19 +94,37 @@ class DomainRunner:
                 # which synchronizes the whole device, collects garbage and
                 # empties the allocator's cache first: with other domains'
                 # steps queued (serving) that waits for all of them
-                g.capture_begin(capture_error_mode=capture_error_mode)
+                _lib.capture_started()
                 try:
-                    self._eager_step()
+                    g.capture_begin(capture_error_mode=capture_error_mode)
+                    try:
+                        self._eager_step()
+                    finally:
+                        g.capture_end()
                 finally:
-                    g.capture_end()
+                    _lib.capture_ended()
             graphs.append(g)
         torch.cuda.current_stream(dev).wait_stream(stream)
         self.graphs = graphs
+        if RAW_LAUNCH:
+            self._execs = [int(g.raw_cuda_graph_exec()) for g in graphs]
 
     def step(self):
         """Issue one 3D step on the current stream."""
         if self.graphs is None:
             self._eager_step()
+        elif self._execs is not None:
+            dev = self.sim.T.device
+            try:
+                _lib.graph_launch(self._execs[(self.steps_done - self._warmup) % 2],
+                                  torch.cuda.current_stream(dev).cuda_stream)
+            except _lib.GetmError as e:
+                # name the device's error, if it holds one
+                try:
+                    torch.cuda.current_stream(dev).synchronize()
+                except RuntimeError as d:
+                    raise RuntimeError(f"{e}; the stream reports: {d}") from e
+                raise
         else:
             self.graphs[(self.steps_done - self._warmup) % 2].replay()
         self.steps_done += 1

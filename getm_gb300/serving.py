@@ -16,7 +16,13 @@ Admission runs on a worker thread with its own stream: building a domain,
 its eager warm-up steps and the capture of its step graphs (in thread-local
 capture mode) overlap with the main loop, which only decides admissions,
 issues graph replays and polls completions, so issuing the steps of running
-requests never waits for a request being set up.
+requests never waits for a request being set up.  Replays go through the
+library's getm_graph_launch on lane streams the server creates for itself
+(never torch's pooled streams, one of which a capture may have drawn in),
+and the worker's library calls release the interpreter lock.  Kernels should
+be loaded when the CUDA context is created (CUDA_MODULE_LOADING=EAGER set
+before CUDA starts): loading one at its first launch on a busy device holds
+up every thread's CUDA calls.
 
 Every step's completion is timed on the device (a CUDA event per step,
 measured against a start event), which gives the per-step latency: the time
@@ -33,7 +39,8 @@ from typing import Callable, Dict, List, Optional
 import numpy as np
 import torch
 
-from .ensemble import DomainRunner, make_member
+from . import _lib
+from .ensemble import RAW_LAUNCH, DomainRunner, make_member
 from .workloads import Workload
 
 GB = 1e9
@@ -85,14 +92,17 @@ class Server:
 
     STATE_FIELDS = ("temp", "salt")
 
-    def __init__(self, budget_bytes: float = 150 * GB, lanes: int = 16, max_inflight: int = 2,
+    def __init__(self, budget_bytes: float = 150 * GB, lanes: int = 32, max_inflight: int = 2,
                  device="cuda", keep=(), admission_thread: bool = True, max_building: int = 2):
         """``admission_thread``: set requests up on a worker thread (False:
         in the main loop, between step issues); ``max_building``: requests
         handed to the worker and not yet ready."""
         self.device = torch.device(device)
         self.budget = float(budget_bytes)
-        self.lanes = [torch.cuda.Stream(device=self.device) for _ in range(lanes)]
+        # lanes of the caller's own (torch's pooled streams can coincide with
+        # a stream that a set-up capture draws in, and a launch into a
+        # capturing stream fails)
+        self.lanes = [_lib.own_stream(self.device) for _ in range(lanes)]
         self.max_inflight = max_inflight
         self.keep = set(keep)
         self.bytes_per_cell: Dict[str, float] = {}
@@ -101,13 +111,16 @@ class Server:
         self.peak_used = 0.0
         # set-up work (eager warm-up steps) on high-priority streams: its
         # kernels go ahead of the queued step replays of running requests
-        self._capture_stream = torch.cuda.Stream(device=self.device, priority=-1)
-        self._build_stream = torch.cuda.Stream(device=self.device, priority=-1)
-        self._lane_next = 0
+        self._capture_stream = _lib.own_stream(self.device, priority=-1)
+        self._build_stream = _lib.own_stream(self.device, priority=-1)
+        self._lane_cells = [0] * lanes
+        self._lane_mutex = threading.Lock()
         # held by the admission worker while it captures a graph and by the
-        # main loop while it issues replays (torch refuses a replay while any
-        # graph is being captured)
+        # main loop while it issues replays, where those go through torch's
+        # CUDAGraph.replay (which refuses a replay while any graph is being
+        # captured); replays through getm_graph_launch need no lock
         self._capture_lock = threading.Lock()
+        self._lock_replays = not RAW_LAUNCH
         self.admission_thread = admission_thread
         self.max_building = max(1, max_building)
         self.admission_host_s: List[float] = []
@@ -148,15 +161,22 @@ class Server:
         cells = wl.T.nx_ * wl.T.ny_ * (wl.T.nz + 1)
         bpc = grown / cells
         self.bytes_per_cell[req.precision] = max(self.bytes_per_cell.get(req.precision, 0.0), bpc)
-        lane = self.lanes[self._lane_next % len(self.lanes)]
-        self._lane_next += 1
-        a = _Active(req, runner, max(self.estimate(req), 1.05 * grown), lane)
+        # the lane with the fewest cells of running requests (a lane runs its
+        # requests' steps one after another)
+        with self._lane_mutex:
+            li = min(range(len(self.lanes)), key=lambda k: self._lane_cells[k])
+            self._lane_cells[li] += runner.cells
+        a = _Active(req, runner, max(self.estimate(req), 1.05 * grown), self.lanes[li])
+        a.lane_index = li
         a.result = res
         return a
 
     def _worker(self, inbox: "queue.Queue", ready: "queue.Queue", start: torch.cuda.Event, t0: float):
         """Admission worker: build, warm up and capture each handed request
-        on the worker's own stream; hand the result (or the exception) back."""
+        on the worker's own stream; hand the result (or the exception) back.
+        Its library calls release the interpreter lock (one that blocks must
+        not stop the main loop's step issue)."""
+        _lib.release_gil_in_this_thread()
         while True:
             item = inbox.get()
             if item is None:
@@ -213,6 +233,7 @@ class Server:
         start.record()
         t0 = time.perf_counter()
         self.admission_host_s = []
+        self._lane_cells = [0] * len(self.lanes)
         inbox: "queue.Queue" = queue.Queue()
         ready: "queue.Queue" = queue.Queue()
         reserved: Dict[int, float] = {}
@@ -272,7 +293,7 @@ class Server:
                 # completion of issued steps, then issue the next ones (not
                 # while the worker captures a graph: this pass skips them)
                 progressed = False
-                may_issue = self._capture_lock.acquire(blocking=False)
+                may_issue = self._capture_lock.acquire(blocking=False) if self._lock_replays else True
                 try:
                     for a in active:
                         while a.inflight and a.inflight[0].query():
@@ -289,7 +310,7 @@ class Server:
                             issued += 1
                             progressed = True
                 finally:
-                    if may_issue:
+                    if may_issue and self._lock_replays:
                         self._capture_lock.release()
                 # retire finished requests
                 keep_active = []
@@ -305,6 +326,8 @@ class Server:
                         # work on the device, every other request's queued
                         # steps included
                         retired.append(a)
+                        with self._lane_mutex:
+                            self._lane_cells[a.lane_index] -= a.runner.cells
                     else:
                         keep_active.append(a)
                 active = keep_active

@@ -176,6 +176,12 @@ class Simulation:
         self.dga = torch.as_tensor(dga, dtype=torch.float64, device=device)[:, None, None]
         self.T = T = make_grids(T_host, device)
         self.U, self.V, self.X = T.ugrid, T.vgrid, T.xgrid
+        if precision == "mixed":
+            # float metric copies now, ordered after the uploads on this
+            # stream (a first use from a kernel would wait for the whole
+            # device, every other domain's queued work included)
+            for g in T.all_grids():
+                g.float_metrics()
         if tiles == "auto":
             from . import autotune
 

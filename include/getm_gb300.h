@@ -66,6 +66,13 @@ int getm_create_grid(int imin, int imax, int jmin, int jmax, int kmin, int kmax,
                      int haloy, getm_grid** grid);
 int getm_grid_finalize(getm_grid* grid);
 int getm_grid_set_array(getm_grid* grid, const char* name, void* device_ptr);
+/* No counterpart in the reference (it has no float arithmetic).  The float
+ * copies of a grid's registered metrics, which the mixed form's kernels read,
+ * converted on `stream` after the metrics' earlier writes on that stream;
+ * returns when `stream` has finished them and waits for no other stream.
+ * Without this call the first float kernel on the grid makes them, and that
+ * first use waits for the whole device.                                       */
+int getm_grid_float_metrics(getm_grid* grid, cudaStream_t stream);
 
 /* ---- advection ----------------------------------------------------------
  * advection_create/finalize: wrapper.F90:188-211 (pyx:35-36)
@@ -305,6 +312,22 @@ int getm_shchepetkin_mcwilliams(int nx, int ny, int nz, int imin, int imax, int 
  * has issued in the process so far (launches captured into a CUDA graph are
  * counted once, at capture).                                                */
 int getm_launch_count(unsigned long long* count);
+
+/* No counterpart in the reference.  Launch an instantiated CUDA graph
+ * (cudaGraphExec_t, e.g. a domain's recorded 3D step) on `stream`.  Unlike
+ * PyTorch's CUDAGraph.replay, this may be called by one host thread while
+ * another captures a graph in thread-local mode (serving: steps of running
+ * requests keep being issued while a new request is recorded).            */
+int getm_graph_launch(void* graph_exec, cudaStream_t stream);
+
+/* No counterpart in the reference.  A stream of the calling thread's current
+ * device that belongs to the caller alone (non-blocking; priority as in
+ * cudaStreamCreateWithPriority).  PyTorch's torch.cuda.Stream() hands out
+ * streams from a small shared pool, so two of them can be the same CUDA
+ * stream: a stream that one thread issues graph launches on must not be one
+ * that another thread's capture has drawn in.                               */
+int getm_stream_create(int priority, cudaStream_t* stream);
+int getm_stream_destroy(cudaStream_t stream);
 
 /* ---- launch-shape knobs (the autotuner's search space) -----------------
  * No counterpart in the reference.  Launch shapes of the hot kernels, read

@@ -80,6 +80,12 @@ class _Active:
         self.inflight: List[torch.cuda.Event] = []
 
 
+def least_loaded(loads: List[int]) -> int:
+    """Index of the lane with the fewest cells of running requests (the
+    first such lane on a tie)."""
+    return min(range(len(loads)), key=lambda k: loads[k])
+
+
 class Server:
     """Continuous-batching server for one GPU.
 
@@ -164,7 +170,7 @@ class Server:
         # the lane with the fewest cells of running requests (a lane runs its
         # requests' steps one after another)
         with self._lane_mutex:
-            li = min(range(len(self.lanes)), key=lambda k: self._lane_cells[k])
+            li = least_loaded(self._lane_cells)
             self._lane_cells[li] += runner.cells
         a = _Active(req, runner, max(self.estimate(req), 1.05 * grown), self.lanes[li])
         a.lane_index = li

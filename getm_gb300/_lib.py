@@ -138,6 +138,7 @@ _SIGS = {
     "getm_density_buoyancy": "ippppps",
     "getm_launch_count": "p",
     "getm_graph_launch": "ps",
+    "getm_advance_time": "pds",
     "getm_stream_create": "is",
     "getm_stream_destroy": "s",
     "getm_advection_apply_3d_batch_f32": "ppppippppppdpppips",

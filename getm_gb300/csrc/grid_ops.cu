@@ -22,6 +22,16 @@ extern "C" int getm_launch_count(unsigned long long* count)
     return GETM_OK;
 }
 
+__global__ void advance_time_kernel(double* time, double dt) { *time = *time + dt; }
+
+extern "C" int getm_advance_time(double* time, double timestep, cudaStream_t stream)
+{
+    if (!time) return GETM_ERR_ARG;
+    advance_time_kernel<<<1, 1, 0, stream>>>(time, timestep);
+    GETM_CHECK_LAUNCH();
+    return GETM_OK;
+}
+
 extern "C" int getm_stream_create(int priority, cudaStream_t* stream)
 {
     if (!stream) return GETM_ERR_ARG;

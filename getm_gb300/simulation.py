@@ -58,7 +58,7 @@ class TracerTransport:
 # ---------------------------------------------------------------------------
 import enum  # noqa: E402
 
-from . import _pygetm  # noqa: E402
+from . import _lib, _pygetm  # noqa: E402
 from .domain import FILL_VALUE, GRAVITY, RHO0  # noqa: E402
 from .momentum import CoriolisScheme, Momentum  # noqa: E402
 from .operators import AdvectionSplit  # noqa: E402
@@ -293,7 +293,8 @@ class Simulation:
         if self._split2d is not None and not macro_active:
             self._split2d_substep()
             return
-        self._time.add_(self.timestep)
+        _lib.call("getm_advance_time", self._time.data_ptr(), float(self.timestep),
+                  torch.cuda.current_stream(self._time.device).cuda_stream)
         self._advance_state(macro_active)
         self._update_forcing_and_diagnostics(macro_active)
 

@@ -320,6 +320,12 @@ int getm_launch_count(unsigned long long* count);
  * requests keep being issued while a new request is recorded).            */
 int getm_graph_launch(void* graph_exec, cudaStream_t stream);
 
+/* The model time of a substep that is not the one-launch substep (which
+ * advances it itself): *time += timestep on the device, so that a captured
+ * step graph advances it too.  pygetm keeps its time on the host
+ * (python/pygetm/simulation.py:291-325, self.time += self.timestep).      */
+int getm_advance_time(double* time, double timestep, cudaStream_t stream);
+
 /* No counterpart in the reference.  A stream of the calling thread's current
  * device that belongs to the caller alone (non-blocking; priority as in
  * cudaStreamCreateWithPriority).  PyTorch's torch.cuda.Stream() hands out

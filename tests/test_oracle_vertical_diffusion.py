@@ -136,3 +136,52 @@ def test_single_layer_shortcut():
     v(nuh, DT, var, ea2=ea2, ea4=ea4, use_ho=True)
     assert np.array_equal(var, expected)
     del T
+
+
+@pytest.mark.parametrize("cnpar", [0.5, 1.0])
+def test_gaussian_against_the_analytic_solution(cnpar):
+    """tests/test_vertical_diffusion.F90:14-75, 145-160 (initial_conditions
+    method 1): a Gaussian of amplitude 5 and width 5 m in a 100 m column of
+    100 one-metre layers, constant diffusivity 0.1 m2/s, 200 steps of 5 s.
+    The analytic solution stays Gaussian, amplitude 5 sqrt(a^2/C),
+    C = 4 Av t + a^2.  The discretisation error is 7e-4 of the amplitude
+    (both weights); the column total is conserved to rounding."""
+    wet, var, ana, total0, total = gaussian_column(O.VerticalDiffusion, cnpar)
+    assert np.abs(var[:, wet] - ana[:, None]).max() / GAUSS["cmax"] < 1.5e-3
+    assert np.abs(total - total0).max() / total0.max() < 1e-13
+
+
+GAUSS = dict(nz=100, depth=100.0, Av=0.1, cmax=5.0, a=5.0, dt=5.0, nstep=200)
+
+
+def gaussian_column(make_diffusion, cnpar, to_device=None, from_device=None, nx=6, ny=5):
+    """The column of tests/test_vertical_diffusion.F90 on an nx x ny patch of
+    identical columns, diffused by ``make_diffusion(grid, cnpar)`` (the
+    oracle's, or a device one with ``to_device``/``from_device`` moving the
+    grid and fields); returns (wet mask, final field, analytic profile,
+    column totals before and after)."""
+    g = GAUSS
+    nz, depth = g["nz"], g["depth"]
+    Th, dga, hn = column_grid(nx=nx, ny=ny, nz=nz, H=depth, land=0.0)
+    dz = depth / nz
+    z = -depth + dz * np.arange(nz)  # level positions of the F90 program (z(1) = -depth)
+    z0 = z[nz // 2 - 1]
+    var = np.broadcast_to((g["cmax"] * np.exp(-(z - z0) ** 2 / g["a"] ** 2))[:, None, None], hn.shape).copy()
+    nuh = np.full((nz + 1,) + hn.shape[1:], g["Av"])
+    if to_device is None:
+        T = O.make_grids(Th)
+        T.hn[...] = hn
+        T.ho[...] = hn
+        wet = T.mask == 1
+        total0 = (var * hn)[:, wet].sum(axis=0)
+        vd = make_diffusion(T, cnpar)
+        for _ in range(g["nstep"]):
+            vd(nuh, g["dt"], var)
+    else:
+        wet = Th.mask == 1
+        total0 = (var * hn)[:, wet].sum(axis=0)
+        var = from_device(to_device(make_diffusion, Th, hn, nuh, var, cnpar, g["dt"], g["nstep"]))
+    C1 = 4.0 * g["Av"] * g["nstep"] * g["dt"] + g["a"] ** 2
+    ana = g["cmax"] * np.sqrt(g["a"] ** 2 / C1) * np.exp(-(z - z0) ** 2 / C1)
+    total = (var * hn)[:, wet].sum(axis=0)
+    return wet, var, ana, total0, total

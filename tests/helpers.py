@@ -50,3 +50,64 @@ def full_grid(nx=40, ny=30, nz=10, seed=0, land=0.15, dx=1000.0, Hmin=10.0, Hmax
     dom = create_cartesian(x, y, mask=mask, H=H, f=f)
     T = dom.create_grids(nz, halox=2, haloy=2, velocity_grids=velocity_grids)
     return T, rng
+
+
+def rotated_pair(nx=24, ny=18, nz=6, seed=3, dx=2000.0):
+    """A closed domain with smoothed random bathymetry (20-100 m) and a land
+    mask (15 %), and the same domain rotated by 90 degrees (arrays A.T[::-1]),
+    as in python/tests/test_rotation.py (Domain.rotate): host grid trees
+    (original, rotated) and the sigma fractions."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+
+    def n01(a):
+        return (a - a.min()) / (a.max() - a.min())
+
+    H = 20.0 + 80.0 * n01(gaussian_filter(rng.standard_normal((ny, nx)), 3))
+    q = gaussian_filter(rng.standard_normal((ny, nx)), 3)
+    mask = (q > np.quantile(q, 0.15)).astype(int)
+    z0 = 0.5 * 50.0 / (np.exp(0.4 / np.sqrt(2.5e-3)) - 1.0)
+
+    def make(H, mask):
+        ny_, nx_ = H.shape
+        dom = create_cartesian(dx * (np.arange(nx_) + 0.5), dx * (np.arange(ny_) + 0.5), mask=mask, H=H, f=1e-4,
+                               z0=z0)
+        return dom.create_grids(nz, halox=2, haloy=2, velocity_grids=2)
+
+    return make(H, mask), make(rot2(H), rot2(mask)), calculate_sigma(nz)
+
+
+def rot2(a):
+    """A 2D array of T points (or of V points, see rotation_errors) rotated
+    with its domain."""
+    return a.T[::-1, :]
+
+
+def rot3(a):
+    return a.transpose(0, 2, 1)[:, ::-1, :]
+
+
+def rotation_errors(orig, rot, masks):
+    """Relative errors of the rotated run against the original run rotated:
+    ``orig``/``rot`` map z, temp, U, V, uk, vk to arrays (numpy) of each run,
+    ``masks`` the rotated domain's T, U and V masks.  Under the rotation
+    x_rot = y and y_rot = -x, so U_rot = V rotated, and V_rot at row p is -U
+    at the original column NX-2-p (the last row has no counterpart)."""
+    mT, mU, mV = (m == 1 for m in masks)
+    mV = mV.copy()
+    mV[-1, :] = False
+
+    def rel(a, b, m):
+        a, b = a[..., m], b[..., m]
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+    def shifted(a):  # -U rotated and shifted by one row (V_rot points)
+        out = np.zeros(a.shape[:-2] + a.shape[-1:] + a.shape[-2:-1])
+        r = rot2(a) if a.ndim == 2 else rot3(a)
+        out[..., :-1, :] = -r[..., 1:, :]
+        return out
+
+    return {"z": rel(rot["z"], rot2(orig["z"]), mT), "temp": rel(rot["temp"], rot3(orig["temp"]), mT),
+            "U": rel(rot["U"], rot2(orig["V"]), mU), "uk": rel(rot["uk"], rot3(orig["vk"]), mU),
+            "V": rel(rot["V"], shifted(orig["U"]), mV), "vk": rel(rot["vk"], shifted(orig["uk"]), mV)}

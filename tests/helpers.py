@@ -52,11 +52,9 @@ def full_grid(nx=40, ny=30, nz=10, seed=0, land=0.15, dx=1000.0, Hmin=10.0, Hmax
     return T, rng
 
 
-def rotated_pair(nx=24, ny=18, nz=6, seed=3, dx=2000.0):
-    """A closed domain with smoothed random bathymetry (20-100 m) and a land
-    mask (15 %), and the same domain rotated by 90 degrees (arrays A.T[::-1]),
-    as in python/tests/test_rotation.py (Domain.rotate): host grid trees
-    (original, rotated) and the sigma fractions."""
+def _random_closed_domain(nx, ny, nz, seed, dx):
+    """Smoothed random bathymetry (20-100 m) and a land mask (15 %) of a
+    closed domain, and a builder of its host grid tree."""
     from scipy.ndimage import gaussian_filter
 
     rng = np.random.default_rng(seed)
@@ -69,13 +67,56 @@ def rotated_pair(nx=24, ny=18, nz=6, seed=3, dx=2000.0):
     mask = (q > np.quantile(q, 0.15)).astype(int)
     z0 = 0.5 * 50.0 / (np.exp(0.4 / np.sqrt(2.5e-3)) - 1.0)
 
-    def make(H, mask):
+    def make(H, mask, f=1e-4):
         ny_, nx_ = H.shape
-        dom = create_cartesian(dx * (np.arange(nx_) + 0.5), dx * (np.arange(ny_) + 0.5), mask=mask, H=H, f=1e-4,
+        dom = create_cartesian(dx * (np.arange(nx_) + 0.5), dx * (np.arange(ny_) + 0.5), mask=mask, H=H, f=f,
                                z0=z0)
         return dom.create_grids(nz, halox=2, haloy=2, velocity_grids=2)
 
+    return H, mask, make
+
+
+def rotated_pair(nx=24, ny=18, nz=6, seed=3, dx=2000.0):
+    """A closed domain with smoothed random bathymetry and land, and the same
+    domain rotated by 90 degrees (arrays A.T[::-1]), as in
+    python/tests/test_rotation.py (Domain.rotate): host grid trees (original,
+    rotated) and the sigma fractions."""
+    H, mask, make = _random_closed_domain(nx, ny, nz, seed, dx)
     return make(H, mask), make(rot2(H), rot2(mask)), calculate_sigma(nz)
+
+
+def mirrored_pair(nx=24, ny=18, nz=6, seed=3, dx=2000.0, f=1e-4):
+    """The same closed domain and its mirror image in y (arrays A[::-1]); the
+    mirror image of a flow on an f-plane is a flow on the f-plane of -f, so
+    the mirrored domain gets -f."""
+    H, mask, make = _random_closed_domain(nx, ny, nz, seed, dx)
+    return make(H, mask, f), make(H[::-1], mask[::-1], -f), calculate_sigma(nz)
+
+
+def mirror_errors(orig, mir, masks):
+    """Relative errors of the mirrored run against the original run mirrored
+    in y: T and U points map row to row (A[..., ::-1, :]); V points (between
+    rows) at row p come from -V at row NY-2-p (the last row has no
+    counterpart)."""
+    mT, mU, mV = (m == 1 for m in masks)
+    mV = mV.copy()
+    mV[-1, :] = False
+
+    def rel(a, b, m):
+        a, b = a[..., m], b[..., m]
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+    def flip(a):
+        return a[..., ::-1, :]
+
+    def shifted(a):
+        out = np.zeros_like(a)
+        out[..., :-1, :] = -flip(a)[..., 1:, :]
+        return out
+
+    return {"z": rel(mir["z"], flip(orig["z"]), mT), "temp": rel(mir["temp"], flip(orig["temp"]), mT),
+            "U": rel(mir["U"], flip(orig["U"]), mU), "uk": rel(mir["uk"], flip(orig["uk"]), mU),
+            "V": rel(mir["V"], shifted(orig["V"]), mV), "vk": rel(mir["vk"], shifted(orig["vk"]), mV)}
 
 
 def rot2(a):

@@ -920,7 +920,7 @@ def run_ours(args):
             "split2d_status": {f: runners[f].sim.split2d_status() for f in forms}}
     if substep is not None:
         line["substep_kernel"] = substep
-    if primary == "mixed" and args.column_solve:
+    if primary == "mixed" and args.column_solve and rank == 0:
         line["column_solve"] = _column_solve_leg(runners[primary].sim, device)
     for f in forms:
         if f != primary:
